@@ -1,0 +1,218 @@
+/*
+ * rtr.h — C ABI of the GB300 (sm_103a) model-to-scene registration hot path.
+ *
+ * This is the drop-in boundary for the registration chain of ICCD/RealTime_Robot
+ * (RealTimeRobot/RealTimeRobot.cpp:27-121 driving key_point.h, matching.h,
+ * model_point.h, scan_point.h and function.h).  The reference reaches the GPU
+ * through exactly one C entry point, ComputeTDFWithCuda (kernel.cu:34-106,
+ * declared at key_point.h:35-36); it is kept below with its exact signature.
+ * Everything else the reference does through PCL on the CPU is offered here as
+ * rtr_* entry points that the C++ entry points (ModelPoint, ScanPoint,
+ * KeyPoint, get_Distance, Ransac, keyPointICP, match_by_*) call.
+ *
+ * Conventions (all rtr_* calls):
+ *   - Plain pointers and sizes only.  "d_" pointers are device pointers, "h_"
+ *     pointers are host pointers.  The caller owns every input and output
+ *     buffer; the context owns scratch memory.
+ *   - Point clouds are arrays of 16-byte points {x, y, z, pad} (float), the
+ *     memory layout of pcl::PointXYZ.  The pad lane is ignored on input.
+ *   - Poses are row-major 4x4 doubles mapping source coordinates into target
+ *     coordinates: q = R p + t.
+ *   - Work is enqueued on the given stream (0 = legacy default stream) and the
+ *     call returns without synchronising unless its comment says otherwise.
+ *   - Every call returns an rtr_status; no C++ exception crosses the ABI.  The
+ *     text of the last failure is available from rtr_last_error().
+ *   - A context is used by one host thread at a time.
+ */
+#ifndef RTR_H_
+#define RTR_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__CUDA_RUNTIME_H__) || defined(__CUDACC__)
+typedef cudaStream_t rtr_stream_t;
+#else
+typedef struct CUstream_st* rtr_stream_t;
+#endif
+
+typedef enum rtr_status {
+  RTR_OK = 0,
+  RTR_ERR_INVALID_ARG = 1,  /* bad pointer, size or parameter                 */
+  RTR_ERR_OOM = 2,          /* device allocation failed                       */
+  RTR_ERR_TIMEOUT = 3,      /* a bounded device-side wait ran out             */
+  RTR_ERR_NOT_FOUND = 4,    /* no model instance / correspondence was found   */
+  RTR_ERR_CUDA = 5,         /* a CUDA runtime call failed                     */
+  RTR_ERR_CAPACITY = 6,     /* scratch too small while a stream is captured   */
+  RTR_ERR_NO_DEVICE = 7     /* no usable sm_103a device                       */
+} rtr_status;
+
+typedef struct rtr_context rtr_context;
+
+/* ---- library / context ------------------------------------------------- */
+
+const char* rtr_status_string(int status);
+/* Text of the last failure recorded on this host thread ("" if none). */
+const char* rtr_last_error(void);
+/* Library version, e.g. "0.1.0". */
+const char* rtr_version(void);
+
+/* Create a context on `device`: owns a scratch arena, a device status word
+ * and the tensor-map cache.  Fails with RTR_ERR_NO_DEVICE when the device is
+ * not compute capability 10.3. */
+rtr_status rtr_context_create(int device, rtr_context** out);
+rtr_status rtr_context_destroy(rtr_context* ctx);
+/* Grow the scratch arena to at least `bytes` (synchronises the device).  Call
+ * before capturing a stream into a CUDA graph. */
+rtr_status rtr_context_reserve(rtr_context* ctx, size_t bytes);
+/* Bytes of scratch currently held. */
+size_t rtr_context_scratch_bytes(const rtr_context* ctx);
+/* Budget of every bounded device-side spin wait, in milliseconds (default 2000). */
+rtr_status rtr_context_set_wait_budget_ms(rtr_context* ctx, double ms);
+/* Synchronise `stream` and read (then clear) the device status word written by
+ * persistent kernels (RTR_OK or RTR_ERR_TIMEOUT). */
+rtr_status rtr_context_check(rtr_context* ctx, rtr_stream_t stream);
+
+/* Stage profiling: when enabled, every rtr_* call records a CUDA event pair
+ * around each of its stages ("grid_build", "icp_kernel", ...) on its stream.
+ * After synchronising, rtr_context_profile_count/get read the recorded stages
+ * in order (milliseconds) and rtr_context_profile_clear forgets them.  Keep
+ * it off while capturing a graph. */
+rtr_status rtr_context_set_profiling(rtr_context* ctx, int enabled);
+int rtr_context_profile_count(rtr_context* ctx);
+rtr_status rtr_context_profile_get(rtr_context* ctx, int i, const char** name, float* ms);
+void rtr_context_profile_clear(rtr_context* ctx);
+/* Kernels launched by this library in this process so far (all contexts). */
+uint64_t rtr_launch_count(void);
+
+/* ---- the reference's own GPU entry point (kept) --------------------------
+ * Replaces kernel.cu:34-106 (declared at key_point.h:35-36).  Same signature,
+ * same meaning: voxel_grid_occ is a HOST array of num_occ integer (x,y,z)
+ * triples; voxel_grid_TDF is a HOST array of 27,000 floats.  For every voxel v
+ * of the dim^3 grid (x fastest, then y, then z) it stores
+ * min(900, min_i |v - occ_i|^2).  Synchronous; uses device 0.
+ * Differences from kernel.cu, all on inputs where the reference misbehaves:
+ *   - dim^3 > 27,000 or num_occ < 0 returns cudaErrorInvalidValue (the
+ *     reference writes outside its 27,000-float device buffer);
+ *   - at dim = 30 the reference's guard (kernel.cu:13) lets one thread write
+ *     one float past the buffer; that write is not reproduced.  For dim < 30
+ *     the same extra element (index dim^3, the voxel (0,0,dim)) lands inside
+ *     the 27,000-float buffer and IS reproduced, so outputs match bit for bit.
+ * Return type is cudaError_t in the reference; declared as int here so this
+ * header does not need cuda_runtime.h (the values are cudaError_t codes). */
+int ComputeTDFWithCuda(const int* voxel_grid_occ, float* voxel_grid_TDF,
+                       int voxel_grid_dim, int num_occ);
+
+/* Batched form of the above for many keypoints at once, device resident:
+ * occupied voxels of keypoint k are d_occ[3*d_offsets[k] .. 3*d_offsets[k+1]),
+ * output d_tdf[k*dim^3 .. (k+1)*dim^3).  d_offsets has n_keys+1 entries. */
+rtr_status rtr_tdf_batch(rtr_context* ctx, const int* d_occ, const int* d_offsets,
+                         int n_keys, int dim, float* d_tdf, rtr_stream_t stream);
+
+/* ---- nearest-neighbour search ---------------------------------------------
+ * Exact searches over a radix-sorted uniform grid.  Squared distances are
+ * computed in FP32 as ((dx*dx + dy*dy) + dz*dz) with dx = q.x - p.x, each
+ * operation rounded separately (no fused multiply-add); ties go to the lowest
+ * target index.  These are the rules of the CPU oracle, so indices are
+ * bit-exact against it. */
+
+/* 1-NN of each query among the targets with d^2 <= max_dist^2
+ * (max_dist <= 0 or infinite: unbounded).  Writes the target index or -1 and
+ * the squared distance (or +inf). */
+rtr_status rtr_knn1(rtr_context* ctx, const float* d_query, int n_query,
+                    const float* d_target, int n_target, float max_dist,
+                    int32_t* d_out_idx, float* d_out_d2, rtr_stream_t stream);
+
+/* k nearest neighbours (1 <= k <= 32), sorted by (d^2, index).  Unbounded. */
+rtr_status rtr_knn(rtr_context* ctx, const float* d_query, int n_query,
+                   const float* d_target, int n_target, int k,
+                   int32_t* d_out_idx, float* d_out_d2, rtr_stream_t stream);
+
+/* ---- ICP (point-to-point) -------------------------------------------------
+ * Replaces the PCL IterativeClosestPoint of keyPointICP (function.h:111-148).
+ * One persistent cooperative kernel runs all iterations: per iteration it
+ * transforms the source, finds the exact 1-NN in the target grid, rejects
+ * pairs beyond max_corr_dist, accumulates the centred 3x3 cross-covariance in
+ * FP32 with compensated (Kahan) sums, reduces the block partials in FP64 and
+ * solves the pose in FP64 (Umeyama, Jacobi SVD). */
+typedef struct rtr_icp_params {
+  int    max_iterations;         /* PCL default 10                                */
+  float  max_corr_dist;          /* metres; <= 0 = unbounded (PCL default)        */
+  double transformation_epsilon; /* stop when |dt|^2 < eps (0: only dt == 0)       */
+  double rotation_epsilon;       /* stop when cos(dangle) > this (0: disabled)     */
+  float  cell_size;              /* target grid cell; 0 = automatic               */
+  int    record_trace;           /* fill d_trace_pose / d_trace_corr if non-NULL  */
+} rtr_icp_params;
+
+typedef struct rtr_icp_result {
+  double pose[16];     /* final source->target transform, row-major          */
+  double fitness;      /* mean squared distance of the last correspondences  */
+  int    iterations;   /* iterations performed                               */
+  int    converged;    /* 1 unless stopped for < 3 correspondences / timeout */
+  int    n_corr;       /* correspondences of the last iteration              */
+  int    status;       /* RTR_OK or RTR_ERR_TIMEOUT                          */
+} rtr_icp_result;
+
+void rtr_icp_default_params(rtr_icp_params* p);
+
+/* h_init_pose: host row-major 4x4 (NULL = identity).  d_result: device
+ * rtr_icp_result.  d_trace_pose (optional): (max_iterations+1)*16 doubles —
+ * the pose before every iteration and after the last.  d_trace_corr
+ * (optional): max_iterations*n_src int32 — the target index (or -1) of every
+ * source point (original order) in every iteration. */
+rtr_status rtr_icp(rtr_context* ctx, const float* d_src, int n_src,
+                   const float* d_tgt, int n_tgt, const rtr_icp_params* params,
+                   const double* h_init_pose, rtr_icp_result* d_result,
+                   double* d_trace_pose, int32_t* d_trace_corr, rtr_stream_t stream);
+
+/* Same with HOST point buffers and a HOST result; copies in and out and
+ * synchronises.  This is the call keyPointICP makes. */
+rtr_status rtr_icp_host(rtr_context* ctx, const float* h_src, int n_src,
+                        const float* h_tgt, int n_tgt, const rtr_icp_params* params,
+                        const double* h_init_pose, rtr_icp_result* h_result);
+
+/* ---- synthetic inputs (host only; seeded, identical on every machine) ----- */
+
+/* Shapes: 0 = chair (seat 0.45x0.45x0.03, four legs 0.03x0.03x0.45, backrest
+ * 0.45x0.03x0.45), 1 = desk (top 1.2x0.6x0.03 on four 0.05x0.05x0.72 legs),
+ * 2 = sofa (2.0x0.9x0.8 box assembly).  n points area-uniform on the boxes'
+ * faces, floor at z = 0. */
+rtr_status rtr_synth_shape(int shape, uint64_t seed, int n, float* h_out_xyz4);
+/* Rigid transform: rotation axis uniform on the sphere, angle uniform in
+ * [0, max_angle_deg], translation uniform in [-max_t, max_t] per axis. */
+void rtr_synth_rigid(uint64_t seed, double max_angle_deg, double max_t, double* h_T16);
+/* out = T * in + N(0, sigma^2) per coordinate (in and out may alias). */
+void rtr_synth_transform_noise(const float* h_in, int n, const double* h_T16, double sigma,
+                               uint64_t seed, float* h_out);
+/* Remove a fraction U[0, max_frac] of the points on one side of a random
+ * plane; writes the kept points in their original order, returns their count. */
+int rtr_synth_crop(const float* h_in, int n, double max_frac, uint64_t seed, float* h_out);
+
+/* One viewpoint of a 5 x 5 x 3 m room (floor z = 0, walls y = +2.5 and
+ * x = -2.5) holding box furniture at seeded yaw and position, ray-cast from a
+ * pinhole camera: each point is the first hit of a ray through a uniformly
+ * drawn pixel, plus N(0, sigma^2) noise per coordinate. */
+typedef struct rtr_room_params {
+  int    n_points;               /* 300,000                               */
+  int    n_chairs, n_desks, n_sofas;
+  double sigma;                  /* 0.003 m                               */
+  double cam[3];                 /* (0, -2.5, 1.5)                        */
+  double look_at[3];             /* (0, 0.8, 0.3)                         */
+  int    width, height;          /* 640 x 480                             */
+  double fx, fy, cx, cy;         /* 400, 400, 319.5, 239.5                */
+} rtr_room_params;
+void rtr_room_default_params(rtr_room_params* p);
+/* h_inst_shape / h_inst_pose16 (optional, max_instances entries): each piece's
+ * shape id and object->world pose (row-major 4x4). */
+rtr_status rtr_synth_room(const rtr_room_params* p, uint64_t seed, float* h_out_xyz4,
+                          int max_instances, int* h_inst_shape, double* h_inst_pose16,
+                          int* h_n_instances);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RTR_H_ */

@@ -1,0 +1,170 @@
+"""CPU oracle (test infrastructure).
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg
+may import this package; the product (``realtime_robot_gb300``) never does.
+It wraps ``liboracle.so`` (oracle.c, a plain-C restatement of the hot path)
+and holds numpy restatements for the later stages.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "liboracle.so"
+_lib = None
+
+_P, _I, _F, _D = C.c_void_p, C.c_int, C.c_float, C.c_double
+
+
+class IcpOut(C.Structure):
+    _fields_ = [("pose", C.c_double * 16), ("fitness", C.c_double), ("iterations", C.c_int),
+                ("converged", C.c_int), ("n_corr", C.c_int)]
+
+
+_SIG = {
+    "orc_num_threads": (_I, []),
+    "orc_set_threads": (None, [_I]),
+    "orc_nn1_brute": (None, [_P, _I, _P, _I, _F, _P, _P]),
+    "orc_nn1_grid": (None, [_P, _I, _P, _I, _F, _F, _P, _P]),
+    "orc_knn_brute": (None, [_P, _I, _P, _I, _I, _P, _P]),
+    "orc_transform_f32": (None, [_P, _P, _I, _P]),
+    "orc_rigid_fit": (_I, [_P, _P, _P, _I, _P]),
+    "orc_icp": (None, [_P, _I, _P, _I, _I, _F, _D, _D, _P, C.POINTER(IcpOut), _P, _P]),
+    "orc_icp_replay": (None, [_P, _I, _P, _I, _F, _P, _I, _P, _P, _P]),
+    "orc_tdf": (None, [_P, _I, _I, _P]),
+}
+
+
+def build() -> Path:
+    """Compile liboracle.so with the recipe in oracle/Makefile."""
+    r = subprocess.run(["make", "-s", "-C", str(HERE)], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            build()
+        L = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in _SIG.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _f4(a) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if a.ndim != 2 or a.shape[1] != 4:
+        raise ValueError("expected [n,4] float32 points")
+    return a
+
+
+def _r2(max_dist: float) -> float:
+    return max_dist * max_dist if (max_dist and 0 < max_dist < 1e18) else float("inf")
+
+
+def set_threads(n: int) -> None:
+    lib().orc_set_threads(int(n))
+
+
+def num_threads() -> int:
+    return lib().orc_num_threads()
+
+
+def nn1(q, t, max_dist: float = 0.0, method: str = "grid", cell: float = 0.0):
+    q, t = _f4(q), _f4(t)
+    idx = np.empty(q.shape[0], np.int32)
+    d2 = np.empty(q.shape[0], np.float32)
+    if method == "brute":
+        lib().orc_nn1_brute(q.ctypes.data, q.shape[0], t.ctypes.data, t.shape[0], _r2(max_dist),
+                            idx.ctypes.data, d2.ctypes.data)
+    else:
+        lib().orc_nn1_grid(q.ctypes.data, q.shape[0], t.ctypes.data, t.shape[0], _r2(max_dist),
+                           float(cell), idx.ctypes.data, d2.ctypes.data)
+    return idx, d2
+
+
+def knn(q, t, k: int):
+    q, t = _f4(q), _f4(t)
+    idx = np.empty((q.shape[0], k), np.int32)
+    d2 = np.empty((q.shape[0], k), np.float32)
+    lib().orc_knn_brute(q.ctypes.data, q.shape[0], t.ctypes.data, t.shape[0], int(k),
+                        idx.ctypes.data, d2.ctypes.data)
+    return idx, d2
+
+
+def transform_f32(T, pts) -> np.ndarray:
+    pts = _f4(pts)
+    Tc = np.ascontiguousarray(T, np.float64).reshape(16)
+    out = np.empty_like(pts)
+    lib().orc_transform_f32(Tc.ctypes.data, pts.ctypes.data, pts.shape[0], out.ctypes.data)
+    return out
+
+
+def rigid_fit(p, q, corr=None) -> tuple[np.ndarray, int]:
+    p, q = _f4(p), _f4(q)
+    T = np.empty(16, np.float64)
+    c = None if corr is None else np.ascontiguousarray(corr, np.int32)
+    m = lib().orc_rigid_fit(p.ctypes.data, q.ctypes.data, None if c is None else c.ctypes.data,
+                            p.shape[0], T.ctypes.data)
+    return T.reshape(4, 4), m
+
+
+def icp(src, tgt, max_iterations=10, max_corr_dist=0.0, init=None, eps_t=0.0, eps_r=0.0,
+        trace=False):
+    src, tgt = _f4(src), _f4(tgt)
+    out = IcpOut()
+    ini = None if init is None else np.ascontiguousarray(init, np.float64).reshape(16)
+    tp = np.zeros((max_iterations + 1, 16), np.float64) if trace else None
+    tc = np.full((max_iterations, src.shape[0]), -2, np.int32) if trace else None
+    lib().orc_icp(src.ctypes.data, src.shape[0], tgt.ctypes.data, tgt.shape[0], max_iterations,
+                  float(max_corr_dist), eps_t, eps_r, None if ini is None else ini.ctypes.data,
+                  C.byref(out), None if tp is None else tp.ctypes.data,
+                  None if tc is None else tc.ctypes.data)
+    res = {"pose": np.array(out.pose[:]).reshape(4, 4), "fitness": out.fitness,
+           "iterations": out.iterations, "converged": out.converged, "n_corr": out.n_corr}
+    if trace:
+        res["trace_pose"] = tp
+        res["trace_corr"] = tc
+    return res
+
+
+def icp_replay(src, tgt, max_corr_dist, poses_in):
+    """Replay GPU iterations: poses_in[k] -> (corr[k], poses_out[k+1])."""
+    src, tgt = _f4(src), _f4(tgt)
+    poses_in = np.ascontiguousarray(poses_in, np.float64).reshape(-1, 16)
+    iters = poses_in.shape[0] - 1
+    corr = np.empty((iters, src.shape[0]), np.int32)
+    pout = np.zeros((iters + 1, 16), np.float64)
+    ncorr = np.zeros(iters, np.int32)
+    lib().orc_icp_replay(src.ctypes.data, src.shape[0], tgt.ctypes.data, tgt.shape[0],
+                         float(max_corr_dist), poses_in.ctypes.data, iters, corr.ctypes.data,
+                         pout.ctypes.data, ncorr.ctypes.data)
+    return corr, pout.reshape(-1, 4, 4), ncorr
+
+
+def tdf(occ, dim: int) -> np.ndarray:
+    occ = np.ascontiguousarray(occ, np.int32).reshape(-1, 3)
+    out = np.empty(dim ** 3, np.float32)
+    lib().orc_tdf(occ.ctypes.data if occ.size else None, occ.shape[0], int(dim), out.ctypes.data)
+    return out
+
+
+def pose_error(Ta, Tb) -> tuple[float, float]:
+    """(translation error m, rotation error rad) between two 4x4 poses."""
+    Ta, Tb = np.asarray(Ta, np.float64), np.asarray(Tb, np.float64)
+    dt = float(np.linalg.norm(Ta[:3, 3] - Tb[:3, 3]))
+    Rd = Ta[:3, :3] @ Tb[:3, :3].T
+    c = np.clip((np.trace(Rd) - 1.0) / 2.0, -1.0, 1.0)
+    # accurate for small angles: use the skew part
+    s = 0.5 * np.linalg.norm([Rd[2, 1] - Rd[1, 2], Rd[0, 2] - Rd[2, 0], Rd[1, 0] - Rd[0, 1]])
+    return dt, float(np.arctan2(s, c))

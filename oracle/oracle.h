@@ -1,0 +1,66 @@
+/*
+ * oracle.h — CPU restatement of the registration hot path, used ONLY as the
+ * checker (tests/, __graft_entry__.smoke) and as the timed CPU baseline
+ * (bench.py cpu_baseline / --impl reference).  Never linked into librtr.so.
+ *
+ * Parity status: the PCL-backed stages (1-NN, ICP, voxel grid, normals,
+ * uniform sampling, SHOT, matching, GC) restate published methods because PCL
+ * 1.8.0's source is not part of the reference; they are pinned only by the
+ * reference's recorded PCD fixtures (translation pairs, see tests/golden).  The
+ * TDF restates kernel.cu:8-31 exactly.
+ *
+ * Arithmetic rules shared with the GPU (compile with -ffp-contract=off):
+ *   d2(q, p)  = ((dx*dx + dy*dy) + dz*dz), dx = q.x - p.x, each op rounded;
+ *   T(p).x    = ((r00*x + r01*y) + r02*z) + t0 with r, t rounded to float;
+ *   ties      = lowest target index.
+ */
+#ifndef RTR_ORACLE_H_
+#define RTR_ORACLE_H_
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+int orc_num_threads(void);
+void orc_set_threads(int n);
+
+/* ---- nearest neighbours (PCL KdTreeFLANN nearestKSearch semantics, made exact) */
+void orc_nn1_brute(const float* q, int nq, const float* t, int nt, float r2max, int32_t* idx,
+                   float* d2);
+void orc_nn1_grid(const float* q, int nq, const float* t, int nt, float r2max, float cell,
+                  int32_t* idx, float* d2);
+void orc_knn_brute(const float* q, int nq, const float* t, int nt, int k, int32_t* idx, float* d2);
+
+/* ---- pose */
+void orc_transform_f32(const double* T16, const float* in, int n, float* out);
+/* Least-squares rigid transform q ~ R p + t over pairs (FP64, Horn's
+ * quaternion method; same minimiser as Umeyama's SVD form). Returns 0 if n<3. */
+int orc_rigid_fit(const float* p, const float* q, const int32_t* corr, int n, double* T16);
+
+/* ---- ICP (function.h:111-148 keyPointICP → PCL IterativeClosestPoint) */
+typedef struct orc_icp_out {
+  double pose[16];
+  double fitness;
+  int iterations;
+  int converged;
+  int n_corr;
+} orc_icp_out;
+/* Full oracle ICP: fixed max_iterations unless eps_t > 0 criteria stop it. */
+void orc_icp(const float* src, int ns, const float* tgt, int nt, int max_it, float max_dist,
+             double eps_t, double eps_r, const double* init16, orc_icp_out* out,
+             double* trace_pose, int32_t* trace_corr);
+/* Replay: for each iteration k, transform the source with the GIVEN pose
+ * poses_in[k] (rounded to float like the GPU), find exact correspondences
+ * (corr_out[k]), fit in FP64 and write poses_out[k+1] = dT * poses_in[k]. */
+void orc_icp_replay(const float* src, int ns, const float* tgt, int nt, float max_dist,
+                    const double* poses_in, int iters, int32_t* corr_out, double* poses_out,
+                    int32_t* ncorr_out);
+
+/* ---- TDF (kernel.cu:8-31): out[v] = min(900, min_i |v - occ_i|^2) */
+void orc_tdf(const int32_t* occ, int n_occ, int dim, float* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,322 @@
+"""realtime_robot_gb300 — Python host mirror of the rtr C ABI (include/rtr.h).
+
+The compute path is ``librtr.so`` (hand-written sm_103a CUDA kernels).  This
+module only loads it with ctypes, passes device pointers of torch tensors and
+turns status codes into exceptions.  There is no CPU fallback: every call that
+computes raises ``RtrError`` when the library or the GPU is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+__all__ = ["lib", "RtrError", "Context", "IcpParams", "IcpResult", "RoomParams", "LIB_PATH"]
+
+LIB_PATH = Path(__file__).resolve().parent / "librtr.so"
+_lib = None
+
+
+class RtrError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{_status_name(status)}: {msg}")
+        self.status = status
+
+
+_STATUS = {0: "RTR_OK", 1: "RTR_ERR_INVALID_ARG", 2: "RTR_ERR_OOM", 3: "RTR_ERR_TIMEOUT",
+           4: "RTR_ERR_NOT_FOUND", 5: "RTR_ERR_CUDA", 6: "RTR_ERR_CAPACITY", 7: "RTR_ERR_NO_DEVICE"}
+
+
+def _status_name(s: int) -> str:
+    return _STATUS.get(s, f"status {s}")
+
+
+class IcpParams(C.Structure):
+    _fields_ = [("max_iterations", C.c_int), ("max_corr_dist", C.c_float),
+                ("transformation_epsilon", C.c_double), ("rotation_epsilon", C.c_double),
+                ("cell_size", C.c_float), ("record_trace", C.c_int)]
+
+
+class IcpResult(C.Structure):
+    _fields_ = [("pose", C.c_double * 16), ("fitness", C.c_double), ("iterations", C.c_int),
+                ("converged", C.c_int), ("n_corr", C.c_int), ("status", C.c_int)]
+
+
+class RoomParams(C.Structure):
+    _fields_ = [("n_points", C.c_int), ("n_chairs", C.c_int), ("n_desks", C.c_int),
+                ("n_sofas", C.c_int), ("sigma", C.c_double), ("cam", C.c_double * 3),
+                ("look_at", C.c_double * 3), ("width", C.c_int), ("height", C.c_int),
+                ("fx", C.c_double), ("fy", C.c_double), ("cx", C.c_double), ("cy", C.c_double)]
+
+
+_P = C.c_void_p
+_I = C.c_int
+_F = C.c_float
+_D = C.c_double
+_U64 = C.c_uint64
+_SIG = {
+    "rtr_status_string": (C.c_char_p, [_I]),
+    "rtr_last_error": (C.c_char_p, []),
+    "rtr_version": (C.c_char_p, []),
+    "rtr_context_create": (_I, [_I, C.POINTER(_P)]),
+    "rtr_context_destroy": (_I, [_P]),
+    "rtr_context_reserve": (_I, [_P, C.c_size_t]),
+    "rtr_context_scratch_bytes": (C.c_size_t, [_P]),
+    "rtr_context_set_wait_budget_ms": (_I, [_P, _D]),
+    "rtr_context_check": (_I, [_P, _P]),
+    "rtr_context_set_profiling": (_I, [_P, _I]),
+    "rtr_context_profile_count": (_I, [_P]),
+    "rtr_context_profile_get": (_I, [_P, _I, C.POINTER(C.c_char_p), C.POINTER(C.c_float)]),
+    "rtr_context_profile_clear": (None, [_P]),
+    "rtr_launch_count": (C.c_uint64, []),
+    "ComputeTDFWithCuda": (_I, [_P, _P, _I, _I]),
+    "rtr_tdf_batch": (_I, [_P, _P, _P, _I, _I, _P, _P]),
+    "rtr_knn1": (_I, [_P, _P, _I, _P, _I, _F, _P, _P, _P]),
+    "rtr_knn": (_I, [_P, _P, _I, _P, _I, _I, _P, _P, _P]),
+    "rtr_icp_default_params": (None, [C.POINTER(IcpParams)]),
+    "rtr_icp": (_I, [_P, _P, _I, _P, _I, C.POINTER(IcpParams), _P, _P, _P, _P, _P]),
+    "rtr_icp_host": (_I, [_P, _P, _I, _P, _I, C.POINTER(IcpParams), _P, C.POINTER(IcpResult)]),
+    "rtr_synth_shape": (_I, [_I, _U64, _I, _P]),
+    "rtr_synth_rigid": (None, [_U64, _D, _D, _P]),
+    "rtr_synth_transform_noise": (None, [_P, _I, _P, _D, _U64, _P]),
+    "rtr_synth_crop": (_I, [_P, _I, _D, _U64, _P]),
+    "rtr_room_default_params": (None, [C.POINTER(RoomParams)]),
+    "rtr_synth_room": (_I, [C.POINTER(RoomParams), _U64, _P, _I, _P, _P, _P]),
+}
+
+
+def lib():
+    """Load librtr.so (built by ``__graft_entry__.build()``); raises if absent."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RtrError(5, f"{LIB_PATH} is missing: run __graft_entry__.build() first")
+        L = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in _SIG.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def declared_symbols() -> list[str]:
+    return list(_SIG)
+
+
+def launch_count() -> int:
+    """Kernels launched by librtr.so in this process so far."""
+    return int(lib().rtr_launch_count())
+
+
+def check(st: int) -> None:
+    if st != 0:
+        raise RtrError(st, lib().rtr_last_error().decode(errors="replace"))
+
+
+def _ptr(t) -> int:
+    if t is None:
+        return None
+    if isinstance(t, np.ndarray):
+        return t.ctypes.data
+    return t.data_ptr()
+
+
+def _stream(stream) -> int:
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    return int(stream)
+
+
+class Context:
+    """Owns an rtr_context (scratch arena + status words) on one device."""
+
+    def __init__(self, device: int = 0):
+        h = _P()
+        check(lib().rtr_context_create(device, C.byref(h)))
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if self.h:
+            lib().rtr_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def reserve(self, nbytes: int):
+        check(lib().rtr_context_reserve(self.h, nbytes))
+
+    def scratch_bytes(self) -> int:
+        return lib().rtr_context_scratch_bytes(self.h)
+
+    def set_wait_budget_ms(self, ms: float):
+        check(lib().rtr_context_set_wait_budget_ms(self.h, ms))
+
+    def check(self, stream=None):
+        check(lib().rtr_context_check(self.h, _stream(stream)))
+
+    def set_profiling(self, on: bool):
+        check(lib().rtr_context_set_profiling(self.h, 1 if on else 0))
+
+    def profile(self, clear: bool = True) -> list[tuple[str, float]]:
+        """Recorded stages [(name, ms)] since the last clear (synchronises)."""
+        out = []
+        for i in range(lib().rtr_context_profile_count(self.h)):
+            nm, ms = C.c_char_p(), C.c_float()
+            check(lib().rtr_context_profile_get(self.h, i, C.byref(nm), C.byref(ms)))
+            out.append((nm.value.decode(), ms.value))
+        if clear:
+            lib().rtr_context_profile_clear(self.h)
+        return out
+
+    # -- searches -----------------------------------------------------------
+    def knn1(self, query, target, max_dist: float = 0.0, stream=None):
+        import torch
+        nq, nt = query.shape[0], target.shape[0]
+        idx = torch.empty(nq, dtype=torch.int32, device=query.device)
+        d2 = torch.empty(nq, dtype=torch.float32, device=query.device)
+        check(lib().rtr_knn1(self.h, _ptr(query), nq, _ptr(target), nt, float(max_dist),
+                             _ptr(idx), _ptr(d2), _stream(stream)))
+        return idx, d2
+
+    def knn(self, query, target, k: int, stream=None):
+        import torch
+        nq, nt = query.shape[0], target.shape[0]
+        idx = torch.empty((nq, k), dtype=torch.int32, device=query.device)
+        d2 = torch.empty((nq, k), dtype=torch.float32, device=query.device)
+        check(lib().rtr_knn(self.h, _ptr(query), nq, _ptr(target), nt, int(k), _ptr(idx),
+                            _ptr(d2), _stream(stream)))
+        return idx, d2
+
+    # -- ICP ------------------------------------------------------------------
+    def icp(self, src, tgt, max_iterations=10, max_corr_dist=0.0, init=None,
+            transformation_epsilon=0.0, rotation_epsilon=0.0, cell_size=0.0,
+            trace=False, result=None, stream=None):
+        """Run ICP on device tensors [n,4] float32.  Returns a device result
+        buffer (bytes of rtr_icp_result) and, with trace=True, the per-iteration
+        poses [(it+1),16] and correspondences [it, n_src]."""
+        import torch
+        p = IcpParams(max_iterations, max_corr_dist, transformation_epsilon, rotation_epsilon,
+                      cell_size, 1 if trace else 0)
+        dev = src.device
+        if result is None:
+            result = torch.zeros(C.sizeof(IcpResult), dtype=torch.uint8, device=dev)
+        tp = tc = None
+        if trace:
+            tp = torch.zeros((max_iterations + 1, 16), dtype=torch.float64, device=dev)
+            tc = torch.full((max_iterations, src.shape[0]), -2, dtype=torch.int32, device=dev)
+        ini = None
+        if init is not None:
+            ini = np.ascontiguousarray(np.asarray(init, dtype=np.float64).reshape(16))
+        check(lib().rtr_icp(self.h, _ptr(src), src.shape[0], _ptr(tgt), tgt.shape[0], C.byref(p),
+                            None if ini is None else ini.ctypes.data, _ptr(result), _ptr(tp),
+                            _ptr(tc), _stream(stream)))
+        return result, tp, tc
+
+    @staticmethod
+    def parse_icp_result(buf) -> dict:
+        raw = bytes(buf.cpu().numpy().tobytes()) if not isinstance(buf, (bytes, bytearray)) else buf
+        r = IcpResult.from_buffer_copy(raw)
+        return {"pose": np.array(r.pose[:], dtype=np.float64).reshape(4, 4), "fitness": r.fitness,
+                "iterations": r.iterations, "converged": r.converged, "n_corr": r.n_corr,
+                "status": r.status}
+
+    def icp_host(self, src: np.ndarray, tgt: np.ndarray, max_iterations=10, max_corr_dist=0.0,
+                 init=None, transformation_epsilon=0.0, rotation_epsilon=0.0, cell_size=0.0):
+        src = np.ascontiguousarray(src, dtype=np.float32)
+        tgt = np.ascontiguousarray(tgt, dtype=np.float32)
+        p = IcpParams(max_iterations, max_corr_dist, transformation_epsilon, rotation_epsilon,
+                      cell_size, 0)
+        r = IcpResult()
+        ini = None if init is None else np.ascontiguousarray(np.asarray(init, np.float64).reshape(16))
+        check(lib().rtr_icp_host(self.h, src.ctypes.data, src.shape[0], tgt.ctypes.data,
+                                 tgt.shape[0], C.byref(p),
+                                 None if ini is None else ini.ctypes.data, C.byref(r)))
+        return {"pose": np.array(r.pose[:]).reshape(4, 4), "fitness": r.fitness,
+                "iterations": r.iterations, "converged": r.converged, "n_corr": r.n_corr,
+                "status": r.status}
+
+    # -- TDF ------------------------------------------------------------------
+    def tdf_batch(self, occ, offsets, dim: int, stream=None):
+        import torch
+        n = offsets.shape[0] - 1
+        out = torch.empty((n, dim * dim * dim), dtype=torch.float32, device=offsets.device)
+        check(lib().rtr_tdf_batch(self.h, _ptr(occ), _ptr(offsets), n, dim, _ptr(out),
+                                  _stream(stream)))
+        return out
+
+
+def compute_tdf_with_cuda(occ: np.ndarray, grid_value: np.ndarray, dim: int) -> int:
+    """The reference's ComputeTDFWithCuda (kernel.cu:34): host arrays in/out."""
+    occ = np.ascontiguousarray(occ, dtype=np.int32).reshape(-1)
+    assert grid_value.dtype == np.float32 and grid_value.flags.c_contiguous
+    return lib().ComputeTDFWithCuda(occ.ctypes.data if occ.size else None, grid_value.ctypes.data,
+                                    int(dim), occ.size // 3)
+
+
+# -- synthetic inputs (host) -------------------------------------------------
+CHAIR, DESK, SOFA = 0, 1, 2
+
+
+def synth_shape(shape: int, n: int, seed: int) -> np.ndarray:
+    out = np.empty((n, 4), dtype=np.float32)
+    check(lib().rtr_synth_shape(shape, seed, n, out.ctypes.data))
+    return out
+
+
+def synth_rigid(seed: int, max_angle_deg: float, max_t: float) -> np.ndarray:
+    T = np.empty(16, dtype=np.float64)
+    lib().rtr_synth_rigid(seed, max_angle_deg, max_t, T.ctypes.data)
+    return T.reshape(4, 4)
+
+
+def synth_transform_noise(pts: np.ndarray, T: np.ndarray, sigma: float, seed: int) -> np.ndarray:
+    pts = np.ascontiguousarray(pts, dtype=np.float32)
+    out = np.empty_like(pts)
+    Tc = np.ascontiguousarray(T, dtype=np.float64).reshape(16)
+    lib().rtr_synth_transform_noise(pts.ctypes.data, pts.shape[0], Tc.ctypes.data, sigma, seed,
+                                    out.ctypes.data)
+    return out
+
+
+def synth_crop(pts: np.ndarray, max_frac: float, seed: int) -> np.ndarray:
+    pts = np.ascontiguousarray(pts, dtype=np.float32)
+    out = np.empty_like(pts)
+    m = lib().rtr_synth_crop(pts.ctypes.data, pts.shape[0], max_frac, seed, out.ctypes.data)
+    return out[:m].copy()
+
+
+def room_default_params() -> RoomParams:
+    p = RoomParams()
+    lib().rtr_room_default_params(C.byref(p))
+    return p
+
+
+def synth_room(seed: int, params: RoomParams | None = None, max_instances: int = 16):
+    p = params or room_default_params()
+    out = np.empty((p.n_points, 4), dtype=np.float32)
+    shapes = np.zeros(max_instances, dtype=np.int32)
+    poses = np.zeros((max_instances, 16), dtype=np.float64)
+    n = C.c_int(0)
+    check(lib().rtr_synth_room(C.byref(p), seed, out.ctypes.data, max_instances,
+                               shapes.ctypes.data, poses.ctypes.data, C.byref(n)))
+    k = min(n.value, max_instances)
+    return out, shapes[:k].copy(), poses[:k].reshape(k, 4, 4).copy()
+
+
+def config0_pair(seed: int, n: int = 20000):
+    """Config-0 ICP pair: chair (n points) and its copy under a seeded rigid
+    transform (axis uniform on S^2, angle U[0,15 deg], t U[+-0.1 m]^3) plus
+    N(0, 2 mm) noise.  Returns (source, target, T_true)."""
+    src = synth_shape(CHAIR, n, seed)
+    T = synth_rigid(seed, 15.0, 0.1)
+    tgt = synth_transform_noise(src, T, 0.002, seed + 7)
+    return src, tgt, T

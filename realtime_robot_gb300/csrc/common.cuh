@@ -1,0 +1,206 @@
+// common.cuh — shared device helpers, context internals and error plumbing for
+// the rtr_* C ABI (include/rtr.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string>
+
+#include "../../include/rtr.h"
+
+#define RTR_VERSION_STRING "0.1.0"
+
+// ---------------------------------------------------------------------------
+// error plumbing (host)
+// ---------------------------------------------------------------------------
+namespace rtr {
+
+void set_error(const char* fmt, ...);
+rtr_status fail(rtr_status st, const char* fmt, ...);
+rtr_status cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+
+}  // namespace rtr
+
+#define RTR_CUDA(call)                                                        \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess) return rtr::cuda_fail(e_, #call, __FILE__, __LINE__); \
+  } while (0)
+
+#define RTR_TRY(call)                   \
+  do {                                  \
+    rtr_status s_ = (call);             \
+    if (s_ != RTR_OK) return s_;        \
+  } while (0)
+
+#define RTR_CHECK_ARG(cond, ...)                                   \
+  do {                                                             \
+    if (!(cond)) return rtr::fail(RTR_ERR_INVALID_ARG, __VA_ARGS__); \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// context (host) + scratch arena
+// ---------------------------------------------------------------------------
+#include <atomic>
+#include <vector>
+
+namespace rtr {
+extern std::atomic<uint64_t> g_launches;
+}
+// Count kernel launches issued by the library (rtr_launch_count).
+#define RTR_LAUNCHED(n) (rtr::g_launches.fetch_add((n), std::memory_order_relaxed))
+
+struct rtr_prof_rec {
+  const char* name;
+  cudaEvent_t a, b;
+};
+
+struct rtr_context {
+  int device = 0;
+  int num_sms = 0;
+  int max_smem_optin = 0;
+  void* arena = nullptr;        // scratch arena (device)
+  size_t arena_bytes = 0;
+  int* d_status = nullptr;      // device status word written by persistent kernels
+  unsigned* d_sync = nullptr;   // 64 words of barrier counters for persistent kernels
+  double wait_budget_ms = 2000.0;
+  long long wait_budget_cycles = 0;
+  int clock_khz = 0;
+  void* io = nullptr;           // device staging for the host-pointer entry points
+  size_t io_bytes = 0;
+  cudaStream_t host_stream = nullptr;  // stream of the host-pointer entry points
+  bool profiling = false;
+  std::vector<rtr_prof_rec> prof;      // recorded stages (in order)
+  std::vector<cudaEvent_t> event_pool; // reusable events
+};
+
+namespace rtr {
+
+// Bump allocator over the context arena.  A top-level call first sums what it
+// needs (ScratchPlan), ensures the arena holds it, then carves pointers.
+struct ScratchPlan {
+  size_t bytes = 0;
+  template <class T>
+  size_t add(size_t n) {
+    size_t off = (bytes + 255) & ~size_t(255);
+    bytes = off + n * sizeof(T);
+    return off;
+  }
+};
+
+struct Scratch {
+  char* base = nullptr;
+  size_t off = 0, cap = 0;
+  template <class T>
+  T* take(size_t n) {
+    size_t o = (off + 255) & ~size_t(255);
+    if (o + n * sizeof(T) > cap) return nullptr;
+    off = o + n * sizeof(T);
+    return reinterpret_cast<T*>(base + o);
+  }
+};
+
+// Ensure the arena holds `bytes`; grows (synchronising) unless `stream` is
+// being captured, in which case RTR_ERR_CAPACITY is returned.
+rtr_status ensure_scratch(rtr_context* ctx, size_t bytes, cudaStream_t stream, Scratch* out);
+
+bool stream_is_capturing(cudaStream_t s);
+
+// Grow the host-entry staging buffer (synchronises when it grows).
+rtr_status ensure_io(rtr_context* ctx, size_t bytes);
+
+// Records a named event pair around a stage when ctx->profiling is on.
+struct ProfScope {
+  rtr_context* ctx;
+  cudaStream_t st;
+  int slot = -1;
+  ProfScope(rtr_context* c, cudaStream_t s, const char* name);
+  void end();
+  ~ProfScope() { end(); }
+};
+
+}  // namespace rtr
+
+// ---------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------
+#ifdef __CUDACC__
+
+// Squared distance with every operation rounded separately:
+// ((dx*dx + dy*dy) + dz*dz), dx = q.x - p.x.  The CPU oracle uses the same
+// expression with floating-point contraction disabled.
+__device__ __forceinline__ float dist2_exact(float4 q, float4 p) {
+  float dx = __fsub_rn(q.x, p.x), dy = __fsub_rn(q.y, p.y), dz = __fsub_rn(q.z, p.z);
+  return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+
+// y = R p + t with R, t in FP32, each row evaluated as ((r0*x + r1*y) + r2*z) + t.
+__device__ __forceinline__ float4 xform_exact(const float* T12, float4 p) {
+  float4 o;
+  o.x = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(T12[0], p.x), __fmul_rn(T12[1], p.y)), __fmul_rn(T12[2], p.z)), T12[3]);
+  o.y = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(T12[4], p.x), __fmul_rn(T12[5], p.y)), __fmul_rn(T12[6], p.z)), T12[7]);
+  o.z = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(T12[8], p.x), __fmul_rn(T12[9], p.y)), __fmul_rn(T12[10], p.z)), T12[11]);
+  o.w = 0.f;
+  return o;
+}
+
+// Knuth TwoSum: s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  float bp = __fsub_rn(s, a);
+  float ap = __fsub_rn(s, bp);
+  e = __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp));
+}
+
+// Kahan–Babuška (Neumaier) accumulator.
+struct KSum {
+  float s, c;
+  __device__ __forceinline__ void init() { s = 0.f; c = 0.f; }
+  __device__ __forceinline__ void add(float x) {
+    float t, e;
+    two_sum(s, x, t, e);
+    s = t;
+    c = __fadd_rn(c, e);
+  }
+};
+
+// Warp-level compensated reduction of (s, c) pairs; lane 0 holds the result.
+__device__ __forceinline__ void warp_ksum(float& s, float& c) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    float s2 = __shfl_down_sync(0xffffffffu, s, off);
+    float c2 = __shfl_down_sync(0xffffffffu, c, off);
+    float t, e;
+    two_sum(s, s2, t, e);
+    s = t;
+    c = __fadd_rn(__fadd_rn(c, c2), e);
+  }
+}
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Float <-> order-preserving unsigned (for atomicMin/Max on floats).
+__device__ __forceinline__ unsigned float_to_ordered(float f) {
+  unsigned u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ordered_to_float(unsigned u) {
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+#endif  // __CUDACC__

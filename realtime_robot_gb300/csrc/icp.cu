@@ -1,0 +1,424 @@
+// icp.cu — persistent point-to-point ICP (replaces the PCL
+// IterativeClosestPoint used by keyPointICP, function.h:111-148).
+//
+// One cooperative launch runs every iteration.  Per iteration each thread
+// transforms its source points with the FP32 pose, finds the exact 1-NN in the
+// target grid within max_corr_dist (rejection), and accumulates the centred
+// sums (dp, dq, dp dq^T, d^2) in FP32 Kahan–Babuška accumulators; warps and
+// the block combine them with TwoSum-compensated shuffles into one (hi, lo)
+// pair per value per block.  The last block to arrive reduces the block pairs
+// in FP64 (fixed order), solves the pose in FP64 (pose.cuh) and releases the
+// others through a generation word.  Every wait is bounded by a clock64
+// budget; a block that runs out writes RTR_ERR_TIMEOUT and leaves.
+#include <math.h>
+#include <string.h>
+
+#include "grid.cuh"
+#include "pose.cuh"
+#include "search.cuh"
+
+namespace rtr {
+
+constexpr int ICP_THREADS = 128;
+constexpr int ICP_WARPS = ICP_THREADS / 32;
+constexpr int ICP_NV = 16;  // dp(3) dq(3) dp*dq^T(9) d^2(1)
+
+struct IcpDev {
+  GridDev grid;
+  const float4* src;      // source sorted by target cell at the initial pose
+  const int* src_idx;     // original index of each sorted source point
+  int n_src;
+  int max_it;
+  float r2max;
+  double eps_t, eps_r;
+  double init[16];
+  double* pose64;         // [16]
+  float* posef;           // [12]
+  float* partial;         // [B][32]
+  int* pcount;            // [B]
+  unsigned* arrive;
+  unsigned* gen;
+  rtr_icp_result* result;
+  double* trace_pose;
+  int* trace_corr;
+  int* status;
+  long long budget;
+};
+
+__device__ __forceinline__ float centre_of(const GridMeta* m, int a) {
+  return 0.5f * (ordered_to_float(m->bmin[a]) + ordered_to_float(m->bmax[a]));
+}
+
+__global__ void __launch_bounds__(ICP_THREADS) k_icp(IcpDev a) {
+  __shared__ float s_red[ICP_WARPS][ICP_NV][2];
+  __shared__ int s_cnt[ICP_WARPS];
+  __shared__ double s_sum[ICP_NV];
+  __shared__ long long s_n;
+  __shared__ int s_last, s_stop;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int B = gridDim.x;
+  const GridView g = load_view(a.grid);
+  const float c[3] = {centre_of(a.grid.meta, 0), centre_of(a.grid.meta, 1), centre_of(a.grid.meta, 2)};
+  const unsigned stride = (unsigned)B * ICP_THREADS;
+
+  for (int it = 0; it < a.max_it; ++it) {
+    float T[12];
+    if (it == 0) {
+#pragma unroll
+      for (int k = 0; k < 12; ++k) T[k] = __double2float_rn(a.init[k]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 12; ++k) T[k] = __ldcg(a.posef + k);
+    }
+    KSum acc[ICP_NV];
+#pragma unroll
+    for (int v = 0; v < ICP_NV; ++v) acc[v].init();
+    int cnt = 0;
+    for (unsigned i = blockIdx.x * ICP_THREADS + tid; i < (unsigned)a.n_src; i += stride) {
+      const float4 p = xform_exact(T, a.src[i]);
+      float d2;
+      int j, pos;
+      grid_nn1(g, p, a.r2max, d2, j, pos);
+      if (j >= 0) {
+        const float4 q = g.pts[pos];
+        const float dp[3] = {__fsub_rn(p.x, c[0]), __fsub_rn(p.y, c[1]), __fsub_rn(p.z, c[2])};
+        const float dq[3] = {__fsub_rn(q.x, c[0]), __fsub_rn(q.y, c[1]), __fsub_rn(q.z, c[2])};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          acc[k].add(dp[k]);
+          acc[3 + k].add(dq[k]);
+        }
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int k = 0; k < 3; ++k) acc[6 + r * 3 + k].add(__fmul_rn(dp[r], dq[k]));
+        acc[15].add(d2);
+        ++cnt;
+      }
+      if (a.trace_corr) a.trace_corr[(size_t)it * (size_t)a.n_src + (size_t)a.src_idx[i]] = j;
+    }
+    // block partial: compensated warp sums, then across warps
+#pragma unroll
+    for (int v = 0; v < ICP_NV; ++v) {
+      float s = acc[v].s, cc = acc[v].c;
+      warp_ksum(s, cc);
+      if (lane == 0) {
+        s_red[warp][v][0] = s;
+        s_red[warp][v][1] = cc;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    if (lane == 0) s_cnt[warp] = cnt;
+    __syncthreads();
+    if (tid < ICP_NV) {
+      float s = s_red[0][tid][0], cc = s_red[0][tid][1];
+      for (int w = 1; w < ICP_WARPS; ++w) {
+        float t, e;
+        two_sum(s, s_red[w][tid][0], t, e);
+        s = t;
+        cc = __fadd_rn(__fadd_rn(cc, s_red[w][tid][1]), e);
+      }
+      a.partial[blockIdx.x * 32 + tid] = s;
+      a.partial[blockIdx.x * 32 + 16 + tid] = cc;
+    }
+    if (tid == 0) {
+      int tot = 0;
+      for (int w = 0; w < ICP_WARPS; ++w) tot += s_cnt[w];
+      a.pcount[blockIdx.x] = tot;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      const unsigned t = atomicAdd(a.arrive, 1u);
+      s_last = (t == (unsigned)(it + 1) * (unsigned)B - 1u) ? 1 : 0;
+    }
+    __syncthreads();
+    if (s_last) {
+      __threadfence();
+      for (int v = warp; v < ICP_NV; v += ICP_WARPS) {
+        double s = 0.0;
+        for (int b = lane; b < B; b += 32)
+          s += (double)__ldcg(a.partial + b * 32 + v) + (double)__ldcg(a.partial + b * 32 + 16 + v);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) s_sum[v] = s;
+      }
+      if (warp == 0) {
+        long long n = 0;
+        for (int b = lane; b < B; b += 32) n += __ldcg(a.pcount + b);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) n += __shfl_down_sync(0xffffffffu, n, o);
+        if (lane == 0) s_n = n;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        double P[16];
+        if (it == 0) {
+          for (int k = 0; k < 16; ++k) P[k] = a.init[k];
+          if (a.trace_pose)
+            for (int k = 0; k < 16; ++k) a.trace_pose[k] = P[k];
+        } else {
+          for (int k = 0; k < 16; ++k) P[k] = a.pose64[k];
+        }
+        const long long n = s_n;
+        int stop = 0, converged = 1;
+        double fitness = 0.0;
+        if (n < 3) {
+          stop = 1;
+          converged = 0;
+        } else {
+          const double inv = 1.0 / (double)n;
+          double mdp[3], mdq[3], H[9], R[9];
+          for (int k = 0; k < 3; ++k) {
+            mdp[k] = s_sum[k] * inv;
+            mdq[k] = s_sum[3 + k] * inv;
+          }
+          for (int r = 0; r < 3; ++r)
+            for (int k = 0; k < 3; ++k) H[r * 3 + k] = s_sum[6 + r * 3 + k] - (double)n * mdp[r] * mdq[k];
+          umeyama_rotation(H, R);
+          double mp[3], mq[3], t[3];
+          for (int k = 0; k < 3; ++k) {
+            mp[k] = mdp[k] + (double)c[k];
+            mq[k] = mdq[k] + (double)c[k];
+          }
+          for (int r = 0; r < 3; ++r) t[r] = mq[r] - (R[r * 3 + 0] * mp[0] + R[r * 3 + 1] * mp[1] + R[r * 3 + 2] * mp[2]);
+          const double D[16] = {R[0], R[1], R[2], t[0], R[3], R[4], R[5], t[1],
+                                R[6], R[7], R[8], t[2], 0.0,  0.0,  0.0,  1.0};
+          mat4_mul(D, P, P);
+          fitness = s_sum[15] * inv;
+          const double cosang = 0.5 * (R[0] + R[4] + R[8] - 1.0);
+          const double tsq = t[0] * t[0] + t[1] * t[1] + t[2] * t[2];
+          if (a.eps_t > 0.0 && tsq < a.eps_t && (a.eps_r <= 0.0 || cosang > a.eps_r)) stop = 1;
+        }
+        if (it + 1 >= a.max_it) stop = 1;
+        for (int k = 0; k < 16; ++k) a.pose64[k] = P[k];
+        for (int k = 0; k < 12; ++k) a.posef[k] = __double2float_rn(P[k]);
+        if (a.trace_pose)
+          for (int k = 0; k < 16; ++k) a.trace_pose[(size_t)(it + 1) * 16 + k] = P[k];
+        for (int k = 0; k < 16; ++k) a.result->pose[k] = P[k];
+        a.result->fitness = fitness;
+        a.result->iterations = it + 1;
+        a.result->converged = converged;
+        a.result->n_corr = (int)n;
+        a.result->status = RTR_OK;
+        s_stop = stop;
+        __threadfence();
+        st_release_gpu(a.gen, (unsigned)(it + 1) | (stop ? 0x80000000u : 0u));
+      }
+      __syncthreads();
+    } else {
+      if (tid == 0) {
+        const long long t0 = clock64();
+        unsigned gv;
+        for (;;) {
+          gv = ld_acquire_gpu(a.gen);
+          if ((gv & 0x7fffffffu) >= (unsigned)(it + 1)) break;
+          if (clock64() - t0 > a.budget) {
+            atomicExch(a.status, (int)RTR_ERR_TIMEOUT);
+            a.result->status = RTR_ERR_TIMEOUT;
+            a.result->converged = 0;
+            gv = 0x80000000u;
+            break;
+          }
+          __nanosleep(64);
+        }
+        s_stop = (gv >> 31) ? 1 : 0;
+      }
+      __syncthreads();
+    }
+    if (s_stop) break;
+  }
+}
+
+// Sort keys of the source under the initial pose, in the target grid.
+__global__ void __launch_bounds__(256) k_src_keys(const float4* __restrict__ src, int n,
+                                                  IcpDev a, uint32_t* __restrict__ keys) {
+  const GridMeta* m = a.grid.meta;
+  float T[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) T[k] = __double2float_rn(a.init[k]);
+  const float ox = m->ox, oy = m->oy, oz = m->oz, ih = m->inv_h;
+  const int nx = m->nx, ny = m->ny, nz = m->nz;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float4 p = xform_exact(T, src[i]);
+    int cx = min(max(q_cell(p.x, ox, ih), 0), nx - 1);
+    int cy = min(max(q_cell(p.y, oy, ih), 0), ny - 1);
+    int cz = min(max(q_cell(p.z, oz, ih), 0), nz - 1);
+    keys[i] = ((uint32_t)cz * (uint32_t)ny + (uint32_t)cy) * (uint32_t)nx + (uint32_t)cx;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_gather_pts(const float4* __restrict__ pts,
+                                                    const uint32_t* __restrict__ order, int n,
+                                                    float4* __restrict__ out, int* __restrict__ idx) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    uint32_t o = order[i];
+    out[i] = pts[o];
+    idx[i] = (int)o;
+  }
+}
+
+static int icp_max_blocks(rtr_context* ctx) {
+  static int cached_dev = -1, cached = 0;
+  if (cached_dev != ctx->device) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_icp, ICP_THREADS, 0);
+    cached = per_sm * ctx->num_sms;
+    cached_dev = ctx->device;
+  }
+  return cached;
+}
+
+static rtr_status launch_icp(rtr_context* ctx, const IcpDev& a, int blocks, cudaStream_t st) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(ICP_THREADS);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  RTR_CUDA(cudaLaunchKernelEx(&cfg, k_icp, a));
+  RTR_LAUNCHED(1);
+  return RTR_OK;
+}
+
+}  // namespace rtr
+
+using namespace rtr;
+
+extern "C" {
+
+void rtr_icp_default_params(rtr_icp_params* p) {
+  if (!p) return;
+  p->max_iterations = 10;
+  p->max_corr_dist = 0.f;
+  p->transformation_epsilon = 0.0;
+  p->rotation_epsilon = 0.0;
+  p->cell_size = 0.f;
+  p->record_trace = 0;
+}
+
+rtr_status rtr_icp(rtr_context* ctx, const float* d_src, int n_src, const float* d_tgt, int n_tgt,
+                   const rtr_icp_params* params, const double* h_init_pose,
+                   rtr_icp_result* d_result, double* d_trace_pose, int32_t* d_trace_corr,
+                   rtr_stream_t stream) {
+  RTR_CHECK_ARG(ctx && params && d_result, "rtr_icp: ctx, params and d_result are required");
+  RTR_CHECK_ARG(n_src > 0 && n_tgt > 0 && d_src && d_tgt, "rtr_icp: empty source or target");
+  RTR_CHECK_ARG(params->max_iterations > 0, "rtr_icp: max_iterations must be > 0");
+  RTR_CHECK_ARG(((uintptr_t)d_src & 15) == 0 && ((uintptr_t)d_tgt & 15) == 0,
+                "rtr_icp: point arrays must be 16-byte aligned");
+  cudaStream_t st = (cudaStream_t)stream;
+  RTR_CUDA(cudaSetDevice(ctx->device));
+
+  const unsigned cell_cap = default_cell_cap(n_tgt);
+  const int maxb = icp_max_blocks(ctx);
+  int blocks = (n_src + ICP_THREADS - 1) / ICP_THREADS;
+  if (blocks > maxb) blocks = maxb;
+  if (blocks < 1) blocks = 1;
+
+  ScratchPlan plan;
+  grid_plan(plan, n_tgt, cell_cap);
+  plan.add<float4>(n_src);
+  plan.add<int>(n_src);
+  for (int i = 0; i < 4; ++i) plan.add<uint32_t>(n_src);
+  plan.add<uint32_t>(radix_hist_entries(n_src));
+  plan.add<double>(16);
+  plan.add<float>(16);
+  plan.add<float>((size_t)blocks * 32);
+  plan.add<int>(blocks);
+  plan.add<unsigned>(64);
+  Scratch s;
+  RTR_TRY(ensure_scratch(ctx, plan.bytes, st, &s));
+  GridBufs gb;
+  if (!grid_take(s, n_tgt, cell_cap, &gb)) return fail(RTR_ERR_CAPACITY, "rtr_icp: scratch carve");
+  float4* src_sorted = s.take<float4>(n_src);
+  int* src_idx = s.take<int>(n_src);
+  uint32_t* k0 = s.take<uint32_t>(n_src);
+  uint32_t* v0 = s.take<uint32_t>(n_src);
+  uint32_t* k1 = s.take<uint32_t>(n_src);
+  uint32_t* v1 = s.take<uint32_t>(n_src);
+  uint32_t* hist = s.take<uint32_t>(radix_hist_entries(n_src));
+  double* pose64 = s.take<double>(16);
+  float* posef = s.take<float>(16);
+  float* partial = s.take<float>((size_t)blocks * 32);
+  int* pcount = s.take<int>(blocks);
+  unsigned* sync = s.take<unsigned>(64);
+  if (!sync) return fail(RTR_ERR_CAPACITY, "rtr_icp: scratch carve");
+
+  float h = params->cell_size;
+  if (!(h > 0.f)) h = params->max_corr_dist > 0.f ? 0.5f * params->max_corr_dist : -1.f;
+  {
+    ProfScope ps(ctx, st, "grid_build");
+    grid_build(gb, reinterpret_cast<const float4*>(d_tgt), n_tgt, nullptr, h, st);
+  }
+
+  IcpDev a;
+  memset(&a, 0, sizeof(a));
+  a.grid = grid_dev(gb);
+  a.src = src_sorted;
+  a.src_idx = src_idx;
+  a.n_src = n_src;
+  a.max_it = params->max_iterations;
+  const float r = params->max_corr_dist;
+  a.r2max = (r > 0.f && r < 1e18f) ? r * r : __builtin_inff();
+  a.eps_t = params->transformation_epsilon;
+  a.eps_r = params->rotation_epsilon;
+  for (int k = 0; k < 16; ++k) a.init[k] = h_init_pose ? h_init_pose[k] : ((k % 5) == 0 ? 1.0 : 0.0);
+  a.pose64 = pose64;
+  a.posef = posef;
+  a.partial = partial;
+  a.pcount = pcount;
+  a.arrive = sync;
+  a.gen = sync + 1;
+  a.result = d_result;
+  a.trace_pose = params->record_trace ? d_trace_pose : nullptr;
+  a.trace_corr = params->record_trace ? d_trace_corr : nullptr;
+  a.status = ctx->d_status;
+  a.budget = ctx->wait_budget_cycles;
+
+  int nb = (n_src + 255) / 256;
+  if (nb > 152 * 8) nb = 152 * 8;
+  ProfScope ps_sort(ctx, st, "src_sort");
+  k_src_keys<<<nb, 256, 0, st>>>(reinterpret_cast<const float4*>(d_src), n_src, a, k0);
+  int bits = 1;
+  while (bits < 32 && (1ull << bits) < (unsigned long long)cell_cap) ++bits;
+  uint32_t *ks, *vs;
+  radix_sort_pairs(k0, v0, k1, v1, hist, n_src, n_src, nullptr, bits, true, st, &ks, &vs);
+  k_gather_pts<<<nb, 256, 0, st>>>(reinterpret_cast<const float4*>(d_src), vs, n_src, src_sorted,
+                                   src_idx);
+  RTR_LAUNCHED(2);
+  RTR_CUDA(cudaMemsetAsync(sync, 0, 64 * sizeof(unsigned), st));
+  RTR_CUDA(cudaGetLastError());
+  ps_sort.end();
+  ProfScope ps(ctx, st, "icp_kernel");
+  return launch_icp(ctx, a, blocks, st);
+}
+
+rtr_status rtr_icp_host(rtr_context* ctx, const float* h_src, int n_src, const float* h_tgt,
+                        int n_tgt, const rtr_icp_params* params, const double* h_init_pose,
+                        rtr_icp_result* h_result) {
+  RTR_CHECK_ARG(ctx && h_src && h_tgt && params && h_result && n_src > 0 && n_tgt > 0,
+                "rtr_icp_host: bad arguments");
+  RTR_CUDA(cudaSetDevice(ctx->device));
+  const size_t bs = (size_t)n_src * 16, bt = (size_t)n_tgt * 16;
+  const size_t need = ((bs + 255) & ~size_t(255)) + ((bt + 255) & ~size_t(255)) + 256;
+  RTR_TRY(ensure_io(ctx, need));
+  char* io = static_cast<char*>(ctx->io);
+  float* d_src = reinterpret_cast<float*>(io);
+  float* d_tgt = reinterpret_cast<float*>(io + ((bs + 255) & ~size_t(255)));
+  rtr_icp_result* d_res =
+      reinterpret_cast<rtr_icp_result*>(io + ((bs + 255) & ~size_t(255)) + ((bt + 255) & ~size_t(255)));
+  cudaStream_t st = ctx->host_stream;
+  RTR_CUDA(cudaMemcpyAsync(d_src, h_src, bs, cudaMemcpyHostToDevice, st));
+  RTR_CUDA(cudaMemcpyAsync(d_tgt, h_tgt, bt, cudaMemcpyHostToDevice, st));
+  RTR_TRY(rtr_icp(ctx, d_src, n_src, d_tgt, n_tgt, params, h_init_pose, d_res, nullptr, nullptr, st));
+  RTR_CUDA(cudaMemcpyAsync(h_result, d_res, sizeof(rtr_icp_result), cudaMemcpyDeviceToHost, st));
+  return rtr_context_check(ctx, st);
+}
+
+}  // extern "C"

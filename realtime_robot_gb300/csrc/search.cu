@@ -1,0 +1,118 @@
+// search.cu — rtr_knn1 / rtr_knn entry points over the radix-sorted grid.
+#include <string.h>
+
+#include "search.cuh"
+
+namespace rtr {
+
+__global__ void __launch_bounds__(128) k_knn1(GridDev gd, const float4* __restrict__ q, int nq,
+                                              float r2max, int* __restrict__ out_idx,
+                                              float* __restrict__ out_d2) {
+  const GridView g = load_view(gd);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nq; i += gridDim.x * blockDim.x) {
+    float d2;
+    int bi, bp;
+    grid_nn1(g, q[i], r2max, d2, bi, bp);
+    out_idx[i] = bi;
+    if (out_d2) out_d2[i] = d2;
+  }
+}
+
+template <int K>
+__global__ void __launch_bounds__(128) k_knn(GridDev gd, const float4* __restrict__ q, int nq, int k,
+                                             int* __restrict__ out_idx, float* __restrict__ out_d2) {
+  const GridView g = load_view(gd);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nq; i += gridDim.x * blockDim.x) {
+    float bd[K];
+    int bi[K];
+    grid_knn<K>(g, q[i], bd, bi);
+#pragma unroll
+    for (int s = 0; s < K; ++s) {
+      if (s < k) {
+        const bool ok = bi[s] != INT_MAX;
+        out_idx[(size_t)i * k + s] = ok ? bi[s] : -1;
+        if (out_d2) out_d2[(size_t)i * k + s] = ok ? bd[s] : __int_as_float(0x7f800000);
+      }
+    }
+  }
+}
+
+static int search_blocks(int n) {
+  int b = (n + 127) / 128;
+  return b < 1 ? 1 : b;
+}
+
+}  // namespace rtr
+
+using namespace rtr;
+
+extern "C" {
+
+rtr_status rtr_knn1(rtr_context* ctx, const float* d_query, int n_query, const float* d_target,
+                    int n_target, float max_dist, int32_t* d_out_idx, float* d_out_d2,
+                    rtr_stream_t stream) {
+  RTR_CHECK_ARG(ctx && n_query >= 0 && n_target >= 0, "rtr_knn1: bad arguments");
+  if (n_query == 0) return RTR_OK;
+  RTR_CHECK_ARG(d_query && d_out_idx, "rtr_knn1: NULL query or output");
+  cudaStream_t st = (cudaStream_t)stream;
+  RTR_CUDA(cudaSetDevice(ctx->device));
+  if (n_target == 0) {
+    RTR_CUDA(cudaMemsetAsync(d_out_idx, 0xff, (size_t)n_query * 4, st));
+    return RTR_OK;  // d_out_d2 left as is: every index is -1
+  }
+  RTR_CHECK_ARG(d_target != nullptr, "rtr_knn1: NULL target");
+  const unsigned cap = default_cell_cap(n_target);
+  ScratchPlan plan;
+  grid_plan(plan, n_target, cap);
+  Scratch s;
+  RTR_TRY(ensure_scratch(ctx, plan.bytes, st, &s));
+  GridBufs gb;
+  if (!grid_take(s, n_target, cap, &gb)) return fail(RTR_ERR_CAPACITY, "rtr_knn1: scratch");
+  const bool bounded = max_dist > 0.f && max_dist < 1e18f;
+  grid_build(gb, reinterpret_cast<const float4*>(d_target), n_target, nullptr,
+             bounded ? 0.5f * max_dist : -1.f, st);
+  ProfScope ps(ctx, st, "knn1");
+  RTR_LAUNCHED(1);
+  k_knn1<<<search_blocks(n_query), 128, 0, st>>>(grid_dev(gb), reinterpret_cast<const float4*>(d_query),
+                                                 n_query, bounded ? max_dist * max_dist : __builtin_inff(),
+                                                 d_out_idx, d_out_d2);
+  RTR_CUDA(cudaGetLastError());
+  return RTR_OK;
+}
+
+rtr_status rtr_knn(rtr_context* ctx, const float* d_query, int n_query, const float* d_target,
+                   int n_target, int k, int32_t* d_out_idx, float* d_out_d2, rtr_stream_t stream) {
+  RTR_CHECK_ARG(ctx && n_query >= 0 && n_target >= 0, "rtr_knn: bad arguments");
+  RTR_CHECK_ARG(k >= 1 && k <= 32, "rtr_knn: k must be in [1, 32]");
+  if (n_query == 0) return RTR_OK;
+  RTR_CHECK_ARG(d_query && d_out_idx, "rtr_knn: NULL query or output");
+  cudaStream_t st = (cudaStream_t)stream;
+  RTR_CUDA(cudaSetDevice(ctx->device));
+  if (n_target == 0) {
+    RTR_CUDA(cudaMemsetAsync(d_out_idx, 0xff, (size_t)n_query * k * 4, st));
+    return RTR_OK;
+  }
+  RTR_CHECK_ARG(d_target != nullptr, "rtr_knn: NULL target");
+  const unsigned cap = default_cell_cap(n_target);
+  ScratchPlan plan;
+  grid_plan(plan, n_target, cap);
+  Scratch s;
+  RTR_TRY(ensure_scratch(ctx, plan.bytes, st, &s));
+  GridBufs gb;
+  if (!grid_take(s, n_target, cap, &gb)) return fail(RTR_ERR_CAPACITY, "rtr_knn: scratch");
+  grid_build(gb, reinterpret_cast<const float4*>(d_target), n_target, nullptr, -1.f, st);
+  const float4* q = reinterpret_cast<const float4*>(d_query);
+  const int nb = search_blocks(n_query);
+  ProfScope ps(ctx, st, "knn");
+  RTR_LAUNCHED(1);
+  if (k <= 8)
+    k_knn<8><<<nb, 128, 0, st>>>(grid_dev(gb), q, n_query, k, d_out_idx, d_out_d2);
+  else if (k <= 16)
+    k_knn<16><<<nb, 128, 0, st>>>(grid_dev(gb), q, n_query, k, d_out_idx, d_out_d2);
+  else
+    k_knn<32><<<nb, 128, 0, st>>>(grid_dev(gb), q, n_query, k, d_out_idx, d_out_d2);
+  RTR_CUDA(cudaGetLastError());
+  return RTR_OK;
+}
+
+}  // extern "C"

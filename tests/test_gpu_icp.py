@@ -1,0 +1,100 @@
+"""GPU parity of the persistent ICP kernel.
+
+Per iteration the FP64 oracle is replayed on the GPU's own pose: the
+correspondences must be bit-exact and the oracle's FP64 pose update (on those
+same correspondences) must agree with the GPU's to <= 1e-5 m and <= 1e-5 rad."""
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL_T = 1e-5  # metres
+TOL_R = 1e-5  # radians
+
+
+def _dev(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda()
+
+
+def _replay_check(ctx, src, tgt, iters, max_dist, init=None):
+    res, tp, tc = ctx.icp(_dev(src), _dev(tgt), iters, max_dist, init=init, trace=True)
+    r = ctx.parse_icp_result(res)
+    assert r["status"] == 0
+    n_it = r["iterations"]
+    poses = tp.cpu().numpy()[: n_it + 1]
+    corr = tc.cpu().numpy()[:n_it]
+    ocorr, opose, ncorr = O.icp_replay(src, tgt, max_dist, poses)
+    worst_t = worst_r = 0.0
+    for k in range(n_it):
+        assert np.array_equal(corr[k], ocorr[k]), f"iteration {k}: correspondences differ"
+        if ncorr[k] >= 3:
+            dt, dr = O.pose_error(poses[k + 1].reshape(4, 4), opose[k + 1])
+            worst_t, worst_r = max(worst_t, dt), max(worst_r, dr)
+    assert worst_t <= TOL_T and worst_r <= TOL_R, (worst_t, worst_r)
+    return r
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_icp_config0_per_iteration_parity(ctx, rtr, seed):
+    src, tgt, T = rtr.config0_pair(seed)
+    r = _replay_check(ctx, src, tgt, 50, 0.05)
+    assert r["iterations"] == 50 and r["converged"] == 1
+    dt, dr = O.pose_error(r["pose"], T)
+    assert dt < 2e-3 and dr < np.deg2rad(0.5)
+
+
+def test_icp_matches_full_oracle_run(ctx, rtr):
+    src, tgt, _ = rtr.config0_pair(4, 8000)
+    res, _, _ = ctx.icp(_dev(src), _dev(tgt), 30, 0.05)
+    g = ctx.parse_icp_result(res)
+    o = O.icp(src, tgt, 30, 0.05)
+    dt, dr = O.pose_error(g["pose"], o["pose"])
+    assert dt < 1e-4 and dr < 1e-4
+    assert abs(g["n_corr"] - o["n_corr"]) <= 2
+
+
+def test_icp_known_answer_pairs(ctx, golden):
+    E = np.eye(4)
+    E[:3, 3] = golden["t5"]
+    r = _replay_check(ctx, golden["p5"], golden["mcloud"], 50, 0.0)
+    dt, dr = O.pose_error(r["pose"], E)
+    assert dt < 1e-5 and dr < 1e-5
+    a, b = golden["p70761"], golden["p70761_c"]
+    init = np.eye(4)
+    init[:3, 3] = b[:, :3].astype(np.float64).mean(0) - a[:, :3].astype(np.float64).mean(0) + 0.01
+    E[:3, 3] = golden["t70761"]
+    r = _replay_check(ctx, a, b, 30, 0.0, init=init)
+    dt, dr = O.pose_error(r["pose"], E)
+    assert dt < 1e-5 and dr < 1e-5
+
+
+def test_icp_host_entry_point(ctx, rtr):
+    src, tgt, T = rtr.config0_pair(6, 5000)
+    r = ctx.icp_host(src, tgt, 40, 0.05)
+    assert r["status"] == 0 and r["iterations"] == 40
+    dt, dr = O.pose_error(r["pose"], T)
+    assert dt < 3e-3 and dr < np.deg2rad(0.5)
+
+
+def test_icp_too_few_correspondences_keeps_pose(ctx, rtr):
+    src, _, _ = rtr.config0_pair(7, 2000)
+    far = src.copy()
+    far[:, 0] += 10.0  # 10 m away: nothing within 5 cm
+    res, _, _ = ctx.icp(_dev(src), _dev(far), 20, 0.05)
+    r = ctx.parse_icp_result(res)
+    assert r["converged"] == 0 and r["iterations"] == 1 and r["n_corr"] == 0
+    assert np.array_equal(r["pose"], np.eye(4))
+    assert np.all(np.isfinite(r["pose"]))
+
+
+def test_icp_early_stop_criteria(ctx, rtr):
+    src, tgt, _ = rtr.config0_pair(8, 5000)
+    res, _, _ = ctx.icp(_dev(src), _dev(tgt), 200, 0.05, transformation_epsilon=1e-16)
+    r = ctx.parse_icp_result(res)
+    assert 1 <= r["iterations"] < 200
+    o = O.icp(src, tgt, 200, 0.05, eps_t=1e-16)
+    dt, dr = O.pose_error(r["pose"], o["pose"])
+    assert dt < 1e-4 and dr < 1e-4

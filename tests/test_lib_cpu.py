@@ -1,0 +1,108 @@
+"""CPU tests of the C-ABI library: it loads without a GPU, exports every entry
+point the headers declare, and its host-only parts (synthetic inputs, argument
+checks) behave."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def _declared_functions():
+    names = set()
+    for h in sorted((ROOT / "include").glob("*.h")):
+        txt = h.read_text()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        txt = re.sub(r"//[^\n]*", "", txt)
+        for m in re.finditer(r"\b([A-Za-z_]\w*)\s*\(([^;{}]*)\)\s*;", txt):
+            name = m.group(1)
+            pre = txt[max(0, m.start() - 200):m.start()]
+            stmt = pre[pre.rfind(";") + 1:] if ";" in pre else pre
+            stmt = stmt[stmt.rfind("}") + 1:] if "}" in stmt else stmt
+            if "typedef" in stmt or name in ("sizeof", "defined"):
+                continue
+            names.add(name)
+    return sorted(names)
+
+
+def test_headers_declare_entry_points():
+    names = _declared_functions()
+    assert "ComputeTDFWithCuda" in names and "rtr_icp" in names and "rtr_knn1" in names
+
+
+def test_library_exports_every_declared_symbol(rtr):
+    L = C.CDLL(str(rtr.LIB_PATH))
+    missing = [n for n in _declared_functions() if not hasattr(L, n)]
+    assert not missing, f"librtr.so lacks {missing}"
+    # the Python mirror binds each of them with a signature
+    unbound = [n for n in _declared_functions() if n not in rtr.declared_symbols()]
+    assert not unbound, f"realtime_robot_gb300 has no binding for {unbound}"
+
+
+def test_status_strings(rtr):
+    L = rtr.lib()
+    assert L.rtr_status_string(0) == b"RTR_OK"
+    assert L.rtr_status_string(3) == b"RTR_ERR_TIMEOUT"
+    assert L.rtr_version().decode().count(".") == 2
+
+
+def test_synth_is_deterministic_and_on_the_chair(rtr):
+    a = rtr.synth_shape(rtr.CHAIR, 5000, 7)
+    b = rtr.synth_shape(rtr.CHAIR, 5000, 7)
+    c = rtr.synth_shape(rtr.CHAIR, 5000, 8)
+    assert np.array_equal(a, b) and not np.array_equal(a, c)
+    lo, hi = a[:, :3].min(0), a[:, :3].max(0)
+    assert np.allclose(lo, [-0.225, -0.225, 0.0], atol=1e-6)
+    assert np.allclose(hi, [0.225, 0.225, 0.93], atol=1e-6)
+    assert np.all(a[:, 3] == 0)
+
+
+def test_synth_rigid_is_a_rotation(rtr):
+    for s in range(20):
+        T = rtr.synth_rigid(s, 15.0, 0.1)
+        R = T[:3, :3]
+        assert np.allclose(R @ R.T, np.eye(3), atol=1e-12)
+        assert abs(np.linalg.det(R) - 1) < 1e-12
+        ang = np.arccos(np.clip((np.trace(R) - 1) / 2, -1, 1))
+        assert ang <= np.deg2rad(15.0) + 1e-12
+        assert np.all(np.abs(T[:3, 3]) <= 0.1)
+
+
+def test_synth_room_shape_and_instances(rtr):
+    p = rtr.room_default_params()
+    p.n_points = 20000
+    pts, shapes, poses = rtr.synth_room(11, p)
+    assert pts.shape == (20000, 4)
+    assert list(shapes).count(0) == 3 and list(shapes).count(1) == 1
+    assert pts[:, 2].min() > -0.05 and pts[:, 1].max() < 2.55
+    # camera at y = -2.5 sees everything in front of it
+    assert pts[:, 1].min() > -2.55
+
+
+def test_synth_crop_keeps_order(rtr):
+    a = rtr.synth_shape(rtr.SOFA, 3000, 1)
+    b = rtr.synth_crop(a, 0.4, 5)
+    assert 0.6 * 3000 <= len(b) <= 3000
+    # kept points appear in their original order
+    pos = {tuple(r): i for i, r in enumerate(a)}
+    order = [pos[tuple(r)] for r in b]
+    assert order == sorted(order)
+
+
+def test_context_without_gpu_fails_cleanly(rtr):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = C.c_void_p()
+    st = rtr.lib().rtr_context_create(0, C.byref(h))
+    assert st == 7  # RTR_ERR_NO_DEVICE
+    assert b"device" in rtr.lib().rtr_last_error()
+
+
+def test_compute_tdf_rejects_bad_sizes_without_touching_the_gpu(rtr):
+    g = np.zeros(27000, np.float32)
+    assert rtr.compute_tdf_with_cuda(np.zeros((1, 3), np.int32), g, 31) == 1  # cudaErrorInvalidValue
+    assert rtr.lib().ComputeTDFWithCuda(None, g.ctypes.data, 30, -1) == 1
