@@ -274,7 +274,7 @@ __global__ void __launch_bounds__(256) k_grid_gather(const float4* __restrict__ 
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     uint32_t o = order[i];
     float4 p = pts[o];
-    p.w = 0.f;
+    p.w = __int_as_float((int)o);  // original index travels with the point
     out[i] = p;
     idx[i] = (int)o;
   }
@@ -328,6 +328,12 @@ static int grid_blocks(int n) {
   if (b < 1) b = 1;
   if (b > 152 * 8) b = 152 * 8;
   return b;
+}
+
+void bbox_build(GridMeta* m, const float4* pts, int n, cudaStream_t st) {
+  k_bbox_init<<<1, 32, 0, st>>>(m);
+  k_bbox<<<grid_blocks(n), 256, 0, st>>>(pts, n, nullptr, m);
+  RTR_LAUNCHED(2);
 }
 
 void grid_build(const GridBufs& b, const float4* pts, int n_host, const int* d_n, float h_req,

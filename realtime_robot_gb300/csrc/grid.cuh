@@ -20,7 +20,7 @@ struct GridMeta {
 
 struct GridDev {
   const GridMeta* meta;  // device
-  const float4* pts;     // points sorted by cell
+  const float4* pts;     // points sorted by cell; w = original index (int bits)
   const int* idx;        // original index of each sorted point
   const uint2* cells;    // per cell {start, end}
 };
@@ -52,6 +52,8 @@ bool grid_take(Scratch& s, int n_cap, unsigned cell_cap, GridBufs* b);
 // edge grows until it fits (searches stay exact, only slower).
 void grid_build(const GridBufs& b, const float4* pts, int n_host, const int* d_n, float h_req,
                 cudaStream_t st);
+// Bounding box only (fills m->bmin / m->bmax).
+void bbox_build(GridMeta* m, const float4* pts, int n, cudaStream_t st);
 inline GridDev grid_dev(const GridBufs& b) { return GridDev{b.meta, b.pts, b.idx, b.cells}; }
 inline unsigned default_cell_cap(int n) {
   unsigned c = (unsigned)n * 8u;

@@ -19,13 +19,15 @@
 
 namespace rtr {
 
-constexpr int ICP_THREADS = 128;
+constexpr int ICP_THREADS = 256;
 constexpr int ICP_WARPS = ICP_THREADS / 32;
+constexpr int ICP_G = 8;  // lanes cooperating on one source point's 1-NN search
 constexpr int ICP_NV = 16;  // dp(3) dq(3) dp*dq^T(9) d^2(1)
 
 struct IcpDev {
   GridDev grid;
-  const float4* src;      // source sorted by target cell at the initial pose
+  const GridMeta* src_meta;  // bounding box of the source (centring)
+  const float4* src;    // source sorted by target cell at the initial pose
   const int* src_idx;     // original index of each sorted source point
   int n_src;
   int max_it;
@@ -53,14 +55,24 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(IcpDev a) {
   __shared__ float s_red[ICP_WARPS][ICP_NV][2];
   __shared__ int s_cnt[ICP_WARPS];
   __shared__ double s_sum[ICP_NV];
+  __shared__ float s_wsum[ICP_WARPS][ICP_NV][2];
+  __shared__ int s_wn[ICP_WARPS];
+  __shared__ double s_P[16], s_D[16], s_H[9];
   __shared__ long long s_n;
   __shared__ int s_last, s_stop;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int B = gridDim.x;
   const GridView g = load_view(a.grid);
+  // Centring: target terms about the target box centre c, source terms about
+  // the source box centre moved by the current pose (cp), so the FP32 products
+  // stay small even while the clouds are far apart.
   const float c[3] = {centre_of(a.grid.meta, 0), centre_of(a.grid.meta, 1), centre_of(a.grid.meta, 2)};
-  const unsigned stride = (unsigned)B * ICP_THREADS;
+  const float4 cs = make_float4(centre_of(a.src_meta, 0), centre_of(a.src_meta, 1), centre_of(a.src_meta, 2), 0.f);
+  constexpr int QPB = ICP_THREADS / ICP_G;  // source points per block per pass
+  const unsigned stride = (unsigned)B * QPB;
+  const int lg = lane & (ICP_G - 1);
+  const unsigned gmask = ((1u << ICP_G) - 1u) << (lane & ~(ICP_G - 1));
 
   for (int it = 0; it < a.max_it; ++it) {
     float T[12];
@@ -71,18 +83,20 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(IcpDev a) {
 #pragma unroll
       for (int k = 0; k < 12; ++k) T[k] = __ldcg(a.posef + k);
     }
+    const float4 cp = xform_exact(T, cs);
     KSum acc[ICP_NV];
 #pragma unroll
     for (int v = 0; v < ICP_NV; ++v) acc[v].init();
     int cnt = 0;
-    for (unsigned i = blockIdx.x * ICP_THREADS + tid; i < (unsigned)a.n_src; i += stride) {
+    for (unsigned i = blockIdx.x * QPB + tid / ICP_G; i < (unsigned)a.n_src; i += stride) {
       const float4 p = xform_exact(T, a.src[i]);
       float d2;
       int j, pos;
-      grid_nn1(g, p, a.r2max, d2, j, pos);
+      grid_nn1_group<ICP_G>(g, p, a.r2max, lg, gmask, d2, j, pos);
+      if (lg != 0) continue;
       if (j >= 0) {
         const float4 q = g.pts[pos];
-        const float dp[3] = {__fsub_rn(p.x, c[0]), __fsub_rn(p.y, c[1]), __fsub_rn(p.z, c[2])};
+        const float dp[3] = {__fsub_rn(p.x, cp.x), __fsub_rn(p.y, cp.y), __fsub_rn(p.z, cp.z)};
         const float dq[3] = {__fsub_rn(q.x, c[0]), __fsub_rn(q.y, c[1]), __fsub_rn(q.z, c[2])};
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
@@ -137,34 +151,79 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(IcpDev a) {
     __syncthreads();
     if (s_last) {
       __threadfence();
-      for (int v = warp; v < ICP_NV; v += ICP_WARPS) {
-        double s = 0.0;
-        for (int b = lane; b < B; b += 32)
-          s += (double)__ldcg(a.partial + b * 32 + v) + (double)__ldcg(a.partial + b * 32 + 16 + v);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        if (lane == 0) s_sum[v] = s;
+      // current pose (FP64) fetched early, used after the solve
+      if (tid < 16) {
+        const double pk = it == 0 ? a.init[tid] : __ldcg(a.pose64 + tid);
+        s_P[tid] = pk;
+        if (it == 0 && a.trace_pose) a.trace_pose[tid] = pk;
       }
-      if (warp == 0) {
-        long long n = 0;
-        for (int b = lane; b < B; b += 32) n += __ldcg(a.pcount + b);
+      // Cross-block reduction.  GB300 issues one FP64 warp-instruction per ~16
+      // SM cycles, so the tree runs on compensated FP32 pairs (TwoSum, ~48-bit
+      // significand) and FP64 closes it: one (double)hi + (double)lo per value.
+      float hs[ICP_NV], ls[ICP_NV];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) n += __shfl_down_sync(0xffffffffu, n, o);
-        if (lane == 0) s_n = n;
+      for (int k = 0; k < ICP_NV; ++k) hs[k] = ls[k] = 0.f;
+      int nloc = 0;
+      for (int b = tid; b < B; b += ICP_THREADS) {
+        const float4* pb = reinterpret_cast<const float4*>(a.partial + b * 32);
+        float4 h4[4], l4[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          h4[k] = __ldcg(pb + k);
+          l4[k] = __ldcg(pb + 4 + k);
+        }
+        nloc += __ldcg(a.pcount + b);
+        const float* hv = reinterpret_cast<const float*>(h4);
+        const float* lv = reinterpret_cast<const float*>(l4);
+#pragma unroll
+        for (int k = 0; k < ICP_NV; ++k) {
+          float t, e;
+          two_sum(hs[k], hv[k], t, e);
+          hs[k] = t;
+          ls[k] = __fadd_rn(__fadd_rn(ls[k], lv[k]), e);
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < ICP_NV; ++k) warp_ksum(hs[k], ls[k]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) nloc += __shfl_down_sync(0xffffffffu, nloc, o);
+      if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < ICP_NV; ++k) {
+          s_wsum[warp][k][0] = hs[k];
+          s_wsum[warp][k][1] = ls[k];
+        }
+        s_wn[warp] = nloc;
+      }
+      __syncthreads();
+      if (tid < ICP_NV) {
+        float s = s_wsum[0][tid][0], c = s_wsum[0][tid][1];
+        for (int w = 1; w < ICP_WARPS; ++w) {
+          float t, e;
+          two_sum(s, s_wsum[w][tid][0], t, e);
+          s = t;
+          c = __fadd_rn(__fadd_rn(c, s_wsum[w][tid][1]), e);
+        }
+        s_sum[tid] = (double)s + (double)c;
+      } else if (tid == 32) {
+        long long n = 0;
+        for (int w = 0; w < ICP_WARPS; ++w) n += s_wn[w];
+        s_n = n;
+      }
+      __syncthreads();
+      // centred cross-covariance, one element per lane
+      if (tid < 9 && s_n >= 3) {
+        const double inv = 1.0 / (double)s_n;
+        const int r = tid / 3, k = tid % 3;
+        s_H[tid] = s_sum[6 + tid] - (double)s_n * (s_sum[r] * inv) * (s_sum[3 + k] * inv);
       }
       __syncthreads();
       if (tid == 0) {
-        double P[16];
-        if (it == 0) {
-          for (int k = 0; k < 16; ++k) P[k] = a.init[k];
-          if (a.trace_pose)
-            for (int k = 0; k < 16; ++k) a.trace_pose[k] = P[k];
-        } else {
-          for (int k = 0; k < 16; ++k) P[k] = a.pose64[k];
-        }
         const long long n = s_n;
         int stop = 0, converged = 1;
         double fitness = 0.0;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) s_D[k] = (k % 5 == 0) ? 1.0 : 0.0;
         if (n < 3) {
           stop = 1;
           converged = 0;
@@ -175,37 +234,49 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(IcpDev a) {
             mdp[k] = s_sum[k] * inv;
             mdq[k] = s_sum[3 + k] * inv;
           }
-          for (int r = 0; r < 3; ++r)
-            for (int k = 0; k < 3; ++k) H[r * 3 + k] = s_sum[6 + r * 3 + k] - (double)n * mdp[r] * mdq[k];
-          umeyama_rotation(H, R);
+#pragma unroll
+          for (int k = 0; k < 9; ++k) H[k] = s_H[k];
+          umeyama_rotation_fast(H, R);
           double mp[3], mq[3], t[3];
           for (int k = 0; k < 3; ++k) {
-            mp[k] = mdp[k] + (double)c[k];
+            mp[k] = mdp[k] + (double)(k == 0 ? cp.x : (k == 1 ? cp.y : cp.z));
             mq[k] = mdq[k] + (double)c[k];
           }
           for (int r = 0; r < 3; ++r) t[r] = mq[r] - (R[r * 3 + 0] * mp[0] + R[r * 3 + 1] * mp[1] + R[r * 3 + 2] * mp[2]);
-          const double D[16] = {R[0], R[1], R[2], t[0], R[3], R[4], R[5], t[1],
-                                R[6], R[7], R[8], t[2], 0.0,  0.0,  0.0,  1.0};
-          mat4_mul(D, P, P);
+#pragma unroll
+          for (int r = 0; r < 3; ++r) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) s_D[r * 4 + k] = R[r * 3 + k];
+            s_D[r * 4 + 3] = t[r];
+          }
           fitness = s_sum[15] * inv;
           const double cosang = 0.5 * (R[0] + R[4] + R[8] - 1.0);
           const double tsq = t[0] * t[0] + t[1] * t[1] + t[2] * t[2];
           if (a.eps_t > 0.0 && tsq < a.eps_t && (a.eps_r <= 0.0 || cosang > a.eps_r)) stop = 1;
         }
         if (it + 1 >= a.max_it) stop = 1;
-        for (int k = 0; k < 16; ++k) a.pose64[k] = P[k];
-        for (int k = 0; k < 12; ++k) a.posef[k] = __double2float_rn(P[k]);
-        if (a.trace_pose)
-          for (int k = 0; k < 16; ++k) a.trace_pose[(size_t)(it + 1) * 16 + k] = P[k];
-        for (int k = 0; k < 16; ++k) a.result->pose[k] = P[k];
         a.result->fitness = fitness;
         a.result->iterations = it + 1;
         a.result->converged = converged;
         a.result->n_corr = (int)n;
         a.result->status = RTR_OK;
         s_stop = stop;
+      }
+      __syncthreads();
+      // pose <- dT * pose, one element per thread
+      if (tid < 16) {
+        const int r = tid >> 2, cidx = tid & 3;
+        const double pk = s_D[r * 4 + 0] * s_P[0 * 4 + cidx] + s_D[r * 4 + 1] * s_P[1 * 4 + cidx] +
+                          s_D[r * 4 + 2] * s_P[2 * 4 + cidx] + s_D[r * 4 + 3] * s_P[3 * 4 + cidx];
+        a.pose64[tid] = pk;
+        if (tid < 12) a.posef[tid] = __double2float_rn(pk);
+        if (a.trace_pose) a.trace_pose[(size_t)(it + 1) * 16 + tid] = pk;
+        a.result->pose[tid] = pk;
+      }
+      __syncthreads();
+      if (tid == 0) {
         __threadfence();
-        st_release_gpu(a.gen, (unsigned)(it + 1) | (stop ? 0x80000000u : 0u));
+        st_release_gpu(a.gen, (unsigned)(it + 1) | (s_stop ? 0x80000000u : 0u));
       }
       __syncthreads();
     } else {
@@ -317,7 +388,7 @@ rtr_status rtr_icp(rtr_context* ctx, const float* d_src, int n_src, const float*
 
   const unsigned cell_cap = default_cell_cap(n_tgt);
   const int maxb = icp_max_blocks(ctx);
-  int blocks = (n_src + ICP_THREADS - 1) / ICP_THREADS;
+  int blocks = (int)(((long long)n_src * ICP_G + ICP_THREADS - 1) / ICP_THREADS);
   if (blocks > maxb) blocks = maxb;
   if (blocks < 1) blocks = 1;
 
@@ -332,6 +403,7 @@ rtr_status rtr_icp(rtr_context* ctx, const float* d_src, int n_src, const float*
   plan.add<float>((size_t)blocks * 32);
   plan.add<int>(blocks);
   plan.add<unsigned>(64);
+  plan.add<GridMeta>(1);
   Scratch s;
   RTR_TRY(ensure_scratch(ctx, plan.bytes, st, &s));
   GridBufs gb;
@@ -348,6 +420,7 @@ rtr_status rtr_icp(rtr_context* ctx, const float* d_src, int n_src, const float*
   float* partial = s.take<float>((size_t)blocks * 32);
   int* pcount = s.take<int>(blocks);
   unsigned* sync = s.take<unsigned>(64);
+  GridMeta* src_meta = s.take<GridMeta>(1);
   if (!sync) return fail(RTR_ERR_CAPACITY, "rtr_icp: scratch carve");
 
   float h = params->cell_size;
@@ -360,6 +433,8 @@ rtr_status rtr_icp(rtr_context* ctx, const float* d_src, int n_src, const float*
   IcpDev a;
   memset(&a, 0, sizeof(a));
   a.grid = grid_dev(gb);
+  a.src_meta = src_meta;
+  bbox_build(src_meta, reinterpret_cast<const float4*>(d_src), n_src, st);
   a.src = src_sorted;
   a.src_idx = src_idx;
   a.n_src = n_src;

@@ -5,16 +5,24 @@
 
 namespace rtr {
 
+constexpr int KNN1_G = 8;  // lanes per query
+
 __global__ void __launch_bounds__(128) k_knn1(GridDev gd, const float4* __restrict__ q, int nq,
                                               float r2max, int* __restrict__ out_idx,
                                               float* __restrict__ out_d2) {
   const GridView g = load_view(gd);
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nq; i += gridDim.x * blockDim.x) {
+  constexpr int G = KNN1_G;
+  const int lane = threadIdx.x & 31, lg = lane & (G - 1);
+  const unsigned gmask = ((1u << G) - 1u) << (lane & ~(G - 1));
+  const int qpb = blockDim.x / G;
+  for (int i = blockIdx.x * qpb + threadIdx.x / G; i < nq; i += gridDim.x * qpb) {
     float d2;
     int bi, bp;
-    grid_nn1(g, q[i], r2max, d2, bi, bp);
-    out_idx[i] = bi;
-    if (out_d2) out_d2[i] = d2;
+    grid_nn1_group<G>(g, q[i], r2max, lg, gmask, d2, bi, bp);
+    if (lg == 0) {
+      out_idx[i] = bi;
+      if (out_d2) out_d2[i] = d2;
+    }
   }
 }
 
@@ -73,7 +81,7 @@ rtr_status rtr_knn1(rtr_context* ctx, const float* d_query, int n_query, const f
              bounded ? 0.5f * max_dist : -1.f, st);
   ProfScope ps(ctx, st, "knn1");
   RTR_LAUNCHED(1);
-  k_knn1<<<search_blocks(n_query), 128, 0, st>>>(grid_dev(gb), reinterpret_cast<const float4*>(d_query),
+  k_knn1<<<search_blocks(n_query * KNN1_G), 128, 0, st>>>(grid_dev(gb), reinterpret_cast<const float4*>(d_query),
                                                  n_query, bounded ? max_dist * max_dist : __builtin_inff(),
                                                  d_out_idx, d_out_d2);
   RTR_CUDA(cudaGetLastError());

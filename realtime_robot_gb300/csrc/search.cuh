@@ -9,6 +9,9 @@
 // farther than the current bound are skipped.  Candidates are compared as
 // (d^2, original index), so ties go to the lowest index and the result does not
 // depend on the visiting order.
+//
+// Sorted points carry their original index in the w lane (as int bits), so one
+// 16-byte load gives both the coordinates and the tie-break key.
 #pragma once
 #include <limits.h>
 
@@ -18,7 +21,6 @@ struct GridView {
   float ox, oy, oz, h, inv_h;
   int nx, ny, nz;
   const float4* __restrict__ pts;
-  const int* __restrict__ idx;
   const uint2* __restrict__ cells;
 };
 
@@ -34,10 +36,11 @@ __device__ __forceinline__ GridView load_view(const GridDev& g) {
   v.ny = m->ny;
   v.nz = m->nz;
   v.pts = g.pts;
-  v.idx = g.idx;
   v.cells = g.cells;
   return v;
 }
+
+__device__ __forceinline__ int pt_index(float4 p) { return __float_as_int(p.w); }
 
 __device__ __forceinline__ int q_cell(float v, float o, float inv_h) {
   float f = __fmul_rn(__fsub_rn(v, o), inv_h);
@@ -69,7 +72,7 @@ __device__ __forceinline__ float cell_box_dist(const GridView& g, float4 q, int 
 }
 
 // Lower bound on the distance to any point outside the ring box of radius k;
-// returns +inf when the ring box already covers the whole grid.
+// +inf when the ring box already covers the whole grid.
 __device__ __forceinline__ float ring_bound(const GridView& g, float4 q, int cx, int cy, int cz, int k) {
   float lb = __int_as_float(0x7f800000);
   if (cx - k > 0) lb = fminf(lb, q.x - (g.ox + (float)(cx - k) * g.h));
@@ -88,7 +91,7 @@ __device__ __forceinline__ bool ring_covers(const GridView& g, int cx, int cy, i
 
 // Visits every in-grid cell at Chebyshev distance exactly k from (cx, cy, cz):
 // rows on a z or y face of the ring are walked in full, the others only at
-// x = cx - k and x = cx + k.  BODY sees the cell as (x, y, z).
+// x = cx - k and x = cx + k.  The body sees the cell as (x, y, z).
 #define RTR_FOR_RING(g, cx, cy, cz, k, ...)                                         \
   {                                                                                 \
     const int z0_ = max((cz) - (k), 0), z1_ = min((cz) + (k), (g).nz - 1);            \
@@ -116,8 +119,18 @@ __device__ __forceinline__ int first_ring(const GridView& g, int cx, int cy, int
   return k;
 }
 
-// Exact 1-NN with d^2 <= r2max (r2max = +inf: unbounded).  Returns the
-// original index (or -1) and the sorted position (for reading the point).
+__device__ __forceinline__ void nn_take(float4 p, unsigned j, float4 q, float& bd, int& bi, int& bpos) {
+  const float d2 = dist2_exact(q, p);
+  const int id = pt_index(p);
+  if (d2 < bd || (d2 == bd && id < bi)) {
+    bd = d2;
+    bi = id;
+    bpos = (int)j;
+  }
+}
+
+// Exact 1-NN with d^2 <= r2max (r2max = +inf: unbounded), one thread per
+// query.  Returns the original index (or -1) and the sorted position.
 __device__ __forceinline__ void grid_nn1(const GridView& g, float4 q, float r2max, float& bd, int& bi,
                                          int& bpos) {
   bd = r2max;
@@ -129,20 +142,97 @@ __device__ __forceinline__ void grid_nn1(const GridView& g, float4 q, float r2ma
     const float margin = search_margin(g, q, k);
     RTR_FOR_RING(g, cx, cy, cz, k, {
       const uint2 c = g.cells[((unsigned)z * (unsigned)g.ny + (unsigned)y) * (unsigned)g.nx + (unsigned)x];
-      if (c.x < c.y && !beyond(cell_box_dist(g, q, x, y, z), margin, bd)) {
-        for (unsigned j = c.x; j < c.y; ++j) {
-          const float d2 = dist2_exact(q, g.pts[j]);
-          if (d2 <= bd) {
-            const int id = g.idx[j];
-            if (d2 < bd || id < bi) {
-              bd = d2;
-              bi = id;
-              bpos = (int)j;
+      if (c.x < c.y && !beyond(cell_box_dist(g, q, x, y, z), margin, bd))
+        for (unsigned j = c.x; j < c.y; ++j) nn_take(g.pts[j], j, q, bd, bi, bpos);
+    })
+    if (ring_covers(g, cx, cy, cz, k)) break;
+    if (beyond(ring_bound(g, q, cx, cy, cz, k), margin, bd)) break;
+  }
+  if (bi == INT_MAX) {
+    bi = -1;
+    bpos = -1;
+    bd = __int_as_float(0x7f800000);
+  }
+}
+
+// Group reduction of (bd, bi, bpos) over the G lanes in gmask.
+template <int G>
+__device__ __forceinline__ void group_best(unsigned gmask, float& bd, int& bi, int& bpos) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) {
+    const float od = __shfl_xor_sync(gmask, bd, o);
+    const int oi = __shfl_xor_sync(gmask, bi, o);
+    const int op = __shfl_xor_sync(gmask, bpos, o);
+    if (od < bd || (od == bd && oi < bi)) {
+      bd = od;
+      bi = oi;
+      bpos = op;
+    }
+  }
+}
+
+// Same search with G lanes per query (G a power of two <= 32; the lanes of a
+// group are contiguous and aligned).  A ring is walked as the (2k+1)^3 cube in
+// chunks of 4G entries: each lane fetches four cell entries at once (interior
+// and out-of-grid entries are dropped), the group ballots the surviving
+// candidate cells and then scans each one's points with all G lanes.  After
+// every ring the group agrees on the best (d^2, index), so the ring loop is
+// uniform inside the group.  A lane skips a cell only when the cell is beyond
+// its own best, which is never better than the group's.
+template <int G>
+__device__ __forceinline__ void grid_nn1_group(const GridView& g, float4 q, float r2max, int lg,
+                                               unsigned gmask, float& bd, int& bi, int& bpos) {
+  bd = r2max;
+  bi = INT_MAX;
+  bpos = -1;
+  const int cx = q_cell(q.x, g.ox, g.inv_h), cy = q_cell(q.y, g.oy, g.inv_h),
+            cz = q_cell(q.z, g.oz, g.inv_h);
+  const int gbase = (threadIdx.x & 31) & ~(G - 1);
+  for (int k = first_ring(g, cx, cy, cz);; ++k) {
+    const float margin = search_margin(g, q, k);
+    // the ring's cube clamped to the grid
+    const int x0 = max(cx - k, 0), y0 = max(cy - k, 0), z0 = max(cz - k, 0);
+    const int ex = min(cx + k, g.nx - 1) - x0 + 1, ey = min(cy + k, g.ny - 1) - y0 + 1,
+              ez = min(cz + k, g.nz - 1) - z0 + 1;
+    const int vol = (ex > 0 && ey > 0 && ez > 0) ? ex * ey * ez : 0;
+    if (vol <= 512) {
+      for (int m0 = 0; m0 < vol; m0 += 4 * G) {
+        uint2 cc[4];
+        bool cand[4];
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+          const int m = m0 + s * G + lg;
+          cand[s] = false;
+          cc[s] = make_uint2(0u, 0u);
+          if (m < vol) {
+            const int x = x0 + m % ex, y = y0 + (m / ex) % ey, z = z0 + m / (ex * ey);
+            if (max(max(abs(x - cx), abs(y - cy)), abs(z - cz)) == k) {
+              cc[s] = g.cells[((unsigned)z * (unsigned)g.ny + (unsigned)y) * (unsigned)g.nx + (unsigned)x];
+              cand[s] = cc[s].x < cc[s].y && !beyond(cell_box_dist(g, q, x, y, z), margin, bd);
             }
           }
         }
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+          unsigned bal = __ballot_sync(gmask, cand[s]) >> gbase;
+          while (bal) {
+            const int src = __ffs(bal) - 1;
+            bal &= bal - 1;
+            const unsigned b0 = __shfl_sync(gmask, cc[s].x, gbase + src);
+            const unsigned b1 = __shfl_sync(gmask, cc[s].y, gbase + src);
+            for (unsigned j = b0 + (unsigned)lg; j < b1; j += G) nn_take(g.pts[j], j, q, bd, bi, bpos);
+          }
+        }
       }
-    })
+    } else {
+      // large rings: walk only the shell, all lanes on the same cell
+      RTR_FOR_RING(g, cx, cy, cz, k, {
+        const uint2 c = g.cells[((unsigned)z * (unsigned)g.ny + (unsigned)y) * (unsigned)g.nx + (unsigned)x];
+        if (c.x < c.y && !beyond(cell_box_dist(g, q, x, y, z), margin, bd))
+          for (unsigned j = c.x + (unsigned)lg; j < c.y; j += G) nn_take(g.pts[j], j, q, bd, bi, bpos);
+      })
+    }
+    group_best<G>(gmask, bd, bi, bpos);
     if (ring_covers(g, cx, cy, cz, k)) break;
     if (beyond(ring_bound(g, q, cx, cy, cz, k), margin, bd)) break;
   }
@@ -155,6 +245,23 @@ __device__ __forceinline__ void grid_nn1(const GridView& g, float4 q, float r2ma
 
 // Exact K-NN (K compile-time), sorted by (d^2, index).  The K nearest by that
 // order are unique, so any k <= K of them form the exact k-NN.
+template <int K>
+__device__ __forceinline__ void knn_insert(float (&bd)[K], int (&bi)[K], float d2, int id) {
+  if (d2 > bd[K - 1] || (d2 == bd[K - 1] && id >= bi[K - 1])) return;
+  bd[K - 1] = d2;
+  bi[K - 1] = id;
+#pragma unroll
+  for (int s = K - 1; s > 0; --s) {
+    const bool lt = bd[s] < bd[s - 1] || (bd[s] == bd[s - 1] && bi[s] < bi[s - 1]);
+    const float da = bd[s], db = bd[s - 1];
+    const int ia = bi[s], ib = bi[s - 1];
+    bd[s] = lt ? db : da;
+    bd[s - 1] = lt ? da : db;
+    bi[s] = lt ? ib : ia;
+    bi[s - 1] = lt ? ia : ib;
+  }
+}
+
 template <int K>
 __device__ __forceinline__ void grid_knn(const GridView& g, float4 q, float (&bd)[K], int (&bi)[K]) {
 #pragma unroll
@@ -170,22 +277,8 @@ __device__ __forceinline__ void grid_knn(const GridView& g, float4 q, float (&bd
       const uint2 c = g.cells[((unsigned)z * (unsigned)g.ny + (unsigned)y) * (unsigned)g.nx + (unsigned)x];
       if (c.x < c.y && !beyond(cell_box_dist(g, q, x, y, z), margin, bd[K - 1])) {
         for (unsigned j = c.x; j < c.y; ++j) {
-          const float d2 = dist2_exact(q, g.pts[j]);
-          if (d2 > bd[K - 1]) continue;
-          const int id = g.idx[j];
-          if (d2 == bd[K - 1] && id >= bi[K - 1]) continue;
-          bd[K - 1] = d2;
-          bi[K - 1] = id;
-#pragma unroll
-          for (int s = K - 1; s > 0; --s) {
-            const bool lt = bd[s] < bd[s - 1] || (bd[s] == bd[s - 1] && bi[s] < bi[s - 1]);
-            const float da = bd[s], db = bd[s - 1];
-            const int ia = bi[s], ib = bi[s - 1];
-            bd[s] = lt ? db : da;
-            bd[s - 1] = lt ? da : db;
-            bi[s] = lt ? ib : ia;
-            bi[s - 1] = lt ? ia : ib;
-          }
+          const float4 p = g.pts[j];
+          knn_insert<K>(bd, bi, dist2_exact(q, p), pt_index(p));
         }
       }
     })
