@@ -175,6 +175,59 @@ rtr_status rtr_icp_host(rtr_context* ctx, const float* h_src, int n_src,
                         const float* h_tgt, int n_tgt, const rtr_icp_params* params,
                         const double* h_init_pose, rtr_icp_result* h_result);
 
+/* ---- recognition stages --------------------------------------------------
+ * The reference computes these inside ModelPoint/ScanPoint::getKeypoint
+ * (model_point.h:99-156, scan_point.h:57-113: PCL normals + keypoints) and
+ * KeyPoint (key_point.h:112-161, 251-334: octree voxels + local descriptor).
+ * Counts written to d_count are device ints, so calls can be chained without
+ * a host round trip. */
+
+/* Voxel-grid filter (PCL VoxelGrid semantics): voxel of p = floor(p / leaf)
+ * per axis (FP32, p * (1/leaf)); one centroid per occupied voxel, in
+ * ascending voxel key (x fastest); centroid = FP32 sum of the voxel's points
+ * in ascending input index divided by the count.  d_out holds n points;
+ * *d_count = number of voxels, or -1 when the key space exceeds 2^32. */
+rtr_status rtr_voxel_downsample(rtr_context* ctx, const float* d_pts, int n, float leaf,
+                                float* d_out, int* d_count, rtr_stream_t stream);
+
+/* Uniform sampling (PCL UniformSampling): per voxel of edge `radius`, the
+ * index of the point nearest the voxel centre ((floor(p / r) + 0.5) * r),
+ * ties to the lowest index; in ascending voxel key.  d_idx holds n. */
+rtr_status rtr_uniform_sample(rtr_context* ctx, const float* d_pts, int n, float radius,
+                              int32_t* d_idx, int* d_count, rtr_stream_t stream);
+
+/* Normals (PCL NormalEstimation with k neighbours incl. the point): FP32 mean
+ * and centred covariance in kNN order, exact Jacobi eigen-solve, the smallest
+ * eigenvector flipped towards h_vp3, curvature = l0 / (l0 + l1 + l2).
+ * d_normals: n x {nx, ny, nz, curvature}.  k in {8, 10, 16}.  search_cell:
+ * grid edge hint for the kNN search (0 = automatic). */
+rtr_status rtr_normals(rtr_context* ctx, const float* d_pts, int n, int k, const float* h_vp3,
+                       float search_cell, float* d_normals, rtr_stream_t stream);
+
+/* Outward orientation for a full (360 degree) model cloud, where no single
+ * viewpoint sees every face: each normal is flipped towards the side whose
+ * cylinder (radius rc, axial distance in (gap, len]) holds fewer points. */
+rtr_status rtr_orient_normals_outward(rtr_context* ctx, const float* d_pts, float* d_normals,
+                                      int n, float rc, float gap, float len,
+                                      rtr_stream_t stream);
+
+/* SHOT-style 352-d descriptor (Tombari, Salti, Di Stefano 2010) at keypoints
+ * d_keys (indices into d_pts): 2 radial x 2 elevation x 8 azimuth volumes x
+ * 11 bins of cos(normal, z), quadrilinear interpolation, L2 normalised.
+ * Support: points within `radius` facing the keypoint's side
+ * (n_j . n_k >= -0.2).  LRF: weighted-covariance eigenvectors (x largest, z
+ * smallest), x signed by the majority rule, z by agreement with the support's
+ * oriented normals.  d_desc: nk x 352; d_lrf (optional): nk x 9 (rows x,y,z). */
+rtr_status rtr_shot352(rtr_context* ctx, const float* d_pts, const float* d_normals, int n,
+                       const int32_t* d_keys, int nk, float radius, float* d_desc,
+                       float* d_lrf, rtr_stream_t stream);
+
+/* Exact FP32 1-NN of 352-d descriptors: d^2 = sum over k in order of
+ * (a_k - b_k)^2, each op rounded separately, ties to the lowest index. */
+rtr_status rtr_match_exact(rtr_context* ctx, const float* d_query, int n_query,
+                           const float* d_db, int n_db, int32_t* d_idx, float* d_d2,
+                           rtr_stream_t stream);
+
 /* ---- synthetic inputs (host only; seeded, identical on every machine) ----- */
 
 /* Shapes: 0 = chair (seat 0.45x0.45x0.03, four legs 0.03x0.03x0.45, backrest

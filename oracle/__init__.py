@@ -36,7 +36,23 @@ _SIG = {
     "orc_icp": (None, [_P, _I, _P, _I, _I, _F, _D, _D, _P, C.POINTER(IcpOut), _P, _P]),
     "orc_icp_replay": (None, [_P, _I, _P, _I, _F, _P, _I, _P, _P, _P]),
     "orc_tdf": (None, [_P, _I, _I, _P]),
+    "orc_voxel_downsample": (_I, [_P, _I, _F, _P]),
+    "orc_normals": (None, [_P, _I, _I, _P, _P]),
+    "orc_eig3": (None, [_P, _P, _P]),
+    "orc_uniform_sample": (_I, [_P, _I, _F, _P]),
+    "orc_shot352": (None, [_P, _P, _I, _P, _I, _F, _P, _P]),
+    "orc_match": (None, [_P, _I, _P, _I, _I, _P, _P]),
+    "orc_gc_group": (_I, [_P, _P, _P, _P, _P, _I, _F, _I, _I, _P, _P, _P]),
+    "orc_orient_outward": (None, [_P, _P, _I, _F, _F, _F]),
 }
+
+
+def orient_outward(pts, nrm, rc=0.01, gap=0.005, length=1.0) -> np.ndarray:
+    pts = _f4(pts)
+    out = np.array(nrm, dtype=np.float32, copy=True, order="C")
+    lib().orc_orient_outward(pts.ctypes.data, out.ctypes.data, pts.shape[0], float(rc), float(gap),
+                             float(length))
+    return out
 
 
 def build() -> Path:
@@ -157,6 +173,76 @@ def tdf(occ, dim: int) -> np.ndarray:
     out = np.empty(dim ** 3, np.float32)
     lib().orc_tdf(occ.ctypes.data if occ.size else None, occ.shape[0], int(dim), out.ctypes.data)
     return out
+
+
+def voxel_downsample(pts, leaf: float) -> np.ndarray:
+    pts = _f4(pts)
+    out = np.empty_like(pts)
+    v = lib().orc_voxel_downsample(pts.ctypes.data, pts.shape[0], float(leaf), out.ctypes.data)
+    if v < 0:
+        raise ValueError("voxel key space exceeds 32 bits")
+    return out[:v].copy()
+
+
+def normals(pts, k: int = 10, vp=(0.0, 0.0, 0.0)) -> np.ndarray:
+    pts = _f4(pts)
+    out = np.empty_like(pts)
+    v = np.ascontiguousarray(vp, np.float32)
+    lib().orc_normals(pts.ctypes.data, pts.shape[0], int(k), v.ctypes.data, out.ctypes.data)
+    return out
+
+
+def eig3(A) -> tuple[np.ndarray, np.ndarray]:
+    A = np.ascontiguousarray(A, np.float32).reshape(9)
+    w = np.empty(3, np.float32)
+    V = np.empty(9, np.float32)
+    lib().orc_eig3(A.ctypes.data, w.ctypes.data, V.ctypes.data)
+    return w, V.reshape(3, 3)
+
+
+def uniform_sample(pts, r: float) -> np.ndarray:
+    pts = _f4(pts)
+    out = np.empty(pts.shape[0], np.int32)
+    k = lib().orc_uniform_sample(pts.ctypes.data, pts.shape[0], float(r), out.ctypes.data)
+    if k < 0:
+        raise ValueError("voxel key space exceeds 32 bits")
+    return out[:k].copy()
+
+
+def shot352(pts, nrm, keys, radius: float):
+    pts, nrm = _f4(pts), _f4(nrm)
+    keys = np.ascontiguousarray(keys, np.int32)
+    desc = np.zeros((keys.shape[0], 352), np.float32)
+    lrf = np.zeros((keys.shape[0], 9), np.float32)
+    lib().orc_shot352(pts.ctypes.data, nrm.ctypes.data, pts.shape[0], keys.ctypes.data,
+                      keys.shape[0], float(radius), desc.ctypes.data, lrf.ctypes.data)
+    return desc, lrf
+
+
+def match(q, db):
+    q = np.ascontiguousarray(q, np.float32)
+    db = np.ascontiguousarray(db, np.float32)
+    idx = np.empty(q.shape[0], np.int32)
+    d2 = np.empty(q.shape[0], np.float32)
+    lib().orc_match(q.ctypes.data, q.shape[0], db.ctypes.data, db.shape[0], q.shape[1],
+                    idx.ctypes.data, d2.ctypes.data)
+    return idx, d2
+
+
+def gc_group(model_kp, scene_kp, corr_m, corr_s, corr_d, gc_size=0.01, gc_thresh=5,
+             max_clusters=64):
+    mk, sk = _f4(model_kp), _f4(scene_kp)
+    cm = np.ascontiguousarray(corr_m, np.int32)
+    cs = np.ascontiguousarray(corr_s, np.int32)
+    cd = np.ascontiguousarray(corr_d, np.float32)
+    nc = cm.shape[0]
+    clus = np.empty(nc, np.int32)
+    poses = np.zeros((max_clusters, 16), np.float64)
+    sizes = np.zeros(max_clusters, np.int32)
+    n = lib().orc_gc_group(mk.ctypes.data, sk.ctypes.data, cm.ctypes.data, cs.ctypes.data,
+                           cd.ctypes.data, nc, float(gc_size), int(gc_thresh), max_clusters,
+                           clus.ctypes.data, poses.ctypes.data, sizes.ctypes.data)
+    return clus, poses[:n].reshape(n, 4, 4), sizes[:n]
 
 
 def pose_error(Ta, Tb) -> tuple[float, float]:

@@ -462,3 +462,504 @@ void orc_tdf(const int32_t* occ, int n_occ, int dim, float* out) {
     out[v] = best;
   }
 }
+
+/* ======================================================================== */
+/* recognition stages                                                       */
+/* ======================================================================== */
+
+typedef struct {
+  uint32_t key;
+  int32_t idx;
+} kv_t;
+
+static int kv_cmp(const void* a, const void* b) {
+  const kv_t* x = (const kv_t*)a;
+  const kv_t* y = (const kv_t*)b;
+  if (x->key != y->key) return x->key < y->key ? -1 : 1;
+  return x->idx < y->idx ? -1 : (x->idx > y->idx);
+}
+
+/* Voxel keys floor(p * inv) relative to the minimum voxel; returns the number
+ * of keys or -1 when the key space does not fit 32 bits.  kv sorted by
+ * (key, index), i.e. a stable sort by key. */
+static int voxel_keys(const float* pts, int n, float inv, kv_t* kv, int* ijk_out) {
+  int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {INT_MIN, INT_MIN, INT_MIN};
+  for (int i = 0; i < n; ++i)
+    for (int a = 0; a < 3; ++a) {
+      float f = pts[4 * i + a] * inv;
+      int v = (int)floorf(f);
+      ijk_out[3 * i + a] = v;
+      if (v < lo[a]) lo[a] = v;
+      if (v > hi[a]) hi[a] = v;
+    }
+  if (n == 0) return 0;
+  uint64_t d0 = (uint64_t)(hi[0] - lo[0] + 1), d1 = (uint64_t)(hi[1] - lo[1] + 1), d2 = (uint64_t)(hi[2] - lo[2] + 1);
+  if (d0 * d1 * d2 > 0xffffffffull) return -1;
+  for (int i = 0; i < n; ++i) {
+    uint32_t x = (uint32_t)(ijk_out[3 * i] - lo[0]), y = (uint32_t)(ijk_out[3 * i + 1] - lo[1]),
+             z = (uint32_t)(ijk_out[3 * i + 2] - lo[2]);
+    kv[i].key = (z * (uint32_t)d1 + y) * (uint32_t)d0 + x;
+    kv[i].idx = i;
+  }
+  qsort(kv, (size_t)n, sizeof(kv_t), kv_cmp);
+  return n;
+}
+
+int orc_voxel_downsample(const float* pts, int n, float leaf, float* out) {
+  const float inv = 1.0f / leaf;
+  kv_t* kv = (kv_t*)malloc(sizeof(kv_t) * (n > 0 ? n : 1));
+  int* ijk = (int*)malloc(sizeof(int) * 3 * (n > 0 ? n : 1));
+  if (voxel_keys(pts, n, inv, kv, ijk) < 0) {
+    free(kv);
+    free(ijk);
+    return -1;
+  }
+  int v = 0;
+  for (int s = 0; s < n;) {
+    int e = s;
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    while (e < n && kv[e].key == kv[s].key) {
+      const float* p = pts + 4 * kv[e].idx;
+      sx = sx + p[0];
+      sy = sy + p[1];
+      sz = sz + p[2];
+      ++e;
+    }
+    const float c = (float)(e - s);
+    out[4 * v] = sx / c;
+    out[4 * v + 1] = sy / c;
+    out[4 * v + 2] = sz / c;
+    out[4 * v + 3] = 0.f;
+    ++v;
+    s = e;
+  }
+  free(kv);
+  free(ijk);
+  return v;
+}
+
+/* Cyclic Jacobi for a symmetric 3x3 in FP32.  Every operation is a single
+ * rounded IEEE op (compiled without contraction); the GPU performs the same
+ * sequence, so results match bit for bit.  Eigenvalues ascending (stable),
+ * eigenvectors in the columns of V. */
+void orc_eig3(const float* A9, float* w, float* V) {
+  float a[3][3], v[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      a[i][j] = A9[i * 3 + j];
+      v[i][j] = (i == j) ? 1.f : 0.f;
+    }
+  for (int sweep = 0; sweep < 16; ++sweep) {
+    float o01 = a[0][1] * a[0][1], o02 = a[0][2] * a[0][2], o12 = a[1][2] * a[1][2];
+    float off = (o01 + o02) + o12;
+    float d0 = a[0][0] * a[0][0], d1 = a[1][1] * a[1][1], d2 = a[2][2] * a[2][2];
+    float dsum = (d0 + d1) + d2;
+    if (!(off > 1e-12f * dsum)) break;
+    for (int pq = 0; pq < 3; ++pq) {
+      const int p = pq == 2 ? 1 : 0, q = pq == 0 ? 1 : 2;
+      const float apq = a[p][q];
+      if (apq == 0.f) continue;
+      const float num = a[q][q] - a[p][p];
+      const float den = 2.f * apq;
+      const float theta = num / den;
+      const float th2 = theta * theta;
+      const float rt = sqrtf(th2 + 1.f);
+      const float at = fabsf(theta) + rt;
+      float t = 1.f / at;
+      if (theta < 0.f) t = -t;
+      const float t2 = t * t;
+      const float c = 1.f / sqrtf(t2 + 1.f);
+      const float s = t * c;
+      for (int k = 0; k < 3; ++k) {
+        const float akp = a[k][p], akq = a[k][q];
+        const float m0 = c * akp, m1 = s * akq, m2 = s * akp, m3 = c * akq;
+        a[k][p] = m0 - m1;
+        a[k][q] = m2 + m3;
+      }
+      for (int k = 0; k < 3; ++k) {
+        const float apk = a[p][k], aqk = a[q][k];
+        const float m0 = c * apk, m1 = s * aqk, m2 = s * apk, m3 = c * aqk;
+        a[p][k] = m0 - m1;
+        a[q][k] = m2 + m3;
+      }
+      for (int k = 0; k < 3; ++k) {
+        const float vkp = v[k][p], vkq = v[k][q];
+        const float m0 = c * vkp, m1 = s * vkq, m2 = s * vkp, m3 = c * vkq;
+        v[k][p] = m0 - m1;
+        v[k][q] = m2 + m3;
+      }
+    }
+  }
+  int ord[3] = {0, 1, 2};
+  /* stable ascending sort of the diagonal */
+  for (int i = 1; i < 3; ++i) {
+    int x = ord[i], j = i;
+    while (j > 0 && a[ord[j - 1]][ord[j - 1]] > a[x][x]) {
+      ord[j] = ord[j - 1];
+      --j;
+    }
+    ord[j] = x;
+  }
+  for (int j = 0; j < 3; ++j) {
+    w[j] = a[ord[j]][ord[j]];
+    for (int i = 0; i < 3; ++i) V[i * 3 + j] = v[i][ord[j]];
+  }
+}
+
+void orc_normals(const float* pts, int n, int k, const float* vp, float* out) {
+  int32_t* nb = (int32_t*)malloc(sizeof(int32_t) * (size_t)n * k + 4);
+  float* nd = (float*)malloc(sizeof(float) * (size_t)n * k + 4);
+  cgrid g;
+  cg_build(&g, pts, n, -1.0);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int i = 0; i < n; ++i) {
+    float bd[64];
+    int bi[64];
+    for (int s = 0; s < k; ++s) {
+      bd[s] = INFINITY;
+      bi[s] = INT_MAX;
+    }
+    topk T = {k, bd, bi};
+    cg_search(&g, pts + 4 * i, &T);
+    int m = 0;
+    for (int s = 0; s < k; ++s)
+      if (bi[s] != INT_MAX) ++m;
+    float mx = 0.f, my = 0.f, mz = 0.f;
+    for (int s = 0; s < m; ++s) {
+      const float* p = pts + 4 * bi[s];
+      mx = mx + p[0];
+      my = my + p[1];
+      mz = mz + p[2];
+    }
+    const float fm = (float)m;
+    mx = mx / fm;
+    my = my / fm;
+    mz = mz / fm;
+    float c00 = 0.f, c01 = 0.f, c02 = 0.f, c11 = 0.f, c12 = 0.f, c22 = 0.f;
+    for (int s = 0; s < m; ++s) {
+      const float* p = pts + 4 * bi[s];
+      const float dx = p[0] - mx, dy = p[1] - my, dz = p[2] - mz;
+      const float xx = dx * dx, xy = dx * dy, xz = dx * dz, yy = dy * dy, yz = dy * dz, zz = dz * dz;
+      c00 = c00 + xx;
+      c01 = c01 + xy;
+      c02 = c02 + xz;
+      c11 = c11 + yy;
+      c12 = c12 + yz;
+      c22 = c22 + zz;
+    }
+    const float A[9] = {c00, c01, c02, c01, c11, c12, c02, c12, c22};
+    float w[3], V[9];
+    orc_eig3(A, w, V);
+    float nx = V[0], ny = V[3], nz = V[6];
+    const float* p = pts + 4 * i;
+    const float vx = vp[0] - p[0], vy = vp[1] - p[1], vz = vp[2] - p[2];
+    const float t0 = vx * nx, t1 = vy * ny, t2 = vz * nz;
+    const float dotv = (t0 + t1) + t2;
+    if (dotv < 0.f) {
+      nx = -nx;
+      ny = -ny;
+      nz = -nz;
+    }
+    const float den = (w[0] + w[1]) + w[2];
+    out[4 * i] = nx;
+    out[4 * i + 1] = ny;
+    out[4 * i + 2] = nz;
+    out[4 * i + 3] = den != 0.f ? w[0] / den : 0.f;
+  }
+  cg_free(&g);
+  free(nb);
+  free(nd);
+}
+
+int orc_uniform_sample(const float* pts, int n, float r, int32_t* out_idx) {
+  const float inv = 1.0f / r;
+  kv_t* kv = (kv_t*)malloc(sizeof(kv_t) * (n > 0 ? n : 1));
+  int* ijk = (int*)malloc(sizeof(int) * 3 * (n > 0 ? n : 1));
+  if (voxel_keys(pts, n, inv, kv, ijk) < 0) {
+    free(kv);
+    free(ijk);
+    return -1;
+  }
+  int K = 0;
+  for (int s = 0; s < n;) {
+    int e = s, best = -1;
+    float bd = INFINITY;
+    while (e < n && kv[e].key == kv[s].key) {
+      const int i = kv[e].idx;
+      const float* p = pts + 4 * i;
+      float c[3];
+      for (int a = 0; a < 3; ++a) {
+        const float fi = (float)ijk[3 * i + a];
+        const float h = fi + 0.5f;
+        c[a] = h * r;
+      }
+      const float dx = p[0] - c[0], dy = p[1] - c[1], dz = p[2] - c[2];
+      const float xx = dx * dx, yy = dy * dy, zz = dz * dz;
+      const float d = (xx + yy) + zz;
+      if (d < bd || (d == bd && i < best)) {
+        bd = d;
+        best = i;
+      }
+      ++e;
+    }
+    out_idx[K++] = best;
+    s = e;
+  }
+  free(kv);
+  free(ijk);
+  return K;
+}
+
+/* SHOT conventions (restated from the paper):
+ *  support: points within radius R of the keypoint (d^2 <= R*R);
+ *  LRF: M = sum (R - d) (p - k)(p - k)^T, x = eigenvector of the largest
+ *  eigenvalue, z of the smallest, each flipped so that at least half of the
+ *  support has (p - k).axis >= 0, y = z cross x;
+ *  histogram: 2 radial shells (split at R/2) x 2 elevations x 8 azimuths x
+ *  11 cosine bins of n_p . z, quadrilinear interpolation (azimuth circular,
+ *  the others clamped at their ends), the keypoint itself excluded; the 352
+ *  values are L2-normalised. */
+#define SHOT_PI 3.14159265358979f
+#define SHOT_FACING (-0.2f)
+static void shot_bins(float pos, int nb, int circular, int* b0, float* w0, int* b1, float* w1) {
+  const float fl = floorf(pos);
+  int lo = (int)fl;
+  const float f = pos - fl;
+  if (circular) {
+    *b0 = ((lo % nb) + nb) % nb;
+    *b1 = (*b0 + 1) % nb;
+    *w0 = 1.f - f;
+    *w1 = f;
+    return;
+  }
+  if (lo < 0) {
+    *b0 = 0; *w0 = 1.f; *b1 = 0; *w1 = 0.f;
+  } else if (lo >= nb - 1) {
+    *b0 = nb - 1; *w0 = 1.f; *b1 = nb - 1; *w1 = 0.f;
+  } else {
+    *b0 = lo; *w0 = 1.f - f; *b1 = lo + 1; *w1 = f;
+  }
+}
+
+void orc_shot352(const float* pts, const float* normals, int n, const int32_t* keys, int nk, float R,
+                 float* desc, float* lrf_out) {
+  cgrid g;
+  cg_build(&g, pts, n, R);
+  const float R2 = R * R;
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int kk = 0; kk < nk; ++kk) {
+    const float* kp = pts + 4 * keys[kk];
+    float* D = desc + (size_t)kk * 352;
+    for (int b = 0; b < 352; ++b) D[b] = 0.f;
+    /* gather support by walking the 27 cells around the keypoint */
+    int cap = 256, cnt = 0;
+    int* sup = (int*)malloc(sizeof(int) * cap);
+    int c[3];
+    for (int a = 0; a < 3; ++a) c[a] = cg_cell(&g, kp[a], a);
+    for (int z = c[2] - 1; z <= c[2] + 1; ++z)
+      for (int y = c[1] - 1; y <= c[1] + 1; ++y)
+        for (int x = c[0] - 1; x <= c[0] + 1; ++x) {
+          if (x < 0 || y < 0 || z < 0 || x >= g.n[0] || y >= g.n[1] || z >= g.n[2]) continue;
+          const int cell = (z * g.n[1] + y) * g.n[0] + x;
+          for (int s = g.start[cell]; s < g.start[cell + 1]; ++s) {
+            const int j = g.order[s];
+            /* support: within R, and facing the keypoint's hemisphere
+             * (n_j . n_k >= SHOT_FACING), i.e. surfaces one view sees together */
+            const float* nj = normals + 4 * j;
+            const float* nkp = normals + 4 * keys[kk];
+            const float f0 = nj[0] * nkp[0], f1 = nj[1] * nkp[1], f2 = nj[2] * nkp[2];
+            const float facing = (f0 + f1) + f2;
+            if (d2f(kp, pts + 4 * j) <= R2 && facing >= SHOT_FACING) {
+              if (cnt == cap) {
+                cap *= 2;
+                sup = (int*)realloc(sup, sizeof(int) * cap);
+              }
+              sup[cnt++] = j;
+            }
+          }
+        }
+    /* ascending index order so sums are order-independent of the walk */
+    for (int i = 1; i < cnt; ++i) {
+      int x = sup[i], j = i;
+      while (j > 0 && sup[j - 1] > x) {
+        sup[j] = sup[j - 1];
+        --j;
+      }
+      sup[j] = x;
+    }
+    float m[6] = {0, 0, 0, 0, 0, 0};
+    for (int s = 0; s < cnt; ++s) {
+      const float* p = pts + 4 * sup[s];
+      const float dx = p[0] - kp[0], dy = p[1] - kp[1], dz = p[2] - kp[2];
+      const float d = sqrtf(d2f(p, kp));
+      const float w = R - d;
+      m[0] += w * dx * dx; m[1] += w * dx * dy; m[2] += w * dx * dz;
+      m[3] += w * dy * dy; m[4] += w * dy * dz; m[5] += w * dz * dz;
+    }
+    /* SHOT LRF (weighted covariance eigenvectors: x largest, z smallest).
+     * Sign of x: the majority rule of the paper.  Sign of z: agreement with
+     * the support's oriented normals, sum_j w_j (n_j . z) >= 0 — the
+     * majority rule is a coin toss on flat patches, where every point lies in
+     * the tangent plane, while oriented normals are consistent between a
+     * model and a scene. */
+    const float M[9] = {m[0], m[1], m[2], m[1], m[3], m[4], m[2], m[4], m[5]};
+    float ev[3], V[9];
+    orc_eig3(M, ev, V);
+    float X[3] = {V[2], V[5], V[8]}, Z[3] = {V[0], V[3], V[6]};
+    int px = 0, nx = 0;
+    float zn = 0.f;
+    for (int s = 0; s < cnt; ++s) {
+      const float* p = pts + 4 * sup[s];
+      const float* nv = normals + 4 * sup[s];
+      const float dx = p[0] - kp[0], dy = p[1] - kp[1], dz = p[2] - kp[2];
+      if (dx * X[0] + dy * X[1] + dz * X[2] >= 0.f) ++px; else ++nx;
+      const float w = R - sqrtf(d2f(p, kp));
+      zn += w * (nv[0] * Z[0] + nv[1] * Z[1] + nv[2] * Z[2]);
+    }
+    if (px < nx) for (int a = 0; a < 3; ++a) X[a] = -X[a];
+    if (zn < 0.f) for (int a = 0; a < 3; ++a) Z[a] = -Z[a];
+    const float Y[3] = {Z[1] * X[2] - Z[2] * X[1], Z[2] * X[0] - Z[0] * X[2], Z[0] * X[1] - Z[1] * X[0]};
+    if (lrf_out) {
+      float* L = lrf_out + (size_t)kk * 9;
+      for (int a = 0; a < 3; ++a) { L[a] = X[a]; L[3 + a] = Y[a]; L[6 + a] = Z[a]; }
+    }
+    for (int s = 0; s < cnt; ++s) {
+      const float* p = pts + 4 * sup[s];
+      const float d2 = d2f(p, kp);
+      if (!(d2 > 0.f)) continue;
+      const float dx = p[0] - kp[0], dy = p[1] - kp[1], dz = p[2] - kp[2];
+      const float lx = dx * X[0] + dy * X[1] + dz * X[2];
+      const float ly = dx * Y[0] + dy * Y[1] + dz * Y[2];
+      const float lz = dx * Z[0] + dy * Z[1] + dz * Z[2];
+      const float* nv = normals + 4 * sup[s];
+      float cs = nv[0] * Z[0] + nv[1] * Z[1] + nv[2] * Z[2];
+      cs = cs > 1.f ? 1.f : (cs < -1.f ? -1.f : cs);
+      const float d = sqrtf(d2);
+      const float az = atan2f(ly, lx);
+      const float el = atan2f(lz, sqrtf(lx * lx + ly * ly));
+      int cb0, cb1, ab0, ab1, eb0, eb1, rb0, rb1;
+      float cw0, cw1, aw0, aw1, ew0, ew1, rw0, rw1;
+      shot_bins((cs + 1.f) * 5.5f - 0.5f, 11, 0, &cb0, &cw0, &cb1, &cw1);
+      shot_bins((az + SHOT_PI) * (8.f / (2.f * SHOT_PI)) - 0.5f, 8, 1, &ab0, &aw0, &ab1, &aw1);
+      shot_bins((el + 0.5f * SHOT_PI) * (2.f / SHOT_PI) - 0.5f, 2, 0, &eb0, &ew0, &eb1, &ew1);
+      shot_bins(d / R * 2.f - 0.5f, 2, 0, &rb0, &rw0, &rb1, &rw1);
+      const int cb[2] = {cb0, cb1}, ab[2] = {ab0, ab1}, eb[2] = {eb0, eb1}, rb[2] = {rb0, rb1};
+      const float cw[2] = {cw0, cw1}, aw[2] = {aw0, aw1}, ew[2] = {ew0, ew1}, rw[2] = {rw0, rw1};
+      for (int i0 = 0; i0 < 2; ++i0)
+        for (int i1 = 0; i1 < 2; ++i1)
+          for (int i2 = 0; i2 < 2; ++i2)
+            for (int i3 = 0; i3 < 2; ++i3) {
+              const float w = rw[i0] * ew[i1] * aw[i2] * cw[i3];
+              if (w == 0.f) continue;
+              D[((rb[i0] * 2 + eb[i1]) * 8 + ab[i2]) * 11 + cb[i3]] += w;
+            }
+    }
+    float ss = 0.f;
+    for (int b = 0; b < 352; ++b) ss += D[b] * D[b];
+    if (ss > 0.f) {
+      const float inv = 1.f / sqrtf(ss);
+      for (int b = 0; b < 352; ++b) D[b] *= inv;
+    }
+    free(sup);
+  }
+  cg_free(&g);
+}
+
+void orc_match(const float* q, int nq, const float* db, int ndb, int dim, int32_t* idx, float* d2) {
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int i = 0; i < nq; ++i) {
+    const float* a = q + (size_t)i * dim;
+    float bd = INFINITY;
+    int bi = -1;
+    for (int j = 0; j < ndb; ++j) {
+      const float* b = db + (size_t)j * dim;
+      float s = 0.f;
+      for (int k = 0; k < dim; ++k) {
+        const float t = a[k] - b[k];
+        const float tt = t * t;
+        s = s + tt;
+      }
+      if (s < bd) {
+        bd = s;
+        bi = j;
+      }
+    }
+    idx[i] = bi;
+    if (d2) d2[i] = bd;
+  }
+}
+
+typedef struct {
+  float d;
+  int i;
+} dk_t;
+
+static int dk_cmp(const void* a, const void* b) {
+  const dk_t* x = (const dk_t*)a;
+  const dk_t* y = (const dk_t*)b;
+  if (x->d != y->d) return x->d < y->d ? -1 : 1;
+  return x->i < y->i ? -1 : (x->i > y->i);
+}
+
+/* Chen & Bhanu / PCL GeometricConsistencyGrouping: correspondences sorted by
+ * descriptor distance (ties: input order); each not-yet-taken one seeds a
+ * consensus set that admits, in the same order, every not-taken
+ * correspondence whose model-side and scene-side distances to EVERY member
+ * differ by at most gc_size; sets of at least gc_thresh members become
+ * clusters and their members are taken.  Pose per cluster: least squares
+ * model -> scene (FP64).  Returns the number of clusters. */
+int orc_gc_group(const float* mk, const float* sk, const int32_t* cm, const int32_t* cs, const float* cd,
+                 int nc, float gc_size, int gc_thresh, int max_clusters, int32_t* cluster_of,
+                 double* poses16, int32_t* sizes) {
+  dk_t* ord = (dk_t*)malloc(sizeof(dk_t) * (nc > 0 ? nc : 1));
+  for (int i = 0; i < nc; ++i) {
+    ord[i].d = cd[i];
+    ord[i].i = i;
+    cluster_of[i] = -1;
+  }
+  qsort(ord, (size_t)nc, sizeof(dk_t), dk_cmp);
+  char* taken = (char*)calloc((size_t)nc + 1, 1);
+  int* set = (int*)malloc(sizeof(int) * (nc > 0 ? nc : 1));
+  float* P = (float*)malloc(sizeof(float) * 4 * (nc > 0 ? nc : 1));
+  float* Q = (float*)malloc(sizeof(float) * 4 * (nc > 0 ? nc : 1));
+  int ncl = 0;
+  for (int a = 0; a < nc; ++a) {
+    const int i = ord[a].i;
+    if (taken[i]) continue;
+    int ns = 0;
+    set[ns++] = i;
+    for (int b = 0; b < nc; ++b) {
+      const int j = ord[b].i;
+      if (j == i || taken[j]) continue;
+      int ok = 1;
+      for (int s = 0; s < ns && ok; ++s) {
+        const int m = set[s];
+        const float dm = sqrtf(d2f(mk + 4 * cm[m], mk + 4 * cm[j]));
+        const float ds = sqrtf(d2f(sk + 4 * cs[m], sk + 4 * cs[j]));
+        if (fabsf(dm - ds) > gc_size) ok = 0;
+      }
+      if (ok) set[ns++] = j;
+    }
+    if (ns >= gc_thresh) {
+      for (int s = 0; s < ns; ++s) {
+        taken[set[s]] = 1;
+        cluster_of[set[s]] = ncl;
+      }
+      if (ncl < max_clusters) {
+        for (int s = 0; s < ns; ++s) {
+          memcpy(P + 4 * s, mk + 4 * cm[set[s]], 16);
+          memcpy(Q + 4 * s, sk + 4 * cs[set[s]], 16);
+        }
+        orc_rigid_fit(P, Q, NULL, ns, poses16 + 16 * ncl);
+        sizes[ncl] = ns;
+      }
+      ++ncl;
+    }
+  }
+  free(ord);
+  free(taken);
+  free(set);
+  free(P);
+  free(Q);
+  return ncl < max_clusters ? ncl : max_clusters;
+}

@@ -60,6 +60,45 @@ void orc_icp_replay(const float* src, int ns, const float* tgt, int nt, float ma
 /* ---- TDF (kernel.cu:8-31): out[v] = min(900, min_i |v - occ_i|^2) */
 void orc_tdf(const int32_t* occ, int n_occ, int dim, float* out);
 
+/* ---- voxel-grid downsample (PCL VoxelGrid, implicit in the reference's
+ * octree voxel centres, key_point.h:143-160, 287-293).  Voxel of p:
+ * floor(p * (1/leaf)) per axis in FP32; output voxels in ascending linear key
+ * (x fastest, relative to the minimum voxel); centroid = FP32 sum of the
+ * voxel's points in ascending input index, divided by the count.  Returns V
+ * (or -1 when the key space exceeds 2^32). */
+int orc_voxel_downsample(const float* pts, int n, float leaf, float* out);
+
+/* ---- normals (PCL NormalEstimation, k nearest incl. the point itself):
+ * mean of the k neighbours (FP32, kNN order), covariance of the centred
+ * neighbours, Jacobi eigen-solve (orc_eig3), normal = eigenvector of the
+ * smallest eigenvalue flipped towards vp, curvature = l_min / (l0+l1+l2).
+ * out: [n][4] = (nx, ny, nz, curvature). */
+void orc_normals(const float* pts, int n, int k, const float* vp3, float* out);
+/* Symmetric 3x3 eigen-decomposition, FP32 cyclic Jacobi with a fixed rule
+ * set shared with the GPU; eigenvalues ascending, vectors in columns. */
+void orc_eig3(const float* A9, float* w3, float* V9);
+
+/* ---- uniform sampling (PCL UniformSampling): per voxel of edge r (voxel
+ * floor(p / r)), keep the point nearest the voxel centre (ties: lowest
+ * index); indices in ascending voxel key.  Returns K. */
+int orc_uniform_sample(const float* pts, int n, float r, int32_t* out_idx);
+
+/* ---- SHOT-style 352-d descriptor (Tombari, Salti, Di Stefano 2010) with the
+ * conventions in oracle.c.  keys: indices into pts. */
+void orc_shot352(const float* pts, const float* normals, int n, const int32_t* keys, int nk,
+                 float radius, float* desc, float* lrf9);
+
+/* ---- descriptor 1-NN (FP32, sequential sum over the 352 dims). */
+void orc_match(const float* q, int nq, const float* db, int ndb, int dim, int32_t* idx, float* d2);
+
+/* ---- outward normals of a full model cloud (orient.c) */
+void orc_orient_outward(const float* pts, float* nrm, int n, float rc, float gap, float len);
+
+/* ---- geometric-consistency grouping (Chen & Bhanu 2007 / PCL GC) */
+int orc_gc_group(const float* model_kp, const float* scene_kp, const int32_t* corr_m,
+                 const int32_t* corr_s, const float* corr_d, int nc, float gc_size, int gc_thresh,
+                 int max_clusters, int32_t* cluster_of, double* poses16, int32_t* sizes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -78,6 +78,12 @@ _SIG = {
     "rtr_icp_default_params": (None, [C.POINTER(IcpParams)]),
     "rtr_icp": (_I, [_P, _P, _I, _P, _I, C.POINTER(IcpParams), _P, _P, _P, _P, _P]),
     "rtr_icp_host": (_I, [_P, _P, _I, _P, _I, C.POINTER(IcpParams), _P, C.POINTER(IcpResult)]),
+    "rtr_voxel_downsample": (_I, [_P, _P, _I, _F, _P, _P, _P]),
+    "rtr_uniform_sample": (_I, [_P, _P, _I, _F, _P, _P, _P]),
+    "rtr_normals": (_I, [_P, _P, _I, _I, _P, _F, _P, _P]),
+    "rtr_orient_normals_outward": (_I, [_P, _P, _P, _I, _F, _F, _F, _P]),
+    "rtr_shot352": (_I, [_P, _P, _P, _I, _P, _I, _F, _P, _P, _P]),
+    "rtr_match_exact": (_I, [_P, _P, _I, _P, _I, _P, _P, _P]),
     "rtr_synth_shape": (_I, [_I, _U64, _I, _P]),
     "rtr_synth_rigid": (None, [_U64, _D, _D, _P]),
     "rtr_synth_transform_noise": (None, [_P, _I, _P, _D, _U64, _P]),
@@ -243,6 +249,62 @@ class Context:
         return {"pose": np.array(r.pose[:]).reshape(4, 4), "fitness": r.fitness,
                 "iterations": r.iterations, "converged": r.converged, "n_corr": r.n_corr,
                 "status": r.status}
+
+    # -- recognition stages ---------------------------------------------------
+    def voxel_downsample(self, pts, leaf: float, stream=None):
+        import torch
+        n = pts.shape[0]
+        out = torch.empty((max(n, 1), 4), dtype=torch.float32, device=pts.device)
+        cnt = torch.zeros(1, dtype=torch.int32, device=pts.device)
+        check(lib().rtr_voxel_downsample(self.h, _ptr(pts), n, float(leaf), _ptr(out), _ptr(cnt),
+                                         _stream(stream)))
+        v = int(cnt.item())
+        if v < 0:
+            raise RtrError(1, "voxel key space exceeds 32 bits")
+        return out[:v]
+
+    def uniform_sample(self, pts, radius: float, stream=None):
+        import torch
+        n = pts.shape[0]
+        out = torch.empty(max(n, 1), dtype=torch.int32, device=pts.device)
+        cnt = torch.zeros(1, dtype=torch.int32, device=pts.device)
+        check(lib().rtr_uniform_sample(self.h, _ptr(pts), n, float(radius), _ptr(out), _ptr(cnt),
+                                       _stream(stream)))
+        k = int(cnt.item())
+        if k < 0:
+            raise RtrError(1, "voxel key space exceeds 32 bits")
+        return out[:k]
+
+    def normals(self, pts, k: int = 10, vp=(0.0, 0.0, 0.0), search_cell: float = 0.0, stream=None):
+        import torch
+        n = pts.shape[0]
+        out = torch.empty((n, 4), dtype=torch.float32, device=pts.device)
+        v = np.ascontiguousarray(vp, np.float32)
+        check(lib().rtr_normals(self.h, _ptr(pts), n, int(k), v.ctypes.data, float(search_cell),
+                                _ptr(out), _stream(stream)))
+        return out
+
+    def orient_outward(self, pts, nrm, rc=0.01, gap=0.005, length=1.0, stream=None):
+        check(lib().rtr_orient_normals_outward(self.h, _ptr(pts), _ptr(nrm), pts.shape[0], float(rc),
+                                               float(gap), float(length), _stream(stream)))
+        return nrm
+
+    def shot352(self, pts, nrm, keys, radius: float, lrf: bool = False, stream=None):
+        import torch
+        nk = keys.shape[0]
+        desc = torch.empty((nk, 352), dtype=torch.float32, device=pts.device)
+        L = torch.empty((nk, 9), dtype=torch.float32, device=pts.device) if lrf else None
+        check(lib().rtr_shot352(self.h, _ptr(pts), _ptr(nrm), pts.shape[0], _ptr(keys), nk,
+                                float(radius), _ptr(desc), _ptr(L), _stream(stream)))
+        return (desc, L) if lrf else desc
+
+    def match_exact(self, q, db, stream=None):
+        import torch
+        idx = torch.empty(q.shape[0], dtype=torch.int32, device=q.device)
+        d2 = torch.empty(q.shape[0], dtype=torch.float32, device=q.device)
+        check(lib().rtr_match_exact(self.h, _ptr(q), q.shape[0], _ptr(db), db.shape[0], _ptr(idx),
+                                    _ptr(d2), _stream(stream)))
+        return idx, d2
 
     # -- TDF ------------------------------------------------------------------
     def tdf_batch(self, occ, offsets, dim: int, stream=None):
