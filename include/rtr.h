@@ -228,6 +228,25 @@ rtr_status rtr_match_exact(rtr_context* ctx, const float* d_query, int n_query,
                            const float* d_db, int n_db, int32_t* d_idx, float* d_d2,
                            rtr_stream_t stream);
 
+/* Geometric-consistency grouping (Chen & Bhanu 2007, PCL
+ * GeometricConsistencyGrouping) — the spec form of the reference's
+ * pair-consensus loop (Ransac, function.h:35-109).  Correspondence i pairs
+ * model keypoint d_corr_m[i] with scene keypoint d_corr_s[i] at descriptor
+ * distance d_corr_d[i].  Correspondences are taken in ascending distance
+ * (ties: input order); each not-yet-taken one seeds a set that admits, in the
+ * same order, every not-taken correspondence whose model-side and scene-side
+ * distances to every member differ by at most gc_size; a set with at least
+ * gc_thresh members becomes a cluster and its members are taken.  Outputs, for
+ * the first max_clusters clusters: members (original correspondence indices,
+ * max_members per row, -1 padded), sizes, and the least-squares model->scene
+ * pose (row-major 4x4, FP64).  Synchronises (the commit walk is host-driven).
+ * Consensus sets longer than 128 members return RTR_ERR_CAPACITY. */
+rtr_status rtr_gc_group(rtr_context* ctx, const float* d_model_kp, const float* d_scene_kp,
+                        const int32_t* d_corr_m, const int32_t* d_corr_s, const float* d_corr_d,
+                        int n_corr, float gc_size, int gc_thresh, int max_clusters,
+                        int max_members, int32_t* d_members, int32_t* d_sizes,
+                        double* d_poses, int* h_n_clusters, rtr_stream_t stream);
+
 /* ---- synthetic inputs (host only; seeded, identical on every machine) ----- */
 
 /* Shapes: 0 = chair (seat 0.45x0.45x0.03, four legs 0.03x0.03x0.45, backrest

@@ -84,6 +84,8 @@ _SIG = {
     "rtr_orient_normals_outward": (_I, [_P, _P, _P, _I, _F, _F, _F, _P]),
     "rtr_shot352": (_I, [_P, _P, _P, _I, _P, _I, _F, _P, _P, _P]),
     "rtr_match_exact": (_I, [_P, _P, _I, _P, _I, _P, _P, _P]),
+    "rtr_gc_group": (_I, [_P, _P, _P, _P, _P, _P, _I, _F, _I, _I, _I, _P, _P, _P,
+                          C.POINTER(C.c_int), _P]),
     "rtr_synth_shape": (_I, [_I, _U64, _I, _P]),
     "rtr_synth_rigid": (None, [_U64, _D, _D, _P]),
     "rtr_synth_transform_noise": (None, [_P, _I, _P, _D, _U64, _P]),
@@ -305,6 +307,21 @@ class Context:
         check(lib().rtr_match_exact(self.h, _ptr(q), q.shape[0], _ptr(db), db.shape[0], _ptr(idx),
                                     _ptr(d2), _stream(stream)))
         return idx, d2
+
+    def gc_group(self, model_kp, scene_kp, corr_m, corr_s, corr_d, gc_size=0.01, gc_thresh=5,
+                 max_clusters=64, max_members=128, stream=None):
+        import torch
+        dev = model_kp.device
+        mem = torch.full((max_clusters, max_members), -1, dtype=torch.int32, device=dev)
+        sizes = torch.zeros(max_clusters, dtype=torch.int32, device=dev)
+        poses = torch.zeros((max_clusters, 16), dtype=torch.float64, device=dev)
+        n = C.c_int(0)
+        check(lib().rtr_gc_group(self.h, _ptr(model_kp), _ptr(scene_kp), _ptr(corr_m), _ptr(corr_s),
+                                 _ptr(corr_d), corr_m.shape[0], float(gc_size), int(gc_thresh),
+                                 int(max_clusters), int(max_members), _ptr(mem), _ptr(sizes),
+                                 _ptr(poses), C.byref(n), _stream(stream)))
+        k = n.value
+        return mem[:k], sizes[:k], poses[:k].reshape(k, 4, 4)
 
     # -- TDF ------------------------------------------------------------------
     def tdf_batch(self, occ, offsets, dim: int, stream=None):

@@ -70,6 +70,7 @@ struct rtr_context {
   void* io = nullptr;           // device staging for the host-pointer entry points
   size_t io_bytes = 0;
   cudaStream_t host_stream = nullptr;  // stream of the host-pointer entry points
+  int* h_pin = nullptr;                // 64 pinned ints for small device->host reads
   bool profiling = false;
   std::vector<rtr_prof_rec> prof;      // recorded stages (in order)
   std::vector<cudaEvent_t> event_pool; // reusable events

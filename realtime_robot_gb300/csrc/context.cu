@@ -156,6 +156,10 @@ rtr_status rtr_context_create(int device, rtr_context** out) {
     return rtr::fail(RTR_ERR_OOM, "rtr_context_create: status words");
   }
   cudaStreamCreateWithFlags(&ctx->host_stream, cudaStreamNonBlocking);
+  if (cudaMallocHost(&ctx->h_pin, 64 * sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    ctx->h_pin = nullptr;
+  }
   cudaMemset(ctx->d_status, 0, 64 * sizeof(int));
   cudaMemset(ctx->d_sync, 0, 64 * sizeof(unsigned));
   RTR_CUDA(cudaDeviceSynchronize());
@@ -203,6 +207,7 @@ rtr_status rtr_context_destroy(rtr_context* ctx) {
   if (ctx->arena) cudaFree(ctx->arena);
   if (ctx->io) cudaFree(ctx->io);
   if (ctx->host_stream) cudaStreamDestroy(ctx->host_stream);
+  if (ctx->h_pin) cudaFreeHost(ctx->h_pin);
   if (ctx->d_status) cudaFree(ctx->d_status);
   if (ctx->d_sync) cudaFree(ctx->d_sync);
   delete ctx;
