@@ -247,6 +247,83 @@ rtr_status rtr_gc_group(rtr_context* ctx, const float* d_model_kp, const float* 
                         int max_members, int32_t* d_members, int32_t* d_sizes,
                         double* d_poses, int* h_n_clusters, rtr_stream_t stream);
 
+/* ---- recognition pipeline ------------------------------------------------
+ * The whole chain of main (RealTimeRobot.cpp:39-105) for one known object
+ * model and one scene: voxel filter -> normals -> uniform keypoints ->
+ * SHOT-352 -> 1-NN descriptor matching -> geometric-consistency grouping ->
+ * hypothesis verification (the role of Ransac, function.h:35-109: every
+ * cluster's pose is scored by the fraction of model points landing within
+ * hv_inlier_r of the scene) -> ICP refinement of the refine_top best
+ * hypotheses in one batched persistent launch -> final score (fraction of
+ * model voxels within accept_inlier_r) -> non-maximum suppression. */
+#define RTR_MAX_INSTANCES 16
+
+typedef struct rtr_recog_params {
+  float voxel_leaf;             /* 0.01 m                                        */
+  int   normal_k;               /* 10                                            */
+  float scene_keypoint_r;       /* uniform sampling of the scene, 0.02 m         */
+  float model_keypoint_r;       /* uniform sampling of the model, 0.01 m         */
+  float descriptor_r;           /* SHOT support radius, 0.04 m                   */
+  float match_max_d2;           /* keep a match when d^2 < this (0.25)           */
+  float gc_size;                /* consistency bin, 0.01 m                       */
+  int   gc_thresh;              /* minimum cluster size, 5                       */
+  int   max_clusters;           /* hypotheses kept from grouping (<= 256)        */
+  float hv_inlier_r;            /* hypothesis score radius, 0.02 m               */
+  int   hv_subsample;           /* score every hv_subsample-th model voxel (4)    */
+  int   refine_top;             /* hypotheses refined by ICP (<= 64)             */
+  int   icp_iterations;         /* 30                                            */
+  float icp_max_dist;           /* 0.02 m                                        */
+  float accept_inlier_r;        /* final score radius, 0.01 m                    */
+  float accept_score;           /* instances need at least this final score      */
+  float nms_dist;               /* refined poses closer than this are one object */
+  int   max_instances;          /* <= RTR_MAX_INSTANCES                           */
+  float viewpoint[3];           /* scene sensor origin (normal orientation)      */
+  float keypoint_min_curvature; /* curvature gate on scene keypoints (0 = off)   */
+  int   scene_outward;          /* 1: the scene is a full object segment; orient  */
+                                /* its normals outward like a model's            */
+} rtr_recog_params;
+
+typedef struct rtr_instance {
+  double pose[16];   /* model -> scene, row-major */
+  float  score;      /* final inlier fraction     */
+  int    hypothesis; /* grouping cluster index    */
+  int    cluster_size;
+  int    pad;
+} rtr_instance;
+
+typedef struct rtr_recog_result {
+  int n_instances;
+  int n_voxels;          /* scene voxels        */
+  int n_keypoints;       /* scene keypoints     */
+  int n_correspondences;
+  int n_clusters;
+  int status;            /* RTR_OK or RTR_ERR_NOT_FOUND */
+  int pad[2];
+  rtr_instance inst[RTR_MAX_INSTANCES];
+} rtr_recog_result;
+
+typedef struct rtr_model rtr_model;
+
+void rtr_recog_default_params(rtr_recog_params* p);
+/* Model preparation (the model side of main, RealTimeRobot.cpp:39-41,
+ * 62-69): voxel filter, normals oriented outward, uniform keypoints, SHOT.
+ * Device points in; the model owns its device buffers.  Synchronises. */
+rtr_status rtr_model_create(rtr_context* ctx, const float* d_pts, int n,
+                            const rtr_recog_params* p, rtr_model** out);
+rtr_status rtr_model_destroy(rtr_model* m);
+rtr_status rtr_model_info(const rtr_model* m, int* n_voxels, int* n_keypoints);
+/* Device views of the model's buffers (any output may be NULL). */
+rtr_status rtr_model_buffers(const rtr_model* m, const float** d_vox, const float** d_normals,
+                             const int32_t** d_keys, const float** d_kp, const float** d_desc);
+/* Recognise the model in a scene (device points).  d_result: device
+ * rtr_recog_result.  Synchronises once (before grouping). */
+rtr_status rtr_recognize(rtr_context* ctx, const rtr_model* model, const float* d_scene, int n,
+                         const rtr_recog_params* p, rtr_recog_result* d_result,
+                         rtr_stream_t stream);
+/* Same with a HOST scene and a HOST result (copies in and out). */
+rtr_status rtr_recognize_host(rtr_context* ctx, const rtr_model* model, const float* h_scene, int n,
+                              const rtr_recog_params* p, rtr_recog_result* h_result);
+
 /* ---- synthetic inputs (host only; seeded, identical on every machine) ----- */
 
 /* Shapes: 0 = chair (seat 0.45x0.45x0.03, four legs 0.03x0.03x0.45, backrest

@@ -51,6 +51,56 @@ class RoomParams(C.Structure):
                 ("fx", C.c_double), ("fy", C.c_double), ("cx", C.c_double), ("cy", C.c_double)]
 
 
+MAX_INSTANCES = 16
+
+
+class RecogParams(C.Structure):
+    _fields_ = [("voxel_leaf", C.c_float), ("normal_k", C.c_int), ("scene_keypoint_r", C.c_float),
+                ("model_keypoint_r", C.c_float), ("descriptor_r", C.c_float),
+                ("match_max_d2", C.c_float), ("gc_size", C.c_float), ("gc_thresh", C.c_int),
+                ("max_clusters", C.c_int), ("hv_inlier_r", C.c_float), ("hv_subsample", C.c_int),
+                ("refine_top", C.c_int), ("icp_iterations", C.c_int), ("icp_max_dist", C.c_float),
+                ("accept_inlier_r", C.c_float), ("accept_score", C.c_float), ("nms_dist", C.c_float),
+                ("max_instances", C.c_int), ("viewpoint", C.c_float * 3),
+                ("keypoint_min_curvature", C.c_float), ("scene_outward", C.c_int)]
+
+
+class Instance(C.Structure):
+    _fields_ = [("pose", C.c_double * 16), ("score", C.c_float), ("hypothesis", C.c_int),
+                ("cluster_size", C.c_int), ("pad", C.c_int)]
+
+
+class RecogResult(C.Structure):
+    _fields_ = [("n_instances", C.c_int), ("n_voxels", C.c_int), ("n_keypoints", C.c_int),
+                ("n_correspondences", C.c_int), ("n_clusters", C.c_int), ("status", C.c_int),
+                ("pad", C.c_int * 2), ("inst", Instance * MAX_INSTANCES)]
+
+
+def recog_default_params(**kw) -> RecogParams:
+    p = RecogParams()
+    lib().rtr_recog_default_params(C.byref(p))
+    for k, v in kw.items():
+        if k == "viewpoint":
+            p.viewpoint[:] = list(v)
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def parse_recog_result(raw) -> dict:
+    if not isinstance(raw, (bytes, bytearray)):
+        raw = bytes(raw.cpu().numpy().tobytes())
+    r = RecogResult.from_buffer_copy(raw[: C.sizeof(RecogResult)])
+    inst = []
+    for i in range(r.n_instances):
+        I = r.inst[i]
+        inst.append({"pose": np.array(I.pose[:]).reshape(4, 4), "score": I.score,
+                     "hypothesis": I.hypothesis, "cluster_size": I.cluster_size})
+    return {"instances": inst, "n_voxels": r.n_voxels, "n_keypoints": r.n_keypoints,
+            "n_correspondences": r.n_correspondences, "n_clusters": r.n_clusters,
+            "status": r.status}
+
+
 _P = C.c_void_p
 _I = C.c_int
 _F = C.c_float
@@ -86,6 +136,14 @@ _SIG = {
     "rtr_match_exact": (_I, [_P, _P, _I, _P, _I, _P, _P, _P]),
     "rtr_gc_group": (_I, [_P, _P, _P, _P, _P, _P, _I, _F, _I, _I, _I, _P, _P, _P,
                           C.POINTER(C.c_int), _P]),
+    "rtr_recog_default_params": (None, [C.POINTER(RecogParams)]),
+    "rtr_model_create": (_I, [_P, _P, _I, C.POINTER(RecogParams), C.POINTER(_P)]),
+    "rtr_model_destroy": (_I, [_P]),
+    "rtr_model_info": (_I, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "rtr_model_buffers": (_I, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P), C.POINTER(_P),
+                               C.POINTER(_P)]),
+    "rtr_recognize": (_I, [_P, _P, _P, _I, C.POINTER(RecogParams), _P, _P]),
+    "rtr_recognize_host": (_I, [_P, _P, _P, _I, C.POINTER(RecogParams), C.POINTER(RecogResult)]),
     "rtr_synth_shape": (_I, [_I, _U64, _I, _P]),
     "rtr_synth_rigid": (None, [_U64, _D, _D, _P]),
     "rtr_synth_transform_noise": (None, [_P, _I, _P, _D, _U64, _P]),
@@ -331,6 +389,57 @@ class Context:
         check(lib().rtr_tdf_batch(self.h, _ptr(occ), _ptr(offsets), n, dim, _ptr(out),
                                   _stream(stream)))
         return out
+
+
+class Model:
+    """A prepared object model (voxel cloud, outward normals, keypoints, SHOT)."""
+
+    def __init__(self, ctx: "Context", pts, params: RecogParams | None = None):
+        self.params = params or recog_default_params()
+        h = _P()
+        check(lib().rtr_model_create(ctx.h, _ptr(pts), pts.shape[0], C.byref(self.params),
+                                     C.byref(h)))
+        self.h = h
+        nv, nk = C.c_int(), C.c_int()
+        check(lib().rtr_model_info(self.h, C.byref(nv), C.byref(nk)))
+        self.n_voxels, self.n_keypoints = nv.value, nk.value
+
+    def buffers(self):
+        ptrs = [_P() for _ in range(5)]
+        check(lib().rtr_model_buffers(self.h, *[C.byref(p) for p in ptrs]))
+        return [p.value for p in ptrs]
+
+    def close(self):
+        if self.h:
+            lib().rtr_model_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def recognize(ctx: "Context", model: Model, scene, params: RecogParams | None = None, result=None,
+              stream=None):
+    """Run rtr_recognize on a device scene [n,4]; returns the device result
+    buffer (parse with parse_recog_result)."""
+    import torch
+    p = params or model.params
+    if result is None:
+        result = torch.zeros(C.sizeof(RecogResult), dtype=torch.uint8, device=scene.device)
+    check(lib().rtr_recognize(ctx.h, model.h, _ptr(scene), scene.shape[0], C.byref(p),
+                              _ptr(result), _stream(stream)))
+    return result
+
+
+def recognize_host(ctx: "Context", model: Model, scene: np.ndarray, params: RecogParams | None = None):
+    p = params or model.params
+    s = np.ascontiguousarray(scene, np.float32)
+    r = RecogResult()
+    check(lib().rtr_recognize_host(ctx.h, model.h, s.ctypes.data, s.shape[0], C.byref(p), C.byref(r)))
+    return parse_recog_result(bytes(r))
 
 
 def compute_tdf_with_cuda(occ: np.ndarray, grid_value: np.ndarray, dim: int) -> int:

@@ -322,24 +322,21 @@ static bool gc_take(Scratch& s, int C, int max_clusters, int max_members, GcBufs
 
 using namespace rtr;
 
-extern "C" rtr_status rtr_gc_group(rtr_context* ctx, const float* d_model_kp, const float* d_scene_kp,
-                                   const int32_t* d_corr_m, const int32_t* d_corr_s, const float* d_corr_d,
-                                   int n_corr, float gc_size, int gc_thresh, int max_clusters,
-                                   int max_members, int32_t* d_members, int32_t* d_sizes, double* d_poses,
-                                   int* h_n_clusters, rtr_stream_t stream) {
-  RTR_CHECK_ARG(ctx && n_corr >= 0 && gc_size >= 0.f && gc_thresh >= 1 && max_clusters >= 1 && h_n_clusters,
-                "rtr_gc_group: bad arguments");
-  RTR_CHECK_ARG(max_members >= 1, "rtr_gc_group: max_members must be >= 1");
-  *h_n_clusters = 0;
-  if (n_corr == 0) return RTR_OK;
-  RTR_CHECK_ARG(d_model_kp && d_scene_kp && d_corr_m && d_corr_s && d_corr_d, "rtr_gc_group: NULL input");
-  cudaStream_t st = (cudaStream_t)stream;
-  RTR_CUDA(cudaSetDevice(ctx->device));
-  const int C = n_corr;
+namespace rtr {
+
+size_t gc_scratch_bytes(int C, int max_clusters) {
   ScratchPlan plan;
   gc_plan(plan, C, max_clusters, GC_MAXS);
-  Scratch s;
-  RTR_TRY(ensure_scratch(ctx, plan.bytes, st, &s));
+  return plan.bytes;
+}
+
+rtr_status gc_group_dev(rtr_context* ctx, Scratch& s, const float* d_model_kp, const float* d_scene_kp,
+                        const int32_t* d_corr_m, const int32_t* d_corr_s, const float* d_corr_d, int n_corr,
+                        float gc_size, int gc_thresh, int max_clusters, int max_members, int32_t* d_members,
+                        int32_t* d_sizes, double* d_poses, int* h_n_clusters, cudaStream_t st) {
+  *h_n_clusters = 0;
+  if (n_corr == 0) return RTR_OK;
+  const int C = n_corr;
   GcBufs b;
   if (!gc_take(s, C, max_clusters, GC_MAXS, &b)) return fail(RTR_ERR_CAPACITY, "rtr_gc_group: scratch");
   ProfScope ps(ctx, st, "gc_group");
@@ -401,4 +398,25 @@ extern "C" rtr_status rtr_gc_group(rtr_context* ctx, const float* d_model_kp, co
   *h_n_clusters = ncl;
   RTR_CUDA(cudaGetLastError());
   return RTR_OK;
+}
+
+}  // namespace rtr
+
+extern "C" rtr_status rtr_gc_group(rtr_context* ctx, const float* d_model_kp, const float* d_scene_kp,
+                                   const int32_t* d_corr_m, const int32_t* d_corr_s, const float* d_corr_d,
+                                   int n_corr, float gc_size, int gc_thresh, int max_clusters,
+                                   int max_members, int32_t* d_members, int32_t* d_sizes, double* d_poses,
+                                   int* h_n_clusters, rtr_stream_t stream) {
+  RTR_CHECK_ARG(ctx && n_corr >= 0 && gc_size >= 0.f && gc_thresh >= 1 && max_clusters >= 1 && h_n_clusters,
+                "rtr_gc_group: bad arguments");
+  RTR_CHECK_ARG(max_members >= 1, "rtr_gc_group: max_members must be >= 1");
+  *h_n_clusters = 0;
+  if (n_corr == 0) return RTR_OK;
+  RTR_CHECK_ARG(d_model_kp && d_scene_kp && d_corr_m && d_corr_s && d_corr_d, "rtr_gc_group: NULL input");
+  cudaStream_t st = (cudaStream_t)stream;
+  RTR_CUDA(cudaSetDevice(ctx->device));
+  Scratch s;
+  RTR_TRY(ensure_scratch(ctx, gc_scratch_bytes(n_corr, max_clusters), st, &s));
+  return gc_group_dev(ctx, s, d_model_kp, d_scene_kp, d_corr_m, d_corr_s, d_corr_d, n_corr, gc_size, gc_thresh,
+                      max_clusters, max_members, d_members, d_sizes, d_poses, h_n_clusters, st);
 }

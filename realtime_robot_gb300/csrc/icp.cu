@@ -14,6 +14,7 @@
 #include <string.h>
 
 #include "grid.cuh"
+#include "icp.cuh"
 #include "pose.cuh"
 #include "search.cuh"
 
@@ -24,34 +25,18 @@ constexpr int ICP_WARPS = ICP_THREADS / 32;
 constexpr int ICP_G = 8;  // lanes cooperating on one source point's 1-NN search
 constexpr int ICP_NV = 16;  // dp(3) dq(3) dp*dq^T(9) d^2(1)
 
-struct IcpDev {
-  GridDev grid;
-  const GridMeta* src_meta;  // bounding box of the source (centring)
-  const float4* src;    // source sorted by target cell at the initial pose
-  const int* src_idx;     // original index of each sorted source point
-  int n_src;
-  int max_it;
-  float r2max;
-  double eps_t, eps_r;
-  double init[16];
-  double* pose64;         // [16]
-  float* posef;           // [12]
-  float* partial;         // [B][32]
-  int* pcount;            // [B]
-  unsigned* arrive;
-  unsigned* gen;
-  rtr_icp_result* result;
-  double* trace_pose;
-  int* trace_corr;
-  int* status;
-  long long budget;
-};
 
 __device__ __forceinline__ float centre_of(const GridMeta* m, int a) {
   return 0.5f * (ordered_to_float(m->bmin[a]) + ordered_to_float(m->bmax[a]));
 }
 
-__global__ void __launch_bounds__(ICP_THREADS) k_icp(IcpDev a) {
+// One launch serves many problems: block b works on problem blk2prob[b]
+// together with that problem's other nblk - 1 blocks; problems never wait on
+// one another.
+__global__ void __launch_bounds__(ICP_THREADS) k_icp(const IcpDev* __restrict__ probs,
+                                                     const int* __restrict__ blk2prob) {
+  const IcpDev& a = probs[blk2prob[blockIdx.x]];
+  const int lb = (int)blockIdx.x - a.blk0;
   __shared__ float s_red[ICP_WARPS][ICP_NV][2];
   __shared__ int s_cnt[ICP_WARPS];
   __shared__ double s_sum[ICP_NV];
@@ -62,7 +47,7 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(IcpDev a) {
   __shared__ int s_last, s_stop;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int B = gridDim.x;
+  const int B = a.nblk;
   const GridView g = load_view(a.grid);
   // Centring: target terms about the target box centre c, source terms about
   // the source box centre moved by the current pose (cp), so the FP32 products
@@ -88,7 +73,7 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(IcpDev a) {
 #pragma unroll
     for (int v = 0; v < ICP_NV; ++v) acc[v].init();
     int cnt = 0;
-    for (unsigned i = blockIdx.x * QPB + tid / ICP_G; i < (unsigned)a.n_src; i += stride) {
+    for (unsigned i = (unsigned)lb * QPB + tid / ICP_G; i < (unsigned)a.n_src; i += stride) {
       const float4 p = xform_exact(T, a.src[i]);
       float d2;
       int j, pos;
@@ -110,7 +95,8 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(IcpDev a) {
         acc[15].add(d2);
         ++cnt;
       }
-      if (a.trace_corr) a.trace_corr[(size_t)it * (size_t)a.n_src + (size_t)a.src_idx[i]] = j;
+      if (a.trace_corr)
+        a.trace_corr[(size_t)it * (size_t)a.n_src + (size_t)(a.src_idx ? a.src_idx[i] : (int)i)] = j;
     }
     // block partial: compensated warp sums, then across warps
 #pragma unroll
@@ -134,13 +120,13 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(IcpDev a) {
         s = t;
         cc = __fadd_rn(__fadd_rn(cc, s_red[w][tid][1]), e);
       }
-      a.partial[blockIdx.x * 32 + tid] = s;
-      a.partial[blockIdx.x * 32 + 16 + tid] = cc;
+      a.partial[lb * 32 + tid] = s;
+      a.partial[lb * 32 + 16 + tid] = cc;
     }
     if (tid == 0) {
       int tot = 0;
       for (int w = 0; w < ICP_WARPS; ++w) tot += s_cnt[w];
-      a.pcount[blockIdx.x] = tot;
+      a.pcount[lb] = tot;
     }
     __syncthreads();
     if (tid == 0) {
@@ -331,7 +317,7 @@ __global__ void __launch_bounds__(256) k_gather_pts(const float4* __restrict__ p
   }
 }
 
-static int icp_max_blocks(rtr_context* ctx) {
+int icp_max_blocks(rtr_context* ctx) {
   static int cached_dev = -1, cached = 0;
   if (cached_dev != ctx->device) {
     int per_sm = 0;
@@ -342,7 +328,7 @@ static int icp_max_blocks(rtr_context* ctx) {
   return cached;
 }
 
-static rtr_status launch_icp(rtr_context* ctx, const IcpDev& a, int blocks, cudaStream_t st) {
+static rtr_status launch_icp(const IcpDev* d_probs, const int* d_blk2prob, int blocks, cudaStream_t st) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(blocks);
   cfg.blockDim = dim3(ICP_THREADS);
@@ -353,9 +339,104 @@ static rtr_status launch_icp(rtr_context* ctx, const IcpDev& a, int blocks, cuda
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  RTR_CUDA(cudaLaunchKernelEx(&cfg, k_icp, a));
+  RTR_CUDA(cudaLaunchKernelEx(&cfg, k_icp, d_probs, d_blk2prob));
   RTR_LAUNCHED(1);
   return RTR_OK;
+}
+
+// Problem descriptors reach device memory through kernel parameters (so a
+// stream capture records them by value).  init_dev (optional) overrides the
+// parameter's initial pose with a pose already on the device.
+constexpr int ICP_SETUP_BATCH = 16;
+struct IcpSetup {
+  IcpDev p[ICP_SETUP_BATCH];
+  const double* init_dev[ICP_SETUP_BATCH];
+  int n, first;
+};
+
+__global__ void k_icp_setup(IcpSetup s, IcpDev* __restrict__ probs, int* __restrict__ blk2prob) {
+  const int k = blockIdx.x;
+  if (k >= s.n) return;
+  const int pid = s.first + k;
+  const IcpDev& a = s.p[k];
+  for (int b = threadIdx.x; b < a.nblk; b += blockDim.x) blk2prob[a.blk0 + b] = pid;
+  if (threadIdx.x == 0) {
+    IcpDev d = a;
+    if (s.init_dev[k])
+      for (int i = 0; i < 16; ++i) d.init[i] = s.init_dev[k][i];
+    probs[pid] = d;
+    d.arrive[0] = 0u;
+    d.gen[0] = 0u;
+  }
+}
+
+void icp_multi_plan(ScratchPlan& p, int n_probs, int max_blocks) {
+  p.add<IcpDev>(n_probs);
+  p.add<int>(max_blocks);
+  p.add<double>((size_t)n_probs * 16);
+  p.add<float>((size_t)n_probs * 16);
+  p.add<float>((size_t)max_blocks * 32);
+  p.add<int>(max_blocks);
+  p.add<unsigned>((size_t)n_probs * 2);
+}
+
+rtr_status icp_multi(rtr_context* ctx, Scratch& s, std::vector<IcpSpec>& specs, cudaStream_t st) {
+  const int M = (int)specs.size();
+  if (M == 0) return RTR_OK;
+  const int maxb = icp_max_blocks(ctx);
+  if (M > maxb) return fail(RTR_ERR_CAPACITY, "icp: %d problems exceed the %d co-resident blocks", M, maxb);
+  IcpDev* d_probs = s.take<IcpDev>(M);
+  int* d_b2p = s.take<int>(maxb);
+  double* pose64 = s.take<double>((size_t)M * 16);
+  float* posef = s.take<float>((size_t)M * 16);
+  float* partial = s.take<float>((size_t)maxb * 32);
+  int* pcount = s.take<int>(maxb);
+  unsigned* sync = s.take<unsigned>((size_t)M * 2);
+  if (!sync) return fail(RTR_ERR_CAPACITY, "icp: scratch carve");
+  // apportion blocks: want_i = ceil(n_i * G / threads), scaled to fit
+  long long want_total = 0;
+  std::vector<long long> want(M);
+  for (int i = 0; i < M; ++i) {
+    want[i] = ((long long)specs[i].dev.n_src * ICP_G + ICP_THREADS - 1) / ICP_THREADS;
+    if (want[i] < 1) want[i] = 1;
+    want_total += want[i];
+  }
+  std::vector<int> nblk(M);
+  int used = 0;
+  for (int i = 0; i < M; ++i) {
+    long long b = want_total <= maxb ? want[i] : (want[i] * (maxb - M)) / want_total + 1;
+    nblk[i] = (int)(b < 1 ? 1 : b);
+    used += nblk[i];
+  }
+  int blk = 0;
+  for (int i = 0; i < M; ++i) {
+    IcpDev& d = specs[i].dev;
+    d.blk0 = blk;
+    d.nblk = nblk[i];
+    d.pose64 = pose64 + 16 * i;
+    d.posef = posef + 16 * i;
+    d.partial = partial + (size_t)blk * 32;
+    d.pcount = pcount + blk;
+    d.arrive = sync + 2 * i;
+    d.gen = sync + 2 * i + 1;
+    d.status = ctx->d_status;
+    d.budget = ctx->wait_budget_cycles;
+    blk += nblk[i];
+  }
+  for (int f = 0; f < M; f += ICP_SETUP_BATCH) {
+    IcpSetup su;
+    memset(&su, 0, sizeof(su));
+    su.first = f;
+    su.n = M - f < ICP_SETUP_BATCH ? M - f : ICP_SETUP_BATCH;
+    for (int k = 0; k < su.n; ++k) {
+      su.p[k] = specs[f + k].dev;
+      su.init_dev[k] = specs[f + k].init_dev;
+    }
+    k_icp_setup<<<su.n, 128, 0, st>>>(su, d_probs, d_b2p);
+    RTR_LAUNCHED(1);
+  }
+  RTR_CUDA(cudaGetLastError());
+  return launch_icp(d_probs, d_b2p, used, st);
 }
 
 }  // namespace rtr
@@ -398,12 +479,8 @@ rtr_status rtr_icp(rtr_context* ctx, const float* d_src, int n_src, const float*
   plan.add<int>(n_src);
   for (int i = 0; i < 4; ++i) plan.add<uint32_t>(n_src);
   plan.add<uint32_t>(radix_hist_entries(n_src));
-  plan.add<double>(16);
-  plan.add<float>(16);
-  plan.add<float>((size_t)blocks * 32);
-  plan.add<int>(blocks);
-  plan.add<unsigned>(64);
   plan.add<GridMeta>(1);
+  icp_multi_plan(plan, 1, maxb);
   Scratch s;
   RTR_TRY(ensure_scratch(ctx, plan.bytes, st, &s));
   GridBufs gb;
@@ -415,13 +492,8 @@ rtr_status rtr_icp(rtr_context* ctx, const float* d_src, int n_src, const float*
   uint32_t* k1 = s.take<uint32_t>(n_src);
   uint32_t* v1 = s.take<uint32_t>(n_src);
   uint32_t* hist = s.take<uint32_t>(radix_hist_entries(n_src));
-  double* pose64 = s.take<double>(16);
-  float* posef = s.take<float>(16);
-  float* partial = s.take<float>((size_t)blocks * 32);
-  int* pcount = s.take<int>(blocks);
-  unsigned* sync = s.take<unsigned>(64);
   GridMeta* src_meta = s.take<GridMeta>(1);
-  if (!sync) return fail(RTR_ERR_CAPACITY, "rtr_icp: scratch carve");
+  if (!src_meta) return fail(RTR_ERR_CAPACITY, "rtr_icp: scratch carve");
 
   float h = params->cell_size;
   if (!(h > 0.f)) h = params->max_corr_dist > 0.f ? 0.5f * params->max_corr_dist : -1.f;
@@ -444,17 +516,9 @@ rtr_status rtr_icp(rtr_context* ctx, const float* d_src, int n_src, const float*
   a.eps_t = params->transformation_epsilon;
   a.eps_r = params->rotation_epsilon;
   for (int k = 0; k < 16; ++k) a.init[k] = h_init_pose ? h_init_pose[k] : ((k % 5) == 0 ? 1.0 : 0.0);
-  a.pose64 = pose64;
-  a.posef = posef;
-  a.partial = partial;
-  a.pcount = pcount;
-  a.arrive = sync;
-  a.gen = sync + 1;
   a.result = d_result;
   a.trace_pose = params->record_trace ? d_trace_pose : nullptr;
   a.trace_corr = params->record_trace ? d_trace_corr : nullptr;
-  a.status = ctx->d_status;
-  a.budget = ctx->wait_budget_cycles;
 
   int nb = (n_src + 255) / 256;
   if (nb > 152 * 8) nb = 152 * 8;
@@ -467,11 +531,13 @@ rtr_status rtr_icp(rtr_context* ctx, const float* d_src, int n_src, const float*
   k_gather_pts<<<nb, 256, 0, st>>>(reinterpret_cast<const float4*>(d_src), vs, n_src, src_sorted,
                                    src_idx);
   RTR_LAUNCHED(2);
-  RTR_CUDA(cudaMemsetAsync(sync, 0, 64 * sizeof(unsigned), st));
   RTR_CUDA(cudaGetLastError());
   ps_sort.end();
   ProfScope ps(ctx, st, "icp_kernel");
-  return launch_icp(ctx, a, blocks, st);
+  std::vector<IcpSpec> specs(1);
+  specs[0].dev = a;
+  specs[0].init_dev = nullptr;
+  return icp_multi(ctx, s, specs, st);
 }
 
 rtr_status rtr_icp_host(rtr_context* ctx, const float* h_src, int n_src, const float* h_tgt,

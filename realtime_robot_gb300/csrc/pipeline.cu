@@ -1,0 +1,600 @@
+// pipeline.cu — model preparation and scene recognition (the chain driven by
+// main, RealTimeRobot.cpp:39-105: model side, scene side, all-pairs
+// correspondence, consensus, transform).
+//
+// rtr_recognize: voxel filter -> normals -> uniform keypoints (optional
+// curvature gate / learned pruning) -> SHOT-352 -> 1-NN descriptor matching ->
+// geometric-consistency grouping -> hypothesis verification (model inliers in
+// the scene) -> batched ICP refinement of the best hypotheses -> final score
+// and non-maximum suppression.  Every count stays on the device except the
+// correspondence count, read once before grouping.
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "grid.cuh"
+#include "pipeline.cuh"
+#include "recog.cuh"
+#include "scan.cuh"
+#include "search.cuh"
+
+namespace rtr {
+
+rtr_status voxel_downsample_dev(rtr_context*, Scratch&, const float4*, int, const int*, float, float4*, int*, cudaStream_t);
+rtr_status uniform_sample_dev(rtr_context*, Scratch&, const float4*, int, const int*, float, int*, int*, cudaStream_t);
+rtr_status normals_dev(rtr_context*, Scratch&, const float4*, int, const int*, int, const float*, float, float4*, cudaStream_t);
+rtr_status shot_dev(rtr_context*, Scratch&, const float4*, const float4*, int, const int*, const int*, int, const int*,
+                    float, float*, float*, cudaStream_t);
+rtr_status match_exact_dev(const float*, int, const int*, const float*, int, int*, float*, cudaStream_t);
+size_t gc_scratch_bytes(int C, int max_clusters);
+__global__ void k_orient_outward(const float4* __restrict__ pts, float4* __restrict__ nrm, int n_host, const int* d_n,
+                                 float rc2, float gap, float len);
+rtr_status gc_group_dev(rtr_context* ctx, Scratch& s, const float* d_model_kp, const float* d_scene_kp,
+                        const int32_t* d_corr_m, const int32_t* d_corr_s, const float* d_corr_d, int n_corr,
+                        float gc_size, int gc_thresh, int max_clusters, int max_members, int32_t* d_members,
+                        int32_t* d_sizes, double* d_poses, int* h_n_clusters, cudaStream_t st);
+
+static int nblocks(int n, int per = 256, int cap = 152 * 16) {
+  int b = (n + per - 1) / per;
+  if (b < 1) b = 1;
+  return b > cap ? cap : b;
+}
+
+__device__ __forceinline__ int dcount(const int* d, int cap) {
+  const int v = *d;
+  return v < 0 ? 0 : (v > cap ? cap : v);
+}
+
+// keep[i] = keep keypoint i (curvature gate); writes 0/1 flags
+__global__ void k_gate_flags(const int* __restrict__ keys, const int* d_nk, int cap, const float4* __restrict__ nrm,
+                             float min_curv, uint32_t* __restrict__ flags) {
+  const int nk = dcount(d_nk, cap);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += gridDim.x * blockDim.x)
+    flags[i] = (i < nk && nrm[keys[i]].w >= min_curv) ? 1u : 0u;
+}
+
+__global__ void k_compact_int(const int* __restrict__ in, const uint32_t* __restrict__ flags,
+                              const uint32_t* __restrict__ pos, int cap, int* __restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += gridDim.x * blockDim.x)
+    if (flags[i]) out[pos[i]] = in[i];
+}
+
+// correspondences: scene keypoint slot i matched to model keypoint idx[i]
+__global__ void k_corr_flags(const int* __restrict__ idx, const float* __restrict__ d2, const int* d_nk, int cap,
+                             float max_d2, uint32_t* __restrict__ flags) {
+  const int nk = dcount(d_nk, cap);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += gridDim.x * blockDim.x)
+    flags[i] = (i < nk && idx[i] >= 0 && d2[i] < max_d2) ? 1u : 0u;
+}
+
+__global__ void k_corr_scatter(const int* __restrict__ idx, const float* __restrict__ d2,
+                               const uint32_t* __restrict__ flags, const uint32_t* __restrict__ pos, int cap,
+                               int* __restrict__ cm, int* __restrict__ cs, float* __restrict__ cd) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += gridDim.x * blockDim.x)
+    if (flags[i]) {
+      const int o = pos[i];
+      cm[o] = idx[i];
+      cs[o] = i;
+      cd[o] = d2[i];
+    }
+}
+
+__global__ void k_gather_kp(const float4* __restrict__ pts, const int* __restrict__ keys, const int* d_nk, int cap,
+                            float4* __restrict__ out) {
+  const int nk = dcount(d_nk, cap);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nk; i += gridDim.x * blockDim.x) out[i] = pts[keys[i]];
+}
+
+// Inlier count of a transformed model cloud in the scene grid: one block per
+// hypothesis, G lanes per model point (exact bounded 1-NN; found = inlier).
+constexpr int HV_G = 4;
+__global__ void __launch_bounds__(256) k_hv_score(GridDev gd, const float4* __restrict__ model, int n_model, int stride,
+                                                  const double* __restrict__ poses, int n_hyp, float r2,
+                                                  float* __restrict__ score) {
+  __shared__ int s_cnt;
+  const int h = blockIdx.x;
+  if (h >= n_hyp) return;
+  const GridView g = load_view(gd);
+  float T[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) T[k] = __double2float_rn(poses[(size_t)h * 16 + k]);
+  if (threadIdx.x == 0) s_cnt = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, lg = lane & (HV_G - 1);
+  const unsigned gmask = ((1u << HV_G) - 1u) << (lane & ~(HV_G - 1));
+  int cnt = 0;
+  const int total = (n_model + stride - 1) / stride;
+  for (int i = threadIdx.x / HV_G; i < total; i += blockDim.x / HV_G) {
+    const float4 p = xform_exact(T, model[(size_t)i * stride]);
+    float d2;
+    int bi, bp;
+    grid_nn1_group<HV_G>(g, p, r2, lg, gmask, d2, bi, bp);
+    if (lg == 0 && bi >= 0) ++cnt;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  if (lane == 0) atomicAdd(&s_cnt, cnt);
+  __syncthreads();
+  if (threadIdx.x == 0) score[h] = total > 0 ? (float)s_cnt / (float)total : 0.f;
+}
+
+// Top-m hypotheses by score (ties: lower hypothesis index) -> order[0..m)
+__global__ void k_topm(const float* __restrict__ score, int n, int m, int* __restrict__ order) {
+  if (threadIdx.x != 0) return;
+  for (int k = 0; k < m; ++k) {
+    int best = -1;
+    for (int h = 0; h < n; ++h) {
+      bool used = false;
+      for (int j = 0; j < k; ++j) used |= order[j] == h;
+      if (used) continue;
+      if (best < 0 || score[h] > score[best]) best = h;
+    }
+    order[k] = best;
+  }
+}
+
+__global__ void k_select_poses(const double* __restrict__ poses, const int* __restrict__ order, int m,
+                               double* __restrict__ out) {
+  for (int i = threadIdx.x; i < m * 16; i += blockDim.x) {
+    const int k = i / 16, e = i % 16;
+    const int h = order[k];
+    out[i] = h >= 0 ? poses[(size_t)h * 16 + e] : ((e % 5) == 0 ? 1.0 : 0.0);
+  }
+}
+
+__global__ void k_copy_result_poses(const rtr_icp_result* __restrict__ r, int m, double* __restrict__ out) {
+  for (int i = threadIdx.x; i < m * 16; i += blockDim.x) out[i] = r[i / 16].pose[i % 16];
+}
+
+// Non-maximum suppression and the result record (one thread).
+__global__ void k_finalize(const float* __restrict__ fscore, const double* __restrict__ refined,
+                           const int* __restrict__ order, const int* __restrict__ cl_sizes, int m, float accept,
+                           float nms2, int max_inst, const int* d_V, const int* d_K, const int* d_C, int ncl,
+                           rtr_recog_result* __restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int picked[RTR_MAX_INSTANCES];
+  int np = 0;
+  bool used[64];
+  for (int k = 0; k < m && k < 64; ++k) used[k] = false;
+  while (np < max_inst && np < RTR_MAX_INSTANCES) {
+    int best = -1;
+    for (int k = 0; k < m && k < 64; ++k) {
+      if (used[k] || order[k] < 0) continue;
+      if (best < 0 || fscore[k] > fscore[best]) best = k;
+    }
+    if (best < 0 || !(fscore[best] >= accept)) break;
+    used[best] = true;
+    bool dup = false;
+    for (int j = 0; j < np; ++j) {
+      const double* A = refined + (size_t)picked[j] * 16;
+      const double* B = refined + (size_t)best * 16;
+      const double dx = A[3] - B[3], dy = A[7] - B[7], dz = A[11] - B[11];
+      if (dx * dx + dy * dy + dz * dz < (double)nms2) dup = true;
+    }
+    if (dup) continue;
+    picked[np] = best;
+    rtr_instance& I = out->inst[np];
+    for (int e = 0; e < 16; ++e) I.pose[e] = refined[(size_t)best * 16 + e];
+    I.score = fscore[best];
+    I.hypothesis = order[best];
+    I.cluster_size = cl_sizes[order[best]];
+    ++np;
+  }
+  out->n_instances = np;
+  out->n_voxels = *d_V;
+  out->n_keypoints = *d_K;
+  out->n_correspondences = d_C ? *d_C : 0;
+  out->n_clusters = ncl;
+  out->status = RTR_OK;
+}
+
+__global__ void k_empty_result(rtr_recog_result* out, const int* d_V, const int* d_K, const int* d_C) {
+  if (threadIdx.x == 0) {
+    out->n_instances = 0;
+    out->n_voxels = *d_V;
+    out->n_keypoints = *d_K;
+    out->n_correspondences = d_C ? *d_C : 0;
+    out->n_clusters = 0;
+    out->status = RTR_ERR_NOT_FOUND;
+  }
+}
+
+}  // namespace rtr
+
+using namespace rtr;
+
+struct rtr_model {
+  int device = 0;
+  int n_vox = 0, n_kp = 0;
+  float4* vox = nullptr;    // voxel cloud
+  float4* nrm = nullptr;    // outward normals
+  int* keys = nullptr;      // keypoint indices into vox
+  float4* kp = nullptr;     // keypoint positions
+  float* desc = nullptr;    // [n_kp][352]
+  GridMeta* vox_meta = nullptr;  // bbox of the voxel cloud (ICP centring)
+};
+
+extern "C" {
+
+void rtr_recog_default_params(rtr_recog_params* p) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->voxel_leaf = 0.01f;
+  p->normal_k = 10;
+  p->scene_keypoint_r = 0.02f;
+  p->model_keypoint_r = 0.01f;
+  p->descriptor_r = 0.04f;
+  p->match_max_d2 = 0.25f;
+  p->gc_size = 0.01f;
+  p->gc_thresh = 5;
+  p->max_clusters = 256;
+  p->hv_inlier_r = 0.02f;
+  p->hv_subsample = 4;
+  p->refine_top = 16;
+  p->icp_iterations = 30;
+  p->icp_max_dist = 0.02f;
+  p->accept_inlier_r = 0.01f;
+  p->accept_score = 0.2f;
+  p->nms_dist = 0.1f;
+  p->max_instances = 8;
+  p->viewpoint[0] = 0.f;
+  p->viewpoint[1] = 0.f;
+  p->viewpoint[2] = 0.f;
+  p->keypoint_min_curvature = 0.f;
+}
+
+rtr_status rtr_model_create(rtr_context* ctx, const float* d_pts, int n, const rtr_recog_params* prm,
+                            rtr_model** out) {
+  RTR_CHECK_ARG(ctx && d_pts && n > 0 && prm && out, "rtr_model_create: bad arguments");
+  *out = nullptr;
+  RTR_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->host_stream;
+  rtr_model* m = new rtr_model();
+  m->device = ctx->device;
+  auto cleanup = [&](rtr_status s) {
+    rtr_model_destroy(m);
+    return s;
+  };
+  if (cudaMalloc(&m->vox, (size_t)n * 16) != cudaSuccess || cudaMalloc(&m->nrm, (size_t)n * 16) != cudaSuccess ||
+      cudaMalloc(&m->keys, (size_t)n * 4) != cudaSuccess || cudaMalloc(&m->vox_meta, sizeof(GridMeta)) != cudaSuccess) {
+    cudaGetLastError();
+    return cleanup(fail(RTR_ERR_OOM, "rtr_model_create: device buffers"));
+  }
+  ScratchPlan plan;
+  plan.add<int>(4);
+  voxseg_plan(plan, n);
+  grid_plan(plan, n, default_cell_cap(n));
+  Scratch s;
+  rtr_status r = ensure_scratch(ctx, plan.bytes, st, &s);
+  if (r != RTR_OK) return cleanup(r);
+  int* d_cnt = s.take<int>(4);  // counts first; the stages below reuse what follows
+  const float4* p4 = reinterpret_cast<const float4*>(d_pts);
+  Scratch sa = s;
+  r = voxel_downsample_dev(ctx, sa, p4, n, nullptr, prm->voxel_leaf, m->vox, d_cnt, st);
+  if (r != RTR_OK) return cleanup(r);
+  if (cudaMemcpyAsync(ctx->h_pin, d_cnt, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return cleanup(fail(RTR_ERR_CUDA, "rtr_model_create: voxel count"));
+  const int V = ctx->h_pin[0];
+  if (V <= 0) return cleanup(fail(RTR_ERR_INVALID_ARG, "rtr_model_create: voxel filter produced %d points", V));
+  m->n_vox = V;
+  const float vp[3] = {0.f, 0.f, 0.f};
+  Scratch sb = s;
+  r = normals_dev(ctx, sb, m->vox, V, nullptr, prm->normal_k, vp, 2.f * prm->voxel_leaf, m->nrm, st);
+  if (r != RTR_OK) return cleanup(r);
+  r = rtr_orient_normals_outward(ctx, reinterpret_cast<float*>(m->vox), reinterpret_cast<float*>(m->nrm), V, 0.01f,
+                                 0.005f, 1.0f, st);
+  if (r != RTR_OK) return cleanup(r);
+  Scratch sc = s;
+  r = uniform_sample_dev(ctx, sc, m->vox, V, nullptr, prm->model_keypoint_r, m->keys, d_cnt + 1, st);
+  if (r != RTR_OK) return cleanup(r);
+  if (cudaMemcpyAsync(ctx->h_pin, d_cnt + 1, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return cleanup(fail(RTR_ERR_CUDA, "rtr_model_create: keypoint count"));
+  const int K = ctx->h_pin[0];
+  if (K <= 0) return cleanup(fail(RTR_ERR_INVALID_ARG, "rtr_model_create: no keypoints"));
+  m->n_kp = K;
+  if (cudaMalloc(&m->kp, (size_t)K * 16) != cudaSuccess ||
+      cudaMalloc(&m->desc, (size_t)K * 352 * sizeof(float)) != cudaSuccess) {
+    cudaGetLastError();
+    return cleanup(fail(RTR_ERR_OOM, "rtr_model_create: descriptor buffers"));
+  }
+  Scratch sd = s;
+  r = shot_dev(ctx, sd, m->vox, m->nrm, V, nullptr, m->keys, K, nullptr, prm->descriptor_r, m->desc, nullptr, st);
+  if (r != RTR_OK) return cleanup(r);
+  k_gather_kp<<<nblocks(K), 256, 0, st>>>(m->vox, m->keys, d_cnt + 1, K, m->kp);
+  bbox_build(m->vox_meta, m->vox, V, st);
+  RTR_LAUNCHED(1);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return cleanup(fail(RTR_ERR_CUDA, "rtr_model_create: sync"));
+  *out = m;
+  return RTR_OK;
+}
+
+rtr_status rtr_model_destroy(rtr_model* m) {
+  if (!m) return RTR_OK;
+  cudaSetDevice(m->device);
+  cudaFree(m->vox);
+  cudaFree(m->nrm);
+  cudaFree(m->keys);
+  cudaFree(m->kp);
+  cudaFree(m->desc);
+  cudaFree(m->vox_meta);
+  delete m;
+  return RTR_OK;
+}
+
+rtr_status rtr_model_info(const rtr_model* m, int* n_voxels, int* n_keypoints) {
+  RTR_CHECK_ARG(m, "rtr_model_info: NULL model");
+  if (n_voxels) *n_voxels = m->n_vox;
+  if (n_keypoints) *n_keypoints = m->n_kp;
+  return RTR_OK;
+}
+
+rtr_status rtr_model_buffers(const rtr_model* m, const float** d_vox, const float** d_normals, const int32_t** d_keys,
+                             const float** d_kp, const float** d_desc) {
+  RTR_CHECK_ARG(m, "rtr_model_buffers: NULL model");
+  if (d_vox) *d_vox = reinterpret_cast<const float*>(m->vox);
+  if (d_normals) *d_normals = reinterpret_cast<const float*>(m->nrm);
+  if (d_keys) *d_keys = m->keys;
+  if (d_kp) *d_kp = reinterpret_cast<const float*>(m->kp);
+  if (d_desc) *d_desc = m->desc;
+  return RTR_OK;
+}
+
+}  // extern "C"
+
+namespace rtr {
+
+// Persistent buffers of one recognition (outlive the stages that fill them).
+struct RecogBufs {
+  int* cnt;                 // [0] V, [1] K (uniform), [2] K (gated), [3] C
+  float4 *sv, *sn, *skp;
+  int *keys, *keys2, *midx, *cm, *cs;
+  float *desc, *md2, *cd;
+  uint32_t *flags, *pos, *tiles;
+  double *poses, *init, *refined;
+  int *sizes, *order;
+  float *hv, *fscore;
+  rtr_icp_result* res;
+  GridBufs grid;
+};
+
+static void recog_persistent_plan(ScratchPlan& p, int n, const rtr_recog_params* q) {
+  const int H = q->max_clusters, M = q->refine_top;
+  p.add<int>(8);
+  p.add<float4>(n);
+  p.add<float4>(n);
+  p.add<float4>(n);
+  for (int i = 0; i < 5; ++i) p.add<int>(n);
+  p.add<float>((size_t)n * 352);
+  p.add<float>(n);
+  p.add<float>(n);
+  p.add<uint32_t>(n);
+  p.add<uint32_t>(n);
+  p.add<uint32_t>(scan_tiles(n));
+  p.add<double>((size_t)H * 16);
+  p.add<double>((size_t)M * 16);
+  p.add<double>((size_t)M * 16);
+  p.add<int>(H);
+  p.add<int>(M);
+  p.add<float>(H);
+  p.add<float>(M);
+  p.add<rtr_icp_result>(M);
+  grid_plan(p, n, default_cell_cap(n));
+}
+
+static bool recog_take(Scratch& s, int n, const rtr_recog_params* q, RecogBufs* b) {
+  const int H = q->max_clusters, M = q->refine_top;
+  b->cnt = s.take<int>(8);
+  b->sv = s.take<float4>(n);
+  b->sn = s.take<float4>(n);
+  b->skp = s.take<float4>(n);
+  b->keys = s.take<int>(n);
+  b->keys2 = s.take<int>(n);
+  b->midx = s.take<int>(n);
+  b->cm = s.take<int>(n);
+  b->cs = s.take<int>(n);
+  b->desc = s.take<float>((size_t)n * 352);
+  b->md2 = s.take<float>(n);
+  b->cd = s.take<float>(n);
+  b->flags = s.take<uint32_t>(n);
+  b->pos = s.take<uint32_t>(n);
+  b->tiles = s.take<uint32_t>(scan_tiles(n));
+  b->poses = s.take<double>((size_t)H * 16);
+  b->init = s.take<double>((size_t)M * 16);
+  b->refined = s.take<double>((size_t)M * 16);
+  b->sizes = s.take<int>(H);
+  b->order = s.take<int>(M);
+  b->hv = s.take<float>(H);
+  b->fscore = s.take<float>(M);
+  b->res = s.take<rtr_icp_result>(M);
+  return b->res && grid_take(s, n, default_cell_cap(n), &b->grid);
+}
+
+size_t recognize_scratch_bytes(int n, int n_model_vox, int n_model_kp, const rtr_recog_params* q) {
+  ScratchPlan p;
+  recog_persistent_plan(p, n, q);
+  size_t stage = 0;
+  {
+    ScratchPlan t;
+    voxseg_plan(t, n);
+    stage = t.bytes > stage ? t.bytes : stage;
+  }
+  {
+    ScratchPlan t;
+    grid_plan(t, n, default_cell_cap(n));
+    stage = t.bytes > stage ? t.bytes : stage;
+  }
+  stage = gc_scratch_bytes(n, q->max_clusters) > stage ? gc_scratch_bytes(n, q->max_clusters) : stage;
+  {
+    ScratchPlan t;
+    icp_multi_plan(t, q->refine_top, 152 * 16);
+    stage = t.bytes > stage ? t.bytes : stage;
+  }
+  (void)n_model_vox;
+  (void)n_model_kp;
+  return p.bytes + stage + 4096;
+}
+
+static rtr_status recognize_impl(rtr_context* ctx, const rtr_model* m, const float4* scene, int n,
+                                 const rtr_recog_params* q, rtr_recog_result* out, cudaStream_t st) {
+  Scratch s;
+  RTR_TRY(ensure_scratch(ctx, recognize_scratch_bytes(n, m->n_vox, m->n_kp, q), st, &s));
+  RecogBufs b;
+  if (!recog_take(s, n, q, &b)) return fail(RTR_ERR_CAPACITY, "rtr_recognize: scratch carve");
+  const Scratch stage = s;  // everything after this point is per-stage scratch
+  int* dV = b.cnt;
+  int* dK = b.cnt + 1;
+  int* dKg = b.cnt + 2;
+  int* dC = b.cnt + 3;
+  const int nb = nblocks(n);
+  {
+    ProfScope ps(ctx, st, "voxel_downsample");
+    Scratch t = stage;
+    RTR_TRY(voxel_downsample_dev(ctx, t, scene, n, nullptr, q->voxel_leaf, b.sv, dV, st));
+  }
+  {
+    ProfScope ps(ctx, st, "normals");
+    Scratch t = stage;
+    RTR_TRY(normals_dev(ctx, t, b.sv, n, dV, q->normal_k, q->viewpoint, 2.f * q->voxel_leaf, b.sn, st));
+    if (q->scene_outward) {
+      k_orient_outward<<<nblocks(n, 8, 152 * 16), 256, 0, st>>>(b.sv, b.sn, n, dV, 0.01f * 0.01f, 0.005f, 1.0f);
+      RTR_LAUNCHED(1);
+    }
+  }
+  {
+    ProfScope ps(ctx, st, "keypoints");
+    Scratch t = stage;
+    RTR_TRY(uniform_sample_dev(ctx, t, b.sv, n, dV, q->scene_keypoint_r, b.keys, dK, st));
+  }
+  const int* keys = b.keys;
+  const int* dKeys = dK;
+  if (q->keypoint_min_curvature > 0.f) {
+    ProfScope ps(ctx, st, "keypoint_gate");
+    k_gate_flags<<<nb, 256, 0, st>>>(b.keys, dK, n, b.sn, q->keypoint_min_curvature, b.flags);
+    scan_exclusive(b.flags, b.pos, b.tiles, n, n, nullptr, reinterpret_cast<uint32_t*>(dKg), st);
+    k_compact_int<<<nb, 256, 0, st>>>(b.keys, b.flags, b.pos, n, b.keys2);
+    RTR_LAUNCHED(2);
+    keys = b.keys2;
+    dKeys = dKg;
+  }
+  {
+    ProfScope ps(ctx, st, "shot352");
+    Scratch t = stage;
+    RTR_TRY(shot_dev(ctx, t, b.sv, b.sn, n, dV, keys, n, dKeys, q->descriptor_r, b.desc, nullptr, st));
+  }
+  {
+    ProfScope ps(ctx, st, "match");
+    RTR_TRY(match_exact_dev(b.desc, n, dKeys, m->desc, m->n_kp, b.midx, b.md2, st));
+  }
+  {
+    ProfScope ps(ctx, st, "correspondences");
+    k_corr_flags<<<nb, 256, 0, st>>>(b.midx, b.md2, dKeys, n, q->match_max_d2, b.flags);
+    scan_exclusive(b.flags, b.pos, b.tiles, n, n, nullptr, reinterpret_cast<uint32_t*>(dC), st);
+    k_corr_scatter<<<nb, 256, 0, st>>>(b.midx, b.md2, b.flags, b.pos, n, b.cm, b.cs, b.cd);
+    k_gather_kp<<<nb, 256, 0, st>>>(b.sv, keys, dKeys, n, b.skp);
+    RTR_LAUNCHED(3);
+  }
+  RTR_CUDA(cudaMemcpyAsync(ctx->h_pin, dC, sizeof(int), cudaMemcpyDeviceToHost, st));
+  RTR_CUDA(cudaStreamSynchronize(st));
+  const int C = ctx->h_pin[0];
+  int ncl = 0;
+  if (C > 0) {
+    ProfScope ps(ctx, st, "gc_group");
+    Scratch t = stage;
+    RTR_TRY(gc_group_dev(ctx, t, reinterpret_cast<const float*>(m->kp), reinterpret_cast<const float*>(b.skp), b.cm,
+                         b.cs, b.cd, C, q->gc_size, q->gc_thresh, q->max_clusters, 1, nullptr, b.sizes, b.poses, &ncl,
+                         st));
+  }
+  if (ncl == 0) {
+    k_empty_result<<<1, 32, 0, st>>>(out, dV, dKeys, dC);
+    RTR_LAUNCHED(1);
+    RTR_CUDA(cudaGetLastError());
+    return RTR_OK;
+  }
+  const int M = ncl < q->refine_top ? ncl : q->refine_top;
+  {
+    ProfScope ps(ctx, st, "verify");
+    grid_build(b.grid, b.sv, n, dV, q->icp_max_dist, st);
+    k_hv_score<<<ncl, 256, 0, st>>>(grid_dev(b.grid), m->vox, m->n_vox, q->hv_subsample > 0 ? q->hv_subsample : 1,
+                                    b.poses, ncl, q->hv_inlier_r * q->hv_inlier_r, b.hv);
+    k_topm<<<1, 32, 0, st>>>(b.hv, ncl, M, b.order);
+    k_select_poses<<<1, 256, 0, st>>>(b.poses, b.order, M, b.init);
+    RTR_LAUNCHED(3);
+  }
+  {
+    ProfScope ps(ctx, st, "icp_refine");
+    Scratch t = stage;
+    std::vector<IcpSpec> specs((size_t)M);
+    for (int k = 0; k < M; ++k) {
+      IcpDev& d = specs[k].dev;
+      memset(&d, 0, sizeof(d));
+      d.grid = grid_dev(b.grid);
+      d.src_meta = m->vox_meta;
+      d.src = m->vox;
+      d.src_idx = nullptr;
+      d.n_src = m->n_vox;
+      d.max_it = q->icp_iterations;
+      d.r2max = q->icp_max_dist * q->icp_max_dist;
+      d.eps_t = 0.0;
+      d.eps_r = 0.0;
+      for (int e = 0; e < 16; ++e) d.init[e] = (e % 5) == 0 ? 1.0 : 0.0;
+      d.result = b.res + k;
+      specs[k].init_dev = b.init + 16 * k;
+    }
+    RTR_TRY(icp_multi(ctx, t, specs, st));
+  }
+  {
+    ProfScope ps(ctx, st, "final_score");
+    k_copy_result_poses<<<1, 256, 0, st>>>(b.res, M, b.refined);
+    k_hv_score<<<M, 256, 0, st>>>(grid_dev(b.grid), m->vox, m->n_vox, 1, b.refined, M,
+                                  q->accept_inlier_r * q->accept_inlier_r, b.fscore);
+    const float nms2 = q->nms_dist * q->nms_dist;
+    k_finalize<<<1, 32, 0, st>>>(b.fscore, b.refined, b.order, b.sizes, M, q->accept_score, nms2,
+                                 q->max_instances, dV, dKeys, dC, ncl, out);
+    RTR_LAUNCHED(3);
+  }
+  RTR_CUDA(cudaGetLastError());
+  return RTR_OK;
+}
+
+}  // namespace rtr
+
+extern "C" {
+
+rtr_status rtr_recognize(rtr_context* ctx, const rtr_model* model, const float* d_scene, int n,
+                         const rtr_recog_params* p, rtr_recog_result* d_result, rtr_stream_t stream) {
+  RTR_CHECK_ARG(ctx && model && p && d_result && n >= 0, "rtr_recognize: bad arguments");
+  RTR_CHECK_ARG(n == 0 || d_scene, "rtr_recognize: NULL scene");
+  RTR_CHECK_ARG(p->max_clusters >= 1 && p->max_clusters <= 256 && p->refine_top >= 1 && p->refine_top <= 64 &&
+                    p->max_instances >= 1 && p->max_instances <= RTR_MAX_INSTANCES && p->voxel_leaf > 0.f &&
+                    p->descriptor_r > 0.f && p->scene_keypoint_r > 0.f && p->icp_iterations >= 1,
+                "rtr_recognize: parameter out of range");
+  RTR_CHECK_ARG(((uintptr_t)d_scene & 15) == 0, "rtr_recognize: scene must be 16-byte aligned");
+  cudaStream_t st = (cudaStream_t)stream;
+  RTR_CUDA(cudaSetDevice(ctx->device));
+  if (n == 0) {
+    RTR_CUDA(cudaMemsetAsync(d_result, 0, sizeof(rtr_recog_result), st));
+    return RTR_OK;
+  }
+  return recognize_impl(ctx, model, reinterpret_cast<const float4*>(d_scene), n, p, d_result, st);
+}
+
+rtr_status rtr_recognize_host(rtr_context* ctx, const rtr_model* model, const float* h_scene, int n,
+                              const rtr_recog_params* p, rtr_recog_result* h_result) {
+  RTR_CHECK_ARG(ctx && model && p && h_result && h_scene && n > 0, "rtr_recognize_host: bad arguments");
+  RTR_CUDA(cudaSetDevice(ctx->device));
+  const size_t bs = ((size_t)n * 16 + 255) & ~size_t(255);
+  RTR_TRY(ensure_io(ctx, bs + sizeof(rtr_recog_result) + 256));
+  char* io = static_cast<char*>(ctx->io);
+  float* d_scene = reinterpret_cast<float*>(io);
+  rtr_recog_result* d_res = reinterpret_cast<rtr_recog_result*>(io + bs);
+  cudaStream_t st = ctx->host_stream;
+  RTR_CUDA(cudaMemcpyAsync(d_scene, h_scene, (size_t)n * 16, cudaMemcpyHostToDevice, st));
+  RTR_TRY(rtr_recognize(ctx, model, d_scene, n, p, d_res, st));
+  RTR_CUDA(cudaMemcpyAsync(h_result, d_res, sizeof(rtr_recog_result), cudaMemcpyDeviceToHost, st));
+  return rtr_context_check(ctx, st);
+}
+
+}  // extern "C"

@@ -1,0 +1,65 @@
+"""End-to-end: rtr_recognize on the GPU vs the oracle pipeline.
+
+Voxel and keypoint counts must match exactly; correspondence and cluster
+counts within a few percent (SHOT is compared with a tolerance); the best
+instance within 1 cm / 1 degree of the oracle's and of the ground truth."""
+import numpy as np
+import pytest
+
+import oracle as O
+from oracle import pipeline as OP
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda()
+
+
+def _pair(R, seed):
+    model = R.synth_shape(R.CHAIR, 20000, 2024)
+    T = R.synth_rigid(100 + seed, 30.0, 0.3)
+    seg = R.synth_transform_noise(R.synth_crop(R.synth_shape(R.CHAIR, 20000, 500 + seed), 0.4, seed), T,
+                                  0.002, 9 + seed)
+    return model, seg, T
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_recognize_pair_matches_oracle(ctx, rtr, seed):
+    model, seg, T = _pair(rtr, seed)
+    prm = rtr.recog_default_params(scene_outward=1)
+    m = rtr.Model(ctx, _dev(model), prm)
+    om = OP.prepare_model(model, OP.params(scene_outward=1))
+    assert m.n_voxels == len(om["vox"]) and m.n_keypoints == len(om["keys"])
+    res = rtr.parse_recog_result(rtr.recognize(ctx, m, _dev(seg), prm))
+    ref = OP.recognize(om, seg, OP.params(scene_outward=1))
+    assert res["n_voxels"] == ref["n_voxels"]
+    assert res["n_keypoints"] == ref["n_keypoints"]
+    assert abs(res["n_correspondences"] - ref["n_correspondences"]) <= 0.03 * ref["n_correspondences"] + 3
+    assert res["instances"], res
+    g = res["instances"][0]["pose"]
+    dt, dr = O.pose_error(g, ref["instances"][0]["pose"])
+    assert dt < 0.01 and dr < np.radians(1.0), (dt, dr)
+    dt, dr = O.pose_error(g, T)
+    assert dt < 0.01 and dr < np.radians(1.0), (dt, dr)
+    m.close()
+
+
+def test_recognize_host_entry_and_empty_scene(ctx, rtr):
+    import torch
+    model, seg, T = _pair(rtr, 0)
+    prm = rtr.recog_default_params(scene_outward=1)
+    m = rtr.Model(ctx, _dev(model), prm)
+    r = rtr.recognize_host(ctx, m, seg, prm)
+    assert r["instances"] and O.pose_error(r["instances"][0]["pose"], T)[0] < 0.01
+    e = torch.zeros((0, 4), dtype=torch.float32, device="cuda")
+    r = rtr.parse_recog_result(rtr.recognize(ctx, m, e, prm))
+    assert r["n_instances"] if "n_instances" in r else len(r["instances"]) == 0
+    # a scene with nothing like the model: no instance, finite outputs
+    far = np.zeros((5000, 4), np.float32)
+    far[:, :3] = np.random.default_rng(0).uniform(-1, 1, (5000, 3))
+    r = rtr.parse_recog_result(rtr.recognize(ctx, m, _dev(far), prm))
+    for inst in r["instances"]:
+        assert np.all(np.isfinite(inst["pose"]))
+    m.close()
