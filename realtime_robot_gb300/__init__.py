@@ -134,6 +134,8 @@ _SIG = {
     "rtr_orient_normals_outward": (_I, [_P, _P, _P, _I, _F, _F, _F, _P]),
     "rtr_shot352": (_I, [_P, _P, _P, _I, _P, _I, _F, _P, _P, _P]),
     "rtr_match_exact": (_I, [_P, _P, _I, _P, _I, _P, _P, _P]),
+    "rtr_match": (_I, [_P, _P, _I, _P, _I, _P, _P, _P]),
+    "rtr_match_stats": (_I, [_P, C.POINTER(C.c_int)]),
     "rtr_gc_group": (_I, [_P, _P, _P, _P, _P, _P, _I, _F, _I, _I, _I, _P, _P, _P,
                           C.POINTER(C.c_int), _P]),
     "rtr_recog_default_params": (None, [C.POINTER(RecogParams)]),
@@ -357,6 +359,19 @@ class Context:
         check(lib().rtr_shot352(self.h, _ptr(pts), _ptr(nrm), pts.shape[0], _ptr(keys), nk,
                                 float(radius), _ptr(desc), _ptr(L), _stream(stream)))
         return (desc, L) if lrf else desc
+
+    def match(self, q, db, stream=None):
+        import torch
+        idx = torch.empty(q.shape[0], dtype=torch.int32, device=q.device)
+        d2 = torch.empty(q.shape[0], dtype=torch.float32, device=q.device)
+        check(lib().rtr_match(self.h, _ptr(q), q.shape[0], _ptr(db), db.shape[0], _ptr(idx), _ptr(d2),
+                              _stream(stream)))
+        return idx, d2
+
+    def match_uncertified(self) -> int:
+        n = C.c_int(0)
+        check(lib().rtr_match_stats(self.h, C.byref(n)))
+        return n.value
 
     def match_exact(self, q, db, stream=None):
         import torch

@@ -1,0 +1,549 @@
+// match_tc.cu — descriptor 1-NN on the 5th-generation tensor cores.
+//
+// d^2(q, b) = |q|^2 + |b|^2 - 2 q.b with the dot product as a BF16 GEMM with
+// FP32 accumulation in tensor memory.  Each FP32 descriptor is split into
+// hi = bf16(x) and lo = bf16(x - hi); the accumulator sums hi.hi + hi.lo +
+// lo.hi (three tcgen05.mma per K step), which leaves |err(q.b)| < ~1e-4 for the
+// unit-norm, non-negative SHOT vectors.  Per query the epilogue keeps the 8
+// smallest approximate distances; an exact FP32 re-rank (sequential sums, as
+// the oracle) picks the winner, and a query is certified when its 8th
+// approximate distance minus the error bound is still above the exact winner,
+// so no unseen descriptor can beat or tie it.  Uncertified queries are
+// re-scanned exactly.  The result is bit-identical to the exact matcher.
+//
+// Kernel layout (one CTA per 128 queries, 6 warps): warp 4 issues TMA loads of
+// the K-blocks (64 bf16 = one 128-byte swizzle row) of Q_hi, Q_lo, B_hi, B_lo
+// into a 2-stage ring; warp 5 issues tcgen05.mma (M=128, N=256, K=16) into one
+// of two TMEM accumulators (2 x 256 columns); warps 0-3 drain the finished
+// accumulator with tcgen05.ld (thread = query row) and update the top-8.
+// Every mbarrier wait is bounded; on timeout the CTA records RTR_ERR_TIMEOUT,
+// stops issuing, waits (bounded) for its in-flight work and frees its TMEM.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <string.h>
+
+#include "common.cuh"
+
+namespace rtr {
+
+constexpr int TC_DIM = 352;
+constexpr int TC_KPAD = 384;              // 6 K-blocks of 64
+constexpr int TC_KB = 64;
+constexpr int TC_NKB = TC_KPAD / TC_KB;
+constexpr int TC_BM = 128;
+constexpr int TC_BN = 256;
+constexpr int TC_STAGES = 2;
+constexpr int TC_TOP = 8;
+constexpr int TC_A_BYTES = TC_BM * TC_KB * 2;   // 16 KB
+constexpr int TC_B_BYTES = TC_BN * TC_KB * 2;   // 32 KB
+constexpr int TC_STAGE_BYTES = 2 * TC_A_BYTES + 2 * TC_B_BYTES;  // 96 KB
+constexpr int TC_THREADS = 192;
+constexpr float TC_ERR = 1.0e-3f;  // conservative bound on |d~ - d| (see top)
+constexpr long long TC_SPIN_LIMIT = 1LL << 26;
+
+// ---------------------------------------------------------------------------
+// PTX helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait; returns false (and raises the CTA abort flag) on timeout
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort) {
+  for (long long i = 0; i < TC_SPIN_LIMIT; ++i) {
+    if (mbar_try(b, parity)) return true;
+    if (*abort) return false;
+  }
+  *abort = 1;
+  return false;
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+      : "memory");
+}
+// UMMA shared-memory descriptor: K-major, 128-byte swizzle, 8-row atoms of
+// 1024 bytes (SBO), start address in 16-byte units, descriptor version 1.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);       // start address
+  d |= (uint64_t)1 << 16;                         // LBO (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;               // SBO
+  d |= (uint64_t)1 << 46;                         // version
+  d |= (uint64_t)2 << 61;                         // SWIZZLE_128B
+  return d;
+}
+// Instruction descriptor, kind::f16: D = F32, A = B = BF16, K-major, N, M.
+__device__ __forceinline__ uint32_t umma_idesc() {
+  uint32_t d = 0;
+  d |= 1u << 4;                          // D format F32
+  d |= 1u << 7;                          // A BF16
+  d |= 1u << 10;                         // B BF16
+  d |= (uint32_t)(TC_BN >> 3) << 17;     // N
+  d |= (uint32_t)(TC_BM >> 4) << 24;     // M
+  return d;
+}
+__device__ __forceinline__ void umma_f16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accum) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(
+          tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accum)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
+      "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// ---------------------------------------------------------------------------
+// FP32 descriptors -> padded (hi, lo) BF16 rows + FP32 squared norms
+// ---------------------------------------------------------------------------
+__global__ void k_split_bf16(const float* __restrict__ x, int n_host, const int* d_n, int n_cap,
+                             __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
+                             float* __restrict__ norm2) {
+  const int n = d_n ? min(*d_n, n_cap) : n_host;
+  const int lane = threadIdx.x & 31;
+  for (int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < n_cap; r += gridDim.x * (blockDim.x >> 5)) {
+    float ss = 0.f;
+    for (int k = lane; k < TC_KPAD; k += 32) {
+      const float v = (r < n && k < TC_DIM) ? x[(size_t)r * TC_DIM + k] : 0.f;
+      const __nv_bfloat16 h = __float2bfloat16_rn(v);
+      const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
+      hi[(size_t)r * TC_KPAD + k] = h;
+      lo[(size_t)r * TC_KPAD + k] = l;
+      ss += v * v;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+    if (lane == 0) norm2[r] = ss;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// GEMM + top-8
+// ---------------------------------------------------------------------------
+struct TcArgs {
+  int nq_host;
+  const int* d_nq;
+  int nq_cap;
+  int ndb;
+  const float* qn;   // [nq_cap] |q|^2
+  const float* dn;   // [ndb]   |b|^2
+  int* cand_idx;     // [nq_cap][8]
+  float* cand_d;     // [nq_cap][8]
+  int* status;
+};
+
+__global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constant__ CUtensorMap mq_hi,
+                                                            const __grid_constant__ CUtensorMap mq_lo,
+                                                            const __grid_constant__ CUtensorMap mb_hi,
+                                                            const __grid_constant__ CUtensorMap mb_lo, TcArgs a) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  __shared__ uint64_t full_bar[TC_STAGES], empty_bar[TC_STAGES], acc_full[2], acc_empty[2];
+  __shared__ uint32_t tmem_base;
+  __shared__ int abort_flag;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nq = a.d_nq ? min(*a.d_nq, a.nq_cap) : a.nq_host;
+  const int q0 = blockIdx.x * TC_BM;
+  if (q0 >= nq) return;  // uniform per CTA, before any barrier or TMEM use
+  const int n_tiles = (a.ndb + TC_BN - 1) / TC_BN;
+
+  if (threadIdx.x == 0) {
+    abort_flag = 0;
+    for (int s = 0; s < TC_STAGES; ++s) {
+      mbar_init(&full_bar[s], 1);
+      mbar_init(&empty_bar[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], 128);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 5) {  // allocate 512 TMEM columns (two 128 x 256 FP32 accumulators)
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(&tmem_base)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base;
+  volatile int* abort = &abort_flag;
+
+  if (warp == 4) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      int it = 0;
+      for (int t = 0; t < n_tiles && !*abort; ++t) {
+        for (int kb = 0; kb < TC_NKB && !*abort; ++kb, ++it) {
+          const int s = it % TC_STAGES;
+          const uint32_t ph = (uint32_t)(it / TC_STAGES) & 1u;
+          if (it >= TC_STAGES && !mbar_wait(&empty_bar[s], ph ^ 1u, abort)) break;
+          uint8_t* st = smem + s * TC_STAGE_BYTES;
+          mbar_expect_tx(&full_bar[s], TC_STAGE_BYTES);
+          tma_load_2d(st, &mq_hi, &full_bar[s], kb * TC_KB, q0);
+          tma_load_2d(st + TC_A_BYTES, &mq_lo, &full_bar[s], kb * TC_KB, q0);
+          tma_load_2d(st + 2 * TC_A_BYTES, &mb_hi, &full_bar[s], kb * TC_KB, t * TC_BN);
+          tma_load_2d(st + 2 * TC_A_BYTES + TC_B_BYTES, &mb_lo, &full_bar[s], kb * TC_KB, t * TC_BN);
+        }
+      }
+    }
+  } else if (warp == 5) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      const uint32_t idesc = umma_idesc();
+      int it = 0;
+      for (int t = 0; t < n_tiles && !*abort; ++t) {
+        const int buf = t & 1;
+        const uint32_t use = (uint32_t)(t >> 1);
+        if (t >= 2 && !mbar_wait(&acc_empty[buf], (use - 1) & 1u, abort)) break;
+        tc_fence_after();
+        const uint32_t dcol = tmem + (uint32_t)buf * TC_BN;
+        for (int kb = 0; kb < TC_NKB; ++kb, ++it) {
+          const int s = it % TC_STAGES;
+          const uint32_t ph = (uint32_t)(it / TC_STAGES) & 1u;
+          if (!mbar_wait(&full_bar[s], ph, abort)) break;
+          tc_fence_after();
+          const uint32_t base = smem_u32(smem + s * TC_STAGE_BYTES);
+          const uint32_t ah = base, al = base + TC_A_BYTES, bh = base + 2 * TC_A_BYTES,
+                         bl = base + 2 * TC_A_BYTES + TC_B_BYTES;
+#pragma unroll
+          for (int k = 0; k < TC_KB / 16; ++k) {
+            const uint32_t off = (uint32_t)k * 32;  // 16 bf16 along K inside the 128-byte swizzle row
+            const uint32_t acc0 = (kb > 0 || k > 0) ? 1u : 0u;
+            umma_f16(dcol, umma_desc(ah + off), umma_desc(bh + off), idesc, acc0);
+            umma_f16(dcol, umma_desc(ah + off), umma_desc(bl + off), idesc, 1u);
+            umma_f16(dcol, umma_desc(al + off), umma_desc(bh + off), idesc, 1u);
+          }
+          umma_commit(&empty_bar[s]);  // stage free once these MMAs have read it
+        }
+        umma_commit(&acc_full[buf]);  // accumulator ready
+      }
+    }
+  } else {
+    // ---------------- epilogue: warps 0-3, thread = query row ----------------
+    const int row = warp * 32 + lane;
+    const int q = q0 + row;
+    const float qn = q < nq ? a.qn[q] : 0.f;
+    float bd[TC_TOP];
+    int bi[TC_TOP];
+#pragma unroll
+    for (int s = 0; s < TC_TOP; ++s) {
+      bd[s] = __int_as_float(0x7f800000);
+      bi[s] = 0x7fffffff;
+    }
+    for (int t = 0; t < n_tiles; ++t) {
+      const int buf = t & 1;
+      const uint32_t use = (uint32_t)(t >> 1);
+      if (!mbar_wait(&acc_full[buf], use & 1u, abort)) break;
+      tc_fence_after();
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)buf * TC_BN;
+      for (int c0 = 0; c0 < TC_BN; c0 += 32) {
+        float v[32];
+        tmem_ld32(taddr + (uint32_t)c0, v);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          const int j = t * TC_BN + c0 + i;
+          if (j >= a.ndb) break;
+          const float d = qn + __ldg(a.dn + j) - 2.f * v[i];
+          if (d < bd[TC_TOP - 1]) {
+            bd[TC_TOP - 1] = d;
+            bi[TC_TOP - 1] = j;
+#pragma unroll
+            for (int s = TC_TOP - 1; s > 0; --s) {
+              const bool lt = bd[s] < bd[s - 1];
+              const float x0 = bd[s], x1 = bd[s - 1];
+              const int y0 = bi[s], y1 = bi[s - 1];
+              bd[s] = lt ? x1 : x0;
+              bd[s - 1] = lt ? x0 : x1;
+              bi[s] = lt ? y1 : y0;
+              bi[s - 1] = lt ? y0 : y1;
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(&acc_empty[buf]);
+    }
+    if (q < nq) {
+#pragma unroll
+      for (int s = 0; s < TC_TOP; ++s) {
+        a.cand_idx[(size_t)q * TC_TOP + s] = bi[s] == 0x7fffffff ? -1 : bi[s];
+        a.cand_d[(size_t)q * TC_TOP + s] = bd[s];
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (abort_flag && threadIdx.x == 0) atomicExch(a.status, (int)RTR_ERR_TIMEOUT);
+  if (warp == 5) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
+  }
+}
+
+// Exact FP32 re-rank of the 8 candidates (sequential sums, as the oracle) and
+// certification; one warp per query, lanes 0-7 one candidate each.
+__global__ void k_rerank(const float* __restrict__ q, int nq_host, const int* d_nq, int nq_cap,
+                         const float* __restrict__ db, int ndb, const int* __restrict__ cand_idx,
+                         const float* __restrict__ cand_d, int* __restrict__ out_idx, float* __restrict__ out_d2,
+                         int* __restrict__ redo, int* __restrict__ n_redo) {
+  const int nq = d_nq ? min(*d_nq, nq_cap) : nq_host;
+  const int lane = threadIdx.x & 31;
+  for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < nq; i += gridDim.x * (blockDim.x >> 5)) {
+    const int c = lane < TC_TOP ? cand_idx[(size_t)i * TC_TOP + lane] : -1;
+    float d = __int_as_float(0x7f800000);
+    if (c >= 0) {
+      const float* x = q + (size_t)i * TC_DIM;
+      const float* y = db + (size_t)c * TC_DIM;
+      float acc = 0.f;
+      for (int k = 0; k < TC_DIM; ++k) {
+        const float t = __fsub_rn(x[k], y[k]);
+        acc = __fadd_rn(acc, __fmul_rn(t, t));
+      }
+      d = acc;
+    }
+    int bi = c >= 0 ? c : 0x7fffffff;
+    float bd = d;
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) {
+      const float od = __shfl_xor_sync(0xffffffffu, bd, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (od < bd || (od == bd && oi < bi)) {
+        bd = od;
+        bi = oi;
+      }
+    }
+    if (lane == 0) {
+      const float worst = cand_d[(size_t)i * TC_TOP + TC_TOP - 1];
+      const int nvalid = ndb < TC_TOP ? ndb : TC_TOP;
+      const bool all_seen = nvalid < TC_TOP;  // every descriptor was a candidate
+      const bool certified = all_seen || (worst - TC_ERR > bd);
+      if (certified) {
+        out_idx[i] = bi == 0x7fffffff ? -1 : bi;
+        if (out_d2) out_d2[i] = bd;
+      } else {
+        redo[atomicAdd(n_redo, 1)] = i;
+      }
+    }
+  }
+}
+
+// Exact scan for the uncertified queries (warp per query, lanes over the db).
+__global__ void k_match_redo(const float* __restrict__ q, const float* __restrict__ db, int ndb,
+                             const int* __restrict__ redo, const int* __restrict__ n_redo, int* __restrict__ out_idx,
+                             float* __restrict__ out_d2) {
+  const int lane = threadIdx.x & 31;
+  const int n = *n_redo;
+  for (int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < n; w += gridDim.x * (blockDim.x >> 5)) {
+    const int i = redo[w];
+    const float* x = q + (size_t)i * TC_DIM;
+    float bd = __int_as_float(0x7f800000);
+    int bi = 0x7fffffff;
+    for (int j = lane; j < ndb; j += 32) {
+      const float* y = db + (size_t)j * TC_DIM;
+      float acc = 0.f;
+      for (int k = 0; k < TC_DIM; ++k) {
+        const float t = __fsub_rn(x[k], y[k]);
+        acc = __fadd_rn(acc, __fmul_rn(t, t));
+      }
+      if (acc < bd) {
+        bd = acc;
+        bi = j;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float od = __shfl_xor_sync(0xffffffffu, bd, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (od < bd || (od == bd && oi < bi)) {
+        bd = od;
+        bi = oi;
+      }
+    }
+    if (lane == 0) {
+      out_idx[i] = bi == 0x7fffffff ? -1 : bi;
+      if (out_d2) out_d2[i] = bd;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host: tensor maps through the driver entry point (no libcuda link)
+// ---------------------------------------------------------------------------
+typedef CUresult (*PFN_encodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                    const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static PFN_encodeTiled get_encode() {
+  static PFN_encodeTiled fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_encodeTiled>(p);
+  }
+  return fn;
+}
+
+static bool make_map(CUtensorMap* m, const void* base, int rows, int box_rows) {
+  PFN_encodeTiled enc = get_encode();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)TC_KPAD, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)TC_KPAD * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)TC_KB, (cuuint32_t)box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+size_t match_tc_bf16_bytes(int rows) { return (size_t)rows * TC_KPAD * 2; }
+
+void match_tc_plan(ScratchPlan& p, int nq_cap, bool with_db, int ndb) {
+  const int nqp = ((nq_cap + TC_BM - 1) / TC_BM) * TC_BM;
+  p.add<__nv_bfloat16>((size_t)nqp * TC_KPAD);
+  p.add<__nv_bfloat16>((size_t)nqp * TC_KPAD);
+  p.add<float>(nqp);
+  if (with_db) {
+    p.add<__nv_bfloat16>((size_t)ndb * TC_KPAD);
+    p.add<__nv_bfloat16>((size_t)ndb * TC_KPAD);
+    p.add<float>(ndb);
+  }
+  p.add<int>((size_t)nqp * TC_TOP);
+  p.add<float>((size_t)nqp * TC_TOP);
+  p.add<int>(nqp);
+  p.add<int>(4);
+}
+
+// Splits a descriptor database once (the model side keeps the result).
+rtr_status match_tc_prepare_db(const float* db, int ndb, __nv_bfloat16* hi, __nv_bfloat16* lo, float* norm2,
+                               cudaStream_t st) {
+  int blocks = (ndb + 7) / 8;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (blocks < 1) blocks = 1;
+  k_split_bf16<<<blocks, 256, 0, st>>>(db, ndb, nullptr, ndb, hi, lo, norm2);
+  RTR_LAUNCHED(1);
+  RTR_CUDA(cudaGetLastError());
+  return RTR_OK;
+}
+
+rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap, const int* d_nq, const float* db,
+                        int ndb, const __nv_bfloat16* db_hi, const __nv_bfloat16* db_lo, const float* db_n2,
+                        int* out_idx, float* out_d2, cudaStream_t st) {
+  const int nqp = ((nq_cap + TC_BM - 1) / TC_BM) * TC_BM;
+  __nv_bfloat16* qhi = s.take<__nv_bfloat16>((size_t)nqp * TC_KPAD);
+  __nv_bfloat16* qlo = s.take<__nv_bfloat16>((size_t)nqp * TC_KPAD);
+  float* qn = s.take<float>(nqp);
+  if (!db_hi) {
+    __nv_bfloat16* h = s.take<__nv_bfloat16>((size_t)ndb * TC_KPAD);
+    __nv_bfloat16* l = s.take<__nv_bfloat16>((size_t)ndb * TC_KPAD);
+    float* n2 = s.take<float>(ndb);
+    if (!n2) return fail(RTR_ERR_CAPACITY, "match_tc: scratch");
+    RTR_TRY(match_tc_prepare_db(db, ndb, h, l, n2, st));
+    db_hi = h;
+    db_lo = l;
+    db_n2 = n2;
+  }
+  int* cidx = s.take<int>((size_t)nqp * TC_TOP);
+  float* cd = s.take<float>((size_t)nqp * TC_TOP);
+  int* redo = s.take<int>(nqp);
+  int* nredo = s.take<int>(4);
+  if (!nredo) return fail(RTR_ERR_CAPACITY, "match_tc: scratch");
+  int sb = (nqp + 7) / 8;
+  if (sb > 152 * 16) sb = 152 * 16;
+  k_split_bf16<<<sb, 256, 0, st>>>(q, nq_cap, d_nq, nqp, qhi, qlo, qn);
+  CUtensorMap m_qh, m_ql, m_bh, m_bl;
+  if (!make_map(&m_qh, qhi, nqp, TC_BM) || !make_map(&m_ql, qlo, nqp, TC_BM) || !make_map(&m_bh, db_hi, ndb, TC_BN) ||
+      !make_map(&m_bl, db_lo, ndb, TC_BN))
+    return fail(RTR_ERR_CUDA, "match_tc: cuTensorMapEncodeTiled failed");
+  const size_t smem = (size_t)TC_STAGES * TC_STAGE_BYTES + 1024;
+  static bool attr = false;
+  if (!attr) {
+    RTR_CUDA(cudaFuncSetAttribute(k_match_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  TcArgs a{nq_cap, d_nq, nq_cap, ndb, qn, db_n2, cidx, cd, ctx->d_status};
+  k_match_tc<<<nqp / TC_BM, TC_THREADS, smem, st>>>(m_qh, m_ql, m_bh, m_bl, a);
+  RTR_CUDA(cudaMemsetAsync(nredo, 0, sizeof(int), st));
+  int rb = (nq_cap + 7) / 8;
+  if (rb > 152 * 16) rb = 152 * 16;
+  k_rerank<<<rb, 256, 0, st>>>(q, nq_cap, d_nq, nq_cap, db, ndb, cidx, cd, out_idx, out_d2, redo, nredo);
+  k_match_redo<<<152 * 4, 256, 0, st>>>(q, db, ndb, redo, nredo, out_idx, out_d2);
+  RTR_LAUNCHED(4);
+  // keep the number of uncertified queries for rtr_match_stats
+  RTR_CUDA(cudaMemcpyAsync(ctx->d_status + 8, nredo, sizeof(int), cudaMemcpyDeviceToDevice, st));
+  RTR_CUDA(cudaGetLastError());
+  return RTR_OK;
+}
+
+}  // namespace rtr
+
+using namespace rtr;
+
+extern "C" rtr_status rtr_match_stats(rtr_context* ctx, int* h_uncertified) {
+  RTR_CHECK_ARG(ctx && h_uncertified, "rtr_match_stats: bad arguments");
+  RTR_CUDA(cudaSetDevice(ctx->device));
+  RTR_CUDA(cudaDeviceSynchronize());
+  RTR_CUDA(cudaMemcpy(h_uncertified, ctx->d_status + 8, sizeof(int), cudaMemcpyDeviceToHost));
+  return RTR_OK;
+}
+
+extern "C" rtr_status rtr_match(rtr_context* ctx, const float* d_query, int n_query, const float* d_db, int n_db,
+                                int32_t* d_idx, float* d_d2, rtr_stream_t stream) {
+  RTR_CHECK_ARG(ctx && n_query >= 0 && n_db >= 0, "rtr_match: bad arguments");
+  if (n_query == 0) return RTR_OK;
+  RTR_CHECK_ARG(d_query && d_idx, "rtr_match: NULL query or output");
+  cudaStream_t st = (cudaStream_t)stream;
+  RTR_CUDA(cudaSetDevice(ctx->device));
+  if (n_db == 0) {
+    RTR_CUDA(cudaMemsetAsync(d_idx, 0xff, (size_t)n_query * 4, st));
+    return RTR_OK;
+  }
+  RTR_CHECK_ARG(d_db != nullptr, "rtr_match: NULL database");
+  ScratchPlan p;
+  match_tc_plan(p, n_query, true, n_db);
+  Scratch s;
+  RTR_TRY(ensure_scratch(ctx, p.bytes, st, &s));
+  ProfScope ps(ctx, st, "match_tc");
+  return match_tc_dev(ctx, s, d_query, n_query, nullptr, d_db, n_db, nullptr, nullptr, nullptr, d_idx, d_d2, st);
+}

@@ -8,6 +8,7 @@
 // the scene) -> batched ICP refinement of the best hypotheses -> final score
 // and non-maximum suppression.  Every count stays on the device except the
 // correspondence count, read once before grouping.
+#include <cuda_bf16.h>
 #include <string.h>
 
 #include <algorithm>
@@ -27,6 +28,13 @@ rtr_status normals_dev(rtr_context*, Scratch&, const float4*, int, const int*, i
 rtr_status shot_dev(rtr_context*, Scratch&, const float4*, const float4*, int, const int*, const int*, int, const int*,
                     float, float*, float*, cudaStream_t);
 rtr_status match_exact_dev(const float*, int, const int*, const float*, int, int*, float*, cudaStream_t);
+size_t match_tc_bf16_bytes(int rows);
+void match_tc_plan(ScratchPlan& p, int nq_cap, bool with_db, int ndb);
+rtr_status match_tc_prepare_db(const float* db, int ndb, __nv_bfloat16* hi, __nv_bfloat16* lo, float* norm2,
+                               cudaStream_t st);
+rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap, const int* d_nq, const float* db,
+                        int ndb, const __nv_bfloat16* db_hi, const __nv_bfloat16* db_lo, const float* db_n2,
+                        int* out_idx, float* out_d2, cudaStream_t st);
 size_t gc_scratch_bytes(int C, int max_clusters);
 __global__ void k_orient_outward(const float4* __restrict__ pts, float4* __restrict__ nrm, int n_host, const int* d_n,
                                  float rc2, float gap, float len);
@@ -213,6 +221,9 @@ struct rtr_model {
   float4* kp = nullptr;     // keypoint positions
   float* desc = nullptr;    // [n_kp][352]
   GridMeta* vox_meta = nullptr;  // bbox of the voxel cloud (ICP centring)
+  __nv_bfloat16* db_hi = nullptr;  // [n_kp][384] descriptor split for the tensor cores
+  __nv_bfloat16* db_lo = nullptr;
+  float* db_n2 = nullptr;          // [n_kp] squared norms
 };
 
 extern "C" {
@@ -306,6 +317,14 @@ rtr_status rtr_model_create(rtr_context* ctx, const float* d_pts, int n, const r
   k_gather_kp<<<nblocks(K), 256, 0, st>>>(m->vox, m->keys, d_cnt + 1, K, m->kp);
   bbox_build(m->vox_meta, m->vox, V, st);
   RTR_LAUNCHED(1);
+  if (cudaMalloc(&m->db_hi, match_tc_bf16_bytes(K)) != cudaSuccess ||
+      cudaMalloc(&m->db_lo, match_tc_bf16_bytes(K)) != cudaSuccess ||
+      cudaMalloc(&m->db_n2, (size_t)K * sizeof(float)) != cudaSuccess) {
+    cudaGetLastError();
+    return cleanup(fail(RTR_ERR_OOM, "rtr_model_create: tensor-core database"));
+  }
+  r = match_tc_prepare_db(m->desc, K, m->db_hi, m->db_lo, m->db_n2, st);
+  if (r != RTR_OK) return cleanup(r);
   if (cudaStreamSynchronize(st) != cudaSuccess) return cleanup(fail(RTR_ERR_CUDA, "rtr_model_create: sync"));
   *out = m;
   return RTR_OK;
@@ -320,6 +339,9 @@ rtr_status rtr_model_destroy(rtr_model* m) {
   cudaFree(m->kp);
   cudaFree(m->desc);
   cudaFree(m->vox_meta);
+  cudaFree(m->db_hi);
+  cudaFree(m->db_lo);
+  cudaFree(m->db_n2);
   delete m;
   return RTR_OK;
 }
@@ -432,6 +454,11 @@ size_t recognize_scratch_bytes(int n, int n_model_vox, int n_model_kp, const rtr
     icp_multi_plan(t, q->refine_top, 152 * 16);
     stage = t.bytes > stage ? t.bytes : stage;
   }
+  {
+    ScratchPlan t;
+    match_tc_plan(t, n, false, 0);
+    stage = t.bytes > stage ? t.bytes : stage;
+  }
   (void)n_model_vox;
   (void)n_model_kp;
   return p.bytes + stage + 4096;
@@ -486,7 +513,9 @@ static rtr_status recognize_impl(rtr_context* ctx, const rtr_model* m, const flo
   }
   {
     ProfScope ps(ctx, st, "match");
-    RTR_TRY(match_exact_dev(b.desc, n, dKeys, m->desc, m->n_kp, b.midx, b.md2, st));
+    Scratch t = stage;
+    RTR_TRY(match_tc_dev(ctx, t, b.desc, n, dKeys, m->desc, m->n_kp, m->db_hi, m->db_lo, m->db_n2, b.midx, b.md2,
+                         st));
   }
   {
     ProfScope ps(ctx, st, "correspondences");
