@@ -84,6 +84,15 @@ __device__ __forceinline__ float ring_bound(const GridView& g, float4 q, int cx,
   return lb;
 }
 
+// Distance from q to the box spanned by the whole grid.
+__device__ __forceinline__ float grid_box_dist(const GridView& g, float4 q) {
+  const float hx = g.ox + (float)g.nx * g.h, hy = g.oy + (float)g.ny * g.h, hz = g.oz + (float)g.nz * g.h;
+  const float dx = fmaxf(fmaxf(g.ox - q.x, q.x - hx), 0.f);
+  const float dy = fmaxf(fmaxf(g.oy - q.y, q.y - hy), 0.f);
+  const float dz = fmaxf(fmaxf(g.oz - q.z, q.z - hz), 0.f);
+  return sqrtf(dx * dx + dy * dy + dz * dz);
+}
+
 __device__ __forceinline__ bool ring_covers(const GridView& g, int cx, int cy, int cz, int k) {
   return cx - k <= 0 && cx + k >= g.nx - 1 && cy - k <= 0 && cy + k >= g.ny - 1 && cz - k <= 0 &&
          cz + k >= g.nz - 1;
@@ -138,6 +147,12 @@ __device__ __forceinline__ void grid_nn1(const GridView& g, float4 q, float r2ma
   bpos = -1;
   const int cx = q_cell(q.x, g.ox, g.inv_h), cy = q_cell(q.y, g.oy, g.inv_h),
             cz = q_cell(q.z, g.oz, g.inv_h);
+  // nothing of the grid within the bound: done before walking any ring
+  if (beyond(grid_box_dist(g, q), search_margin(g, q, 0), r2max)) {
+    bi = -1;
+    bd = __int_as_float(0x7f800000);
+    return;
+  }
   for (int k = first_ring(g, cx, cy, cz);; ++k) {
     const float margin = search_margin(g, q, k);
     RTR_FOR_RING(g, cx, cy, cz, k, {
@@ -188,6 +203,12 @@ __device__ __forceinline__ void grid_nn1_group(const GridView& g, float4 q, floa
   const int cx = q_cell(q.x, g.ox, g.inv_h), cy = q_cell(q.y, g.oy, g.inv_h),
             cz = q_cell(q.z, g.oz, g.inv_h);
   const int gbase = (threadIdx.x & 31) & ~(G - 1);
+  // nothing of the grid within the bound (uniform inside the group)
+  if (beyond(grid_box_dist(g, q), search_margin(g, q, 0), r2max)) {
+    bi = -1;
+    bd = __int_as_float(0x7f800000);
+    return;
+  }
   for (int k = first_ring(g, cx, cy, cz);; ++k) {
     const float margin = search_margin(g, q, k);
     // the ring's cube clamped to the grid
