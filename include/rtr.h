@@ -127,6 +127,30 @@ rtr_status rtr_knn1(rtr_context* ctx, const float* d_query, int n_query,
                     const float* d_target, int n_target, float max_dist,
                     int32_t* d_out_idx, float* d_out_d2, rtr_stream_t stream);
 
+/* rtr_knn1 without any allocation, for callers that may not allocate device
+ * memory (a real-time control loop with a fixed memory budget, a caller that
+ * owns every allocation itself, code running where cudaMalloc would
+ * synchronise the device).  No counterpart in the reference.
+ *
+ * Same arguments and results as rtr_knn1 (bit-identical outputs), minus the
+ * context: it runs on the calling thread's current device.  Its grid lives in
+ * one fixed device array of about 7 MiB compiled into the library, so
+ * n_target is limited to RTR_KNN1_STATIC_MAX_TARGET (larger sets return
+ * RTR_ERR_CAPACITY before anything is launched; use rtr_knn1 for those).
+ * n_query is not limited.  Nothing in the array needs to start at zero:
+ * each call rebuilds every part it reads.
+ *
+ * The first call on a device looks up the array's address
+ * (cudaGetSymbolAddress), which may load the module; make that first call
+ * before capturing a stream.  The array is shared by every call on a device:
+ * two calls whose work overlaps in time (different streams, or different
+ * host threads, without ordering between them) race and both may return wrong
+ * indices.  Order them on one stream or with events. */
+#define RTR_KNN1_STATIC_MAX_TARGET 65536
+rtr_status rtr_knn1_static(const float* d_query, int n_query, const float* d_target,
+                           int n_target, float max_dist, int32_t* d_out_idx,
+                           float* d_out_d2, rtr_stream_t stream);
+
 /* k nearest neighbours (1 <= k <= 32), sorted by (d^2, index).  Unbounded. */
 rtr_status rtr_knn(rtr_context* ctx, const float* d_query, int n_query,
                    const float* d_target, int n_target, int k,

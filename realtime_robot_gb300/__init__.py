@@ -52,6 +52,7 @@ class RoomParams(C.Structure):
 
 
 MAX_INSTANCES = 16
+KNN1_STATIC_MAX_TARGET = 65536  # RTR_KNN1_STATIC_MAX_TARGET
 
 
 class RecogParams(C.Structure):
@@ -124,6 +125,7 @@ _SIG = {
     "ComputeTDFWithCuda": (_I, [_P, _P, _I, _I]),
     "rtr_tdf_batch": (_I, [_P, _P, _P, _I, _I, _P, _P]),
     "rtr_knn1": (_I, [_P, _P, _I, _P, _I, _F, _P, _P, _P]),
+    "rtr_knn1_static": (_I, [_P, _I, _P, _I, _F, _P, _P, _P]),
     "rtr_knn": (_I, [_P, _P, _I, _P, _I, _I, _P, _P, _P]),
     "rtr_icp_default_params": (None, [C.POINTER(IcpParams)]),
     "rtr_icp": (_I, [_P, _P, _I, _P, _I, C.POINTER(IcpParams), _P, _P, _P, _P, _P]),
@@ -253,6 +255,21 @@ class Context:
         d2 = torch.empty(nq, dtype=torch.float32, device=query.device)
         check(lib().rtr_knn1(self.h, _ptr(query), nq, _ptr(target), nt, float(max_dist),
                              _ptr(idx), _ptr(d2), _stream(stream)))
+        return idx, d2
+
+    def knn1_static(self, query, target, max_dist: float = 0.0, out=None, stream=None):
+        """rtr_knn1_static: rtr_knn1 with its grid in the library's fixed
+        device array (no allocation inside the call; n_target at most
+        KNN1_STATIC_MAX_TARGET).  `out` = (idx int32 [nq], d2 float32 [nq])
+        preallocated by the caller; allocated here when omitted."""
+        import torch
+        nq, nt = query.shape[0], target.shape[0]
+        if out is None:
+            out = (torch.empty(nq, dtype=torch.int32, device=query.device),
+                   torch.empty(nq, dtype=torch.float32, device=query.device))
+        idx, d2 = out
+        check(lib().rtr_knn1_static(_ptr(query), nq, _ptr(target), nt, float(max_dist),
+                                    _ptr(idx), _ptr(d2), _stream(stream)))
         return idx, d2
 
     def knn(self, query, target, k: int, stream=None):

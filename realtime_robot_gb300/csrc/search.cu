@@ -1,6 +1,8 @@
 // search.cu — rtr_knn1 / rtr_knn entry points over the radix-sorted grid.
 #include <string.h>
 
+#include <mutex>
+
 #include "search.cuh"
 
 namespace rtr {
@@ -50,6 +52,16 @@ static int search_blocks(int n) {
   return b < 1 ? 1 : b;
 }
 
+// Fixed grid storage of rtr_knn1_static: the grid of up to
+// RTR_KNN1_STATIC_MAX_TARGET points with the default cell table
+// (8 cells per point) needs about 6.6 MB.
+constexpr size_t KNN1_STATIC_BYTES = size_t(7) << 20;
+static __device__ __align__(256) unsigned char g_knn1_static[KNN1_STATIC_BYTES];
+
+constexpr int KNN1_STATIC_DEVICES = 64;
+static std::mutex g_knn1_static_mu;
+static void* g_knn1_static_ptr[KNN1_STATIC_DEVICES];
+
 }  // namespace rtr
 
 using namespace rtr;
@@ -80,6 +92,64 @@ rtr_status rtr_knn1(rtr_context* ctx, const float* d_query, int n_query, const f
   grid_build(gb, reinterpret_cast<const float4*>(d_target), n_target, nullptr,
              bounded ? 0.5f * max_dist : -1.f, st);
   ProfScope ps(ctx, st, "knn1");
+  RTR_LAUNCHED(1);
+  k_knn1<<<search_blocks(n_query * KNN1_G), 128, 0, st>>>(grid_dev(gb), reinterpret_cast<const float4*>(d_query),
+                                                 n_query, bounded ? max_dist * max_dist : __builtin_inff(),
+                                                 d_out_idx, d_out_d2);
+  RTR_CUDA(cudaGetLastError());
+  return RTR_OK;
+}
+
+rtr_status rtr_knn1_static(const float* d_query, int n_query, const float* d_target,
+                           int n_target, float max_dist, int32_t* d_out_idx, float* d_out_d2,
+                           rtr_stream_t stream) {
+  RTR_CHECK_ARG(n_query >= 0 && n_target >= 0, "rtr_knn1_static: bad arguments");
+  if (n_target > RTR_KNN1_STATIC_MAX_TARGET)
+    return fail(RTR_ERR_CAPACITY,
+                "rtr_knn1_static: n_target %d exceeds the fixed maximum %d (use rtr_knn1)",
+                n_target, RTR_KNN1_STATIC_MAX_TARGET);
+  if (n_query == 0) return RTR_OK;
+  RTR_CHECK_ARG(d_query && d_out_idx, "rtr_knn1_static: NULL query or output");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (n_target == 0) {
+    RTR_CUDA(cudaMemsetAsync(d_out_idx, 0xff, (size_t)n_query * 4, st));
+    return RTR_OK;  // d_out_d2 left as is: every index is -1
+  }
+  RTR_CHECK_ARG(d_target != nullptr, "rtr_knn1_static: NULL target");
+  int dev = 0;
+  RTR_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= KNN1_STATIC_DEVICES)
+    return fail(RTR_ERR_INVALID_ARG, "rtr_knn1_static: device %d beyond the supported %d", dev,
+                KNN1_STATIC_DEVICES);
+  void* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_knn1_static_mu);
+    if (!g_knn1_static_ptr[dev]) {
+      void* p = nullptr;
+      const cudaError_t e = cudaGetSymbolAddress(&p, g_knn1_static);
+      if (e != cudaSuccess || !p) {
+        (void)cudaGetLastError();
+        return fail(RTR_ERR_CUDA, "rtr_knn1_static: cudaGetSymbolAddress failed on device %d: %s",
+                    dev, cudaGetErrorString(e));
+      }
+      g_knn1_static_ptr[dev] = p;
+    }
+    base = g_knn1_static_ptr[dev];
+  }
+  const unsigned cap = default_cell_cap(RTR_KNN1_STATIC_MAX_TARGET);
+  ScratchPlan plan;
+  grid_plan(plan, n_target, cap);
+  if (plan.bytes > KNN1_STATIC_BYTES)
+    return fail(RTR_ERR_CAPACITY, "rtr_knn1_static: grid needs %zu bytes, fixed array holds %zu",
+                plan.bytes, KNN1_STATIC_BYTES);
+  Scratch s;
+  s.base = static_cast<char*>(base);
+  s.cap = KNN1_STATIC_BYTES;
+  GridBufs gb;
+  if (!grid_take(s, n_target, cap, &gb)) return fail(RTR_ERR_CAPACITY, "rtr_knn1_static: scratch");
+  const bool bounded = max_dist > 0.f && max_dist < 1e18f;
+  grid_build(gb, reinterpret_cast<const float4*>(d_target), n_target, nullptr,
+             bounded ? 0.5f * max_dist : -1.f, st);
   RTR_LAUNCHED(1);
   k_knn1<<<search_blocks(n_query * KNN1_G), 128, 0, st>>>(grid_dev(gb), reinterpret_cast<const float4*>(d_query),
                                                  n_query, bounded ? max_dist * max_dist : __builtin_inff(),
