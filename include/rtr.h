@@ -247,7 +247,7 @@ rtr_status rtr_shot352(rtr_context* ctx, const float* d_pts, const float* d_norm
                        float* d_lrf, rtr_stream_t stream);
 
 /* Descriptor 1-NN on the tensor cores (the all-pairs loop of
- * RealTimeRobot.cpp:73-102 in its spec form): BF16 (hi + lo split)
+ * RealTimeRobot.cpp:73-102, recast as SHOT 1-NN): BF16 (hi + lo split)
  * tcgen05 GEMM with FP32 accumulation, per-query top-8, exact FP32 re-rank and
  * a certified error bound (uncertified queries are re-scanned exactly).  The
  * indices and distances equal rtr_match_exact's bit for bit. */
@@ -264,7 +264,7 @@ rtr_status rtr_match_exact(rtr_context* ctx, const float* d_query, int n_query,
                            rtr_stream_t stream);
 
 /* Geometric-consistency grouping (Chen & Bhanu 2007, PCL
- * GeometricConsistencyGrouping) — the spec form of the reference's
+ * GeometricConsistencyGrouping), which takes the place of the reference's
  * pair-consensus loop (Ransac, function.h:35-109).  Correspondence i pairs
  * model keypoint d_corr_m[i] with scene keypoint d_corr_s[i] at descriptor
  * distance d_corr_d[i].  Correspondences are taken in ascending distance
@@ -274,8 +274,10 @@ rtr_status rtr_match_exact(rtr_context* ctx, const float* d_query, int n_query,
  * gc_thresh members becomes a cluster and its members are taken.  Outputs, for
  * the first max_clusters clusters: members (original correspondence indices,
  * max_members per row, -1 padded), sizes, and the least-squares model->scene
- * pose (row-major 4x4, FP64).  Synchronises (the commit walk is host-driven).
- * Consensus sets longer than 128 members return RTR_ERR_CAPACITY. */
+ * pose (row-major 4x4, FP64).  The walk runs on the device in one cooperative
+ * launch; the call synchronises once, to return the cluster count.  Consensus
+ * sets longer than 128 members, or more than 1,474,560 correspondences,
+ * return RTR_ERR_CAPACITY. */
 rtr_status rtr_gc_group(rtr_context* ctx, const float* d_model_kp, const float* d_scene_kp,
                         const int32_t* d_corr_m, const int32_t* d_corr_s, const float* d_corr_d,
                         int n_corr, float gc_size, int gc_thresh, int max_clusters,

@@ -1,5 +1,5 @@
 // gc.cu — geometric-consistency grouping (Chen & Bhanu 2007; PCL
-// GeometricConsistencyGrouping), the spec stand-in for the reference's
+// GeometricConsistencyGrouping), which takes the place of the reference's
 // pair-consensus loop (Ransac, function.h:35-109).
 //
 // Semantics (shared with the oracle): correspondences sorted by descriptor
@@ -9,14 +9,15 @@
 // member differ by at most gc_size; a set of >= gc_thresh members becomes a
 // cluster and its members are taken.
 //
-// GPU form.  The sequential loop is O(C^2); its parallel part is computing
-// every seed's set.  Pass 1 computes all sets speculatively (no correspondence
-// taken), warp per seed, candidates streamed through shared memory in tiles.
-// The commit loop then walks seeds in order: a seed whose stored set does not
-// intersect anything taken since it was computed is exact (removing rejected
-// candidates never changes a greedy walk); the first exact seed with a large
-// set commits; seeds whose set intersects the commit are marked stale and are
-// recomputed, in parallel, when the walk reaches them.
+// GPU form.  The sequential loop is O(C^2) but its parallel part, each
+// seed's set, is only needed for the seeds the walk reaches before it stops
+// (at max_clusters, often a few hundred seeds into a cluttered scene).  One
+// cooperative launch alternates two phases: all warps compute the sets of a
+// window of upcoming seeds under the current taken state, then one warp walks
+// the seeds in order and commits.  A stored set stays exact while none of its
+// members is taken (removing rejected candidates never changes a greedy
+// walk); the walk stops at the first seed whose set lost a member and the
+// next window starts there.  No host round trip inside the grouping.
 #include "common.cuh"
 #include "pose.cuh"
 #include "grid.cuh"
@@ -32,10 +33,9 @@ struct GcDev {
   const float4* ps;        // scene keypoint of sorted correspondence a
   int C;
   float gc;
-  const unsigned* taken;   // bitset over sorted positions
+  unsigned* taken;         // bitset over sorted positions
   int* set_size;           // [C]
   int* set_mem;            // [C][GC_MAXS] sorted positions
-  int* stale;              // [C]
 };
 
 __device__ __forceinline__ bool gc_consistent(float4 am, float4 as, float4 bm, float4 bs, float gc) {
@@ -44,107 +44,223 @@ __device__ __forceinline__ bool gc_consistent(float4 am, float4 as, float4 bm, f
   return !(fabsf(__fsub_rn(dm, ds)) > gc);
 }
 
-__device__ __forceinline__ bool bit(const unsigned* b, int i) { return (b[i >> 5] >> (i & 31)) & 1u; }
+// Device-side control block of the grouping walk.
+struct GcCoop {
+  int* ctl;            // [0] walk position, [1] clusters, [2] done, [3] error status, [4] rounds
+  unsigned* arrive;    // grid barrier counter (zero at launch)
+  int* computed;       // [C] 1 once the seed's set has been computed
+  int* cl_members;     // [max_clusters][GC_MAXS] sorted positions
+  int* cl_sizes;       // [max_clusters]
+  int thresh, max_clusters;
+  long long budget;    // clock64 cycles per barrier wait
+  int* status;         // context status word
+};
 
-// Pass over seeds listed in `seeds` (or all seeds 0..C-1 when seeds == NULL).
-__global__ void __launch_bounds__(GC_WARPS * 32) k_gc_sets(GcDev g, const int* __restrict__ seeds,
-                                                           const int* __restrict__ n_seeds) {
+__device__ __forceinline__ bool sbit(const unsigned* s, int i) { return (s[i >> 5] >> (i & 31)) & 1u; }
+
+// Grid barrier (all blocks co-resident: cooperative launch).  Bounded: a
+// block that waits longer than the budget records RTR_ERR_TIMEOUT and
+// returns false.
+__device__ __forceinline__ bool gc_barrier(const GcCoop& c, unsigned target, int* s_ok) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(c.arrive, 1u);
+    const long long t0 = clock64();
+    int ok = 1;
+    while (ld_acquire_gpu(c.arrive) < target) {
+      if (clock64() - t0 > c.budget) {
+        atomicExch(c.status, (int)RTR_ERR_TIMEOUT);
+        atomicExch(c.ctl + 3, (int)RTR_ERR_TIMEOUT);
+        ok = 0;
+        break;
+      }
+      __nanosleep(32);
+    }
+    *s_ok = ok;
+  }
+  __syncthreads();
+  return *s_ok != 0;
+}
+
+// The whole grouping in one cooperative launch.  Rounds of two phases:
+//  A. every warp takes one seed of the window [pos, pos + warps) and, unless
+//     the seed is taken or its stored set is still exact (no member taken
+//     since it was computed), computes its consensus set under the current
+//     taken state: candidates streamed through shared memory in tiles;
+//  B. warp 0 of block 0 walks the seeds in order from pos: taken seeds are
+//     skipped, a seed whose set lost a member to a commit of this walk ends
+//     the round (it is recomputed by the next phase A), a set of >= thresh
+//     members commits.  The walk also ends at the window's end, at the last
+//     seed, or at max_clusters.
+// Every round advances the walk by at least one seed (the seed at pos is
+// exact when phase B starts), so the loop ends.
+__global__ void __launch_bounds__(GC_WARPS * 32) k_gc_coop(GcDev g, GcCoop c) {
+  extern __shared__ unsigned s_taken[];  // copy of the taken bitset
   __shared__ float4 tm[GC_TILE], ts[GC_TILE];
   __shared__ float4 mem_m[GC_WARPS][GC_MAXS], mem_s[GC_WARPS][GC_MAXS];
+  __shared__ int s_pos, s_done, s_ok;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int ns = seeds ? *n_seeds : g.C;
-  for (int base = blockIdx.x * GC_WARPS; base < ns; base += gridDim.x * GC_WARPS) {
-    const int si = base + wid;
-    const int a = si < ns ? (seeds ? seeds[si] : si) : -1;
-    const bool active = a >= 0 && !bit(g.taken, a);
-    float4 am = make_float4(0, 0, 0, 0), as = am;
-    if (a >= 0) {
-      am = g.pm[a];
-      as = g.ps[a];
+  const int nwords = (g.C + 31) >> 5;
+  const int W = gridDim.x * GC_WARPS;
+  if (threadIdx.x == 0) {
+    s_pos = 0;
+    s_done = 0;
+  }
+  unsigned target = 0;
+  for (int round = 0;; ++round) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < nwords; i += blockDim.x) s_taken[i] = __ldcg(g.taken + i);
+    __syncthreads();
+    const int pos = s_pos;
+    // ---- phase A
+    const int a = pos + blockIdx.x * GC_WARPS + wid;
+    bool need = false;
+    if (a < g.C && !sbit(s_taken, a)) {
+      if (!__ldcg(c.computed + a)) {
+        need = true;
+      } else {
+        const int n = min(__ldcg(g.set_size + a), GC_MAXS);
+        bool st = false;
+        for (int k = lane; k < n; k += 32) st |= sbit(s_taken, __ldcg(g.set_mem + (size_t)a * GC_MAXS + k));
+        need = __any_sync(0xffffffffu, st);
+      }
     }
-    int cnt = 1;  // the seed itself is member 0
-    if (lane == 0) {
-      mem_m[wid][0] = am;
-      mem_s[wid][0] = as;
-    }
-    __syncwarp();
-    for (int t0 = 0; t0 < g.C; t0 += GC_TILE) {
-      __syncthreads();
-      for (int i = threadIdx.x; i < GC_TILE; i += blockDim.x) {
-        const int b = t0 + i;
-        if (b < g.C) {
-          tm[i] = g.pm[b];
-          ts[i] = g.ps[b];
+    if (__syncthreads_or(need ? 1 : 0)) {
+      float4 am = make_float4(0, 0, 0, 0), as = am;
+      if (need) {
+        am = __ldg(g.pm + a);
+        as = __ldg(g.ps + a);
+        if (lane == 0) {
+          mem_m[wid][0] = am;
+          mem_s[wid][0] = as;
         }
       }
-      __syncthreads();
-      if (!active) continue;
-      const int tn = min(GC_TILE, g.C - t0);
-      for (int c0 = 0; c0 < tn; c0 += 32) {
-        const int b = t0 + c0 + lane;
-        bool cand = false;
-        if (c0 + lane < tn && b != a && !bit(g.taken, b))
-          cand = gc_consistent(am, as, tm[c0 + lane], ts[c0 + lane], g.gc);
-        unsigned bal = __ballot_sync(0xffffffffu, cand);
-        while (bal) {  // ascending candidate order
-          const int src = __ffs(bal) - 1;
-          bal &= bal - 1;
-          const float4 cm = tm[c0 + src], cs = ts[c0 + src];
-          // consistency with members 1..cnt-1 (member 0, the seed, already checked)
-          bool ok = true;
-          const int stored = min(cnt, GC_MAXS);
-          for (int m0 = 1; m0 < stored; m0 += 32) {
-            const int m = m0 + lane;
-            const bool bad = m < stored && !gc_consistent(mem_m[wid][m], mem_s[wid][m], cm, cs, g.gc);
-            if (__any_sync(0xffffffffu, bad)) {
-              ok = false;
-              break;
-            }
+      int cnt = 1;  // the seed itself is member 0
+      __syncwarp();
+      for (int t0 = 0; t0 < g.C; t0 += GC_TILE) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < GC_TILE; i += blockDim.x) {
+          const int b = t0 + i;
+          if (b < g.C) {
+            tm[i] = __ldg(g.pm + b);
+            ts[i] = __ldg(g.ps + b);
           }
-          if (ok) {
-            if (cnt >= GC_MAXS) {  // set longer than supported: reported by the caller
+        }
+        __syncthreads();
+        if (!need) continue;
+        const int tn = min(GC_TILE, g.C - t0);
+        for (int c0 = 0; c0 < tn; c0 += 32) {
+          const int b = t0 + c0 + lane;
+          bool cand = false;
+          if (c0 + lane < tn && b != a && !sbit(s_taken, b))
+            cand = gc_consistent(am, as, tm[c0 + lane], ts[c0 + lane], g.gc);
+          unsigned bal = __ballot_sync(0xffffffffu, cand);
+          while (bal) {  // ascending candidate order
+            const int src = __ffs(bal) - 1;
+            bal &= bal - 1;
+            const float4 cm = tm[c0 + src], cs = ts[c0 + src];
+            // consistency with members 1..cnt-1 (member 0, the seed, already checked)
+            bool ok = true;
+            const int stored = min(cnt, GC_MAXS);
+            for (int m0 = 1; m0 < stored; m0 += 32) {
+              const int m = m0 + lane;
+              const bool bad = m < stored && !gc_consistent(mem_m[wid][m], mem_s[wid][m], cm, cs, g.gc);
+              if (__any_sync(0xffffffffu, bad)) {
+                ok = false;
+                break;
+              }
+            }
+            if (ok) {
+              if (cnt >= GC_MAXS) {  // longer than supported: reported by the walk
+                ++cnt;
+                continue;
+              }
+              if (lane == 0) {
+                mem_m[wid][cnt] = cm;
+                mem_s[wid][cnt] = cs;
+                g.set_mem[(size_t)a * GC_MAXS + cnt] = t0 + c0 + src;
+              }
               ++cnt;
-              continue;
+              __syncwarp();
             }
-            if (lane == 0) {
-              mem_m[wid][cnt] = cm;
-              mem_s[wid][cnt] = cs;
-              g.set_mem[(size_t)a * GC_MAXS + cnt] = t0 + c0 + src;
-            }
-            ++cnt;
-            __syncwarp();
           }
         }
       }
+      if (need && lane == 0) {
+        g.set_mem[(size_t)a * GC_MAXS] = a;
+        g.set_size[a] = cnt;
+        c.computed[a] = 1;
+      }
     }
-    if (a >= 0 && lane == 0) {
-      if (active) g.set_mem[(size_t)a * GC_MAXS] = a;
-      g.set_size[a] = active ? cnt : 0;
-      g.stale[a] = 0;
-    }
-  }
-}
-
-// First seed >= pos that is not taken and either stale or large.
-__global__ void k_gc_find(GcDev g, int pos, int thresh, int* out) {
-  int best = 0x7fffffff;
-  for (int a = pos + blockIdx.x * blockDim.x + threadIdx.x; a < g.C; a += gridDim.x * blockDim.x) {
-    if (bit(g.taken, a)) continue;
-    if (g.stale[a] == 1 || g.set_size[a] >= thresh) {
-      best = a;
-      break;
-    }
-  }
+    target += gridDim.x;
+    if (!gc_barrier(c, target, &s_ok)) return;
+    // ---- phase B
+    if (blockIdx.x == 0 && wid == 0) {
+      int ncl = __ldcg(c.ctl + 1), err = 0;
+      bool done = false;
+      int p = pos;
+      const int wend = min(pos + W, g.C);
+      while (p < wend) {
+        if (sbit(s_taken, p)) {
+          ++p;
+          continue;
+        }
+        const int n = __ldcg(g.set_size + p);
+        const int ns = min(n, GC_MAXS);
+        int mb[GC_MAXS / 32];
+        bool st = false;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) best = min(best, __shfl_xor_sync(0xffffffffu, best, o));
-  if ((threadIdx.x & 31) == 0 && best != 0x7fffffff) atomicMin(out, best);
-}
-
-// Copy the found seed's state next to it for one host read.
-__global__ void k_gc_peek(GcDev g, int* misc) {
-  const int a = misc[0];
-  misc[1] = a < g.C ? g.stale[a] : 0;
-  misc[2] = a < g.C ? g.set_size[a] : 0;
+        for (int q = 0; q < GC_MAXS / 32; ++q) {
+          const int k = lane + 32 * q;
+          mb[q] = k < ns ? __ldcg(g.set_mem + (size_t)p * GC_MAXS + k) : -1;
+          if (mb[q] >= 0 && sbit(s_taken, mb[q])) st = true;
+        }
+        if (__any_sync(0xffffffffu, st)) break;  // lost a member: recompute from p
+        if (n >= c.thresh) {
+          if (n > GC_MAXS) {
+            err = (int)RTR_ERR_CAPACITY;
+            done = true;
+            break;
+          }
+#pragma unroll
+          for (int q = 0; q < GC_MAXS / 32; ++q)
+            if (mb[q] >= 0) {
+              atomicOr(&s_taken[mb[q] >> 5], 1u << (mb[q] & 31));
+              c.cl_members[(size_t)ncl * GC_MAXS + lane + 32 * q] = mb[q];
+            }
+          if (lane == 0) c.cl_sizes[ncl] = n;
+          __syncwarp();
+          ++ncl;
+          if (ncl >= c.max_clusters) {
+            done = true;
+            ++p;
+            break;
+          }
+        }
+        ++p;
+      }
+      if (p >= g.C) done = true;
+      __syncwarp();
+      for (int i = lane; i < nwords; i += 32) g.taken[i] = s_taken[i];
+      if (lane == 0) {
+        c.ctl[0] = p;
+        c.ctl[1] = ncl;
+        c.ctl[2] = done ? 1 : 0;
+        if (err) c.ctl[3] = err;
+        c.ctl[4] = round + 1;
+      }
+      __syncwarp();
+    }
+    target += gridDim.x;
+    if (!gc_barrier(c, target, &s_ok)) return;
+    if (threadIdx.x == 0) {
+      s_pos = __ldcg(c.ctl + 0);
+      s_done = __ldcg(c.ctl + 2) || __ldcg(c.ctl + 3);
+    }
+    __syncthreads();
+    if (s_done) break;
+  }
 }
 
 // Members as original correspondence indices.
@@ -155,46 +271,6 @@ __global__ void k_gc_members_out(const int* __restrict__ mem, const int* __restr
     const int c = i / max_members, k = i - c * max_members;
     out[i] = k < sizes[c] ? (int)order[mem[(size_t)c * stride + k]] : -1;
   }
-}
-
-// Commit seed a: take its members (recomputed exactly when the set was too
-// long to store: then the walk is redone here by one warp).
-__global__ void k_gc_commit(GcDev g, int a, unsigned* taken, int* newly, int* cluster_members,
-                            int* cluster_size, int cid, int max_members) {
-  const int n = g.set_size[a];
-  const int stored = min(n, GC_MAXS);
-  for (int k = threadIdx.x; k < stored; k += blockDim.x) {
-    const int b = g.set_mem[(size_t)a * GC_MAXS + k];
-    atomicOr(&taken[b >> 5], 1u << (b & 31));
-    newly[b] = 1;
-    if (k < max_members) cluster_members[(size_t)cid * max_members + k] = b;
-  }
-  if (threadIdx.x == 0) cluster_size[cid] = stored;
-}
-
-// Seeds after `a` whose stored set touches the commit become stale.
-__global__ void k_gc_invalidate(GcDev g, int a, const int* __restrict__ newly) {
-  for (int s = a + 1 + blockIdx.x * blockDim.x + threadIdx.x; s < g.C; s += gridDim.x * blockDim.x) {
-    if (bit(g.taken, s) || g.stale[s]) continue;
-    const int n = min(g.set_size[s], GC_MAXS);
-    for (int k = 0; k < n; ++k)
-      if (newly[g.set_mem[(size_t)s * GC_MAXS + k]]) {
-        g.stale[s] = 1;
-        break;
-      }
-  }
-}
-
-__global__ void k_gc_clear_newly(int* newly, const int* __restrict__ cluster_members, const int* cluster_size,
-                                 int cid, int max_members) {
-  const int n = cluster_size[cid];
-  for (int k = threadIdx.x; k < n && k < max_members; k += blockDim.x) newly[cluster_members[(size_t)cid * max_members + k]] = 0;
-}
-
-// Stale seeds in [pos, C) -> compact list (ascending).
-__global__ void k_gc_stale_list(GcDev g, int pos, int* list, int* n) {
-  for (int a = pos + blockIdx.x * blockDim.x + threadIdx.x; a < g.C; a += gridDim.x * blockDim.x)
-    if (g.stale[a] && !bit(g.taken, a)) list[atomicAdd(n, 1)] = a;
 }
 
 // Gather the sorted correspondence endpoints.
@@ -273,7 +349,8 @@ struct GcBufs {
   uint32_t *k0, *v0, *k1, *v1, *hist;
   float4 *pm, *ps;
   unsigned* taken;
-  int *set_size, *set_mem, *stale, *newly, *list, *misc;
+  int *set_size, *set_mem, *computed, *misc;
+  unsigned* arrive;
   int *members, *sizes;
   double* poses;
 };
@@ -288,9 +365,8 @@ static void gc_plan(ScratchPlan& p, int C, int max_clusters, int max_members) {
   p.add<int>(n);
   p.add<int>((size_t)n * GC_MAXS);
   p.add<int>(n);
-  p.add<int>(n);
-  p.add<int>(n);
   p.add<int>(16);
+  p.add<unsigned>(1);
   p.add<int>((size_t)max_clusters * max_members);
   p.add<int>(max_clusters);
   p.add<double>((size_t)max_clusters * 16);
@@ -308,15 +384,17 @@ static bool gc_take(Scratch& s, int C, int max_clusters, int max_members, GcBufs
   b->taken = s.take<unsigned>((n + 31) / 32);
   b->set_size = s.take<int>(n);
   b->set_mem = s.take<int>((size_t)n * GC_MAXS);
-  b->stale = s.take<int>(n);
-  b->newly = s.take<int>(n);
-  b->list = s.take<int>(n);
+  b->computed = s.take<int>(n);
   b->misc = s.take<int>(16);
+  b->arrive = s.take<unsigned>(1);
   b->members = s.take<int>((size_t)max_clusters * max_members);
   b->sizes = s.take<int>(max_clusters);
   b->poses = s.take<double>((size_t)max_clusters * 16);
   return b->poses != nullptr;
 }
+
+// Shared memory of k_gc_coop beyond its static part: the taken bitset.
+constexpr size_t GC_MAX_DYN_SMEM = 180 * 1024;
 
 }  // namespace rtr
 
@@ -339,51 +417,52 @@ rtr_status gc_group_dev(rtr_context* ctx, Scratch& s, const float* d_model_kp, c
   const int C = n_corr;
   GcBufs b;
   if (!gc_take(s, C, max_clusters, GC_MAXS, &b)) return fail(RTR_ERR_CAPACITY, "rtr_gc_group: scratch");
-  ProfScope ps(ctx, st, "gc_group");
   const int nb = (C + 255) / 256 > 152 * 8 ? 152 * 8 : (C + 255) / 256;
   k_gc_keys<<<nb, 256, 0, st>>>(d_corr_d, C, b.k0);
   uint32_t *ks, *vs;
   radix_sort_pairs(b.k0, b.v0, b.k1, b.v1, b.hist, C, C, nullptr, 32, true, st, &ks, &vs);
   k_gc_gather<<<nb, 256, 0, st>>>(reinterpret_cast<const float4*>(d_model_kp),
                                   reinterpret_cast<const float4*>(d_scene_kp), d_corr_m, d_corr_s, vs, C, b.pm, b.ps);
-  RTR_CUDA(cudaMemsetAsync(b.taken, 0, sizeof(unsigned) * ((C + 31) / 32), st));
-  RTR_CUDA(cudaMemsetAsync(b.stale, 0, sizeof(int) * C, st));
-  RTR_CUDA(cudaMemsetAsync(b.newly, 0, sizeof(int) * C, st));
-  GcDev g{b.pm, b.ps, C, gc_size, b.taken, b.set_size, b.set_mem, b.stale};
-  int sb = (C + GC_WARPS - 1) / GC_WARPS;
-  if (sb > 152 * 4) sb = 152 * 4;
-  k_gc_sets<<<sb, GC_WARPS * 32, 0, st>>>(g, nullptr, nullptr);
-  RTR_LAUNCHED(5);
-  int pos = 0, ncl = 0;
-  int* h = ctx->h_pin;
-  for (int guard = 0; guard < 4 * C + 16 && ncl < max_clusters; ++guard) {
-    RTR_CUDA(cudaMemsetAsync(b.misc, 0x7f, sizeof(int), st));
-    k_gc_find<<<nb, 256, 0, st>>>(g, pos, gc_thresh, b.misc);
-    k_gc_peek<<<1, 1, 0, st>>>(g, b.misc);
-    RTR_LAUNCHED(2);
-    RTR_CUDA(cudaMemcpyAsync(h, b.misc, 3 * sizeof(int), cudaMemcpyDeviceToHost, st));
-    RTR_CUDA(cudaStreamSynchronize(st));
-    const int a = h[0];
-    if (a >= C || a < 0) break;
-    if (h[2] > GC_MAXS)
-      return fail(RTR_ERR_CAPACITY, "rtr_gc_group: a consensus set exceeds %d members", GC_MAXS);
-    if (h[1] == 1) {
-      // recompute every stale seed from a on, under the current taken state
-      RTR_CUDA(cudaMemsetAsync(b.misc + 4, 0, sizeof(int), st));
-      k_gc_stale_list<<<nb, 256, 0, st>>>(g, a, b.list, b.misc + 4);
-      k_gc_sets<<<sb, GC_WARPS * 32, 0, st>>>(g, b.list, b.misc + 4);
-      RTR_LAUNCHED(2);
-      pos = a;
-      continue;
-    }
-    // exact seed with a large set: commit
-    k_gc_commit<<<1, 128, 0, st>>>(g, a, b.taken, b.newly, b.members, b.sizes, ncl, GC_MAXS);
-    k_gc_invalidate<<<nb, 256, 0, st>>>(g, a, b.newly);
-    k_gc_clear_newly<<<1, 128, 0, st>>>(b.newly, b.members, b.sizes, ncl, GC_MAXS);
-    RTR_LAUNCHED(3);
-    ++ncl;
-    pos = a + 1;
+  const size_t dyn = sizeof(unsigned) * (size_t)((C + 31) / 32);
+  if (dyn > GC_MAX_DYN_SMEM)
+    return fail(RTR_ERR_CAPACITY, "rtr_gc_group: %d correspondences exceed the supported %d", C,
+                (int)(GC_MAX_DYN_SMEM * 8));
+  RTR_CUDA(cudaMemsetAsync(b.taken, 0, dyn, st));
+  RTR_CUDA(cudaMemsetAsync(b.computed, 0, sizeof(int) * C, st));
+  RTR_CUDA(cudaMemsetAsync(b.misc, 0, sizeof(int) * 16, st));
+  RTR_CUDA(cudaMemsetAsync(b.arrive, 0, sizeof(unsigned), st));
+  GcDev g{b.pm, b.ps, C, gc_size, b.taken, b.set_size, b.set_mem};
+  GcCoop c{b.misc, b.arrive, b.computed, b.members, b.sizes, gc_thresh, max_clusters,
+           ctx->wait_budget_cycles, ctx->d_status};
+  RTR_CUDA(cudaFuncSetAttribute(k_gc_coop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+  int per_sm = 0;
+  RTR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gc_coop, GC_WARPS * 32, dyn));
+  if (per_sm < 1) return fail(RTR_ERR_CAPACITY, "rtr_gc_group: grouping kernel does not fit an SM");
+  const int blocks = (per_sm < 2 ? per_sm : 2) * ctx->num_sms;
+  {
+    ProfScope pw(ctx, st, "gc_walk");
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(GC_WARPS * 32);
+    cfg.dynamicSmemBytes = dyn;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    RTR_CUDA(cudaLaunchKernelEx(&cfg, k_gc_coop, g, c));
   }
+  RTR_LAUNCHED(3);
+  int* h = ctx->h_pin;
+  RTR_CUDA(cudaMemcpyAsync(h, b.misc, 5 * sizeof(int), cudaMemcpyDeviceToHost, st));
+  RTR_CUDA(cudaStreamSynchronize(st));
+  const int ncl = h[1];
+  if (h[3] == (int)RTR_ERR_CAPACITY)
+    return fail(RTR_ERR_CAPACITY, "rtr_gc_group: a consensus set exceeds %d members", GC_MAXS);
+  if (h[3] == (int)RTR_ERR_TIMEOUT)
+    return fail(RTR_ERR_TIMEOUT, "rtr_gc_group: a grid barrier wait exceeded the budget");
+  ctx->gc_rounds = h[4];
   if (ncl > 0) {
     k_gc_poses<<<(ncl + 3) / 4, 128, 0, st>>>(b.pm, b.ps, b.members, b.sizes, ncl, GC_MAXS, b.poses);
     RTR_LAUNCHED(1);
@@ -417,6 +496,7 @@ extern "C" rtr_status rtr_gc_group(rtr_context* ctx, const float* d_model_kp, co
   RTR_CUDA(cudaSetDevice(ctx->device));
   Scratch s;
   RTR_TRY(ensure_scratch(ctx, gc_scratch_bytes(n_corr, max_clusters), st, &s));
+  ProfScope ps(ctx, st, "gc_group");
   return gc_group_dev(ctx, s, d_model_kp, d_scene_kp, d_corr_m, d_corr_s, d_corr_d, n_corr, gc_size, gc_thresh,
                       max_clusters, max_members, d_members, d_sizes, d_poses, h_n_clusters, st);
 }

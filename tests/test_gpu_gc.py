@@ -82,3 +82,51 @@ def test_gc_no_correspondences(ctx):
     ef = torch.zeros(0, dtype=torch.float32, device="cuda")
     mem, sizes, poses = ctx.gc_group(e4, e4, ei, ei, ef)
     assert len(sizes) == 0
+
+
+def _random_scene(seed, nm, ns, C, spread=2.0):
+    rng = np.random.default_rng(seed)
+    mk = np.zeros((nm, 4), np.float32)
+    mk[:, :3] = rng.uniform(-0.3, 0.3, (nm, 3))
+    sk = np.zeros((ns, 4), np.float32)
+    sk[:, :3] = rng.uniform(-spread, spread, (ns, 3))
+    cm = rng.integers(0, nm, C).astype(np.int32)
+    cs = rng.integers(0, ns, C).astype(np.int32)
+    cd = rng.uniform(0, 0.3, C).astype(np.float32)
+    cd[rng.choice(C, C // 10, replace=False)] = cd[0]  # many equal distances: ties keep input order
+    return mk, sk, cm, cs, cd
+
+
+@pytest.mark.parametrize("maxc", [1, 7, 256])
+def test_gc_many_clusters_walk_stops_at_cap(ctx, maxc):
+    # random correspondences in a small scene: nearly every seed forms a
+    # cluster, so the walk commits densely, loses members to earlier commits
+    # (recomputed sets) and stops at max_clusters
+    mk, sk, cm, cs, cd = _random_scene(3, 600, 4000, 20000, 0.5)
+    n = _check(ctx, mk, sk, cm, cs, cd, 0.01, 3, maxc)
+    assert n == maxc
+
+
+def test_gc_walk_reaches_the_end(ctx):
+    # few clusters form: the walk runs past many windows to the last seed
+    mk, sk, cm, cs, cd = _random_scene(4, 300, 3000, 9000, 3.0)
+    _check(ctx, mk, sk, cm, cs, cd, 0.005, 4, 256)
+
+
+def test_gc_wait_budget_runs_out_then_recovers(rtr):
+    # a grid-barrier wait with no budget left returns RTR_ERR_TIMEOUT and the
+    # context stays usable; the same call with the normal budget is exact
+    mk, sk, cm, cs, cd = _random_scene(5, 600, 4000, 20000, 0.5)
+    c = rtr.Context(0)
+    try:
+        args = (_dev(mk), _dev(sk), _dev(cm, np.int32), _dev(cs, np.int32), _dev(cd), 0.01, 3, 64, 128)
+        c.set_wait_budget_ms(1e-6)
+        with pytest.raises(rtr.RtrError, match="RTR_ERR_TIMEOUT"):
+            c.gc_group(*args)
+        with pytest.raises(rtr.RtrError, match="RTR_ERR_TIMEOUT"):
+            c.check()  # the device status word saw it too (and is cleared by reading)
+        c.set_wait_budget_ms(2000.0)
+        c.check()
+        _check(c, mk, sk, cm, cs, cd, 0.01, 3, 64)
+    finally:
+        c.close()
