@@ -283,6 +283,10 @@ rtr_status rtr_gc_group(rtr_context* ctx, const float* d_model_kp, const float* 
                         int n_corr, float gc_size, int gc_thresh, int max_clusters,
                         int max_members, int32_t* d_members, int32_t* d_sizes,
                         double* d_poses, int* h_n_clusters, rtr_stream_t stream);
+/* Work of the last grouping on this context: h_stats3[0] = rounds of the
+ * window/walk loop, [1] = position where the walk ended, [2] = consensus
+ * sets computed (including recomputations).  No synchronisation. */
+rtr_status rtr_gc_stats(rtr_context* ctx, int* h_stats3);
 
 /* ---- recognition pipeline ------------------------------------------------
  * The whole chain of main (RealTimeRobot.cpp:39-105) for one known object

@@ -140,6 +140,7 @@ _SIG = {
     "rtr_match_stats": (_I, [_P, C.POINTER(C.c_int)]),
     "rtr_gc_group": (_I, [_P, _P, _P, _P, _P, _P, _I, _F, _I, _I, _I, _P, _P, _P,
                           C.POINTER(C.c_int), _P]),
+    "rtr_gc_stats": (_I, [_P, C.POINTER(C.c_int * 3)]),
     "rtr_recog_default_params": (None, [C.POINTER(RecogParams)]),
     "rtr_model_create": (_I, [_P, _P, _I, C.POINTER(RecogParams), C.POINTER(_P)]),
     "rtr_model_destroy": (_I, [_P]),
@@ -397,6 +398,12 @@ class Context:
         check(lib().rtr_match_exact(self.h, _ptr(q), q.shape[0], _ptr(db), db.shape[0], _ptr(idx),
                                     _ptr(d2), _stream(stream)))
         return idx, d2
+
+    def gc_stats(self) -> dict:
+        """Work of the last grouping: rounds, walk end position, sets computed."""
+        v = (C.c_int * 3)()
+        check(lib().rtr_gc_stats(self.h, C.byref(v)))
+        return {"rounds": v[0], "walk_end": v[1], "sets": v[2]}
 
     def gc_group(self, model_kp, scene_kp, corr_m, corr_s, corr_d, gc_size=0.01, gc_thresh=5,
                  max_clusters=64, max_members=128, stream=None):

@@ -71,7 +71,7 @@ struct rtr_context {
   size_t io_bytes = 0;
   cudaStream_t host_stream = nullptr;  // stream of the host-pointer entry points
   int* h_pin = nullptr;                // 64 pinned ints for small device->host reads
-  int gc_rounds = 0;                   // rounds of the last grouping walk
+  int gc_stats[3] = {0, 0, 0};         // last grouping: rounds, walk end, sets computed
   bool profiling = false;
   std::vector<rtr_prof_rec> prof;      // recorded stages (in order)
   std::vector<cudaEvent_t> event_pool; // reusable events

@@ -25,7 +25,6 @@
 namespace rtr {
 
 constexpr int GC_WARPS = 8;
-constexpr int GC_TILE = 256;
 constexpr int GC_MAXS = 128;  // members per consensus set (larger sets: RTR_ERR_CAPACITY)
 
 struct GcDev {
@@ -38,15 +37,36 @@ struct GcDev {
   int* set_mem;            // [C][GC_MAXS] sorted positions
 };
 
-__device__ __forceinline__ bool gc_consistent(float4 am, float4 as, float4 bm, float4 bs, float gc) {
-  const float dm = __fsqrt_rn(dist2_exact(am, bm));
-  const float ds = __fsqrt_rn(dist2_exact(as, bs));
-  return !(fabsf(__fsub_rn(dm, ds)) > gc);
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// The consistency test of the oracle, !(|sqrt(dm2) - sqrt(ds2)| > gc) with
+// IEEE square roots, answered without them when the answer is certain:
+//  - ds2 > r2max: the scene distance exceeds the largest model distance plus
+//    gc (r2max carries a relative margin far above the rounding of both
+//    sides), so the test fails;
+//  - otherwise approximate roots (relative error far below 1e-5) decide
+//    unless |a - b| lies within 1e-5 (a + b) + 1e-6 of gc, where the exact
+//    form runs.  NaN differences fall through to the exact form.
+__device__ __forceinline__ bool gc_consistent(float4 am, float4 as, float4 bm, float4 bs, float gc, float r2max) {
+  const float v = dist2_exact(as, bs);
+  if (v > r2max) return false;
+  const float u = dist2_exact(am, bm);
+  const float a = sqrt_approx(u), b = sqrt_approx(v);
+  const float diff = fabsf(a - b);
+  const float tol = 1.0e-5f * (a + b) + 1.0e-6f;
+  if (diff > gc + tol) return false;
+  if (diff < gc - tol) return true;
+  return !(fabsf(__fsub_rn(__fsqrt_rn(u), __fsqrt_rn(v))) > gc);
 }
 
 // Device-side control block of the grouping walk.
 struct GcCoop {
-  int* ctl;            // [0] walk position, [1] clusters, [2] done, [3] error status, [4] rounds
+  int* ctl;            // [0] walk position, [1] clusters, [2] done, [3] error status, [4] rounds,
+                       // [5] sets computed, [6] seeds needing a set this round
   unsigned* arrive;    // grid barrier counter (zero at launch)
   int* computed;       // [C] 1 once the seed's set has been computed
   int* cl_members;     // [max_clusters][GC_MAXS] sorted positions
@@ -54,6 +74,11 @@ struct GcCoop {
   int thresh, max_clusters;
   long long budget;    // clock64 cycles per barrier wait
   int* status;         // context status word
+  const GridMeta* mbox;  // bounding box of the model endpoints
+  int* need;           // [win] seeds whose set is computed this round
+  unsigned* mask;      // [win][nwp] seed-test pass bits, one row per needed seed
+  int win;             // seeds per window
+  int nwp;             // words per mask row (C/32 rounded up to a multiple of 4)
 };
 
 __device__ __forceinline__ bool sbit(const unsigned* s, int i) { return (s[i >> 5] >> (i & 31)) & 1u; }
@@ -83,162 +108,260 @@ __device__ __forceinline__ bool gc_barrier(const GcCoop& c, unsigned target, int
   return *s_ok != 0;
 }
 
-// The whole grouping in one cooperative launch.  Rounds of two phases:
-//  A. every warp takes one seed of the window [pos, pos + warps) and, unless
-//     the seed is taken or its stored set is still exact (no member taken
-//     since it was computed), computes its consensus set under the current
-//     taken state: candidates streamed through shared memory in tiles;
-//  B. warp 0 of block 0 walks the seeds in order from pos: taken seeds are
-//     skipped, a seed whose set lost a member to a commit of this walk ends
-//     the round (it is recomputed by the next phase A), a set of >= thresh
-//     members commits.  The walk also ends at the window's end, at the last
-//     seed, or at max_clusters.
-// Every round advances the walk by at least one seed (the seed at pos is
-// exact when phase B starts), so the loop ends.
-__global__ void __launch_bounds__(GC_WARPS * 32) k_gc_coop(GcDev g, GcCoop c) {
+__device__ __forceinline__ float4 shfl4(float4 v, int src) {
+  return make_float4(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src),
+                     __shfl_sync(0xffffffffu, v.z, src), __shfl_sync(0xffffffffu, v.w, src));
+}
+
+constexpr int GC_PEND = 64;  // candidates staged per warp before admission
+
+// Greedy admission of the n (<= 32) staged candidates, in slot order, into
+// the warp's set (members in mem_m/mem_s; member 0 is the seed, which every
+// staged candidate already passed).
+__device__ __forceinline__ void gc_admit(const GcDev& g, int a, const int* slot, int n, float4* mem_m,
+                                         float4* mem_s, int& cnt, float r2max) {
+  const int lane = threadIdx.x & 31;
+  const int pj = lane < n ? slot[lane] : -1;
+  float4 cm_l = make_float4(0, 0, 0, 0), cs_l = cm_l;
+  if (pj >= 0) {
+    cm_l = __ldg(g.pm + pj);
+    cs_l = __ldg(g.ps + pj);
+  }
+  for (int t = 0; t < n; ++t) {
+    const int pb = __shfl_sync(0xffffffffu, pj, t);
+    const float4 cm = shfl4(cm_l, t), cs = shfl4(cs_l, t);
+    bool ok = true;
+    const int stored = min(cnt, GC_MAXS);
+    for (int m0 = 1; m0 < stored; m0 += 32) {
+      const int m = m0 + lane;
+      const bool bad = m < stored && !gc_consistent(mem_m[m], mem_s[m], cm, cs, g.gc, r2max);
+      if (__any_sync(0xffffffffu, bad)) {
+        ok = false;
+        break;
+      }
+    }
+    if (ok) {
+      if (cnt < GC_MAXS && lane == 0) {
+        mem_m[cnt] = cm;
+        mem_s[cnt] = cs;
+        g.set_mem[(size_t)a * GC_MAXS + cnt] = pb;
+      }
+      ++cnt;  // counted beyond GC_MAXS too: reported by the walk
+      __syncwarp();
+    }
+  }
+}
+
+// The whole grouping in one cooperative launch.  Each round:
+//  P. warps check the seeds of the window [pos, pos + win): a seed that is
+//     not taken and has no set yet, or whose set lost a member to a commit,
+//     joins this round's list;
+//  A1. seed tests of every listed seed against every candidate, spread over
+//     all warps (a warp loads 32 candidates once and tests them against 8
+//     seeds); the results are pass bitmasks in candidate order;
+//  A2. one warp per listed seed admits the passing candidates in ascending
+//     order, greedily, against the members so far;
+//  B.  warp 0 of block 0 walks the seeds in order from pos: taken seeds are
+//     skipped, a seed whose set lost a member ends the round (recomputed in
+//     the next one), a set of >= thresh members commits.  The walk also ends
+//     at the window's end, at the last seed, or at max_clusters.
+// A stored set stays exact while none of its members is taken (removing
+// rejected candidates never changes a greedy walk).  Every round advances the
+// walk by at least one seed (the seed at pos is exact when B starts).
+__global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c) {
   extern __shared__ unsigned s_taken[];  // copy of the taken bitset
-  __shared__ float4 tm[GC_TILE], ts[GC_TILE];
   __shared__ float4 mem_m[GC_WARPS][GC_MAXS], mem_s[GC_WARPS][GC_MAXS];
+  __shared__ int s_slot[GC_WARPS][GC_PEND];
+  __shared__ int s_bmem[32][32];  // walk: first 32 members of the next 32 seeds
+  __shared__ int s_bsize[32];
   __shared__ int s_pos, s_done, s_ok;
+  __shared__ float s_r2max;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int nwords = (g.C + 31) >> 5;
-  const int W = gridDim.x * GC_WARPS;
+  const int gw = blockIdx.x * GC_WARPS + wid, nwarps = gridDim.x * GC_WARPS;
   if (threadIdx.x == 0) {
     s_pos = 0;
     s_done = 0;
+    // largest model-side distance: the diagonal of the endpoints' box
+    float d2 = 0.f;
+    for (int k = 0; k < 3; ++k) {
+      const float e = ordered_to_float(c.mbox->bmax[k]) - ordered_to_float(c.mbox->bmin[k]);
+      d2 += e * e;
+    }
+    const float R = (sqrtf(d2) + g.gc) * 1.0001f + 1.0e-5f;
+    const float r2 = R * R * 1.0001f;
+    s_r2max = r2 < 3.0e38f ? r2 : __int_as_float(0x7f800000);
   }
+  __syncthreads();
+  const float r2max = s_r2max;
   unsigned target = 0;
   for (int round = 0;; ++round) {
     __syncthreads();
     for (int i = threadIdx.x; i < nwords; i += blockDim.x) s_taken[i] = __ldcg(g.taken + i);
     __syncthreads();
     const int pos = s_pos;
-    // ---- phase A
-    const int a = pos + blockIdx.x * GC_WARPS + wid;
-    bool need = false;
-    if (a < g.C && !sbit(s_taken, a)) {
-      if (!__ldcg(c.computed + a)) {
-        need = true;
-      } else {
-        const int n = min(__ldcg(g.set_size + a), GC_MAXS);
-        bool st = false;
-        for (int k = lane; k < n; k += 32) st |= sbit(s_taken, __ldcg(g.set_mem + (size_t)a * GC_MAXS + k));
-        need = __any_sync(0xffffffffu, st);
+    // ---- P: seeds that need a set this round
+    for (int t = gw; t < c.win; t += nwarps) {
+      const int a = pos + t;
+      bool need = false;
+      if (a < g.C && !sbit(s_taken, a)) {
+        if (!__ldcg(c.computed + a)) {
+          need = true;
+        } else {
+          const int n = min(__ldcg(g.set_size + a), GC_MAXS);
+          bool st = false;
+          for (int k = lane; k < n; k += 32) st |= sbit(s_taken, __ldcg(g.set_mem + (size_t)a * GC_MAXS + k));
+          need = __any_sync(0xffffffffu, st);
+        }
       }
+      if (need && lane == 0) c.need[atomicAdd(c.ctl + 6, 1)] = a;
     }
-    if (__syncthreads_or(need ? 1 : 0)) {
-      float4 am = make_float4(0, 0, 0, 0), as = am;
-      if (need) {
-        am = __ldg(g.pm + a);
-        as = __ldg(g.ps + a);
-        if (lane == 0) {
-          mem_m[wid][0] = am;
-          mem_s[wid][0] = as;
+    target += gridDim.x;
+    if (!gc_barrier(c, target, &s_ok)) return;
+    const int nneed = __ldcg(c.ctl + 6);
+    // ---- A1: seed tests -> pass bitmasks
+    if (nneed > 0) {
+      const int ngrp = (nneed + 7) >> 3;
+      const long long items = (long long)c.nwp * ngrp;
+      for (long long it = gw; it < items; it += nwarps) {
+        const int ch = (int)(it % c.nwp), grp = (int)(it / c.nwp);
+        const int b = ch * 32 + lane;
+        const bool okb = b < g.C && !sbit(s_taken, b);
+        float4 bm = make_float4(0, 0, 0, 0), bs = bm;
+        if (okb) {
+          bm = __ldg(g.pm + b);
+          bs = __ldg(g.ps + b);
         }
-      }
-      int cnt = 1;  // the seed itself is member 0
-      __syncwarp();
-      for (int t0 = 0; t0 < g.C; t0 += GC_TILE) {
-        __syncthreads();
-        for (int i = threadIdx.x; i < GC_TILE; i += blockDim.x) {
-          const int b = t0 + i;
-          if (b < g.C) {
-            tm[i] = __ldg(g.pm + b);
-            ts[i] = __ldg(g.ps + b);
-          }
+        const int kend = min(8, nneed - grp * 8);
+        for (int k = 0; k < kend; ++k) {
+          const int slot = grp * 8 + k;
+          const int a = __ldcg(c.need + slot);
+          const float4 am = __ldg(g.pm + a), as = __ldg(g.ps + a);
+          const bool pass = okb && b != a && gc_consistent(am, as, bm, bs, g.gc, r2max);
+          const unsigned bal = __ballot_sync(0xffffffffu, pass);
+          if (lane == 0) c.mask[(size_t)slot * c.nwp + ch] = bal;
         }
-        __syncthreads();
-        if (!need) continue;
-        const int tn = min(GC_TILE, g.C - t0);
-        for (int c0 = 0; c0 < tn; c0 += 32) {
-          const int b = t0 + c0 + lane;
-          bool cand = false;
-          if (c0 + lane < tn && b != a && !sbit(s_taken, b))
-            cand = gc_consistent(am, as, tm[c0 + lane], ts[c0 + lane], g.gc);
-          unsigned bal = __ballot_sync(0xffffffffu, cand);
-          while (bal) {  // ascending candidate order
-            const int src = __ffs(bal) - 1;
-            bal &= bal - 1;
-            const float4 cm = tm[c0 + src], cs = ts[c0 + src];
-            // consistency with members 1..cnt-1 (member 0, the seed, already checked)
-            bool ok = true;
-            const int stored = min(cnt, GC_MAXS);
-            for (int m0 = 1; m0 < stored; m0 += 32) {
-              const int m = m0 + lane;
-              const bool bad = m < stored && !gc_consistent(mem_m[wid][m], mem_s[wid][m], cm, cs, g.gc);
-              if (__any_sync(0xffffffffu, bad)) {
-                ok = false;
-                break;
-              }
-            }
-            if (ok) {
-              if (cnt >= GC_MAXS) {  // longer than supported: reported by the walk
-                ++cnt;
-                continue;
-              }
-              if (lane == 0) {
-                mem_m[wid][cnt] = cm;
-                mem_s[wid][cnt] = cs;
-                g.set_mem[(size_t)a * GC_MAXS + cnt] = t0 + c0 + src;
-              }
-              ++cnt;
-              __syncwarp();
-            }
-          }
-        }
-      }
-      if (need && lane == 0) {
-        g.set_mem[(size_t)a * GC_MAXS] = a;
-        g.set_size[a] = cnt;
-        c.computed[a] = 1;
       }
     }
     target += gridDim.x;
     if (!gc_barrier(c, target, &s_ok)) return;
-    // ---- phase B
+    // ---- A2: ordered admission, warp per listed seed
+    for (int slot = gw; slot < nneed; slot += nwarps) {
+      const int a = __ldcg(c.need + slot);
+      if (lane == 0) {
+        mem_m[wid][0] = __ldg(g.pm + a);
+        mem_s[wid][0] = __ldg(g.ps + a);
+        g.set_mem[(size_t)a * GC_MAXS] = a;
+      }
+      __syncwarp();
+      int cnt = 1, npend = 0;
+      const uint4* row = reinterpret_cast<const uint4*>(c.mask + (size_t)slot * c.nwp);
+      for (int w0 = 0; w0 < c.nwp; w0 += 128) {
+        unsigned wv[4] = {0u, 0u, 0u, 0u};
+        if (w0 + lane * 4 < c.nwp) {
+          const uint4 v = __ldcg(row + (w0 >> 2) + lane);
+          wv[0] = v.x;
+          wv[1] = v.y;
+          wv[2] = v.z;
+          wv[3] = v.w;
+        }
+        int rc = __popc(wv[0]) + __popc(wv[1]) + __popc(wv[2]) + __popc(wv[3]);
+        while (__any_sync(0xffffffffu, rc > 0)) {
+          int incl = rc;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+          }
+          const int total = __shfl_sync(0xffffffffu, incl, 31);
+          const int ex = incl - rc;
+          const int room = GC_PEND - npend;
+          // lanes whose lower neighbours all fit emit their first candidates
+          int take = min(max(room - ex, 0), rc);
+          int dst = npend + ex;
+          for (int q = 0; q < 4 && take > 0; ++q) {
+            while (wv[q] && take > 0) {
+              const int bit = __ffs(wv[q]) - 1;
+              wv[q] &= wv[q] - 1;
+              s_slot[wid][dst++] = (w0 + lane * 4 + q) * 32 + bit;
+              --take;
+              --rc;
+            }
+          }
+          npend += min(total, room);
+          __syncwarp();
+          while (npend >= 32) {
+            gc_admit(g, a, s_slot[wid], 32, mem_m[wid], mem_s[wid], cnt, r2max);
+            const int rest = npend - 32;
+            const int mv = lane < rest ? s_slot[wid][32 + lane] : 0;
+            __syncwarp();
+            if (lane < rest) s_slot[wid][lane] = mv;
+            npend = rest;
+            __syncwarp();
+          }
+        }
+      }
+      if (npend > 0) gc_admit(g, a, s_slot[wid], npend, mem_m[wid], mem_s[wid], cnt, r2max);
+      if (lane == 0) {
+        g.set_size[a] = cnt;
+        c.computed[a] = 1;
+        atomicAdd(c.ctl + 5, 1);
+      }
+      __syncwarp();
+    }
+    target += gridDim.x;
+    if (!gc_barrier(c, target, &s_ok)) return;
+    // ---- B: the ordered walk
     if (blockIdx.x == 0 && wid == 0) {
       int ncl = __ldcg(c.ctl + 1), err = 0;
-      bool done = false;
+      bool done = false, stop = false;
       int p = pos;
-      const int wend = min(pos + W, g.C);
-      while (p < wend) {
-        if (sbit(s_taken, p)) {
-          ++p;
-          continue;
-        }
-        const int n = __ldcg(g.set_size + p);
-        const int ns = min(n, GC_MAXS);
-        int mb[GC_MAXS / 32];
-        bool st = false;
-#pragma unroll
-        for (int q = 0; q < GC_MAXS / 32; ++q) {
-          const int k = lane + 32 * q;
-          mb[q] = k < ns ? __ldcg(g.set_mem + (size_t)p * GC_MAXS + k) : -1;
-          if (mb[q] >= 0 && sbit(s_taken, mb[q])) st = true;
-        }
-        if (__any_sync(0xffffffffu, st)) break;  // lost a member: recompute from p
-        if (n >= c.thresh) {
-          if (n > GC_MAXS) {
-            err = (int)RTR_ERR_CAPACITY;
-            done = true;
+      const int wend = min(pos + c.win, g.C);
+      while (p < wend && !stop) {
+        const int nb = min(32, wend - p);
+        s_bsize[lane] = lane < nb ? __ldcg(g.set_size + p + lane) : 0;
+        for (int t = 0; t < nb; ++t) s_bmem[t][lane] = __ldcg(g.set_mem + (size_t)(p + t) * GC_MAXS + lane);
+        __syncwarp();
+        int t = 0;
+        for (; t < nb; ++t) {
+          const int q = p + t;
+          if (sbit(s_taken, q)) continue;
+          const int n = s_bsize[t];
+          const int ns = min(n, GC_MAXS);
+          bool st = false;
+          for (int k = lane; k < ns; k += 32) {
+            const int mb = k < 32 ? s_bmem[t][k] : __ldcg(g.set_mem + (size_t)q * GC_MAXS + k);
+            st |= sbit(s_taken, mb);
+          }
+          if (__any_sync(0xffffffffu, st)) {  // lost a member: recompute from q
+            stop = true;
             break;
           }
-#pragma unroll
-          for (int q = 0; q < GC_MAXS / 32; ++q)
-            if (mb[q] >= 0) {
-              atomicOr(&s_taken[mb[q] >> 5], 1u << (mb[q] & 31));
-              c.cl_members[(size_t)ncl * GC_MAXS + lane + 32 * q] = mb[q];
+          if (n >= c.thresh) {
+            if (n > GC_MAXS) {
+              err = (int)RTR_ERR_CAPACITY;
+              done = true;
+              stop = true;
+              break;
             }
-          if (lane == 0) c.cl_sizes[ncl] = n;
-          __syncwarp();
-          ++ncl;
-          if (ncl >= c.max_clusters) {
-            done = true;
-            ++p;
-            break;
+            for (int k = lane; k < ns; k += 32) {
+              const int mb = k < 32 ? s_bmem[t][k] : __ldcg(g.set_mem + (size_t)q * GC_MAXS + k);
+              atomicOr(&s_taken[mb >> 5], 1u << (mb & 31));
+              c.cl_members[(size_t)ncl * GC_MAXS + k] = mb;
+            }
+            if (lane == 0) c.cl_sizes[ncl] = n;
+            __syncwarp();
+            ++ncl;
+            if (ncl >= c.max_clusters) {
+              done = true;
+              stop = true;
+              ++t;
+              break;
+            }
           }
         }
-        ++p;
+        p += t;
+        __syncwarp();
       }
       if (p >= g.C) done = true;
       __syncwarp();
@@ -249,6 +372,7 @@ __global__ void __launch_bounds__(GC_WARPS * 32) k_gc_coop(GcDev g, GcCoop c) {
         c.ctl[2] = done ? 1 : 0;
         if (err) c.ctl[3] = err;
         c.ctl[4] = round + 1;
+        c.ctl[6] = 0;
       }
       __syncwarp();
     }
@@ -353,7 +477,21 @@ struct GcBufs {
   unsigned* arrive;
   int *members, *sizes;
   double* poses;
+  GridMeta* mbox;
+  int* need;
+  unsigned* mask;
 };
+
+// Window of the walk and the width of a pass-mask row.
+constexpr int GC_WIN = 1024;
+static int gc_nwp(int C) { return (((C > 0 ? C : 1) + 31) / 32 + 3) & ~3; }
+static int gc_win(int C) {
+  const size_t row = (size_t)gc_nwp(C) * 4;
+  size_t w = (size_t(256) << 20) / row;  // masks within 256 MB
+  if (w > (size_t)GC_WIN) w = GC_WIN;
+  if (w < 32) w = 32;
+  return (int)w;
+}
 
 static void gc_plan(ScratchPlan& p, int C, int max_clusters, int max_members) {
   const int n = C > 0 ? C : 1;
@@ -370,6 +508,9 @@ static void gc_plan(ScratchPlan& p, int C, int max_clusters, int max_members) {
   p.add<int>((size_t)max_clusters * max_members);
   p.add<int>(max_clusters);
   p.add<double>((size_t)max_clusters * 16);
+  p.add<GridMeta>(1);
+  p.add<int>(gc_win(C));
+  p.add<unsigned>((size_t)gc_win(C) * gc_nwp(C));
 }
 
 static bool gc_take(Scratch& s, int C, int max_clusters, int max_members, GcBufs* b) {
@@ -390,7 +531,10 @@ static bool gc_take(Scratch& s, int C, int max_clusters, int max_members, GcBufs
   b->members = s.take<int>((size_t)max_clusters * max_members);
   b->sizes = s.take<int>(max_clusters);
   b->poses = s.take<double>((size_t)max_clusters * 16);
-  return b->poses != nullptr;
+  b->mbox = s.take<GridMeta>(1);
+  b->need = s.take<int>(gc_win(C));
+  b->mask = s.take<unsigned>((size_t)gc_win(C) * gc_nwp(C));
+  return b->mask != nullptr;
 }
 
 // Shared memory of k_gc_coop beyond its static part: the taken bitset.
@@ -432,8 +576,9 @@ rtr_status gc_group_dev(rtr_context* ctx, Scratch& s, const float* d_model_kp, c
   RTR_CUDA(cudaMemsetAsync(b.misc, 0, sizeof(int) * 16, st));
   RTR_CUDA(cudaMemsetAsync(b.arrive, 0, sizeof(unsigned), st));
   GcDev g{b.pm, b.ps, C, gc_size, b.taken, b.set_size, b.set_mem};
+  bbox_build(b.mbox, b.pm, C, st);
   GcCoop c{b.misc, b.arrive, b.computed, b.members, b.sizes, gc_thresh, max_clusters,
-           ctx->wait_budget_cycles, ctx->d_status};
+           ctx->wait_budget_cycles, ctx->d_status, b.mbox, b.need, b.mask, gc_win(C), gc_nwp(C)};
   RTR_CUDA(cudaFuncSetAttribute(k_gc_coop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
   int per_sm = 0;
   RTR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gc_coop, GC_WARPS * 32, dyn));
@@ -455,14 +600,16 @@ rtr_status gc_group_dev(rtr_context* ctx, Scratch& s, const float* d_model_kp, c
   }
   RTR_LAUNCHED(3);
   int* h = ctx->h_pin;
-  RTR_CUDA(cudaMemcpyAsync(h, b.misc, 5 * sizeof(int), cudaMemcpyDeviceToHost, st));
+  RTR_CUDA(cudaMemcpyAsync(h, b.misc, 6 * sizeof(int), cudaMemcpyDeviceToHost, st));
   RTR_CUDA(cudaStreamSynchronize(st));
   const int ncl = h[1];
   if (h[3] == (int)RTR_ERR_CAPACITY)
     return fail(RTR_ERR_CAPACITY, "rtr_gc_group: a consensus set exceeds %d members", GC_MAXS);
   if (h[3] == (int)RTR_ERR_TIMEOUT)
     return fail(RTR_ERR_TIMEOUT, "rtr_gc_group: a grid barrier wait exceeded the budget");
-  ctx->gc_rounds = h[4];
+  ctx->gc_stats[0] = h[4];
+  ctx->gc_stats[1] = h[0];
+  ctx->gc_stats[2] = h[5];
   if (ncl > 0) {
     k_gc_poses<<<(ncl + 3) / 4, 128, 0, st>>>(b.pm, b.ps, b.members, b.sizes, ncl, GC_MAXS, b.poses);
     RTR_LAUNCHED(1);
@@ -480,6 +627,12 @@ rtr_status gc_group_dev(rtr_context* ctx, Scratch& s, const float* d_model_kp, c
 }
 
 }  // namespace rtr
+
+extern "C" rtr_status rtr_gc_stats(rtr_context* ctx, int* h_stats3) {
+  RTR_CHECK_ARG(ctx && h_stats3, "rtr_gc_stats: bad arguments");
+  for (int i = 0; i < 3; ++i) h_stats3[i] = ctx->gc_stats[i];
+  return RTR_OK;
+}
 
 extern "C" rtr_status rtr_gc_group(rtr_context* ctx, const float* d_model_kp, const float* d_scene_kp,
                                    const int32_t* d_corr_m, const int32_t* d_corr_s, const float* d_corr_d,

@@ -319,31 +319,58 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constan
   }
 }
 
-// Exact FP32 re-rank of the 8 candidates (sequential sums, as the oracle) and
-// certification; one warp per query, lanes 0-7 one candidate each.
-__global__ void k_rerank(const float* __restrict__ q, int nq_host, const int* d_nq, int nq_cap,
-                         const float* __restrict__ db, int ndb, const int* __restrict__ cand_idx,
-                         const float* __restrict__ cand_d, int* __restrict__ out_idx, float* __restrict__ out_d2,
-                         int* __restrict__ redo, int* __restrict__ n_redo) {
-  const int nq = d_nq ? min(*d_nq, nq_cap) : nq_host;
-  const int lane = threadIdx.x & 31;
-  for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < nq; i += gridDim.x * (blockDim.x >> 5)) {
-    const int c = lane < TC_TOP ? cand_idx[(size_t)i * TC_TOP + lane] : -1;
-    float d = __int_as_float(0x7f800000);
-    if (c >= 0) {
-      const float* x = q + (size_t)i * TC_DIM;
-      const float* y = db + (size_t)c * TC_DIM;
-      float acc = 0.f;
-      for (int k = 0; k < TC_DIM; ++k) {
-        const float t = __fsub_rn(x[k], y[k]);
-        acc = __fadd_rn(acc, __fmul_rn(t, t));
-      }
-      d = acc;
+// Exact d^2 of one 352-float row pair: sequential sum in k order, each
+// operation rounded (the oracle's order).  V4: both rows 16-byte aligned.
+template <bool V4>
+__device__ __forceinline__ float exact_d2(const float* __restrict__ x, const float* __restrict__ y) {
+  float acc = 0.f;
+  if (V4) {
+    const float4* x4 = reinterpret_cast<const float4*>(x);
+    const float4* y4 = reinterpret_cast<const float4*>(y);
+#pragma unroll 4
+    for (int k = 0; k < TC_DIM / 4; ++k) {
+      const float4 a = __ldg(x4 + k), b = __ldg(y4 + k);
+      float t = __fsub_rn(a.x, b.x);
+      acc = __fadd_rn(acc, __fmul_rn(t, t));
+      t = __fsub_rn(a.y, b.y);
+      acc = __fadd_rn(acc, __fmul_rn(t, t));
+      t = __fsub_rn(a.z, b.z);
+      acc = __fadd_rn(acc, __fmul_rn(t, t));
+      t = __fsub_rn(a.w, b.w);
+      acc = __fadd_rn(acc, __fmul_rn(t, t));
     }
+  } else {
+    for (int k = 0; k < TC_DIM; ++k) {
+      const float t = __fsub_rn(x[k], y[k]);
+      acc = __fadd_rn(acc, __fmul_rn(t, t));
+    }
+  }
+  return acc;
+}
+
+// Exact FP32 re-rank of the 8 candidates and certification; four queries per
+// warp, one lane per candidate.  Uncertified queries go to the redo list with
+// their running minimum reset.
+template <bool V4>
+__global__ void __launch_bounds__(256) k_rerank(const float* __restrict__ q, int nq_host, const int* d_nq, int nq_cap,
+                                                const float* __restrict__ db, int ndb,
+                                                const int* __restrict__ cand_idx, const float* __restrict__ cand_d,
+                                                int* __restrict__ out_idx, float* __restrict__ out_d2,
+                                                int* __restrict__ redo, int* __restrict__ n_redo,
+                                                unsigned long long* __restrict__ redo_best) {
+  const int nq = d_nq ? min(*d_nq, nq_cap) : nq_host;
+  const int lane = threadIdx.x & 31, sub = lane >> 3, l8 = lane & 7;
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  for (int base = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 4; base < nq; base += warps * 4) {
+    const int i = base + sub;
+    const bool valid = i < nq;
+    const int c = valid ? cand_idx[(size_t)i * TC_TOP + l8] : -1;
+    float d = __int_as_float(0x7f800000);
+    if (c >= 0) d = exact_d2<V4>(q + (size_t)i * TC_DIM, db + (size_t)c * TC_DIM);
     int bi = c >= 0 ? c : 0x7fffffff;
     float bd = d;
 #pragma unroll
-    for (int o = 4; o > 0; o >>= 1) {
+    for (int o = 4; o > 0; o >>= 1) {  // within the aligned group of 8 lanes
       const float od = __shfl_xor_sync(0xffffffffu, bd, o);
       const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
       if (od < bd || (od == bd && oi < bi)) {
@@ -351,7 +378,7 @@ __global__ void k_rerank(const float* __restrict__ q, int nq_host, const int* d_
         bi = oi;
       }
     }
-    if (lane == 0) {
+    if (valid && l8 == 0) {
       const float worst = cand_d[(size_t)i * TC_TOP + TC_TOP - 1];
       const int nvalid = ndb < TC_TOP ? ndb : TC_TOP;
       const bool all_seen = nvalid < TC_TOP;  // every descriptor was a candidate
@@ -360,48 +387,52 @@ __global__ void k_rerank(const float* __restrict__ q, int nq_host, const int* d_
         out_idx[i] = bi == 0x7fffffff ? -1 : bi;
         if (out_d2) out_d2[i] = bd;
       } else {
-        redo[atomicAdd(n_redo, 1)] = i;
+        const int p = atomicAdd(n_redo, 1);
+        redo[p] = i;
+        redo_best[p] = ~0ull;
       }
     }
   }
 }
 
-// Exact scan for the uncertified queries (warp per query, lanes over the db).
-__global__ void k_match_redo(const float* __restrict__ q, const float* __restrict__ db, int ndb,
-                             const int* __restrict__ redo, const int* __restrict__ n_redo, int* __restrict__ out_idx,
-                             float* __restrict__ out_d2) {
-  const int lane = threadIdx.x & 31;
+// Exact scan for the uncertified queries: one CTA per (query, 256 database
+// rows), thread per row; the winner is the minimum of (d^2 bits, index)
+// packed in 64 bits (d^2 >= 0, so its bits order like the value).  A row
+// wins only with d^2 < +inf, as in the sequential scan.
+template <bool V4>
+__global__ void __launch_bounds__(256) k_match_redo(const float* __restrict__ q, const float* __restrict__ db, int ndb,
+                                                    const int* __restrict__ redo, const int* __restrict__ n_redo,
+                                                    unsigned long long* __restrict__ redo_best) {
   const int n = *n_redo;
-  for (int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < n; w += gridDim.x * (blockDim.x >> 5)) {
+  const int rblocks = (ndb + 255) >> 8;
+  const int lane = threadIdx.x & 31;
+  for (long long item = blockIdx.x; item < (long long)n * rblocks; item += gridDim.x) {
+    const int w = (int)(item / rblocks), rb = (int)(item - (long long)w * rblocks);
     const int i = redo[w];
-    const float* x = q + (size_t)i * TC_DIM;
-    float bd = __int_as_float(0x7f800000);
-    int bi = 0x7fffffff;
-    for (int j = lane; j < ndb; j += 32) {
-      const float* y = db + (size_t)j * TC_DIM;
-      float acc = 0.f;
-      for (int k = 0; k < TC_DIM; ++k) {
-        const float t = __fsub_rn(x[k], y[k]);
-        acc = __fadd_rn(acc, __fmul_rn(t, t));
-      }
-      if (acc < bd) {
-        bd = acc;
-        bi = j;
-      }
+    const int j = rb * 256 + threadIdx.x;
+    unsigned long long key = ~0ull;
+    if (j < ndb) {
+      const float d = exact_d2<V4>(q + (size_t)i * TC_DIM, db + (size_t)j * TC_DIM);
+      if (d < __int_as_float(0x7f800000)) key = ((unsigned long long)__float_as_uint(d) << 32) | (unsigned)j;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      const float od = __shfl_xor_sync(0xffffffffu, bd, o);
-      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-      if (od < bd || (od == bd && oi < bi)) {
-        bd = od;
-        bi = oi;
-      }
+      const unsigned long long ok = __shfl_xor_sync(0xffffffffu, key, o);
+      key = ok < key ? ok : key;
     }
-    if (lane == 0) {
-      out_idx[i] = bi == 0x7fffffff ? -1 : bi;
-      if (out_d2) out_d2[i] = bd;
-    }
+    if (lane == 0 && key != ~0ull) atomicMin(redo_best + w, key);
+  }
+}
+
+__global__ void k_match_redo_out(const int* __restrict__ redo, const int* __restrict__ n_redo,
+                                 const unsigned long long* __restrict__ redo_best, int* __restrict__ out_idx,
+                                 float* __restrict__ out_d2) {
+  const int n = *n_redo;
+  for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < n; w += gridDim.x * blockDim.x) {
+    const int i = redo[w];
+    const unsigned long long key = redo_best[w];
+    out_idx[i] = key == ~0ull ? -1 : (int)(unsigned)(key & 0xffffffffull);
+    if (out_d2) out_d2[i] = key == ~0ull ? __int_as_float(0x7f800000) : __uint_as_float((unsigned)(key >> 32));
   }
 }
 
@@ -452,6 +483,7 @@ void match_tc_plan(ScratchPlan& p, int nq_cap, bool with_db, int ndb) {
   p.add<int>((size_t)nqp * TC_TOP);
   p.add<float>((size_t)nqp * TC_TOP);
   p.add<int>(nqp);
+  p.add<unsigned long long>(nqp);
   p.add<int>(4);
 }
 
@@ -487,6 +519,7 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
   int* cidx = s.take<int>((size_t)nqp * TC_TOP);
   float* cd = s.take<float>((size_t)nqp * TC_TOP);
   int* redo = s.take<int>(nqp);
+  unsigned long long* redo_best = s.take<unsigned long long>(nqp);
   int* nredo = s.take<int>(4);
   if (!nredo) return fail(RTR_ERR_CAPACITY, "match_tc: scratch");
   int sb = (nqp + 7) / 8;
@@ -503,13 +536,25 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
     attr = true;
   }
   TcArgs a{nq_cap, d_nq, nq_cap, ndb, qn, db_n2, cidx, cd, ctx->d_status};
-  k_match_tc<<<nqp / TC_BM, TC_THREADS, smem, st>>>(m_qh, m_ql, m_bh, m_bl, a);
+  {
+    ProfScope pg(ctx, st, "match_gemm");
+    k_match_tc<<<nqp / TC_BM, TC_THREADS, smem, st>>>(m_qh, m_ql, m_bh, m_bl, a);
+  }
   RTR_CUDA(cudaMemsetAsync(nredo, 0, sizeof(int), st));
-  int rb = (nq_cap + 7) / 8;
+  int rb = (nq_cap + 31) / 32;
   if (rb > 152 * 16) rb = 152 * 16;
-  k_rerank<<<rb, 256, 0, st>>>(q, nq_cap, d_nq, nq_cap, db, ndb, cidx, cd, out_idx, out_d2, redo, nredo);
-  k_match_redo<<<152 * 4, 256, 0, st>>>(q, db, ndb, redo, nredo, out_idx, out_d2);
-  RTR_LAUNCHED(4);
+  const bool v4 = ((reinterpret_cast<uintptr_t>(q) | reinterpret_cast<uintptr_t>(db)) & 15u) == 0;
+  if (v4) {
+    k_rerank<true><<<rb, 256, 0, st>>>(q, nq_cap, d_nq, nq_cap, db, ndb, cidx, cd, out_idx, out_d2, redo, nredo,
+                                       redo_best);
+    k_match_redo<true><<<152 * 8, 256, 0, st>>>(q, db, ndb, redo, nredo, redo_best);
+  } else {
+    k_rerank<false><<<rb, 256, 0, st>>>(q, nq_cap, d_nq, nq_cap, db, ndb, cidx, cd, out_idx, out_d2, redo, nredo,
+                                        redo_best);
+    k_match_redo<false><<<152 * 8, 256, 0, st>>>(q, db, ndb, redo, nredo, redo_best);
+  }
+  k_match_redo_out<<<4, 256, 0, st>>>(redo, nredo, redo_best, out_idx, out_d2);
+  RTR_LAUNCHED(5);
   // keep the number of uncertified queries for rtr_match_stats
   RTR_CUDA(cudaMemcpyAsync(ctx->d_status + 8, nredo, sizeof(int), cudaMemcpyDeviceToDevice, st));
   RTR_CUDA(cudaGetLastError());
