@@ -61,6 +61,13 @@ const char* rtr_last_error(void);
 /* Library version, e.g. "0.1.0". */
 const char* rtr_version(void);
 
+/* Tuning knobs of this context (value 0 restores the automatic choice):
+ *   "icp_group"  lanes cooperating on one ICP source point's 1-NN search
+ *                (2, 4 or 8).
+ * Unknown keys or values return RTR_ERR_INVALID_ARG.  Results do not depend
+ * on the knobs beyond FP32 summation order. */
+rtr_status rtr_context_set_tuning(rtr_context* ctx, const char* key, int value);
+
 /* Create a context on `device`: owns a scratch arena, a device status word
  * and the tensor-map cache.  Fails with RTR_ERR_NO_DEVICE when the device is
  * not compute capability 10.3. */
@@ -283,10 +290,13 @@ rtr_status rtr_gc_group(rtr_context* ctx, const float* d_model_kp, const float* 
                         int n_corr, float gc_size, int gc_thresh, int max_clusters,
                         int max_members, int32_t* d_members, int32_t* d_sizes,
                         double* d_poses, int* h_n_clusters, rtr_stream_t stream);
-/* Work of the last grouping on this context: h_stats3[0] = rounds of the
+/* Work of the last grouping on this context: h_stats8[0] = rounds of the
  * window/walk loop, [1] = position where the walk ended, [2] = consensus
- * sets computed (including recomputations).  No synchronisation. */
-rtr_status rtr_gc_stats(rtr_context* ctx, int* h_stats3);
+ * sets computed (including recomputations), [3..6] = microseconds spent in
+ * the round phases (seed selection, seed tests, admission, walk; barrier
+ * waits included), [7] = candidates that passed a seed test, summed over the
+ * computed sets.  No synchronisation. */
+rtr_status rtr_gc_stats(rtr_context* ctx, int* h_stats8);
 
 /* ---- recognition pipeline ------------------------------------------------
  * The whole chain of main (RealTimeRobot.cpp:39-105) for one known object

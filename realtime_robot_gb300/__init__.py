@@ -117,6 +117,7 @@ _SIG = {
     "rtr_context_scratch_bytes": (C.c_size_t, [_P]),
     "rtr_context_set_wait_budget_ms": (_I, [_P, _D]),
     "rtr_context_check": (_I, [_P, _P]),
+    "rtr_context_set_tuning": (_I, [_P, C.c_char_p, _I]),
     "rtr_context_set_profiling": (_I, [_P, _I]),
     "rtr_context_profile_count": (_I, [_P]),
     "rtr_context_profile_get": (_I, [_P, _I, C.POINTER(C.c_char_p), C.POINTER(C.c_float)]),
@@ -140,7 +141,7 @@ _SIG = {
     "rtr_match_stats": (_I, [_P, C.POINTER(C.c_int)]),
     "rtr_gc_group": (_I, [_P, _P, _P, _P, _P, _P, _I, _F, _I, _I, _I, _P, _P, _P,
                           C.POINTER(C.c_int), _P]),
-    "rtr_gc_stats": (_I, [_P, C.POINTER(C.c_int * 3)]),
+    "rtr_gc_stats": (_I, [_P, C.POINTER(C.c_int * 8)]),
     "rtr_recog_default_params": (None, [C.POINTER(RecogParams)]),
     "rtr_model_create": (_I, [_P, _P, _I, C.POINTER(RecogParams), C.POINTER(_P)]),
     "rtr_model_destroy": (_I, [_P]),
@@ -230,6 +231,9 @@ class Context:
 
     def set_wait_budget_ms(self, ms: float):
         check(lib().rtr_context_set_wait_budget_ms(self.h, ms))
+
+    def set_tuning(self, key: str, value: int):
+        check(lib().rtr_context_set_tuning(self.h, key.encode(), int(value)))
 
     def check(self, stream=None):
         check(lib().rtr_context_check(self.h, _stream(stream)))
@@ -400,10 +404,12 @@ class Context:
         return idx, d2
 
     def gc_stats(self) -> dict:
-        """Work of the last grouping: rounds, walk end position, sets computed."""
-        v = (C.c_int * 3)()
+        """Work of the last grouping: rounds, walk end position, sets computed,
+        microseconds per round phase."""
+        v = (C.c_int * 8)()
         check(lib().rtr_gc_stats(self.h, C.byref(v)))
-        return {"rounds": v[0], "walk_end": v[1], "sets": v[2]}
+        return {"rounds": v[0], "walk_end": v[1], "sets": v[2], "candidates": v[7],
+                "us": {"select": v[3], "seed_tests": v[4], "admission": v[5], "walk": v[6]}}
 
     def gc_group(self, model_kp, scene_kp, corr_m, corr_s, corr_d, gc_size=0.01, gc_thresh=5,
                  max_clusters=64, max_members=128, stream=None):

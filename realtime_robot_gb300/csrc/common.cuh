@@ -71,7 +71,8 @@ struct rtr_context {
   size_t io_bytes = 0;
   cudaStream_t host_stream = nullptr;  // stream of the host-pointer entry points
   int* h_pin = nullptr;                // 64 pinned ints for small device->host reads
-  int gc_stats[3] = {0, 0, 0};         // last grouping: rounds, walk end, sets computed
+  int tune_icp_group = 0;              // lanes per ICP source point (0: automatic)
+  int gc_stats[8] = {};                // last grouping: rounds, walk end, sets, phase us, candidates
   bool profiling = false;
   std::vector<rtr_prof_rec> prof;      // recorded stages (in order)
   std::vector<cudaEvent_t> event_pool; // reusable events

@@ -230,6 +230,17 @@ rtr_status rtr_context_set_wait_budget_ms(rtr_context* ctx, double ms) {
   return RTR_OK;
 }
 
+rtr_status rtr_context_set_tuning(rtr_context* ctx, const char* key, int value) {
+  if (!ctx || !key) return rtr::fail(RTR_ERR_INVALID_ARG, "rtr_context_set_tuning: NULL argument");
+  if (strcmp(key, "icp_group") == 0) {
+    if (value != 0 && value != 2 && value != 4 && value != 8)
+      return rtr::fail(RTR_ERR_INVALID_ARG, "icp_group must be 0, 2, 4 or 8 (got %d)", value);
+    ctx->tune_icp_group = value;
+    return RTR_OK;
+  }
+  return rtr::fail(RTR_ERR_INVALID_ARG, "rtr_context_set_tuning: unknown key '%s'", key);
+}
+
 rtr_status rtr_context_check(rtr_context* ctx, rtr_stream_t stream) {
   if (!ctx) return rtr::fail(RTR_ERR_INVALID_ARG, "rtr_context_check: ctx is NULL");
   int st = 0;

@@ -66,7 +66,9 @@ __device__ __forceinline__ bool gc_consistent(float4 am, float4 as, float4 bm, f
 // Device-side control block of the grouping walk.
 struct GcCoop {
   int* ctl;            // [0] walk position, [1] clusters, [2] done, [3] error status, [4] rounds,
-                       // [5] sets computed, [6] seeds needing a set this round
+                       // [5] sets computed, [6] seeds needing a set this round,
+                       // [7] candidates that passed a seed test (summed over sets),
+                       // [8..11] microseconds in phases P, A1, A2, B (block 0's view)
   unsigned* arrive;    // grid barrier counter (zero at launch)
   int* computed;       // [C] 1 once the seed's set has been computed
   int* cl_members;     // [max_clusters][GC_MAXS] sorted positions
@@ -108,48 +110,57 @@ __device__ __forceinline__ bool gc_barrier(const GcCoop& c, unsigned target, int
   return *s_ok != 0;
 }
 
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 __device__ __forceinline__ float4 shfl4(float4 v, int src) {
   return make_float4(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src),
                      __shfl_sync(0xffffffffu, v.z, src), __shfl_sync(0xffffffffu, v.w, src));
 }
 
 constexpr int GC_PEND = 64;  // candidates staged per warp before admission
+constexpr int GC_PREF = 7;   // mask loads in flight per lane during admission
 
 // Greedy admission of the n (<= 32) staged candidates, in slot order, into
 // the warp's set (members in mem_m/mem_s; member 0 is the seed, which every
-// staged candidate already passed).
+// staged candidate already passed).  Lane k tests candidate k against the
+// members so far in parallel; then, lowest lane first, the next passing
+// candidate is admitted and every later candidate is also tested against
+// it.  Same result as admitting one candidate at a time.
 __device__ __forceinline__ void gc_admit(const GcDev& g, int a, const int* slot, int n, float4* mem_m,
-                                         float4* mem_s, int& cnt, float r2max) {
+                                         float4* mem_s, int& cnt, float r2max, int* n_tested) {
   const int lane = threadIdx.x & 31;
   const int pj = lane < n ? slot[lane] : -1;
-  float4 cm_l = make_float4(0, 0, 0, 0), cs_l = cm_l;
+  float4 cm = make_float4(0, 0, 0, 0), cs = cm;
   if (pj >= 0) {
-    cm_l = __ldg(g.pm + pj);
-    cs_l = __ldg(g.ps + pj);
+    cm = __ldg(g.pm + pj);
+    cs = __ldg(g.ps + pj);
   }
-  for (int t = 0; t < n; ++t) {
-    const int pb = __shfl_sync(0xffffffffu, pj, t);
-    const float4 cm = shfl4(cm_l, t), cs = shfl4(cs_l, t);
-    bool ok = true;
-    const int stored = min(cnt, GC_MAXS);
-    for (int m0 = 1; m0 < stored; m0 += 32) {
-      const int m = m0 + lane;
-      const bool bad = m < stored && !gc_consistent(mem_m[m], mem_s[m], cm, cs, g.gc, r2max);
-      if (__any_sync(0xffffffffu, bad)) {
-        ok = false;
-        break;
-      }
-    }
-    if (ok) {
-      if (cnt < GC_MAXS && lane == 0) {
-        mem_m[cnt] = cm;
-        mem_s[cnt] = cs;
-        g.set_mem[(size_t)a * GC_MAXS + cnt] = pb;
-      }
-      ++cnt;  // counted beyond GC_MAXS too: reported by the walk
-      __syncwarp();
-    }
+  *n_tested += n;
+  bool pass = pj >= 0;
+  const int stored = min(cnt, GC_MAXS);
+  for (int m = 1; m < stored; ++m) {
+    if (pass) pass = gc_consistent(mem_m[m], mem_s[m], cm, cs, g.gc, r2max);
+    if ((m & 3) == 0 && !__any_sync(0xffffffffu, pass)) break;
   }
+  unsigned bal = __ballot_sync(0xffffffffu, pass);
+  while (bal) {
+    const int f = __ffs(bal) - 1;
+    const float4 fm = shfl4(cm, f), fs = shfl4(cs, f);
+    if (lane == f && cnt < GC_MAXS) {
+      mem_m[cnt] = cm;
+      mem_s[cnt] = cs;
+      g.set_mem[(size_t)a * GC_MAXS + cnt] = pj;
+    }
+    ++cnt;  // counted beyond GC_MAXS too: reported by the walk
+    if (lane > f && pass) pass = gc_consistent(fm, fs, cm, cs, g.gc, r2max);
+    if (lane <= f) pass = false;
+    bal = __ballot_sync(0xffffffffu, pass);
+  }
+  __syncwarp();
 }
 
 // The whole grouping in one cooperative launch.  Each round:
@@ -172,8 +183,9 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
   extern __shared__ unsigned s_taken[];  // copy of the taken bitset
   __shared__ float4 mem_m[GC_WARPS][GC_MAXS], mem_s[GC_WARPS][GC_MAXS];
   __shared__ int s_slot[GC_WARPS][GC_PEND];
-  __shared__ int s_bmem[32][32];  // walk: first 32 members of the next 32 seeds
-  __shared__ int s_bsize[32];
+  __shared__ float4 s_gm[GC_WARPS][32], s_gs[GC_WARPS][32];  // seed tests: the group's seeds
+  __shared__ int s_ga[GC_WARPS][32];
+  __shared__ int s_bmem[32][33];  // walk: first 32 members of the next 32 seeds (padded rows)
   __shared__ int s_pos, s_done, s_ok;
   __shared__ float s_r2max;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -195,6 +207,15 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
   __syncthreads();
   const float r2max = s_r2max;
   unsigned target = 0;
+  unsigned long long ph[4] = {0, 0, 0, 0}, tp = 0;
+  const bool timer = blockIdx.x == 0 && threadIdx.x == 0;
+  if (timer) tp = gtimer();
+#define GC_PHASE(k)                            \
+  if (timer) {                                 \
+    const unsigned long long tn_ = gtimer();   \
+    ph[k] += tn_ - tp;                         \
+    tp = tn_;                                  \
+  }
   for (int round = 0;; ++round) {
     __syncthreads();
     for (int i = threadIdx.x; i < nwords; i += blockDim.x) s_taken[i] = __ldcg(g.taken + i);
@@ -218,13 +239,32 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
     }
     target += gridDim.x;
     if (!gc_barrier(c, target, &s_ok)) return;
+    GC_PHASE(0)
     const int nneed = __ldcg(c.ctl + 6);
-    // ---- A1: seed tests -> pass bitmasks
+    // ---- A1: seed tests -> pass bitmasks.  Items are (group of 32 listed
+    // seeds, chunk of 32 candidates); every warp takes a contiguous run of
+    // items, keeps its group's seed endpoints in shared memory, loads each
+    // candidate chunk once and tests it against all 32 seeds.
     if (nneed > 0) {
-      const int ngrp = (nneed + 7) >> 3;
+      const int ngrp = (nneed + 31) >> 5;
       const long long items = (long long)c.nwp * ngrp;
-      for (long long it = gw; it < items; it += nwarps) {
-        const int ch = (int)(it % c.nwp), grp = (int)(it / c.nwp);
+      const long long per = (items + nwarps - 1) / nwarps;
+      const long long it0 = (long long)gw * per, it1 = min(items, it0 + per);
+      int cur = -1;
+      for (long long it = it0; it < it1; ++it) {
+        const int grp = (int)(it / c.nwp), ch = (int)(it - (long long)grp * c.nwp);
+        const int kend = min(32, nneed - grp * 32);
+        if (grp != cur) {
+          __syncwarp();
+          if (lane < kend) {
+            const int a = __ldcg(c.need + grp * 32 + lane);
+            s_ga[wid][lane] = a;
+            s_gm[wid][lane] = __ldg(g.pm + a);
+            s_gs[wid][lane] = __ldg(g.ps + a);
+          }
+          __syncwarp();
+          cur = grp;
+        }
         const int b = ch * 32 + lane;
         const bool okb = b < g.C && !sbit(s_taken, b);
         float4 bm = make_float4(0, 0, 0, 0), bs = bm;
@@ -232,19 +272,18 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
           bm = __ldg(g.pm + b);
           bs = __ldg(g.ps + b);
         }
-        const int kend = min(8, nneed - grp * 8);
+        unsigned mine = 0u;  // lane k keeps the word of seed k
         for (int k = 0; k < kend; ++k) {
-          const int slot = grp * 8 + k;
-          const int a = __ldcg(c.need + slot);
-          const float4 am = __ldg(g.pm + a), as = __ldg(g.ps + a);
-          const bool pass = okb && b != a && gc_consistent(am, as, bm, bs, g.gc, r2max);
+          const bool pass = okb && b != s_ga[wid][k] && gc_consistent(s_gm[wid][k], s_gs[wid][k], bm, bs, g.gc, r2max);
           const unsigned bal = __ballot_sync(0xffffffffu, pass);
-          if (lane == 0) c.mask[(size_t)slot * c.nwp + ch] = bal;
+          if (lane == k) mine = bal;
         }
+        if (lane < kend) c.mask[(size_t)(grp * 32 + lane) * c.nwp + ch] = mine;
       }
     }
     target += gridDim.x;
     if (!gc_barrier(c, target, &s_ok)) return;
+    GC_PHASE(1)
     // ---- A2: ordered admission, warp per listed seed
     for (int slot = gw; slot < nneed; slot += nwarps) {
       const int a = __ldcg(c.need + slot);
@@ -254,64 +293,73 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
         g.set_mem[(size_t)a * GC_MAXS] = a;
       }
       __syncwarp();
-      int cnt = 1, npend = 0;
+      int cnt = 1, npend = 0, ntest = 0;
       const uint4* row = reinterpret_cast<const uint4*>(c.mask + (size_t)slot * c.nwp);
-      for (int w0 = 0; w0 < c.nwp; w0 += 128) {
-        unsigned wv[4] = {0u, 0u, 0u, 0u};
-        if (w0 + lane * 4 < c.nwp) {
-          const uint4 v = __ldcg(row + (w0 >> 2) + lane);
-          wv[0] = v.x;
-          wv[1] = v.y;
-          wv[2] = v.z;
-          wv[3] = v.w;
-        }
-        int rc = __popc(wv[0]) + __popc(wv[1]) + __popc(wv[2]) + __popc(wv[3]);
-        while (__any_sync(0xffffffffu, rc > 0)) {
-          int incl = rc;
+      const int nv = c.nwp >> 2;
+      for (int v0 = 0; v0 < nv; v0 += 32 * GC_PREF) {
+        uint4 buf[GC_PREF];
 #pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
-          }
-          const int total = __shfl_sync(0xffffffffu, incl, 31);
-          const int ex = incl - rc;
-          const int room = GC_PEND - npend;
-          // lanes whose lower neighbours all fit emit their first candidates
-          int take = min(max(room - ex, 0), rc);
-          int dst = npend + ex;
-          for (int q = 0; q < 4 && take > 0; ++q) {
-            while (wv[q] && take > 0) {
-              const int bit = __ffs(wv[q]) - 1;
-              wv[q] &= wv[q] - 1;
-              s_slot[wid][dst++] = (w0 + lane * 4 + q) * 32 + bit;
-              --take;
-              --rc;
+        for (int j = 0; j < GC_PREF; ++j) {
+          const int idx = v0 + j * 32 + lane;
+          buf[j] = idx < nv ? __ldcg(row + idx) : make_uint4(0u, 0u, 0u, 0u);
+        }
+#pragma unroll
+        for (int j = 0; j < GC_PREF; ++j) {
+          const int w0 = (v0 + j * 32) * 4;  // first word of this 128-word block
+          unsigned wv[4] = {buf[j].x, buf[j].y, buf[j].z, buf[j].w};
+          int rc = __popc(wv[0]) + __popc(wv[1]) + __popc(wv[2]) + __popc(wv[3]);
+          while (__any_sync(0xffffffffu, rc > 0)) {
+            int incl = rc;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+              const int y = __shfl_up_sync(0xffffffffu, incl, o);
+              if (lane >= o) incl += y;
             }
-          }
-          npend += min(total, room);
-          __syncwarp();
-          while (npend >= 32) {
-            gc_admit(g, a, s_slot[wid], 32, mem_m[wid], mem_s[wid], cnt, r2max);
-            const int rest = npend - 32;
-            const int mv = lane < rest ? s_slot[wid][32 + lane] : 0;
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            const int ex = incl - rc;
+            const int room = GC_PEND - npend;
+            // lanes whose lower neighbours all fit emit their first candidates
+            int take = min(max(room - ex, 0), rc);
+            int dst = npend + ex;
+            for (int q = 0; q < 4 && take > 0; ++q) {
+              while (wv[q] && take > 0) {
+                const int bit = __ffs(wv[q]) - 1;
+                wv[q] &= wv[q] - 1;
+                s_slot[wid][dst++] = (w0 + lane * 4 + q) * 32 + bit;
+                --take;
+                --rc;
+              }
+            }
+            npend += min(total, room);
             __syncwarp();
-            if (lane < rest) s_slot[wid][lane] = mv;
-            npend = rest;
-            __syncwarp();
+            while (npend >= 32) {
+              gc_admit(g, a, s_slot[wid], 32, mem_m[wid], mem_s[wid], cnt, r2max, &ntest);
+              const int rest = npend - 32;
+              const int mv = lane < rest ? s_slot[wid][32 + lane] : 0;
+              __syncwarp();
+              if (lane < rest) s_slot[wid][lane] = mv;
+              npend = rest;
+              __syncwarp();
+            }
           }
         }
       }
-      if (npend > 0) gc_admit(g, a, s_slot[wid], npend, mem_m[wid], mem_s[wid], cnt, r2max);
+      if (npend > 0) gc_admit(g, a, s_slot[wid], npend, mem_m[wid], mem_s[wid], cnt, r2max, &ntest);
       if (lane == 0) {
         g.set_size[a] = cnt;
         c.computed[a] = 1;
         atomicAdd(c.ctl + 5, 1);
+        atomicAdd(c.ctl + 7, ntest);
       }
       __syncwarp();
     }
     target += gridDim.x;
     if (!gc_barrier(c, target, &s_ok)) return;
-    // ---- B: the ordered walk
+    GC_PHASE(2)
+    // ---- B: the ordered walk, 32 seeds per batch.  Lane l evaluates seed
+    // p + l (taken? lost a member?) in parallel; only events (a commit or a
+    // stale set) are handled in order, and after a commit the later lanes
+    // evaluate again.
     if (blockIdx.x == 0 && wid == 0) {
       int ncl = __ldcg(c.ctl + 1), err = 0;
       bool done = false, stop = false;
@@ -319,48 +367,62 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
       const int wend = min(pos + c.win, g.C);
       while (p < wend && !stop) {
         const int nb = min(32, wend - p);
-        s_bsize[lane] = lane < nb ? __ldcg(g.set_size + p + lane) : 0;
-        for (int t = 0; t < nb; ++t) s_bmem[t][lane] = __ldcg(g.set_mem + (size_t)(p + t) * GC_MAXS + lane);
+        const int my = p + lane;
+        const int n_l = lane < nb ? __ldcg(g.set_size + my) : 0;
+        {
+          int mv[32];  // all 32 loads in flight before the first store
+#pragma unroll
+          for (int t = 0; t < 32; ++t) mv[t] = t < nb ? __ldcg(g.set_mem + (size_t)(p + t) * GC_MAXS + lane) : 0;
+#pragma unroll
+          for (int t = 0; t < 32; ++t) s_bmem[t][lane] = mv[t];  // member `lane` of seed p + t
+        }
         __syncwarp();
-        int t = 0;
-        for (; t < nb; ++t) {
-          const int q = p + t;
-          if (sbit(s_taken, q)) continue;
-          const int n = s_bsize[t];
-          const int ns = min(n, GC_MAXS);
-          bool st = false;
-          for (int k = lane; k < ns; k += 32) {
-            const int mb = k < 32 ? s_bmem[t][k] : __ldcg(g.set_mem + (size_t)q * GC_MAXS + k);
-            st |= sbit(s_taken, mb);
+        const int ns_l = min(n_l, GC_MAXS);
+        int cursor = 0;
+        for (;;) {
+          bool taken_l = true, stale_l = false;
+          if (lane >= cursor && lane < nb) {
+            taken_l = sbit(s_taken, my);
+            if (!taken_l)
+              for (int k = 0; k < ns_l && !stale_l; ++k) {
+                const int mb = k < 32 ? s_bmem[lane][k] : __ldcg(g.set_mem + (size_t)my * GC_MAXS + k);
+                stale_l = sbit(s_taken, mb);
+              }
           }
-          if (__any_sync(0xffffffffu, st)) {  // lost a member: recompute from q
+          const unsigned ev = __ballot_sync(0xffffffffu, !taken_l && (stale_l || n_l >= c.thresh));
+          if (!ev) {
+            p += nb;
+            break;
+          }
+          const int f = __ffs(ev) - 1;
+          const bool f_stale = __shfl_sync(0xffffffffu, stale_l, f);
+          const int nf = __shfl_sync(0xffffffffu, n_l, f);
+          if (f_stale) {  // lost a member: recompute from p + f
+            p += f;
             stop = true;
             break;
           }
-          if (n >= c.thresh) {
-            if (n > GC_MAXS) {
-              err = (int)RTR_ERR_CAPACITY;
-              done = true;
-              stop = true;
-              break;
-            }
-            for (int k = lane; k < ns; k += 32) {
-              const int mb = k < 32 ? s_bmem[t][k] : __ldcg(g.set_mem + (size_t)q * GC_MAXS + k);
-              atomicOr(&s_taken[mb >> 5], 1u << (mb & 31));
-              c.cl_members[(size_t)ncl * GC_MAXS + k] = mb;
-            }
-            if (lane == 0) c.cl_sizes[ncl] = n;
-            __syncwarp();
-            ++ncl;
-            if (ncl >= c.max_clusters) {
-              done = true;
-              stop = true;
-              ++t;
-              break;
-            }
+          if (nf > GC_MAXS) {
+            err = (int)RTR_ERR_CAPACITY;
+            done = stop = true;
+            p += f;
+            break;
           }
+          for (int k = lane; k < nf; k += 32) {
+            const int mb = k < 32 ? s_bmem[f][k] : __ldcg(g.set_mem + (size_t)(p + f) * GC_MAXS + k);
+            atomicOr(&s_taken[mb >> 5], 1u << (mb & 31));
+            c.cl_members[(size_t)ncl * GC_MAXS + k] = mb;
+          }
+          if (lane == 0) c.cl_sizes[ncl] = nf;
+          __syncwarp();
+          ++ncl;
+          if (ncl >= c.max_clusters) {
+            done = stop = true;
+            p += f + 1;
+            break;
+          }
+          cursor = f + 1;
         }
-        p += t;
         __syncwarp();
       }
       if (p >= g.C) done = true;
@@ -378,6 +440,7 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
     }
     target += gridDim.x;
     if (!gc_barrier(c, target, &s_ok)) return;
+    GC_PHASE(3)
     if (threadIdx.x == 0) {
       s_pos = __ldcg(c.ctl + 0);
       s_done = __ldcg(c.ctl + 2) || __ldcg(c.ctl + 3);
@@ -385,6 +448,9 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
     __syncthreads();
     if (s_done) break;
   }
+#undef GC_PHASE
+  if (timer)
+    for (int k = 0; k < 4; ++k) c.ctl[8 + k] = (int)(ph[k] / 1000ull);
 }
 
 // Members as original correspondence indices.
@@ -600,7 +666,7 @@ rtr_status gc_group_dev(rtr_context* ctx, Scratch& s, const float* d_model_kp, c
   }
   RTR_LAUNCHED(3);
   int* h = ctx->h_pin;
-  RTR_CUDA(cudaMemcpyAsync(h, b.misc, 6 * sizeof(int), cudaMemcpyDeviceToHost, st));
+  RTR_CUDA(cudaMemcpyAsync(h, b.misc, 12 * sizeof(int), cudaMemcpyDeviceToHost, st));
   RTR_CUDA(cudaStreamSynchronize(st));
   const int ncl = h[1];
   if (h[3] == (int)RTR_ERR_CAPACITY)
@@ -610,6 +676,8 @@ rtr_status gc_group_dev(rtr_context* ctx, Scratch& s, const float* d_model_kp, c
   ctx->gc_stats[0] = h[4];
   ctx->gc_stats[1] = h[0];
   ctx->gc_stats[2] = h[5];
+  for (int k = 0; k < 4; ++k) ctx->gc_stats[3 + k] = h[8 + k];
+  ctx->gc_stats[7] = h[7];
   if (ncl > 0) {
     k_gc_poses<<<(ncl + 3) / 4, 128, 0, st>>>(b.pm, b.ps, b.members, b.sizes, ncl, GC_MAXS, b.poses);
     RTR_LAUNCHED(1);
@@ -628,9 +696,9 @@ rtr_status gc_group_dev(rtr_context* ctx, Scratch& s, const float* d_model_kp, c
 
 }  // namespace rtr
 
-extern "C" rtr_status rtr_gc_stats(rtr_context* ctx, int* h_stats3) {
-  RTR_CHECK_ARG(ctx && h_stats3, "rtr_gc_stats: bad arguments");
-  for (int i = 0; i < 3; ++i) h_stats3[i] = ctx->gc_stats[i];
+extern "C" rtr_status rtr_gc_stats(rtr_context* ctx, int* h_stats8) {
+  RTR_CHECK_ARG(ctx && h_stats8, "rtr_gc_stats: bad arguments");
+  for (int i = 0; i < 8; ++i) h_stats8[i] = ctx->gc_stats[i];
   return RTR_OK;
 }
 

@@ -22,7 +22,6 @@ namespace rtr {
 
 constexpr int ICP_THREADS = 256;
 constexpr int ICP_WARPS = ICP_THREADS / 32;
-constexpr int ICP_G = 8;  // lanes cooperating on one source point's 1-NN search
 constexpr int ICP_NV = 16;  // dp(3) dq(3) dp*dq^T(9) d^2(1)
 
 
@@ -33,6 +32,7 @@ __device__ __forceinline__ float centre_of(const GridMeta* m, int a) {
 // One launch serves many problems: block b works on problem blk2prob[b]
 // together with that problem's other nblk - 1 blocks; problems never wait on
 // one another.
+template <int G>  // lanes cooperating on one source point's 1-NN search
 __global__ void __launch_bounds__(ICP_THREADS) k_icp(const IcpDev* __restrict__ probs,
                                                      const int* __restrict__ blk2prob) {
   const IcpDev& a = probs[blk2prob[blockIdx.x]];
@@ -54,10 +54,10 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(const IcpDev* __restrict__ 
   // stay small even while the clouds are far apart.
   const float c[3] = {centre_of(a.grid.meta, 0), centre_of(a.grid.meta, 1), centre_of(a.grid.meta, 2)};
   const float4 cs = make_float4(centre_of(a.src_meta, 0), centre_of(a.src_meta, 1), centre_of(a.src_meta, 2), 0.f);
-  constexpr int QPB = ICP_THREADS / ICP_G;  // source points per block per pass
+  constexpr int QPB = ICP_THREADS / G;  // source points per block per pass
   const unsigned stride = (unsigned)B * QPB;
-  const int lg = lane & (ICP_G - 1);
-  const unsigned gmask = ((1u << ICP_G) - 1u) << (lane & ~(ICP_G - 1));
+  const int lg = lane & (G - 1);
+  const unsigned gmask = ((1u << G) - 1u) << (lane & ~(G - 1));
 
   for (int it = 0; it < a.max_it; ++it) {
     float T[12];
@@ -73,11 +73,11 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(const IcpDev* __restrict__ 
 #pragma unroll
     for (int v = 0; v < ICP_NV; ++v) acc[v].init();
     int cnt = 0;
-    for (unsigned i = (unsigned)lb * QPB + tid / ICP_G; i < (unsigned)a.n_src; i += stride) {
+    for (unsigned i = (unsigned)lb * QPB + tid / G; i < (unsigned)a.n_src; i += stride) {
       const float4 p = xform_exact(T, a.src[i]);
       float d2;
       int j, pos;
-      grid_nn1_group<ICP_G>(g, p, a.r2max, lg, gmask, d2, j, pos);
+      grid_nn1_group<G>(g, p, a.r2max, lg, gmask, d2, j, pos);
       if (lg != 0) continue;
       if (j >= 0) {
         const float4 q = g.pts[pos];
@@ -317,18 +317,35 @@ __global__ void __launch_bounds__(256) k_gather_pts(const float4* __restrict__ p
   }
 }
 
+// Co-resident blocks of the ICP kernel (the smallest over the group sizes,
+// so a plan made for one group size fits every variant).
 int icp_max_blocks(rtr_context* ctx) {
   static int cached_dev = -1, cached = 0;
   if (cached_dev != ctx->device) {
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_icp, ICP_THREADS, 0);
+    int a = 0, b = 0, c = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_icp<2>, ICP_THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icp<4>, ICP_THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_icp<8>, ICP_THREADS, 0);
+    int per_sm = a < b ? a : b;
+    per_sm = per_sm < c ? per_sm : c;
     cached = per_sm * ctx->num_sms;
     cached_dev = ctx->device;
   }
   return cached;
 }
 
-static rtr_status launch_icp(const IcpDev* d_probs, const int* d_blk2prob, int blocks, cudaStream_t st) {
+// Lanes per source point: the tuning override when set, else 8 while the
+// launch needs at most four passes with 8 lanes per point, 4 beyond that
+// (measured on GB300: a 20k-point ICP is fastest at 8, sixteen 11k-point
+// refinements at 4; 2 was slower in both).
+int icp_pick_group(const rtr_context* ctx, long long total_pts, int blocks) {
+  const int t = ctx->tune_icp_group;
+  if (t == 2 || t == 4 || t == 8) return t;
+  const long long lanes = (long long)blocks * ICP_THREADS;
+  return total_pts * 8 <= 4 * lanes ? 8 : 4;
+}
+
+static rtr_status launch_icp(int G, const IcpDev* d_probs, const int* d_blk2prob, int blocks, cudaStream_t st) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(blocks);
   cfg.blockDim = dim3(ICP_THREADS);
@@ -339,7 +356,12 @@ static rtr_status launch_icp(const IcpDev* d_probs, const int* d_blk2prob, int b
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  RTR_CUDA(cudaLaunchKernelEx(&cfg, k_icp, d_probs, d_blk2prob));
+  if (G == 2)
+    RTR_CUDA(cudaLaunchKernelEx(&cfg, k_icp<2>, d_probs, d_blk2prob));
+  else if (G == 4)
+    RTR_CUDA(cudaLaunchKernelEx(&cfg, k_icp<4>, d_probs, d_blk2prob));
+  else
+    RTR_CUDA(cudaLaunchKernelEx(&cfg, k_icp<8>, d_probs, d_blk2prob));
   RTR_LAUNCHED(1);
   return RTR_OK;
 }
@@ -397,7 +419,7 @@ rtr_status icp_multi(rtr_context* ctx, Scratch& s, std::vector<IcpSpec>& specs, 
   long long want_total = 0;
   std::vector<long long> want(M);
   for (int i = 0; i < M; ++i) {
-    want[i] = ((long long)specs[i].dev.n_src * ICP_G + ICP_THREADS - 1) / ICP_THREADS;
+    want[i] = ((long long)specs[i].dev.n_src * 8 + ICP_THREADS - 1) / ICP_THREADS;
     if (want[i] < 1) want[i] = 1;
     want_total += want[i];
   }
@@ -436,7 +458,9 @@ rtr_status icp_multi(rtr_context* ctx, Scratch& s, std::vector<IcpSpec>& specs, 
     RTR_LAUNCHED(1);
   }
   RTR_CUDA(cudaGetLastError());
-  return launch_icp(d_probs, d_b2p, used, st);
+  long long total = 0;
+  for (int i = 0; i < M; ++i) total += specs[i].dev.n_src;
+  return launch_icp(icp_pick_group(ctx, total, used), d_probs, d_b2p, used, st);
 }
 
 }  // namespace rtr
@@ -469,7 +493,7 @@ rtr_status rtr_icp(rtr_context* ctx, const float* d_src, int n_src, const float*
 
   const unsigned cell_cap = default_cell_cap(n_tgt);
   const int maxb = icp_max_blocks(ctx);
-  int blocks = (int)(((long long)n_src * ICP_G + ICP_THREADS - 1) / ICP_THREADS);
+  int blocks = (int)(((long long)n_src * 8 + ICP_THREADS - 1) / ICP_THREADS);
   if (blocks > maxb) blocks = maxb;
   if (blocks < 1) blocks = 1;
 

@@ -36,6 +36,7 @@ struct IcpSpec {
 };
 
 int icp_max_blocks(rtr_context* ctx);
+int icp_pick_group(const rtr_context* ctx, long long total_pts, int blocks);
 void icp_multi_plan(ScratchPlan& p, int n_probs, int max_blocks);
 // Runs every problem; specs are completed (blocks, state buffers) in place.
 rtr_status icp_multi(rtr_context* ctx, Scratch& s, std::vector<IcpSpec>& specs, cudaStream_t st);

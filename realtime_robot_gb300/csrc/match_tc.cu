@@ -3,8 +3,11 @@
 // d^2(q, b) = |q|^2 + |b|^2 - 2 q.b with the dot product as a BF16 GEMM with
 // FP32 accumulation in tensor memory.  Each FP32 descriptor is split into
 // hi = bf16(x) and lo = bf16(x - hi); the accumulator sums hi.hi + hi.lo +
-// lo.hi (three tcgen05.mma per K step), which leaves |err(q.b)| < ~1e-4 for the
-// unit-norm, non-negative SHOT vectors.  Per query the epilogue keeps the 8
+// lo.hi (three tcgen05.mma per K step), which leaves |err(q.b)| of order
+// 1e-4 |q| |b| (dropped lo.lo, the split's rounding, FP32 accumulation); the
+// certification uses TC_ERR * max(|q|, max |b|)^2, which covers that and the
+// FP32 norms with margin (unit-norm SHOT vectors: 1e-3).  Inf or NaN values
+// make a query uncertified.  Per query the epilogue keeps the 8
 // smallest approximate distances; an exact FP32 re-rank (sequential sums, as
 // the oracle) picks the winner, and a query is certified when its 8th
 // approximate distance minus the error bound is still above the exact winner,
@@ -135,7 +138,7 @@ __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::
 // ---------------------------------------------------------------------------
 __global__ void k_split_bf16(const float* __restrict__ x, int n_host, const int* d_n, int n_cap,
                              __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
-                             float* __restrict__ norm2) {
+                             float* __restrict__ norm2, unsigned* __restrict__ max_bits) {
   const int n = d_n ? min(*d_n, n_cap) : n_host;
   const int lane = threadIdx.x & 31;
   for (int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < n_cap; r += gridDim.x * (blockDim.x >> 5)) {
@@ -150,7 +153,10 @@ __global__ void k_split_bf16(const float* __restrict__ x, int n_host, const int*
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
-    if (lane == 0) norm2[r] = ss;
+    if (lane == 0) {
+      norm2[r] = ss;
+      if (max_bits && r < n) atomicMax(max_bits, __float_as_uint(ss));  // ss >= 0 (or NaN: stays largest)
+    }
   }
 }
 
@@ -357,7 +363,8 @@ __global__ void __launch_bounds__(256) k_rerank(const float* __restrict__ q, int
                                                 const int* __restrict__ cand_idx, const float* __restrict__ cand_d,
                                                 int* __restrict__ out_idx, float* __restrict__ out_d2,
                                                 int* __restrict__ redo, int* __restrict__ n_redo,
-                                                unsigned long long* __restrict__ redo_best) {
+                                                unsigned long long* __restrict__ redo_best,
+                                                const float* __restrict__ qn, const float* __restrict__ db_max) {
   const int nq = d_nq ? min(*d_nq, nq_cap) : nq_host;
   const int lane = threadIdx.x & 31, sub = lane >> 3, l8 = lane & 7;
   const int warps = gridDim.x * (blockDim.x >> 5);
@@ -382,7 +389,9 @@ __global__ void __launch_bounds__(256) k_rerank(const float* __restrict__ q, int
       const float worst = cand_d[(size_t)i * TC_TOP + TC_TOP - 1];
       const int nvalid = ndb < TC_TOP ? ndb : TC_TOP;
       const bool all_seen = nvalid < TC_TOP;  // every descriptor was a candidate
-      const bool certified = all_seen || (worst - TC_ERR > bd);
+      // the bound scales with the norms: |err| <= TC_ERR * max(|q|, |b|max)^2
+      const float err = TC_ERR * fmaxf(qn[i], *db_max);
+      const bool certified = all_seen || (worst - err > bd);
       if (certified) {
         out_idx[i] = bi == 0x7fffffff ? -1 : bi;
         if (out_d2) out_d2[i] = bd;
@@ -478,7 +487,7 @@ void match_tc_plan(ScratchPlan& p, int nq_cap, bool with_db, int ndb) {
   if (with_db) {
     p.add<__nv_bfloat16>((size_t)ndb * TC_KPAD);
     p.add<__nv_bfloat16>((size_t)ndb * TC_KPAD);
-    p.add<float>(ndb);
+    p.add<float>(ndb + 1);
   }
   p.add<int>((size_t)nqp * TC_TOP);
   p.add<float>((size_t)nqp * TC_TOP);
@@ -493,7 +502,9 @@ rtr_status match_tc_prepare_db(const float* db, int ndb, __nv_bfloat16* hi, __nv
   int blocks = (ndb + 7) / 8;
   if (blocks > 152 * 16) blocks = 152 * 16;
   if (blocks < 1) blocks = 1;
-  k_split_bf16<<<blocks, 256, 0, st>>>(db, ndb, nullptr, ndb, hi, lo, norm2);
+  // norm2[ndb] receives the largest squared norm (scales the error bound)
+  RTR_CUDA(cudaMemsetAsync(norm2 + ndb, 0, sizeof(float), st));
+  k_split_bf16<<<blocks, 256, 0, st>>>(db, ndb, nullptr, ndb, hi, lo, norm2, reinterpret_cast<unsigned*>(norm2 + ndb));
   RTR_LAUNCHED(1);
   RTR_CUDA(cudaGetLastError());
   return RTR_OK;
@@ -509,7 +520,7 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
   if (!db_hi) {
     __nv_bfloat16* h = s.take<__nv_bfloat16>((size_t)ndb * TC_KPAD);
     __nv_bfloat16* l = s.take<__nv_bfloat16>((size_t)ndb * TC_KPAD);
-    float* n2 = s.take<float>(ndb);
+    float* n2 = s.take<float>(ndb + 1);
     if (!n2) return fail(RTR_ERR_CAPACITY, "match_tc: scratch");
     RTR_TRY(match_tc_prepare_db(db, ndb, h, l, n2, st));
     db_hi = h;
@@ -524,7 +535,7 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
   if (!nredo) return fail(RTR_ERR_CAPACITY, "match_tc: scratch");
   int sb = (nqp + 7) / 8;
   if (sb > 152 * 16) sb = 152 * 16;
-  k_split_bf16<<<sb, 256, 0, st>>>(q, nq_cap, d_nq, nqp, qhi, qlo, qn);
+  k_split_bf16<<<sb, 256, 0, st>>>(q, nq_cap, d_nq, nqp, qhi, qlo, qn, nullptr);
   CUtensorMap m_qh, m_ql, m_bh, m_bl;
   if (!make_map(&m_qh, qhi, nqp, TC_BM) || !make_map(&m_ql, qlo, nqp, TC_BM) || !make_map(&m_bh, db_hi, ndb, TC_BN) ||
       !make_map(&m_bl, db_lo, ndb, TC_BN))
@@ -546,11 +557,11 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
   const bool v4 = ((reinterpret_cast<uintptr_t>(q) | reinterpret_cast<uintptr_t>(db)) & 15u) == 0;
   if (v4) {
     k_rerank<true><<<rb, 256, 0, st>>>(q, nq_cap, d_nq, nq_cap, db, ndb, cidx, cd, out_idx, out_d2, redo, nredo,
-                                       redo_best);
+                                       redo_best, qn, db_n2 + ndb);
     k_match_redo<true><<<152 * 8, 256, 0, st>>>(q, db, ndb, redo, nredo, redo_best);
   } else {
     k_rerank<false><<<rb, 256, 0, st>>>(q, nq_cap, d_nq, nq_cap, db, ndb, cidx, cd, out_idx, out_d2, redo, nredo,
-                                        redo_best);
+                                        redo_best, qn, db_n2 + ndb);
     k_match_redo<false><<<152 * 8, 256, 0, st>>>(q, db, ndb, redo, nredo, redo_best);
   }
   k_match_redo_out<<<4, 256, 0, st>>>(redo, nredo, redo_best, out_idx, out_d2);

@@ -97,11 +97,16 @@ __global__ void k_gather_kp(const float4* __restrict__ pts, const int* __restric
 // Inlier count of a transformed model cloud in the scene grid: one block per
 // hypothesis, G lanes per model point (exact bounded 1-NN; found = inlier).
 constexpr int HV_G = 4;
-__global__ void __launch_bounds__(256) k_hv_score(GridDev gd, const float4* __restrict__ model, int n_model, int stride,
-                                                  const double* __restrict__ poses, int n_hyp, float r2,
-                                                  float* __restrict__ score) {
+// Inlier count of every hypothesis: model points (every stride-th) moved by
+// the hypothesis pose with a scene point within sqrt(r2).  Blocks cover
+// (hypothesis, run of HV_PPB points); counts are integers, so the order of
+// the atomic adds does not matter.
+constexpr int HV_PPB = 256;
+__global__ void __launch_bounds__(256) k_hv_count(GridDev gd, const float4* __restrict__ model, int n_model, int stride,
+                                                  const double* __restrict__ poses, int n_hyp, float r2, int bph,
+                                                  int* __restrict__ counts) {
   __shared__ int s_cnt;
-  const int h = blockIdx.x;
+  const int h = blockIdx.x / bph, part = blockIdx.x - h * bph;
   if (h >= n_hyp) return;
   const GridView g = load_view(gd);
   float T[12];
@@ -113,7 +118,8 @@ __global__ void __launch_bounds__(256) k_hv_score(GridDev gd, const float4* __re
   const unsigned gmask = ((1u << HV_G) - 1u) << (lane & ~(HV_G - 1));
   int cnt = 0;
   const int total = (n_model + stride - 1) / stride;
-  for (int i = threadIdx.x / HV_G; i < total; i += blockDim.x / HV_G) {
+  const int i1 = min(total, (part + 1) * HV_PPB);
+  for (int i = part * HV_PPB + threadIdx.x / HV_G; i < i1; i += blockDim.x / HV_G) {
     const float4 p = xform_exact(T, model[(size_t)i * stride]);
     float d2;
     int bi, bp;
@@ -122,23 +128,60 @@ __global__ void __launch_bounds__(256) k_hv_score(GridDev gd, const float4* __re
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-  if (lane == 0) atomicAdd(&s_cnt, cnt);
+  if (lane == 0 && cnt) atomicAdd(&s_cnt, cnt);
   __syncthreads();
-  if (threadIdx.x == 0) score[h] = total > 0 ? (float)s_cnt / (float)total : 0.f;
+  if (threadIdx.x == 0 && s_cnt) atomicAdd(counts + h, s_cnt);
 }
 
-// Top-m hypotheses by score (ties: lower hypothesis index) -> order[0..m)
+__global__ void k_hv_finish(const int* __restrict__ counts, int n_hyp, int total, float* __restrict__ score) {
+  for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < n_hyp; h += gridDim.x * blockDim.x)
+    score[h] = total > 0 ? (float)counts[h] / (float)total : 0.f;
+}
+
+static rtr_status hv_score(GridDev gd, const float4* model, int n_model, int stride, const double* poses, int n_hyp,
+                           float r2, int* counts, float* score, cudaStream_t st) {
+  const int total = (n_model + stride - 1) / stride;
+  const int bph = (total + HV_PPB - 1) / HV_PPB > 0 ? (total + HV_PPB - 1) / HV_PPB : 1;
+  RTR_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * (size_t)n_hyp, st));
+  k_hv_count<<<n_hyp * bph, 256, 0, st>>>(gd, model, n_model, stride, poses, n_hyp, r2, bph, counts);
+  k_hv_finish<<<(n_hyp + 255) / 256, 256, 0, st>>>(counts, n_hyp, total, score);
+  RTR_LAUNCHED(2);
+  return RTR_OK;
+}
+
+// Top-m hypotheses by score (ties: lower hypothesis index) -> order[0..m);
+// one warp, scores staged in shared memory (n <= 256).
 __global__ void k_topm(const float* __restrict__ score, int n, int m, int* __restrict__ order) {
-  if (threadIdx.x != 0) return;
+  __shared__ float s_sc[256];
+  const int lane = threadIdx.x;
+  if (lane >= 32) return;
+  for (int h = lane; h < 256; h += 32) s_sc[h] = h < n ? score[h] : 0.f;
+  bool used[8] = {false, false, false, false, false, false, false, false};  // hypothesis lane + 32 q taken
+  __syncwarp();
   for (int k = 0; k < m; ++k) {
     int best = -1;
-    for (int h = 0; h < n; ++h) {
-      bool used = false;
-      for (int j = 0; j < k; ++j) used |= order[j] == h;
-      if (used) continue;
-      if (best < 0 || score[h] > score[best]) best = h;
+    float bs = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int h = lane + 32 * q;
+      if (h < n && !used[q] && (best < 0 || s_sc[h] > bs)) {
+        best = h;
+        bs = s_sc[h];
+      }
     }
-    order[k] = best;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const int ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const float os = __shfl_xor_sync(0xffffffffu, bs, o);
+      if (ob >= 0 && (best < 0 || os > bs || (os == bs && ob < best))) {
+        best = ob;
+        bs = os;
+      }
+    }
+    if (lane == 0) order[k] = best;
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (best == lane + 32 * q) used[q] = true;
   }
 }
 
@@ -223,7 +266,7 @@ struct rtr_model {
   GridMeta* vox_meta = nullptr;  // bbox of the voxel cloud (ICP centring)
   __nv_bfloat16* db_hi = nullptr;  // [n_kp][384] descriptor split for the tensor cores
   __nv_bfloat16* db_lo = nullptr;
-  float* db_n2 = nullptr;          // [n_kp] squared norms
+  float* db_n2 = nullptr;          // [n_kp + 1] squared norms, then their maximum
 };
 
 extern "C" {
@@ -319,7 +362,7 @@ rtr_status rtr_model_create(rtr_context* ctx, const float* d_pts, int n, const r
   RTR_LAUNCHED(1);
   if (cudaMalloc(&m->db_hi, match_tc_bf16_bytes(K)) != cudaSuccess ||
       cudaMalloc(&m->db_lo, match_tc_bf16_bytes(K)) != cudaSuccess ||
-      cudaMalloc(&m->db_n2, (size_t)K * sizeof(float)) != cudaSuccess) {
+      cudaMalloc(&m->db_n2, (size_t)(K + 1) * sizeof(float)) != cudaSuccess) {
     cudaGetLastError();
     return cleanup(fail(RTR_ERR_OOM, "rtr_model_create: tensor-core database"));
   }
@@ -378,6 +421,7 @@ struct RecogBufs {
   double *poses, *init, *refined;
   int *sizes, *order;
   float *hv, *fscore;
+  int* hvcnt;
   rtr_icp_result* res;
   GridBufs grid;
 };
@@ -402,6 +446,7 @@ static void recog_persistent_plan(ScratchPlan& p, int n, const rtr_recog_params*
   p.add<int>(M);
   p.add<float>(H);
   p.add<float>(M);
+  p.add<int>(H > M ? H : M);
   p.add<rtr_icp_result>(M);
   grid_plan(p, n, default_cell_cap(n));
 }
@@ -430,6 +475,7 @@ static bool recog_take(Scratch& s, int n, const rtr_recog_params* q, RecogBufs* 
   b->order = s.take<int>(M);
   b->hv = s.take<float>(H);
   b->fscore = s.take<float>(M);
+  b->hvcnt = s.take<int>(H > M ? H : M);
   b->res = s.take<rtr_icp_result>(M);
   return b->res && grid_take(s, n, default_cell_cap(n), &b->grid);
 }
@@ -546,11 +592,11 @@ static rtr_status recognize_impl(rtr_context* ctx, const rtr_model* m, const flo
   {
     ProfScope ps(ctx, st, "verify");
     grid_build(b.grid, b.sv, n, dV, q->icp_max_dist, st);
-    k_hv_score<<<ncl, 256, 0, st>>>(grid_dev(b.grid), m->vox, m->n_vox, q->hv_subsample > 0 ? q->hv_subsample : 1,
-                                    b.poses, ncl, q->hv_inlier_r * q->hv_inlier_r, b.hv);
+    RTR_TRY(hv_score(grid_dev(b.grid), m->vox, m->n_vox, q->hv_subsample > 0 ? q->hv_subsample : 1, b.poses, ncl,
+                     q->hv_inlier_r * q->hv_inlier_r, b.hvcnt, b.hv, st));
     k_topm<<<1, 32, 0, st>>>(b.hv, ncl, M, b.order);
     k_select_poses<<<1, 256, 0, st>>>(b.poses, b.order, M, b.init);
-    RTR_LAUNCHED(3);
+    RTR_LAUNCHED(2);
   }
   {
     ProfScope ps(ctx, st, "icp_refine");
@@ -577,12 +623,12 @@ static rtr_status recognize_impl(rtr_context* ctx, const rtr_model* m, const flo
   {
     ProfScope ps(ctx, st, "final_score");
     k_copy_result_poses<<<1, 256, 0, st>>>(b.res, M, b.refined);
-    k_hv_score<<<M, 256, 0, st>>>(grid_dev(b.grid), m->vox, m->n_vox, 1, b.refined, M,
-                                  q->accept_inlier_r * q->accept_inlier_r, b.fscore);
+    RTR_TRY(hv_score(grid_dev(b.grid), m->vox, m->n_vox, 1, b.refined, M, q->accept_inlier_r * q->accept_inlier_r,
+                     b.hvcnt, b.fscore, st));
     const float nms2 = q->nms_dist * q->nms_dist;
     k_finalize<<<1, 32, 0, st>>>(b.fscore, b.refined, b.order, b.sizes, M, q->accept_score, nms2,
                                  q->max_instances, dV, dKeys, dC, ncl, out);
-    RTR_LAUNCHED(3);
+    RTR_LAUNCHED(2);
   }
   RTR_CUDA(cudaGetLastError());
   return RTR_OK;

@@ -56,3 +56,27 @@ def test_match_tc_duplicates_tie_to_lowest(ctx, descs):
     db = np.concatenate([md[:50]] * 12)  # every descriptor 12 times
     idx, _ = ctx.match(_dev(md[:50]), _dev(db))
     assert np.array_equal(idx.cpu().numpy(), np.arange(50))
+
+
+@pytest.mark.parametrize("scale", [1e-3, 37.0, 1e3])
+def test_match_tc_scaled_descriptors(ctx, descs, scale):
+    # the certification bound scales with the descriptor norms
+    md, sd = descs
+    q = (sd[:3000] * np.float32(scale)).astype(np.float32)
+    db = (md * np.float32(scale)).astype(np.float32)
+    idx, d2 = ctx.match(_dev(q), _dev(db))
+    ri, rd = O.match(q, db)
+    assert np.array_equal(idx.cpu().numpy(), ri)
+    assert np.array_equal(d2.cpu().numpy(), rd)
+
+
+def test_match_tc_general_vectors(ctx):
+    # signed, non-normalised vectors whose distances crowd together: most
+    # queries cannot be certified and go through the exact re-scan
+    rng = np.random.default_rng(12)
+    q = rng.standard_normal((1500, 352)).astype(np.float32)
+    db = rng.standard_normal((2500, 352)).astype(np.float32)
+    idx, d2 = ctx.match(_dev(q), _dev(db))
+    ri, rd = O.match(q, db)
+    assert np.array_equal(idx.cpu().numpy(), ri)
+    assert np.array_equal(d2.cpu().numpy(), rd)
