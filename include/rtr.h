@@ -375,6 +375,40 @@ rtr_status rtr_recognize(rtr_context* ctx, const rtr_model* model, const float* 
 rtr_status rtr_recognize_host(rtr_context* ctx, const rtr_model* model, const float* h_scene, int n,
                               const rtr_recog_params* p, rtr_recog_result* h_result);
 
+/* ---- learned keypoint credibility ------------------------------------------
+ * A small MLP scores each keypoint's SHOT-352 descriptor (352 -> 128 -> 64 ->
+ * 1, ReLU, ReLU, sigmoid) so that low-credibility keypoints can be dropped
+ * before matching.  No counterpart in the reference, whose README names the
+ * problem.  Parameters (RTR_MLP_PARAMS floats, in this order): W1[128][352],
+ * b1[128], W2[64][128], b2[64], w3[64], b3.  Forward passes use the weight
+ * matrices rounded to BF16 and accumulate in FP32; training is Adam (beta1
+ * 0.9, beta2 0.999, eps 1e-8) on the mean binary cross-entropy of the logit,
+ * with gradients taken for the FP32 master weights. */
+#define RTR_MLP_PARAMS 53505
+typedef struct rtr_mlp rtr_mlp;
+/* h_params: RTR_MLP_PARAMS floats, or NULL for a seeded He-uniform start
+ * (zero biases).  Synchronises. */
+rtr_status rtr_mlp_create(rtr_context* ctx, const float* h_params, uint64_t seed, rtr_mlp** out);
+rtr_status rtr_mlp_destroy(rtr_mlp* m);
+/* FP32 master weights to / from the host (setting them resets Adam). */
+rtr_status rtr_mlp_get_params(const rtr_mlp* m, float* h_params);
+rtr_status rtr_mlp_set_params(rtr_mlp* m, const float* h_params);
+/* Credibility in (0, 1) of n descriptors (device [n][352] -> device [n]). */
+rtr_status rtr_mlp_score(rtr_context* ctx, const rtr_mlp* m, const float* d_x, int n, float* d_score,
+                         rtr_stream_t stream);
+/* Mean loss and its gradient (RTR_MLP_PARAMS floats, device) on n labelled
+ * rows (labels 0 or 1, device [n]); no update. */
+rtr_status rtr_mlp_loss_grad(rtr_context* ctx, const rtr_mlp* m, const float* d_x, const float* d_y, int n,
+                             float* d_grad, float* d_loss, rtr_stream_t stream);
+/* One Adam step on the n rows given. */
+rtr_status rtr_mlp_train_step(rtr_context* ctx, rtr_mlp* m, const float* d_x, const float* d_y, int n, float lr,
+                              float* d_loss, rtr_stream_t stream);
+/* Minibatch training: `epochs` passes over the n rows in a seeded shuffled
+ * order, batches of `batch` rows.  h_epoch_loss (optional, `epochs` floats)
+ * receives the row-weighted mean batch loss of each epoch.  Synchronises. */
+rtr_status rtr_mlp_train(rtr_context* ctx, rtr_mlp* m, const float* d_x, const float* d_y, int n, int batch,
+                         int epochs, float lr, uint64_t seed, float* h_epoch_loss);
+
 /* ---- synthetic inputs (host only; seeded, identical on every machine) ----- */
 
 /* Shapes: 0 = chair (seat 0.45x0.45x0.03, four legs 0.03x0.03x0.45, backrest

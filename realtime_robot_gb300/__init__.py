@@ -142,6 +142,14 @@ _SIG = {
     "rtr_gc_group": (_I, [_P, _P, _P, _P, _P, _P, _I, _F, _I, _I, _I, _P, _P, _P,
                           C.POINTER(C.c_int), _P]),
     "rtr_gc_stats": (_I, [_P, C.POINTER(C.c_int * 8)]),
+    "rtr_mlp_create": (_I, [_P, _P, _U64, C.POINTER(_P)]),
+    "rtr_mlp_destroy": (_I, [_P]),
+    "rtr_mlp_get_params": (_I, [_P, _P]),
+    "rtr_mlp_set_params": (_I, [_P, _P]),
+    "rtr_mlp_score": (_I, [_P, _P, _P, _I, _P, _P]),
+    "rtr_mlp_loss_grad": (_I, [_P, _P, _P, _P, _I, _P, _P, _P]),
+    "rtr_mlp_train_step": (_I, [_P, _P, _P, _P, _I, _F, _P, _P]),
+    "rtr_mlp_train": (_I, [_P, _P, _P, _P, _I, _I, _I, _F, _U64, _P]),
     "rtr_recog_default_params": (None, [C.POINTER(RecogParams)]),
     "rtr_model_create": (_I, [_P, _P, _I, C.POINTER(RecogParams), C.POINTER(_P)]),
     "rtr_model_destroy": (_I, [_P]),
@@ -434,6 +442,67 @@ class Context:
         check(lib().rtr_tdf_batch(self.h, _ptr(occ), _ptr(offsets), n, dim, _ptr(out),
                                   _stream(stream)))
         return out
+
+
+MLP_PARAMS = 53505  # RTR_MLP_PARAMS
+
+
+class Mlp:
+    """The keypoint-credibility MLP on the device (rtr_mlp_*)."""
+
+    def __init__(self, ctx: "Context", params: np.ndarray | None = None, seed: int = 0):
+        self.ctx = ctx
+        h = _P()
+        p = None if params is None else np.ascontiguousarray(params, np.float32)
+        check(lib().rtr_mlp_create(ctx.h, None if p is None else p.ctypes.data, seed, C.byref(h)))
+        self.h = h
+
+    def params(self) -> np.ndarray:
+        out = np.empty(MLP_PARAMS, np.float32)
+        check(lib().rtr_mlp_get_params(self.h, out.ctypes.data))
+        return out
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, np.float32)
+        check(lib().rtr_mlp_set_params(self.h, p.ctypes.data))
+
+    def score(self, x, stream=None):
+        import torch
+        s = torch.empty(x.shape[0], dtype=torch.float32, device=x.device)
+        check(lib().rtr_mlp_score(self.ctx.h, self.h, _ptr(x), x.shape[0], _ptr(s), _stream(stream)))
+        return s
+
+    def loss_grad(self, x, y, stream=None):
+        import torch
+        g = torch.empty(MLP_PARAMS, dtype=torch.float32, device=x.device)
+        loss = torch.empty(1, dtype=torch.float32, device=x.device)
+        check(lib().rtr_mlp_loss_grad(self.ctx.h, self.h, _ptr(x), _ptr(y), x.shape[0], _ptr(g), _ptr(loss),
+                                      _stream(stream)))
+        return loss, g
+
+    def train_step(self, x, y, lr=1e-3, stream=None):
+        import torch
+        loss = torch.empty(1, dtype=torch.float32, device=x.device)
+        check(lib().rtr_mlp_train_step(self.ctx.h, self.h, _ptr(x), _ptr(y), x.shape[0], float(lr), _ptr(loss),
+                                       _stream(stream)))
+        return loss
+
+    def train(self, x, y, batch=4096, epochs=20, lr=1e-3, seed=0) -> np.ndarray:
+        out = np.zeros(epochs, np.float32)
+        check(lib().rtr_mlp_train(self.ctx.h, self.h, _ptr(x), _ptr(y), x.shape[0], int(batch), int(epochs),
+                                  float(lr), int(seed), out.ctypes.data))
+        return out
+
+    def close(self):
+        if self.h:
+            lib().rtr_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Model:

@@ -136,14 +136,18 @@ __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::
 // ---------------------------------------------------------------------------
 // FP32 descriptors -> padded (hi, lo) BF16 rows + FP32 squared norms
 // ---------------------------------------------------------------------------
+// hi/lo split of each row, padded to TC_KPAD.  Column TC_DIM carries the
+// norm term so that the GEMM yields q.b - |b|^2 / 2 directly: 1 in query
+// rows, -|b|^2 / 2 (itself split) in database rows.
 __global__ void k_split_bf16(const float* __restrict__ x, int n_host, const int* d_n, int n_cap,
                              __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
-                             float* __restrict__ norm2, unsigned* __restrict__ max_bits) {
+                             float* __restrict__ norm2, unsigned* __restrict__ max_bits, bool is_db) {
   const int n = d_n ? min(*d_n, n_cap) : n_host;
   const int lane = threadIdx.x & 31;
   for (int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < n_cap; r += gridDim.x * (blockDim.x >> 5)) {
     float ss = 0.f;
     for (int k = lane; k < TC_KPAD; k += 32) {
+      if (k == TC_DIM) continue;  // written below
       const float v = (r < n && k < TC_DIM) ? x[(size_t)r * TC_DIM + k] : 0.f;
       const __nv_bfloat16 h = __float2bfloat16_rn(v);
       const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
@@ -156,6 +160,10 @@ __global__ void k_split_bf16(const float* __restrict__ x, int n_host, const int*
     if (lane == 0) {
       norm2[r] = ss;
       if (max_bits && r < n) atomicMax(max_bits, __float_as_uint(ss));  // ss >= 0 (or NaN: stays largest)
+      const float v = r < n ? (is_db ? -0.5f * ss : 1.f) : 0.f;
+      const __nv_bfloat16 h = __float2bfloat16_rn(v);
+      hi[(size_t)r * TC_KPAD + TC_DIM] = h;
+      lo[(size_t)r * TC_KPAD + TC_DIM] = __float2bfloat16_rn(v - __bfloat162float(h));
     }
   }
 }
@@ -169,7 +177,6 @@ struct TcArgs {
   int nq_cap;
   int ndb;
   const float* qn;   // [nq_cap] |q|^2
-  const float* dn;   // [ndb]   |b|^2
   int* cand_idx;     // [nq_cap][8]
   float* cand_d;     // [nq_cap][8]
   int* status;
@@ -265,14 +272,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constan
     }
   } else {
     // ---------------- epilogue: warps 0-3, thread = query row ----------------
+    // The accumulator holds q.b - |b|^2 / 2, so the nearest rows are the
+    // largest values: one compare per element, d~ = |q|^2 - 2 acc at the end.
     const int row = warp * 32 + lane;
     const int q = q0 + row;
     const float qn = q < nq ? a.qn[q] : 0.f;
-    float bd[TC_TOP];
+    float ba[TC_TOP];
     int bi[TC_TOP];
 #pragma unroll
     for (int s = 0; s < TC_TOP; ++s) {
-      bd[s] = __int_as_float(0x7f800000);
+      ba[s] = -__int_as_float(0x7f800000);
       bi[s] = 0x7fffffff;
     }
     for (int t = 0; t < n_tiles; ++t) {
@@ -281,26 +290,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constan
       if (!mbar_wait(&acc_full[buf], use & 1u, abort)) break;
       tc_fence_after();
       const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)buf * TC_BN;
+      const int valid = min(TC_BN, a.ndb - t * TC_BN);  // rows past the database read as zero
       for (int c0 = 0; c0 < TC_BN; c0 += 32) {
         float v[32];
         tmem_ld32(taddr + (uint32_t)c0, v);
+        const int jb = t * TC_BN + c0;
+        const int lim = valid - c0;
 #pragma unroll
         for (int i = 0; i < 32; ++i) {
-          const int j = t * TC_BN + c0 + i;
-          if (j >= a.ndb) break;
-          const float d = qn + __ldg(a.dn + j) - 2.f * v[i];
-          if (d < bd[TC_TOP - 1]) {
-            bd[TC_TOP - 1] = d;
-            bi[TC_TOP - 1] = j;
+          if (v[i] > ba[TC_TOP - 1] && i < lim) {
+            ba[TC_TOP - 1] = v[i];
+            bi[TC_TOP - 1] = jb + i;
 #pragma unroll
             for (int s = TC_TOP - 1; s > 0; --s) {
-              const bool lt = bd[s] < bd[s - 1];
-              const float x0 = bd[s], x1 = bd[s - 1];
+              const bool gt = ba[s] > ba[s - 1];
+              const float x0 = ba[s], x1 = ba[s - 1];
               const int y0 = bi[s], y1 = bi[s - 1];
-              bd[s] = lt ? x1 : x0;
-              bd[s - 1] = lt ? x0 : x1;
-              bi[s] = lt ? y1 : y0;
-              bi[s - 1] = lt ? y0 : y1;
+              ba[s] = gt ? x1 : x0;
+              ba[s - 1] = gt ? x0 : x1;
+              bi[s] = gt ? y1 : y0;
+              bi[s - 1] = gt ? y0 : y1;
             }
           }
         }
@@ -312,7 +321,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constan
 #pragma unroll
       for (int s = 0; s < TC_TOP; ++s) {
         a.cand_idx[(size_t)q * TC_TOP + s] = bi[s] == 0x7fffffff ? -1 : bi[s];
-        a.cand_d[(size_t)q * TC_TOP + s] = bd[s];
+        a.cand_d[(size_t)q * TC_TOP + s] = bi[s] == 0x7fffffff ? __int_as_float(0x7f800000) : qn - 2.f * ba[s];
       }
     }
   }
@@ -504,7 +513,8 @@ rtr_status match_tc_prepare_db(const float* db, int ndb, __nv_bfloat16* hi, __nv
   if (blocks < 1) blocks = 1;
   // norm2[ndb] receives the largest squared norm (scales the error bound)
   RTR_CUDA(cudaMemsetAsync(norm2 + ndb, 0, sizeof(float), st));
-  k_split_bf16<<<blocks, 256, 0, st>>>(db, ndb, nullptr, ndb, hi, lo, norm2, reinterpret_cast<unsigned*>(norm2 + ndb));
+  k_split_bf16<<<blocks, 256, 0, st>>>(db, ndb, nullptr, ndb, hi, lo, norm2, reinterpret_cast<unsigned*>(norm2 + ndb),
+                                       true);
   RTR_LAUNCHED(1);
   RTR_CUDA(cudaGetLastError());
   return RTR_OK;
@@ -535,7 +545,7 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
   if (!nredo) return fail(RTR_ERR_CAPACITY, "match_tc: scratch");
   int sb = (nqp + 7) / 8;
   if (sb > 152 * 16) sb = 152 * 16;
-  k_split_bf16<<<sb, 256, 0, st>>>(q, nq_cap, d_nq, nqp, qhi, qlo, qn, nullptr);
+  k_split_bf16<<<sb, 256, 0, st>>>(q, nq_cap, d_nq, nqp, qhi, qlo, qn, nullptr, false);
   CUtensorMap m_qh, m_ql, m_bh, m_bl;
   if (!make_map(&m_qh, qhi, nqp, TC_BM) || !make_map(&m_ql, qlo, nqp, TC_BM) || !make_map(&m_bh, db_hi, ndb, TC_BN) ||
       !make_map(&m_bl, db_lo, ndb, TC_BN))
@@ -546,7 +556,7 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
     RTR_CUDA(cudaFuncSetAttribute(k_match_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = true;
   }
-  TcArgs a{nq_cap, d_nq, nq_cap, ndb, qn, db_n2, cidx, cd, ctx->d_status};
+  TcArgs a{nq_cap, d_nq, nq_cap, ndb, qn, cidx, cd, ctx->d_status};
   {
     ProfScope pg(ctx, st, "match_gemm");
     k_match_tc<<<nqp / TC_BM, TC_THREADS, smem, st>>>(m_qh, m_ql, m_bh, m_bl, a);

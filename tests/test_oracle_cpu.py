@@ -124,3 +124,25 @@ def test_tdf_oracle_small_cases():
     # layout: x fastest (kernel.cu:16-18)
     out = O.tdf(np.array([[5, 0, 0]]), 6)
     assert out[5] == 0 and out[6 * 6 * 6 - 1] == (0 + 25 + 25)
+
+
+def test_mlp_oracle_gradient_finite_differences():
+    # pins the oracle's backward pass: central differences of its own loss
+    # along the biases (the weight matrices are rounded to BF16 in the
+    # forward pass, so their finite differences are steps, not slopes)
+    from oracle import mlp as OM
+    rng = np.random.default_rng(0)
+    theta = OM.init_params(9).astype(np.float64)
+    X = np.abs(rng.standard_normal((64, 352))).astype(np.float32)
+    X /= np.linalg.norm(X, axis=1, keepdims=True)
+    y = (rng.random(64) > 0.5).astype(np.float32)
+    _, g = OM.loss_and_grad(theta, X, y)
+    p = OM.unpack(np.arange(OM.N_PARAMS))
+    for name in ("b1", "b2", "b3"):
+        for idx in p[name].ravel()[:8]:
+            e = np.zeros(OM.N_PARAMS)
+            e[int(idx)] = 1e-5
+            lp, _ = OM.loss_and_grad((theta + e).astype(np.float32), X, y)
+            lm, _ = OM.loss_and_grad((theta - e).astype(np.float32), X, y)
+            fd = (lp - lm) / (2e-5)
+            assert abs(fd - g[int(idx)]) < 2e-4 + 1e-2 * abs(fd), (name, int(idx), fd, g[int(idx)])
