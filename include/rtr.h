@@ -52,6 +52,7 @@ typedef enum rtr_status {
 } rtr_status;
 
 typedef struct rtr_context rtr_context;
+typedef struct rtr_mlp rtr_mlp;   /* learned keypoint credibility (below) */
 
 /* ---- library / context ------------------------------------------------- */
 
@@ -371,6 +372,14 @@ rtr_status rtr_model_buffers(const rtr_model* m, const float** d_vox, const floa
 rtr_status rtr_recognize(rtr_context* ctx, const rtr_model* model, const float* d_scene, int n,
                          const rtr_recog_params* p, rtr_recog_result* d_result,
                          rtr_stream_t stream);
+/* Recognition with learned keypoint pruning (the "learned" form): after the
+ * SHOT stage, `mlp` scores every scene keypoint's descriptor and only the
+ * ceil(keep * K) most credible keypoints (ties: lower keypoint index) go on to
+ * matching, in their original order; the rest is rtr_recognize's chain.
+ * keep in (0, 1] (0.25 keeps the top quarter). */
+rtr_status rtr_recognize_learned(rtr_context* ctx, const rtr_model* model, const rtr_mlp* mlp, float keep,
+                                 const float* d_scene, int n, const rtr_recog_params* p,
+                                 rtr_recog_result* d_result, rtr_stream_t stream);
 /* Same with a HOST scene and a HOST result (copies in and out). */
 rtr_status rtr_recognize_host(rtr_context* ctx, const rtr_model* model, const float* h_scene, int n,
                               const rtr_recog_params* p, rtr_recog_result* h_result);
@@ -385,7 +394,6 @@ rtr_status rtr_recognize_host(rtr_context* ctx, const rtr_model* model, const fl
  * 0.9, beta2 0.999, eps 1e-8) on the mean binary cross-entropy of the logit,
  * with gradients taken for the FP32 master weights. */
 #define RTR_MLP_PARAMS 53505
-typedef struct rtr_mlp rtr_mlp;
 /* h_params: RTR_MLP_PARAMS floats, or NULL for a seeded He-uniform start
  * (zero biases).  Synchronises. */
 rtr_status rtr_mlp_create(rtr_context* ctx, const float* h_params, uint64_t seed, rtr_mlp** out);

@@ -157,6 +157,7 @@ _SIG = {
     "rtr_model_buffers": (_I, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P), C.POINTER(_P),
                                C.POINTER(_P)]),
     "rtr_recognize": (_I, [_P, _P, _P, _I, C.POINTER(RecogParams), _P, _P]),
+    "rtr_recognize_learned": (_I, [_P, _P, _P, _F, _P, _I, C.POINTER(RecogParams), _P, _P]),
     "rtr_recognize_host": (_I, [_P, _P, _P, _I, C.POINTER(RecogParams), C.POINTER(RecogResult)]),
     "rtr_synth_shape": (_I, [_I, _U64, _I, _P]),
     "rtr_synth_rigid": (None, [_U64, _D, _D, _P]),
@@ -545,6 +546,19 @@ def recognize(ctx: "Context", model: Model, scene, params: RecogParams | None = 
         result = torch.zeros(C.sizeof(RecogResult), dtype=torch.uint8, device=scene.device)
     check(lib().rtr_recognize(ctx.h, model.h, _ptr(scene), scene.shape[0], C.byref(p),
                               _ptr(result), _stream(stream)))
+    return result
+
+
+def recognize_learned(ctx: "Context", model: Model, mlp: "Mlp", scene, keep: float = 0.25,
+                      params: RecogParams | None = None, result=None, stream=None):
+    """rtr_recognize_learned: recognition with the MLP keeping the `keep`
+    fraction of most credible scene keypoints before matching."""
+    import torch
+    p = params or model.params
+    if result is None:
+        result = torch.zeros(C.sizeof(RecogResult), dtype=torch.uint8, device=scene.device)
+    check(lib().rtr_recognize_learned(ctx.h, model.h, mlp.h, float(keep), _ptr(scene), scene.shape[0], C.byref(p),
+                                      _ptr(result), _stream(stream)))
     return result
 
 

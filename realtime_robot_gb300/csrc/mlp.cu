@@ -60,10 +60,12 @@ template <typename TB, int EPI>
 __global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, const float* __restrict__ A, long long sam,
                                               long long sak, const TB* __restrict__ B, long long sbn, long long sbk,
                                               float* __restrict__ Cm, int ldc, const float* __restrict__ bias,
-                                              const float* __restrict__ mask) {
+                                              const float* __restrict__ mask, const int* __restrict__ dM) {
   __shared__ float As[GK][GT + 4], Bs[GK][GT + 4];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const int m0 = blockIdx.y * GT, n0 = blockIdx.x * GT;
+  if (dM) M = min(*dM, M);  // rows counted on the device (grid sized for the capacity)
+  if (m0 >= M) return;      // uniform per block, before any barrier
   float acc[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
@@ -128,9 +130,10 @@ __global__ void __launch_bounds__(256) k_gemm(int M, int N, int K, const float* 
 
 template <typename TB, int EPI>
 static void gemm(int M, int N, int K, const float* A, long long sam, long long sak, const TB* B, long long sbn,
-                 long long sbk, float* C, int ldc, const float* bias, const float* mask, cudaStream_t st) {
+                 long long sbk, float* C, int ldc, const float* bias, const float* mask, cudaStream_t st,
+                 const int* dM = nullptr) {
   const dim3 grid((N + GT - 1) / GT, (M + GT - 1) / GT);
-  k_gemm<TB, EPI><<<grid, 256, 0, st>>>(M, N, K, A, sam, sak, B, sbn, sbk, C, ldc, bias, mask);
+  k_gemm<TB, EPI><<<grid, 256, 0, st>>>(M, N, K, A, sam, sak, B, sbn, sbk, C, ldc, bias, mask, dM);
   RTR_LAUNCHED(1);
 }
 
@@ -140,7 +143,9 @@ static void gemm(int M, int N, int K, const float* A, long long sam, long long s
 // ---------------------------------------------------------------------------
 __global__ void k_head(const float* __restrict__ h2, int n, const __nv_bfloat16* __restrict__ w3bf,
                        const float* __restrict__ theta, const float* __restrict__ y, float* __restrict__ score,
-                       float* __restrict__ dz, float* __restrict__ dh2, float* __restrict__ loss_terms) {
+                       float* __restrict__ dz, float* __restrict__ dh2, float* __restrict__ loss_terms,
+                       const int* __restrict__ d_n) {
+  if (d_n) n = min(*d_n, n);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float* h = h2 + (size_t)i * MLP_H2;
     float z = 0.f;
@@ -258,7 +263,7 @@ static void mlp_pass(const rtr_mlp* m, const float* X, const float* y, int n, fl
   int hb = (n + 255) / 256;
   if (hb > 152 * 8) hb = 152 * 8;
   if (hb < 1) hb = 1;
-  k_head<<<hb, 256, 0, st>>>(w.h2, n, m->wbf + BF_W3, th, y, score, w.dz, w.dh2, w.loss_terms);
+  k_head<<<hb, 256, 0, st>>>(w.h2, n, m->wbf + BF_W3, th, y, score, w.dz, w.dh2, w.loss_terms, nullptr);
   RTR_LAUNCHED(1);
   if (!y) return;
   float* g = w.grad;
@@ -317,6 +322,34 @@ rtr_status mlp_score_dev(rtr_context* ctx, Scratch& s, const rtr_mlp* m, const f
   if (!mlp_take(s, n, &w)) return fail(RTR_ERR_CAPACITY, "mlp: scratch");
   (void)ctx;
   mlp_pass(m, X, nullptr, n, score, w, nullptr, st);
+  RTR_CUDA(cudaGetLastError());
+  return RTR_OK;
+}
+
+// Scores of the first *d_n (<= n_cap) rows of X, for callers whose row count
+// lives on the device; needs mlp_infer_bytes(n_cap) of scratch.
+size_t mlp_infer_bytes(int n_cap) {
+  ScratchPlan p;
+  p.add<float>((size_t)(n_cap > 0 ? n_cap : 1) * MLP_H1);
+  p.add<float>((size_t)(n_cap > 0 ? n_cap : 1) * MLP_H2);
+  return p.bytes;
+}
+
+rtr_status mlp_score_rows(Scratch& s, const rtr_mlp* m, const float* X, int n_cap, const int* d_n, float* score,
+                          cudaStream_t st) {
+  if (n_cap <= 0) return RTR_OK;
+  float* h1 = s.take<float>((size_t)n_cap * MLP_H1);
+  float* h2 = s.take<float>((size_t)n_cap * MLP_H2);
+  if (!h2) return fail(RTR_ERR_CAPACITY, "mlp: scratch");
+  const float* th = m->theta;
+  gemm<__nv_bfloat16, 1>(n_cap, MLP_H1, MLP_IN, X, MLP_IN, 1, m->wbf + BF_W1, MLP_IN, 1, h1, MLP_H1, th + OFF_B1,
+                         nullptr, st, d_n);
+  gemm<__nv_bfloat16, 1>(n_cap, MLP_H2, MLP_H1, h1, MLP_H1, 1, m->wbf + BF_W2, MLP_H1, 1, h2, MLP_H2, th + OFF_B2,
+                         nullptr, st, d_n);
+  int hb = (n_cap + 255) / 256;
+  if (hb > 152 * 8) hb = 152 * 8;
+  k_head<<<hb, 256, 0, st>>>(h2, n_cap, m->wbf + BF_W3, th, nullptr, score, nullptr, nullptr, nullptr, d_n);
+  RTR_LAUNCHED(1);
   RTR_CUDA(cudaGetLastError());
   return RTR_OK;
 }

@@ -36,6 +36,9 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
                         int ndb, const __nv_bfloat16* db_hi, const __nv_bfloat16* db_lo, const float* db_n2,
                         int* out_idx, float* out_d2, cudaStream_t st);
 size_t gc_scratch_bytes(int C, int max_clusters);
+size_t mlp_infer_bytes(int n_cap);
+rtr_status mlp_score_rows(Scratch& s, const rtr_mlp* m, const float* X, int n_cap, const int* d_n, float* score,
+                          cudaStream_t st);
 __global__ void k_orient_outward(const float4* __restrict__ pts, float4* __restrict__ nrm, int n_host, const int* d_n,
                                  float rc2, float gap, float len);
 rtr_status gc_group_dev(rtr_context* ctx, Scratch& s, const float* d_model_kp, const float* d_scene_kp,
@@ -66,6 +69,44 @@ __global__ void k_compact_int(const int* __restrict__ in, const uint32_t* __rest
                               const uint32_t* __restrict__ pos, int cap, int* __restrict__ out) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += gridDim.x * blockDim.x)
     if (flags[i]) out[pos[i]] = in[i];
+}
+
+// Learned pruning: sort keys putting higher credibility first (scores are
+// in (0, 1); anything else sorts last), then flags for the first
+// ceil(keep * K) keypoints of that order.
+__global__ void k_score_keys(const float* __restrict__ score, const int* d_nk, int cap, uint32_t* __restrict__ keys) {
+  const int nk = dcount(d_nk, cap);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nk; i += gridDim.x * blockDim.x) {
+    const float v = score[i];
+    keys[i] = (v >= 0.f && v <= 1.f) ? ~__float_as_uint(v) : 0xffffffffu;
+  }
+}
+
+__global__ void k_mark_top(const uint32_t* __restrict__ order, const int* d_nk, int cap, float keep,
+                           uint32_t* __restrict__ flags) {
+  const int nk = dcount(d_nk, cap);
+  int kk = (int)ceil((double)keep * (double)nk);
+  kk = kk < nk ? kk : nk;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += gridDim.x * blockDim.x) {
+    if (i < nk)
+      flags[order[i]] = i < kk ? 1u : 0u;  // order is a permutation of [0, nk)
+    else
+      flags[i] = 0u;
+  }
+}
+
+// Rows of a [cap][352] descriptor array kept by flags, packed in order (warp
+// per row, float4 copies).
+__global__ void k_compact_rows(const float* __restrict__ in, const uint32_t* __restrict__ flags,
+                               const uint32_t* __restrict__ pos, const int* d_nk, int cap, float* __restrict__ out) {
+  const int nk = dcount(d_nk, cap);
+  const int lane = threadIdx.x & 31;
+  for (int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < nk; r += gridDim.x * (blockDim.x >> 5)) {
+    if (!flags[r]) continue;
+    const float4* src = reinterpret_cast<const float4*>(in + (size_t)r * 352);
+    float4* dst = reinterpret_cast<float4*>(out + (size_t)pos[r] * 352);
+    for (int k = lane; k < 88; k += 32) dst[k] = src[k];
+  }
 }
 
 // correspondences: scene keypoint slot i matched to model keypoint idx[i]
@@ -413,7 +454,7 @@ namespace rtr {
 
 // Persistent buffers of one recognition (outlive the stages that fill them).
 struct RecogBufs {
-  int* cnt;                 // [0] V, [1] K (uniform), [2] K (gated), [3] C
+  int* cnt;                 // [0] V, [1] K (uniform), [2] K (gated), [3] C, [4] K (pruned)
   float4 *sv, *sn, *skp;
   int *keys, *keys2, *midx, *cm, *cs;
   float *desc, *md2, *cd;
@@ -423,10 +464,12 @@ struct RecogBufs {
   float *hv, *fscore;
   int* hvcnt;
   rtr_icp_result* res;
+  int* keys_p;              // learned pruning: kept keypoints
+  float* desc_p;            // and their descriptors
   GridBufs grid;
 };
 
-static void recog_persistent_plan(ScratchPlan& p, int n, const rtr_recog_params* q) {
+static void recog_persistent_plan(ScratchPlan& p, int n, const rtr_recog_params* q, bool learned) {
   const int H = q->max_clusters, M = q->refine_top;
   p.add<int>(8);
   p.add<float4>(n);
@@ -449,9 +492,13 @@ static void recog_persistent_plan(ScratchPlan& p, int n, const rtr_recog_params*
   p.add<int>(H > M ? H : M);
   p.add<rtr_icp_result>(M);
   grid_plan(p, n, default_cell_cap(n));
+  if (learned) {
+    p.add<int>(n);
+    p.add<float>((size_t)n * 352);
+  }
 }
 
-static bool recog_take(Scratch& s, int n, const rtr_recog_params* q, RecogBufs* b) {
+static bool recog_take(Scratch& s, int n, const rtr_recog_params* q, bool learned, RecogBufs* b) {
   const int H = q->max_clusters, M = q->refine_top;
   b->cnt = s.take<int>(8);
   b->sv = s.take<float4>(n);
@@ -477,13 +524,29 @@ static bool recog_take(Scratch& s, int n, const rtr_recog_params* q, RecogBufs* 
   b->fscore = s.take<float>(M);
   b->hvcnt = s.take<int>(H > M ? H : M);
   b->res = s.take<rtr_icp_result>(M);
-  return b->res && grid_take(s, n, default_cell_cap(n), &b->grid);
+  if (!b->res || !grid_take(s, n, default_cell_cap(n), &b->grid)) return false;
+  b->keys_p = nullptr;
+  b->desc_p = nullptr;
+  if (learned) {
+    b->keys_p = s.take<int>(n);
+    b->desc_p = s.take<float>((size_t)n * 352);
+    return b->desc_p != nullptr;
+  }
+  return true;
 }
 
-size_t recognize_scratch_bytes(int n, int n_model_vox, int n_model_kp, const rtr_recog_params* q) {
+size_t recognize_scratch_bytes(int n, int n_model_vox, int n_model_kp, const rtr_recog_params* q, bool learned) {
   ScratchPlan p;
-  recog_persistent_plan(p, n, q);
+  recog_persistent_plan(p, n, q, learned);
   size_t stage = 0;
+  if (learned) {
+    ScratchPlan t;
+    t.add<float>(n);
+    for (int i = 0; i < 4; ++i) t.add<uint32_t>(n);
+    t.add<uint32_t>(radix_hist_entries(n));
+    const size_t b = t.bytes + mlp_infer_bytes(n) + 512;
+    stage = b > stage ? b : stage;
+  }
   {
     ScratchPlan t;
     voxseg_plan(t, n);
@@ -511,11 +574,13 @@ size_t recognize_scratch_bytes(int n, int n_model_vox, int n_model_kp, const rtr
 }
 
 static rtr_status recognize_impl(rtr_context* ctx, const rtr_model* m, const float4* scene, int n,
-                                 const rtr_recog_params* q, rtr_recog_result* out, cudaStream_t st) {
+                                 const rtr_recog_params* q, rtr_recog_result* out, cudaStream_t st,
+                                 const rtr_mlp* mlp = nullptr, float keep = 1.f) {
+  const bool learned = mlp != nullptr;
   Scratch s;
-  RTR_TRY(ensure_scratch(ctx, recognize_scratch_bytes(n, m->n_vox, m->n_kp, q), st, &s));
+  RTR_TRY(ensure_scratch(ctx, recognize_scratch_bytes(n, m->n_vox, m->n_kp, q, learned), st, &s));
   RecogBufs b;
-  if (!recog_take(s, n, q, &b)) return fail(RTR_ERR_CAPACITY, "rtr_recognize: scratch carve");
+  if (!recog_take(s, n, q, learned, &b)) return fail(RTR_ERR_CAPACITY, "rtr_recognize: scratch carve");
   const Scratch stage = s;  // everything after this point is per-stage scratch
   int* dV = b.cnt;
   int* dK = b.cnt + 1;
@@ -557,10 +622,36 @@ static rtr_status recognize_impl(rtr_context* ctx, const rtr_model* m, const flo
     Scratch t = stage;
     RTR_TRY(shot_dev(ctx, t, b.sv, b.sn, n, dV, keys, n, dKeys, q->descriptor_r, b.desc, nullptr, st));
   }
+  const float* desc = b.desc;
+  if (learned) {
+    // learned pruning: keep the ceil(keep * K) most credible keypoints (ties:
+    // lower keypoint index), in their original order
+    ProfScope ps(ctx, st, "prune");
+    Scratch t = stage;
+    float* score = t.take<float>(n);
+    uint32_t* k0 = t.take<uint32_t>(n);
+    uint32_t* v0 = t.take<uint32_t>(n);
+    uint32_t* k1 = t.take<uint32_t>(n);
+    uint32_t* v1 = t.take<uint32_t>(n);
+    uint32_t* hist = t.take<uint32_t>(radix_hist_entries(n));
+    if (!hist) return fail(RTR_ERR_CAPACITY, "rtr_recognize_learned: scratch carve");
+    RTR_TRY(mlp_score_rows(t, mlp, b.desc, n, dKeys, score, st));
+    k_score_keys<<<nb, 256, 0, st>>>(score, dKeys, n, k0);
+    uint32_t *ks, *vs;
+    radix_sort_pairs(k0, v0, k1, v1, hist, n, n, dKeys, 32, true, st, &ks, &vs);
+    k_mark_top<<<nb, 256, 0, st>>>(vs, dKeys, n, keep, b.flags);
+    scan_exclusive(b.flags, b.pos, b.tiles, n, n, nullptr, reinterpret_cast<uint32_t*>(b.cnt + 4), st);
+    k_compact_int<<<nb, 256, 0, st>>>(keys, b.flags, b.pos, n, b.keys_p);
+    k_compact_rows<<<nblocks(n, 8, 152 * 16), 256, 0, st>>>(b.desc, b.flags, b.pos, dKeys, n, b.desc_p);
+    RTR_LAUNCHED(4);
+    keys = b.keys_p;
+    dKeys = b.cnt + 4;
+    desc = b.desc_p;
+  }
   {
     ProfScope ps(ctx, st, "match");
     Scratch t = stage;
-    RTR_TRY(match_tc_dev(ctx, t, b.desc, n, dKeys, m->desc, m->n_kp, m->db_hi, m->db_lo, m->db_n2, b.midx, b.md2,
+    RTR_TRY(match_tc_dev(ctx, t, desc, n, dKeys, m->desc, m->n_kp, m->db_hi, m->db_lo, m->db_n2, b.midx, b.md2,
                          st));
   }
   {
@@ -654,6 +745,26 @@ rtr_status rtr_recognize(rtr_context* ctx, const rtr_model* model, const float* 
     return RTR_OK;
   }
   return recognize_impl(ctx, model, reinterpret_cast<const float4*>(d_scene), n, p, d_result, st);
+}
+
+rtr_status rtr_recognize_learned(rtr_context* ctx, const rtr_model* model, const rtr_mlp* mlp, float keep,
+                                 const float* d_scene, int n, const rtr_recog_params* p, rtr_recog_result* d_result,
+                                 rtr_stream_t stream) {
+  RTR_CHECK_ARG(mlp && keep > 0.f && keep <= 1.f, "rtr_recognize_learned: need an MLP and keep in (0, 1]");
+  RTR_CHECK_ARG(ctx && model && p && d_result && n >= 0, "rtr_recognize_learned: bad arguments");
+  RTR_CHECK_ARG(n == 0 || d_scene, "rtr_recognize_learned: NULL scene");
+  RTR_CHECK_ARG(p->max_clusters >= 1 && p->max_clusters <= 256 && p->refine_top >= 1 && p->refine_top <= 64 &&
+                    p->max_instances >= 1 && p->max_instances <= RTR_MAX_INSTANCES && p->voxel_leaf > 0.f &&
+                    p->descriptor_r > 0.f && p->scene_keypoint_r > 0.f && p->icp_iterations >= 1,
+                "rtr_recognize_learned: parameter out of range");
+  RTR_CHECK_ARG(((uintptr_t)d_scene & 15) == 0, "rtr_recognize_learned: scene must be 16-byte aligned");
+  cudaStream_t st = (cudaStream_t)stream;
+  RTR_CUDA(cudaSetDevice(ctx->device));
+  if (n == 0) {
+    RTR_CUDA(cudaMemsetAsync(d_result, 0, sizeof(rtr_recog_result), st));
+    return RTR_OK;
+  }
+  return recognize_impl(ctx, model, reinterpret_cast<const float4*>(d_scene), n, p, d_result, st, mlp, keep);
 }
 
 rtr_status rtr_recognize_host(rtr_context* ctx, const rtr_model* model, const float* h_scene, int n,
