@@ -63,8 +63,9 @@ const char* rtr_last_error(void);
 const char* rtr_version(void);
 
 /* Tuning knobs of this context (value 0 restores the automatic choice):
- *   "icp_group"  lanes cooperating on one ICP source point's 1-NN search
- *                (2, 4 or 8).
+ *   "icp_group"      lanes cooperating on one ICP source point's 1-NN search
+ *                    (2, 4 or 8);
+ *   "batch_workers"  worker threads of rtr_recognize_batch (1..16).
  * Unknown keys or values return RTR_ERR_INVALID_ARG.  Results do not depend
  * on the knobs beyond FP32 summation order. */
 rtr_status rtr_context_set_tuning(rtr_context* ctx, const char* key, int value);
@@ -380,6 +381,31 @@ rtr_status rtr_recognize(rtr_context* ctx, const rtr_model* model, const float* 
 rtr_status rtr_recognize_learned(rtr_context* ctx, const rtr_model* model, const rtr_mlp* mlp, float keep,
                                  const float* d_scene, int n, const rtr_recog_params* p,
                                  rtr_recog_result* d_result, rtr_stream_t stream);
+/* ---- batched registration (many model x segment pairs) ---------------------
+ * The pairs run concurrently: a pool of worker threads, each with a child
+ * context and its own stream, takes the pairs largest first and runs the
+ * recognition chain on each (rtr_recognize, or rtr_recognize_learned when
+ * mlp is not NULL).  Result i (device, d_results[i]) is identical to what
+ * the single-pair call gives.  The number of workers is the context's
+ * "batch_workers" tuning knob (default 4; see rtr_batch_autotune).  A model
+ * may appear in several pairs.  Synchronises; the caller's inputs must be
+ * complete when it is called (it synchronises the device first). */
+typedef struct rtr_batch_pair {
+  const rtr_model* model;
+  const float* d_scene;   /* n points, 16-byte aligned */
+  int n;
+} rtr_batch_pair;
+rtr_status rtr_recognize_batch(rtr_context* ctx, const rtr_batch_pair* h_pairs, int n_pairs,
+                               const rtr_recog_params* p, const rtr_mlp* mlp, float keep,
+                               rtr_recog_result* d_results);
+/* Times the batch under each (workers 1/2/4/8) x (ICP lanes per point 4/8)
+ * setting and keeps the fastest in the context's tuning knobs; reports it in
+ * h_workers / h_icp_group (either may be NULL).  Runs the batch 16 times;
+ * d_results holds the last run's results. */
+rtr_status rtr_batch_autotune(rtr_context* ctx, const rtr_batch_pair* h_pairs, int n_pairs,
+                              const rtr_recog_params* p, const rtr_mlp* mlp, float keep,
+                              rtr_recog_result* d_results, int* h_workers, int* h_icp_group);
+
 /* Same with a HOST scene and a HOST result (copies in and out). */
 rtr_status rtr_recognize_host(rtr_context* ctx, const rtr_model* model, const float* h_scene, int n,
                               const rtr_recog_params* p, rtr_recog_result* h_result);

@@ -158,6 +158,9 @@ _SIG = {
                                C.POINTER(_P)]),
     "rtr_recognize": (_I, [_P, _P, _P, _I, C.POINTER(RecogParams), _P, _P]),
     "rtr_recognize_learned": (_I, [_P, _P, _P, _F, _P, _I, C.POINTER(RecogParams), _P, _P]),
+    "rtr_recognize_batch": (_I, [_P, _P, _I, C.POINTER(RecogParams), _P, _F, _P]),
+    "rtr_batch_autotune": (_I, [_P, _P, _I, C.POINTER(RecogParams), _P, _F, _P, C.POINTER(C.c_int),
+                                C.POINTER(C.c_int)]),
     "rtr_recognize_host": (_I, [_P, _P, _P, _I, C.POINTER(RecogParams), C.POINTER(RecogResult)]),
     "rtr_synth_shape": (_I, [_I, _U64, _I, _P]),
     "rtr_synth_rigid": (None, [_U64, _D, _D, _P]),
@@ -560,6 +563,44 @@ def recognize_learned(ctx: "Context", model: Model, mlp: "Mlp", scene, keep: flo
     check(lib().rtr_recognize_learned(ctx.h, model.h, mlp.h, float(keep), _ptr(scene), scene.shape[0], C.byref(p),
                                       _ptr(result), _stream(stream)))
     return result
+
+
+class BatchPair(C.Structure):
+    _fields_ = [("model", _P), ("d_scene", _P), ("n", C.c_int)]
+
+
+def _batch_args(models, scenes):
+    arr = (BatchPair * len(scenes))()
+    for i, (m, s) in enumerate(zip(models, scenes)):
+        arr[i].model = m.h.value if isinstance(m.h, C.c_void_p) else m.h
+        arr[i].d_scene = _ptr(s)
+        arr[i].n = s.shape[0]
+    return arr
+
+
+def recognize_batch(ctx: "Context", models, scenes, params: RecogParams, mlp: "Mlp | None" = None,
+                    keep: float = 1.0, results=None):
+    """rtr_recognize_batch over pairs (models[i], scenes[i]); returns the device
+    result buffer [n_pairs, sizeof(rtr_recog_result)]."""
+    import torch
+    n = len(scenes)
+    if results is None:
+        results = torch.zeros((max(n, 1), C.sizeof(RecogResult)), dtype=torch.uint8, device="cuda")
+    arr = _batch_args(models, scenes)
+    check(lib().rtr_recognize_batch(ctx.h, arr, n, C.byref(params), mlp.h if mlp else None, float(keep),
+                                    _ptr(results)))
+    return results
+
+
+def batch_autotune(ctx: "Context", models, scenes, params: RecogParams, mlp: "Mlp | None" = None,
+                   keep: float = 1.0):
+    import torch
+    n = len(scenes)
+    results = torch.zeros((max(n, 1), C.sizeof(RecogResult)), dtype=torch.uint8, device="cuda")
+    w, g = C.c_int(), C.c_int()
+    check(lib().rtr_batch_autotune(ctx.h, _batch_args(models, scenes), n, C.byref(params),
+                                   mlp.h if mlp else None, float(keep), _ptr(results), C.byref(w), C.byref(g)))
+    return w.value, g.value
 
 
 def recognize_host(ctx: "Context", model: Model, scene: np.ndarray, params: RecogParams | None = None):

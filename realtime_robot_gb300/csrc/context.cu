@@ -202,6 +202,9 @@ rtr_status rtr_context_destroy(rtr_context* ctx) {
   if (!ctx) return RTR_OK;
   cudaSetDevice(ctx->device);
   cudaDeviceSynchronize();
+  for (rtr_context* w : ctx->workers) rtr_context_destroy(w);
+  ctx->workers.clear();
+  cudaSetDevice(ctx->device);
   rtr_context_profile_clear(ctx);
   for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
   if (ctx->arena) cudaFree(ctx->arena);
@@ -232,6 +235,12 @@ rtr_status rtr_context_set_wait_budget_ms(rtr_context* ctx, double ms) {
 
 rtr_status rtr_context_set_tuning(rtr_context* ctx, const char* key, int value) {
   if (!ctx || !key) return rtr::fail(RTR_ERR_INVALID_ARG, "rtr_context_set_tuning: NULL argument");
+  if (strcmp(key, "batch_workers") == 0) {
+    if (value < 0 || value > 16)
+      return rtr::fail(RTR_ERR_INVALID_ARG, "batch_workers must be 0..16 (got %d)", value);
+    ctx->tune_batch_workers = value;
+    return RTR_OK;
+  }
   if (strcmp(key, "icp_group") == 0) {
     if (value != 0 && value != 2 && value != 4 && value != 8)
       return rtr::fail(RTR_ERR_INVALID_ARG, "icp_group must be 0, 2, 4 or 8 (got %d)", value);

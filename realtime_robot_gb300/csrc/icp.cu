@@ -11,6 +11,7 @@
 // others through a generation word.  Every wait is bounded by a clock64
 // budget; a block that runs out writes RTR_ERR_TIMEOUT and leaves.
 #include <math.h>
+#include <atomic>
 #include <string.h>
 
 #include "grid.cuh"
@@ -320,18 +321,21 @@ __global__ void __launch_bounds__(256) k_gather_pts(const float4* __restrict__ p
 // Co-resident blocks of the ICP kernel (the smallest over the group sizes,
 // so a plan made for one group size fits every variant).
 int icp_max_blocks(rtr_context* ctx) {
-  static int cached_dev = -1, cached = 0;
-  if (cached_dev != ctx->device) {
-    int a = 0, b = 0, c = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_icp<2>, ICP_THREADS, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icp<4>, ICP_THREADS, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_icp<8>, ICP_THREADS, 0);
-    int per_sm = a < b ? a : b;
-    per_sm = per_sm < c ? per_sm : c;
-    cached = per_sm * ctx->num_sms;
-    cached_dev = ctx->device;
+  static std::atomic<int> cached[64];  // per device; 0 = not yet known
+  const int dev = ctx->device;
+  if (dev >= 0 && dev < 64) {
+    const int v = cached[dev].load(std::memory_order_relaxed);
+    if (v > 0) return v;
   }
-  return cached;
+  int a = 0, b = 0, c = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_icp<2>, ICP_THREADS, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icp<4>, ICP_THREADS, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_icp<8>, ICP_THREADS, 0);
+  int per_sm = a < b ? a : b;
+  per_sm = per_sm < c ? per_sm : c;
+  const int v = per_sm * ctx->num_sms;
+  if (dev >= 0 && dev < 64) cached[dev].store(v, std::memory_order_relaxed);
+  return v;
 }
 
 // Lanes per source point: the tuning override when set, else 8 while the

@@ -86,11 +86,8 @@ __global__ void __launch_bounds__(MT_WARPS * 32) k_match_exact(const float* __re
 rtr_status match_exact_dev(const float* q, int nq_cap, const int* d_nq, const float* db, int ndb, int* idx,
                            float* d2, cudaStream_t st) {
   const size_t smem = (size_t)(MT_Q + MT_T) * MT_DIM * sizeof(float);
-  static bool attr = false;
-  if (!attr) {
-    RTR_CUDA(cudaFuncSetAttribute(k_match_exact, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  // per call: the attribute is per device, and calls may come from several threads
+  RTR_CUDA(cudaFuncSetAttribute(k_match_exact, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int blocks = (nq_cap + MT_Q - 1) / MT_Q;
   if (blocks > 152 * 8) blocks = 152 * 8;
   if (blocks < 1) blocks = 1;

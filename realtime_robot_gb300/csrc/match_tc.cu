@@ -462,15 +462,16 @@ typedef CUresult (*PFN_encodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_
                                     CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 static PFN_encodeTiled get_encode() {
-  static PFN_encodeTiled fn = nullptr;
-  if (!fn) {
+  // resolved once (thread-safe static initialisation)
+  static const PFN_encodeTiled fn = []() -> PFN_encodeTiled {
     void* p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
             cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_encodeTiled>(p);
-  }
+      return reinterpret_cast<PFN_encodeTiled>(p);
+    return nullptr;
+  }();
   return fn;
 }
 
@@ -551,11 +552,8 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
       !make_map(&m_bl, db_lo, ndb, TC_BN))
     return fail(RTR_ERR_CUDA, "match_tc: cuTensorMapEncodeTiled failed");
   const size_t smem = (size_t)TC_STAGES * TC_STAGE_BYTES + 1024;
-  static bool attr = false;
-  if (!attr) {
-    RTR_CUDA(cudaFuncSetAttribute(k_match_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  // per call: the attribute is per device, and calls may come from several threads
+  RTR_CUDA(cudaFuncSetAttribute(k_match_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   TcArgs a{nq_cap, d_nq, nq_cap, ndb, qn, cidx, cd, ctx->d_status};
   {
     ProfScope pg(ctx, st, "match_gemm");
