@@ -383,6 +383,8 @@ def run_ours(args):
                         "algorithmic_bytes_per_launch": icp_bytes},
            "pose_error_vs_truth": list(O.pose_error(ir["pose"], T))}
 
+    batch = batch_block(ctx, R, args.steps)
+
     line = {
         "metric": METRIC, "value": value, "unit": "recognitions/s", "n_gpus": ws, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -399,6 +401,7 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "clocks": clocks,
         "icp": icp,
+        "batch": batch,
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_recognition_sample(scene, model)
@@ -410,6 +413,74 @@ def run_ours(args):
     if dist:
         tdist.destroy_process_group()
     return 0
+
+
+def batch_block(ctx, R, steps: int) -> dict:
+    """Config 2: 64 model x segment pairs (chairs, desks, sofas; 2k-60k points,
+    <= 30 deg, +-0.3 m, 2 mm noise, 0-40 % crop) through rtr_recognize_batch,
+    plain and learned (MLP trained here on the GPU, top 25 % of keypoints),
+    against the same pairs one rtr_recognize call at a time."""
+    import torch
+    from realtime_robot_gb300 import learned as L
+    prm = R.recog_default_params(viewpoint=(0.0, 0.0, 0.0))
+    models, mods, scenes, npts = {}, [], [], 0
+    for seed in range(3000, 3064):
+        shape, model, seg, _ = L.make_pair(seed)
+        if shape not in models:
+            models[shape] = R.Model(ctx, torch.from_numpy(model).cuda(), prm)
+        mods.append(models[shape])
+        scenes.append(torch.from_numpy(seg).cuda())
+        npts += seg.shape[0]
+    t0 = time.perf_counter()
+    X, y = L.build_dataset(ctx, range(4000, 4040), prm, label_pose="truth")
+    mlp, losses = L.train(ctx, X, y, epochs=20, batch=4096, lr=1e-3)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+
+    def seq():
+        for m, s in zip(mods, scenes):
+            R.recognize(ctx, m, s, prm)
+        torch.cuda.synchronize()
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t) / reps
+
+    reps = max(1, min(steps, 5))
+    t_seq = timed(seq, reps)
+    workers, group = R.batch_autotune(ctx, mods[:16], scenes[:16], prm)
+    t_plain = timed(lambda: R.recognize_batch(ctx, mods, scenes, prm), reps)
+    t_learned = timed(lambda: R.recognize_batch(ctx, mods, scenes, prm, mlp=mlp, keep=0.25), reps)
+    ctx.set_tuning("batch_workers", 0)
+    ctx.set_tuning("icp_group", 0)
+    res_p = [R.parse_recog_result(bytes(r)) for r in R.recognize_batch(ctx, mods, scenes, prm).cpu().numpy()]
+    res_l = [R.parse_recog_result(bytes(r)) for r in
+             R.recognize_batch(ctx, mods, scenes, prm, mlp=mlp, keep=0.25).cpu().numpy()]
+    agree = 0
+    for a, b in zip(res_p, res_l):
+        if a["instances"] and b["instances"]:
+            dt, dr = L.pose_diff(a["instances"][0]["pose"], b["instances"][0]["pose"])
+            agree += int(dt <= 0.01 and dr <= 1.0)
+        else:
+            agree += int(not a["instances"] and not b["instances"])
+    for m in models.values():
+        m.close()
+    n = len(scenes)
+    return {"metric": "pairs/s (config 2: 64 model x segment pairs, 2k-60k points)", "unit": "pairs/s",
+            "pairs": n, "points": npts,
+            "sequential_plain": n / t_seq, "batched_plain": n / t_plain, "batched_learned": n / t_learned,
+            # a pair whose learned pose disagrees with the plain one is re-run plain
+            "batched_learned_with_fallback": n / (t_learned + (n - agree) / n * t_plain),
+            "learned_batched_over_plain_sequential": t_seq / t_learned,
+            "autotuned": {"workers": workers, "icp_group": group},
+            "learned": {"keep": 0.25, "train_rows": int(X.shape[0]), "positive_rate": float(y.mean()),
+                        "train_s_incl_harvest": train_s, "final_loss": float(losses[-1]),
+                        "pairs_agreeing_with_plain_1cm_1deg": agree, "fallbacks": n - agree}}
 
 
 def main():

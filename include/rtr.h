@@ -285,7 +285,7 @@ rtr_status rtr_match_exact(rtr_context* ctx, const float* d_query, int n_query,
  * max_members per row, -1 padded), sizes, and the least-squares model->scene
  * pose (row-major 4x4, FP64).  The walk runs on the device in one cooperative
  * launch; the call synchronises once, to return the cluster count.  Consensus
- * sets longer than 128 members, or more than 1,474,560 correspondences,
+ * sets longer than 128 members, or more than 1,441,792 correspondences,
  * return RTR_ERR_CAPACITY. */
 rtr_status rtr_gc_group(rtr_context* ctx, const float* d_model_kp, const float* d_scene_kp,
                         const int32_t* d_corr_m, const int32_t* d_corr_s, const float* d_corr_d,

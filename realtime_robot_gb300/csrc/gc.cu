@@ -603,8 +603,11 @@ static bool gc_take(Scratch& s, int C, int max_clusters, int max_members, GcBufs
   return b->mask != nullptr;
 }
 
-// Shared memory of k_gc_coop beyond its static part: the taken bitset.
-constexpr size_t GC_MAX_DYN_SMEM = 180 * 1024;
+// Shared memory of k_gc_coop beyond its static part (the taken bitset).  The
+// kernel's dynamic-shared-memory limit is always set to this one value, so
+// calls from several threads (the batch driver) never lower it under each
+// other's launches.
+constexpr size_t GC_MAX_DYN_SMEM = 176 * 1024;
 
 }  // namespace rtr
 
@@ -645,7 +648,7 @@ rtr_status gc_group_dev(rtr_context* ctx, Scratch& s, const float* d_model_kp, c
   bbox_build(b.mbox, b.pm, C, st);
   GcCoop c{b.misc, b.arrive, b.computed, b.members, b.sizes, gc_thresh, max_clusters,
            ctx->wait_budget_cycles, ctx->d_status, b.mbox, b.need, b.mask, gc_win(C), gc_nwp(C)};
-  RTR_CUDA(cudaFuncSetAttribute(k_gc_coop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+  RTR_CUDA(cudaFuncSetAttribute(k_gc_coop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GC_MAX_DYN_SMEM));
   int per_sm = 0;
   RTR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gc_coop, GC_WARPS * 32, dyn));
   if (per_sm < 1) return fail(RTR_ERR_CAPACITY, "rtr_gc_group: grouping kernel does not fit an SM");
