@@ -369,7 +369,10 @@ rtr_status rtr_model_info(const rtr_model* m, int* n_voxels, int* n_keypoints);
 rtr_status rtr_model_buffers(const rtr_model* m, const float** d_vox, const float** d_normals,
                              const int32_t** d_keys, const float** d_kp, const float** d_desc);
 /* Recognise the model in a scene (device points).  d_result: device
- * rtr_recog_result.  Synchronises once (before grouping). */
+ * rtr_recog_result.  Does not synchronise: every count stays on the device
+ * and errors reach the context status word (rtr_context_check).  The first
+ * call at a scene size may grow the context's scratch (that synchronises);
+ * after it, calls of at most that size can be captured into a CUDA graph. */
 rtr_status rtr_recognize(rtr_context* ctx, const rtr_model* model, const float* d_scene, int n,
                          const rtr_recog_params* p, rtr_recog_result* d_result,
                          rtr_stream_t stream);
@@ -385,8 +388,12 @@ rtr_status rtr_recognize_learned(rtr_context* ctx, const rtr_model* model, const
  * The pairs run concurrently: a pool of worker threads, each with a child
  * context and its own stream, takes the pairs largest first and runs the
  * recognition chain on each (rtr_recognize, or rtr_recognize_learned when
- * mlp is not NULL).  Result i (device, d_results[i]) is identical to what
- * the single-pair call gives.  The number of workers is the context's
+ * mlp is not NULL).  One host thread enqueues every pair: each worker is a
+ * child context with its own stream, forked from and joined back to the
+ * context's stream.  Result i (device, d_results[i]) is what the
+ * single-pair call gives, except that each worker's cooperative kernels use a
+ * share of the GPU: an ICP problem split over fewer blocks rounds its FP32
+ * block sums differently (poses agree within 1e-5).  The number of workers is the context's
  * "batch_workers" tuning knob (default 4; see rtr_batch_autotune).  A model
  * may appear in several pairs.  Synchronises; the caller's inputs must be
  * complete when it is called (it synchronises the device first). */
@@ -398,6 +405,19 @@ typedef struct rtr_batch_pair {
 rtr_status rtr_recognize_batch(rtr_context* ctx, const rtr_batch_pair* h_pairs, int n_pairs,
                                const rtr_recog_params* p, const rtr_mlp* mlp, float keep,
                                rtr_recog_result* d_results);
+/* The same batch captured once into a CUDA graph: create runs the batch once
+ * (sizing every worker's scratch), then records its enqueue sequence; each
+ * launch replays it on `stream` and returns without synchronising (check the
+ * results after synchronising; rtr_context_check on the workers is not
+ * needed: errors also leave a non-OK status in each result).  The scenes
+ * must stay at the same device addresses; their contents, and the model
+ * buffers' contents, may change between launches (same sizes). */
+typedef struct rtr_batch_graph rtr_batch_graph;
+rtr_status rtr_batch_graph_create(rtr_context* ctx, const rtr_batch_pair* h_pairs, int n_pairs,
+                                  const rtr_recog_params* p, const rtr_mlp* mlp, float keep,
+                                  rtr_recog_result* d_results, rtr_batch_graph** out);
+rtr_status rtr_batch_graph_launch(rtr_batch_graph* g, rtr_stream_t stream);
+rtr_status rtr_batch_graph_destroy(rtr_batch_graph* g);
 /* Times the batch under each (workers 1/2/4/8) x (ICP lanes per point 4/8)
  * setting and keeps the fastest in the context's tuning knobs; reports it in
  * h_workers / h_icp_group (either may be NULL).  Runs the batch 16 times;

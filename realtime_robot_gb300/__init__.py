@@ -159,6 +159,9 @@ _SIG = {
     "rtr_recognize": (_I, [_P, _P, _P, _I, C.POINTER(RecogParams), _P, _P]),
     "rtr_recognize_learned": (_I, [_P, _P, _P, _F, _P, _I, C.POINTER(RecogParams), _P, _P]),
     "rtr_recognize_batch": (_I, [_P, _P, _I, C.POINTER(RecogParams), _P, _F, _P]),
+    "rtr_batch_graph_create": (_I, [_P, _P, _I, C.POINTER(RecogParams), _P, _F, _P, C.POINTER(_P)]),
+    "rtr_batch_graph_launch": (_I, [_P, _P]),
+    "rtr_batch_graph_destroy": (_I, [_P]),
     "rtr_batch_autotune": (_I, [_P, _P, _I, C.POINTER(RecogParams), _P, _F, _P, C.POINTER(C.c_int),
                                 C.POINTER(C.c_int)]),
     "rtr_recognize_host": (_I, [_P, _P, _P, _I, C.POINTER(RecogParams), C.POINTER(RecogResult)]),
@@ -590,6 +593,37 @@ def recognize_batch(ctx: "Context", models, scenes, params: RecogParams, mlp: "M
     check(lib().rtr_recognize_batch(ctx.h, arr, n, C.byref(params), mlp.h if mlp else None, float(keep),
                                     _ptr(results)))
     return results
+
+
+class BatchGraph:
+    """rtr_batch_graph_*: the batch captured once, replayed by launch()."""
+
+    def __init__(self, ctx: "Context", models, scenes, params: RecogParams, mlp: "Mlp | None" = None,
+                 keep: float = 1.0, results=None):
+        import torch
+        n = len(scenes)
+        self.results = results if results is not None else torch.zeros(
+            (n, C.sizeof(RecogResult)), dtype=torch.uint8, device="cuda")
+        self._keep = (models, scenes, params, mlp)  # inputs must outlive the graph
+        h = _P()
+        check(lib().rtr_batch_graph_create(ctx.h, _batch_args(models, scenes), n, C.byref(params),
+                                           mlp.h if mlp else None, float(keep), _ptr(self.results), C.byref(h)))
+        self.h = h
+
+    def launch(self, stream=None):
+        check(lib().rtr_batch_graph_launch(self.h, _stream(stream)))
+        return self.results
+
+    def close(self):
+        if self.h:
+            lib().rtr_batch_graph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def batch_autotune(ctx: "Context", models, scenes, params: RecogParams, mlp: "Mlp | None" = None,

@@ -1,26 +1,31 @@
 // batch.cu — batched registration: many model x segment pairs at once.
 //
-// One pair (2k-60k points) fills a small part of a GB300: its stages are a
-// few hundred thousand threads each, and the pipeline synchronises twice
-// (correspondence count, cluster count).  The batch driver therefore runs
-// the pairs concurrently: a pool of worker threads, each with its own child
-// context (scratch arena, stream, status words), takes pairs largest first
-// (LPT order by point count) and runs the full recognition chain on its own
-// stream.  Concurrent streams overlap one pair's host round trips and small
-// kernels with the other pairs' work.  Every pair's result is identical to
-// a single rtr_recognize / rtr_recognize_learned call.
+// One pair (2k-60k points) fills a small part of a GB300.  The recognition
+// chain keeps every count on the device (no host round trip), so one host
+// thread can spread a batch over several streams: each worker is a child
+// context (scratch arena, stream, status words), the pairs are dealt out
+// round-robin in largest-first order, and the worker streams are forked from
+// and joined back to the caller's stream with events.  The same enqueue
+// sequence can be captured once into a CUDA graph (rtr_batch_graph_*) and
+// replayed, which removes the per-launch host cost of the ~130 kernels of
+// every pair.
 //
-// The worker count (and the ICP lanes per point) can be chosen by
-// rtr_batch_autotune, which times the candidates on the caller's batch.
+// Each worker's cooperative kernels (grouping, ICP) take 1/workers of the
+// co-resident blocks so they run side by side.  A pair's result is the
+// single-call result up to the FP32 rounding of ICP block sums over a
+// different block count.  rtr_batch_autotune picks the worker count and the
+// ICP lanes per point by timing the caller's batch.
 #include <algorithm>
-#include <atomic>
 #include <chrono>
-#include <mutex>
-#include <string>
-#include <thread>
 #include <vector>
 
 #include "common.cuh"
+
+struct rtr_batch_graph {
+  rtr_context* ctx = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
 
 namespace rtr {
 
@@ -30,7 +35,11 @@ static rtr_status ensure_workers(rtr_context* ctx, int n) {
     RTR_TRY(rtr_context_create(ctx->device, &w));
     ctx->workers.push_back(w);
   }
+  RTR_CUDA(cudaSetDevice(ctx->device));
+  if (!ctx->ev_fork) RTR_CUDA(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
   for (rtr_context* w : ctx->workers) {
+    if (!w->ev_fork) RTR_CUDA(cudaEventCreateWithFlags(&w->ev_fork, cudaEventDisableTiming));
+    w->coop_div = n;  // cooperative kernels of the n workers fit the GPU side by side
     w->wait_budget_ms = ctx->wait_budget_ms;
     w->wait_budget_cycles = ctx->wait_budget_cycles;
     w->tune_icp_group = ctx->tune_icp_group;
@@ -43,45 +52,50 @@ static int batch_workers(const rtr_context* ctx, int n_pairs) {
   return w < n_pairs ? w : n_pairs;
 }
 
-static rtr_status run_batch(rtr_context* ctx, const rtr_batch_pair* pairs, int n_pairs, const rtr_recog_params* p,
-                            const rtr_mlp* mlp, float keep, int nw, rtr_recog_result* d_results) {
+// Enqueue the batch on `origin` (forked to the workers' streams and joined
+// back); returns without synchronising.
+static rtr_status enqueue_batch(rtr_context* ctx, const rtr_batch_pair* pairs, int n_pairs, const rtr_recog_params* p,
+                                const rtr_mlp* mlp, float keep, int nw, rtr_recog_result* d_results,
+                                cudaStream_t origin) {
   RTR_TRY(ensure_workers(ctx, nw));
-  // largest pairs first, so the last ones to finish are short
   std::vector<int> order((size_t)n_pairs);
   for (int i = 0; i < n_pairs; ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return pairs[a].n > pairs[b].n; });
-  std::atomic<int> next{0};
-  std::mutex mu;
-  rtr_status first = RTR_OK;
-  std::string first_msg;
-  auto work = [&](int wi) {
+  RTR_CUDA(cudaEventRecord(ctx->ev_fork, origin));
+  for (int wi = 0; wi < nw; ++wi) RTR_CUDA(cudaStreamWaitEvent(ctx->workers[wi]->host_stream, ctx->ev_fork, 0));
+  for (int k = 0; k < n_pairs; ++k) {
+    rtr_context* w = ctx->workers[k % nw];
+    const int i = order[k];
+    const rtr_batch_pair& q = pairs[i];
+    const rtr_status r = mlp ? rtr_recognize_learned(w, q.model, mlp, keep, q.d_scene, q.n, p, d_results + i,
+                                                     w->host_stream)
+                             : rtr_recognize(w, q.model, q.d_scene, q.n, p, d_results + i, w->host_stream);
+    if (r != RTR_OK) return fail(r, "rtr_recognize_batch: pair %d: %s", i, rtr_last_error());
+  }
+  for (int wi = 0; wi < nw; ++wi) {
     rtr_context* w = ctx->workers[wi];
-    cudaStream_t st = w->host_stream;
-    for (;;) {
-      const int k = next.fetch_add(1);
-      if (k >= n_pairs) break;
-      const int i = order[k];
-      const rtr_batch_pair& q = pairs[i];
-      rtr_status r = mlp ? rtr_recognize_learned(w, q.model, mlp, keep, q.d_scene, q.n, p, d_results + i, st)
-                         : rtr_recognize(w, q.model, q.d_scene, q.n, p, d_results + i, st);
-      if (r == RTR_OK) r = rtr_context_check(w, st);
-      if (r != RTR_OK) {
-        std::lock_guard<std::mutex> lk(mu);
-        if (first == RTR_OK) {
-          first = r;
-          first_msg = std::string("pair ") + std::to_string(i) + ": " + rtr_last_error();
-        }
-        break;
-      }
-    }
-    cudaStreamSynchronize(st);
-  };
-  std::vector<std::thread> threads;
-  for (int wi = 1; wi < nw; ++wi) threads.emplace_back(work, wi);
-  work(0);
-  for (auto& t : threads) t.join();
+    RTR_CUDA(cudaEventRecord(w->ev_fork, w->host_stream));
+    RTR_CUDA(cudaStreamWaitEvent(origin, w->ev_fork, 0));
+  }
   RTR_CUDA(cudaSetDevice(ctx->device));
-  if (first != RTR_OK) return fail(first, "rtr_recognize_batch: %s", first_msg.c_str());
+  return RTR_OK;
+}
+
+// Device status words of the workers (timeouts, capacity) after a batch.
+static rtr_status check_workers(rtr_context* ctx, int nw) {
+  for (int wi = 0; wi < nw; ++wi) RTR_TRY(rtr_context_check(ctx->workers[wi], ctx->workers[wi]->host_stream));
+  RTR_CUDA(cudaSetDevice(ctx->device));
+  return RTR_OK;
+}
+
+static rtr_status check_args(rtr_context* ctx, const rtr_batch_pair* h_pairs, int n_pairs, const rtr_recog_params* p,
+                             const rtr_mlp* mlp, float keep, const rtr_recog_result* d_results) {
+  RTR_CHECK_ARG(ctx && p && n_pairs >= 0 && (n_pairs == 0 || (h_pairs && d_results)),
+                "rtr_recognize_batch: bad arguments");
+  RTR_CHECK_ARG(!mlp || (keep > 0.f && keep <= 1.f), "rtr_recognize_batch: keep must be in (0, 1]");
+  for (int i = 0; i < n_pairs; ++i)
+    RTR_CHECK_ARG(h_pairs[i].model && h_pairs[i].n >= 0 && (h_pairs[i].n == 0 || h_pairs[i].d_scene),
+                  "rtr_recognize_batch: pair %d is incomplete", i);
   return RTR_OK;
 }
 
@@ -94,16 +108,66 @@ extern "C" {
 rtr_status rtr_recognize_batch(rtr_context* ctx, const rtr_batch_pair* h_pairs, int n_pairs,
                                const rtr_recog_params* p, const rtr_mlp* mlp, float keep,
                                rtr_recog_result* d_results) {
-  RTR_CHECK_ARG(ctx && p && n_pairs >= 0 && (n_pairs == 0 || (h_pairs && d_results)),
-                "rtr_recognize_batch: bad arguments");
-  RTR_CHECK_ARG(!mlp || (keep > 0.f && keep <= 1.f), "rtr_recognize_batch: keep must be in (0, 1]");
-  for (int i = 0; i < n_pairs; ++i)
-    RTR_CHECK_ARG(h_pairs[i].model && h_pairs[i].n >= 0 && (h_pairs[i].n == 0 || h_pairs[i].d_scene),
-                  "rtr_recognize_batch: pair %d is incomplete", i);
+  RTR_TRY(check_args(ctx, h_pairs, n_pairs, p, mlp, keep, d_results));
   if (n_pairs == 0) return RTR_OK;
   RTR_CUDA(cudaSetDevice(ctx->device));
   RTR_CUDA(cudaDeviceSynchronize());  // inputs written on other streams are complete
-  return run_batch(ctx, h_pairs, n_pairs, p, mlp, keep, batch_workers(ctx, n_pairs), d_results);
+  const int nw = batch_workers(ctx, n_pairs);
+  RTR_TRY(enqueue_batch(ctx, h_pairs, n_pairs, p, mlp, keep, nw, d_results, ctx->host_stream));
+  RTR_CUDA(cudaStreamSynchronize(ctx->host_stream));
+  return check_workers(ctx, nw);
+}
+
+rtr_status rtr_batch_graph_create(rtr_context* ctx, const rtr_batch_pair* h_pairs, int n_pairs,
+                                  const rtr_recog_params* p, const rtr_mlp* mlp, float keep,
+                                  rtr_recog_result* d_results, rtr_batch_graph** out) {
+  RTR_CHECK_ARG(out, "rtr_batch_graph_create: out is NULL");
+  *out = nullptr;
+  RTR_TRY(check_args(ctx, h_pairs, n_pairs, p, mlp, keep, d_results));
+  RTR_CHECK_ARG(n_pairs > 0, "rtr_batch_graph_create: empty batch");
+  // one plain run sizes every worker's scratch for its pairs
+  RTR_TRY(rtr_recognize_batch(ctx, h_pairs, n_pairs, p, mlp, keep, d_results));
+  const int nw = batch_workers(ctx, n_pairs);
+  for (int wi = 0; wi < nw; ++wi)
+    RTR_CHECK_ARG(!ctx->workers[wi]->profiling, "rtr_batch_graph_create: profiling is on");
+  cudaStream_t origin = ctx->host_stream;
+  RTR_CUDA(cudaStreamBeginCapture(origin, cudaStreamCaptureModeThreadLocal));
+  const rtr_status r = enqueue_batch(ctx, h_pairs, n_pairs, p, mlp, keep, nw, d_results, origin);
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(origin, &g);
+  if (r != RTR_OK) {
+    if (g) cudaGraphDestroy(g);
+    return r;
+  }
+  if (e != cudaSuccess) return fail(RTR_ERR_CUDA, "rtr_batch_graph_create: capture failed: %s", cudaGetErrorString(e));
+  cudaGraphExec_t x = nullptr;
+  const cudaError_t ei = cudaGraphInstantiate(&x, g, 0);
+  if (ei != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return fail(RTR_ERR_CUDA, "rtr_batch_graph_create: instantiate failed: %s", cudaGetErrorString(ei));
+  }
+  rtr_batch_graph* bg = new rtr_batch_graph();
+  bg->ctx = ctx;
+  bg->graph = g;
+  bg->exec = x;
+  *out = bg;
+  return RTR_OK;
+}
+
+rtr_status rtr_batch_graph_launch(rtr_batch_graph* bg, rtr_stream_t stream) {
+  RTR_CHECK_ARG(bg && bg->exec, "rtr_batch_graph_launch: bad graph");
+  RTR_CUDA(cudaSetDevice(bg->ctx->device));
+  RTR_CUDA(cudaGraphLaunch(bg->exec, (cudaStream_t)stream));
+  return RTR_OK;
+}
+
+rtr_status rtr_batch_graph_destroy(rtr_batch_graph* bg) {
+  if (!bg) return RTR_OK;
+  cudaSetDevice(bg->ctx->device);
+  if (bg->exec) cudaGraphExecDestroy(bg->exec);
+  if (bg->graph) cudaGraphDestroy(bg->graph);
+  delete bg;
+  return RTR_OK;
 }
 
 rtr_status rtr_batch_autotune(rtr_context* ctx, const rtr_batch_pair* h_pairs, int n_pairs,
@@ -121,15 +185,10 @@ rtr_status rtr_batch_autotune(rtr_context* ctx, const rtr_batch_pair* h_pairs, i
       if (w > n_pairs && w != 1) continue;
       ctx->tune_batch_workers = w;
       ctx->tune_icp_group = g;
-      // one untimed pass (scratch growth, module load), then one timed pass
+      // one untimed pass (scratch growth), then one timed pass
       rtr_status r = rtr_recognize_batch(ctx, h_pairs, n_pairs, p, mlp, keep, d_results);
-      if (r != RTR_OK) {
-        ctx->tune_batch_workers = saved_w;
-        ctx->tune_icp_group = saved_g;
-        return r;
-      }
       const auto t0 = std::chrono::steady_clock::now();
-      r = rtr_recognize_batch(ctx, h_pairs, n_pairs, p, mlp, keep, d_results);
+      if (r == RTR_OK) r = rtr_recognize_batch(ctx, h_pairs, n_pairs, p, mlp, keep, d_results);
       const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
       if (r != RTR_OK) {
         ctx->tune_batch_workers = saved_w;

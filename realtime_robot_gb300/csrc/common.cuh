@@ -73,7 +73,9 @@ struct rtr_context {
   int* h_pin = nullptr;                // 64 pinned ints for small device->host reads
   int tune_icp_group = 0;              // lanes per ICP source point (0: automatic)
   int tune_batch_workers = 0;          // workers of rtr_recognize_batch (0: automatic)
+  int coop_div = 1;                    // cooperative grids use 1/coop_div of the GPU
   std::vector<rtr_context*> workers;   // child contexts of the batch driver
+  cudaEvent_t ev_fork = nullptr;       // fork/join event of the batch driver
   int gc_stats[8] = {};                // last grouping: rounds, walk end, sets, phase us, candidates
   bool profiling = false;
   std::vector<rtr_prof_rec> prof;      // recorded stages (in order)

@@ -207,6 +207,7 @@ rtr_status rtr_context_destroy(rtr_context* ctx) {
   cudaSetDevice(ctx->device);
   rtr_context_profile_clear(ctx);
   for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
   if (ctx->arena) cudaFree(ctx->arena);
   if (ctx->io) cudaFree(ctx->io);
   if (ctx->host_stream) cudaStreamDestroy(ctx->host_stream);

@@ -30,7 +30,8 @@ constexpr int GC_MAXS = 128;  // members per consensus set (larger sets: RTR_ERR
 struct GcDev {
   const float4* pm;        // model keypoint of sorted correspondence a
   const float4* ps;        // scene keypoint of sorted correspondence a
-  int C;
+  int C;                   // correspondences (the capacity when d_C is set)
+  const int* d_C;          // device count of correspondences, or NULL
   float gc;
   unsigned* taken;         // bitset over sorted positions
   int* set_size;           // [C]
@@ -189,7 +190,9 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
   __shared__ int s_pos, s_done, s_ok;
   __shared__ float s_r2max;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (g.d_C) g.C = min(max(*g.d_C, 0), g.C);  // counted on the device
   const int nwords = (g.C + 31) >> 5;
+  const int nwp = (nwords + 3) & ~3;  // live width of a mask row (rows are c.nwp apart)
   const int gw = blockIdx.x * GC_WARPS + wid, nwarps = gridDim.x * GC_WARPS;
   if (threadIdx.x == 0) {
     s_pos = 0;
@@ -247,12 +250,12 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
     // candidate chunk once and tests it against all 32 seeds.
     if (nneed > 0) {
       const int ngrp = (nneed + 31) >> 5;
-      const long long items = (long long)c.nwp * ngrp;
+      const long long items = (long long)nwp * ngrp;
       const long long per = (items + nwarps - 1) / nwarps;
       const long long it0 = (long long)gw * per, it1 = min(items, it0 + per);
       int cur = -1;
       for (long long it = it0; it < it1; ++it) {
-        const int grp = (int)(it / c.nwp), ch = (int)(it - (long long)grp * c.nwp);
+        const int grp = (int)(it / nwp), ch = (int)(it - (long long)grp * nwp);
         const int kend = min(32, nneed - grp * 32);
         if (grp != cur) {
           __syncwarp();
@@ -295,7 +298,7 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
       __syncwarp();
       int cnt = 1, npend = 0, ntest = 0;
       const uint4* row = reinterpret_cast<const uint4*>(c.mask + (size_t)slot * c.nwp);
-      const int nv = c.nwp >> 2;
+      const int nv = nwp >> 2;
       for (int v0 = 0; v0 < nv; v0 += 32 * GC_PREF) {
         uint4 buf[GC_PREF];
 #pragma unroll
@@ -465,8 +468,9 @@ __global__ void k_gc_members_out(const int* __restrict__ mem, const int* __restr
 
 // Gather the sorted correspondence endpoints.
 __global__ void k_gc_gather(const float4* __restrict__ mk, const float4* __restrict__ sk, const int* __restrict__ cm,
-                            const int* __restrict__ cs, const uint32_t* __restrict__ order, int C,
+                            const int* __restrict__ cs, const uint32_t* __restrict__ order, int C, const int* d_C,
                             float4* __restrict__ pm, float4* __restrict__ ps) {
+  if (d_C) C = min(*d_C, C);
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < C; a += gridDim.x * blockDim.x) {
     const int i = (int)order[a];
     pm[a] = mk[cm[i]];
@@ -477,9 +481,10 @@ __global__ void k_gc_gather(const float4* __restrict__ mk, const float4* __restr
 // Per-cluster least-squares pose model -> scene in FP64 (one warp per cluster).
 __global__ void k_gc_poses(const float4* __restrict__ pm, const float4* __restrict__ ps,
                            const int* __restrict__ members, const int* __restrict__ sizes, int ncl,
-                           int max_members, double* __restrict__ poses) {
+                           const int* d_ncl, int max_members, double* __restrict__ poses) {
   const int lane = threadIdx.x & 31;
   const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (d_ncl) ncl = min(*d_ncl, ncl);
   if (c >= ncl) return;
   const int n = min(sizes[c], max_members);
   double s[15];
@@ -528,11 +533,22 @@ __global__ void k_gc_poses(const float4* __restrict__ pm, const float4* __restri
 }
 
 // Sort keys: non-negative float bits order like the floats.
-__global__ void k_gc_keys(const float* __restrict__ d, int C, uint32_t* __restrict__ keys) {
+__global__ void k_gc_keys(const float* __restrict__ d, int C, const int* d_C, uint32_t* __restrict__ keys) {
+  if (d_C) C = min(*d_C, C);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
     const float v = d[i];
     keys[i] = v > 0.f ? __float_as_uint(v) : 0u;
   }
+}
+
+// After the walk: the cluster count for the next stages, the error (if any)
+// into the context status word, and the walk's statistics beside it.
+__global__ void k_gc_post(const int* __restrict__ ctl, int max_clusters, int* d_ncl, int* status, int* stats) {
+  if (threadIdx.x != 0) return;
+  const int err = ctl[3];
+  if (d_ncl) *d_ncl = err ? 0 : min(ctl[1], max_clusters);
+  if (err) atomicCAS(status, 0, err);
+  for (int k = 0; k < 12; ++k) stats[k] = ctl[k];
 }
 
 struct GcBufs {
@@ -621,38 +637,45 @@ size_t gc_scratch_bytes(int C, int max_clusters) {
   return plan.bytes;
 }
 
-rtr_status gc_group_dev(rtr_context* ctx, Scratch& s, const float* d_model_kp, const float* d_scene_kp,
-                        const int32_t* d_corr_m, const int32_t* d_corr_s, const float* d_corr_d, int n_corr,
-                        float gc_size, int gc_thresh, int max_clusters, int max_members, int32_t* d_members,
-                        int32_t* d_sizes, double* d_poses, int* h_n_clusters, cudaStream_t st) {
-  *h_n_clusters = 0;
-  if (n_corr == 0) return RTR_OK;
-  const int C = n_corr;
-  GcBufs b;
+// The grouping up to the walk's end, without a host round trip.  C_cap
+// bounds the correspondences; with d_C the live count is read on the device.
+static rtr_status gc_launch(rtr_context* ctx, Scratch& s, const float* d_model_kp, const float* d_scene_kp,
+                            const int32_t* d_corr_m, const int32_t* d_corr_s, const float* d_corr_d, int C_cap,
+                            const int* d_C, float gc_size, int gc_thresh, int max_clusters, cudaStream_t st,
+                            GcBufs* bo, uint32_t** order) {
+  const int C = C_cap;
+  GcBufs& b = *bo;
   if (!gc_take(s, C, max_clusters, GC_MAXS, &b)) return fail(RTR_ERR_CAPACITY, "rtr_gc_group: scratch");
-  const int nb = (C + 255) / 256 > 152 * 8 ? 152 * 8 : (C + 255) / 256;
-  k_gc_keys<<<nb, 256, 0, st>>>(d_corr_d, C, b.k0);
-  uint32_t *ks, *vs;
-  radix_sort_pairs(b.k0, b.v0, b.k1, b.v1, b.hist, C, C, nullptr, 32, true, st, &ks, &vs);
-  k_gc_gather<<<nb, 256, 0, st>>>(reinterpret_cast<const float4*>(d_model_kp),
-                                  reinterpret_cast<const float4*>(d_scene_kp), d_corr_m, d_corr_s, vs, C, b.pm, b.ps);
   const size_t dyn = sizeof(unsigned) * (size_t)((C + 31) / 32);
   if (dyn > GC_MAX_DYN_SMEM)
     return fail(RTR_ERR_CAPACITY, "rtr_gc_group: %d correspondences exceed the supported %d", C,
                 (int)(GC_MAX_DYN_SMEM * 8));
+  const int nb = (C + 255) / 256 > 152 * 8 ? 152 * 8 : (C + 255) / 256;
+  k_gc_keys<<<nb, 256, 0, st>>>(d_corr_d, C, d_C, b.k0);
+  uint32_t *ks, *vs;
+  radix_sort_pairs(b.k0, b.v0, b.k1, b.v1, b.hist, C, C, d_C, 32, true, st, &ks, &vs);
+  k_gc_gather<<<nb, 256, 0, st>>>(reinterpret_cast<const float4*>(d_model_kp),
+                                  reinterpret_cast<const float4*>(d_scene_kp), d_corr_m, d_corr_s, vs, C, d_C, b.pm,
+                                  b.ps);
   RTR_CUDA(cudaMemsetAsync(b.taken, 0, dyn, st));
   RTR_CUDA(cudaMemsetAsync(b.computed, 0, sizeof(int) * C, st));
   RTR_CUDA(cudaMemsetAsync(b.misc, 0, sizeof(int) * 16, st));
   RTR_CUDA(cudaMemsetAsync(b.arrive, 0, sizeof(unsigned), st));
-  GcDev g{b.pm, b.ps, C, gc_size, b.taken, b.set_size, b.set_mem};
-  bbox_build(b.mbox, b.pm, C, st);
+  GcDev g{b.pm, b.ps, C, d_C, gc_size, b.taken, b.set_size, b.set_mem};
+  bbox_build(b.mbox, b.pm, C, d_C, st);
   GcCoop c{b.misc, b.arrive, b.computed, b.members, b.sizes, gc_thresh, max_clusters,
            ctx->wait_budget_cycles, ctx->d_status, b.mbox, b.need, b.mask, gc_win(C), gc_nwp(C)};
   RTR_CUDA(cudaFuncSetAttribute(k_gc_coop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GC_MAX_DYN_SMEM));
   int per_sm = 0;
   RTR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gc_coop, GC_WARPS * 32, dyn));
   if (per_sm < 1) return fail(RTR_ERR_CAPACITY, "rtr_gc_group: grouping kernel does not fit an SM");
-  const int blocks = (per_sm < 2 ? per_sm : 2) * ctx->num_sms;
+  // enough warps for the work (a few thousand correspondences need a few
+  // blocks), and a share of the GPU when several contexts run at once
+  int blocks = (per_sm < 2 ? per_sm : 2) * ctx->num_sms;
+  const int div = ctx->coop_div > 0 ? ctx->coop_div : 1;
+  blocks = blocks / div > 0 ? blocks / div : 1;
+  const int by_work = (C + 255) / 256;
+  if (by_work < blocks) blocks = by_work > 4 ? by_work : 4;
   {
     ProfScope pw(ctx, st, "gc_walk");
     cudaLaunchConfig_t cfg = {};
@@ -668,6 +691,45 @@ rtr_status gc_group_dev(rtr_context* ctx, Scratch& s, const float* d_model_kp, c
     RTR_CUDA(cudaLaunchKernelEx(&cfg, k_gc_coop, g, c));
   }
   RTR_LAUNCHED(3);
+  *order = vs;
+  return RTR_OK;
+}
+
+// Grouping with every count on the device (no host round trip; the
+// pipeline's form).  Writes the cluster count to *d_ncl, the first
+// max_clusters sizes and poses; an error goes to the context status word.
+rtr_status gc_group_async(rtr_context* ctx, Scratch& s, const float* d_model_kp, const float* d_scene_kp,
+                          const int32_t* d_corr_m, const int32_t* d_corr_s, const float* d_corr_d, int C_cap,
+                          const int* d_C, float gc_size, int gc_thresh, int max_clusters, int32_t* d_sizes,
+                          double* d_poses, int* d_ncl, cudaStream_t st) {
+  GcBufs b;
+  uint32_t* order = nullptr;
+  RTR_TRY(gc_launch(ctx, s, d_model_kp, d_scene_kp, d_corr_m, d_corr_s, d_corr_d, C_cap > 0 ? C_cap : 1, d_C,
+                    gc_size, gc_thresh, max_clusters, st, &b, &order));
+  k_gc_post<<<1, 32, 0, st>>>(b.misc, max_clusters, d_ncl, ctx->d_status, ctx->d_status + 16);
+  k_gc_poses<<<(max_clusters + 3) / 4, 128, 0, st>>>(b.pm, b.ps, b.members, b.sizes, max_clusters, d_ncl, GC_MAXS,
+                                                      b.poses);
+  RTR_LAUNCHED(2);
+  if (d_poses)
+    RTR_CUDA(cudaMemcpyAsync(d_poses, b.poses, sizeof(double) * 16 * max_clusters, cudaMemcpyDeviceToDevice, st));
+  if (d_sizes) RTR_CUDA(cudaMemcpyAsync(d_sizes, b.sizes, sizeof(int) * max_clusters, cudaMemcpyDeviceToDevice, st));
+  RTR_CUDA(cudaGetLastError());
+  return RTR_OK;
+}
+
+rtr_status gc_group_dev(rtr_context* ctx, Scratch& s, const float* d_model_kp, const float* d_scene_kp,
+                        const int32_t* d_corr_m, const int32_t* d_corr_s, const float* d_corr_d, int n_corr,
+                        float gc_size, int gc_thresh, int max_clusters, int max_members, int32_t* d_members,
+                        int32_t* d_sizes, double* d_poses, int* h_n_clusters, cudaStream_t st) {
+  *h_n_clusters = 0;
+  if (n_corr == 0) return RTR_OK;
+  GcBufs b;
+  uint32_t* vs = nullptr;
+  RTR_TRY(gc_launch(ctx, s, d_model_kp, d_scene_kp, d_corr_m, d_corr_s, d_corr_d, n_corr, nullptr, gc_size,
+                    gc_thresh, max_clusters, st, &b, &vs));
+  // errors come back as this call's status, so they go to a spare status slot
+  k_gc_post<<<1, 32, 0, st>>>(b.misc, max_clusters, nullptr, ctx->d_status + 15, ctx->d_status + 16);
+  RTR_LAUNCHED(1);
   int* h = ctx->h_pin;
   RTR_CUDA(cudaMemcpyAsync(h, b.misc, 12 * sizeof(int), cudaMemcpyDeviceToHost, st));
   RTR_CUDA(cudaStreamSynchronize(st));
@@ -676,13 +738,8 @@ rtr_status gc_group_dev(rtr_context* ctx, Scratch& s, const float* d_model_kp, c
     return fail(RTR_ERR_CAPACITY, "rtr_gc_group: a consensus set exceeds %d members", GC_MAXS);
   if (h[3] == (int)RTR_ERR_TIMEOUT)
     return fail(RTR_ERR_TIMEOUT, "rtr_gc_group: a grid barrier wait exceeded the budget");
-  ctx->gc_stats[0] = h[4];
-  ctx->gc_stats[1] = h[0];
-  ctx->gc_stats[2] = h[5];
-  for (int k = 0; k < 4; ++k) ctx->gc_stats[3 + k] = h[8 + k];
-  ctx->gc_stats[7] = h[7];
   if (ncl > 0) {
-    k_gc_poses<<<(ncl + 3) / 4, 128, 0, st>>>(b.pm, b.ps, b.members, b.sizes, ncl, GC_MAXS, b.poses);
+    k_gc_poses<<<(ncl + 3) / 4, 128, 0, st>>>(b.pm, b.ps, b.members, b.sizes, ncl, nullptr, GC_MAXS, b.poses);
     RTR_LAUNCHED(1);
     if (d_poses) RTR_CUDA(cudaMemcpyAsync(d_poses, b.poses, sizeof(double) * 16 * ncl, cudaMemcpyDeviceToDevice, st));
     if (d_sizes) RTR_CUDA(cudaMemcpyAsync(d_sizes, b.sizes, sizeof(int) * ncl, cudaMemcpyDeviceToDevice, st));
@@ -701,7 +758,15 @@ rtr_status gc_group_dev(rtr_context* ctx, Scratch& s, const float* d_model_kp, c
 
 extern "C" rtr_status rtr_gc_stats(rtr_context* ctx, int* h_stats8) {
   RTR_CHECK_ARG(ctx && h_stats8, "rtr_gc_stats: bad arguments");
-  for (int i = 0; i < 8; ++i) h_stats8[i] = ctx->gc_stats[i];
+  RTR_CUDA(cudaSetDevice(ctx->device));
+  RTR_CUDA(cudaDeviceSynchronize());
+  int h[12];
+  RTR_CUDA(cudaMemcpy(h, ctx->d_status + 16, sizeof(h), cudaMemcpyDeviceToHost));
+  h_stats8[0] = h[4];  // rounds
+  h_stats8[1] = h[0];  // walk end
+  h_stats8[2] = h[5];  // sets computed
+  for (int k = 0; k < 4; ++k) h_stats8[3 + k] = h[8 + k];
+  h_stats8[7] = h[7];  // candidates
   return RTR_OK;
 }
 

@@ -330,9 +330,11 @@ static int grid_blocks(int n) {
   return b;
 }
 
-void bbox_build(GridMeta* m, const float4* pts, int n, cudaStream_t st) {
+void bbox_build(GridMeta* m, const float4* pts, int n, cudaStream_t st) { bbox_build(m, pts, n, nullptr, st); }
+
+void bbox_build(GridMeta* m, const float4* pts, int n_cap, const int* d_n, cudaStream_t st) {
   k_bbox_init<<<1, 32, 0, st>>>(m);
-  k_bbox<<<grid_blocks(n), 256, 0, st>>>(pts, n, nullptr, m);
+  k_bbox<<<grid_blocks(n_cap), 256, 0, st>>>(pts, n_cap, d_n, m);
   RTR_LAUNCHED(2);
 }
 

@@ -54,6 +54,8 @@ void grid_build(const GridBufs& b, const float4* pts, int n_host, const int* d_n
                 cudaStream_t st);
 // Bounding box only (fills m->bmin / m->bmax).
 void bbox_build(GridMeta* m, const float4* pts, int n, cudaStream_t st);
+// Same over the first *d_n (<= n_cap) points.
+void bbox_build(GridMeta* m, const float4* pts, int n_cap, const int* d_n, cudaStream_t st);
 inline GridDev grid_dev(const GridBufs& b) { return GridDev{b.meta, b.pts, b.idx, b.cells}; }
 inline unsigned default_cell_cap(int n) {
   unsigned c = (unsigned)n * 8u;

@@ -48,6 +48,16 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(const IcpDev* __restrict__ 
   __shared__ int s_last, s_stop;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (a.d_active && a.slot >= *a.d_active) {  // a capacity slot left unused: every block of it leaves
+    if (lb == 0 && tid == 0) {
+      a.result->iterations = 0;
+      a.result->converged = 0;
+      a.result->n_corr = 0;
+      a.result->fitness = 0.0;
+      a.result->status = RTR_OK;
+    }
+    return;
+  }
   const int B = a.nblk;
   const GridView g = load_view(a.grid);
   // Centring: target terms about the target box centre c, source terms about
@@ -78,7 +88,7 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(const IcpDev* __restrict__ 
       const float4 p = xform_exact(T, a.src[i]);
       float d2;
       int j, pos;
-      grid_nn1_group<G>(g, p, a.r2max, lg, gmask, d2, j, pos);
+      grid_nn1_group<G, true>(g, p, a.r2max, lg, gmask, d2, j, pos);
       if (lg != 0) continue;
       if (j >= 0) {
         const float4 q = g.pts[pos];
@@ -411,6 +421,9 @@ rtr_status icp_multi(rtr_context* ctx, Scratch& s, std::vector<IcpSpec>& specs, 
   if (M == 0) return RTR_OK;
   const int maxb = icp_max_blocks(ctx);
   if (M > maxb) return fail(RTR_ERR_CAPACITY, "icp: %d problems exceed the %d co-resident blocks", M, maxb);
+  // a share of the GPU when several contexts run cooperative kernels at once
+  int budget = maxb / (ctx->coop_div > 0 ? ctx->coop_div : 1);
+  if (budget < M) budget = M;
   IcpDev* d_probs = s.take<IcpDev>(M);
   int* d_b2p = s.take<int>(maxb);
   double* pose64 = s.take<double>((size_t)M * 16);
@@ -430,7 +443,7 @@ rtr_status icp_multi(rtr_context* ctx, Scratch& s, std::vector<IcpSpec>& specs, 
   std::vector<int> nblk(M);
   int used = 0;
   for (int i = 0; i < M; ++i) {
-    long long b = want_total <= maxb ? want[i] : (want[i] * (maxb - M)) / want_total + 1;
+    long long b = want_total <= budget ? want[i] : (want[i] * (budget - M)) / want_total + 1;
     nblk[i] = (int)(b < 1 ? 1 : b);
     used += nblk[i];
   }

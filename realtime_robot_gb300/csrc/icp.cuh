@@ -28,6 +28,8 @@ struct IcpDev {
   int* status;
   long long budget;
   int blk0, nblk;             // this problem's blocks in the launch
+  const int* d_active;        // when set: the problem runs only if slot < *d_active
+  int slot;
 };
 
 struct IcpSpec {

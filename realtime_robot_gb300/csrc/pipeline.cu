@@ -6,8 +6,8 @@
 // curvature gate / learned pruning) -> SHOT-352 -> 1-NN descriptor matching ->
 // geometric-consistency grouping -> hypothesis verification (model inliers in
 // the scene) -> batched ICP refinement of the best hypotheses -> final score
-// and non-maximum suppression.  Every count stays on the device except the
-// correspondence count, read once before grouping.
+// and non-maximum suppression.  Every count stays on the device: no stage
+// reads back to the host, so a warmed-up call can be captured in a CUDA graph.
 #include <cuda_bf16.h>
 #include <string.h>
 
@@ -36,6 +36,10 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
                         int ndb, const __nv_bfloat16* db_hi, const __nv_bfloat16* db_lo, const float* db_n2,
                         int* out_idx, float* out_d2, cudaStream_t st);
 size_t gc_scratch_bytes(int C, int max_clusters);
+rtr_status gc_group_async(rtr_context* ctx, Scratch& s, const float* d_model_kp, const float* d_scene_kp,
+                          const int32_t* d_corr_m, const int32_t* d_corr_s, const float* d_corr_d, int C_cap,
+                          const int* d_C, float gc_size, int gc_thresh, int max_clusters, int32_t* d_sizes,
+                          double* d_poses, int* d_ncl, cudaStream_t st);
 size_t mlp_infer_bytes(int n_cap);
 rtr_status mlp_score_rows(Scratch& s, const rtr_mlp* m, const float* X, int n_cap, const int* d_n, float* score,
                           cudaStream_t st);
@@ -144,10 +148,11 @@ constexpr int HV_G = 4;
 // the atomic adds does not matter.
 constexpr int HV_PPB = 256;
 __global__ void __launch_bounds__(256) k_hv_count(GridDev gd, const float4* __restrict__ model, int n_model, int stride,
-                                                  const double* __restrict__ poses, int n_hyp, float r2, int bph,
-                                                  int* __restrict__ counts) {
+                                                  const double* __restrict__ poses, int n_hyp, const int* d_nhyp,
+                                                  float r2, int bph, int* __restrict__ counts) {
   __shared__ int s_cnt;
   const int h = blockIdx.x / bph, part = blockIdx.x - h * bph;
+  if (d_nhyp) n_hyp = min(*d_nhyp, n_hyp);
   if (h >= n_hyp) return;
   const GridView g = load_view(gd);
   float T[12];
@@ -164,7 +169,7 @@ __global__ void __launch_bounds__(256) k_hv_count(GridDev gd, const float4* __re
     const float4 p = xform_exact(T, model[(size_t)i * stride]);
     float d2;
     int bi, bp;
-    grid_nn1_group<HV_G>(g, p, r2, lg, gmask, d2, bi, bp);
+    grid_nn1_group<HV_G, true>(g, p, r2, lg, gmask, d2, bi, bp);
     if (lg == 0 && bi >= 0) ++cnt;
   }
 #pragma unroll
@@ -174,28 +179,36 @@ __global__ void __launch_bounds__(256) k_hv_count(GridDev gd, const float4* __re
   if (threadIdx.x == 0 && s_cnt) atomicAdd(counts + h, s_cnt);
 }
 
-__global__ void k_hv_finish(const int* __restrict__ counts, int n_hyp, int total, float* __restrict__ score) {
+__global__ void k_hv_finish(const int* __restrict__ counts, int n_hyp, const int* d_nhyp, int total,
+                            float* __restrict__ score) {
+  if (d_nhyp) n_hyp = min(*d_nhyp, n_hyp);
   for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < n_hyp; h += gridDim.x * blockDim.x)
     score[h] = total > 0 ? (float)counts[h] / (float)total : 0.f;
 }
 
 static rtr_status hv_score(GridDev gd, const float4* model, int n_model, int stride, const double* poses, int n_hyp,
-                           float r2, int* counts, float* score, cudaStream_t st) {
+                           const int* d_nhyp, float r2, int* counts, float* score, cudaStream_t st) {
   const int total = (n_model + stride - 1) / stride;
   const int bph = (total + HV_PPB - 1) / HV_PPB > 0 ? (total + HV_PPB - 1) / HV_PPB : 1;
   RTR_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * (size_t)n_hyp, st));
-  k_hv_count<<<n_hyp * bph, 256, 0, st>>>(gd, model, n_model, stride, poses, n_hyp, r2, bph, counts);
-  k_hv_finish<<<(n_hyp + 255) / 256, 256, 0, st>>>(counts, n_hyp, total, score);
+  k_hv_count<<<n_hyp * bph, 256, 0, st>>>(gd, model, n_model, stride, poses, n_hyp, d_nhyp, r2, bph, counts);
+  k_hv_finish<<<(n_hyp + 255) / 256, 256, 0, st>>>(counts, n_hyp, d_nhyp, total, score);
   RTR_LAUNCHED(2);
   return RTR_OK;
 }
 
-// Top-m hypotheses by score (ties: lower hypothesis index) -> order[0..m);
-// one warp, scores staged in shared memory (n <= 256).
-__global__ void k_topm(const float* __restrict__ score, int n, int m, int* __restrict__ order) {
+// Top-m hypotheses by score (ties: lower hypothesis index) -> order[0..m),
+// with n = min(*d_n, n_cap) hypotheses and m = min(n, m_cap); order[m..m_cap)
+// = -1 and *d_m = m.  One warp, scores staged in shared memory (n <= 256).
+__global__ void k_topm(const float* __restrict__ score, int n_cap, const int* d_n, int m_cap,
+                       int* __restrict__ order, int* __restrict__ d_m) {
   __shared__ float s_sc[256];
   const int lane = threadIdx.x;
   if (lane >= 32) return;
+  const int n = d_n ? min(*d_n, n_cap) : n_cap;
+  const int m = min(n, m_cap);
+  if (lane == 0) *d_m = m;
+  for (int k = m + lane; k < m_cap; k += 32) order[k] = -1;
   for (int h = lane; h < 256; h += 32) s_sc[h] = h < n ? score[h] : 0.f;
   bool used[8] = {false, false, false, false, false, false, false, false};  // hypothesis lane + 32 q taken
   __syncwarp();
@@ -241,10 +254,11 @@ __global__ void k_copy_result_poses(const rtr_icp_result* __restrict__ r, int m,
 
 // Non-maximum suppression and the result record (one thread).
 __global__ void k_finalize(const float* __restrict__ fscore, const double* __restrict__ refined,
-                           const int* __restrict__ order, const int* __restrict__ cl_sizes, int m, float accept,
-                           float nms2, int max_inst, const int* d_V, const int* d_K, const int* d_C, int ncl,
-                           rtr_recog_result* __restrict__ out) {
+                           const int* __restrict__ order, const int* __restrict__ cl_sizes, int m_cap,
+                           const int* d_m, float accept, float nms2, int max_inst, const int* d_V, const int* d_K,
+                           const int* d_C, const int* d_ncl, const int* d_status, rtr_recog_result* __restrict__ out) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int m = min(*d_m, m_cap), ncl = *d_ncl;
   int picked[RTR_MAX_INSTANCES];
   int np = 0;
   bool used[64];
@@ -278,18 +292,8 @@ __global__ void k_finalize(const float* __restrict__ fscore, const double* __res
   out->n_keypoints = *d_K;
   out->n_correspondences = d_C ? *d_C : 0;
   out->n_clusters = ncl;
-  out->status = RTR_OK;
-}
-
-__global__ void k_empty_result(rtr_recog_result* out, const int* d_V, const int* d_K, const int* d_C) {
-  if (threadIdx.x == 0) {
-    out->n_instances = 0;
-    out->n_voxels = *d_V;
-    out->n_keypoints = *d_K;
-    out->n_correspondences = d_C ? *d_C : 0;
-    out->n_clusters = 0;
-    out->status = RTR_ERR_NOT_FOUND;
-  }
+  const int err = *d_status;  // a failed stage of this context (timeout, capacity)
+  out->status = err ? err : (ncl > 0 ? RTR_OK : RTR_ERR_NOT_FOUND);
 }
 
 }  // namespace rtr
@@ -454,7 +458,8 @@ namespace rtr {
 
 // Persistent buffers of one recognition (outlive the stages that fill them).
 struct RecogBufs {
-  int* cnt;                 // [0] V, [1] K (uniform), [2] K (gated), [3] C, [4] K (pruned)
+  int* cnt;                 // [0] V, [1] K (uniform), [2] K (gated), [3] C, [4] K (pruned),
+                            // [5] clusters, [6] hypotheses refined
   float4 *sv, *sn, *skp;
   int *keys, *keys2, *midx, *cm, *cs;
   float *desc, *md2, *cd;
@@ -662,30 +667,25 @@ static rtr_status recognize_impl(rtr_context* ctx, const rtr_model* m, const flo
     k_gather_kp<<<nb, 256, 0, st>>>(b.sv, keys, dKeys, n, b.skp);
     RTR_LAUNCHED(3);
   }
-  RTR_CUDA(cudaMemcpyAsync(ctx->h_pin, dC, sizeof(int), cudaMemcpyDeviceToHost, st));
-  RTR_CUDA(cudaStreamSynchronize(st));
-  const int C = ctx->h_pin[0];
-  int ncl = 0;
-  if (C > 0) {
+  // From here on every count stays on the device (no host round trip): the
+  // stages are sized for their capacities (n correspondences, max_clusters
+  // hypotheses, refine_top refinements) and read the live counts.
+  int* dNcl = b.cnt + 5;
+  int* dM = b.cnt + 6;
+  {
     ProfScope ps(ctx, st, "gc_group");
     Scratch t = stage;
-    RTR_TRY(gc_group_dev(ctx, t, reinterpret_cast<const float*>(m->kp), reinterpret_cast<const float*>(b.skp), b.cm,
-                         b.cs, b.cd, C, q->gc_size, q->gc_thresh, q->max_clusters, 1, nullptr, b.sizes, b.poses, &ncl,
-                         st));
+    RTR_TRY(gc_group_async(ctx, t, reinterpret_cast<const float*>(m->kp), reinterpret_cast<const float*>(b.skp), b.cm,
+                           b.cs, b.cd, n, dC, q->gc_size, q->gc_thresh, q->max_clusters, b.sizes, b.poses, dNcl,
+                           st));
   }
-  if (ncl == 0) {
-    k_empty_result<<<1, 32, 0, st>>>(out, dV, dKeys, dC);
-    RTR_LAUNCHED(1);
-    RTR_CUDA(cudaGetLastError());
-    return RTR_OK;
-  }
-  const int M = ncl < q->refine_top ? ncl : q->refine_top;
+  const int H = q->max_clusters, M = q->refine_top;
   {
     ProfScope ps(ctx, st, "verify");
     grid_build(b.grid, b.sv, n, dV, q->icp_max_dist, st);
-    RTR_TRY(hv_score(grid_dev(b.grid), m->vox, m->n_vox, q->hv_subsample > 0 ? q->hv_subsample : 1, b.poses, ncl,
-                     q->hv_inlier_r * q->hv_inlier_r, b.hvcnt, b.hv, st));
-    k_topm<<<1, 32, 0, st>>>(b.hv, ncl, M, b.order);
+    RTR_TRY(hv_score(grid_dev(b.grid), m->vox, m->n_vox, q->hv_subsample > 0 ? q->hv_subsample : 1, b.poses, H,
+                     dNcl, q->hv_inlier_r * q->hv_inlier_r, b.hvcnt, b.hv, st));
+    k_topm<<<1, 32, 0, st>>>(b.hv, H, dNcl, M, b.order, dM);
     k_select_poses<<<1, 256, 0, st>>>(b.poses, b.order, M, b.init);
     RTR_LAUNCHED(2);
   }
@@ -707,6 +707,8 @@ static rtr_status recognize_impl(rtr_context* ctx, const rtr_model* m, const flo
       d.eps_r = 0.0;
       for (int e = 0; e < 16; ++e) d.init[e] = (e % 5) == 0 ? 1.0 : 0.0;
       d.result = b.res + k;
+      d.d_active = dM;  // slots past the hypotheses found leave at once
+      d.slot = k;
       specs[k].init_dev = b.init + 16 * k;
     }
     RTR_TRY(icp_multi(ctx, t, specs, st));
@@ -714,11 +716,11 @@ static rtr_status recognize_impl(rtr_context* ctx, const rtr_model* m, const flo
   {
     ProfScope ps(ctx, st, "final_score");
     k_copy_result_poses<<<1, 256, 0, st>>>(b.res, M, b.refined);
-    RTR_TRY(hv_score(grid_dev(b.grid), m->vox, m->n_vox, 1, b.refined, M, q->accept_inlier_r * q->accept_inlier_r,
-                     b.hvcnt, b.fscore, st));
+    RTR_TRY(hv_score(grid_dev(b.grid), m->vox, m->n_vox, 1, b.refined, M, dM,
+                     q->accept_inlier_r * q->accept_inlier_r, b.hvcnt, b.fscore, st));
     const float nms2 = q->nms_dist * q->nms_dist;
-    k_finalize<<<1, 32, 0, st>>>(b.fscore, b.refined, b.order, b.sizes, M, q->accept_score, nms2,
-                                 q->max_instances, dV, dKeys, dC, ncl, out);
+    k_finalize<<<1, 32, 0, st>>>(b.fscore, b.refined, b.order, b.sizes, M, dM, q->accept_score, nms2,
+                                 q->max_instances, dV, dKeys, dC, dNcl, ctx->d_status, out);
     RTR_LAUNCHED(2);
   }
   RTR_CUDA(cudaGetLastError());

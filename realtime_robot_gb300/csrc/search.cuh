@@ -194,7 +194,10 @@ __device__ __forceinline__ void group_best(unsigned gmask, float& bd, int& bi, i
 // every ring the group agrees on the best (d^2, index), so the ring loop is
 // uniform inside the group.  A lane skips a cell only when the cell is beyond
 // its own best, which is never better than the group's.
-template <int G>
+// CP (cell-parallel): each lane scans its own candidate cells of a chunk,
+// with the first two points of all four issued as independent loads, instead
+// of the group scanning one candidate cell after another.  Same result.
+template <int G, bool CP = false>
 __device__ __forceinline__ void grid_nn1_group(const GridView& g, float4 q, float r2max, int lg,
                                                unsigned gmask, float& bd, int& bi, int& bpos) {
   bd = r2max;
@@ -233,15 +236,33 @@ __device__ __forceinline__ void grid_nn1_group(const GridView& g, float4 q, floa
             }
           }
         }
+        if (CP) {
+          float4 p0[4], p1[4];
 #pragma unroll
-        for (int s = 0; s < 4; ++s) {
-          unsigned bal = __ballot_sync(gmask, cand[s]) >> gbase;
-          while (bal) {
-            const int src = __ffs(bal) - 1;
-            bal &= bal - 1;
-            const unsigned b0 = __shfl_sync(gmask, cc[s].x, gbase + src);
-            const unsigned b1 = __shfl_sync(gmask, cc[s].y, gbase + src);
-            for (unsigned j = b0 + (unsigned)lg; j < b1; j += G) nn_take(g.pts[j], j, q, bd, bi, bpos);
+          for (int s = 0; s < 4; ++s) {
+            const unsigned a = cc[s].x, e = cc[s].y;
+            p0[s] = (cand[s] && a < e) ? g.pts[a] : q;
+            p1[s] = (cand[s] && a + 1 < e) ? g.pts[a + 1] : q;
+          }
+#pragma unroll
+          for (int s = 0; s < 4; ++s) {
+            if (!cand[s]) continue;
+            const unsigned a = cc[s].x, e = cc[s].y;
+            if (a < e) nn_take(p0[s], a, q, bd, bi, bpos);
+            if (a + 1 < e) nn_take(p1[s], a + 1, q, bd, bi, bpos);
+            for (unsigned j = a + 2; j < e; ++j) nn_take(g.pts[j], j, q, bd, bi, bpos);
+          }
+        } else {
+#pragma unroll
+          for (int s = 0; s < 4; ++s) {
+            unsigned bal = __ballot_sync(gmask, cand[s]) >> gbase;
+            while (bal) {
+              const int src = __ffs(bal) - 1;
+              bal &= bal - 1;
+              const unsigned b0 = __shfl_sync(gmask, cc[s].x, gbase + src);
+              const unsigned b1 = __shfl_sync(gmask, cc[s].y, gbase + src);
+              for (unsigned j = b0 + (unsigned)lg; j < b1; j += G) nn_take(g.pts[j], j, q, bd, bi, bpos);
+            }
           }
         }
       }

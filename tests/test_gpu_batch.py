@@ -1,5 +1,10 @@
 """rtr_recognize_batch: every pair's result equals the single-pair call's,
-for the plain and the learned form; the autotuner picks a valid setting."""
+for the plain and the learned form; the autotuner picks a valid setting.
+
+Batch workers each get a share of the GPU for the cooperative kernels, so an
+ICP problem may be split over fewer blocks than in a single call; its FP32
+block sums then round differently.  Counts must match exactly, poses within
+1e-5 (the ICP tolerance against the FP64 oracle) and scores within 1e-3."""
 import ctypes as C
 
 import numpy as np
@@ -28,13 +33,24 @@ def _rows(res):
     return [bytes(r) for r in res.cpu().numpy()]
 
 
+def _same(rtr, a: bytes, b: bytes):
+    ra, rb = rtr.parse_recog_result(a), rtr.parse_recog_result(b)
+    for k in ("n_voxels", "n_keypoints", "n_correspondences", "n_clusters", "status"):
+        assert ra[k] == rb[k], k
+    assert len(ra["instances"]) == len(rb["instances"])
+    for x, y in zip(ra["instances"], rb["instances"]):
+        assert x["hypothesis"] == y["hypothesis"] and x["cluster_size"] == y["cluster_size"]
+        np.testing.assert_allclose(x["pose"], y["pose"], atol=1e-5)
+        assert abs(x["score"] - y["score"]) <= 1e-3
+
+
 def test_batch_equals_single_calls(ctx, rtr, batch):
     prm, mods, scenes = batch
     ctx.set_tuning("batch_workers", 3)
     got = _rows(rtr.recognize_batch(ctx, mods, scenes, prm))
     for i, (m, s) in enumerate(zip(mods, scenes)):
         ref = rtr.recognize(ctx, m, s, prm).cpu().numpy().tobytes()
-        assert got[i] == ref, i
+        _same(rtr, got[i], ref)
     ctx.set_tuning("batch_workers", 0)
 
 
@@ -44,7 +60,7 @@ def test_batch_learned_equals_single_calls(ctx, rtr, batch):
     got = _rows(rtr.recognize_batch(ctx, mods, scenes, prm, mlp=mlp, keep=0.5))
     for i, (m, s) in enumerate(zip(mods, scenes)):
         ref = rtr.recognize_learned(ctx, m, mlp, s, keep=0.5, params=prm).cpu().numpy().tobytes()
-        assert got[i] == ref, i
+        _same(rtr, got[i], ref)
 
 
 def test_batch_autotune(ctx, rtr, batch):
@@ -58,3 +74,39 @@ def test_batch_autotune(ctx, rtr, batch):
 def test_batch_empty(ctx, rtr, batch):
     prm, _, _ = batch
     rtr.recognize_batch(ctx, [], [], prm)
+
+
+def test_batch_graph_replays_the_batch(ctx, rtr, batch):
+    import torch
+    prm, mods, scenes = batch
+    ctx.set_tuning("batch_workers", 4)
+    ref = _rows(rtr.recognize_batch(ctx, mods, scenes, prm))
+    g = rtr.BatchGraph(ctx, mods, scenes, prm)
+    for _ in range(2):
+        g.results.zero_()
+        g.launch()
+        torch.cuda.synchronize()
+        got = _rows(g.results)
+        for a, b in zip(got, ref):
+            assert a == b  # same workers, same blocks: identical
+    g.close()
+    ctx.set_tuning("batch_workers", 0)
+
+
+def test_single_recognition_captured_in_a_graph(ctx, rtr, batch):
+    import torch
+    prm, mods, scenes = batch
+    m, s = mods[0], scenes[0]
+    ref = rtr.recognize(ctx, m, s, prm).cpu().numpy().tobytes()
+    st = torch.cuda.Stream()
+    res = torch.zeros(C.sizeof(rtr.RecogResult), dtype=torch.uint8, device="cuda")
+    with torch.cuda.stream(st):
+        rtr.recognize(ctx, m, s, prm, result=res, stream=st.cuda_stream)  # sizes the scratch
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=st, capture_error_mode="thread_local"):
+        rtr.recognize(ctx, m, s, prm, result=res, stream=st.cuda_stream)
+    res.zero_()
+    g.replay()
+    torch.cuda.synchronize()
+    assert res.cpu().numpy().tobytes() == ref
