@@ -417,9 +417,10 @@ def run_ours(args):
 
 def batch_block(ctx, R, steps: int) -> dict:
     """Config 2: 64 model x segment pairs (chairs, desks, sofas; 2k-60k points,
-    <= 30 deg, +-0.3 m, 2 mm noise, 0-40 % crop) through rtr_recognize_batch,
-    plain and learned (MLP trained here on the GPU, top 25 % of keypoints),
-    against the same pairs one rtr_recognize call at a time."""
+    <= 30 deg, +-0.3 m, 2 mm noise, 0-40 % crop) through rtr_recognize_batch
+    and as a replayed CUDA graph (rtr_batch_graph_*), plain and learned (MLP
+    trained here on the GPU, top 25 % of keypoints), against the same pairs
+    one rtr_recognize call at a time."""
     import torch
     from realtime_robot_gb300 import learned as L
     prm = R.recog_default_params(viewpoint=(0.0, 0.0, 0.0))
@@ -456,6 +457,13 @@ def batch_block(ctx, R, steps: int) -> dict:
     workers, group = R.batch_autotune(ctx, mods[:16], scenes[:16], prm)
     t_plain = timed(lambda: R.recognize_batch(ctx, mods, scenes, prm), reps)
     t_learned = timed(lambda: R.recognize_batch(ctx, mods, scenes, prm, mlp=mlp, keep=0.25), reps)
+    # the same batches captured once into CUDA graphs and replayed
+    gp = R.BatchGraph(ctx, mods, scenes, prm)
+    gl = R.BatchGraph(ctx, mods, scenes, prm, mlp=mlp, keep=0.25)
+    t_gplain = timed(lambda: gp.launch(), reps)
+    t_glearned = timed(lambda: gl.launch(), reps)
+    gp.close()
+    gl.close()
     ctx.set_tuning("batch_workers", 0)
     ctx.set_tuning("icp_group", 0)
     res_p = [R.parse_recog_result(bytes(r)) for r in R.recognize_batch(ctx, mods, scenes, prm).cpu().numpy()]
@@ -474,9 +482,10 @@ def batch_block(ctx, R, steps: int) -> dict:
     return {"metric": "pairs/s (config 2: 64 model x segment pairs, 2k-60k points)", "unit": "pairs/s",
             "pairs": n, "points": npts,
             "sequential_plain": n / t_seq, "batched_plain": n / t_plain, "batched_learned": n / t_learned,
+            "graph_plain": n / t_gplain, "graph_learned": n / t_glearned,
             # a pair whose learned pose disagrees with the plain one is re-run plain
-            "batched_learned_with_fallback": n / (t_learned + (n - agree) / n * t_plain),
-            "learned_batched_over_plain_sequential": t_seq / t_learned,
+            "graph_learned_with_fallback": n / (t_glearned + (n - agree) / n * t_gplain),
+            "learned_graph_over_plain_sequential": t_seq / t_glearned,
             "autotuned": {"workers": workers, "icp_group": group},
             "learned": {"keep": 0.25, "train_rows": int(X.shape[0]), "positive_rate": float(y.mean()),
                         "train_s_incl_harvest": train_s, "final_loss": float(losses[-1]),

@@ -65,7 +65,8 @@ const char* rtr_version(void);
 /* Tuning knobs of this context (value 0 restores the automatic choice):
  *   "icp_group"      lanes cooperating on one ICP source point's 1-NN search
  *                    (2, 4 or 8);
- *   "batch_workers"  worker threads of rtr_recognize_batch (1..16).
+ *   "batch_workers"  workers (streams) of rtr_recognize_batch (1..16);
+ *   "gc_window"      seeds per window of the grouping walk (32..1024).
  * Unknown keys or values return RTR_ERR_INVALID_ARG.  Results do not depend
  * on the knobs beyond FP32 summation order. */
 rtr_status rtr_context_set_tuning(rtr_context* ctx, const char* key, int value);

@@ -242,6 +242,12 @@ rtr_status rtr_context_set_tuning(rtr_context* ctx, const char* key, int value) 
     ctx->tune_batch_workers = value;
     return RTR_OK;
   }
+  if (strcmp(key, "gc_window") == 0) {
+    if (value < 0 || value > 1024)
+      return rtr::fail(RTR_ERR_INVALID_ARG, "gc_window must be 0..1024 (got %d)", value);
+    ctx->tune_gc_window = value;
+    return RTR_OK;
+  }
   if (strcmp(key, "icp_group") == 0) {
     if (value != 0 && value != 2 && value != 4 && value != 8)
       return rtr::fail(RTR_ERR_INVALID_ARG, "icp_group must be 0, 2, 4 or 8 (got %d)", value);
