@@ -464,6 +464,39 @@ rtr_status rtr_mlp_train_step(rtr_context* ctx, rtr_mlp* m, const float* d_x, co
 rtr_status rtr_mlp_train(rtr_context* ctx, rtr_mlp* m, const float* d_x, const float* d_y, int n, int batch,
                          int epochs, float lr, uint64_t seed, float* h_epoch_loss);
 
+/* ---- streaming: depth frames, back-projection, fusion map ------------------
+ * Depth frames are organised width x height float32 images of z in metres
+ * (0 = no return), pinhole (fx, fy, cx, cy).  A pose maps camera
+ * coordinates (x right, y down, z forward) to world coordinates (row-major
+ * 4x4, FP64 on the host). */
+
+/* Points of a depth frame with min_z < z < max_z, in pixel order (row by
+ * row), as world points pose * ((u - cx) z / fx, (v - cy) z / fy, z), each
+ * operation rounded in FP32 (h_pose16 NULL = identity).  d_points holds
+ * width * height points; the count goes to the device int d_count.
+ * Synchronises (the pose is staged from the host). */
+rtr_status rtr_depth_to_points(rtr_context* ctx, const float* d_depth, int width, int height, float fx,
+                               float fy, float cx, float cy, const double* h_pose16, float min_z,
+                               float max_z, float* d_points, int* d_count, rtr_stream_t stream);
+
+/* Fusion map: a GPU hash table of voxels (edge `voxel`) keeping, per voxel,
+ * its point count and the mean of its points.  Sums are kept in fixed point
+ * (2^-40 m) with integer atomics, so the contents do not depend on the order
+ * in which points arrive.  capacity is rounded up to a power of two and
+ * should be at least twice the voxels the map will hold: an insert looks at
+ * no more than 256 slots, and a point that finds none free is dropped and
+ * makes rtr_map_extract return RTR_ERR_CAPACITY. */
+typedef struct rtr_map rtr_map;
+rtr_status rtr_map_create(rtr_context* ctx, int capacity, float voxel, rtr_map** out);
+rtr_status rtr_map_destroy(rtr_map* m);
+rtr_status rtr_map_clear(rtr_map* m, rtr_stream_t stream);
+/* Adds the first *d_n (d_n NULL: n_cap) points (device). */
+rtr_status rtr_map_integrate(rtr_map* m, const float* d_points, int n_cap, const int* d_n, rtr_stream_t stream);
+/* Occupied voxels as {mean x, mean y, mean z, count (int bits)} into d_out
+ * (in table order), their number into *h_count; with more than max_out
+ * voxels only the count is written.  Synchronises. */
+rtr_status rtr_map_extract(rtr_context* ctx, rtr_map* m, float* d_out, int max_out, int* h_count);
+
 /* ---- synthetic inputs (host only; seeded, identical on every machine) ----- */
 
 /* Shapes: 0 = chair (seat 0.45x0.45x0.03, four legs 0.03x0.03x0.45, backrest
@@ -500,6 +533,24 @@ void rtr_room_default_params(rtr_room_params* p);
 rtr_status rtr_synth_room(const rtr_room_params* p, uint64_t seed, float* h_out_xyz4,
                           int max_instances, int* h_inst_shape, double* h_inst_pose16,
                           int* h_n_instances);
+/* The furniture of the same room (same placement rule) as world boxes: 12
+ * floats per box {cos yaw, sin yaw, x, y, lo[3], hi[3], shape, instance}
+ * (lo/hi in the object frame). */
+rtr_status rtr_synth_room_boxes(const rtr_room_params* p, uint64_t seed, float* h_boxes12, int max_boxes,
+                                int* h_n_boxes, int* h_inst_shape, double* h_inst_pose16,
+                                int max_instances, int* h_n_instances);
+/* A smooth seeded camera path through the room at `fps`: x sweeps +-1.2 m
+ * (peak 0.5 m/s) near y = -2.3 at 1.5 m height, yaw +-20 deg (peak
+ * 17.5 deg/s), 25 deg down.  Poses camera -> world, 16 doubles per frame. */
+void rtr_synth_trajectory(uint64_t seed, int n_frames, double fps, double* h_poses16);
+/* Ray-cast depth frames of a room (floor, two walls, the boxes) from the
+ * given camera poses into d_depth (n_frames x height x width), with
+ * N(0, (noise_k z^2)^2) depth noise from a counter-based hash of (seed, frame,
+ * pixel).  On the GPU; synchronises. */
+rtr_status rtr_synth_depth_frames(rtr_context* ctx, const float* h_boxes12, int n_boxes,
+                                  const double* h_poses16, int n_frames, int width, int height, float fx,
+                                  float fy, float cx, float cy, float noise_k, uint64_t seed, float* d_depth,
+                                  rtr_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -170,6 +170,16 @@ _SIG = {
     "rtr_synth_transform_noise": (None, [_P, _I, _P, _D, _U64, _P]),
     "rtr_synth_crop": (_I, [_P, _I, _D, _U64, _P]),
     "rtr_room_default_params": (None, [C.POINTER(RoomParams)]),
+    "rtr_synth_room_boxes": (_I, [C.POINTER(RoomParams), _U64, _P, _I, C.POINTER(C.c_int), _P, _P, _I,
+                                  C.POINTER(C.c_int)]),
+    "rtr_synth_trajectory": (None, [_U64, _I, _D, _P]),
+    "rtr_synth_depth_frames": (_I, [_P, _P, _I, _P, _I, _I, _I, _F, _F, _F, _F, _F, _U64, _P, _P]),
+    "rtr_depth_to_points": (_I, [_P, _P, _I, _I, _F, _F, _F, _F, _P, _F, _F, _P, _P, _P]),
+    "rtr_map_create": (_I, [_P, _I, _F, C.POINTER(_P)]),
+    "rtr_map_destroy": (_I, [_P]),
+    "rtr_map_clear": (_I, [_P, _P]),
+    "rtr_map_integrate": (_I, [_P, _P, _I, _P, _P]),
+    "rtr_map_extract": (_I, [_P, _P, _P, _I, C.POINTER(C.c_int)]),
     "rtr_synth_room": (_I, [C.POINTER(RoomParams), _U64, _P, _I, _P, _P, _P]),
 }
 
@@ -291,6 +301,34 @@ class Context:
         check(lib().rtr_knn1_static(_ptr(query), nq, _ptr(target), nt, float(max_dist),
                                     _ptr(idx), _ptr(d2), _stream(stream)))
         return idx, d2
+
+    def synth_depth_frames(self, boxes: np.ndarray, poses: np.ndarray, width=640, height=480, fx=525.0, fy=525.0,
+                           cx=319.5, cy=239.5, noise_k=0.0015, seed=0, stream=None):
+        """Ray-cast depth frames [n_frames, height, width] (device) of the room
+        boxes from camera->world poses [n_frames, 4, 4]."""
+        import torch
+        boxes = np.ascontiguousarray(boxes, np.float32).reshape(-1, 12)
+        poses = np.ascontiguousarray(poses, np.float64).reshape(-1, 16)
+        out = torch.empty((poses.shape[0], height, width), dtype=torch.float32, device="cuda")
+        check(lib().rtr_synth_depth_frames(self.h, boxes.ctypes.data, boxes.shape[0], poses.ctypes.data,
+                                           poses.shape[0], width, height, fx, fy, cx, cy, noise_k, seed,
+                                           _ptr(out), _stream(stream)))
+        return out
+
+    def depth_to_points(self, depth, fx=525.0, fy=525.0, cx=319.5, cy=239.5, pose=None, min_z=0.05, max_z=8.0,
+                        out=None, count=None, stream=None):
+        """World points [k, 4] of one depth frame [height, width] (device)."""
+        import torch
+        h, w = depth.shape
+        if out is None:
+            out = torch.empty((h * w, 4), dtype=torch.float32, device=depth.device)
+        if count is None:
+            count = torch.zeros(1, dtype=torch.int32, device=depth.device)
+        P = None if pose is None else np.ascontiguousarray(pose, np.float64).reshape(16)
+        check(lib().rtr_depth_to_points(self.h, _ptr(depth), w, h, fx, fy, cx, cy,
+                                        None if P is None else P.ctypes.data, min_z, max_z, _ptr(out),
+                                        _ptr(count), _stream(stream)))
+        return out, count
 
     def knn(self, query, target, k: int, stream=None):
         import torch
@@ -683,6 +721,69 @@ def synth_crop(pts: np.ndarray, max_frac: float, seed: int) -> np.ndarray:
     out = np.empty_like(pts)
     m = lib().rtr_synth_crop(pts.ctypes.data, pts.shape[0], max_frac, seed, out.ctypes.data)
     return out[:m].copy()
+
+
+class FusionMap:
+    """rtr_map_*: GPU voxel-hash map of point means and counts."""
+
+    def __init__(self, ctx: "Context", capacity: int = 1 << 23, voxel: float = 0.005):
+        self.ctx = ctx
+        h = _P()
+        check(lib().rtr_map_create(ctx.h, int(capacity), float(voxel), C.byref(h)))
+        self.h = h
+
+    def clear(self, stream=None):
+        check(lib().rtr_map_clear(self.h, _stream(stream)))
+
+    def integrate(self, pts, count=None, stream=None):
+        check(lib().rtr_map_integrate(self.h, _ptr(pts), pts.shape[0], _ptr(count), _stream(stream)))
+
+    def extract(self, max_out: int = 1 << 23):
+        """[k, 4] device tensor {mean x, y, z, count as int bits} of the occupied voxels."""
+        import torch
+        out = torch.empty((max_out, 4), dtype=torch.float32, device="cuda")
+        n = C.c_int(0)
+        check(lib().rtr_map_extract(self.ctx.h, self.h, _ptr(out), int(max_out), C.byref(n)))
+        if n.value > max_out:  # only counted: extract again into a buffer that holds them
+            out = torch.empty((n.value, 4), dtype=torch.float32, device="cuda")
+            check(lib().rtr_map_extract(self.ctx.h, self.h, _ptr(out), n.value, C.byref(n)))
+        return out[: n.value]
+
+    def count(self) -> int:
+        """Occupied voxels (synchronises)."""
+        n = C.c_int(0)
+        check(lib().rtr_map_extract(self.ctx.h, self.h, None, 0, C.byref(n)))
+        return n.value
+
+    def close(self):
+        if self.h:
+            lib().rtr_map_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def synth_room_boxes(seed: int, params: RoomParams | None = None, max_boxes: int = 256, max_instances: int = 32):
+    """(boxes [k, 12], shapes, poses [n, 4, 4]) of the room's furniture."""
+    p = params or room_default_params()
+    boxes = np.zeros((max_boxes, 12), np.float32)
+    nb, ni = C.c_int(0), C.c_int(0)
+    shapes = np.zeros(max_instances, np.int32)
+    poses = np.zeros((max_instances, 16), np.float64)
+    check(lib().rtr_synth_room_boxes(C.byref(p), seed, boxes.ctypes.data, max_boxes, C.byref(nb),
+                                     shapes.ctypes.data, poses.ctypes.data, max_instances, C.byref(ni)))
+    k = min(ni.value, max_instances)
+    return boxes[: nb.value], shapes[:k], poses[:k].reshape(k, 4, 4)
+
+
+def synth_trajectory(seed: int, n_frames: int, fps: float = 30.0) -> np.ndarray:
+    out = np.zeros((n_frames, 16), np.float64)
+    lib().rtr_synth_trajectory(seed, n_frames, fps, out.ctypes.data)
+    return out.reshape(n_frames, 4, 4)
 
 
 def room_default_params() -> RoomParams:

@@ -120,9 +120,104 @@ double ray_box(const double o[3], const double d[3], const Box& b) {
   return t0 > 1e-9 ? t0 : -1;  // origin inside a box: no visible surface
 }
 
+struct Inst { int shape; double yaw, x, y; };
+
+// Furniture of a room: largest first, non-overlapping bounding circles.
+void place_furniture(const rtr_room_params* P, Rng& r, std::vector<Inst>& inst) {
+  std::vector<int> order;
+  for (int i = 0; i < P->n_sofas; ++i) order.push_back(2);
+  for (int i = 0; i < P->n_desks; ++i) order.push_back(1);
+  for (int i = 0; i < P->n_chairs; ++i) order.push_back(0);
+  for (int sh : order) {
+    const double rad = shape_radius(sh);
+    for (int tries = 0; tries < 2000; ++tries) {
+      const double x = -1.9 + rad * 0.5 + r.uniform() * (3.8 - rad);
+      const double y = -0.6 + r.uniform() * (2.6 - rad * 0.5);
+      const double yaw = 6.283185307179586 * r.uniform();
+      bool ok = x - rad > -2.45 && y + rad < 2.45;
+      for (const Inst& o : inst) {
+        const double dx = x - o.x, dy = y - o.y;
+        if (sqrt(dx * dx + dy * dy) < rad + shape_radius(o.shape) + 0.05) ok = false;
+      }
+      if (ok) {
+        inst.push_back({sh, yaw, x, y});
+        break;
+      }
+    }
+  }
+}
+
 }  // namespace
 
 extern "C" {
+
+rtr_status rtr_synth_room_boxes(const rtr_room_params* P, uint64_t seed, float* h_boxes, int max_boxes,
+                                int* h_n_boxes, int* h_inst_shape, double* h_inst_pose16, int max_instances,
+                                int* h_n_instances) {
+  if (!P || !h_boxes || !h_n_boxes) return RTR_ERR_INVALID_ARG;
+  Rng r(seed);
+  std::vector<Inst> inst;
+  place_furniture(P, r, inst);
+  int nb = 0;
+  for (size_t i = 0; i < inst.size(); ++i) {
+    std::vector<Box> boxes;
+    shape_boxes(inst[i].shape, boxes);
+    for (const Box& B : boxes) {
+      if (nb >= max_boxes) return RTR_ERR_CAPACITY;
+      float* o = h_boxes + 12 * nb;
+      o[0] = (float)cos(inst[i].yaw);
+      o[1] = (float)sin(inst[i].yaw);
+      o[2] = (float)inst[i].x;
+      o[3] = (float)inst[i].y;
+      for (int k = 0; k < 3; ++k) {
+        o[4 + k] = (float)(B.c[k] - B.h[k]);
+        o[7 + k] = (float)(B.c[k] + B.h[k]);
+      }
+      o[10] = (float)inst[i].shape;
+      o[11] = (float)i;
+      ++nb;
+    }
+    if ((int)i < max_instances) {
+      if (h_inst_shape) h_inst_shape[i] = inst[i].shape;
+      if (h_inst_pose16) {
+        const double c = cos(inst[i].yaw), sn = sin(inst[i].yaw);
+        const double M[16] = {c, -sn, 0, inst[i].x, sn, c, 0, inst[i].y, 0, 0, 1, 0, 0, 0, 0, 1};
+        memcpy(h_inst_pose16 + 16 * i, M, sizeof(M));
+      }
+    }
+  }
+  *h_n_boxes = nb;
+  if (h_n_instances) *h_n_instances = (int)inst.size();
+  return RTR_OK;
+}
+
+void rtr_synth_trajectory(uint64_t seed, int n_frames, double fps, double* h_poses16) {
+  Rng r(seed);
+  const double ph1 = 6.283185307179586 * r.uniform(), ph2 = 6.283185307179586 * r.uniform();
+  const double A = 1.2, w1 = 0.5 / A;                          // x sweep, peak speed 0.5 m/s
+  const double Ay = 0.349065850398866, w2 = 0.872664625997165;  // yaw +-20 deg, peak rate 17.5 deg/s
+  const double pitch = -0.436332312998582;                      // 25 deg down
+  for (int f = 0; f < n_frames; ++f) {
+    const double t = f / fps;
+    const double C[3] = {A * sin(w1 * t + ph1), -2.3 + 0.15 * sin(0.3 * t + ph2), 1.5};
+    const double yaw = Ay * sin(w2 * t + ph2);
+    const double fw[3] = {sin(yaw) * cos(pitch), cos(yaw) * cos(pitch), sin(pitch)};
+    double rt[3] = {fw[1], -fw[0], 0.0};  // fw x (0,0,1)
+    const double rn = sqrt(rt[0] * rt[0] + rt[1] * rt[1]);
+    rt[0] /= rn;
+    rt[1] /= rn;
+    const double dn[3] = {fw[1] * rt[2] - fw[2] * rt[1], fw[2] * rt[0] - fw[0] * rt[2], fw[0] * rt[1] - fw[1] * rt[0]};
+    double* T = h_poses16 + 16 * f;  // camera (x right, y down, z forward) -> world
+    for (int k = 0; k < 3; ++k) {
+      T[4 * k + 0] = rt[k];
+      T[4 * k + 1] = dn[k];
+      T[4 * k + 2] = fw[k];
+      T[4 * k + 3] = C[k];
+    }
+    T[12] = T[13] = T[14] = 0.0;
+    T[15] = 1.0;
+  }
+}
 
 rtr_status rtr_synth_shape(int shape, uint64_t seed, int n, float* h_out_xyz4) {
   if (shape < 0 || shape > 2 || n < 0 || (n > 0 && !h_out_xyz4)) return RTR_ERR_INVALID_ARG;
@@ -204,30 +299,8 @@ rtr_status rtr_synth_room(const rtr_room_params* P, uint64_t seed, float* out, i
                           int* inst_shape, double* inst_pose, int* n_instances) {
   if (!P || !out || P->n_points < 0) return RTR_ERR_INVALID_ARG;
   Rng r(seed);
-  // place furniture: largest first, non-overlapping bounding circles
-  struct Inst { int shape; double yaw, x, y; };
   std::vector<Inst> inst;
-  std::vector<int> order;
-  for (int i = 0; i < P->n_sofas; ++i) order.push_back(2);
-  for (int i = 0; i < P->n_desks; ++i) order.push_back(1);
-  for (int i = 0; i < P->n_chairs; ++i) order.push_back(0);
-  for (int sh : order) {
-    const double rad = shape_radius(sh);
-    for (int tries = 0; tries < 2000; ++tries) {
-      const double x = -1.9 + rad * 0.5 + r.uniform() * (3.8 - rad);
-      const double y = -0.6 + r.uniform() * (2.6 - rad * 0.5);
-      const double yaw = 6.283185307179586 * r.uniform();
-      bool ok = x - rad > -2.45 && y + rad < 2.45;
-      for (const Inst& o : inst) {
-        const double dx = x - o.x, dy = y - o.y;
-        if (sqrt(dx * dx + dy * dy) < rad + shape_radius(o.shape) + 0.05) ok = false;
-      }
-      if (ok) {
-        inst.push_back({sh, yaw, x, y});
-        break;
-      }
-    }
-  }
+  place_furniture(P, r, inst);
   std::vector<std::vector<Box>> boxes(inst.size());
   for (size_t i = 0; i < inst.size(); ++i) shape_boxes(inst[i].shape, boxes[i]);
   if (n_instances) *n_instances = (int)inst.size();
