@@ -259,13 +259,19 @@ rtr_status rtr_shot352(rtr_context* ctx, const float* d_pts, const float* d_norm
 /* Descriptor 1-NN on the tensor cores (the all-pairs loop of
  * RealTimeRobot.cpp:73-102, recast as SHOT 1-NN): BF16 (hi + lo split)
  * tcgen05 GEMM with FP32 accumulation, per-query top-8, exact FP32 re-rank and
- * a certified error bound (uncertified queries are re-scanned exactly).  The
- * indices and distances equal rtr_match_exact's bit for bit. */
+ * a certified error bound.  Uncertified queries (near-ties: flat faces give
+ * many near-equal descriptors) take a second GEMM pass that lists every row
+ * within the tie margin, and the exact minimum over that band; a band over
+ * 256 rows falls back to an exact scan of the whole database.  The indices
+ * and distances equal rtr_match_exact's bit for bit. */
 rtr_status rtr_match(rtr_context* ctx, const float* d_query, int n_query, const float* d_db,
                      int n_db, int32_t* d_idx, float* d_d2, rtr_stream_t stream);
 /* Queries of the last tensor-core match whose top-8 could not be certified
  * (re-scanned exactly).  Synchronises the device. */
 rtr_status rtr_match_stats(rtr_context* ctx, int* h_uncertified);
+/* The same, and how many of them needed the exact scan of the whole
+ * database.  Synchronises the device. */
+rtr_status rtr_match_stats_ex(rtr_context* ctx, int* h_uncertified, int* h_full_scans);
 
 /* Exact FP32 1-NN of 352-d descriptors: d^2 = sum over k in order of
  * (a_k - b_k)^2, each op rounded separately, ties to the lowest index. */

@@ -139,6 +139,7 @@ _SIG = {
     "rtr_match_exact": (_I, [_P, _P, _I, _P, _I, _P, _P, _P]),
     "rtr_match": (_I, [_P, _P, _I, _P, _I, _P, _P, _P]),
     "rtr_match_stats": (_I, [_P, C.POINTER(C.c_int)]),
+    "rtr_match_stats_ex": (_I, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "rtr_gc_group": (_I, [_P, _P, _P, _P, _P, _P, _I, _F, _I, _I, _I, _P, _P, _P,
                           C.POINTER(C.c_int), _P]),
     "rtr_gc_stats": (_I, [_P, C.POINTER(C.c_int * 8)]),
@@ -447,6 +448,13 @@ class Context:
         n = C.c_int(0)
         check(lib().rtr_match_stats(self.h, C.byref(n)))
         return n.value
+
+    def match_full_scans(self) -> int:
+        """Uncertified queries of the last match that needed the exact scan
+        of the whole database (band over 256 rows or non-finite values)."""
+        n, f = C.c_int(0), C.c_int(0)
+        check(lib().rtr_match_stats_ex(self.h, C.byref(n), C.byref(f)))
+        return f.value
 
     def match_exact(self, q, db, stream=None):
         import torch

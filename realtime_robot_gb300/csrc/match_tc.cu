@@ -37,6 +37,8 @@ constexpr int TC_BM = 128;
 constexpr int TC_BN = 256;
 constexpr int TC_STAGES = 2;
 constexpr int TC_TOP = 8;
+constexpr int TC_BAND = 256;      // band pass: rows listed per uncertified query
+constexpr int TC_BAND_Q = 16384;  // band pass: uncertified queries it takes (the rest: full scan)
 constexpr int TC_A_BYTES = TC_BM * TC_KB * 2;   // 16 KB
 constexpr int TC_B_BYTES = TC_BN * TC_KB * 2;   // 32 KB
 constexpr int TC_STAGE_BYTES = 2 * TC_A_BYTES + 2 * TC_B_BYTES;  // 96 KB
@@ -177,11 +179,19 @@ struct TcArgs {
   int nq_cap;
   int ndb;
   const float* qn;   // [nq_cap] |q|^2
-  int* cand_idx;     // [nq_cap][8]
+  int* cand_idx;     // [nq_cap][8]; band pass: [nq_cap][TC_BAND] rows within the threshold
   float* cand_d;     // [nq_cap][8]
   int* status;
+  const float* thr;  // band pass: [nq_cap] largest d~ a row may have and still tie the winner
+  int* band_n;       // band pass: [nq_cap] rows within the threshold (may exceed TC_BAND)
 };
 
+// BAND = false: per query the 8 smallest d~ (the first pass).  BAND = true:
+// per query every row with d~ <= thr[q] (the band pass over uncertified
+// queries), the first TC_BAND of them listed, all of them counted in
+// band_n[q] (zeroed by the caller); its grid splits the database into
+// gridDim.y ranges so that a few uncertified queries still fill the GPU.
+template <bool BAND>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constant__ CUtensorMap mq_hi,
                                                             const __grid_constant__ CUtensorMap mq_lo,
                                                             const __grid_constant__ CUtensorMap mb_hi,
@@ -196,7 +206,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constan
   const int nq = a.d_nq ? min(*a.d_nq, a.nq_cap) : a.nq_host;
   const int q0 = blockIdx.x * TC_BM;
   if (q0 >= nq) return;  // uniform per CTA, before any barrier or TMEM use
-  const int n_tiles = (a.ndb + TC_BN - 1) / TC_BN;
+  // database tiles of this CTA: all of them, or (band pass, gridDim.y > 1)
+  // one of gridDim.y contiguous ranges
+  const int n_all = (a.ndb + TC_BN - 1) / TC_BN;
+  const int t_lo = (int)((long long)blockIdx.y * n_all / gridDim.y);
+  const int t_hi = (int)((long long)(blockIdx.y + 1) * n_all / gridDim.y);
 
   if (threadIdx.x == 0) {
     abort_flag = 0;
@@ -224,7 +238,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constan
     // ---------------- TMA producer ----------------
     if (lane == 0) {
       int it = 0;
-      for (int t = 0; t < n_tiles && !*abort; ++t) {
+      for (int t = t_lo; t < t_hi && !*abort; ++t) {
         for (int kb = 0; kb < TC_NKB && !*abort; ++kb, ++it) {
           const int s = it % TC_STAGES;
           const uint32_t ph = (uint32_t)(it / TC_STAGES) & 1u;
@@ -243,10 +257,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constan
     if (lane == 0) {
       const uint32_t idesc = umma_idesc();
       int it = 0;
-      for (int t = 0; t < n_tiles && !*abort; ++t) {
-        const int buf = t & 1;
-        const uint32_t use = (uint32_t)(t >> 1);
-        if (t >= 2 && !mbar_wait(&acc_empty[buf], (use - 1) & 1u, abort)) break;
+      for (int t = t_lo; t < t_hi && !*abort; ++t) {
+        const int buf = (t - t_lo) & 1;
+        const uint32_t use = (uint32_t)((t - t_lo) >> 1);
+        if (t - t_lo >= 2 && !mbar_wait(&acc_empty[buf], (use - 1) & 1u, abort)) break;
         tc_fence_after();
         const uint32_t dcol = tmem + (uint32_t)buf * TC_BN;
         for (int kb = 0; kb < TC_NKB; ++kb, ++it) {
@@ -277,6 +291,36 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constan
     const int row = warp * 32 + lane;
     const int q = q0 + row;
     const float qn = q < nq ? a.qn[q] : 0.f;
+    if (BAND) {
+      // rows past the live queries (stale scratch, any bits) list nothing
+      const bool live = q < nq;
+      const float thr = live ? a.thr[q] : 0.f;
+      int* list = a.cand_idx + (size_t)(live ? q : 0) * TC_BAND;
+      for (int t = t_lo; t < t_hi; ++t) {
+        const int buf = (t - t_lo) & 1;
+        const uint32_t use = (uint32_t)((t - t_lo) >> 1);
+        if (!mbar_wait(&acc_full[buf], use & 1u, abort)) break;
+        tc_fence_after();
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)buf * TC_BN;
+        const int valid = min(TC_BN, a.ndb - t * TC_BN);
+        for (int c0 = 0; c0 < TC_BN; c0 += 32) {
+          float v[32];
+          tmem_ld32(taddr + (uint32_t)c0, v);
+          const int jb = t * TC_BN + c0;
+          const int lim = valid - c0;
+#pragma unroll
+          for (int i = 0; i < 32; ++i) {
+            // d~ exactly as the first pass forms it for its candidates
+            if (live && i < lim && qn - 2.f * v[i] <= thr) {
+              const int pos = atomicAdd(a.band_n + q, 1);  // CTAs of other ranges list into it too
+              if (pos < TC_BAND) list[pos] = jb + i;
+            }
+          }
+        }
+        tc_fence_before();
+        mbar_arrive(&acc_empty[buf]);
+      }
+    } else {
     float ba[TC_TOP];
     int bi[TC_TOP];
 #pragma unroll
@@ -284,9 +328,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constan
       ba[s] = -__int_as_float(0x7f800000);
       bi[s] = 0x7fffffff;
     }
-    for (int t = 0; t < n_tiles; ++t) {
-      const int buf = t & 1;
-      const uint32_t use = (uint32_t)(t >> 1);
+    for (int t = t_lo; t < t_hi; ++t) {
+      const int buf = (t - t_lo) & 1;
+      const uint32_t use = (uint32_t)((t - t_lo) >> 1);
       if (!mbar_wait(&acc_full[buf], use & 1u, abort)) break;
       tc_fence_after();
       const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)buf * TC_BN;
@@ -323,6 +367,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constan
         a.cand_idx[(size_t)q * TC_TOP + s] = bi[s] == 0x7fffffff ? -1 : bi[s];
         a.cand_d[(size_t)q * TC_TOP + s] = bi[s] == 0x7fffffff ? __int_as_float(0x7f800000) : qn - 2.f * ba[s];
       }
+    }
     }
   }
   tc_fence_before();
@@ -373,6 +418,7 @@ __global__ void __launch_bounds__(256) k_rerank(const float* __restrict__ q, int
                                                 int* __restrict__ out_idx, float* __restrict__ out_d2,
                                                 int* __restrict__ redo, int* __restrict__ n_redo,
                                                 unsigned long long* __restrict__ redo_best,
+                                                float* __restrict__ redo_thr,
                                                 const float* __restrict__ qn, const float* __restrict__ db_max) {
   const int nq = d_nq ? min(*d_nq, nq_cap) : nq_host;
   const int lane = threadIdx.x & 31, sub = lane >> 3, l8 = lane & 7;
@@ -408,24 +454,87 @@ __global__ void __launch_bounds__(256) k_rerank(const float* __restrict__ q, int
         const int p = atomicAdd(n_redo, 1);
         redo[p] = i;
         redo_best[p] = ~0ull;
+        // a row that ties or beats the exact winner has d~ <= bd + err; the
+        // band pass lists rows up to twice that margin
+        redo_thr[p] = bd + 2.f * err;
       }
     }
   }
 }
 
-// Exact scan for the uncertified queries: one CTA per (query, 256 database
-// rows), thread per row; the winner is the minimum of (d^2 bits, index)
-// packed in 64 bits (d^2 >= 0, so its bits order like the value).  A row
-// wins only with d^2 < +inf, as in the sequential scan.
+// Band pass, step 1: the first TC_BAND_Q uncertified queries' split rows and
+// norms, gathered into compact arrays (warp per row, 16-byte copies).
+__global__ void k_band_gather(const uint4* __restrict__ qhi, const uint4* __restrict__ qlo,
+                              const float* __restrict__ qn, const int* __restrict__ redo,
+                              const int* __restrict__ n_redo, int cap, uint4* __restrict__ hi2, uint4* __restrict__ lo2,
+                              float* __restrict__ qn2) {
+  const int n = min(*n_redo, cap);
+  constexpr int V = TC_KPAD * 2 / 16;  // uint4 per row
+  const int lane = threadIdx.x & 31;
+  for (int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < n; w += gridDim.x * (blockDim.x >> 5)) {
+    const int i = redo[w];
+    for (int k = lane; k < V; k += 32) {
+      hi2[(size_t)w * V + k] = qhi[(size_t)i * V + k];
+      lo2[(size_t)w * V + k] = qlo[(size_t)i * V + k];
+    }
+    if (lane == 0) qn2[w] = qn[i];
+  }
+}
+
+// Band pass, step 3: exact FP32 distances to the listed rows, warp per
+// query.  The band holds every row that can tie or beat the exact winner, so
+// its exact minimum (lowest index on ties) is the scan's.  Queries past
+// TC_BAND_Q, with a band over TC_BAND rows, or with a non-finite threshold
+// (Inf or NaN values) go to the full scan list.
+template <bool V4>
+__global__ void __launch_bounds__(256) k_band_rerank(const float* __restrict__ q, const float* __restrict__ db,
+                                                     const int* __restrict__ redo, const int* __restrict__ n_redo,
+                                                     const float* __restrict__ thr, const int* __restrict__ band_idx,
+                                                     const int* __restrict__ band_n, int cap, int ndb,
+                                                     unsigned long long* __restrict__ redo_best,
+                                                     int* __restrict__ full, int* __restrict__ n_full) {
+  const int n = *n_redo;
+  const int lane = threadIdx.x & 31;
+  for (int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < n; w += gridDim.x * (blockDim.x >> 5)) {
+    const int cnt = w < cap ? band_n[w] : TC_BAND + 1;
+    if (cnt > TC_BAND || !isfinite(w < cap ? thr[w] : 0.f)) {
+      if (lane == 0) full[atomicAdd(n_full, 1)] = w;
+      continue;
+    }
+    const int i = redo[w];
+    unsigned long long key = ~0ull;
+    for (int m = lane; m < cnt; m += 32) {
+      const int j = band_idx[(size_t)w * TC_BAND + m];
+      if ((unsigned)j >= (unsigned)ndb) continue;  // only after a timed-out band pass (status set)
+      const float d = exact_d2<V4>(q + (size_t)i * TC_DIM, db + (size_t)j * TC_DIM);
+      if (d < __int_as_float(0x7f800000)) {
+        const unsigned long long k2 = ((unsigned long long)__float_as_uint(d) << 32) | (unsigned)j;
+        key = k2 < key ? k2 : key;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long ok = __shfl_xor_sync(0xffffffffu, key, o);
+      key = ok < key ? ok : key;
+    }
+    if (lane == 0) redo_best[w] = key;
+  }
+}
+
+// Exact scan for the queries the band pass could not settle: one CTA per
+// (query, 256 database rows), thread per row; the winner is the minimum of
+// (d^2 bits, index) packed in 64 bits (d^2 >= 0, so its bits order like the
+// value).  A row wins only with d^2 < +inf, as in the sequential scan.
 template <bool V4>
 __global__ void __launch_bounds__(256) k_match_redo(const float* __restrict__ q, const float* __restrict__ db, int ndb,
-                                                    const int* __restrict__ redo, const int* __restrict__ n_redo,
+                                                    const int* __restrict__ redo, const int* __restrict__ full,
+                                                    const int* __restrict__ n_full,
                                                     unsigned long long* __restrict__ redo_best) {
-  const int n = *n_redo;
+  const int n = *n_full;
   const int rblocks = (ndb + 255) >> 8;
   const int lane = threadIdx.x & 31;
   for (long long item = blockIdx.x; item < (long long)n * rblocks; item += gridDim.x) {
-    const int w = (int)(item / rblocks), rb = (int)(item - (long long)w * rblocks);
+    const int w = full[(int)(item / rblocks)], rb = (int)(item % rblocks);
     const int i = redo[w];
     const int j = rb * 256 + threadIdx.x;
     unsigned long long key = ~0ull;
@@ -489,6 +598,9 @@ static bool make_map(CUtensorMap* m, const void* base, int rows, int box_rows) {
 
 size_t match_tc_bf16_bytes(int rows) { return (size_t)rows * TC_KPAD * 2; }
 
+// rows of the band pass (a multiple of TC_BM)
+static int band_rows(int nqp) { return nqp < TC_BAND_Q ? nqp : TC_BAND_Q; }
+
 void match_tc_plan(ScratchPlan& p, int nq_cap, bool with_db, int ndb) {
   const int nqp = ((nq_cap + TC_BM - 1) / TC_BM) * TC_BM;
   p.add<__nv_bfloat16>((size_t)nqp * TC_KPAD);
@@ -504,6 +616,15 @@ void match_tc_plan(ScratchPlan& p, int nq_cap, bool with_db, int ndb) {
   p.add<int>(nqp);
   p.add<unsigned long long>(nqp);
   p.add<int>(4);
+  // band pass
+  const int bq = band_rows(nqp);
+  p.add<float>(nqp);
+  p.add<int>(nqp);
+  p.add<__nv_bfloat16>((size_t)bq * TC_KPAD);
+  p.add<__nv_bfloat16>((size_t)bq * TC_KPAD);
+  p.add<float>(bq);
+  p.add<int>((size_t)bq * TC_BAND);
+  p.add<int>(bq);
 }
 
 // Splits a descriptor database once (the model side keeps the result).
@@ -542,40 +663,70 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
   float* cd = s.take<float>((size_t)nqp * TC_TOP);
   int* redo = s.take<int>(nqp);
   unsigned long long* redo_best = s.take<unsigned long long>(nqp);
-  int* nredo = s.take<int>(4);
-  if (!nredo) return fail(RTR_ERR_CAPACITY, "match_tc: scratch");
+  int* nredo = s.take<int>(4);  // [0] uncertified, [1] left to the full scan
+  const int bq = band_rows(nqp);
+  float* redo_thr = s.take<float>(nqp);
+  int* full = s.take<int>(nqp);
+  __nv_bfloat16* hi2 = s.take<__nv_bfloat16>((size_t)bq * TC_KPAD);
+  __nv_bfloat16* lo2 = s.take<__nv_bfloat16>((size_t)bq * TC_KPAD);
+  float* qn2 = s.take<float>(bq);
+  int* band_idx = s.take<int>((size_t)bq * TC_BAND);
+  int* band_n = s.take<int>(bq);
+  if (!band_n) return fail(RTR_ERR_CAPACITY, "match_tc: scratch");
   int sb = (nqp + 7) / 8;
   if (sb > 152 * 16) sb = 152 * 16;
   k_split_bf16<<<sb, 256, 0, st>>>(q, nq_cap, d_nq, nqp, qhi, qlo, qn, nullptr, false);
-  CUtensorMap m_qh, m_ql, m_bh, m_bl;
+  CUtensorMap m_qh, m_ql, m_bh, m_bl, m_qh2, m_ql2;
   if (!make_map(&m_qh, qhi, nqp, TC_BM) || !make_map(&m_ql, qlo, nqp, TC_BM) || !make_map(&m_bh, db_hi, ndb, TC_BN) ||
-      !make_map(&m_bl, db_lo, ndb, TC_BN))
+      !make_map(&m_bl, db_lo, ndb, TC_BN) || !make_map(&m_qh2, hi2, bq, TC_BM) || !make_map(&m_ql2, lo2, bq, TC_BM))
     return fail(RTR_ERR_CUDA, "match_tc: cuTensorMapEncodeTiled failed");
   const size_t smem = (size_t)TC_STAGES * TC_STAGE_BYTES + 1024;
   // per call: the attribute is per device, and calls may come from several threads
-  RTR_CUDA(cudaFuncSetAttribute(k_match_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  TcArgs a{nq_cap, d_nq, nq_cap, ndb, qn, cidx, cd, ctx->d_status};
+  RTR_CUDA(cudaFuncSetAttribute(k_match_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  RTR_CUDA(cudaFuncSetAttribute(k_match_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  TcArgs a{nq_cap, d_nq, nq_cap, ndb, qn, cidx, cd, ctx->d_status, nullptr, nullptr};
   {
     ProfScope pg(ctx, st, "match_gemm");
-    k_match_tc<<<nqp / TC_BM, TC_THREADS, smem, st>>>(m_qh, m_ql, m_bh, m_bl, a);
+    k_match_tc<false><<<nqp / TC_BM, TC_THREADS, smem, st>>>(m_qh, m_ql, m_bh, m_bl, a);
   }
-  RTR_CUDA(cudaMemsetAsync(nredo, 0, sizeof(int), st));
+  RTR_CUDA(cudaMemsetAsync(nredo, 0, 2 * sizeof(int), st));
   int rb = (nq_cap + 31) / 32;
   if (rb > 152 * 16) rb = 152 * 16;
+  int wb = (nqp + 7) / 8;  // warp per uncertified query
+  if (wb > 152 * 16) wb = 152 * 16;
   const bool v4 = ((reinterpret_cast<uintptr_t>(q) | reinterpret_cast<uintptr_t>(db)) & 15u) == 0;
-  if (v4) {
+  // band pass over the uncertified queries: the GEMM again, listing every
+  // row within the tie margin, then exact distances to those rows only
+  TcArgs ab{bq, nredo, bq, ndb, qn2, band_idx, nullptr, ctx->d_status, redo_thr, band_n};
+  if (v4)
     k_rerank<true><<<rb, 256, 0, st>>>(q, nq_cap, d_nq, nq_cap, db, ndb, cidx, cd, out_idx, out_d2, redo, nredo,
-                                       redo_best, qn, db_n2 + ndb);
-    k_match_redo<true><<<152 * 8, 256, 0, st>>>(q, db, ndb, redo, nredo, redo_best);
-  } else {
+                                       redo_best, redo_thr, qn, db_n2 + ndb);
+  else
     k_rerank<false><<<rb, 256, 0, st>>>(q, nq_cap, d_nq, nq_cap, db, ndb, cidx, cd, out_idx, out_d2, redo, nredo,
-                                        redo_best, qn, db_n2 + ndb);
-    k_match_redo<false><<<152 * 8, 256, 0, st>>>(q, db, ndb, redo, nredo, redo_best);
+                                        redo_best, redo_thr, qn, db_n2 + ndb);
+  k_band_gather<<<(bq + 7) / 8, 256, 0, st>>>(reinterpret_cast<const uint4*>(qhi), reinterpret_cast<const uint4*>(qlo),
+                                              qn, redo, nredo, bq, reinterpret_cast<uint4*>(hi2),
+                                              reinterpret_cast<uint4*>(lo2), qn2);
+  RTR_CUDA(cudaMemsetAsync(band_n, 0, sizeof(int) * bq, st));
+  {
+    ProfScope pb(ctx, st, "match_band");
+    const int n_tiles = (ndb + TC_BN - 1) / TC_BN;
+    const dim3 grid(bq / TC_BM, n_tiles < 8 ? n_tiles : 8);
+    k_match_tc<true><<<grid, TC_THREADS, smem, st>>>(m_qh2, m_ql2, m_bh, m_bl, ab);
+  }
+  if (v4) {
+    k_band_rerank<true><<<wb, 256, 0, st>>>(q, db, redo, nredo, redo_thr, band_idx, band_n, bq, ndb, redo_best, full,
+                                            nredo + 1);
+    k_match_redo<true><<<152 * 8, 256, 0, st>>>(q, db, ndb, redo, full, nredo + 1, redo_best);
+  } else {
+    k_band_rerank<false><<<wb, 256, 0, st>>>(q, db, redo, nredo, redo_thr, band_idx, band_n, bq, ndb, redo_best, full,
+                                             nredo + 1);
+    k_match_redo<false><<<152 * 8, 256, 0, st>>>(q, db, ndb, redo, full, nredo + 1, redo_best);
   }
   k_match_redo_out<<<4, 256, 0, st>>>(redo, nredo, redo_best, out_idx, out_d2);
-  RTR_LAUNCHED(5);
-  // keep the number of uncertified queries for rtr_match_stats
-  RTR_CUDA(cudaMemcpyAsync(ctx->d_status + 8, nredo, sizeof(int), cudaMemcpyDeviceToDevice, st));
+  RTR_LAUNCHED(8);
+  // keep the number of uncertified queries and of full scans for rtr_match_stats
+  RTR_CUDA(cudaMemcpyAsync(ctx->d_status + 8, nredo, 2 * sizeof(int), cudaMemcpyDeviceToDevice, st));
   RTR_CUDA(cudaGetLastError());
   return RTR_OK;
 }
@@ -589,6 +740,17 @@ extern "C" rtr_status rtr_match_stats(rtr_context* ctx, int* h_uncertified) {
   RTR_CUDA(cudaSetDevice(ctx->device));
   RTR_CUDA(cudaDeviceSynchronize());
   RTR_CUDA(cudaMemcpy(h_uncertified, ctx->d_status + 8, sizeof(int), cudaMemcpyDeviceToHost));
+  return RTR_OK;
+}
+
+extern "C" rtr_status rtr_match_stats_ex(rtr_context* ctx, int* h_uncertified, int* h_full_scans) {
+  RTR_CHECK_ARG(ctx && h_uncertified && h_full_scans, "rtr_match_stats_ex: bad arguments");
+  RTR_CUDA(cudaSetDevice(ctx->device));
+  RTR_CUDA(cudaDeviceSynchronize());
+  int h[2];
+  RTR_CUDA(cudaMemcpy(h, ctx->d_status + 8, sizeof(h), cudaMemcpyDeviceToHost));
+  *h_uncertified = h[0];
+  *h_full_scans = h[1];
   return RTR_OK;
 }
 

@@ -80,3 +80,69 @@ def test_match_tc_general_vectors(ctx):
     ri, rd = O.match(q, db)
     assert np.array_equal(idx.cpu().numpy(), ri)
     assert np.array_equal(d2.cpu().numpy(), rd)
+
+
+def _near_tie_db(md, group, n_groups, seed):
+    """n_groups clusters of `group` rows each, equal to a model descriptor up
+    to a 1e-6 perturbation: their distances to a query differ far below the
+    certification margin, so every query near a cluster is uncertified."""
+    rng = np.random.default_rng(seed)
+    base = []
+    for i in rng.permutation(len(md)):  # well-separated cluster centres (d^2 > 0.05)
+        if all(float(((md[i] - b) ** 2).sum()) > 0.05 for b in base):
+            base.append(md[i])
+        if len(base) == n_groups:
+            break
+    base = np.asarray(base, np.float32)
+    db = np.repeat(base, group, axis=0)
+    db = db + np.float32(1e-6) * rng.standard_normal(db.shape).astype(np.float32)
+    perm = rng.permutation(len(db))  # cluster members spread over the database
+    return base, np.ascontiguousarray(db[perm], np.float32)
+
+
+@pytest.mark.parametrize("group,expect_full", [(100, False), (400, True)])
+def test_match_tc_near_tie_bands(ctx, descs, group, expect_full):
+    # clusters up to 256 rows are settled by the band pass; larger ones by
+    # the exact scan of the whole database
+    md, _ = descs
+    base, db = _near_tie_db(md, group, 8, 5 + group)
+    rng = np.random.default_rng(group)
+    q = np.repeat(base, 40, axis=0) + np.float32(1e-3) * rng.standard_normal((320, 352)).astype(np.float32)
+    q = q.astype(np.float32)
+    idx, d2 = ctx.match(_dev(q), _dev(db))
+    unc, full = ctx.match_uncertified(), ctx.match_full_scans()
+    ri, rd = O.match(q, db)
+    assert np.array_equal(idx.cpu().numpy(), ri)
+    assert np.array_equal(d2.cpu().numpy(), rd)
+    assert unc == len(q)
+    assert (full == unc) if expect_full else (full == 0), (unc, full)
+
+
+def test_match_tc_more_uncertified_than_band_rows(ctx, descs):
+    # past 16384 uncertified queries the rest take the full scan
+    md, _ = descs
+    base, db = _near_tie_db(md, 64, 4, 77)
+    rng = np.random.default_rng(3)
+    q = (np.repeat(base, 4200, axis=0) + np.float32(1e-3) * rng.standard_normal((16800, 352))).astype(np.float32)
+    idx, d2 = ctx.match(_dev(q), _dev(db))
+    unc, full = ctx.match_uncertified(), ctx.match_full_scans()
+    ri, rd = O.match(q, db)
+    assert np.array_equal(idx.cpu().numpy(), ri)
+    assert np.array_equal(d2.cpu().numpy(), rd)
+    assert unc == len(q) and full == len(q) - 16384, (unc, full)
+
+
+def test_match_tc_zero_and_nonfinite_queries(ctx, descs):
+    # a zero query ties with every unit-norm row (band = whole database);
+    # Inf or NaN values make the threshold non-finite: both take the full scan
+    md, sd = descs
+    q = sd[:64].copy()
+    q[:8] = 0.0
+    q[8, 5] = np.inf
+    q[9, 7] = np.nan
+    q[10, :] = -np.inf
+    idx, d2 = ctx.match(_dev(q), _dev(md))
+    ri, rd = O.match(q, md)
+    assert np.array_equal(idx.cpu().numpy(), ri)
+    assert np.array_equal(d2.cpu().numpy(), rd, equal_nan=True)
+    assert ctx.match_full_scans() >= 3
