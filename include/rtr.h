@@ -433,6 +433,19 @@ rtr_status rtr_batch_autotune(rtr_context* ctx, const rtr_batch_pair* h_pairs, i
                               const rtr_recog_params* p, const rtr_mlp* mlp, float keep,
                               rtr_recog_result* d_results, int* h_workers, int* h_icp_group);
 
+/* Several models in one scene (the streaming workload's per-frame form):
+ * the scene's stages (voxels, normals, keypoints, descriptors and, with mlp,
+ * learned pruning) run once; each model's matching, grouping, verification
+ * and refinement run on a worker stream ("batch_workers" knob, at most
+ * n_models workers; one worker runs them in turn on `stream`).  Result i
+ * (device, d_results[i]) is rtr_recognize(_learned) of h_models[i], up to the
+ * FP32 rounding of ICP block sums when the workers share the GPU.
+ * Synchronises and reports the workers' status words. */
+rtr_status rtr_recognize_multi(rtr_context* ctx, const rtr_model* const* h_models, int n_models,
+                               const rtr_mlp* mlp, float keep, const float* d_scene, int n,
+                               const rtr_recog_params* p, rtr_recog_result* d_results,
+                               rtr_stream_t stream);
+
 /* Same with a HOST scene and a HOST result (copies in and out). */
 rtr_status rtr_recognize_host(rtr_context* ctx, const rtr_model* model, const float* h_scene, int n,
                               const rtr_recog_params* p, rtr_recog_result* h_result);

@@ -159,6 +159,7 @@ _SIG = {
                                C.POINTER(_P)]),
     "rtr_recognize": (_I, [_P, _P, _P, _I, C.POINTER(RecogParams), _P, _P]),
     "rtr_recognize_learned": (_I, [_P, _P, _P, _F, _P, _I, C.POINTER(RecogParams), _P, _P]),
+    "rtr_recognize_multi": (_I, [_P, _P, _I, _P, _F, _P, _I, C.POINTER(RecogParams), _P, _P]),
     "rtr_recognize_batch": (_I, [_P, _P, _I, C.POINTER(RecogParams), _P, _F, _P]),
     "rtr_batch_graph_create": (_I, [_P, _P, _I, C.POINTER(RecogParams), _P, _F, _P, C.POINTER(_P)]),
     "rtr_batch_graph_launch": (_I, [_P, _P]),
@@ -638,6 +639,23 @@ def recognize_batch(ctx: "Context", models, scenes, params: RecogParams, mlp: "M
     arr = _batch_args(models, scenes)
     check(lib().rtr_recognize_batch(ctx.h, arr, n, C.byref(params), mlp.h if mlp else None, float(keep),
                                     _ptr(results)))
+    return results
+
+
+def recognize_multi(ctx: "Context", models, scene, params: RecogParams, mlp: "Mlp | None" = None,
+                    keep: float = 1.0, results=None, stream=None):
+    """rtr_recognize_multi: every model in one device scene [n, 4], the
+    scene's stages once; returns the device result buffer [n_models,
+    sizeof(rtr_recog_result)]."""
+    import torch
+    n = len(models)
+    if results is None:
+        results = torch.zeros((max(n, 1), C.sizeof(RecogResult)), dtype=torch.uint8, device="cuda")
+    arr = (_P * max(n, 1))()
+    for i, m in enumerate(models):
+        arr[i] = m.h.value if isinstance(m.h, C.c_void_p) else m.h
+    check(lib().rtr_recognize_multi(ctx.h, arr, n, mlp.h if mlp else None, float(keep), _ptr(scene), scene.shape[0],
+                                    C.byref(params), _ptr(results), _stream(stream)))
     return results
 
 

@@ -29,7 +29,7 @@ struct rtr_batch_graph {
 
 namespace rtr {
 
-static rtr_status ensure_workers(rtr_context* ctx, int n) {
+rtr_status batch_ensure_workers(rtr_context* ctx, int n) {
   while ((int)ctx->workers.size() < n) {
     rtr_context* w = nullptr;
     RTR_TRY(rtr_context_create(ctx->device, &w));
@@ -47,7 +47,7 @@ static rtr_status ensure_workers(rtr_context* ctx, int n) {
   return RTR_OK;
 }
 
-static int batch_workers(const rtr_context* ctx, int n_pairs) {
+int batch_worker_count(const rtr_context* ctx, int n_pairs) {
   int w = ctx->tune_batch_workers > 0 ? ctx->tune_batch_workers : 4;
   return w < n_pairs ? w : n_pairs;
 }
@@ -57,7 +57,7 @@ static int batch_workers(const rtr_context* ctx, int n_pairs) {
 static rtr_status enqueue_batch(rtr_context* ctx, const rtr_batch_pair* pairs, int n_pairs, const rtr_recog_params* p,
                                 const rtr_mlp* mlp, float keep, int nw, rtr_recog_result* d_results,
                                 cudaStream_t origin) {
-  RTR_TRY(ensure_workers(ctx, nw));
+  RTR_TRY(batch_ensure_workers(ctx, nw));
   std::vector<int> order((size_t)n_pairs);
   for (int i = 0; i < n_pairs; ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return pairs[a].n > pairs[b].n; });
@@ -82,7 +82,7 @@ static rtr_status enqueue_batch(rtr_context* ctx, const rtr_batch_pair* pairs, i
 }
 
 // Device status words of the workers (timeouts, capacity) after a batch.
-static rtr_status check_workers(rtr_context* ctx, int nw) {
+rtr_status batch_check_workers(rtr_context* ctx, int nw) {
   for (int wi = 0; wi < nw; ++wi) RTR_TRY(rtr_context_check(ctx->workers[wi], ctx->workers[wi]->host_stream));
   RTR_CUDA(cudaSetDevice(ctx->device));
   return RTR_OK;
@@ -112,10 +112,10 @@ rtr_status rtr_recognize_batch(rtr_context* ctx, const rtr_batch_pair* h_pairs, 
   if (n_pairs == 0) return RTR_OK;
   RTR_CUDA(cudaSetDevice(ctx->device));
   RTR_CUDA(cudaDeviceSynchronize());  // inputs written on other streams are complete
-  const int nw = batch_workers(ctx, n_pairs);
+  const int nw = batch_worker_count(ctx, n_pairs);
   RTR_TRY(enqueue_batch(ctx, h_pairs, n_pairs, p, mlp, keep, nw, d_results, ctx->host_stream));
   RTR_CUDA(cudaStreamSynchronize(ctx->host_stream));
-  return check_workers(ctx, nw);
+  return batch_check_workers(ctx, nw);
 }
 
 rtr_status rtr_batch_graph_create(rtr_context* ctx, const rtr_batch_pair* h_pairs, int n_pairs,
@@ -127,7 +127,7 @@ rtr_status rtr_batch_graph_create(rtr_context* ctx, const rtr_batch_pair* h_pair
   RTR_CHECK_ARG(n_pairs > 0, "rtr_batch_graph_create: empty batch");
   // one plain run sizes every worker's scratch for its pairs
   RTR_TRY(rtr_recognize_batch(ctx, h_pairs, n_pairs, p, mlp, keep, d_results));
-  const int nw = batch_workers(ctx, n_pairs);
+  const int nw = batch_worker_count(ctx, n_pairs);
   for (int wi = 0; wi < nw; ++wi)
     RTR_CHECK_ARG(!ctx->workers[wi]->profiling, "rtr_batch_graph_create: profiling is on");
   cudaStream_t origin = ctx->host_stream;

@@ -115,6 +115,13 @@ rtr_status ensure_scratch(rtr_context* ctx, size_t bytes, cudaStream_t stream, S
 
 bool stream_is_capturing(cudaStream_t s);
 
+// Worker contexts of a batch (batch.cu): make sure `n` exist and share the
+// GPU's co-resident blocks; how many a call of `n_items` uses; and their
+// status words after a synchronised batch.
+rtr_status batch_ensure_workers(rtr_context* ctx, int n);
+int batch_worker_count(const rtr_context* ctx, int n_items);
+rtr_status batch_check_workers(rtr_context* ctx, int nw);
+
 // Grow the host-entry staging buffer (synchronises when it grows).
 rtr_status ensure_io(rtr_context* ctx, size_t bytes);
 

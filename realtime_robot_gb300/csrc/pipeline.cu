@@ -456,32 +456,80 @@ rtr_status rtr_model_buffers(const rtr_model* m, const float** d_vox, const floa
 
 namespace rtr {
 
-// Persistent buffers of one recognition (outlive the stages that fill them).
-struct RecogBufs {
-  int* cnt;                 // [0] V, [1] K (uniform), [2] K (gated), [3] C, [4] K (pruned),
-                            // [5] clusters, [6] hypotheses refined
-  float4 *sv, *sn, *skp;
-  int *keys, *keys2, *midx, *cm, *cs;
-  float *desc, *md2, *cd;
+// Scene-side buffers of one recognition: everything that depends on the
+// scene alone, shared by every model recognised in it.
+struct SceneBufs {
+  int* cnt;                 // [0] V, [1] K (uniform), [2] K (gated), [3] K (pruned)
+  float4 *sv, *sn;
+  int *keys, *keys2;
+  float* desc;
+  uint32_t *flags, *pos, *tiles;
+  GridBufs grid;            // scene voxels at the ICP distance (verification, refinement)
+  int* keys_p;              // learned pruning: kept keypoints
+  float* desc_p;            // and their descriptors
+  // what goes on to matching (set by scene_stages)
+  const int* keys_m;
+  const int* d_nk;
+  const float* desc_m;
+};
+
+// Model-side buffers: correspondences, hypotheses, refinement.
+struct ModelBufs {
+  int* cnt;                 // [0] C, [1] clusters, [2] hypotheses refined
+  float4* skp;
+  int *midx, *cm, *cs;
+  float *md2, *cd;
   uint32_t *flags, *pos, *tiles;
   double *poses, *init, *refined;
   int *sizes, *order;
   float *hv, *fscore;
   int* hvcnt;
   rtr_icp_result* res;
-  int* keys_p;              // learned pruning: kept keypoints
-  float* desc_p;            // and their descriptors
-  GridBufs grid;
 };
 
-static void recog_persistent_plan(ScratchPlan& p, int n, const rtr_recog_params* q, bool learned) {
-  const int H = q->max_clusters, M = q->refine_top;
+static void scene_plan(ScratchPlan& p, int n, bool learned) {
   p.add<int>(8);
   p.add<float4>(n);
   p.add<float4>(n);
-  p.add<float4>(n);
-  for (int i = 0; i < 5; ++i) p.add<int>(n);
+  p.add<int>(n);
+  p.add<int>(n);
   p.add<float>((size_t)n * 352);
+  p.add<uint32_t>(n);
+  p.add<uint32_t>(n);
+  p.add<uint32_t>(scan_tiles(n));
+  grid_plan(p, n, default_cell_cap(n));
+  if (learned) {
+    p.add<int>(n);
+    p.add<float>((size_t)n * 352);
+  }
+}
+
+static bool scene_take(Scratch& s, int n, bool learned, SceneBufs* b) {
+  b->cnt = s.take<int>(8);
+  b->sv = s.take<float4>(n);
+  b->sn = s.take<float4>(n);
+  b->keys = s.take<int>(n);
+  b->keys2 = s.take<int>(n);
+  b->desc = s.take<float>((size_t)n * 352);
+  b->flags = s.take<uint32_t>(n);
+  b->pos = s.take<uint32_t>(n);
+  b->tiles = s.take<uint32_t>(scan_tiles(n));
+  if (!b->tiles || !grid_take(s, n, default_cell_cap(n), &b->grid)) return false;
+  b->keys_p = nullptr;
+  b->desc_p = nullptr;
+  if (learned) {
+    b->keys_p = s.take<int>(n);
+    b->desc_p = s.take<float>((size_t)n * 352);
+    return b->desc_p != nullptr;
+  }
+  return true;
+}
+
+static void model_plan(ScratchPlan& p, int n, const rtr_recog_params* q) {
+  const int H = q->max_clusters, M = q->refine_top;
+  p.add<int>(8);
+  p.add<float4>(n);
+  for (int i = 0; i < 3; ++i) p.add<int>(n);
   p.add<float>(n);
   p.add<float>(n);
   p.add<uint32_t>(n);
@@ -496,25 +544,15 @@ static void recog_persistent_plan(ScratchPlan& p, int n, const rtr_recog_params*
   p.add<float>(M);
   p.add<int>(H > M ? H : M);
   p.add<rtr_icp_result>(M);
-  grid_plan(p, n, default_cell_cap(n));
-  if (learned) {
-    p.add<int>(n);
-    p.add<float>((size_t)n * 352);
-  }
 }
 
-static bool recog_take(Scratch& s, int n, const rtr_recog_params* q, bool learned, RecogBufs* b) {
+static bool model_take(Scratch& s, int n, const rtr_recog_params* q, ModelBufs* b) {
   const int H = q->max_clusters, M = q->refine_top;
   b->cnt = s.take<int>(8);
-  b->sv = s.take<float4>(n);
-  b->sn = s.take<float4>(n);
   b->skp = s.take<float4>(n);
-  b->keys = s.take<int>(n);
-  b->keys2 = s.take<int>(n);
   b->midx = s.take<int>(n);
   b->cm = s.take<int>(n);
   b->cs = s.take<int>(n);
-  b->desc = s.take<float>((size_t)n * 352);
   b->md2 = s.take<float>(n);
   b->cd = s.take<float>(n);
   b->flags = s.take<uint32_t>(n);
@@ -529,20 +567,11 @@ static bool recog_take(Scratch& s, int n, const rtr_recog_params* q, bool learne
   b->fscore = s.take<float>(M);
   b->hvcnt = s.take<int>(H > M ? H : M);
   b->res = s.take<rtr_icp_result>(M);
-  if (!b->res || !grid_take(s, n, default_cell_cap(n), &b->grid)) return false;
-  b->keys_p = nullptr;
-  b->desc_p = nullptr;
-  if (learned) {
-    b->keys_p = s.take<int>(n);
-    b->desc_p = s.take<float>((size_t)n * 352);
-    return b->desc_p != nullptr;
-  }
-  return true;
+  return b->res != nullptr;
 }
 
-size_t recognize_scratch_bytes(int n, int n_model_vox, int n_model_kp, const rtr_recog_params* q, bool learned) {
-  ScratchPlan p;
-  recog_persistent_plan(p, n, q, learned);
+// Per-stage scratch: the largest of the stages' own needs.
+static size_t stage_bytes(int n, const rtr_recog_params* q, bool learned) {
   size_t stage = 0;
   if (learned) {
     ScratchPlan t;
@@ -573,24 +602,23 @@ size_t recognize_scratch_bytes(int n, int n_model_vox, int n_model_kp, const rtr
     match_tc_plan(t, n, false, 0);
     stage = t.bytes > stage ? t.bytes : stage;
   }
-  (void)n_model_vox;
-  (void)n_model_kp;
-  return p.bytes + stage + 4096;
+  return stage;
 }
 
-static rtr_status recognize_impl(rtr_context* ctx, const rtr_model* m, const float4* scene, int n,
-                                 const rtr_recog_params* q, rtr_recog_result* out, cudaStream_t st,
-                                 const rtr_mlp* mlp = nullptr, float keep = 1.f) {
-  const bool learned = mlp != nullptr;
-  Scratch s;
-  RTR_TRY(ensure_scratch(ctx, recognize_scratch_bytes(n, m->n_vox, m->n_kp, q, learned), st, &s));
-  RecogBufs b;
-  if (!recog_take(s, n, q, learned, &b)) return fail(RTR_ERR_CAPACITY, "rtr_recognize: scratch carve");
-  const Scratch stage = s;  // everything after this point is per-stage scratch
+size_t recognize_scratch_bytes(int n, const rtr_recog_params* q, bool learned) {
+  ScratchPlan p;
+  scene_plan(p, n, learned);
+  model_plan(p, n, q);
+  return p.bytes + stage_bytes(n, q, learned) + 4096;
+}
+
+// The scene's stages: voxels, normals, keypoints (gated), descriptors,
+// learned pruning, the scene grid at the ICP distance.
+static rtr_status scene_stages(rtr_context* ctx, const Scratch& stage, SceneBufs& b, const float4* scene, int n,
+                               const rtr_recog_params* q, const rtr_mlp* mlp, float keep, cudaStream_t st) {
   int* dV = b.cnt;
   int* dK = b.cnt + 1;
   int* dKg = b.cnt + 2;
-  int* dC = b.cnt + 3;
   const int nb = nblocks(n);
   {
     ProfScope ps(ctx, st, "voxel_downsample");
@@ -628,7 +656,7 @@ static rtr_status recognize_impl(rtr_context* ctx, const rtr_model* m, const flo
     RTR_TRY(shot_dev(ctx, t, b.sv, b.sn, n, dV, keys, n, dKeys, q->descriptor_r, b.desc, nullptr, st));
   }
   const float* desc = b.desc;
-  if (learned) {
+  if (mlp) {
     // learned pruning: keep the ceil(keep * K) most credible keypoints (ties:
     // lower keypoint index), in their original order
     ProfScope ps(ctx, st, "prune");
@@ -645,33 +673,51 @@ static rtr_status recognize_impl(rtr_context* ctx, const rtr_model* m, const flo
     uint32_t *ks, *vs;
     radix_sort_pairs(k0, v0, k1, v1, hist, n, n, dKeys, 32, true, st, &ks, &vs);
     k_mark_top<<<nb, 256, 0, st>>>(vs, dKeys, n, keep, b.flags);
-    scan_exclusive(b.flags, b.pos, b.tiles, n, n, nullptr, reinterpret_cast<uint32_t*>(b.cnt + 4), st);
+    scan_exclusive(b.flags, b.pos, b.tiles, n, n, nullptr, reinterpret_cast<uint32_t*>(b.cnt + 3), st);
     k_compact_int<<<nb, 256, 0, st>>>(keys, b.flags, b.pos, n, b.keys_p);
     k_compact_rows<<<nblocks(n, 8, 152 * 16), 256, 0, st>>>(b.desc, b.flags, b.pos, dKeys, n, b.desc_p);
     RTR_LAUNCHED(4);
     keys = b.keys_p;
-    dKeys = b.cnt + 4;
+    dKeys = b.cnt + 3;
     desc = b.desc_p;
   }
   {
+    ProfScope ps(ctx, st, "scene_grid");
+    grid_build(b.grid, b.sv, n, dV, q->icp_max_dist, st);
+  }
+  b.keys_m = keys;
+  b.d_nk = dKeys;
+  b.desc_m = desc;
+  RTR_CUDA(cudaGetLastError());
+  return RTR_OK;
+}
+
+// One model against a scene whose stages are done: matching,
+// correspondences, grouping, verification, ICP refinement, final scoring.
+// Every count stays on the device (no host round trip): the stages are sized
+// for their capacities (n correspondences, max_clusters hypotheses,
+// refine_top refinements) and read the live counts.
+static rtr_status model_stages(rtr_context* ctx, const Scratch& stage, const SceneBufs& sb, ModelBufs& b,
+                               const rtr_model* m, int n, const rtr_recog_params* q, rtr_recog_result* out,
+                               cudaStream_t st) {
+  int* dC = b.cnt;
+  int* dNcl = b.cnt + 1;
+  int* dM = b.cnt + 2;
+  const int nb = nblocks(n);
+  {
     ProfScope ps(ctx, st, "match");
     Scratch t = stage;
-    RTR_TRY(match_tc_dev(ctx, t, desc, n, dKeys, m->desc, m->n_kp, m->db_hi, m->db_lo, m->db_n2, b.midx, b.md2,
-                         st));
+    RTR_TRY(match_tc_dev(ctx, t, sb.desc_m, n, sb.d_nk, m->desc, m->n_kp, m->db_hi, m->db_lo, m->db_n2, b.midx,
+                         b.md2, st));
   }
   {
     ProfScope ps(ctx, st, "correspondences");
-    k_corr_flags<<<nb, 256, 0, st>>>(b.midx, b.md2, dKeys, n, q->match_max_d2, b.flags);
+    k_corr_flags<<<nb, 256, 0, st>>>(b.midx, b.md2, sb.d_nk, n, q->match_max_d2, b.flags);
     scan_exclusive(b.flags, b.pos, b.tiles, n, n, nullptr, reinterpret_cast<uint32_t*>(dC), st);
     k_corr_scatter<<<nb, 256, 0, st>>>(b.midx, b.md2, b.flags, b.pos, n, b.cm, b.cs, b.cd);
-    k_gather_kp<<<nb, 256, 0, st>>>(b.sv, keys, dKeys, n, b.skp);
+    k_gather_kp<<<nb, 256, 0, st>>>(sb.sv, sb.keys_m, sb.d_nk, n, b.skp);
     RTR_LAUNCHED(3);
   }
-  // From here on every count stays on the device (no host round trip): the
-  // stages are sized for their capacities (n correspondences, max_clusters
-  // hypotheses, refine_top refinements) and read the live counts.
-  int* dNcl = b.cnt + 5;
-  int* dM = b.cnt + 6;
   {
     ProfScope ps(ctx, st, "gc_group");
     Scratch t = stage;
@@ -682,8 +728,7 @@ static rtr_status recognize_impl(rtr_context* ctx, const rtr_model* m, const flo
   const int H = q->max_clusters, M = q->refine_top;
   {
     ProfScope ps(ctx, st, "verify");
-    grid_build(b.grid, b.sv, n, dV, q->icp_max_dist, st);
-    RTR_TRY(hv_score(grid_dev(b.grid), m->vox, m->n_vox, q->hv_subsample > 0 ? q->hv_subsample : 1, b.poses, H,
+    RTR_TRY(hv_score(grid_dev(sb.grid), m->vox, m->n_vox, q->hv_subsample > 0 ? q->hv_subsample : 1, b.poses, H,
                      dNcl, q->hv_inlier_r * q->hv_inlier_r, b.hvcnt, b.hv, st));
     k_topm<<<1, 32, 0, st>>>(b.hv, H, dNcl, M, b.order, dM);
     k_select_poses<<<1, 256, 0, st>>>(b.poses, b.order, M, b.init);
@@ -696,7 +741,7 @@ static rtr_status recognize_impl(rtr_context* ctx, const rtr_model* m, const flo
     for (int k = 0; k < M; ++k) {
       IcpDev& d = specs[k].dev;
       memset(&d, 0, sizeof(d));
-      d.grid = grid_dev(b.grid);
+      d.grid = grid_dev(sb.grid);
       d.src_meta = m->vox_meta;
       d.src = m->vox;
       d.src_idx = nullptr;
@@ -716,14 +761,81 @@ static rtr_status recognize_impl(rtr_context* ctx, const rtr_model* m, const flo
   {
     ProfScope ps(ctx, st, "final_score");
     k_copy_result_poses<<<1, 256, 0, st>>>(b.res, M, b.refined);
-    RTR_TRY(hv_score(grid_dev(b.grid), m->vox, m->n_vox, 1, b.refined, M, dM,
+    RTR_TRY(hv_score(grid_dev(sb.grid), m->vox, m->n_vox, 1, b.refined, M, dM,
                      q->accept_inlier_r * q->accept_inlier_r, b.hvcnt, b.fscore, st));
     const float nms2 = q->nms_dist * q->nms_dist;
     k_finalize<<<1, 32, 0, st>>>(b.fscore, b.refined, b.order, b.sizes, M, dM, q->accept_score, nms2,
-                                 q->max_instances, dV, dKeys, dC, dNcl, ctx->d_status, out);
+                                 q->max_instances, sb.cnt, sb.d_nk, dC, dNcl, ctx->d_status, out);
     RTR_LAUNCHED(2);
   }
   RTR_CUDA(cudaGetLastError());
+  return RTR_OK;
+}
+
+static rtr_status recognize_impl(rtr_context* ctx, const rtr_model* m, const float4* scene, int n,
+                                 const rtr_recog_params* q, rtr_recog_result* out, cudaStream_t st,
+                                 const rtr_mlp* mlp = nullptr, float keep = 1.f) {
+  const bool learned = mlp != nullptr;
+  Scratch s;
+  RTR_TRY(ensure_scratch(ctx, recognize_scratch_bytes(n, q, learned), st, &s));
+  SceneBufs sb;
+  ModelBufs mb;
+  if (!scene_take(s, n, learned, &sb) || !model_take(s, n, q, &mb))
+    return fail(RTR_ERR_CAPACITY, "rtr_recognize: scratch carve");
+  const Scratch stage = s;  // everything after this point is per-stage scratch
+  RTR_TRY(scene_stages(ctx, stage, sb, scene, n, q, mlp, keep, st));
+  return model_stages(ctx, stage, sb, mb, m, n, q, out, st);
+}
+
+// Several models in one scene: the scene's stages once on the caller's
+// stream, then each model's stages on a worker's stream (forked and joined
+// with events), or all on the caller's stream with one worker.
+static rtr_status recognize_multi_impl(rtr_context* ctx, const rtr_model* const* models, int nm, const float4* scene,
+                                       int n, const rtr_recog_params* q, const rtr_mlp* mlp, float keep,
+                                       rtr_recog_result* out, int nw, cudaStream_t st) {
+  const bool learned = mlp != nullptr;
+  const size_t stage_b = stage_bytes(n, q, learned);
+  ScratchPlan sp;
+  scene_plan(sp, n, learned);
+  if (nw <= 1) model_plan(sp, n, q);
+  Scratch s;
+  RTR_TRY(ensure_scratch(ctx, sp.bytes + stage_b + 4096, st, &s));
+  SceneBufs sb;
+  if (!scene_take(s, n, learned, &sb)) return fail(RTR_ERR_CAPACITY, "rtr_recognize_multi: scratch carve");
+  if (nw <= 1) {
+    ModelBufs mb;
+    if (!model_take(s, n, q, &mb)) return fail(RTR_ERR_CAPACITY, "rtr_recognize_multi: scratch carve");
+    const Scratch stage = s;
+    RTR_TRY(scene_stages(ctx, stage, sb, scene, n, q, mlp, keep, st));
+    for (int i = 0; i < nm; ++i) RTR_TRY(model_stages(ctx, stage, sb, mb, models[i], n, q, out + i, st));
+    return RTR_OK;
+  }
+  RTR_TRY(scene_stages(ctx, s, sb, scene, n, q, mlp, keep, st));
+  RTR_TRY(batch_ensure_workers(ctx, nw));
+  ScratchPlan mp;
+  model_plan(mp, n, q);
+  for (int wi = 0; wi < nw; ++wi) {  // sized before the fork: growing synchronises
+    Scratch ws;
+    RTR_TRY(ensure_scratch(ctx->workers[wi], mp.bytes + stage_b + 4096, ctx->workers[wi]->host_stream, &ws));
+  }
+  RTR_CUDA(cudaSetDevice(ctx->device));
+  RTR_CUDA(cudaEventRecord(ctx->ev_fork, st));
+  for (int wi = 0; wi < nw; ++wi) RTR_CUDA(cudaStreamWaitEvent(ctx->workers[wi]->host_stream, ctx->ev_fork, 0));
+  for (int i = 0; i < nm; ++i) {
+    rtr_context* w = ctx->workers[i % nw];
+    Scratch ws;
+    RTR_TRY(ensure_scratch(w, mp.bytes + stage_b + 4096, w->host_stream, &ws));
+    ModelBufs mb;
+    if (!model_take(ws, n, q, &mb)) return fail(RTR_ERR_CAPACITY, "rtr_recognize_multi: scratch carve");
+    const rtr_status r = model_stages(w, ws, sb, mb, models[i], n, q, out + i, w->host_stream);
+    if (r != RTR_OK) return fail(r, "rtr_recognize_multi: model %d: %s", i, rtr_last_error());
+  }
+  for (int wi = 0; wi < nw; ++wi) {
+    rtr_context* w = ctx->workers[wi];
+    RTR_CUDA(cudaEventRecord(w->ev_fork, w->host_stream));
+    RTR_CUDA(cudaStreamWaitEvent(st, w->ev_fork, 0));
+  }
+  RTR_CUDA(cudaSetDevice(ctx->device));
   return RTR_OK;
 }
 
@@ -767,6 +879,35 @@ rtr_status rtr_recognize_learned(rtr_context* ctx, const rtr_model* model, const
     return RTR_OK;
   }
   return recognize_impl(ctx, model, reinterpret_cast<const float4*>(d_scene), n, p, d_result, st, mlp, keep);
+}
+
+rtr_status rtr_recognize_multi(rtr_context* ctx, const rtr_model* const* h_models, int n_models, const rtr_mlp* mlp,
+                               float keep, const float* d_scene, int n, const rtr_recog_params* p,
+                               rtr_recog_result* d_results, rtr_stream_t stream) {
+  RTR_CHECK_ARG(ctx && p && n >= 0 && n_models >= 0 && (n_models == 0 || (h_models && d_results)),
+                "rtr_recognize_multi: bad arguments");
+  for (int i = 0; i < n_models; ++i) RTR_CHECK_ARG(h_models[i], "rtr_recognize_multi: model %d is NULL", i);
+  RTR_CHECK_ARG(!mlp || (keep > 0.f && keep <= 1.f), "rtr_recognize_multi: keep must be in (0, 1]");
+  RTR_CHECK_ARG(n == 0 || d_scene, "rtr_recognize_multi: NULL scene");
+  RTR_CHECK_ARG(p->max_clusters >= 1 && p->max_clusters <= 256 && p->refine_top >= 1 && p->refine_top <= 64 &&
+                    p->max_instances >= 1 && p->max_instances <= RTR_MAX_INSTANCES && p->voxel_leaf > 0.f &&
+                    p->descriptor_r > 0.f && p->scene_keypoint_r > 0.f && p->icp_iterations >= 1,
+                "rtr_recognize_multi: parameter out of range");
+  RTR_CHECK_ARG(((uintptr_t)d_scene & 15) == 0, "rtr_recognize_multi: scene must be 16-byte aligned");
+  if (n_models == 0) return RTR_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  RTR_CUDA(cudaSetDevice(ctx->device));
+  if (n == 0) {
+    RTR_CUDA(cudaMemsetAsync(d_results, 0, sizeof(rtr_recog_result) * (size_t)n_models, st));
+    RTR_CUDA(cudaStreamSynchronize(st));
+    return RTR_OK;
+  }
+  const int nw = batch_worker_count(ctx, n_models);
+  RTR_TRY(recognize_multi_impl(ctx, h_models, n_models, reinterpret_cast<const float4*>(d_scene), n, p, mlp, keep,
+                               d_results, nw, st));
+  RTR_CUDA(cudaStreamSynchronize(st));
+  RTR_TRY(rtr_context_check(ctx, st));
+  return nw > 1 ? batch_check_workers(ctx, nw) : RTR_OK;
 }
 
 rtr_status rtr_recognize_host(rtr_context* ctx, const rtr_model* model, const float* h_scene, int n,

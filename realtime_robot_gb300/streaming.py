@@ -12,7 +12,7 @@ import time
 
 import numpy as np
 
-from . import FusionMap, parse_recog_result, recog_default_params, recognize_batch
+from . import FusionMap, parse_recog_result, recog_default_params, recognize_multi
 
 FX, FY, CX, CY = 525.0, 525.0, 319.5, 239.5
 
@@ -63,8 +63,9 @@ class StreamPipeline:
             self.vel = T
             self.pose = self.pose @ T
         self.prev = cloud
-        scenes = [cloud] * len(self.models)
-        out = recognize_batch(ctx, self.models, scenes, self.params, mlp=self.mlp, keep=self.keep if self.mlp else 1.0,
+        # every model class in this frame: the scene's stages once, the
+        # models' stages side by side on worker streams
+        out = recognize_multi(ctx, self.models, cloud, self.params, mlp=self.mlp, keep=self.keep if self.mlp else 1.0,
                               results=self.results)
         self.results = out
         wpts, wcnt = ctx.depth_to_points(depth, FX, FY, CX, CY, pose=self.pose)

@@ -110,3 +110,43 @@ def test_single_recognition_captured_in_a_graph(ctx, rtr, batch):
     g.replay()
     torch.cuda.synchronize()
     assert res.cpu().numpy().tobytes() == ref
+
+
+@pytest.mark.parametrize("workers", [1, 3])
+def test_multi_model_one_scene_equals_single_calls(ctx, rtr, batch, workers):
+    # rtr_recognize_multi: the scene's stages once, every model on it; one
+    # worker runs the models in turn on the caller's stream (bit-identical),
+    # several share the GPU (ICP block sums may round differently)
+    prm, mods, scenes = batch
+    uniq = list({id(m): m for m in mods}.values())
+    scene = scenes[0]
+    ctx.set_tuning("batch_workers", workers)
+    got = _rows(rtr.recognize_multi(ctx, uniq, scene, prm))
+    ctx.set_tuning("batch_workers", 0)
+    for i, m in enumerate(uniq):
+        ref = rtr.recognize(ctx, m, scene, prm).cpu().numpy().tobytes()
+        if workers == 1:
+            assert got[i] == ref
+        else:
+            _same(rtr, got[i], ref)
+
+
+def test_multi_model_learned_equals_single_calls(ctx, rtr, batch):
+    prm, mods, scenes = batch
+    uniq = list({id(m): m for m in mods}.values())
+    mlp = rtr.Mlp(ctx, seed=9)
+    for scene in scenes[:3]:
+        got = _rows(rtr.recognize_multi(ctx, uniq, scene, prm, mlp=mlp, keep=0.5))
+        for i, m in enumerate(uniq):
+            ref = rtr.recognize_learned(ctx, m, mlp, scene, keep=0.5, params=prm).cpu().numpy().tobytes()
+            _same(rtr, got[i], ref)
+
+
+def test_multi_model_edge_cases(ctx, rtr, batch):
+    import torch
+    prm, mods, _ = batch
+    rtr.recognize_multi(ctx, [], torch.zeros((0, 4), device="cuda"), prm)
+    res = rtr.recognize_multi(ctx, mods[:2], torch.zeros((0, 4), device="cuda"), prm)
+    for r in _rows(res):
+        d = rtr.parse_recog_result(r)
+        assert d["n_voxels"] == 0 and d["instances"] == []
