@@ -209,6 +209,14 @@ rtr_status rtr_icp_host(rtr_context* ctx, const float* h_src, int n_src,
                         const float* h_tgt, int n_tgt, const rtr_icp_params* params,
                         const double* h_init_pose, rtr_icp_result* h_result);
 
+/* Where the last ICP launch of the context spent its time (first problem of
+ * the launch, summed over iterations, nanoseconds): [0] block 0's search and
+ * block sums, [1] the last-arriving block's serial section (cross-block
+ * reduction, pose solve, release), [2] block 0's wait for the release, [3]
+ * iterations, [4] and [5] the serial section up to the end of its
+ * cross-block reduction and of its pose solve.  Synchronises. */
+rtr_status rtr_icp_stats(rtr_context* ctx, long long* h_stats6);
+
 /* ---- recognition stages --------------------------------------------------
  * The reference computes these inside ModelPoint/ScanPoint::getKeypoint
  * (model_point.h:99-156, scan_point.h:57-113: PCL normals + keypoints) and

@@ -139,6 +139,7 @@ _SIG = {
     "rtr_match_exact": (_I, [_P, _P, _I, _P, _I, _P, _P, _P]),
     "rtr_match": (_I, [_P, _P, _I, _P, _I, _P, _P, _P]),
     "rtr_match_stats": (_I, [_P, C.POINTER(C.c_int)]),
+    "rtr_icp_stats": (_I, [_P, _P]),
     "rtr_match_stats_ex": (_I, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "rtr_gc_group": (_I, [_P, _P, _P, _P, _P, _P, _I, _F, _I, _I, _I, _P, _P, _P,
                           C.POINTER(C.c_int), _P]),
@@ -464,6 +465,13 @@ class Context:
         check(lib().rtr_match_exact(self.h, _ptr(q), q.shape[0], _ptr(db), db.shape[0], _ptr(idx),
                                     _ptr(d2), _stream(stream)))
         return idx, d2
+
+    def icp_stats(self) -> dict:
+        """Time of the last ICP launch (first problem), summed over iterations."""
+        v = (C.c_longlong * 6)()
+        check(lib().rtr_icp_stats(self.h, v))
+        return {"search_ns": v[0], "serial_ns": v[1], "wait_ns": v[2], "iterations": v[3],
+                "serial_reduce_ns": v[4], "serial_solve_ns": v[5]}
 
     def gc_stats(self) -> dict:
         """Work of the last grouping: rounds, walk end position, sets computed,

@@ -26,6 +26,12 @@ constexpr int ICP_WARPS = ICP_THREADS / 32;
 constexpr int ICP_NV = 16;  // dp(3) dq(3) dp*dq^T(9) d^2(1)
 
 
+__device__ __forceinline__ unsigned long long icp_timer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 __device__ __forceinline__ float centre_of(const GridMeta* m, int a) {
   return 0.5f * (ordered_to_float(m->bmin[a]) + ordered_to_float(m->bmax[a]));
 }
@@ -41,8 +47,6 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(const IcpDev* __restrict__ 
   __shared__ float s_red[ICP_WARPS][ICP_NV][2];
   __shared__ int s_cnt[ICP_WARPS];
   __shared__ double s_sum[ICP_NV];
-  __shared__ float s_wsum[ICP_WARPS][ICP_NV][2];
-  __shared__ int s_wn[ICP_WARPS];
   __shared__ double s_P[16], s_D[16], s_H[9];
   __shared__ long long s_n;
   __shared__ int s_last, s_stop;
@@ -66,11 +70,15 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(const IcpDev* __restrict__ 
   const float c[3] = {centre_of(a.grid.meta, 0), centre_of(a.grid.meta, 1), centre_of(a.grid.meta, 2)};
   const float4 cs = make_float4(centre_of(a.src_meta, 0), centre_of(a.src_meta, 1), centre_of(a.src_meta, 2), 0.f);
   constexpr int QPB = ICP_THREADS / G;  // source points per block per pass
+  constexpr int NVL = ICP_NV / G;        // sums kept per lane
   const unsigned stride = (unsigned)B * QPB;
   const int lg = lane & (G - 1);
   const unsigned gmask = ((1u << G) - 1u) << (lane & ~(G - 1));
 
+  const bool prof0 = a.prof != nullptr && lb == 0 && tid == 0;
+  unsigned long long t_it = 0, t_arr = 0;
   for (int it = 0; it < a.max_it; ++it) {
+    if (prof0) t_it = icp_timer();
     float T[12];
     if (it == 0) {
 #pragma unroll
@@ -80,45 +88,62 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(const IcpDev* __restrict__ 
       for (int k = 0; k < 12; ++k) T[k] = __ldcg(a.posef + k);
     }
     const float4 cp = xform_exact(T, cs);
-    KSum acc[ICP_NV];
+    // The G lanes of a group share the 16 sums of their points: lane lg keeps
+    // values lg*NVL .. lg*NVL+NVL-1 (dp 0-2, dq 3-5, dp dq^T 6-14, d^2 15),
+    // each over the group's points in order, as one lane holding all 16 would.
+    KSum acc[NVL];
 #pragma unroll
-    for (int v = 0; v < ICP_NV; ++v) acc[v].init();
+    for (int k = 0; k < NVL; ++k) acc[k].init();
     int cnt = 0;
     for (unsigned i = (unsigned)lb * QPB + tid / G; i < (unsigned)a.n_src; i += stride) {
       const float4 p = xform_exact(T, a.src[i]);
       float d2;
       int j, pos;
-      grid_nn1_group<G, true>(g, p, a.r2max, lg, gmask, d2, j, pos);
-      if (lg != 0) continue;
+      grid_nn1_group<G, true>(g, p, a.r2max, lg, gmask, d2, j, pos);  // the group agrees on (d2, j, pos)
       if (j >= 0) {
         const float4 q = g.pts[pos];
         const float dp[3] = {__fsub_rn(p.x, cp.x), __fsub_rn(p.y, cp.y), __fsub_rn(p.z, cp.z)};
         const float dq[3] = {__fsub_rn(q.x, c[0]), __fsub_rn(q.y, c[1]), __fsub_rn(q.z, c[2])};
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          acc[k].add(dp[k]);
-          acc[3 + k].add(dq[k]);
+        for (int k = 0; k < NVL; ++k) {
+          const int v = lg * NVL + k;
+          float x;
+          if (v < 3)
+            x = v == 0 ? dp[0] : (v == 1 ? dp[1] : dp[2]);
+          else if (v < 6)
+            x = v == 3 ? dq[0] : (v == 4 ? dq[1] : dq[2]);
+          else if (v < 15) {
+            const int r = (v - 6) / 3, kk = (v - 6) % 3;
+            x = __fmul_rn(r == 0 ? dp[0] : (r == 1 ? dp[1] : dp[2]), kk == 0 ? dq[0] : (kk == 1 ? dq[1] : dq[2]));
+          } else
+            x = d2;
+          acc[k].add(x);
         }
-#pragma unroll
-        for (int r = 0; r < 3; ++r)
-#pragma unroll
-          for (int k = 0; k < 3; ++k) acc[6 + r * 3 + k].add(__fmul_rn(dp[r], dq[k]));
-        acc[15].add(d2);
         ++cnt;
       }
-      if (a.trace_corr)
+      if (a.trace_corr && lg == 0)
         a.trace_corr[(size_t)it * (size_t)a.n_src + (size_t)(a.src_idx ? a.src_idx[i] : (int)i)] = j;
     }
-    // block partial: compensated warp sums, then across warps
+    // block partial: compensated sums over the warp's groups (offsets >= G,
+    // the same tree a single lane per group would meet), then across warps
 #pragma unroll
-    for (int v = 0; v < ICP_NV; ++v) {
-      float s = acc[v].s, cc = acc[v].c;
-      warp_ksum(s, cc);
-      if (lane == 0) {
-        s_red[warp][v][0] = s;
-        s_red[warp][v][1] = cc;
+    for (int k = 0; k < NVL; ++k) {
+      float s = acc[k].s, cc = acc[k].c;
+#pragma unroll
+      for (int off = 16; off >= G; off >>= 1) {
+        const float s2 = __shfl_down_sync(0xffffffffu, s, off);
+        const float c2 = __shfl_down_sync(0xffffffffu, cc, off);
+        float t, e;
+        two_sum(s, s2, t, e);
+        s = t;
+        cc = __fadd_rn(__fadd_rn(cc, c2), e);
+      }
+      if (lane < G) {
+        s_red[warp][lane * NVL + k][0] = s;
+        s_red[warp][lane * NVL + k][1] = cc;
       }
     }
+    cnt = lg == 0 ? cnt : 0;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
     if (lane == 0) s_cnt[warp] = cnt;
@@ -141,12 +166,17 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(const IcpDev* __restrict__ 
     }
     __syncthreads();
     if (tid == 0) {
+      if (prof0) {
+        t_arr = icp_timer();
+        atomicAdd(a.prof + 0, t_arr - t_it);
+      }
       __threadfence();
       const unsigned t = atomicAdd(a.arrive, 1u);
       s_last = (t == (unsigned)(it + 1) * (unsigned)B - 1u) ? 1 : 0;
     }
     __syncthreads();
     if (s_last) {
+      const unsigned long long t_s0 = a.prof && tid == 0 ? icp_timer() : 0ull;
       __threadfence();
       // current pose (FP64) fetched early, used after the solve
       if (tid < 16) {
@@ -157,57 +187,37 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(const IcpDev* __restrict__ 
       // Cross-block reduction.  GB300 issues one FP64 warp-instruction per ~16
       // SM cycles, so the tree runs on compensated FP32 pairs (TwoSum, ~48-bit
       // significand) and FP64 closes it: one (double)hi + (double)lo per value.
-      float hs[ICP_NV], ls[ICP_NV];
-#pragma unroll
-      for (int k = 0; k < ICP_NV; ++k) hs[k] = ls[k] = 0.f;
-      int nloc = 0;
-      for (int b = tid; b < B; b += ICP_THREADS) {
-        const float4* pb = reinterpret_cast<const float4*>(a.partial + b * 32);
-        float4 h4[4], l4[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          h4[k] = __ldcg(pb + k);
-          l4[k] = __ldcg(pb + 4 + k);
-        }
-        nloc += __ldcg(a.pcount + b);
-        const float* hv = reinterpret_cast<const float*>(h4);
-        const float* lv = reinterpret_cast<const float*>(l4);
-#pragma unroll
-        for (int k = 0; k < ICP_NV; ++k) {
+      // Warp w reduces values 2w and 2w + 1 (lanes stride over the blocks in
+      // a fixed order), so no thread holds all sixteen pairs.
+      static_assert(ICP_WARPS * 2 == ICP_NV, "two values per warp");
+      {
+        float hs0 = 0.f, ls0 = 0.f, hs1 = 0.f, ls1 = 0.f;
+        int nloc = 0;
+        const int v0 = 2 * warp;
+        for (int b = lane; b < B; b += 32) {
+          const float2 h = __ldcg(reinterpret_cast<const float2*>(a.partial + b * 32 + v0));
+          const float2 l = __ldcg(reinterpret_cast<const float2*>(a.partial + b * 32 + 16 + v0));
+          if (warp == 0) nloc += __ldcg(a.pcount + b);
           float t, e;
-          two_sum(hs[k], hv[k], t, e);
-          hs[k] = t;
-          ls[k] = __fadd_rn(__fadd_rn(ls[k], lv[k]), e);
+          two_sum(hs0, h.x, t, e);
+          hs0 = t;
+          ls0 = __fadd_rn(__fadd_rn(ls0, l.x), e);
+          two_sum(hs1, h.y, t, e);
+          hs1 = t;
+          ls1 = __fadd_rn(__fadd_rn(ls1, l.y), e);
         }
-      }
+        warp_ksum(hs0, ls0);
+        warp_ksum(hs1, ls1);
 #pragma unroll
-      for (int k = 0; k < ICP_NV; ++k) warp_ksum(hs[k], ls[k]);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) nloc += __shfl_down_sync(0xffffffffu, nloc, o);
-      if (lane == 0) {
-#pragma unroll
-        for (int k = 0; k < ICP_NV; ++k) {
-          s_wsum[warp][k][0] = hs[k];
-          s_wsum[warp][k][1] = ls[k];
+        for (int o = 16; o > 0; o >>= 1) nloc += __shfl_down_sync(0xffffffffu, nloc, o);
+        if (lane == 0) {
+          s_sum[v0] = (double)hs0 + (double)ls0;
+          s_sum[v0 + 1] = (double)hs1 + (double)ls1;
+          if (warp == 0) s_n = nloc;
         }
-        s_wn[warp] = nloc;
       }
       __syncthreads();
-      if (tid < ICP_NV) {
-        float s = s_wsum[0][tid][0], c = s_wsum[0][tid][1];
-        for (int w = 1; w < ICP_WARPS; ++w) {
-          float t, e;
-          two_sum(s, s_wsum[w][tid][0], t, e);
-          s = t;
-          c = __fadd_rn(__fadd_rn(c, s_wsum[w][tid][1]), e);
-        }
-        s_sum[tid] = (double)s + (double)c;
-      } else if (tid == 32) {
-        long long n = 0;
-        for (int w = 0; w < ICP_WARPS; ++w) n += s_wn[w];
-        s_n = n;
-      }
-      __syncthreads();
+      if (a.prof && tid == 0) atomicAdd(a.prof + 4, icp_timer() - t_s0);
       // centred cross-covariance, one element per lane
       if (tid < 9 && s_n >= 3) {
         const double inv = 1.0 / (double)s_n;
@@ -258,6 +268,7 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(const IcpDev* __restrict__ 
         a.result->n_corr = (int)n;
         a.result->status = RTR_OK;
         s_stop = stop;
+        if (a.prof) atomicAdd(a.prof + 5, icp_timer() - t_s0);
       }
       __syncthreads();
       // pose <- dT * pose, one element per thread
@@ -274,6 +285,10 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(const IcpDev* __restrict__ 
       if (tid == 0) {
         __threadfence();
         st_release_gpu(a.gen, (unsigned)(it + 1) | (s_stop ? 0x80000000u : 0u));
+        if (a.prof) {
+          atomicAdd(a.prof + 1, icp_timer() - t_s0);
+          atomicAdd(a.prof + 3, 1ull);
+        }
       }
       __syncthreads();
     } else {
@@ -293,6 +308,7 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(const IcpDev* __restrict__ 
           __nanosleep(64);
         }
         s_stop = (gv >> 31) ? 1 : 0;
+        if (prof0) atomicAdd(a.prof + 2, icp_timer() - t_arr);
       }
       __syncthreads();
     }
@@ -460,8 +476,10 @@ rtr_status icp_multi(rtr_context* ctx, Scratch& s, std::vector<IcpSpec>& specs, 
     d.gen = sync + 2 * i + 1;
     d.status = ctx->d_status;
     d.budget = ctx->wait_budget_cycles;
+    d.prof = i == 0 ? reinterpret_cast<unsigned long long*>(ctx->d_status + 32) : nullptr;
     blk += nblk[i];
   }
+  RTR_CUDA(cudaMemsetAsync(ctx->d_status + 32, 0, 6 * sizeof(unsigned long long), st));
   for (int f = 0; f < M; f += ICP_SETUP_BATCH) {
     IcpSetup su;
     memset(&su, 0, sizeof(su));
@@ -604,3 +622,11 @@ rtr_status rtr_icp_host(rtr_context* ctx, const float* h_src, int n_src, const f
 }
 
 }  // extern "C"
+
+extern "C" rtr_status rtr_icp_stats(rtr_context* ctx, long long* h_stats6) {
+  RTR_CHECK_ARG(ctx && h_stats6, "rtr_icp_stats: bad arguments");
+  RTR_CUDA(cudaSetDevice(ctx->device));
+  RTR_CUDA(cudaDeviceSynchronize());
+  RTR_CUDA(cudaMemcpy(h_stats6, ctx->d_status + 32, 6 * sizeof(long long), cudaMemcpyDeviceToHost));
+  return RTR_OK;
+}

@@ -30,6 +30,11 @@ struct IcpDev {
   int blk0, nblk;             // this problem's blocks in the launch
   const int* d_active;        // when set: the problem runs only if slot < *d_active
   int slot;
+  // when set (the launch's first problem): ns of block 0's search, of the
+  // last block's serial section and of block 0's wait, summed over the
+  // iterations, the iteration count, and the serial section's time to the
+  // end of its cross-block reduction and of its pose solve
+  unsigned long long* prof;
 };
 
 struct IcpSpec {

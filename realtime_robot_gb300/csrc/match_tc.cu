@@ -11,8 +11,12 @@
 // smallest approximate distances; an exact FP32 re-rank (sequential sums, as
 // the oracle) picks the winner, and a query is certified when its 8th
 // approximate distance minus the error bound is still above the exact winner,
-// so no unseen descriptor can beat or tie it.  Uncertified queries are
-// re-scanned exactly.  The result is bit-identical to the exact matcher.
+// so no unseen descriptor can beat or tie it.  Uncertified queries (near-ties)
+// take a band pass: the same GEMM over them lists every row whose d~ is
+// within twice the bound of the exact winner (every row that could tie or beat
+// it), and exact distances to those rows decide; a band over TC_BAND rows
+// falls back to an exact scan of the whole database.  The result is
+// bit-identical to the exact matcher.
 //
 // Kernel layout (one CTA per 128 queries, 6 warps): warp 4 issues TMA loads of
 // the K-blocks (64 bf16 = one 128-byte swizzle row) of Q_hi, Q_lo, B_hi, B_lo
@@ -183,14 +187,15 @@ struct TcArgs {
   float* cand_d;     // [nq_cap][8]
   int* status;
   const float* thr;  // band pass: [nq_cap] largest d~ a row may have and still tie the winner
-  int* band_n;       // band pass: [nq_cap] rows within the threshold (may exceed TC_BAND)
+  int* band_n;       // band pass: [nq_cap] rows listed (over TC_BAND: overflowed)
 };
 
 // BAND = false: per query the 8 smallest d~ (the first pass).  BAND = true:
 // per query every row with d~ <= thr[q] (the band pass over uncertified
-// queries), the first TC_BAND of them listed, all of them counted in
-// band_n[q] (zeroed by the caller); its grid splits the database into
-// gridDim.y ranges so that a few uncertified queries still fill the GPU.
+// queries), the first TC_BAND of them listed in band_n[q] (zeroed by the
+// caller; a count over TC_BAND means the band overflowed and the row stops
+// counting); its grid splits the database into gridDim.y ranges so that a
+// few uncertified queries still fill the GPU.
 template <bool BAND>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constant__ CUtensorMap mq_hi,
                                                             const __grid_constant__ CUtensorMap mq_lo,
@@ -296,6 +301,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constan
       const bool live = q < nq;
       const float thr = live ? a.thr[q] : 0.f;
       int* list = a.cand_idx + (size_t)(live ? q : 0) * TC_BAND;
+      bool over = false;  // this row's band already past TC_BAND: count no further
       for (int t = t_lo; t < t_hi; ++t) {
         const int buf = (t - t_lo) & 1;
         const uint32_t use = (uint32_t)((t - t_lo) >> 1);
@@ -308,12 +314,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constan
           tmem_ld32(taddr + (uint32_t)c0, v);
           const int jb = t * TC_BN + c0;
           const int lim = valid - c0;
+          // d~ exactly as the first pass forms it for its candidates
+          uint32_t hit = 0;
 #pragma unroll
-          for (int i = 0; i < 32; ++i) {
-            // d~ exactly as the first pass forms it for its candidates
-            if (live && i < lim && qn - 2.f * v[i] <= thr) {
-              const int pos = atomicAdd(a.band_n + q, 1);  // CTAs of other ranges list into it too
-              if (pos < TC_BAND) list[pos] = jb + i;
+          for (int i = 0; i < 32; ++i) hit |= (i < lim && qn - 2.f * v[i] <= thr) ? (1u << i) : 0u;
+          if (live && hit && !over) {
+            // one atomic per chunk (CTAs of other database ranges list into the same row)
+            int pos = atomicAdd(a.band_n + q, __popc(hit));
+            over = pos + __popc(hit) > TC_BAND;
+            while (hit && pos < TC_BAND) {
+              list[pos++] = jb + __ffs(hit) - 1;
+              hit &= hit - 1;
             }
           }
         }

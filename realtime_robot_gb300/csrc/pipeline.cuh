@@ -4,8 +4,7 @@
 
 namespace rtr {
 
-// Scratch need of rtr_recognize for a scene of n points and a model.
-size_t recognize_scratch_bytes(int n_scene, int n_model_vox, int n_model_kp, const rtr_recog_params* p,
-                               bool learned = false);
+// Scratch need of rtr_recognize for a scene of n points.
+size_t recognize_scratch_bytes(int n_scene, const rtr_recog_params* p, bool learned);
 
 }  // namespace rtr
