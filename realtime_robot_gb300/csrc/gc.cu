@@ -49,6 +49,10 @@ __device__ __forceinline__ float sqrt_approx(float x) {
 //  - ds2 > r2max: the scene distance exceeds the largest model distance plus
 //    gc (r2max carries a relative margin far above the rounding of both
 //    sides), so the test fails;
+//  - |sqrt u - sqrt v| = |u - v| / (sqrt u + sqrt v) >= |u - v| / (2 sqrt(max(u, v))),
+//    so (u - v)^2 > 4.004 gc^2 max(u, v) fails the test with a 0.05 % margin
+//    on gc; while gc >= 1e-3 sqrt(max(u, v)) that margin is far above the
+//    rounding of the roots, their difference and this bound (< 2e-4 gc);
 //  - otherwise approximate roots (relative error far below 1e-5) decide
 //    unless |a - b| lies within 1e-5 (a + b) + 1e-6 of gc, where the exact
 //    form runs.  NaN differences fall through to the exact form.
@@ -56,6 +60,8 @@ __device__ __forceinline__ bool gc_consistent(float4 am, float4 as, float4 bm, f
   const float v = dist2_exact(as, bs);
   if (v > r2max) return false;
   const float u = dist2_exact(am, bm);
+  const float duv = u - v, m = fmaxf(u, v), gc2 = gc * gc;
+  if (gc2 >= 1.0e-6f * m && duv * duv > 4.004f * gc2 * m) return false;
   const float a = sqrt_approx(u), b = sqrt_approx(v);
   const float diff = fabsf(a - b);
   const float tol = 1.0e-5f * (a + b) + 1.0e-6f;
@@ -169,8 +175,9 @@ __device__ __forceinline__ void gc_admit(const GcDev& g, int a, const int* slot,
 //     not taken and has no set yet, or whose set lost a member to a commit,
 //     joins this round's list;
 //  A1. seed tests of every listed seed against every candidate, spread over
-//     all warps (a warp loads 32 candidates once and tests them against 8
-//     seeds); the results are pass bitmasks in candidate order;
+//     all warps (a warp stages 32 candidates once and tests them against
+//     its group's 32 seeds, one seed per lane); the results are pass
+//     bitmasks in candidate order;
 //  A2. one warp per listed seed admits the passing candidates in ascending
 //     order, greedily, against the members so far;
 //  B.  warp 0 of block 0 walks the seeds in order from pos: taken seeds are
@@ -184,8 +191,8 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
   extern __shared__ unsigned s_taken[];  // copy of the taken bitset
   __shared__ float4 mem_m[GC_WARPS][GC_MAXS], mem_s[GC_WARPS][GC_MAXS];
   __shared__ int s_slot[GC_WARPS][GC_PEND];
-  __shared__ float4 s_gm[GC_WARPS][32], s_gs[GC_WARPS][32];  // seed tests: the group's seeds
-  __shared__ int s_ga[GC_WARPS][32];
+  __shared__ float4 s_gm[GC_WARPS][32], s_gs[GC_WARPS][32];  // seed tests: the chunk's candidates
+  __shared__ int s_ga[GC_WARPS][32];                          // (sorted position, -1: skipped)
   __shared__ int s_bmem[32][33];  // walk: first 32 members of the next 32 seeds (padded rows)
   __shared__ int s_pos, s_done, s_ok;
   __shared__ float s_r2max;
@@ -246,42 +253,47 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
     const int nneed = __ldcg(c.ctl + 6);
     // ---- A1: seed tests -> pass bitmasks.  Items are (group of 32 listed
     // seeds, chunk of 32 candidates); every warp takes a contiguous run of
-    // items, keeps its group's seed endpoints in shared memory, loads each
-    // candidate chunk once and tests it against all 32 seeds.
+    // items.  Lane k holds seed k of its group in registers; the chunk's
+    // candidates are staged in shared memory once, and each lane tests its
+    // seed against all 32 of them, building its mask word bit by bit.
     if (nneed > 0) {
       const int ngrp = (nneed + 31) >> 5;
       const long long items = (long long)nwp * ngrp;
       const long long per = (items + nwarps - 1) / nwarps;
       const long long it0 = (long long)gw * per, it1 = min(items, it0 + per);
-      int cur = -1;
+      int cur = -1, kend = 0, sa = -1;
+      float4 sm = make_float4(0, 0, 0, 0), ss = sm;
       for (long long it = it0; it < it1; ++it) {
         const int grp = (int)(it / nwp), ch = (int)(it - (long long)grp * nwp);
-        const int kend = min(32, nneed - grp * 32);
         if (grp != cur) {
-          __syncwarp();
+          kend = min(32, nneed - grp * 32);
+          sa = -1;
           if (lane < kend) {
-            const int a = __ldcg(c.need + grp * 32 + lane);
-            s_ga[wid][lane] = a;
-            s_gm[wid][lane] = __ldg(g.pm + a);
-            s_gs[wid][lane] = __ldg(g.ps + a);
+            sa = __ldcg(c.need + grp * 32 + lane);
+            sm = __ldg(g.pm + sa);
+            ss = __ldg(g.ps + sa);
           }
-          __syncwarp();
           cur = grp;
         }
         const int b = ch * 32 + lane;
         const bool okb = b < g.C && !sbit(s_taken, b);
-        float4 bm = make_float4(0, 0, 0, 0), bs = bm;
+        __syncwarp();
+        s_ga[wid][lane] = okb ? b : -1;
         if (okb) {
-          bm = __ldg(g.pm + b);
-          bs = __ldg(g.ps + b);
+          s_gm[wid][lane] = __ldg(g.pm + b);
+          s_gs[wid][lane] = __ldg(g.ps + b);
         }
-        unsigned mine = 0u;  // lane k keeps the word of seed k
-        for (int k = 0; k < kend; ++k) {
-          const bool pass = okb && b != s_ga[wid][k] && gc_consistent(s_gm[wid][k], s_gs[wid][k], bm, bs, g.gc, r2max);
-          const unsigned bal = __ballot_sync(0xffffffffu, pass);
-          if (lane == k) mine = bal;
+        __syncwarp();
+        unsigned mine = 0u;
+        if (lane < kend) {
+#pragma unroll 4
+          for (int j = 0; j < 32; ++j) {
+            const int cb = s_ga[wid][j];
+            if (cb >= 0 && cb != sa && gc_consistent(sm, ss, s_gm[wid][j], s_gs[wid][j], g.gc, r2max))
+              mine |= 1u << j;
+          }
+          c.mask[(size_t)(grp * 32 + lane) * c.nwp + ch] = mine;
         }
-        if (lane < kend) c.mask[(size_t)(grp * 32 + lane) * c.nwp + ch] = mine;
       }
     }
     target += gridDim.x;
