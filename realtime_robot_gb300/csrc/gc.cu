@@ -531,9 +531,13 @@ __global__ void k_gc_poses(const float4* __restrict__ pm, const float4* __restri
   for (int k = 0; k < 9; ++k)
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) H[k] += __shfl_xor_sync(0xffffffffu, H[k], o);
+  // the whole warp solves the rotation, on lane 0's sums (the butterfly
+  // leaves every lane a total, not necessarily the same bits)
+#pragma unroll
+  for (int k = 0; k < 9; ++k) H[k] = __shfl_sync(0xffffffffu, H[k], 0);
+  double R[9];
+  umeyama_rotation_warp(H, R);
   if (lane == 0) {
-    double R[9];
-    umeyama_rotation_fast(H, R);
     double* T = poses + (size_t)c * 16;
     for (int r = 0; r < 3; ++r) {
       for (int cc = 0; cc < 3; ++cc) T[r * 4 + cc] = R[r * 3 + cc];

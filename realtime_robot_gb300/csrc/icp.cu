@@ -225,12 +225,11 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(const IcpDev* __restrict__ 
         s_H[tid] = s_sum[6 + tid] - (double)s_n * (s_sum[r] * inv) * (s_sum[3 + k] * inv);
       }
       __syncthreads();
-      if (tid == 0) {
+      if (warp == 0) {  // the pose solve: warp 0, FP64 products spread over its lanes
         const long long n = s_n;
         int stop = 0, converged = 1;
         double fitness = 0.0;
-#pragma unroll
-        for (int k = 0; k < 16; ++k) s_D[k] = (k % 5 == 0) ? 1.0 : 0.0;
+        double D[12] = {1.0, 0.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 0.0, 1.0, 0.0};
         if (n < 3) {
           stop = 1;
           converged = 0;
@@ -243,7 +242,7 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(const IcpDev* __restrict__ 
           }
 #pragma unroll
           for (int k = 0; k < 9; ++k) H[k] = s_H[k];
-          umeyama_rotation_fast(H, R);
+          umeyama_rotation_warp(H, R);
           double mp[3], mq[3], t[3];
           for (int k = 0; k < 3; ++k) {
             mp[k] = mdp[k] + (double)(k == 0 ? cp.x : (k == 1 ? cp.y : cp.z));
@@ -253,8 +252,8 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(const IcpDev* __restrict__ 
 #pragma unroll
           for (int r = 0; r < 3; ++r) {
 #pragma unroll
-            for (int k = 0; k < 3; ++k) s_D[r * 4 + k] = R[r * 3 + k];
-            s_D[r * 4 + 3] = t[r];
+            for (int k = 0; k < 3; ++k) D[r * 4 + k] = R[r * 3 + k];
+            D[r * 4 + 3] = t[r];
           }
           fitness = s_sum[15] * inv;
           const double cosang = 0.5 * (R[0] + R[4] + R[8] - 1.0);
@@ -262,13 +261,17 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(const IcpDev* __restrict__ 
           if (a.eps_t > 0.0 && tsq < a.eps_t && (a.eps_r <= 0.0 || cosang > a.eps_r)) stop = 1;
         }
         if (it + 1 >= a.max_it) stop = 1;
-        a.result->fitness = fitness;
-        a.result->iterations = it + 1;
-        a.result->converged = converged;
-        a.result->n_corr = (int)n;
-        a.result->status = RTR_OK;
-        s_stop = stop;
-        if (a.prof) atomicAdd(a.prof + 5, icp_timer() - t_s0);
+        if (lane == 0) {
+#pragma unroll
+          for (int k = 0; k < 16; ++k) s_D[k] = k < 12 ? D[k] : (k == 15 ? 1.0 : 0.0);
+          a.result->fitness = fitness;
+          a.result->iterations = it + 1;
+          a.result->converged = converged;
+          a.result->n_corr = (int)n;
+          a.result->status = RTR_OK;
+          s_stop = stop;
+          if (a.prof) atomicAdd(a.prof + 5, icp_timer() - t_s0);
+        }
       }
       __syncthreads();
       // pose <- dT * pose, one element per thread

@@ -220,10 +220,11 @@ __device__ __forceinline__ float newton_f32(const float Hf[9], float R[9]) {
   return sqrtf(w0 * w0 + w1 * w1 + w2 * w2);
 }
 
-// Umeyama rotation: an FP32 start (Newton from the identity, which is where
-// ICP increments live; the FP32 Jacobi SVD when that does not converge) and
-// one FP64 Newton step (see above).
-__device__ __forceinline__ bool umeyama_rotation_fast(const double H[9], double R[9]) {
+// Umeyama rotation, FP32 start: Newton from the identity (where ICP
+// increments live), the FP32 Jacobi SVD when that does not converge.  Writes
+// the start to R0 and the scale applied to H to *sc_out; false (R0 = I) when
+// H is zero or not finite.
+__device__ __forceinline__ bool umeyama_start_f32(const double H[9], double R0[9], float* sc_out) {
   float Hf[9];
   float hmax = 0.f;
 #pragma unroll
@@ -232,10 +233,12 @@ __device__ __forceinline__ bool umeyama_rotation_fast(const double H[9], double 
     hmax = fmaxf(hmax, fabsf(Hf[i]));
   }
   if (!(hmax > 0.f) || !isfinite(hmax)) {
-    for (int i = 0; i < 9; ++i) R[i] = (i % 4 == 0) ? 1.0 : 0.0;
+    for (int i = 0; i < 9; ++i) R0[i] = (i % 4 == 0) ? 1.0 : 0.0;
+    *sc_out = 0.f;
     return false;
   }
   const float sc = 1.f / hmax;
+  *sc_out = sc;
 #pragma unroll
   for (int i = 0; i < 9; ++i) Hf[i] *= sc;
   float Rf[9] = {1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f};
@@ -248,7 +251,6 @@ __device__ __forceinline__ bool umeyama_rotation_fast(const double H[9], double 
       break;
     }
   }
-  double R0[9];
   if (ok) {
 #pragma unroll
     for (int i = 0; i < 9; ++i) R0[i] = (double)Rf[i];
@@ -270,6 +272,18 @@ __device__ __forceinline__ bool umeyama_rotation_fast(const double H[9], double 
         for (int j = 0; j < 3; ++j) s += V[i * 3 + j] * (j == jmin ? d : 1.f) * U[k * 3 + j];
         R0[i * 3 + k] = (double)s;
       }
+  }
+  return true;
+}
+
+// Umeyama rotation: the FP32 start and FP64 polishing (one Newton-Schulz
+// step, then Newton steps; see above), one thread.
+__device__ __forceinline__ bool umeyama_rotation_fast(const double H[9], double R[9]) {
+  double R0[9];
+  float sc;
+  if (!umeyama_start_f32(H, R0, &sc)) {
+    for (int i = 0; i < 9; ++i) R[i] = R0[i];
+    return false;
   }
   // One FP64 Newton-Schulz step, R0 <- R0 (3I - R0^T R0) / 2, takes the FP32
   // start's ~1e-7 loss of orthogonality to ~1e-14 without a division.
@@ -338,6 +352,81 @@ __device__ __forceinline__ bool umeyama_rotation_fast(const double H[9], double 
   }
 #pragma unroll
   for (int i = 0; i < 9; ++i) R[i] = R0[i];
+  return true;
+}
+
+// Entry e of a row-major 3x3 held in registers, e the same or different in
+// every lane (unrolled selects: no local memory).
+__device__ __forceinline__ double pick9(const double M[9], int e) {
+  double v = M[0];
+#pragma unroll
+  for (int q = 1; q < 9; ++q)
+    if (e == q) v = M[q];
+  return v;
+}
+
+// The same rotation computed by a whole warp: every lane passes the same H
+// and gets the same R.  GB300 issues FP64 at a small fraction of the FP32
+// rate and charges per warp instruction, not per active lane, so the FP64
+// 3x3 products run distributed, lane e (0..8) computing entry e from
+// operands fetched with shuffles, and only the scalar chain of each Newton
+// step (on the gathered S) runs on every lane.  The FP32 start is computed
+// by every lane alike, so every branch is warp-uniform.
+__device__ __forceinline__ bool umeyama_rotation_warp(const double H[9], double R[9]) {
+  double R0[9];
+  float sc;
+  if (!umeyama_start_f32(H, R0, &sc)) {
+    for (int i = 0; i < 9; ++i) R[i] = R0[i];
+    return false;
+  }
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int e = lane < 9 ? lane : 8, ei = e / 3, ek = e % 3;
+  double r0 = pick9(R0, e);  // R0 distributed: entry e in lane e
+  {  // Newton-Schulz: R0 <- R0 (3I - R0^T R0) / 2
+    const double g = (ei == ek ? 1.5 : 0.0) -
+                     0.5 * (__shfl_sync(full, r0, ei) * __shfl_sync(full, r0, ek) +
+                            __shfl_sync(full, r0, 3 + ei) * __shfl_sync(full, r0, 3 + ek) +
+                            __shfl_sync(full, r0, 6 + ei) * __shfl_sync(full, r0, 6 + ek));
+    r0 = __shfl_sync(full, r0, ei * 3 + 0) * __shfl_sync(full, g, 0 * 3 + ek) +
+         __shfl_sync(full, r0, ei * 3 + 1) * __shfl_sync(full, g, 1 * 3 + ek) +
+         __shfl_sync(full, r0, ei * 3 + 2) * __shfl_sync(full, g, 2 * 3 + ek);
+  }
+  const double inv = (double)sc;
+  const double h0 = pick9(H, ei * 3 + 0), h1 = pick9(H, ei * 3 + 1), h2 = pick9(H, ei * 3 + 2);
+#pragma unroll 1
+  for (int step = 0; step < 3; ++step) {
+    const double sm = (h0 * __shfl_sync(full, r0, 0 * 3 + ek) + h1 * __shfl_sync(full, r0, 1 * 3 + ek) +
+                       h2 * __shfl_sync(full, r0, 2 * 3 + ek)) * inv;
+    double Sm[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) Sm[q] = __shfl_sync(full, sm, q);
+    const double b0 = 0.5 * (Sm[7] - Sm[5]), b1 = 0.5 * (Sm[2] - Sm[6]), b2 = 0.5 * (Sm[3] - Sm[1]);
+    const double s01 = 0.5 * (Sm[1] + Sm[3]), s02 = 0.5 * (Sm[2] + Sm[6]), s12 = 0.5 * (Sm[5] + Sm[7]);
+    const double tr = Sm[0] + Sm[4] + Sm[8];
+    const double a00 = tr - Sm[0], a11 = tr - Sm[4], a22 = tr - Sm[8];
+    const double a01 = -s01, a02 = -s02, a12 = -s12;
+    const double c00 = a11 * a22 - a12 * a12, c01 = a02 * a12 - a01 * a22, c02 = a01 * a12 - a02 * a11;
+    const double c11 = a00 * a22 - a02 * a02, c12 = a01 * a02 - a00 * a12, c22 = a00 * a11 - a01 * a01;
+    const double det = a00 * c00 + a01 * c01 + a02 * c02;
+    if (!(fabs(det) > 1e-12)) break;
+    const double f = -2.0 / det;
+    const double w0 = f * (c00 * b0 + c01 * b1 + c02 * b2);
+    const double w1 = f * (c01 * b0 + c11 * b1 + c12 * b2);
+    const double w2 = f * (c02 * b0 + c12 * b1 + c22 * b2);
+    const double W[9] = {0.0, -w2, w1, w2, 0.0, -w0, -w1, w0, 0.0};
+    // E = I + W + W^2 / 2, entry e
+    const double ee = (ei == ek ? 1.0 : 0.0) + pick9(W, e) +
+                      0.5 * (pick9(W, ei * 3 + 0) * pick9(W, 0 * 3 + ek) + pick9(W, ei * 3 + 1) * pick9(W, 1 * 3 + ek) +
+                             pick9(W, ei * 3 + 2) * pick9(W, 2 * 3 + ek));
+    r0 = __shfl_sync(full, r0, ei * 3 + 0) * __shfl_sync(full, ee, 0 * 3 + ek) +
+         __shfl_sync(full, r0, ei * 3 + 1) * __shfl_sync(full, ee, 1 * 3 + ek) +
+         __shfl_sync(full, r0, ei * 3 + 2) * __shfl_sync(full, ee, 2 * 3 + ek);
+    const double lmin = det / fmax(fmax(c00, c11), c22);
+    if (w0 * w0 + w1 * w1 + w2 * w2 < 1e-13 * lmin) break;
+  }
+#pragma unroll
+  for (int q = 0; q < 9; ++q) R[q] = __shfl_sync(full, r0, q);
   return true;
 }
 #endif
