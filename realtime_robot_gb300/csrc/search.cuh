@@ -230,9 +230,11 @@ __device__ __forceinline__ void grid_nn1_group(const GridView& g, float4 q, floa
           cc[s] = make_uint2(0u, 0u);
           if (m < vol) {
             const int x = x0 + m % ex, y = y0 + (m / ex) % ey, z = z0 + m / (ex * ey);
-            if (max(max(abs(x - cx), abs(y - cy)), abs(z - cz)) == k) {
+            // the cell's box first: a cell beyond the current best is not fetched
+            if (max(max(abs(x - cx), abs(y - cy)), abs(z - cz)) == k &&
+                !beyond(cell_box_dist(g, q, x, y, z), margin, bd)) {
               cc[s] = g.cells[((unsigned)z * (unsigned)g.ny + (unsigned)y) * (unsigned)g.nx + (unsigned)x];
-              cand[s] = cc[s].x < cc[s].y && !beyond(cell_box_dist(g, q, x, y, z), margin, bd);
+              cand[s] = cc[s].x < cc[s].y;
             }
           }
         }
