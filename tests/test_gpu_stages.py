@@ -92,7 +92,9 @@ def test_shot352_matches_oracle(ctx, clouds):
         err = np.abs(got - ref).max(axis=1)
         # the LRF sign rules can flip on exact ties; everything else agrees
         assert (err < 1e-3).mean() > 0.995, (err < 1e-3).mean()
-        assert np.allclose(np.linalg.norm(got, axis=1), 1.0, atol=1e-5) or True
+        # unit-norm histograms, or all-zero for a keypoint with an empty support
+        nrm = np.linalg.norm(got, axis=1)
+        assert np.all((np.abs(nrm - 1.0) < 1e-5) | (nrm == 0.0))
 
 
 def test_match_exact_bit_exact(ctx, clouds):
