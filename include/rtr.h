@@ -66,7 +66,12 @@ const char* rtr_version(void);
  *   "icp_group"      lanes cooperating on one ICP source point's 1-NN search
  *                    (2, 4 or 8);
  *   "batch_workers"  workers (streams) of rtr_recognize_batch (1..16);
- *   "gc_window"      seeds per window of the grouping walk (32..1024).
+ *   "gc_window"      seeds per window of the grouping walk (32..1024);
+ *   "scene_grid_mm"  cell edge (mm) of the recognition's scene grid, used by
+ *                    verification and ICP refinement (default: 1.5 x the ICP
+ *                    distance; the table's size limit may widen it);
+ *   "normals_grid_mm" cell edge (mm) of the scene normals' k-NN grid
+ *                    (default: five voxel leaves).
  * Unknown keys or values return RTR_ERR_INVALID_ARG.  Results do not depend
  * on the knobs beyond FP32 summation order. */
 rtr_status rtr_context_set_tuning(rtr_context* ctx, const char* key, int value);

@@ -75,6 +75,8 @@ struct rtr_context {
   int tune_batch_workers = 0;          // workers of rtr_recognize_batch (0: automatic)
   int coop_div = 1;                    // cooperative grids use 1/coop_div of the GPU
   int tune_gc_window = 0;              // seeds per grouping window (0: automatic)
+  int tune_scene_grid_mm = 0;          // cell edge of the recognition's scene grid (0: 1.5 ICP distances)
+  int tune_normals_grid_mm = 0;        // cell edge of the scene normals' k-NN grid (0: 5 voxel leaves)
   std::vector<rtr_context*> workers;   // child contexts of the batch driver
   cudaEvent_t ev_fork = nullptr;       // fork/join event of the batch driver
   int gc_stats[8] = {};                // last grouping: rounds, walk end, sets, phase us, candidates

@@ -248,6 +248,12 @@ rtr_status rtr_context_set_tuning(rtr_context* ctx, const char* key, int value) 
     ctx->tune_gc_window = value;
     return RTR_OK;
   }
+  if (strcmp(key, "scene_grid_mm") == 0 || strcmp(key, "normals_grid_mm") == 0) {
+    if (value < 0 || value > 1000)
+      return rtr::fail(RTR_ERR_INVALID_ARG, "%s must be 0..1000 (got %d)", key, value);
+    (key[0] == 's' ? ctx->tune_scene_grid_mm : ctx->tune_normals_grid_mm) = value;
+    return RTR_OK;
+  }
   if (strcmp(key, "icp_group") == 0) {
     if (value != 0 && value != 2 && value != 4 && value != 8)
       return rtr::fail(RTR_ERR_INVALID_ARG, "icp_group must be 0, 2, 4 or 8 (got %d)", value);
