@@ -430,14 +430,24 @@ __global__ void __launch_bounds__(256) k_rerank(const float* __restrict__ q, int
                                                 int* __restrict__ redo, int* __restrict__ n_redo,
                                                 unsigned long long* __restrict__ redo_best,
                                                 float* __restrict__ redo_thr,
-                                                const float* __restrict__ qn, const float* __restrict__ db_max) {
+                                                const float* __restrict__ qn, const float* __restrict__ db_max,
+                                                const unsigned long long* __restrict__ zero_best) {
   const int nq = d_nq ? min(*d_nq, nq_cap) : nq_host;
   const int lane = threadIdx.x & 31, sub = lane >> 3, l8 = lane & 7;
   const int warps = gridDim.x * (blockDim.x >> 5);
   for (int base = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 4; base < nq; base += warps * 4) {
     const int i = base + sub;
     const bool valid = i < nq;
-    const int c = valid ? cand_idx[(size_t)i * TC_TOP + l8] : -1;
+    // an all-zero query ties (up to rounding) with every unit-norm row: its
+    // answer is the same for every such query, the row of least exact
+    // sequential |b|^2 (lowest index on ties), found once per call
+    bool nz = false;
+    if (valid)
+      for (int k = l8; k < TC_DIM; k += 8) nz |= q[(size_t)i * TC_DIM + k] != 0.f;
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) nz |= __shfl_xor_sync(0xffffffffu, (int)nz, o) != 0;
+    const bool zq = valid && !nz;  // (no early exit: the shuffles below need every lane)
+    const int c = valid && !zq ? cand_idx[(size_t)i * TC_TOP + l8] : -1;
     float d = __int_as_float(0x7f800000);
     if (c >= 0) d = exact_d2<V4>(q + (size_t)i * TC_DIM, db + (size_t)c * TC_DIM);
     int bi = c >= 0 ? c : 0x7fffffff;
@@ -451,7 +461,11 @@ __global__ void __launch_bounds__(256) k_rerank(const float* __restrict__ q, int
         bi = oi;
       }
     }
-    if (valid && l8 == 0) {
+    if (zq && l8 == 0) {
+      const unsigned long long key = *zero_best;
+      out_idx[i] = key == ~0ull ? -1 : (int)(unsigned)(key & 0xffffffffull);
+      if (out_d2) out_d2[i] = key == ~0ull ? __int_as_float(0x7f800000) : __uint_as_float((unsigned)(key >> 32));
+    } else if (valid && l8 == 0) {
       const float worst = cand_d[(size_t)i * TC_TOP + TC_TOP - 1];
       const int nvalid = ndb < TC_TOP ? ndb : TC_TOP;
       const bool all_seen = nvalid < TC_TOP;  // every descriptor was a candidate
@@ -470,6 +484,23 @@ __global__ void __launch_bounds__(256) k_rerank(const float* __restrict__ q, int
         redo_thr[p] = bd + 2.f * err;
       }
     }
+  }
+}
+
+// The answer for an all-zero query: min over rows of the exact sequential
+// sum of (0 - b_k)^2 = b_k^2 (each operation rounded, as exact_d2 with a
+// zero row), packed (d^2 bits, index) so that atomicMin keeps the lowest
+// index on ties.  Rows with an infinite or NaN sum never win.
+__global__ void k_zero_best(const float* __restrict__ db, int ndb, unsigned long long* __restrict__ best) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < ndb; j += gridDim.x * blockDim.x) {
+    const float* y = db + (size_t)j * TC_DIM;
+    float acc = 0.f;
+    for (int k = 0; k < TC_DIM; ++k) {
+      const float t = __fsub_rn(0.f, y[k]);
+      acc = __fadd_rn(acc, __fmul_rn(t, t));
+    }
+    if (acc < __int_as_float(0x7f800000))
+      atomicMin(best, ((unsigned long long)__float_as_uint(acc) << 32) | (unsigned)j);
   }
 }
 
@@ -627,6 +658,7 @@ void match_tc_plan(ScratchPlan& p, int nq_cap, bool with_db, int ndb) {
   p.add<int>(nqp);
   p.add<unsigned long long>(nqp);
   p.add<int>(4);
+  p.add<unsigned long long>(1);
   // band pass
   const int bq = band_rows(nqp);
   p.add<float>(nqp);
@@ -675,6 +707,7 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
   int* redo = s.take<int>(nqp);
   unsigned long long* redo_best = s.take<unsigned long long>(nqp);
   int* nredo = s.take<int>(4);  // [0] uncertified, [1] left to the full scan
+  unsigned long long* zero_best = s.take<unsigned long long>(1);
   const int bq = band_rows(nqp);
   float* redo_thr = s.take<float>(nqp);
   int* full = s.take<int>(nqp);
@@ -701,6 +734,8 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
     k_match_tc<false><<<nqp / TC_BM, TC_THREADS, smem, st>>>(m_qh, m_ql, m_bh, m_bl, a);
   }
   RTR_CUDA(cudaMemsetAsync(nredo, 0, 2 * sizeof(int), st));
+  RTR_CUDA(cudaMemsetAsync(zero_best, 0xff, sizeof(unsigned long long), st));
+  k_zero_best<<<(ndb + 255) / 256 < 152 * 4 ? (ndb + 255) / 256 : 152 * 4, 256, 0, st>>>(db, ndb, zero_best);
   int rb = (nq_cap + 31) / 32;
   if (rb > 152 * 16) rb = 152 * 16;
   int wb = (nqp + 7) / 8;  // warp per uncertified query
@@ -711,10 +746,10 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
   TcArgs ab{bq, nredo, bq, ndb, qn2, band_idx, nullptr, ctx->d_status, redo_thr, band_n};
   if (v4)
     k_rerank<true><<<rb, 256, 0, st>>>(q, nq_cap, d_nq, nq_cap, db, ndb, cidx, cd, out_idx, out_d2, redo, nredo,
-                                       redo_best, redo_thr, qn, db_n2 + ndb);
+                                       redo_best, redo_thr, qn, db_n2 + ndb, zero_best);
   else
     k_rerank<false><<<rb, 256, 0, st>>>(q, nq_cap, d_nq, nq_cap, db, ndb, cidx, cd, out_idx, out_d2, redo, nredo,
-                                        redo_best, redo_thr, qn, db_n2 + ndb);
+                                        redo_best, redo_thr, qn, db_n2 + ndb, zero_best);
   k_band_gather<<<(bq + 7) / 8, 256, 0, st>>>(reinterpret_cast<const uint4*>(qhi), reinterpret_cast<const uint4*>(qlo),
                                               qn, redo, nredo, bq, reinterpret_cast<uint4*>(hi2),
                                               reinterpret_cast<uint4*>(lo2), qn2);
@@ -735,7 +770,7 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
     k_match_redo<false><<<152 * 8, 256, 0, st>>>(q, db, ndb, redo, full, nredo + 1, redo_best);
   }
   k_match_redo_out<<<4, 256, 0, st>>>(redo, nredo, redo_best, out_idx, out_d2);
-  RTR_LAUNCHED(8);
+  RTR_LAUNCHED(9);
   // keep the number of uncertified queries and of full scans for rtr_match_stats
   RTR_CUDA(cudaMemcpyAsync(ctx->d_status + 8, nredo, 2 * sizeof(int), cudaMemcpyDeviceToDevice, st));
   RTR_CUDA(cudaGetLastError());
