@@ -19,8 +19,8 @@
 // bit-identical to the exact matcher.
 //
 // Kernel layout (one CTA per 128 queries, 6 warps): warp 4 issues TMA loads of
-// the K-blocks (64 bf16 = one 128-byte swizzle row) of Q_hi, Q_lo, B_hi, B_lo
-// into a 2-stage ring; warp 5 issues tcgen05.mma (M=128, N=256, K=16) into one
+// the K-blocks (32 bf16 = one 64-byte swizzle row) of Q_hi, Q_lo, B_hi, B_lo
+// into a 4-stage ring; warp 5 issues tcgen05.mma (M=128, N=256, K=16) into one
 // of two TMEM accumulators (2 x 256 columns); warps 0-3 drain the finished
 // accumulator with tcgen05.ld (thread = query row) and update the top-8.
 // Every mbarrier wait is bounded; on timeout the CTA records RTR_ERR_TIMEOUT,
@@ -35,17 +35,20 @@ namespace rtr {
 
 constexpr int TC_DIM = 352;
 constexpr int TC_KPAD = 384;              // 6 K-blocks of 64
-constexpr int TC_KB = 64;
+// K-blocks of 32 bf16 (one 64-byte swizzle row): 48 KB stages, four of
+// them in flight (two 96 KB stages of 64-wide K-blocks ran 3 % slower).
+constexpr int TC_KB = 32;
 constexpr int TC_NKB = TC_KPAD / TC_KB;
+constexpr int TC_SW = TC_KB * 2;          // swizzle row bytes (64)
 constexpr int TC_BM = 128;
 constexpr int TC_BN = 256;
-constexpr int TC_STAGES = 2;
+constexpr int TC_STAGES = 4;
 constexpr int TC_TOP = 8;
 constexpr int TC_BAND = 256;      // band pass: rows listed per uncertified query
 constexpr int TC_BAND_Q = 16384;  // band pass: uncertified queries it takes (the rest: full scan)
-constexpr int TC_A_BYTES = TC_BM * TC_KB * 2;   // 16 KB
-constexpr int TC_B_BYTES = TC_BN * TC_KB * 2;   // 32 KB
-constexpr int TC_STAGE_BYTES = 2 * TC_A_BYTES + 2 * TC_B_BYTES;  // 96 KB
+constexpr int TC_A_BYTES = TC_BM * TC_KB * 2;   // 8 KB
+constexpr int TC_B_BYTES = TC_BN * TC_KB * 2;   // 16 KB
+constexpr int TC_STAGE_BYTES = 2 * TC_A_BYTES + 2 * TC_B_BYTES;  // 48 KB
 constexpr int TC_THREADS = 192;
 constexpr float TC_ERR = 1.0e-3f;  // conservative bound on |d~ - d| (see top)
 constexpr long long TC_SPIN_LIMIT = 1LL << 26;
@@ -90,15 +93,16 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, u
       "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
       : "memory");
 }
-// UMMA shared-memory descriptor: K-major, 128-byte swizzle, 8-row atoms of
-// 1024 bytes (SBO), start address in 16-byte units, descriptor version 1.
+// UMMA shared-memory descriptor: K-major, TC_SW-byte swizzle rows, 8-row
+// atoms of 8 * TC_SW bytes (SBO), start address in 16-byte units, descriptor
+// version 1; layout type 4 = 64-byte swizzle, 2 = 128-byte swizzle.
 __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
   uint64_t d = 0;
   d |= (uint64_t)((saddr & 0x3FFFF) >> 4);       // start address
   d |= (uint64_t)1 << 16;                         // LBO (unused for swizzled K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;               // SBO
+  d |= (uint64_t)((8 * TC_SW) >> 4) << 32;        // SBO
   d |= (uint64_t)1 << 46;                         // version
-  d |= (uint64_t)2 << 61;                         // SWIZZLE_128B
+  d |= (uint64_t)(TC_SW == 128 ? 2 : 4) << 61;    // swizzle mode
   return d;
 }
 // Instruction descriptor, kind::f16: D = F32, A = B = BF16, K-major, N, M.
@@ -278,7 +282,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constan
                          bl = base + 2 * TC_A_BYTES + TC_B_BYTES;
 #pragma unroll
           for (int k = 0; k < TC_KB / 16; ++k) {
-            const uint32_t off = (uint32_t)k * 32;  // 16 bf16 along K inside the 128-byte swizzle row
+            const uint32_t off = (uint32_t)k * 32;  // 16 bf16 along K inside the swizzle row
             const uint32_t acc0 = (kb > 0 || k > 0) ? 1u : 0u;
             umma_f16(dcol, umma_desc(ah + off), umma_desc(bh + off), idesc, acc0);
             umma_f16(dcol, umma_desc(ah + off), umma_desc(bl + off), idesc, 1u);
@@ -634,7 +638,8 @@ static bool make_map(CUtensorMap* m, const void* base, int rows, int box_rows) {
   const cuuint32_t box[2] = {(cuuint32_t)TC_KB, (cuuint32_t)box_rows};
   const cuuint32_t estr[2] = {1, 1};
   return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
-             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, TC_SW == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
