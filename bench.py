@@ -394,9 +394,10 @@ def run_ours(args):
                         "algorithmic_bytes_per_launch": icp_bytes},
            "pose_error_vs_truth": list(O.pose_error(ir["pose"], T))}
 
-    batch = streaming = None
+    batch = streaming = learned_room = None
     if not args.no_extra:
         mlp, batch = batch_block(ctx, R, args.steps)
+        learned_room = learned_room_block(ctx, R, m, s_d, prm, mlp, args.steps, stream, flush, r)
         streaming = stream_block(ctx, R, mlp)
 
     line = {
@@ -416,6 +417,7 @@ def run_ours(args):
         "clocks": clocks,
         "icp": icp,
         "batch": batch,
+        "learned_room": learned_room,
         "streaming": streaming,
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -505,6 +507,36 @@ def batch_block(ctx, R, steps: int):
             "learned": {"keep": 0.25, "train_rows": int(X.shape[0]), "positive_rate": float(y.mean()),
                         "train_s_incl_harvest": train_s, "final_loss": float(losses[-1]),
                         "pairs_agreeing_with_plain_1cm_1deg": agree, "fallbacks": n - agree}}
+
+
+def learned_room_block(ctx, R, m, s_d, prm, mlp, steps, stream, flush, plain) -> dict:
+    """The headline room recognised in the learned form (the MLP trained in
+    the batch block keeps the 25 % most credible scene keypoints), timed like
+    `value`, and compared with the plain result."""
+    import torch
+    res = torch.zeros(R.C.sizeof(R.RecogResult), dtype=torch.uint8, device=s_d.device)
+
+    def step():
+        R.recognize_learned(ctx, m, mlp, s_d, keep=0.25, params=prm, result=res, stream=stream.cuda_stream)
+
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for i in range(steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        step()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+    rl = R.parse_recog_result(res)
+    same = len(rl["instances"]) == len(plain["instances"]) and all(
+        np.abs(a["pose"][:3, 3] - b["pose"][:3, 3]).max() <= 0.01 for a, b in zip(rl["instances"], plain["instances"]))
+    return {"metric": "scene recognitions/s, learned form (keep 0.25), config 1", "value": 1e3 / ms,
+            "unit": "recognitions/s", "ms_per_step": ms, "n_keypoints_matched": rl["n_keypoints"],
+            "n_correspondences": rl["n_correspondences"], "instances": len(rl["instances"]),
+            "agrees_with_plain_1cm": bool(same)}
 
 
 def stream_block(ctx, R, mlp) -> dict:
