@@ -75,7 +75,8 @@ struct GcCoop {
   int* ctl;            // [0] walk position, [1] clusters, [2] done, [3] error status, [4] rounds,
                        // [5] sets computed, [6] seeds needing a set this round,
                        // [7] candidates that passed a seed test (summed over sets),
-                       // [8..11] microseconds in phases P, A1, A2, B (block 0's view)
+                       // [8..11] microseconds in phases P, A1, A2, B (block 0's view),
+                       // [12] the next round's window (0: the first window)
   unsigned* arrive;    // grid barrier counter (zero at launch)
   int* computed;       // [C] 1 once the seed's set has been computed
   int* cl_members;     // [max_clusters][GC_MAXS] sorted positions
@@ -86,7 +87,8 @@ struct GcCoop {
   const GridMeta* mbox;  // bounding box of the model endpoints
   int* need;           // [win] seeds whose set is computed this round
   unsigned* mask;      // [win][nwp] seed-test pass bits, one row per needed seed
-  int win;             // seeds per window
+  int win;             // seeds in the first window
+  int win_max;         // seeds a window may grow to (the need/mask capacity)
   int nwp;             // words per mask row (C/32 rounded up to a multiple of 4)
 };
 
@@ -194,7 +196,7 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
   __shared__ float4 s_gm[GC_WARPS][32], s_gs[GC_WARPS][32];  // seed tests: the chunk's candidates
   __shared__ int s_ga[GC_WARPS][32];                          // (sorted position, -1: skipped)
   __shared__ int s_bmem[32][33];  // walk: first 32 members of the next 32 seeds (padded rows)
-  __shared__ int s_pos, s_done, s_ok;
+  __shared__ int s_pos, s_done, s_ok, s_win;
   __shared__ float s_r2max;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (g.d_C) g.C = min(max(*g.d_C, 0), g.C);  // counted on the device
@@ -203,6 +205,7 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
   const int gw = blockIdx.x * GC_WARPS + wid, nwarps = gridDim.x * GC_WARPS;
   if (threadIdx.x == 0) {
     s_pos = 0;
+    s_win = c.win;
     s_done = 0;
     // largest model-side distance: the diagonal of the endpoints' box
     float d2 = 0.f;
@@ -232,7 +235,8 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
     __syncthreads();
     const int pos = s_pos;
     // ---- P: seeds that need a set this round
-    for (int t = gw; t < c.win; t += nwarps) {
+    const int win = s_win;
+    for (int t = gw; t < win; t += nwarps) {
       const int a = pos + t;
       bool need = false;
       if (a < g.C && !sbit(s_taken, a)) {
@@ -379,7 +383,7 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
       int ncl = __ldcg(c.ctl + 1), err = 0;
       bool done = false, stop = false;
       int p = pos;
-      const int wend = min(pos + c.win, g.C);
+      const int wend = min(pos + win, g.C);
       while (p < wend && !stop) {
         const int nb = min(32, wend - p);
         const int my = p + lane;
@@ -444,6 +448,10 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
       __syncwarp();
       for (int i = lane; i < nwords; i += 32) g.taken[i] = s_taken[i];
       if (lane == 0) {
+        // a walk that used its whole window (no stale set, no cap) doubles
+        // the next window: scenes whose walk runs far (few clusters) take
+        // fewer rounds; a stale stop goes back to the first window
+        c.ctl[12] = (!stop && p >= wend) ? min(2 * win, c.win_max) : c.win;
         c.ctl[0] = p;
         c.ctl[1] = ncl;
         c.ctl[2] = done ? 1 : 0;
@@ -459,6 +467,7 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
     if (threadIdx.x == 0) {
       s_pos = __ldcg(c.ctl + 0);
       s_done = __ldcg(c.ctl + 2) || __ldcg(c.ctl + 3);
+      s_win = __ldcg(c.ctl + 12);
     }
     __syncthreads();
     if (s_done) break;
@@ -581,7 +590,8 @@ struct GcBufs {
 };
 
 // Window of the walk and the width of a pass-mask row.
-constexpr int GC_WIN = 256;  // measured on the room: 2.69 ms (256) vs 3.06 ms (1024); results identical
+constexpr int GC_WIN = 256;      // first window: room 2.69 ms (256) vs 3.06 ms (1024 throughout); results identical
+constexpr int GC_WIN_MAX = 2048;  // a window grows to this while the walk keeps using whole windows
 static int gc_nwp(int C) { return (((C > 0 ? C : 1) + 31) / 32 + 3) & ~3; }
 static int gc_win(int C, int want = 0) {
   const size_t row = (size_t)gc_nwp(C) * 4;
@@ -608,8 +618,8 @@ static void gc_plan(ScratchPlan& p, int C, int max_clusters, int max_members) {
   p.add<int>(max_clusters);
   p.add<double>((size_t)max_clusters * 16);
   p.add<GridMeta>(1);
-  p.add<int>(gc_win(C, 1024));
-  p.add<unsigned>((size_t)gc_win(C, 1024) * gc_nwp(C));
+  p.add<int>(gc_win(C, GC_WIN_MAX));
+  p.add<unsigned>((size_t)gc_win(C, GC_WIN_MAX) * gc_nwp(C));
 }
 
 static bool gc_take(Scratch& s, int C, int max_clusters, int max_members, GcBufs* b) {
@@ -631,8 +641,8 @@ static bool gc_take(Scratch& s, int C, int max_clusters, int max_members, GcBufs
   b->sizes = s.take<int>(max_clusters);
   b->poses = s.take<double>((size_t)max_clusters * 16);
   b->mbox = s.take<GridMeta>(1);
-  b->need = s.take<int>(gc_win(C, 1024));
-  b->mask = s.take<unsigned>((size_t)gc_win(C, 1024) * gc_nwp(C));
+  b->need = s.take<int>(gc_win(C, GC_WIN_MAX));
+  b->mask = s.take<unsigned>((size_t)gc_win(C, GC_WIN_MAX) * gc_nwp(C));
   return b->mask != nullptr;
 }
 
@@ -682,7 +692,7 @@ static rtr_status gc_launch(rtr_context* ctx, Scratch& s, const float* d_model_k
   bbox_build(b.mbox, b.pm, C, d_C, st);
   GcCoop c{b.misc, b.arrive, b.computed, b.members, b.sizes, gc_thresh, max_clusters,
            ctx->wait_budget_cycles, ctx->d_status, b.mbox, b.need, b.mask,
-           gc_win(C, ctx->tune_gc_window > 0 ? ctx->tune_gc_window : 0), gc_nwp(C)};
+           gc_win(C, ctx->tune_gc_window > 0 ? ctx->tune_gc_window : 0), gc_win(C, GC_WIN_MAX), gc_nwp(C)};
   RTR_CUDA(cudaFuncSetAttribute(k_gc_coop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GC_MAX_DYN_SMEM));
   int per_sm = 0;
   RTR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gc_coop, GC_WARPS * 32, dyn));
