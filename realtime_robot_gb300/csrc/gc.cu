@@ -384,18 +384,29 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
       bool done = false, stop = false;
       int p = pos;
       const int wend = min(pos + win, g.C);
+      // the batch's sizes and first 32 members are loaded one batch ahead:
+      // they do not change during the walk (only the taken bits do), and the
+      // walk goes on to the next batch only as a whole
+      int nbc = min(32, wend - p);
+      int n_pre = (p < wend && lane < nbc) ? __ldcg(g.set_size + p + lane) : 0;
+      int mv[32];
+#pragma unroll
+      for (int t = 0; t < 32; ++t) mv[t] = (p < wend && t < nbc) ? __ldcg(g.set_mem + (size_t)(p + t) * GC_MAXS + lane) : 0;
       while (p < wend && !stop) {
-        const int nb = min(32, wend - p);
+        const int nb = nbc;
         const int my = p + lane;
-        const int n_l = lane < nb ? __ldcg(g.set_size + my) : 0;
-        {
-          int mv[32];  // all 32 loads in flight before the first store
+        const int n_l = n_pre;
 #pragma unroll
-          for (int t = 0; t < 32; ++t) mv[t] = t < nb ? __ldcg(g.set_mem + (size_t)(p + t) * GC_MAXS + lane) : 0;
-#pragma unroll
-          for (int t = 0; t < 32; ++t) s_bmem[t][lane] = mv[t];  // member `lane` of seed p + t
-        }
+        for (int t = 0; t < 32; ++t) s_bmem[t][lane] = mv[t];  // member `lane` of seed p + t
         __syncwarp();
+        {
+          const int pn = p + nb;
+          nbc = min(32, wend - pn);
+          n_pre = (pn < wend && lane < nbc) ? __ldcg(g.set_size + pn + lane) : 0;
+#pragma unroll
+          for (int t = 0; t < 32; ++t)
+            mv[t] = (pn < wend && t < nbc) ? __ldcg(g.set_mem + (size_t)(pn + t) * GC_MAXS + lane) : 0;
+        }
         const int ns_l = min(n_l, GC_MAXS);
         int cursor = 0;
         for (;;) {
