@@ -438,9 +438,9 @@ rtr_status rtr_batch_graph_create(rtr_context* ctx, const rtr_batch_pair* h_pair
                                   rtr_recog_result* d_results, rtr_batch_graph** out);
 rtr_status rtr_batch_graph_launch(rtr_batch_graph* g, rtr_stream_t stream);
 rtr_status rtr_batch_graph_destroy(rtr_batch_graph* g);
-/* Times the batch under each (workers 1/2/4/8) x (ICP lanes per point 4/8)
+/* Times the batch under each (workers 1/2/4/8) x (ICP lanes per point 2/4/8)
  * setting and keeps the fastest in the context's tuning knobs; reports it in
- * h_workers / h_icp_group (either may be NULL).  Runs the batch 16 times;
+ * h_workers / h_icp_group (either may be NULL).  Runs the batch 24 times;
  * d_results holds the last run's results. */
 rtr_status rtr_batch_autotune(rtr_context* ctx, const rtr_batch_pair* h_pairs, int n_pairs,
                               const rtr_recog_params* p, const rtr_mlp* mlp, float keep,

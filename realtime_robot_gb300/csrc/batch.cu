@@ -176,7 +176,7 @@ rtr_status rtr_batch_autotune(rtr_context* ctx, const rtr_batch_pair* h_pairs, i
   RTR_CHECK_ARG(ctx && p && h_pairs && d_results && n_pairs > 0, "rtr_batch_autotune: bad arguments");
   RTR_CUDA(cudaSetDevice(ctx->device));
   static const int kWorkers[] = {1, 2, 4, 8};
-  static const int kGroups[] = {4, 8};
+  static const int kGroups[] = {2, 4, 8};
   double best = 1e300;
   int bw = 4, bg = 0;
   const int saved_w = ctx->tune_batch_workers, saved_g = ctx->tune_icp_group;

@@ -367,15 +367,16 @@ int icp_max_blocks(rtr_context* ctx) {
   return v;
 }
 
-// Lanes per source point: the tuning override when set, else 8 while the
-// launch needs at most four passes with 8 lanes per point, 4 beyond that
-// (measured on GB300: a 20k-point ICP is fastest at 8, sixteen 11k-point
-// refinements at 4; 2 was slower in both).
+// Lanes per source point: the tuning override when set, else the most lanes
+// (8, 4, 2) with which the launch needs at most four passes over its points
+// (measured on GB300: a 20k-point ICP is fastest at 8, two passes; sixteen
+// 9.2k-point refinements at 2, 3.8 passes: 2.35 ms against 2.48 at 4).
 int icp_pick_group(const rtr_context* ctx, long long total_pts, int blocks) {
   const int t = ctx->tune_icp_group;
   if (t == 2 || t == 4 || t == 8) return t;
   const long long lanes = (long long)blocks * ICP_THREADS;
-  return total_pts * 8 <= 4 * lanes ? 8 : 4;
+  if (total_pts * 8 <= 4 * lanes) return 8;
+  return total_pts * 4 <= 4 * lanes ? 4 : 2;
 }
 
 static rtr_status launch_icp(int G, const IcpDev* d_probs, const int* d_blk2prob, int blocks, cudaStream_t st) {

@@ -66,7 +66,7 @@ def test_batch_learned_equals_single_calls(ctx, rtr, batch):
 def test_batch_autotune(ctx, rtr, batch):
     prm, mods, scenes = batch
     w, g = rtr.batch_autotune(ctx, mods[:4], scenes[:4], prm)
-    assert w in (1, 2, 4, 8) and g in (4, 8)
+    assert w in (1, 2, 4, 8) and g in (2, 4, 8)
     ctx.set_tuning("batch_workers", 0)
     ctx.set_tuning("icp_group", 0)
 
