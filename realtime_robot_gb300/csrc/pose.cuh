@@ -1,103 +1,10 @@
-// pose.cuh — FP64 closed-form rigid pose from a 3x3 cross-covariance
-// (Umeyama 1991, without scale): H = sum (p - mp)(q - mq)^T = U S V^T,
-// R = V diag(1, 1, det(V U^T)) U^T, t = mq - R mp.  The SVD is a one-sided
-// Jacobi iteration on H (Hestenes): rotate column pairs of A = H V until they
-// are orthogonal; then S = column norms, U = normalised columns.
+// pose.cuh — the rotation of the closed-form rigid pose from a 3x3
+// cross-covariance (Umeyama 1991, without scale): R maximises tr(R H) over
+// SO(3), t = mq - R mp follows.  An FP32 start (Newton iteration on the polar
+// condition from the identity, an FP32 one-sided Jacobi SVD when that does
+// not converge) is polished in FP64 by a whole warp.
 #pragma once
 #include <math.h>
-
-#ifdef __CUDACC__
-#define RTR_HD __host__ __device__ __forceinline__
-#else
-#define RTR_HD inline
-#endif
-
-RTR_HD void svd3_jacobi(const double H[9], double U[9], double S[3], double V[9]) {
-  double A[9];
-  for (int i = 0; i < 9; ++i) A[i] = H[i];
-  for (int i = 0; i < 9; ++i) V[i] = (i % 4 == 0) ? 1.0 : 0.0;
-  for (int sweep = 0; sweep < 12; ++sweep) {
-    double off = 0.0;
-    for (int pq = 0; pq < 3; ++pq) {
-      const int p = pq == 2 ? 1 : 0;
-      const int q = pq == 0 ? 1 : 2;
-      double alpha = 0, beta = 0, gamma = 0;
-      for (int i = 0; i < 3; ++i) {
-        alpha += A[i * 3 + p] * A[i * 3 + p];
-        beta += A[i * 3 + q] * A[i * 3 + q];
-        gamma += A[i * 3 + p] * A[i * 3 + q];
-      }
-      const double nrm = sqrt(alpha * beta);
-      if (nrm == 0.0 || fabs(gamma) <= 1e-15 * nrm) continue;
-      const double r = fabs(gamma) / nrm;
-      off = r > off ? r : off;
-      const double zeta = (beta - alpha) / (2.0 * gamma);
-      const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-      const double c = 1.0 / sqrt(1.0 + t * t);
-      const double s = c * t;
-      for (int i = 0; i < 3; ++i) {
-        const double ap = A[i * 3 + p], aq = A[i * 3 + q];
-        A[i * 3 + p] = c * ap - s * aq;
-        A[i * 3 + q] = s * ap + c * aq;
-        const double vp = V[i * 3 + p], vq = V[i * 3 + q];
-        V[i * 3 + p] = c * vp - s * vq;
-        V[i * 3 + q] = s * vp + c * vq;
-      }
-    }
-    if (off < 1e-15) break;
-  }
-  for (int j = 0; j < 3; ++j) {
-    double n = 0;
-    for (int i = 0; i < 3; ++i) n += A[i * 3 + j] * A[i * 3 + j];
-    n = sqrt(n);
-    S[j] = n;
-    for (int i = 0; i < 3; ++i) U[i * 3 + j] = n > 0 ? A[i * 3 + j] / n : 0.0;
-  }
-  // complete U where a singular value vanished: column = cross of the other two
-  for (int j = 0; j < 3; ++j) {
-    const int a = (j + 1) % 3, b = (j + 2) % 3;
-    const double smax = fmax(fmax(S[0], S[1]), S[2]);
-    if (S[j] <= 1e-13 * smax && S[a] > 0 && S[b] > 0) {
-      U[0 * 3 + j] = U[1 * 3 + a] * U[2 * 3 + b] - U[2 * 3 + a] * U[1 * 3 + b];
-      U[1 * 3 + j] = U[2 * 3 + a] * U[0 * 3 + b] - U[0 * 3 + a] * U[2 * 3 + b];
-      U[2 * 3 + j] = U[0 * 3 + a] * U[1 * 3 + b] - U[1 * 3 + a] * U[0 * 3 + b];
-    }
-  }
-}
-
-RTR_HD double det3(const double M[9]) {
-  return M[0] * (M[4] * M[8] - M[5] * M[7]) - M[1] * (M[3] * M[8] - M[5] * M[6]) +
-         M[2] * (M[3] * M[7] - M[4] * M[6]);
-}
-
-// R (3x3 row-major) from H; returns false when H is (numerically) zero.
-RTR_HD bool umeyama_rotation(const double H[9], double R[9]) {
-  double U[9], S[3], V[9];
-  svd3_jacobi(H, U, S, V);
-  if (!(S[0] + S[1] + S[2] > 0)) {
-    for (int i = 0; i < 9; ++i) R[i] = (i % 4 == 0) ? 1.0 : 0.0;
-    return false;
-  }
-  // D = diag(1,1,d) applied to the column of the smallest singular value
-  int jmin = 0;
-  for (int j = 1; j < 3; ++j)
-    if (S[j] < S[jmin]) jmin = j;
-  double VUt[9];
-  for (int i = 0; i < 3; ++i)
-    for (int k = 0; k < 3; ++k) {
-      double s = 0;
-      for (int j = 0; j < 3; ++j) s += V[i * 3 + j] * U[k * 3 + j];
-      VUt[i * 3 + k] = s;
-    }
-  const double d = det3(VUt) < 0 ? -1.0 : 1.0;
-  for (int i = 0; i < 3; ++i)
-    for (int k = 0; k < 3; ++k) {
-      double s = 0;
-      for (int j = 0; j < 3; ++j) s += V[i * 3 + j] * (j == jmin ? d : 1.0) * U[k * 3 + j];
-      R[i * 3 + k] = s;
-    }
-  return true;
-}
 
 // ---------------------------------------------------------------------------
 // Fast FP64 rotation for the GPU.  FP64 instructions are scarce on GB300 (a
@@ -276,85 +183,6 @@ __device__ __forceinline__ bool umeyama_start_f32(const double H[9], double R0[9
   return true;
 }
 
-// Umeyama rotation: the FP32 start and FP64 polishing (one Newton-Schulz
-// step, then Newton steps; see above), one thread.
-__device__ __forceinline__ bool umeyama_rotation_fast(const double H[9], double R[9]) {
-  double R0[9];
-  float sc;
-  if (!umeyama_start_f32(H, R0, &sc)) {
-    for (int i = 0; i < 9; ++i) R[i] = R0[i];
-    return false;
-  }
-  // One FP64 Newton-Schulz step, R0 <- R0 (3I - R0^T R0) / 2, takes the FP32
-  // start's ~1e-7 loss of orthogonality to ~1e-14 without a division.
-  {
-    double G[9], Rn[9];
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-        G[i * 3 + k] = (i == k ? 1.5 : 0.0) -
-                       0.5 * (R0[0 * 3 + i] * R0[0 * 3 + k] + R0[1 * 3 + i] * R0[1 * 3 + k] + R0[2 * 3 + i] * R0[2 * 3 + k]);
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-        Rn[i * 3 + k] = R0[i * 3 + 0] * G[0 * 3 + k] + R0[i * 3 + 1] * G[1 * 3 + k] + R0[i * 3 + 2] * G[2 * 3 + k];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) R0[i] = Rn[i];
-  }
-  // FP64 Newton steps from R0; one is enough when H is well conditioned (the
-  // step error scales with |w|^2 / (s2 + s3)), more when it is not.  Steps are
-  // ~1e-6 here, so I + W + W^2/2 is exact to ~1e-19.
-  const double inv = (double)sc;
-#pragma unroll 1
-  for (int step = 0; step < 3; ++step) {
-    double Sm[9];
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-        Sm[i * 3 + k] = (H[i * 3 + 0] * R0[0 * 3 + k] + H[i * 3 + 1] * R0[1 * 3 + k] + H[i * 3 + 2] * R0[2 * 3 + k]) * inv;
-    // b = vex(asym(S0)); A = tr(sym S0) I - sym S0
-    const double b0 = 0.5 * (Sm[7] - Sm[5]), b1 = 0.5 * (Sm[2] - Sm[6]), b2 = 0.5 * (Sm[3] - Sm[1]);
-    const double s01 = 0.5 * (Sm[1] + Sm[3]), s02 = 0.5 * (Sm[2] + Sm[6]), s12 = 0.5 * (Sm[5] + Sm[7]);
-    const double tr = Sm[0] + Sm[4] + Sm[8];
-    const double a00 = tr - Sm[0], a11 = tr - Sm[4], a22 = tr - Sm[8];
-    const double a01 = -s01, a02 = -s02, a12 = -s12;
-    // solve A w = -2 b by the adjugate (A symmetric)
-    const double c00 = a11 * a22 - a12 * a12, c01 = a02 * a12 - a01 * a22, c02 = a01 * a12 - a02 * a11;
-    const double c11 = a00 * a22 - a02 * a02, c12 = a01 * a02 - a00 * a12, c22 = a00 * a11 - a01 * a01;
-    const double det = a00 * c00 + a01 * c01 + a02 * c02;
-    if (!(fabs(det) > 1e-12)) break;
-    const double f = -2.0 / det;
-    const double w0 = f * (c00 * b0 + c01 * b1 + c02 * b2);
-    const double w1 = f * (c01 * b0 + c11 * b1 + c12 * b2);
-    const double w2 = f * (c02 * b0 + c12 * b1 + c22 * b2);
-    // E = I + W + W^2/2,  W = [w]x
-    const double W[9] = {0.0, -w2, w1, w2, 0.0, -w0, -w1, w0, 0.0};
-    double E[9], Rn[9];
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-        E[i * 3 + k] = (i == k ? 1.0 : 0.0) + W[i * 3 + k] +
-                       0.5 * (W[i * 3 + 0] * W[0 * 3 + k] + W[i * 3 + 1] * W[1 * 3 + k] + W[i * 3 + 2] * W[2 * 3 + k]);
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-        Rn[i * 3 + k] = R0[i * 3 + 0] * E[0 * 3 + k] + R0[i * 3 + 1] * E[1 * 3 + k] + R0[i * 3 + 2] * E[2 * 3 + k];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) R0[i] = Rn[i];
-    // the new R is off by about |w|^2 / lambda_min(A); lambda_min ~ det / max c_ii
-    const double lmin = det / fmax(fmax(c00, c11), c22);
-    if (w0 * w0 + w1 * w1 + w2 * w2 < 1e-13 * lmin) break;
-  }
-#pragma unroll
-  for (int i = 0; i < 9; ++i) R[i] = R0[i];
-  return true;
-}
-
 // Entry e of a row-major 3x3 held in registers, e the same or different in
 // every lane (unrolled selects: no local memory).
 __device__ __forceinline__ double pick9(const double M[9], int e) {
@@ -431,14 +259,3 @@ __device__ __forceinline__ bool umeyama_rotation_warp(const double H[9], double 
 }
 #endif
 
-// C = A * B for row-major 4x4.
-RTR_HD void mat4_mul(const double A[16], const double B[16], double C[16]) {
-  double T[16];
-  for (int i = 0; i < 4; ++i)
-    for (int j = 0; j < 4; ++j) {
-      double s = 0;
-      for (int k = 0; k < 4; ++k) s += A[i * 4 + k] * B[k * 4 + j];
-      T[i * 4 + j] = s;
-    }
-  for (int i = 0; i < 16; ++i) C[i] = T[i];
-}
