@@ -392,7 +392,10 @@ rtr_status rtr_model_buffers(const rtr_model* m, const float** d_vox, const floa
  * rtr_recog_result.  Does not synchronise: every count stays on the device
  * and errors reach the context status word (rtr_context_check).  The first
  * call at a scene size may grow the context's scratch (that synchronises);
- * after it, calls of at most that size can be captured into a CUDA graph. */
+ * after it, calls of at most that size can be captured into a CUDA graph.
+ * Such a graph holds the scratch's address: a later call that grows the
+ * scratch (a larger scene, the learned form) moves it, and the graph must not
+ * be launched again (rtr_context_reserve the largest size first). */
 rtr_status rtr_recognize(rtr_context* ctx, const rtr_model* model, const float* d_scene, int n,
                          const rtr_recog_params* p, rtr_recog_result* d_result,
                          rtr_stream_t stream);
@@ -431,7 +434,12 @@ rtr_status rtr_recognize_batch(rtr_context* ctx, const rtr_batch_pair* h_pairs, 
  * results after synchronising; rtr_context_check on the workers is not
  * needed: errors also leave a non-OK status in each result).  The scenes
  * must stay at the same device addresses; their contents, and the model
- * buffers' contents, may change between launches (same sizes). */
+ * buffers' contents, may change between launches (same sizes).  The graph
+ * also holds the addresses of the context's and its workers' scratch: a
+ * later call on the context that needs more scratch (a larger batch, the
+ * learned form after a plain graph) reallocates it, and launch then returns
+ * RTR_ERR_INVALID_ARG instead of running; create the largest graphs first,
+ * or size the scratch with the largest batch before creating any. */
 typedef struct rtr_batch_graph rtr_batch_graph;
 rtr_status rtr_batch_graph_create(rtr_context* ctx, const rtr_batch_pair* h_pairs, int n_pairs,
                                   const rtr_recog_params* p, const rtr_mlp* mlp, float keep,

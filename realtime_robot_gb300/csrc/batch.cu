@@ -25,6 +25,10 @@ struct rtr_batch_graph {
   rtr_context* ctx = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  // scratch generations of the context and of each worker at capture: the
+  // graph holds their arena addresses, so it may run only while none of the
+  // arenas has been reallocated since
+  std::vector<unsigned> gens;
 };
 
 namespace rtr {
@@ -150,12 +154,20 @@ rtr_status rtr_batch_graph_create(rtr_context* ctx, const rtr_batch_pair* h_pair
   bg->ctx = ctx;
   bg->graph = g;
   bg->exec = x;
+  bg->gens.push_back(ctx->scratch_gen);
+  for (int wi = 0; wi < nw; ++wi) bg->gens.push_back(ctx->workers[wi]->scratch_gen);
   *out = bg;
   return RTR_OK;
 }
 
 rtr_status rtr_batch_graph_launch(rtr_batch_graph* bg, rtr_stream_t stream) {
   RTR_CHECK_ARG(bg && bg->exec, "rtr_batch_graph_launch: bad graph");
+  bool same = !bg->gens.empty() && bg->gens[0] == bg->ctx->scratch_gen &&
+              bg->gens.size() <= bg->ctx->workers.size() + 1;
+  for (size_t k = 1; same && k < bg->gens.size(); ++k) same = bg->gens[k] == bg->ctx->workers[k - 1]->scratch_gen;
+  RTR_CHECK_ARG(same,
+                "rtr_batch_graph_launch: a call on this context grew its scratch after the graph was made (its "
+                "buffers moved); destroy and recreate the graph, or reserve scratch before creating it");
   RTR_CUDA(cudaSetDevice(bg->ctx->device));
   RTR_CUDA(cudaGraphLaunch(bg->exec, (cudaStream_t)stream));
   return RTR_OK;

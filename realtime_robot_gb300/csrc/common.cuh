@@ -61,6 +61,7 @@ struct rtr_context {
   int num_sms = 0;
   int max_smem_optin = 0;
   void* arena = nullptr;        // scratch arena (device)
+  unsigned scratch_gen = 0;     // times the arena was (re)allocated: a captured graph is valid only for one
   size_t arena_bytes = 0;
   int* d_status = nullptr;      // device status word written by persistent kernels
   unsigned* d_sync = nullptr;   // 64 words of barrier counters for persistent kernels

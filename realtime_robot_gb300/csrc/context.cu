@@ -79,6 +79,7 @@ rtr_status ensure_scratch(rtr_context* ctx, size_t bytes, cudaStream_t stream, S
                   cudaGetErrorString(e));
     }
     ctx->arena_bytes = grow;
+    ++ctx->scratch_gen;
   }
   out->base = static_cast<char*>(ctx->arena);
   out->off = 0;

@@ -93,6 +93,31 @@ def test_batch_graph_replays_the_batch(ctx, rtr, batch):
     ctx.set_tuning("batch_workers", 0)
 
 
+def test_batch_graph_refuses_to_run_after_scratch_moved(rtr, batch):
+    # a fresh context: the plain graph is made on scratch sized for the plain
+    # batch; the learned batch then needs more and reallocates it, so the
+    # graph's launch must be refused on the host (no kernel runs)
+    import torch
+    prm, mods, scenes = batch
+    c2 = rtr.Context(0)
+    c2.set_tuning("batch_workers", 2)
+    g = rtr.BatchGraph(c2, mods[:4], scenes[:4], prm)
+    g.launch()
+    torch.cuda.synchronize()
+    mlp = rtr.Mlp(c2, seed=11)
+    rtr.recognize_batch(c2, mods[:4], scenes[:4], prm, mlp=mlp, keep=0.5)
+    with pytest.raises(rtr.RtrError) as e:
+        g.launch()
+    assert e.value.status == 1 and "recreate" in str(e.value)
+    g.close()
+    # made again after the growth, it runs
+    g = rtr.BatchGraph(c2, mods[:4], scenes[:4], prm)
+    g.launch()
+    torch.cuda.synchronize()
+    g.close()
+    c2.close()
+
+
 def test_single_recognition_captured_in_a_graph(ctx, rtr, batch):
     import torch
     prm, mods, scenes = batch
