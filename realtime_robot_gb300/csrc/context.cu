@@ -69,6 +69,7 @@ rtr_status ensure_scratch(rtr_context* ctx, size_t bytes, cudaStream_t stream, S
                   ctx->arena_bytes, bytes);
     size_t grow = bytes + bytes / 4 + (1u << 20);
     RTR_CUDA(cudaDeviceSynchronize());
+    ++ctx->scratch_gen;  // from here on the old arena is gone, whatever the allocation below does
     if (ctx->arena) RTR_CUDA(cudaFree(ctx->arena));
     ctx->arena = nullptr;
     ctx->arena_bytes = 0;
@@ -79,7 +80,6 @@ rtr_status ensure_scratch(rtr_context* ctx, size_t bytes, cudaStream_t stream, S
                   cudaGetErrorString(e));
     }
     ctx->arena_bytes = grow;
-    ++ctx->scratch_gen;
   }
   out->base = static_cast<char*>(ctx->arena);
   out->off = 0;
