@@ -439,7 +439,8 @@ rtr_status rtr_recognize_batch(rtr_context* ctx, const rtr_batch_pair* h_pairs, 
  * later call on the context that needs more scratch (a larger batch, the
  * learned form after a plain graph) reallocates it, and launch then returns
  * RTR_ERR_INVALID_ARG instead of running; create the largest graphs first,
- * or size the scratch with the largest batch before creating any. */
+ * or size the scratch with the largest batch before creating any.  Destroy
+ * a graph before its context. */
 typedef struct rtr_batch_graph rtr_batch_graph;
 rtr_status rtr_batch_graph_create(rtr_context* ctx, const rtr_batch_pair* h_pairs, int n_pairs,
                                   const rtr_recog_params* p, const rtr_mlp* mlp, float keep,
