@@ -305,13 +305,15 @@ def run_ours(args):
         # one FP32-equivalent GEMM: 2 * scene keypoints * model keypoints * 352
         "match_gemm": ("tensor", 2.0 * Ks * Km * 352, "k_match_tc (tcgen05 BF16 hi/lo split, FP32 accumulate, top-8)",
                        "three BF16 MMAs per K step; two 96 KB TMA stages per CTA"),
-        # every computed consensus set reads both endpoints (32 B) of every correspondence once
-        "gc_walk": ("hbm", 32.0 * C * gcs["sets"], "k_gc_coop (cooperative grouping walk)",
-                    "C x sets consistency checks; the endpoints (3.5 MB) are re-read from L2, not HBM: "
-                    "compute- and barrier-bound"),
+        # the unique bytes the walk must move: both endpoints (32 B) of every
+        # correspondence; everything else (C x sets consistency checks over
+        # those endpoints, the pass masks, the sets) lives in L2
+        "gc_walk": ("hbm", 32.0 * C, "k_gc_coop (cooperative grouping walk)",
+                    f"compute- and barrier-bound: {C} x {gcs['sets']} = {C * gcs['sets']:.3g} consistency checks "
+                    f"in {gcs['rounds']} rounds of four grid-wide phases; the 32 B x C endpoints stay in L2"),
         # per hypothesis and iteration: each model voxel (16 B) and its matched scene point (16 B)
         "icp_refine": ("hbm", 32.0 * M_ref * prm.icp_iterations * m.n_voxels, "k_icp (multi-problem refinement)",
-                       "latency-bound: ~8 dependent grid lookups per source point, 7-8 points per lane group "
+                       "latency-bound: ~8 dependent grid lookups per source point, ~4 points per 2-lane group "
                        "per iteration, then a grid barrier and the FP64 pose solve"),
     }
     kern = {k: v for k, v in kern.items() if k in stage_ms}
