@@ -82,7 +82,29 @@ def build(verbose: bool = False, ptxas_verbose: bool = False) -> Path:
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
+    build_demo()
     return LIB
+
+
+CPP = PKG / "cpp"
+DEMO = PKG / "realtime_robot_demo"
+
+
+def build_demo() -> Path:
+    """The C++ mirror of the reference's entry points (cpp/realtime_robot.hpp)
+    exercised by its driver (cpp/realtime_robot_demo.cpp), linked to librtr.so."""
+    src = CPP / "realtime_robot_demo.cpp"
+    deps = [src, CPP / "realtime_robot.hpp", INCLUDE / "rtr.h", LIB]
+    if DEMO.exists() and DEMO.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
+        return DEMO
+    cuda_inc = Path(_nvcc()).resolve().parent.parent / "include"
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-I", str(INCLUDE), "-I", str(CPP), "-I", str(cuda_inc), str(src),
+           "-o", str(DEMO), "-L", str(PKG), "-lrtr", "-L", str(_cuda_lib_dir()), "-lcudart_static", "-ldl", "-lrt",
+           "-lpthread", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"demo build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return DEMO
 
 
 if __name__ == "__main__":

@@ -1,0 +1,442 @@
+// realtime_robot.hpp — the reference's C++ entry points for the registration
+// path, kept by name and argument meaning, on top of the rtr C ABI (rtr.h):
+//
+//   ModelPoint(Ptr) / getKeypoint()      model_point.h:82-94, 99-156
+//   ScanPoint(Ptr)  / getKeypoint()      scan_point.h:50-53, 57-113
+//   KeyPoint, PairPoint                  key_point.h:59-86, matching.h
+//   the all-pairs correspondence loop    RealTimeRobot.cpp:70-102  -> match_keypoints()
+//   Eigen::Matrix4f Ransac(...)          function.h:35-109
+//   void keyPointICP(...)                function.h:111-148
+//   ComputeTDFWithCuda                   kernel.cu:34-106 (declared in rtr.h, same signature)
+//
+// The stages are the ones the GPU path implements: 1 cm voxels, k = 10
+// normals, 2 cm uniform keypoints and SHOT-352 descriptors at 4 cm in place
+// of Harris3D keypoints and TDF / plane-area descriptors; descriptor 1-NN in
+// place of get_Distance and the ratio gates; geometric-consistency grouping
+// in place of the pair-consensus loop; point-to-point ICP as before.  Errors
+// raise rtr_error (what() carries rtr_last_error()).
+//
+// Without PCL and Eigen (this machine has neither) a minimal stand-in of the
+// types the signatures use is defined here: pcl::PointXYZ (16 bytes, the
+// layout every rtr entry point reads), pcl::PointCloud<T>, Eigen::Matrix4f,
+// pcl::transformPointCloud.  Define RTR_HAVE_PCL to use the real ones.
+#pragma once
+
+#include <cuda_runtime_api.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <iostream>
+#include <memory>
+#include <ostream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "rtr.h"
+
+#ifndef RTR_HAVE_PCL
+namespace Eigen {
+struct Matrix4f {
+  float m[16];
+  Matrix4f() { std::memset(m, 0, sizeof(m)); }
+  static Matrix4f Identity() {
+    Matrix4f r;
+    for (int i = 0; i < 4; ++i) r.m[i * 5] = 1.f;
+    return r;
+  }
+  float& operator()(int r, int c) { return m[r * 4 + c]; }
+  float operator()(int r, int c) const { return m[r * 4 + c]; }
+};
+inline std::ostream& operator<<(std::ostream& o, const Matrix4f& T) {
+  for (int r = 0; r < 4; ++r) {
+    for (int c = 0; c < 4; ++c) o << (c ? " " : "") << T(r, c);
+    o << "\n";
+  }
+  return o;
+}
+}  // namespace Eigen
+
+namespace pcl {
+struct PointXYZ {
+  float x = 0.f, y = 0.f, z = 0.f, pad = 1.f;
+  PointXYZ() = default;
+  PointXYZ(float x_, float y_, float z_) : x(x_), y(y_), z(z_) {}
+};
+static_assert(sizeof(PointXYZ) == 16, "the rtr entry points read 16-byte points");
+
+template <class T>
+struct PointCloud {
+  using Ptr = std::shared_ptr<PointCloud<T>>;
+  std::vector<T> points;
+  uint32_t width = 0, height = 1;
+  bool is_dense = true;
+  size_t size() const { return points.size(); }
+  void push_back(const T& p) {
+    points.push_back(p);
+    width = (uint32_t)points.size();
+  }
+  typename std::vector<T>::iterator begin() { return points.begin(); }
+  typename std::vector<T>::iterator end() { return points.end(); }
+  typename std::vector<T>::const_iterator begin() const { return points.begin(); }
+  typename std::vector<T>::const_iterator end() const { return points.end(); }
+};
+
+inline void transformPointCloud(const PointCloud<PointXYZ>& in, PointCloud<PointXYZ>& out,
+                                const Eigen::Matrix4f& T) {
+  std::vector<PointXYZ> r(in.points.size());
+  for (size_t i = 0; i < r.size(); ++i) {
+    const PointXYZ& p = in.points[i];
+    r[i] = PointXYZ(T(0, 0) * p.x + T(0, 1) * p.y + T(0, 2) * p.z + T(0, 3),
+                    T(1, 0) * p.x + T(1, 1) * p.y + T(1, 2) * p.z + T(1, 3),
+                    T(2, 0) * p.x + T(2, 1) * p.y + T(2, 2) * p.z + T(2, 3));
+  }
+  out.points.swap(r);
+  out.width = (uint32_t)out.points.size();
+  out.height = 1;
+}
+}  // namespace pcl
+#endif  // RTR_HAVE_PCL
+
+namespace rtr_robot {
+
+using Cloud = pcl::PointCloud<pcl::PointXYZ>;
+
+struct rtr_error : std::runtime_error {
+  rtr_status status;
+  rtr_error(rtr_status s, const std::string& where)
+      : std::runtime_error(where + ": " + rtr_status_string(s) + ": " + rtr_last_error()), status(s) {}
+};
+
+inline void check(rtr_status s, const char* where) {
+  if (s != RTR_OK) throw rtr_error(s, where);
+}
+
+inline void check_cuda(cudaError_t e, const char* where) {
+  if (e != cudaSuccess) throw std::runtime_error(std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+// Device buffer owned by the host objects below.
+template <class T>
+struct DeviceArray {
+  T* p = nullptr;
+  size_t n = 0;
+  DeviceArray() = default;
+  explicit DeviceArray(size_t count) { resize(count); }
+  DeviceArray(const DeviceArray&) = delete;
+  DeviceArray& operator=(const DeviceArray&) = delete;
+  DeviceArray(DeviceArray&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr, o.n = 0; }
+  ~DeviceArray() { cudaFree(p); }
+  void resize(size_t count) {
+    cudaFree(p);
+    p = nullptr;
+    n = count;
+    if (count) check_cuda(cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T)), "cudaMalloc");
+  }
+  void upload(const T* h, size_t count) {
+    if (count > n) resize(count);
+    if (count) check_cuda(cudaMemcpy(p, h, count * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+  }
+  void download(T* h, size_t count) const {
+    if (count) check_cuda(cudaMemcpy(h, p, count * sizeof(T), cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+  }
+};
+
+// One context per host thread (the reference is single-threaded; so is the
+// context).
+inline rtr_context* thread_context() {
+  struct Holder {
+    rtr_context* ctx = nullptr;
+    ~Holder() {
+      if (ctx) rtr_context_destroy(ctx);
+    }
+  };
+  thread_local Holder h;
+  if (!h.ctx) check(rtr_context_create(0, &h.ctx), "rtr_context_create");
+  return h.ctx;
+}
+
+constexpr int kDescDim = 352;
+
+// A keypoint and its SHOT-352 descriptor (key_point.h:59-86 keeps the TDF
+// grid, the occupancy cloud and the plane-area vector here instead).
+struct KeyPoint {
+  pcl::PointXYZ Key_coordinate;
+  std::vector<float> descriptor;  // kDescDim values, L2-normalised
+  KeyPoint() = default;
+  explicit KeyPoint(const pcl::PointXYZ& p) : Key_coordinate(p) {}
+};
+
+// A model keypoint paired with a scene keypoint (point_i model, point_j
+// scene, as main builds them), with the descriptor distance that ranks it.
+struct PairPoint {
+  KeyPoint point_i, point_j;
+  int model_index = -1, scene_index = -1;
+  float distance2 = 0.f;
+};
+
+// Keypoints and descriptors of a cloud: voxels, normals, uniform keypoints,
+// SHOT (the body of both getKeypoint()s).  Device copies are kept for the
+// matching and grouping stages.
+struct KeypointSet {
+  Cloud key_coordinates;
+  std::vector<KeyPoint> keyPoint;
+  DeviceArray<float> d_kp;    // K x 4
+  DeviceArray<float> d_desc;  // K x 352
+  int n_kp = 0;
+
+  void compute(const Cloud& cloud, const float viewpoint[3], bool outward, bool model_side) {
+    rtr_context* ctx = thread_context();
+    rtr_recog_params prm;
+    rtr_recog_default_params(&prm);
+    const int n = (int)cloud.size();
+    if (n <= 0) throw std::invalid_argument("getKeypoint: empty cloud");
+    DeviceArray<float> d_pts(4 * (size_t)n), d_vox(4 * (size_t)n), d_nrm(4 * (size_t)n);
+    DeviceArray<int> d_cnt(2);
+    DeviceArray<int32_t> d_keys((size_t)n);
+    d_pts.upload(reinterpret_cast<const float*>(cloud.points.data()), 4 * (size_t)n);
+    check(rtr_voxel_downsample(ctx, d_pts.p, n, prm.voxel_leaf, d_vox.p, d_cnt.p, nullptr), "rtr_voxel_downsample");
+    int V = 0;
+    d_cnt.download(&V, 1);
+    if (V <= 0) throw std::runtime_error("getKeypoint: the voxel filter kept no point");
+    check(rtr_normals(ctx, d_vox.p, V, prm.normal_k, viewpoint, 2.f * prm.voxel_leaf, d_nrm.p, nullptr),
+          "rtr_normals");
+    if (outward) check(rtr_orient_normals_outward(ctx, d_vox.p, d_nrm.p, V, 0.01f, 0.005f, 1.0f, nullptr),
+                       "rtr_orient_normals_outward");
+    const float r_kp = model_side ? prm.model_keypoint_r : prm.scene_keypoint_r;
+    check(rtr_uniform_sample(ctx, d_vox.p, V, r_kp, d_keys.p, d_cnt.p + 1, nullptr), "rtr_uniform_sample");
+    int K = 0;
+    check_cuda(cudaMemcpy(&K, d_cnt.p + 1, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    n_kp = K;
+    d_desc.resize((size_t)K * kDescDim);
+    if (K > 0)
+      check(rtr_shot352(ctx, d_vox.p, d_nrm.p, V, d_keys.p, K, prm.descriptor_r, d_desc.p, nullptr, nullptr),
+            "rtr_shot352");
+    std::vector<float> vox(4 * (size_t)V), desc((size_t)K * kDescDim);
+    std::vector<int32_t> keys((size_t)K);
+    d_vox.download(vox.data(), vox.size());
+    d_keys.download(keys.data(), keys.size());
+    d_desc.download(desc.data(), desc.size());
+    std::vector<float> kp(4 * (size_t)K);
+    key_coordinates = Cloud();
+    keyPoint.assign((size_t)K, KeyPoint());
+    for (int i = 0; i < K; ++i) {
+      const float* v = &vox[4 * (size_t)keys[i]];
+      pcl::PointXYZ p(v[0], v[1], v[2]);
+      key_coordinates.push_back(p);
+      keyPoint[i] = KeyPoint(p);
+      keyPoint[i].descriptor.assign(desc.begin() + (size_t)i * kDescDim, desc.begin() + (size_t)(i + 1) * kDescDim);
+      std::memcpy(&kp[4 * (size_t)i], v, 3 * sizeof(float));
+      kp[4 * (size_t)i + 3] = 0.f;
+    }
+    d_kp.upload(kp.data(), kp.size());
+  }
+};
+
+// model_point.h:82-94: the model cloud (a full 360-degree cloud: normals are
+// oriented outward; keypoints at the model radius).
+class ModelPoint : public KeypointSet {
+ public:
+  Cloud::Ptr Mpoint;
+  ModelPoint() = default;
+  explicit ModelPoint(Cloud::Ptr m) : Mpoint(std::move(m)) {}
+  void getKeypoint() {
+    const float vp[3] = {0.f, 0.f, 0.f};
+    compute(*Mpoint, vp, true, true);
+  }
+};
+
+// scan_point.h:50-53: the scene.  A sensor view keeps its normals facing
+// `viewpoint`; a segmented object seen from all sides (orient_outward) has
+// them oriented outward like the model's.
+class ScanPoint : public KeypointSet {
+ public:
+  Cloud::Ptr Spoint;
+  float viewpoint[3] = {0.f, 0.f, 0.f};
+  bool orient_outward = false;
+  ScanPoint() = default;
+  explicit ScanPoint(Cloud::Ptr s) : Spoint(std::move(s)) {}
+  void getKeypoint() { compute(*Spoint, viewpoint, orient_outward, false); }
+};
+
+// The correspondence loop of main (RealTimeRobot.cpp:70-102): every scene
+// keypoint paired with its nearest model descriptor, kept when the squared
+// descriptor distance is below max_d2 (the recognition default, 0.25).
+inline std::vector<PairPoint> match_keypoints(const ModelPoint& model, const ScanPoint& scan, float max_d2 = -1.f) {
+  rtr_context* ctx = thread_context();
+  if (max_d2 < 0.f) {
+    rtr_recog_params prm;
+    rtr_recog_default_params(&prm);
+    max_d2 = prm.match_max_d2;
+  }
+  std::vector<PairPoint> out;
+  if (model.n_kp == 0 || scan.n_kp == 0) return out;
+  DeviceArray<int32_t> d_idx((size_t)scan.n_kp);
+  DeviceArray<float> d_d2((size_t)scan.n_kp);
+  check(rtr_match(ctx, scan.d_desc.p, scan.n_kp, model.d_desc.p, model.n_kp, d_idx.p, d_d2.p, nullptr), "rtr_match");
+  std::vector<int32_t> idx((size_t)scan.n_kp);
+  std::vector<float> d2((size_t)scan.n_kp);
+  d_idx.download(idx.data(), idx.size());
+  d_d2.download(d2.data(), d2.size());
+  for (int s = 0; s < scan.n_kp; ++s) {
+    if (idx[s] < 0 || !(d2[s] < max_d2)) continue;
+    PairPoint p;
+    p.point_i = model.keyPoint[(size_t)idx[s]];
+    p.point_j = scan.keyPoint[(size_t)s];
+    p.model_index = idx[s];
+    p.scene_index = s;
+    p.distance2 = d2[s];
+    out.push_back(std::move(p));
+  }
+  return out;
+}
+
+// Inlier counts of candidate model -> scene poses (row-major 4x4 doubles):
+// for each pose, how many points of mcloud it brings within r of a point of
+// the scene cloud (already on the device), from one exact grid 1-NN call
+// over all poses' transformed points.
+inline std::vector<long long> pose_inliers(rtr_context* ctx, const std::vector<double>& poses, const Cloud& mcloud,
+                                           const float* d_scene, int ns, float r) {
+  const int np = (int)(poses.size() / 16), nm = (int)mcloud.size();
+  std::vector<long long> out((size_t)np, 0);
+  if (np == 0 || nm == 0 || ns == 0) return out;
+  if ((size_t)np * (size_t)nm > (size_t)INT32_MAX) throw rtr_error(RTR_ERR_INVALID_ARG, "pose_inliers: too many points");
+  std::vector<float> q((size_t)np * nm * 4);
+  for (int c = 0; c < np; ++c) {
+    const double* T = &poses[(size_t)c * 16];
+    for (int i = 0; i < nm; ++i) {
+      const pcl::PointXYZ& m = mcloud.points[(size_t)i];
+      float* o = &q[((size_t)c * nm + i) * 4];
+      for (int k = 0; k < 3; ++k) o[k] = (float)(T[k * 4] * m.x + T[k * 4 + 1] * m.y + T[k * 4 + 2] * m.z + T[k * 4 + 3]);
+      o[3] = 0.f;
+    }
+  }
+  DeviceArray<float> d_q(q.size()), d_d2((size_t)np * nm);
+  DeviceArray<int32_t> d_idx((size_t)np * nm);
+  d_q.upload(q.data(), q.size());
+  check(rtr_knn1(ctx, d_q.p, np * nm, d_scene, ns, r, d_idx.p, d_d2.p, nullptr), "rtr_knn1");
+  std::vector<int32_t> idx((size_t)np * nm);
+  d_idx.download(idx.data(), idx.size());
+  for (int c = 0; c < np; ++c)
+    for (int i = 0; i < nm; ++i) out[(size_t)c] += idx[(size_t)c * nm + i] >= 0;
+  return out;
+}
+
+// function.h:35-109.  The reference scores candidate transforms and keeps
+// the best.  Here the candidates are the groups of geometric-consistency
+// grouping (bin 1 cm, at least 5 members, the configs' parameters), each
+// with its least-squares pose, verified as the library's recognition does:
+// each pose scored by the model points (mcloud) it brings within
+// 2 * inlier_r of a scene point (cloud), the 16 best refined by ICP
+// (30 iterations, 2 cm), and the refined pose with the most model points
+// within inlier_r kept (ties: the better first score).  As in main, the
+// result maps the scene onto the model (main applies it to `cloud`).
+// ransac_times is kept for the signature (the grouping is deterministic).
+// Identity when no group reaches 5 members.
+inline Eigen::Matrix4f Ransac(std::vector<PairPoint> pairpoint, int ransac_times, Cloud::Ptr cloud, Cloud::Ptr mcloud,
+                              float inlier_r = 0.01f) {
+  (void)ransac_times;
+  rtr_context* ctx = thread_context();
+  const int C = (int)pairpoint.size();
+  Eigen::Matrix4f best = Eigen::Matrix4f::Identity();
+  if (C == 0) return best;
+  std::vector<float> mk(4 * (size_t)C), sk(4 * (size_t)C), cd((size_t)C);
+  std::vector<int32_t> cm((size_t)C), cs((size_t)C);
+  for (int i = 0; i < C; ++i) {
+    const PairPoint& p = pairpoint[(size_t)i];
+    const pcl::PointXYZ a = p.point_i.Key_coordinate, b = p.point_j.Key_coordinate;
+    mk[4 * (size_t)i] = a.x, mk[4 * (size_t)i + 1] = a.y, mk[4 * (size_t)i + 2] = a.z, mk[4 * (size_t)i + 3] = 0.f;
+    sk[4 * (size_t)i] = b.x, sk[4 * (size_t)i + 1] = b.y, sk[4 * (size_t)i + 2] = b.z, sk[4 * (size_t)i + 3] = 0.f;
+    cm[(size_t)i] = i;
+    cs[(size_t)i] = i;
+    cd[(size_t)i] = p.distance2;
+  }
+  constexpr int kMaxClusters = 256, kMaxMembers = 128;
+  DeviceArray<float> d_mk(mk.size()), d_sk(sk.size()), d_cd(cd.size());
+  DeviceArray<int32_t> d_cm(cm.size()), d_cs(cs.size()), d_mem((size_t)kMaxClusters * kMaxMembers), d_sizes(kMaxClusters);
+  DeviceArray<double> d_poses((size_t)kMaxClusters * 16);
+  d_mk.upload(mk.data(), mk.size());
+  d_sk.upload(sk.data(), sk.size());
+  d_cd.upload(cd.data(), cd.size());
+  d_cm.upload(cm.data(), cm.size());
+  d_cs.upload(cs.data(), cs.size());
+  int ncl = 0;
+  check(rtr_gc_group(ctx, d_mk.p, d_sk.p, d_cm.p, d_cs.p, d_cd.p, C, 0.01f, 5, kMaxClusters, kMaxMembers, d_mem.p,
+                     d_sizes.p, d_poses.p, &ncl, nullptr),
+        "rtr_gc_group");
+  if (ncl <= 0) return best;
+  std::vector<double> poses((size_t)ncl * 16);
+  d_poses.download(poses.data(), poses.size());
+  const int ns = (int)cloud->size();
+  DeviceArray<float> d_s(4 * (size_t)ns);
+  d_s.upload(reinterpret_cast<const float*>(cloud->points.data()), 4 * (size_t)ns);
+  const std::vector<long long> first = pose_inliers(ctx, poses, *mcloud, d_s.p, ns, 2.f * inlier_r);
+  std::vector<int> order((size_t)ncl);
+  for (int c = 0; c < ncl; ++c) order[(size_t)c] = c;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return first[(size_t)x] > first[(size_t)y]; });
+  const int top = ncl < 16 ? ncl : 16;
+  rtr_icp_params ip;
+  rtr_icp_default_params(&ip);
+  ip.max_iterations = 30;
+  ip.max_corr_dist = 0.02f;
+  std::vector<double> refined((size_t)top * 16);
+  for (int k = 0; k < top; ++k) {
+    rtr_icp_result r;
+    check(rtr_icp_host(ctx, reinterpret_cast<const float*>(mcloud->points.data()), (int)mcloud->size(),
+                       reinterpret_cast<const float*>(cloud->points.data()), ns, &ip,
+                       &poses[(size_t)order[(size_t)k] * 16], &r),
+          "rtr_icp_host");
+    std::memcpy(&refined[(size_t)k * 16], r.pose, sizeof(r.pose));
+  }
+  const std::vector<long long> fin = pose_inliers(ctx, refined, *mcloud, d_s.p, ns, inlier_r);
+  int w = 0;
+  for (int k = 1; k < top; ++k)
+    if (fin[(size_t)k] > fin[(size_t)w]) w = k;
+  // model -> scene (R, t) inverted: scene -> model (R^T, -R^T t)
+  const double* T = &refined[(size_t)w * 16];
+  for (int r = 0; r < 3; ++r) {
+    double t = 0.0;
+    for (int c = 0; c < 3; ++c) {
+      best(r, c) = (float)T[c * 4 + r];
+      t -= T[c * 4 + r] * T[c * 4 + 3];
+    }
+    best(r, 3) = (float)t;
+  }
+  return best;
+}
+
+// function.h:111-148 without the viewer and the PCD files: ICP of mcloud
+// (source) onto cloud (target) with PCL's default settings, the final
+// transform printed as the reference does, and returned.  SpointCloud and
+// mPointCloud are kept for the signature.
+inline Eigen::Matrix4f keyPointICP_pose(Cloud::Ptr SpointCloud, Cloud::Ptr mPointCloud, Cloud::Ptr cloud, Cloud::Ptr mcloud,
+                                        const Eigen::Matrix4f* init = nullptr, int max_iterations = -1,
+                                        float max_corr_dist = -1.f) {
+  (void)SpointCloud;
+  (void)mPointCloud;
+  rtr_context* ctx = thread_context();
+  rtr_icp_params p;
+  rtr_icp_default_params(&p);
+  if (max_iterations > 0) p.max_iterations = max_iterations;
+  if (max_corr_dist > 0.f) p.max_corr_dist = max_corr_dist;
+  double T0[16];
+  if (init)
+    for (int i = 0; i < 16; ++i) T0[i] = (*init)(i / 4, i % 4);
+  rtr_icp_result r;
+  check(rtr_icp_host(ctx, reinterpret_cast<const float*>(mcloud->points.data()), (int)mcloud->size(),
+                     reinterpret_cast<const float*>(cloud->points.data()), (int)cloud->size(), &p, init ? T0 : nullptr,
+                     &r),
+        "rtr_icp_host");
+  Eigen::Matrix4f T;
+  for (int i = 0; i < 16; ++i) T(i / 4, i % 4) = (float)r.pose[i];
+  return T;
+}
+
+inline void keyPointICP(Cloud::Ptr SpointCloud, Cloud::Ptr mPointCloud, Cloud::Ptr cloud, Cloud::Ptr mcloud) {
+  const Eigen::Matrix4f T = keyPointICP_pose(SpointCloud, mPointCloud, cloud, mcloud);
+  std::cout << T << std::endl;
+}
+
+}  // namespace rtr_robot

@@ -1,0 +1,92 @@
+// realtime_robot_demo.cpp — main (RealTimeRobot.cpp:30-110) on the C++
+// entry points of realtime_robot.hpp, with seeded synthetic clouds in place
+// of the PCD files: the box chair as the model (chair1.pcd's role) and a
+// cropped, moved, noisy copy of it as the scan (T0_m8111.pcd's role).
+//
+// Flow as in main: ModelPoint / ScanPoint keypoints and descriptors, the
+// correspondence loop, Ransac (grouping, verification against the scan, ICP
+// refinement of the best candidates), the scan moved onto the model,
+// then keyPointICP refines model onto scan.  Prints the pair count, both
+// poses and their error against the generator's transform; exits 0 when the
+// refined pose is within 1 cm / 1 degree of it, 1 otherwise, 2 on an error.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <iostream>
+#include <vector>
+
+#include "realtime_robot.hpp"
+
+using rtr_robot::Cloud;
+
+static Cloud::Ptr to_cloud(const std::vector<float>& xyz4, int n) {
+  Cloud::Ptr c(new Cloud);
+  c->points.resize((size_t)n);
+  for (int i = 0; i < n; ++i) c->points[(size_t)i] = pcl::PointXYZ(xyz4[4 * i], xyz4[4 * i + 1], xyz4[4 * i + 2]);
+  c->width = (uint32_t)n;
+  return c;
+}
+
+// translation (m) and rotation (rad) between two model->scene poses
+static void pose_error(const Eigen::Matrix4f& A, const double* B, double* dt, double* dr) {
+  double t2 = 0.0, tr = 0.0;
+  for (int r = 0; r < 3; ++r) {
+    const double d = A(r, 3) - B[r * 4 + 3];
+    t2 += d * d;
+    for (int c = 0; c < 3; ++c) tr += (double)A(r, c) * B[r * 4 + c];  // trace(A_R^T B_R)
+  }
+  *dt = std::sqrt(t2);
+  *dr = std::acos(std::fmax(-1.0, std::fmin(1.0, 0.5 * (tr - 1.0))));
+}
+
+int main(int argc, char** argv) {
+  const unsigned long long seed = argc > 1 ? std::strtoull(argv[1], nullptr, 10) : 0ull;
+  try {
+    // the clouds (main loads chair1.pcd and T0_m8111.pcd)
+    const int n = 20000;
+    std::vector<float> model(4 * (size_t)n), part(4 * (size_t)n), scan(4 * (size_t)n);
+    rtr_robot::check(rtr_synth_shape(0, 2024, n, model.data()), "rtr_synth_shape");
+    rtr_robot::check(rtr_synth_shape(0, 500 + seed, n, part.data()), "rtr_synth_shape");
+    const int kept = rtr_synth_crop(part.data(), n, 0.4, seed, scan.data());
+    double T[16];
+    rtr_synth_rigid(100 + seed, 30.0, 0.3, T);
+    rtr_synth_transform_noise(scan.data(), kept, T, 0.002, 9 + seed, scan.data());
+    Cloud::Ptr mcloud = to_cloud(model, n), cloud = to_cloud(scan, kept);
+
+    rtr_robot::ModelPoint modelpoint(mcloud);
+    modelpoint.getKeypoint();
+    rtr_robot::ScanPoint scanpoint(cloud);
+    scanpoint.orient_outward = true;  // a segmented object, not one sensor view
+    scanpoint.getKeypoint();
+    std::vector<rtr_robot::PairPoint> pairpoint = rtr_robot::match_keypoints(modelpoint, scanpoint);
+    std::cout << "model keypoints " << modelpoint.n_kp << ", scan keypoints " << scanpoint.n_kp << ", pairs "
+              << pairpoint.size() << std::endl;
+
+    // Ransac gives scan -> model; main moves the scan with it
+    const Eigen::Matrix4f to_model = rtr_robot::Ransac(pairpoint, 20, cloud, mcloud);
+    Cloud::Ptr moved(new Cloud);
+    pcl::transformPointCloud(*cloud, *moved, to_model);
+    // keyPointICP refines model onto the (original) scan, starting from the
+    // grouping's pose inverted back to model -> scene
+    Eigen::Matrix4f init = Eigen::Matrix4f::Identity();
+    for (int r = 0; r < 3; ++r) {
+      float t = 0.f;
+      for (int c = 0; c < 3; ++c) {
+        init(r, c) = to_model(c, r);
+        t -= to_model(c, r) * to_model(c, 3);
+      }
+      init(r, 3) = t;
+    }
+    const Eigen::Matrix4f refined = rtr_robot::keyPointICP_pose(nullptr, nullptr, cloud, mcloud, &init, 30, 0.02f);
+    std::cout << refined;
+    double dt0, dr0, dt1, dr1;
+    pose_error(init, T, &dt0, &dr0);
+    pose_error(refined, T, &dt1, &dr1);
+    std::printf("grouping pose error %.4f m %.4f deg; refined %.4f m %.4f deg\n", dt0, dr0 * 57.29577951308232,
+                dt1, dr1 * 57.29577951308232);
+    return (dt1 < 0.01 && dr1 < 0.017453292519943295) ? 0 : 1;
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "error: %s\n", e.what());
+    return 2;
+  }
+}

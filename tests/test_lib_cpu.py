@@ -106,3 +106,18 @@ def test_compute_tdf_rejects_bad_sizes_without_touching_the_gpu(rtr):
     g = np.zeros(27000, np.float32)
     assert rtr.compute_tdf_with_cuda(np.zeros((1, 3), np.int32), g, 31) == 1  # cudaErrorInvalidValue
     assert rtr.lib().ComputeTDFWithCuda(None, g.ctypes.data, 30, -1) == 1
+
+
+def test_cpp_mirror_fails_cleanly_without_a_gpu(rtr):
+    """The C++ driver of the reference's entry points reports the missing
+    device through rtr_status (exit 2), not a crash."""
+    import subprocess
+    from pathlib import Path
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    demo = Path(__file__).resolve().parents[1] / "realtime_robot_gb300" / "realtime_robot_demo"
+    if not demo.exists():
+        pytest.skip("demo not built")
+    r = subprocess.run([str(demo)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2 and "RTR_ERR_NO_DEVICE" in r.stderr, (r.returncode, r.stderr)
