@@ -128,6 +128,91 @@ int ComputeTDFWithCuda(const int* voxel_grid_occ, float* voxel_grid_TDF,
 rtr_status rtr_tdf_batch(rtr_context* ctx, const int* d_occ, const int* d_offsets,
                          int n_keys, int dim, float* d_tdf, rtr_stream_t stream);
 
+/* ---- the reference's own descriptor route ---------------------------------
+ * The occupancy / TDF / 36-yaw matcher of main (RealTimeRobot.cpp:56-108),
+ * batched.  The reference builds a PCL octree per keypoint, per pair and per
+ * rotation; here an octree with a defined box is a cube of 2^depth leaves
+ * (leaf = integer key, depth-first order = Morton order with x the high bit),
+ * with PCL's rules for sizing the cube and growing it when a point lands
+ * outside (ceil((hi - lo - FLT_EPSILON) / res) leaves on the widest axis,
+ * padded equally on both sides; growth adds a level, the old cube becoming
+ * the upper half on every axis the point is not above; points are inserted
+ * in ascending cloud index).  All calls synchronise the stream. */
+
+/* KeyPoint::getOccupiedGrid (key_point.h:112-161) for n_keys keypoints over
+ * one cloud: the points inside [key - half_box, key + half_box] (float box,
+ * inclusive) as CSR d_offsets[n_keys + 1] / d_indices (ascending index), and
+ * d_number[k] = Occupiedgrid.Number, the occupied leaves of edge resolution
+ * in the octree of that box.  *h_total = the number of indices; when it
+ * exceeds cap_indices the call returns RTR_ERR_CAPACITY with offsets and
+ * numbers written (allocate and call again).  2 * half_box / resolution <= 30. */
+rtr_status rtr_ref_occupancy(rtr_context* ctx, const float* d_cloud, int n, const float* d_keys,
+                             int n_keys, float resolution, float half_box, int32_t* d_number,
+                             int32_t* d_offsets, int32_t* d_indices, long long cap_indices,
+                             long long* h_total, rtr_stream_t stream);
+
+/* KeyPoint::get_TSDF (key_point.h:251-334): from each keypoint's occupancy
+ * CSR, the occupied leaves of the +-half_tdf octree, the first in tree order
+ * dropped, as integer voxels (centre - box corner) / resolution, then the
+ * field of ComputeTDFWithCuda.  d_tdf: n_keys * dim^3 floats with
+ * dim = (int)(half_tdf / resolution * 2) (30 at the defaults 0.01 / 0.15),
+ * written to *h_dim.  A keypoint without occupied leaves gets 900
+ * everywhere (the reference allocates a negative-size array there). */
+rtr_status rtr_ref_tdf(rtr_context* ctx, const float* d_cloud, const float* d_keys, int n_keys,
+                       const int32_t* d_offsets, const int32_t* d_indices, float resolution,
+                       float half_tdf, float* d_tdf, int* h_dim, rtr_stream_t stream);
+
+/* get_Distance (matching.h:122-222) for n_pairs (model keypoint, scan
+ * keypoint) pairs, or for all n_model * n_scan pairs model-major when
+ * d_pair_m and d_pair_s are NULL.  The model keypoint's occupancy cloud is
+ * moved by (k - sk), turned 36 times by 10 degrees about the keypoint's
+ * vertical axis (cumulatively, in float), and each time its occupied leaves
+ * in the keypoint's field box (all but the first) read the field as
+ * grid[y*30 + z*900 + x]; the running score is (score + sum of squared field
+ * values) / (leaves - 1), the lowest wins.  d_score[p] = that score (float),
+ * d_T[16p] = the row-major 4x4 scale(kz/sz) * T(k) * Rz(best) * T(-k) *
+ * T(k - sk).  Definitions where the reference is undefined: a field index
+ * outside [0, 27000) reads 900; a cloud that would need more than 21 octree
+ * levels, or a non-finite keypoint, gives score NaN and the identity.  One
+ * change: each rotation's sum is exact (integers) and the running score is
+ * kept in double (the reference adds in float, leaf by leaf; the two agree
+ * to a few parts in 10^5).  The field must be 30^3 (half_tdf / resolution
+ * = 15); occupancy clouds of up to 8192 points whose rotated extent stays
+ * within 32 leaves (half_box <= 0.106 m at 1 cm). */
+rtr_status rtr_ref_distance(rtr_context* ctx, const float* d_mcloud, const float* d_mkeys,
+                            int n_model, const int32_t* d_moffsets, const int32_t* d_mindices,
+                            const float* d_mtdf, const float* d_skeys, int n_scan,
+                            const int32_t* d_pair_m, const int32_t* d_pair_s, long long n_pairs,
+                            float resolution, float half_tdf, float* d_score, float* d_T,
+                            rtr_stream_t stream);
+
+/* The all-pairs loop of main (RealTimeRobot.cpp:70-102): pair p = m * n_scan
+ * + s is kept when d_score_all[p] < max_score (3 in main) and the gates of
+ * function.h:158-178 pass as written: match_by_height passes unless the
+ * ratio is NaN (float(2/3) is 0), match_by_area rejects a ratio above 3 or
+ * below 0 (float(1/3) is 0) over the 3 plane areas per keypoint (d_*v3,
+ * NULL = the KeyPoint default 0.16), match_by_occupied keeps
+ * Number_m / Number_s (integer quotient) in [1, 2].  d_pair_idx gets the
+ * kept p ascending; *h_n_pairs their number (RTR_ERR_CAPACITY above cap). */
+rtr_status rtr_ref_correspond(rtr_context* ctx, const float* d_mkeys, const int32_t* d_mnumber,
+                              const double* d_mv3, int n_model, const float* d_skeys,
+                              const int32_t* d_snumber, const double* d_sv3, int n_scan,
+                              const float* d_score_all, float max_score, int32_t* d_pair_idx,
+                              int cap, int* h_n_pairs, rtr_stream_t stream);
+
+/* Ransac (function.h:35-109) over the kept pairs: pair i's transform
+ * (d_T_all[16 * p_i]) moves every kept pair's scan keypoint; pair j is an
+ * inlier when |k_j - T sk_j| < inlier_dist (0.15; float distance) and
+ * d_score_all[p_j] < max_des (100).  The first transform with the most
+ * inliers wins: h_T (16 floats, row-major; identity when no pair has an
+ * inlier, where the reference returns an uninitialised matrix), *h_inliers,
+ * *h_best = its position in d_pair_idx or -1. */
+rtr_status rtr_ref_ransac(rtr_context* ctx, const float* d_mkeys, int n_model, const float* d_skeys,
+                          int n_scan, const int32_t* d_pair_idx, int n_pairs,
+                          const float* d_score_all, const float* d_T_all, float inlier_dist,
+                          float max_des, float* h_T, int* h_inliers, int* h_best,
+                          rtr_stream_t stream);
+
 /* ---- nearest-neighbour search ---------------------------------------------
  * Exact searches over a radix-sorted uniform grid.  Squared distances are
  * computed in FP32 as ((dx*dx + dy*dy) + dz*dz) with dx = q.x - p.x, each

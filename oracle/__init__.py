@@ -44,6 +44,12 @@ _SIG = {
     "orc_match": (None, [_P, _I, _P, _I, _I, _P, _P]),
     "orc_gc_group": (_I, [_P, _P, _P, _P, _P, _I, _F, _I, _I, _P, _P, _P]),
     "orc_orient_outward": (None, [_P, _P, _I, _F, _F, _F]),
+    "orc_ref_occupancy": (C.c_longlong, [_P, _I, _P, _I, _F, _F, _P, _P, _P, C.c_longlong]),
+    "orc_ref_tdf": (_I, [_P, _P, _I, _P, _P, _F, _F, _P]),
+    "orc_ref_distance": (None, [_P, _P, _P, _P, _P, _I, _P, _I, _P, _P, C.c_longlong, _F, _F, _I, _P, _P]),
+    "orc_ref_gates": (_I, [_P, _I, _P, _P, _I, _P]),
+    "orc_ref_correspond": (C.c_longlong, [_P, _P, _P, _I, _P, _P, _P, _I, _P, _F, _P, C.c_longlong]),
+    "orc_ref_ransac": (_I, [_P, _P, _I, _P, _I, _P, _P, _F, _F, _P, _P]),
 }
 
 
@@ -254,3 +260,92 @@ def pose_error(Ta, Tb) -> tuple[float, float]:
     # accurate for small angles: use the skew part
     s = 0.5 * np.linalg.norm([Rd[2, 1] - Rd[1, 2], Rd[0, 2] - Rd[2, 0], Rd[1, 0] - Rd[0, 1]])
     return dt, float(np.arctan2(s, c))
+
+
+# ---- the reference's own descriptor route (refmatch.c) ---------------------
+def _i32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _ptr(a):
+    return a.ctypes.data if a is not None and a.size else None
+
+
+def ref_occupancy(cloud, keys, res: float = 0.01, half: float = 0.1):
+    """KeyPoint::getOccupiedGrid for every keypoint: (number, offsets,
+    indices), the box's points in ascending index order."""
+    cloud, keys = _f4(cloud), _f4(keys)
+    nk = keys.shape[0]
+    number = np.zeros(nk, np.int32)
+    offsets = np.zeros(nk + 1, np.int32)
+    total = lib().orc_ref_occupancy(_ptr(cloud), cloud.shape[0], _ptr(keys), nk, float(res), float(half),
+                                    _ptr(number), offsets.ctypes.data, None, 0)
+    indices = np.zeros(max(total, 1), np.int32)
+    lib().orc_ref_occupancy(_ptr(cloud), cloud.shape[0], _ptr(keys), nk, float(res), float(half), _ptr(number),
+                            offsets.ctypes.data, indices.ctypes.data, total)
+    return number, offsets, indices[:total]
+
+
+def ref_tdf(cloud, keys, offsets, indices, res: float = 0.01, half: float = 0.15) -> np.ndarray:
+    """KeyPoint::get_TSDF for every keypoint: [nk, dim^3] float32."""
+    cloud, keys, offsets, indices = _f4(cloud), _f4(keys), _i32(offsets), _i32(indices)
+    dim = int(np.float32(np.float32(half) / np.float32(res)) * np.float32(2))
+    out = np.zeros((keys.shape[0], dim ** 3), np.float32)
+    got = lib().orc_ref_tdf(_ptr(cloud), _ptr(keys), keys.shape[0], offsets.ctypes.data, _ptr(indices), float(res),
+                            float(half), _ptr(out))
+    if got != dim:
+        raise ValueError(f"dim {got} (expected {dim})")
+    return out
+
+
+def ref_distance(mcloud, mkeys, moff, midx, mtdf, skeys, pair_m=None, pair_s=None, res: float = 0.01,
+                 half: float = 0.15, float_order: bool = False):
+    """get_Distance for pairs (all model x scan pairs, model-major, when
+    pair_m is None): (score [P] float32, T [P, 4, 4] float32)."""
+    mcloud, mkeys, skeys = _f4(mcloud), _f4(mkeys), _f4(skeys)
+    moff, midx = _i32(moff), _i32(midx)
+    mtdf = np.ascontiguousarray(mtdf, np.float32)
+    nm, ns = mkeys.shape[0], skeys.shape[0]
+    if pair_m is None:
+        pm = ps = None
+        P = nm * ns
+    else:
+        pm, ps = _i32(pair_m), _i32(pair_s)
+        P = pm.shape[0]
+    score = np.zeros(P, np.float32)
+    T = np.zeros((P, 4, 4), np.float32)
+    lib().orc_ref_distance(_ptr(mcloud), _ptr(mkeys), moff.ctypes.data, _ptr(midx), _ptr(mtdf), nm, _ptr(skeys), ns,
+                           _ptr(pm), _ptr(ps), P, float(res), float(half), int(bool(float_order)), _ptr(score),
+                           _ptr(T))
+    return score, T
+
+
+def ref_correspond(mkeys, mnum, skeys, snum, score_all, max_score: float = 3.0, mv3=None, sv3=None) -> np.ndarray:
+    """The all-pairs loop with its gates: indices p = m * ns + s of the kept
+    pairs, ascending."""
+    mkeys, skeys = _f4(mkeys), _f4(skeys)
+    mnum, snum = _i32(mnum), _i32(snum)
+    score_all = np.ascontiguousarray(score_all, np.float32)
+    mv3 = None if mv3 is None else np.ascontiguousarray(mv3, np.float64)
+    sv3 = None if sv3 is None else np.ascontiguousarray(sv3, np.float64)
+    nm, ns = mkeys.shape[0], skeys.shape[0]
+    args = (_ptr(mkeys), _ptr(mnum), _ptr(mv3), nm, _ptr(skeys), _ptr(snum), _ptr(sv3), ns, _ptr(score_all),
+            float(max_score))
+    c = lib().orc_ref_correspond(*args, None, 0)
+    out = np.zeros(max(c, 1), np.int32)
+    lib().orc_ref_correspond(*args, out.ctypes.data, c)
+    return out[:c]
+
+
+def ref_ransac(mkeys, skeys, pair_idx, score_all, T_all, inlier: float = 0.15, max_des: float = 100.0):
+    """Ransac over the kept pairs: (T [4, 4] float32, inliers, position of
+    the winner in pair_idx or -1)."""
+    mkeys, skeys, pair_idx = _f4(mkeys), _f4(skeys), _i32(pair_idx)
+    score_all = np.ascontiguousarray(score_all, np.float32)
+    T_all = np.ascontiguousarray(T_all, np.float32)
+    T = np.zeros((4, 4), np.float32)
+    inl = np.zeros(1, np.int32)
+    best = lib().orc_ref_ransac(_ptr(mkeys), _ptr(skeys), skeys.shape[0], _ptr(pair_idx), pair_idx.shape[0],
+                                _ptr(score_all), _ptr(T_all), float(inlier), float(max_des), T.ctypes.data,
+                                inl.ctypes.data)
+    return T, int(inl[0]), int(best)

@@ -99,6 +99,24 @@ int orc_gc_group(const float* model_kp, const float* scene_kp, const int32_t* co
                  const int32_t* corr_s, const float* corr_d, int nc, float gc_size, int gc_thresh,
                  int max_clusters, int32_t* cluster_of, double* poses16, int32_t* sizes);
 
+/* ---- the reference's own descriptor route (refmatch.c) */
+long long orc_ref_occupancy(const float* cloud, int n, const float* keys, int nk, float res, float half,
+                            int32_t* number, int32_t* offsets, int32_t* indices, long long cap);
+int orc_ref_tdf(const float* cloud, const float* keys, int nk, const int32_t* offsets, const int32_t* indices,
+                float res, float half, float* tdf);
+void orc_ref_distance(const float* mcloud, const float* mkeys, const int32_t* moff, const int32_t* midx,
+                      const float* mtdf, int nm, const float* skeys, int ns, const int32_t* pair_m,
+                      const int32_t* pair_s, long long np, float res, float half, int float_order, float* score,
+                      float* T);
+int orc_ref_gates(const float* km, int nm_number, const double* mv3, const float* ks, int ns_number,
+                  const double* sv3);
+long long orc_ref_correspond(const float* mkeys, const int32_t* mnum, const double* mv3, int nm, const float* skeys,
+                             const int32_t* snum, const double* sv3, int ns, const float* score_all,
+                             float max_score, int32_t* pair_idx, long long cap);
+int orc_ref_ransac(const float* mkeys, const float* skeys, int ns, const int32_t* pair_idx, int np,
+                   const float* score_all, const float* T_all, float inlier, float max_des, float* T_out,
+                   int32_t* best_inliers);
+
 #ifdef __cplusplus
 }
 #endif

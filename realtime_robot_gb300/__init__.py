@@ -125,6 +125,12 @@ _SIG = {
     "rtr_launch_count": (C.c_uint64, []),
     "ComputeTDFWithCuda": (_I, [_P, _P, _I, _I]),
     "rtr_tdf_batch": (_I, [_P, _P, _P, _I, _I, _P, _P]),
+    "rtr_ref_occupancy": (_I, [_P, _P, _I, _P, _I, _F, _F, _P, _P, _P, C.c_longlong, C.POINTER(C.c_longlong), _P]),
+    "rtr_ref_tdf": (_I, [_P, _P, _P, _I, _P, _P, _F, _F, _P, C.POINTER(C.c_int), _P]),
+    "rtr_ref_distance": (_I, [_P, _P, _P, _I, _P, _P, _P, _P, _I, _P, _P, C.c_longlong, _F, _F, _P, _P, _P]),
+    "rtr_ref_correspond": (_I, [_P, _P, _P, _P, _I, _P, _P, _P, _I, _P, _F, _P, _I, C.POINTER(C.c_int), _P]),
+    "rtr_ref_ransac": (_I, [_P, _P, _I, _P, _I, _P, _I, _P, _P, _F, _F, _P, C.POINTER(C.c_int),
+                            C.POINTER(C.c_int), _P]),
     "rtr_knn1": (_I, [_P, _P, _I, _P, _I, _F, _P, _P, _P]),
     "rtr_knn1_static": (_I, [_P, _I, _P, _I, _F, _P, _P, _P]),
     "rtr_knn": (_I, [_P, _P, _I, _P, _I, _I, _P, _P, _P]),
@@ -497,6 +503,80 @@ class Context:
         return mem[:k], sizes[:k], poses[:k].reshape(k, 4, 4)
 
     # -- TDF ------------------------------------------------------------------
+    # ---- the reference's own descriptor route (rtr_ref_*) -----------------
+    def ref_occupancy(self, cloud, keys, resolution: float = 0.01, half_box: float = 0.1, stream=None):
+        """KeyPoint::getOccupiedGrid for every keypoint: (number [nk] int32,
+        offsets [nk+1] int32, indices [total] int32), device tensors."""
+        import torch
+        nk = keys.shape[0]
+        dev = keys.device
+        number = torch.empty(nk, dtype=torch.int32, device=dev)
+        offsets = torch.empty(nk + 1, dtype=torch.int32, device=dev)
+        total = C.c_longlong(0)
+        cap = 1 << 16
+        for _ in range(2):
+            indices = torch.empty(max(cap, 1), dtype=torch.int32, device=dev)
+            st = lib().rtr_ref_occupancy(self.h, _ptr(cloud), cloud.shape[0], _ptr(keys), nk, float(resolution),
+                                         float(half_box), _ptr(number), _ptr(offsets), _ptr(indices), cap,
+                                         C.byref(total), _stream(stream))
+            if st == 6 and total.value > cap:  # RTR_ERR_CAPACITY: allocate and call again
+                cap = total.value
+                continue
+            check(st)
+            return number, offsets, indices[:total.value]
+        raise RtrError(6, "rtr_ref_occupancy: capacity")
+
+    def ref_tdf(self, cloud, keys, offsets, indices, resolution: float = 0.01, half_tdf: float = 0.15,
+                stream=None):
+        """KeyPoint::get_TSDF for every keypoint: [nk, dim^3] float32."""
+        import torch
+        nk = keys.shape[0]
+        dim = int(np.float32(np.float32(half_tdf) / np.float32(resolution)) * np.float32(2))
+        out = torch.empty((nk, max(dim, 1) ** 3), dtype=torch.float32, device=keys.device)
+        got = C.c_int(0)
+        check(lib().rtr_ref_tdf(self.h, _ptr(cloud), _ptr(keys), nk, _ptr(offsets), _ptr(indices),
+                                float(resolution), float(half_tdf), _ptr(out), C.byref(got), _stream(stream)))
+        return out
+
+    def ref_distance(self, mcloud, mkeys, moffsets, mindices, mtdf, skeys, pair_m=None, pair_s=None,
+                     resolution: float = 0.01, half_tdf: float = 0.15, stream=None):
+        """get_Distance for explicit pairs, or all model x scan pairs
+        (model-major) when pair_m is None: (score [P], T [P, 4, 4])."""
+        import torch
+        nm, ns = mkeys.shape[0], skeys.shape[0]
+        P = nm * ns if pair_m is None else pair_m.shape[0]
+        score = torch.empty(P, dtype=torch.float32, device=mkeys.device)
+        T = torch.empty((P, 4, 4), dtype=torch.float32, device=mkeys.device)
+        check(lib().rtr_ref_distance(self.h, _ptr(mcloud), _ptr(mkeys), nm, _ptr(moffsets), _ptr(mindices),
+                                     _ptr(mtdf), _ptr(skeys), ns, _ptr(pair_m), _ptr(pair_s), P,
+                                     float(resolution), float(half_tdf), _ptr(score), _ptr(T), _stream(stream)))
+        return score, T
+
+    def ref_correspond(self, mkeys, mnumber, skeys, snumber, score_all, max_score: float = 3.0, mv3=None,
+                       sv3=None, stream=None):
+        """The all-pairs loop with its gates: kept pair indices
+        p = m * n_scan + s, ascending (device int32)."""
+        import torch
+        nm, ns = mkeys.shape[0], skeys.shape[0]
+        cap = max(nm * ns, 1)
+        out = torch.empty(cap, dtype=torch.int32, device=mkeys.device)
+        n = C.c_int(0)
+        check(lib().rtr_ref_correspond(self.h, _ptr(mkeys), _ptr(mnumber), _ptr(mv3), nm, _ptr(skeys),
+                                       _ptr(snumber), _ptr(sv3), ns, _ptr(score_all), float(max_score), _ptr(out),
+                                       cap, C.byref(n), _stream(stream)))
+        return out[:n.value]
+
+    def ref_ransac(self, mkeys, skeys, pair_idx, score_all, T_all, inlier: float = 0.15, max_des: float = 100.0,
+                   stream=None):
+        """Ransac over the kept pairs: (T [4, 4] numpy float32, inliers,
+        position of the winner in pair_idx or -1)."""
+        T = np.zeros(16, np.float32)
+        inl, best = C.c_int(0), C.c_int(-1)
+        check(lib().rtr_ref_ransac(self.h, _ptr(mkeys), mkeys.shape[0], _ptr(skeys), skeys.shape[0],
+                                   _ptr(pair_idx), pair_idx.shape[0], _ptr(score_all), _ptr(T_all), float(inlier),
+                                   float(max_des), T.ctypes.data, C.byref(inl), C.byref(best), _stream(stream)))
+        return T.reshape(4, 4), inl.value, best.value
+
     def tdf_batch(self, occ, offsets, dim: int, stream=None):
         import torch
         n = offsets.shape[0] - 1

@@ -12,6 +12,10 @@ Fixtures:
     RealTimeRobot/5.pcd -> mcloud.pcd, a translation by (+0.8, +0.8, 0), the
     keyPointICP input pair, function.h:111-127) and the recorded failure
     transformed_cloud.pcd (an uninitialised pose applied, function.h:39,108).
+  main_clouds.npz — the two clouds main registers (RealTimeRobot.cpp:34-35):
+    chair1.pcd, the model (1,818 points), and T0_m8111.pcd, the scan
+    (3,218 points); the inputs of the reference's own descriptor route
+    (occupancy grids, TDF, get_Distance, Ransac).
 """
 from __future__ import annotations
 
@@ -81,6 +85,9 @@ def main(ref_root: str) -> None:
     np.savez_compressed(HERE / "pcd_pairs.npz", p70761=a, p70761_c=ac, p5=b, mcloud=bm,
                         t70761=np.array([1.0, 0.5, 0.0]), t5=np.array([0.8, 0.8, 0.0]),
                         transformed_cloud_head=bad[:16])
+    chair, scan = read_pcd(d / "chair1.pcd"), read_pcd(d / "T0_m8111.pcd")
+    print(f"chair1 {chair.shape[0]} points, T0_m8111 {scan.shape[0]} points")
+    np.savez_compressed(HERE / "main_clouds.npz", chair1=chair, T0_m8111=scan)
 
 
 if __name__ == "__main__":
