@@ -396,11 +396,12 @@ def run_ours(args):
                         "algorithmic_bytes_per_launch": icp_bytes},
            "pose_error_vs_truth": list(O.pose_error(ir["pose"], T))}
 
-    batch = streaming = learned_room = None
+    batch = streaming = learned_room = ref_route = None
     if not args.no_extra:
         mlp, batch = batch_block(ctx, R, args.steps)
         learned_room = learned_room_block(ctx, R, m, s_d, prm, mlp, args.steps, stream, flush, r)
         streaming = stream_block(ctx, R, mlp)
+        ref_route = ref_route_block(ctx, R, args.steps, rank == 0 and ws == 1 and not args.no_cpu_baseline)
 
     line = {
         "metric": METRIC, "value": value, "unit": "recognitions/s", "n_gpus": ws, "steps": args.steps,
@@ -421,6 +422,7 @@ def run_ours(args):
         "batch": batch,
         "learned_room": learned_room,
         "streaming": streaming,
+        "reference_route": ref_route,
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_recognition_sample(scene, model)
@@ -539,6 +541,71 @@ def learned_room_block(ctx, R, m, s_d, prm, mlp, steps, stream, flush, plain) ->
             "unit": "recognitions/s", "ms_per_step": ms, "n_keypoints_matched": rl["n_keypoints"],
             "n_correspondences": rl["n_correspondences"], "instances": len(rl["instances"]),
             "agrees_with_plain_1cm": bool(same)}
+
+
+def ref_route_block(ctx, R, steps: int, cpu: bool) -> dict:
+    """The reference's own descriptor route (occupancy grids, TDF fields,
+    36-yaw get_Distance over every model x scan keypoint pair, the gated
+    all-pairs loop, Ransac) on main's own inputs: chair1.pcd (1,818 points)
+    and T0_m8111.pcd (3,218 points), keypoints by uniform sampling at 5 cm.
+    Each step runs the whole route from the device clouds (every call
+    synchronises); get_Distance is also timed alone with CUDA events."""
+    import torch
+    d = np.load(Path(__file__).resolve().parent / "tests" / "golden" / "main_clouds.npz")
+    model, scan = d["chair1"], d["T0_m8111"]
+    dm, ds = torch.from_numpy(model).cuda(), torch.from_numpy(scan).cuda()
+    dkm = dm[ctx.uniform_sample(dm, 0.05).long()].contiguous()
+    dks = ds[ctx.uniform_sample(ds, 0.05).long()].contiguous()
+    nm, ns = dkm.shape[0], dks.shape[0]
+
+    def route():
+        mn, mo, mi = ctx.ref_occupancy(dm, dkm)
+        sn, _, _ = ctx.ref_occupancy(ds, dks)
+        tdf = ctx.ref_tdf(dm, dkm, mo, mi)
+        sc, T = ctx.ref_distance(dm, dkm, mo, mi, tdf, dks)
+        pi = ctx.ref_correspond(dkm, mn, dks, sn, sc)
+        Tb, inl, best = ctx.ref_ransac(dkm, dks, pi, sc, T) if pi.shape[0] else (None, 0, -1)
+        return (mn, mo, mi, tdf), pi, inl
+
+    for _ in range(2):
+        route()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        occ, pi, inl = route()
+    route_ms = (time.perf_counter() - t0) * 1e3 / steps
+    mn, mo, mi, tdf = occ
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dist_ms = []
+    for _ in range(steps):
+        a.record()
+        ctx.ref_distance(dm, dkm, mo, mi, tdf, dks)
+        b.record()
+        torch.cuda.synchronize()
+        dist_ms.append(a.elapsed_time(b))
+    dms = float(np.median(dist_ms))
+    out = {"metric": "get_Distance pairs/s and route ms (main's clouds: chair1.pcd x T0_m8111.pcd, 5 cm keypoints)",
+           "model_keypoints": nm, "scan_keypoints": ns, "pairs": nm * ns,
+           "value": nm * ns / (dms * 1e-3), "unit": "pairs/s", "get_distance_ms": dms, "route_ms": route_ms,
+           "kept_pairs": int(pi.shape[0]), "ransac_inliers": int(inl),
+           "occupancy_points_max": int((mo[1:] - mo[:-1]).max().item())}
+    if cpu:
+        # the oracle (oracle/refmatch.c, all host threads) on the first model
+        # keypoints' pairs, a bounded sample of the same workload
+        import oracle as O
+        km, ks = dkm.cpu().numpy(), dks.cpu().numpy()
+        rmo, rmi = mo.cpu().numpy(), mi.cpu().numpy()
+        rtdf = tdf.cpu().numpy()
+        take = max(1, min(nm, 24))
+        pm = np.repeat(np.arange(take, dtype=np.int32), ns)
+        ps = np.tile(np.arange(ns, dtype=np.int32), take)
+        t0 = time.perf_counter()
+        O.ref_distance(model, km, rmo, rmi, rtdf, ks, pm, ps)
+        cs = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": pm.shape[0] / cs, "unit": "pairs/s", "cores": O.num_threads(),
+                               "kind": "port", "sample": f"get_Distance of the first {take} model keypoints x all "
+                               f"{ns} scan keypoints ({pm.shape[0]} pairs)"}
+    return out
 
 
 def stream_block(ctx, R, mlp) -> dict:

@@ -131,22 +131,79 @@ __device__ __forceinline__ unsigned oct_key1(const OctBox& b, float p, int a, do
   return v > top ? top : v;
 }
 
-__device__ __forceinline__ unsigned long long morton3(unsigned kx, unsigned ky, unsigned kz, int depth) {
-  unsigned long long m = 0;
-  for (int l = depth - 1; l >= 0; --l)
-    m = (m << 3) | ((unsigned long long)((kx >> l) & 1u) << 2) | ((unsigned long long)((ky >> l) & 1u) << 1) |
-        (unsigned long long)((kz >> l) & 1u);
-  return m;
+// The cube's float view.  For a float p and a double bound c, p < c exactly
+// when p < (c rounded up to float), and p >= c exactly when p >= (c rounded
+// up): no float lies strictly between c and its upward rounding.  So the
+// inside test needs no double arithmetic.
+struct OctBoxF {
+  float mn_up[3], mx_up[3], mn_f[3];
+};
+
+__device__ __forceinline__ void oct_float(const OctBox& b, OctBoxF& f) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    f.mn_up[a] = __double2float_ru(b.mn[a]);
+    f.mx_up[a] = __double2float_ru(b.mx[a]);
+    f.mn_f[a] = __double2float_rn(b.mn[a]);
+  }
 }
 
-__device__ __forceinline__ void demorton3(unsigned long long m, int depth, unsigned& kx, unsigned& ky,
-                                          unsigned& kz) {
-  kx = ky = kz = 0;
-  for (int l = 0; l < depth; ++l) {
-    kz |= (unsigned)((m >> (3 * l)) & 1ull) << l;
-    ky |= (unsigned)((m >> (3 * l + 1)) & 1ull) << l;
-    kx |= (unsigned)((m >> (3 * l + 2)) & 1ull) << l;
+__device__ __forceinline__ bool oct_outside_f(const OctBoxF& f, float x, float y, float z) {
+  return x < f.mn_up[0] || y < f.mn_up[1] || z < f.mn_up[2] || x >= f.mx_up[0] || y >= f.mx_up[1] ||
+         z >= f.mx_up[2];
+}
+
+// oct_key1 with a float estimate first: y = (p - min) * (1/res) in float is
+// within (|min|/res + 3|y|) * 2^-24 of the exact quotient t, so when y is
+// farther than four times that from every integer, floor(y) = floor(t) =
+// the double-precision key.  Otherwise (a few keys in 10^5) the double path.
+__device__ __forceinline__ unsigned oct_key_f(const OctBox& b, const OctBoxF& f, float p, int a, double res,
+                                              float inv) {
+  const float y = __fmul_rn(__fsub_rn(p, f.mn_f[a]), inv);
+  const float fl = floorf(y);
+  const float gap = fminf(__fsub_rn(y, fl), __fsub_rn(__fadd_rn(fl, 1.f), y));
+  const float margin = __fmul_rn(__fadd_rn(__fadd_rn(__fmul_rn(fabsf(f.mn_f[a]), inv), __fmul_rn(4.f, fabsf(y))), 4.f),
+                                 2.4e-7f);
+  if (gap > margin && fl >= 0.f && fl < 4194304.f) {
+    const unsigned top = (1u << b.depth) - 1u;
+    const unsigned v = (unsigned)fl;
+    return v > top ? top : v;
   }
+  return oct_key1(b, p, a, res);
+}
+
+// Morton code of a key (each coordinate < 2^21): the bits of x, y, z
+// interleaved with x the high bit of each triple, so ascending codes list the
+// leaves depth-first in child order (x << 2 | y << 1 | z) at any depth.
+__device__ __forceinline__ unsigned long long spread3(unsigned v) {
+  unsigned long long x = v & 0x1fffffu;
+  x = (x | x << 32) & 0x1f00000000ffffull;
+  x = (x | x << 16) & 0x1f0000ff0000ffull;
+  x = (x | x << 8) & 0x100f00f00f00f00full;
+  x = (x | x << 4) & 0x10c30c30c30c30c3ull;
+  x = (x | x << 2) & 0x1249249249249249ull;
+  return x;
+}
+
+__device__ __forceinline__ unsigned compact3(unsigned long long x) {
+  x &= 0x1249249249249249ull;
+  x = (x ^ (x >> 2)) & 0x10c30c30c30c30c3ull;
+  x = (x ^ (x >> 4)) & 0x100f00f00f00f00full;
+  x = (x ^ (x >> 8)) & 0x1f0000ff0000ffull;
+  x = (x ^ (x >> 16)) & 0x1f00000000ffffull;
+  x = (x ^ (x >> 32)) & 0x1fffffull;
+  return (unsigned)x;
+}
+
+__device__ __forceinline__ unsigned long long morton3(unsigned kx, unsigned ky, unsigned kz, int /*depth*/) {
+  return (spread3(kx) << 2) | (spread3(ky) << 1) | spread3(kz);
+}
+
+__device__ __forceinline__ void demorton3(unsigned long long m, int /*depth*/, unsigned& kx, unsigned& ky,
+                                          unsigned& kz) {
+  kx = compact3(m >> 2);
+  ky = compact3(m >> 1);
+  kz = compact3(m);
 }
 
 __device__ __forceinline__ float oct_centre(const OctBox& b, unsigned key, int a, double res) {
@@ -377,6 +434,21 @@ __device__ __forceinline__ float field_at(const float* __restrict__ grid, const 
   return (idx >= 0 && idx < REF_VOL) ? __ldg(grid + idx) : 900.f;
 }
 
+// field_at from the leaf centres (cx, cy, cz).
+__device__ __forceinline__ float field_at_c(const float* __restrict__ grid, float cx, float cy, float cz,
+                                            const float lo[3], float res) {
+  const float c[3] = {cx, cy, cz};
+  long long ix[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float q = __fdiv_rn(__fsub_rn(c[a], lo[a]), res);
+    if (!(q > -2147483648.f && q < 2147483648.f)) return 900.f;
+    ix[a] = (long long)__float2int_rz(q);
+  }
+  const long long idx = ix[1] * REF_DIM + ix[2] * (REF_DIM * REF_DIM) + ix[0];
+  return (idx >= 0 && idx < REF_VOL) ? __ldg(grid + idx) : 900.f;
+}
+
 template <int NT>
 __global__ void __launch_bounds__(NT) k_ref_distance(const float4* __restrict__ mcloud,
                                                      const float4* __restrict__ mkeys,
@@ -406,6 +478,7 @@ __global__ void __launch_bounds__(NT) k_ref_distance(const float4* __restrict__ 
   const int beg = moff[m], n = moff[m + 1] - beg;
   const float* grid = mtdf + (size_t)m * REF_VOL;
   const double dres = (double)res;
+  const float inv = __fdiv_rn(1.f, res);
   const float lo[3] = {__fsub_rn(km.x, half), __fsub_rn(km.y, half), __fsub_rn(km.z, half)};
   const float hi[3] = {__fadd_rn(km.x, half), __fadd_rn(km.y, half), __fadd_rn(km.z, half)};
   float Tm[16], T1[16], T3[16], M[16];
@@ -447,12 +520,14 @@ __global__ void __launch_bounds__(NT) k_ref_distance(const float4* __restrict__ 
     // the tree's growth, point by point in index order: every thread keeps
     // the same cube, grown by the first point outside it until none is
     OctBox b = b0;
+    OctBoxF bf;
+    oct_float(b, bf);
     for (int round = 0; round < 4 * REF_MAX_DEPTH + 4; ++round) {
       int first = 0x7fffffff;
 #pragma unroll
       for (int q = 0; q < REF_PPT; ++q) {
         const int j = tid + q * NT;
-        if (j < n && first == 0x7fffffff && oct_outside(b, px[q], py[q], pz[q])) first = j;
+        if (j < n && first == 0x7fffffff && oct_outside_f(bf, px[q], py[q], pz[q])) first = j;
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) first = min(first, __shfl_xor_sync(0xffffffffu, first, o));
@@ -470,6 +545,7 @@ __global__ void __launch_bounds__(NT) k_ref_distance(const float4* __restrict__ 
       }
       __syncthreads();
       if (!oct_fit(b, sh.px, sh.py, sh.pz, dres)) bad = true;
+      oct_float(b, bf);
       __syncthreads();
       if (bad) break;
     }
@@ -482,8 +558,8 @@ __global__ void __launch_bounds__(NT) k_ref_distance(const float4* __restrict__ 
     for (int q = 0; q < REF_PPT; ++q) {
       mc[q] = ~0ull;
       if (tid + q * NT < n) {
-        const unsigned kx = oct_key1(b, px[q], 0, dres), ky = oct_key1(b, py[q], 1, dres),
-                       kz = oct_key1(b, pz[q], 2, dres);
+        const unsigned kx = oct_key_f(b, bf, px[q], 0, dres, inv), ky = oct_key_f(b, bf, py[q], 1, dres, inv),
+                       kz = oct_key_f(b, bf, pz[q], 2, dres, inv);
         mc[q] = morton3(kx, ky, kz, b.depth);
         mmin = min(mmin, mc[q]);
         kmin[0] = min(kmin[0], kx), kmin[1] = min(kmin[1], ky), kmin[2] = min(kmin[2], kz);
@@ -571,6 +647,212 @@ __global__ void __launch_bounds__(NT) k_ref_distance(const float4* __restrict__ 
   mm4(A, T1, A);
   mm4(A, Tm, A);
   for (int i = 0; i < 16; ++i) To[i] = A[i];
+}
+
+// get_Distance, one warp per pair, for occupancy clouds of up to 256 points
+// (8 per lane): the same steps as k_ref_distance with every reduction a
+// shuffle, the growth's point broadcast by shuffle, and the warp's own 4 KB
+// bitmap cleared by the points that set it.
+constexpr int REFW_PPT = 8;
+constexpr int REFW_WARPS = 8;
+
+__global__ void __launch_bounds__(32 * REFW_WARPS, 2)
+    k_ref_distance_warp(const float4* __restrict__ mcloud, const float4* __restrict__ mkeys,
+                        const int* __restrict__ moff, const int* __restrict__ midx, const float* __restrict__ mtdf,
+                        const float4* __restrict__ skeys, int ns, const int* __restrict__ pair_m,
+                        const int* __restrict__ pair_s, long long n_pairs, float res, float half, RefRot rot,
+                        float* __restrict__ score, float* __restrict__ Tout, int* __restrict__ err) {
+  __shared__ unsigned s_bm[REFW_WARPS][REF_WIN * REF_WIN * REF_WIN / 32];
+  __shared__ long long s_ix[REFW_WARPS][3][REF_WIN];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned* bm = s_bm[w];
+  const float inv = __fdiv_rn(1.f, res);
+  for (int i = lane; i < REF_WIN * REF_WIN * REF_WIN / 32; i += 32) bm[i] = 0u;
+  __syncwarp();
+  const double dres = (double)res;
+  for (long long p = (long long)blockIdx.x * REFW_WARPS + w; p < n_pairs; p += (long long)gridDim.x * REFW_WARPS) {
+    const int m = pair_m ? pair_m[p] : (int)(p / ns);
+    const int s = pair_s ? pair_s[p] : (int)(p % ns);
+    const float4 km = mkeys[m], ks = skeys[s];
+    float* To = Tout + 16 * p;
+    if (!(isfinite(km.x) && isfinite(km.y) && isfinite(km.z) && isfinite(ks.x) && isfinite(ks.y) &&
+          isfinite(ks.z))) {
+      if (lane == 0) {
+        score[p] = __int_as_float(0x7fc00000);
+        eye4(To);
+      }
+      continue;
+    }
+    const int beg = moff[m], n = moff[m + 1] - beg;
+    const float* grid = mtdf + (size_t)m * REF_VOL;
+    const float lo[3] = {__fsub_rn(km.x, half), __fsub_rn(km.y, half), __fsub_rn(km.z, half)};
+    const float hi[3] = {__fadd_rn(km.x, half), __fadd_rn(km.y, half), __fadd_rn(km.z, half)};
+    float Tm[16], T1[16], T3[16], M[16];
+    eye4(Tm);
+    Tm[3] = __fsub_rn(km.x, ks.x), Tm[7] = __fsub_rn(km.y, ks.y), Tm[11] = __fsub_rn(km.z, ks.z);
+    eye4(T1);
+    T1[3] = -km.x, T1[7] = -km.y;
+    eye4(T3);
+    T3[3] = km.x, T3[7] = km.y;
+    {
+      float Rs[16];
+      eye4(Rs);
+      Rs[0] = rot.c1, Rs[4] = rot.s1, Rs[1] = -rot.s1, Rs[5] = rot.c1;
+      mm4(T3, Rs, M);
+      mm4(M, T1, M);
+    }
+    float px[REFW_PPT], py[REFW_PPT], pz[REFW_PPT];
+#pragma unroll
+    for (int q = 0; q < REFW_PPT; ++q) {
+      const int j = lane + 32 * q;
+      px[q] = py[q] = pz[q] = 0.f;
+      if (j < n) {
+        const float4 c = mcloud[midx[beg + j]];
+        px[q] = c.x, py[q] = c.y, pz[q] = c.z;
+        xf3(Tm, px[q], py[q], pz[q]);
+      }
+    }
+    OctBox b0;
+    oct_define(b0, lo, hi, dres);
+    double dt = 0.0, best = 100000000.0;
+    int best_i = 0;
+    bool bad = false;
+    for (int it = 0; it < 36 && !bad; ++it) {
+      if (it != 0) {
+#pragma unroll
+        for (int q = 0; q < REFW_PPT; ++q)
+          if (lane + 32 * q < n) xf3(M, px[q], py[q], pz[q]);
+      }
+      OctBox b = b0;
+      OctBoxF bf;
+      oct_float(b, bf);
+      for (int round = 0; round < 4 * REF_MAX_DEPTH + 4; ++round) {
+        int first = 0x7fffffff;
+#pragma unroll
+        for (int q = 0; q < REFW_PPT; ++q) {
+          const int j = lane + 32 * q;
+          if (j < n && first == 0x7fffffff && oct_outside_f(bf, px[q], py[q], pz[q])) first = j;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) first = min(first, __shfl_xor_sync(0xffffffffu, first, o));
+        if (first == 0x7fffffff) break;
+        const int q0 = first >> 5, src = first & 31;
+        float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+        for (int q = 0; q < REFW_PPT; ++q)
+          if (q == q0) sx = px[q], sy = py[q], sz = pz[q];
+        sx = __shfl_sync(0xffffffffu, sx, src);
+        sy = __shfl_sync(0xffffffffu, sy, src);
+        sz = __shfl_sync(0xffffffffu, sz, src);
+        if (!oct_fit(b, sx, sy, sz, dres)) {
+          bad = true;
+          break;
+        }
+        oct_float(b, bf);
+      }
+      if (bad) break;
+      // keys packed 21 bits per axis; the Morton code only for the first leaf
+      unsigned long long pk[REFW_PPT];
+      unsigned long long mmin = ~0ull;
+      unsigned kmin[3] = {~0u, ~0u, ~0u}, kmax[3] = {0u, 0u, 0u};
+#pragma unroll
+      for (int q = 0; q < REFW_PPT; ++q) {
+        pk[q] = ~0ull;
+        if (lane + 32 * q < n) {
+          const unsigned kx = oct_key_f(b, bf, px[q], 0, dres, inv), ky = oct_key_f(b, bf, py[q], 1, dres, inv),
+                         kz = oct_key_f(b, bf, pz[q], 2, dres, inv);
+          pk[q] = (unsigned long long)kx | ((unsigned long long)ky << 21) | ((unsigned long long)kz << 42);
+          mmin = min(mmin, morton3(kx, ky, kz, b.depth));
+          kmin[0] = min(kmin[0], kx), kmin[1] = min(kmin[1], ky), kmin[2] = min(kmin[2], kz);
+          kmax[0] = max(kmax[0], kx), kmax[1] = max(kmax[1], ky), kmax[2] = max(kmax[2], kz);
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        mmin = min(mmin, __shfl_xor_sync(0xffffffffu, mmin, o));
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          kmin[a] = min(kmin[a], __shfl_xor_sync(0xffffffffu, kmin[a], o));
+          kmax[a] = max(kmax[a], __shfl_xor_sync(0xffffffffu, kmax[a], o));
+        }
+      }
+      const bool window_ok = n == 0 || (kmax[0] - kmin[0] < (unsigned)REF_WIN &&
+                                        kmax[1] - kmin[1] < (unsigned)REF_WIN && kmax[2] - kmin[2] < (unsigned)REF_WIN);
+      if (!window_ok && lane == 0) atomicOr(err, REF_ERR_WINDOW);
+      // the field's integer coordinate of every leaf column of the window,
+      // one per lane and axis (a huge negative value where get_Distance's
+      // float quotient leaves the int range: the index is then out of range)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const float c = oct_centre(b, kmin[a] + (unsigned)lane, a, dres);
+        const float qv = __fdiv_rn(__fsub_rn(c, lo[a]), res);
+        s_ix[w][a][lane] = (qv > -2147483648.f && qv < 2147483648.f) ? (long long)__float2int_rz(qv)
+                                                                      : -(1ll << 50);
+      }
+      unsigned long long pk_first;
+      {
+        unsigned fx, fy, fz;
+        demorton3(mmin, b.depth, fx, fy, fz);
+        pk_first = (unsigned long long)fx | ((unsigned long long)fy << 21) | ((unsigned long long)fz << 42);
+      }
+      __syncwarp();
+      long long sum = 0;
+      int cnt = 0;
+      unsigned lw[REFW_PPT];
+#pragma unroll
+      for (int q = 0; q < REFW_PPT; ++q) {
+        lw[q] = 0xffffffffu;
+        if (!window_ok || pk[q] == ~0ull) continue;
+        const unsigned lx = (unsigned)(pk[q] & 0x1fffffull) - kmin[0];
+        const unsigned ly = (unsigned)((pk[q] >> 21) & 0x1fffffull) - kmin[1];
+        const unsigned lz = (unsigned)(pk[q] >> 42) - kmin[2];
+        const unsigned l = lx + REF_WIN * (ly + REF_WIN * lz);
+        lw[q] = l >> 5;
+        const unsigned bit = 1u << (l & 31u);
+        const unsigned old = atomicOr(&bm[l >> 5], bit);
+        if (old & bit) continue;
+        ++cnt;
+        if (pk[q] == pk_first) continue;
+        const long long idx = s_ix[w][1][ly] * REF_DIM + s_ix[w][2][lz] * (REF_DIM * REF_DIM) + s_ix[w][0][lx];
+        const float v = (idx >= 0 && idx < REF_VOL) ? __ldg(grid + idx) : 900.f;
+        sum += (long long)v * (long long)v;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+      }
+      const double div = cnt == 0 ? REF_SIZE_MAX : (double)(cnt - 1);
+      dt = __ddiv_rn(__dadd_rn(dt, (double)sum), div);
+      if (dt < best) {
+        best = dt;
+        best_i = it;
+      }
+      __syncwarp();
+#pragma unroll
+      for (int q = 0; q < REFW_PPT; ++q)
+        if (lw[q] != 0xffffffffu) bm[lw[q]] = 0u;
+      __syncwarp();
+    }
+    if (lane != 0) continue;
+    if (bad) {
+      score[p] = __int_as_float(0x7fc00000);
+      eye4(To);
+      continue;
+    }
+    score[p] = __double2float_rn(best);
+    float S[16], R2[16], A[16];
+    eye4(S);
+    const float cs = __fdiv_rn(km.z, ks.z);
+    S[0] = S[5] = S[10] = cs;
+    eye4(R2);
+    R2[0] = rot.c2[best_i], R2[4] = rot.s2[best_i], R2[1] = -rot.s2[best_i], R2[5] = rot.c2[best_i];
+    mm4(S, T3, A);
+    mm4(A, R2, A);
+    mm4(A, T1, A);
+    mm4(A, Tm, A);
+    for (int i = 0; i < 16; ++i) To[i] = A[i];
+  }
 }
 
 __global__ void k_ref_sum_counts(const uint32_t* __restrict__ cnt, int n, unsigned long long* __restrict__ out) {
@@ -892,7 +1174,12 @@ rtr_status rtr_ref_distance(rtr_context* ctx, const float* d_mcloud, const float
   const float4* mk = reinterpret_cast<const float4*>(d_mkeys);
   const float4* sk = reinterpret_cast<const float4*>(d_skeys);
   const unsigned nb = (unsigned)n_pairs;
-  if (nmax <= REF_PPT * 256)
+  if (nmax <= REFW_PPT * 32) {
+    const long long nbw = (n_pairs + REFW_WARPS - 1) / REFW_WARPS;
+    k_ref_distance_warp<<<(unsigned)nbw, 32 * REFW_WARPS, 0, st>>>(mc, mk, d_moffsets, d_mindices, d_mtdf, sk, n_scan,
+                                                                   d_pair_m, d_pair_s, n_pairs, resolution, half_tdf,
+                                                                   rot, d_score, d_T, err);
+  } else if (nmax <= REF_PPT * 256)
     k_ref_distance<256><<<nb, 256, 0, st>>>(mc, mk, d_moffsets, d_mindices, d_mtdf, sk, n_scan, d_pair_m, d_pair_s,
                                             resolution, half_tdf, rot, d_score, d_T, err);
   else if (nmax <= REF_PPT * 512)
