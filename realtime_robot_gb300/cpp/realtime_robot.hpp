@@ -160,13 +160,33 @@ inline rtr_context* thread_context() {
 
 constexpr int kDescDim = 352;
 
-// A keypoint and its SHOT-352 descriptor (key_point.h:59-86 keeps the TDF
-// grid, the occupancy cloud and the plane-area vector here instead).
+// OccupiedGrid (key_point.h:52-57): the points of the keypoint's box and the
+// number of occupied 1 cm leaves among them.
+struct OccupiedGrid {
+  Cloud::Ptr cloud{new Cloud};
+  float Border[6] = {0, 0, 0, 0, 0, 0};
+  int Number = 0;
+};
+
+// A keypoint (key_point.h:59-86).  The SHOT route fills `descriptor`; the
+// reference's own route fills Occupiedgrid (getOccupiedGrid), grid_value and
+// Border (get_TSDF); vector3D is the plane-area vector (0.16 each by
+// default, as the reference's constructor sets it; plane areas are not
+// computed here).
 struct KeyPoint {
   pcl::PointXYZ Key_coordinate;
   std::vector<float> descriptor;  // kDescDim values, L2-normalised
+  OccupiedGrid Occupiedgrid;
+  std::vector<double> vector3D{0.16, 0.16, 0.16};
+  std::vector<float> grid_value;  // 27000 values after get_TSDF
+  float Border[6] = {0, 0, 0, 0, 0, 0};
   KeyPoint() = default;
   explicit KeyPoint(const pcl::PointXYZ& p) : Key_coordinate(p) {}
+
+  // key_point.h:112-161 through rtr_ref_occupancy (one keypoint).
+  void getOccupiedGrid(Cloud::Ptr cloud, float resolution = 0.01f, float f_adjust = 0.1f);
+  // key_point.h:251-334 through rtr_ref_tdf, from Occupiedgrid.cloud.
+  void get_TSDF(Cloud::Ptr cloud, float resolution = 0.01f, float f_adjust = 0.15f);
 };
 
 // A model keypoint paired with a scene keypoint (point_i model, point_j
@@ -291,6 +311,108 @@ inline std::vector<PairPoint> match_keypoints(const ModelPoint& model, const Sca
     out.push_back(std::move(p));
   }
   return out;
+}
+
+// ---- the reference's own descriptor route, one keypoint / pair per call ----
+inline void KeyPoint::getOccupiedGrid(Cloud::Ptr cloud, float resolution, float f_adjust) {
+  rtr_context* ctx = thread_context();
+  const int n = (int)cloud->size();
+  const float key[4] = {Key_coordinate.x, Key_coordinate.y, Key_coordinate.z, 0.f};
+  DeviceArray<float> d_cloud(4 * (size_t)(n > 0 ? n : 1)), d_key(4);
+  DeviceArray<int32_t> d_num(1), d_off(2), d_idx((size_t)(n > 0 ? n : 1));
+  d_cloud.upload(reinterpret_cast<const float*>(cloud->points.data()), 4 * (size_t)n);
+  d_key.upload(key, 4);
+  long long total = 0;
+  check(rtr_ref_occupancy(ctx, d_cloud.p, n, d_key.p, 1, resolution, f_adjust, d_num.p, d_off.p, d_idx.p,
+                          (long long)d_idx.n, &total, nullptr),
+        "rtr_ref_occupancy");
+  std::vector<int32_t> idx((size_t)total);
+  d_idx.download(idx.data(), idx.size());
+  d_num.download(&Occupiedgrid.Number, 1);
+  Occupiedgrid.cloud.reset(new Cloud);
+  Occupiedgrid.cloud->points.reserve(idx.size());
+  for (int32_t i : idx) Occupiedgrid.cloud->points.push_back(cloud->points[(size_t)i]);
+  Occupiedgrid.cloud->width = (uint32_t)idx.size();
+}
+
+inline void KeyPoint::get_TSDF(Cloud::Ptr cloud, float resolution, float f_adjust) {
+  (void)cloud;  // the reference reads Occupiedgrid.cloud here too
+  rtr_context* ctx = thread_context();
+  const Cloud& occ = *Occupiedgrid.cloud;
+  const int n = (int)occ.size();
+  const float key[4] = {Key_coordinate.x, Key_coordinate.y, Key_coordinate.z, 0.f};
+  std::vector<int32_t> idx((size_t)(n > 0 ? n : 1));
+  for (int i = 0; i < n; ++i) idx[(size_t)i] = i;
+  const int32_t off[2] = {0, n};
+  DeviceArray<float> d_cloud(4 * (size_t)(n > 0 ? n : 1)), d_key(4), d_tdf(27000);
+  DeviceArray<int32_t> d_off(2), d_idx(idx.size());
+  d_cloud.upload(reinterpret_cast<const float*>(occ.points.data()), 4 * (size_t)n);
+  d_key.upload(key, 4);
+  d_off.upload(off, 2);
+  d_idx.upload(idx.data(), idx.size());
+  int dim = 0;
+  check(rtr_ref_tdf(ctx, d_cloud.p, d_key.p, 1, d_off.p, d_idx.p, resolution, f_adjust, d_tdf.p, &dim, nullptr),
+        "rtr_ref_tdf");
+  grid_value.assign(27000, 0.f);
+  d_tdf.download(grid_value.data(), (size_t)dim * dim * dim);
+  const float k3[3] = {Key_coordinate.x, Key_coordinate.y, Key_coordinate.z};
+  for (int a = 0; a < 3; ++a) {
+    Border[a] = k3[a] - f_adjust;
+    Border[3 + a] = k3[a] + f_adjust;
+  }
+}
+
+// matching.h:122-222 through rtr_ref_distance (one pair): p1_key is the model
+// keypoint after getOccupiedGrid and get_TSDF (30^3 field), p2_scan the scan
+// keypoint.  Returns the score; key_transform gets the pair's transform.
+inline float get_Distance(Eigen::Matrix4f& key_transform, KeyPoint& p1_key, KeyPoint& p2_scan,
+                          const float resolution = 0.01f) {
+  if (p1_key.grid_value.size() != 27000) throw rtr_error(RTR_ERR_INVALID_ARG, "get_Distance: call get_TSDF first");
+  rtr_context* ctx = thread_context();
+  const Cloud& occ = *p1_key.Occupiedgrid.cloud;
+  const int n = (int)occ.size();
+  const float km[4] = {p1_key.Key_coordinate.x, p1_key.Key_coordinate.y, p1_key.Key_coordinate.z, 0.f};
+  const float ks[4] = {p2_scan.Key_coordinate.x, p2_scan.Key_coordinate.y, p2_scan.Key_coordinate.z, 0.f};
+  std::vector<int32_t> idx((size_t)(n > 0 ? n : 1));
+  for (int i = 0; i < n; ++i) idx[(size_t)i] = i;
+  const int32_t off[2] = {0, n}, pm = 0, ps = 0;
+  DeviceArray<float> d_cloud(4 * (size_t)(n > 0 ? n : 1)), d_km(4), d_ks(4), d_tdf(27000), d_score(1), d_T(16);
+  DeviceArray<int32_t> d_off(2), d_idx(idx.size()), d_pm(1), d_ps(1);
+  d_cloud.upload(reinterpret_cast<const float*>(occ.points.data()), 4 * (size_t)n);
+  d_km.upload(km, 4);
+  d_ks.upload(ks, 4);
+  d_tdf.upload(p1_key.grid_value.data(), 27000);
+  d_off.upload(off, 2);
+  d_idx.upload(idx.data(), idx.size());
+  d_pm.upload(&pm, 1);
+  d_ps.upload(&ps, 1);
+  check(rtr_ref_distance(ctx, d_cloud.p, d_km.p, 1, d_off.p, d_idx.p, d_tdf.p, d_ks.p, 1, d_pm.p, d_ps.p, 1,
+                         resolution, 0.15f, d_score.p, d_T.p, nullptr),
+        "rtr_ref_distance");
+  float score = 0.f, T[16];
+  d_score.download(&score, 1);
+  d_T.download(T, 16);
+  for (int i = 0; i < 16; ++i) key_transform(i / 4, i % 4) = T[i];
+  return score;
+}
+
+// function.h:158-178, as written: float(2/3) and float(1/3) are 0, and the
+// occupancy ratio is an integer quotient.
+inline bool match_by_height(pcl::PointXYZ& key1, pcl::PointXYZ& key2) {
+  const float ratio = key1.z / key2.z;
+  return ratio >= 0.f || ratio <= 1.5f;
+}
+inline bool match_by_area(std::vector<double> v1, std::vector<double> v2) {
+  for (int a = 0; a < 3; ++a) {
+    const double r = v1[(size_t)a] / v2[(size_t)a];
+    if (r > 3 || r < 0.0) return false;
+  }
+  return true;
+}
+inline bool match_by_occupied(OccupiedGrid& o1, OccupiedGrid& o2) {
+  if (o2.Number == 0) return false;
+  const float q = (float)(o1.Number / o2.Number);
+  return !(q > 2 || q < 0.5);
 }
 
 // Inlier counts of candidate model -> scene poses (row-major 4x4 doubles):

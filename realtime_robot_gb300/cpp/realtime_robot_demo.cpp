@@ -9,10 +9,14 @@
 // then keyPointICP refines model onto scan.  Prints the pair count, both
 // poses and their error against the generator's transform; exits 0 when the
 // refined pose is within 1 cm / 1 degree of it, 1 otherwise, 2 on an error.
+// `realtime_robot_demo ref <seed>` runs main's own descriptor route instead
+// (occupancy grids, TDF, get_Distance, the gates) on the kept KeyPoint calls.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <iostream>
+#include <string>
 #include <vector>
 
 #include "realtime_robot.hpp"
@@ -39,7 +43,57 @@ static void pose_error(const Eigen::Matrix4f& A, const double* B, double* dt, do
   *dr = std::acos(std::fmax(-1.0, std::fmin(1.0, 0.5 * (tr - 1.0))));
 }
 
+// main's own descriptor route (RealTimeRobot.cpp:56-102) on the kept
+// KeyPoint members, one keypoint and one pair per call as main makes them:
+// a 3,000-point chair and a second sampling of it moved by (dx, 0, 0), every
+// 150th / 200th point a keypoint.  Prints every pair as
+// "pair m s <score bits in hex> <kept>" and the count of kept pairs.
+static int reference_route(unsigned long long seed) {
+  const int n = 3000;
+  std::vector<float> model(4 * (size_t)n), scan(4 * (size_t)n);
+  rtr_robot::check(rtr_synth_shape(0, 40 + seed, n, model.data()), "rtr_synth_shape");
+  rtr_robot::check(rtr_synth_shape(0, 41 + seed, n, scan.data()), "rtr_synth_shape");
+  for (int i = 0; i < n; ++i) scan[4 * (size_t)i] += 0.01f * (float)(seed % 5);
+  Cloud::Ptr mcloud = to_cloud(model, n), cloud = to_cloud(scan, n);
+  std::vector<rtr_robot::KeyPoint> mk, sk;
+  for (int i = 0; i < n; i += 150) {
+    rtr_robot::KeyPoint p(mcloud->points[(size_t)i]);
+    p.getOccupiedGrid(mcloud);
+    p.get_TSDF(mcloud);
+    mk.push_back(std::move(p));
+  }
+  for (int i = 0; i < n; i += 200) {
+    rtr_robot::KeyPoint p(cloud->points[(size_t)i]);
+    p.getOccupiedGrid(cloud);
+    sk.push_back(std::move(p));
+  }
+  int kept = 0;
+  for (size_t m = 0; m < mk.size(); ++m)
+    for (size_t s = 0; s < sk.size(); ++s) {
+      Eigen::Matrix4f T;
+      const float d = rtr_robot::get_Distance(T, mk[m], sk[s]);
+      const bool keydistance = d < 3;
+      const bool keep = rtr_robot::match_by_height(mk[m].Key_coordinate, sk[s].Key_coordinate) &&
+                        rtr_robot::match_by_area(mk[m].vector3D, sk[s].vector3D) &&
+                        rtr_robot::match_by_occupied(mk[m].Occupiedgrid, sk[s].Occupiedgrid) && keydistance;
+      uint32_t bits;
+      std::memcpy(&bits, &d, 4);
+      std::printf("pair %zu %zu %08x %d\n", m, s, bits, keep ? 1 : 0);
+      kept += keep;
+    }
+  std::printf("reference route: %zu x %zu keypoints, %d pairs\n", mk.size(), sk.size(), kept);
+  return 0;
+}
+
 int main(int argc, char** argv) {
+  if (argc > 1 && std::string(argv[1]) == "ref") {
+    try {
+      return reference_route(argc > 2 ? std::strtoull(argv[2], nullptr, 10) : 0ull);
+    } catch (const std::exception& e) {
+      std::fprintf(stderr, "error: %s\n", e.what());
+      return 2;
+    }
+  }
   const unsigned long long seed = argc > 1 ? std::strtoull(argv[1], nullptr, 10) : 0ull;
   try {
     // the clouds (main loads chair1.pcd and T0_m8111.pcd)

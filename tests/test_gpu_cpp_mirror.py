@@ -52,3 +52,29 @@ def test_cpp_entry_points_register_a_chair(rtr):
         assert within == _oracle_within(rtr, O, OP, om, seed), (seed, r.stdout)
         ok += within
     assert ok >= 6, ok
+
+
+@pytest.mark.parametrize("seed", [1, 3])
+def test_cpp_reference_route_members(rtr, seed):
+    """main's own route on the kept KeyPoint members (getOccupiedGrid,
+    get_TSDF, get_Distance, match_by_*; one keypoint / pair per call):
+    every pair's score bit for bit and every keep decision equal to the
+    oracle's batched route on the same clouds."""
+    from oracle import ref_correspond, ref_distance, ref_occupancy, ref_tdf
+    r = subprocess.run([str(DEMO), "ref", str(seed)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, (r.returncode, r.stdout[-2000:], r.stderr)
+    got = [ln.split() for ln in r.stdout.splitlines() if ln.startswith("pair ")]
+    model = rtr.synth_shape(rtr.CHAIR, 3000, 40 + seed)
+    scan = rtr.synth_shape(rtr.CHAIR, 3000, 41 + seed).copy()
+    scan[:, 0] += np.float32(0.01) * np.float32(seed % 5)
+    km, ks = model[::150].copy(), scan[::200].copy()
+    mn, mo, mi = ref_occupancy(model, km)
+    sn, _, _ = ref_occupancy(scan, ks)
+    sc, _ = ref_distance(model, km, mo, mi, ref_tdf(model, km, mo, mi), ks)
+    kept = set(ref_correspond(km, mn, ks, sn, sc).tolist())
+    assert len(got) == km.shape[0] * ks.shape[0]
+    for g in got:
+        m, s = int(g[1]), int(g[2])
+        p = m * ks.shape[0] + s
+        assert int(g[3], 16) == int(sc[p:p + 1].view(np.uint32)[0]), (m, s, g, sc[p])
+        assert (g[4] == "1") == (p in kept), (m, s)
