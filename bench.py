@@ -647,9 +647,17 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the batch and streaming blocks (profiling runs)")
+    ap.add_argument("--only-ref-route", action="store_true",
+                    help="run only the reference descriptor route block and print its JSON (profiling runs)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.only_ref_route:
+        import realtime_robot_gb300 as R
+        ctx = R.Context(0)
+        print(json.dumps(ref_route_block(ctx, R, args.steps, not args.no_cpu_baseline)), flush=True)
+        ctx.close()
+        return 0
     return run_ours(args)
 
 

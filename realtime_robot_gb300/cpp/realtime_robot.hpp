@@ -27,6 +27,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <iostream>
 #include <memory>
@@ -97,6 +99,170 @@ inline void transformPointCloud(const PointCloud<PointXYZ>& in, PointCloud<Point
   out.width = (uint32_t)out.points.size();
   out.height = 1;
 }
+
+// PCD files (pcl::io::loadPCDFile / savePCDFileASCII / savePCDFileBinary,
+// as main uses them at RealTimeRobot.cpp:34-35, 108-109).  Reads PCD v0.5-0.7
+// headers with DATA ascii or binary (binary_compressed is refused), takes x,
+// y and z from any field layout (F 4/8, I or U 1/2/4/8 bytes, any COUNT), and
+// ignores the other fields.  Writes x y z as float: ascii with 9 significant
+// digits (float values read back exactly), binary as 12-byte records.
+// Returns 0, or -1 on a missing file or a header / data it cannot read.
+namespace io {
+namespace detail {
+struct PcdField {
+  std::string name;
+  int size = 4, count = 1;
+  char type = 'F';
+};
+
+inline bool pcd_value(const unsigned char* p, const PcdField& f, double* out) {
+  switch (f.type) {
+    case 'F':
+      if (f.size == 4) { float v; std::memcpy(&v, p, 4); *out = v; return true; }
+      if (f.size == 8) { double v; std::memcpy(&v, p, 8); *out = v; return true; }
+      return false;
+    case 'I':
+      if (f.size == 1) { int8_t v; std::memcpy(&v, p, 1); *out = v; return true; }
+      if (f.size == 2) { int16_t v; std::memcpy(&v, p, 2); *out = v; return true; }
+      if (f.size == 4) { int32_t v; std::memcpy(&v, p, 4); *out = v; return true; }
+      if (f.size == 8) { int64_t v; std::memcpy(&v, p, 8); *out = (double)v; return true; }
+      return false;
+    case 'U':
+      if (f.size == 1) { uint8_t v; std::memcpy(&v, p, 1); *out = v; return true; }
+      if (f.size == 2) { uint16_t v; std::memcpy(&v, p, 2); *out = v; return true; }
+      if (f.size == 4) { uint32_t v; std::memcpy(&v, p, 4); *out = v; return true; }
+      if (f.size == 8) { uint64_t v; std::memcpy(&v, p, 8); *out = (double)v; return true; }
+      return false;
+  }
+  return false;
+}
+}  // namespace detail
+
+inline int loadPCDFile(const std::string& path, PointCloud<PointXYZ>& cloud) {
+  FILE* fp = std::fopen(path.c_str(), "rb");
+  if (!fp) return -1;
+  std::vector<unsigned char> raw;
+  unsigned char buf[65536];
+  size_t got;
+  while ((got = std::fread(buf, 1, sizeof(buf), fp)) > 0) raw.insert(raw.end(), buf, buf + got);
+  std::fclose(fp);
+  std::vector<detail::PcdField> fields;
+  long long points = -1, width = -1, height = 1;
+  std::string data;
+  size_t pos = 0;
+  while (pos < raw.size() && data.empty()) {
+    size_t end = pos;
+    while (end < raw.size() && raw[end] != '\n') ++end;
+    std::string line(raw.begin() + (long)pos, raw.begin() + (long)end);
+    pos = end + 1;
+    if (!line.empty() && line.back() == '\r') line.pop_back();
+    if (line.empty() || line[0] == '#') continue;
+    std::vector<std::string> tok;
+    for (size_t i = 0; i < line.size();) {
+      while (i < line.size() && (line[i] == ' ' || line[i] == '\t')) ++i;
+      size_t j = i;
+      while (j < line.size() && line[j] != ' ' && line[j] != '\t') ++j;
+      if (j > i) tok.push_back(line.substr(i, j - i));
+      i = j;
+    }
+    if (tok.empty()) continue;
+    const std::string& key = tok[0];
+    if (key == "FIELDS" || key == "COLUMNS") {
+      fields.assign(tok.size() - 1, detail::PcdField());
+      for (size_t i = 1; i < tok.size(); ++i) fields[i - 1].name = tok[i];
+    } else if (key == "SIZE" || key == "TYPE" || key == "COUNT") {
+      if (tok.size() - 1 != fields.size()) return -1;
+      for (size_t i = 1; i < tok.size(); ++i) {
+        if (key == "SIZE") fields[i - 1].size = std::atoi(tok[i].c_str());
+        if (key == "TYPE") fields[i - 1].type = tok[i][0];
+        if (key == "COUNT") fields[i - 1].count = std::atoi(tok[i].c_str());
+      }
+    } else if (key == "WIDTH" && tok.size() > 1) {
+      width = std::atoll(tok[1].c_str());
+    } else if (key == "HEIGHT" && tok.size() > 1) {
+      height = std::atoll(tok[1].c_str());
+    } else if (key == "POINTS" && tok.size() > 1) {
+      points = std::atoll(tok[1].c_str());
+    } else if (key == "DATA" && tok.size() > 1) {
+      data = tok[1];
+    }
+  }
+  if (points < 0) points = width * height;
+  if (points < 0 || data.empty() || fields.empty()) return -1;
+  int col[3] = {-1, -1, -1};
+  size_t rec = 0;
+  std::vector<size_t> off(fields.size()), first_col(fields.size());
+  size_t ncol = 0;
+  for (size_t i = 0; i < fields.size(); ++i) {
+    if (fields[i].size <= 0 || fields[i].count <= 0) return -1;
+    off[i] = rec;
+    first_col[i] = ncol;
+    rec += (size_t)fields[i].size * (size_t)fields[i].count;
+    ncol += (size_t)fields[i].count;
+    for (int a = 0; a < 3; ++a)
+      if (fields[i].name == std::string(1, "xyz"[a])) col[a] = (int)i;
+  }
+  if (col[0] < 0 || col[1] < 0 || col[2] < 0) return -1;
+  cloud.points.assign((size_t)points, PointXYZ());
+  if (data == "binary") {
+    if (raw.size() < pos + rec * (size_t)points) return -1;
+    for (long long i = 0; i < points; ++i) {
+      const unsigned char* r = raw.data() + pos + rec * (size_t)i;
+      double v[3];
+      for (int a = 0; a < 3; ++a)
+        if (!detail::pcd_value(r + off[(size_t)col[a]], fields[(size_t)col[a]], &v[a])) return -1;
+      cloud.points[(size_t)i] = PointXYZ((float)v[0], (float)v[1], (float)v[2]);
+    }
+  } else if (data == "ascii") {
+    std::vector<double> row(ncol);
+    const char* c = reinterpret_cast<const char*>(raw.data()) + pos;
+    const char* e = reinterpret_cast<const char*>(raw.data()) + raw.size();
+    for (long long i = 0; i < points; ++i) {
+      for (size_t k = 0; k < ncol; ++k) {
+        while (c < e && (*c == ' ' || *c == '\t' || *c == '\n' || *c == '\r')) ++c;
+        if (c >= e) return -1;
+        std::string tokv;
+        while (c < e && *c != ' ' && *c != '\t' && *c != '\n' && *c != '\r') tokv.push_back(*c++);
+        row[k] = std::strtod(tokv.c_str(), nullptr);
+      }
+      cloud.points[(size_t)i] = PointXYZ((float)row[first_col[(size_t)col[0]]], (float)row[first_col[(size_t)col[1]]],
+                                         (float)row[first_col[(size_t)col[2]]]);
+    }
+  } else {
+    return -1;  // binary_compressed (LZF) is not read
+  }
+  cloud.width = (uint32_t)points;
+  cloud.height = 1;
+  return 0;
+}
+
+inline int pcd_write(const std::string& path, const PointCloud<PointXYZ>& cloud, bool binary) {
+  FILE* fp = std::fopen(path.c_str(), "wb");
+  if (!fp) return -1;
+  const size_t n = cloud.points.size();
+  std::fprintf(fp,
+               "# .PCD v0.7 - Point Cloud Data file format\nVERSION 0.7\nFIELDS x y z\nSIZE 4 4 4\nTYPE F F F\n"
+               "COUNT 1 1 1\nWIDTH %zu\nHEIGHT 1\nVIEWPOINT 0 0 0 1 0 0 0\nPOINTS %zu\nDATA %s\n",
+               n, n, binary ? "binary" : "ascii");
+  for (size_t i = 0; i < n; ++i) {
+    const PointXYZ& p = cloud.points[i];
+    if (binary) {
+      const float v[3] = {p.x, p.y, p.z};
+      std::fwrite(v, sizeof(float), 3, fp);
+    } else {
+      std::fprintf(fp, "%.9g %.9g %.9g\n", (double)p.x, (double)p.y, (double)p.z);
+    }
+  }
+  return std::fclose(fp) == 0 ? 0 : -1;
+}
+
+inline int savePCDFileASCII(const std::string& path, const PointCloud<PointXYZ>& cloud) {
+  return pcd_write(path, cloud, false);
+}
+inline int savePCDFileBinary(const std::string& path, const PointCloud<PointXYZ>& cloud) {
+  return pcd_write(path, cloud, true);
+}
+}  // namespace io
 }  // namespace pcl
 #endif  // RTR_HAVE_PCL
 

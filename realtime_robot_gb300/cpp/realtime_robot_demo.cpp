@@ -10,7 +10,9 @@
 // poses and their error against the generator's transform; exits 0 when the
 // refined pose is within 1 cm / 1 degree of it, 1 otherwise, 2 on an error.
 // `realtime_robot_demo ref <seed>` runs main's own descriptor route instead
-// (occupancy grids, TDF, get_Distance, the gates) on the kept KeyPoint calls.
+// (occupancy grids, TDF, get_Distance, the gates) on the kept KeyPoint calls;
+// `realtime_robot_demo pcd <in> <ascii out> <binary out>` round-trips a PCD
+// file through pcl::io (no GPU).
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -86,6 +88,18 @@ static int reference_route(unsigned long long seed) {
 }
 
 int main(int argc, char** argv) {
+  if (argc > 1 && std::string(argv[1]) == "pcd") {
+    // pcd <in> <out ascii> <out binary>: pcl::io round trip (no GPU)
+    if (argc != 5) return 2;
+    Cloud c;
+    if (pcl::io::loadPCDFile(argv[2], c) != 0) {
+      std::fprintf(stderr, "error: cannot read %s\n", argv[2]);
+      return 2;
+    }
+    if (pcl::io::savePCDFileASCII(argv[3], c) != 0 || pcl::io::savePCDFileBinary(argv[4], c) != 0) return 2;
+    std::printf("points %zu\n", c.size());
+    return 0;
+  }
   if (argc > 1 && std::string(argv[1]) == "ref") {
     try {
       return reference_route(argc > 2 ? std::strtoull(argv[2], nullptr, 10) : 0ull);

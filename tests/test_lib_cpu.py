@@ -3,6 +3,7 @@ point the headers declare, and its host-only parts (synthetic inputs, argument
 checks) behave."""
 import ctypes as C
 import re
+import subprocess
 from pathlib import Path
 
 import numpy as np
@@ -121,3 +122,52 @@ def test_cpp_mirror_fails_cleanly_without_a_gpu(rtr):
         pytest.skip("demo not built")
     r = subprocess.run([str(demo)], capture_output=True, text=True, timeout=60)
     assert r.returncode == 2 and "RTR_ERR_NO_DEVICE" in r.stderr, (r.returncode, r.stderr)
+
+
+def _write_pcd(path, pts, binary, extra_rgb=False):
+    """A PCD v0.7 file laid out like the reference's (chair1.pcd: binary
+    x y z rgb; T0_m8111.pcd: ascii x y z)."""
+    n = pts.shape[0]
+    fields = "x y z rgb" if extra_rgb else "x y z"
+    k = 4 if extra_rgb else 3
+    hdr = (f"# .PCD v0.7 - Point Cloud Data file format\nVERSION 0.7\nFIELDS {fields}\nSIZE {' '.join(['4'] * k)}\n"
+           f"TYPE {' '.join(['F'] * k)}\nCOUNT {' '.join(['1'] * k)}\nWIDTH {n}\nHEIGHT 1\n"
+           f"VIEWPOINT 0 0 0 1 0 0 0\nPOINTS {n}\nDATA {'binary' if binary else 'ascii'}\n")
+    rec = np.zeros((n, k), np.float32)
+    rec[:, :3] = pts[:, :3]
+    if extra_rgb:
+        rec[:, 3] = np.arange(n, dtype=np.float32)
+    with open(path, "wb") as f:
+        f.write(hdr.encode())
+        if binary:
+            f.write(rec.tobytes())
+        else:
+            f.write("".join(" ".join(f"{v:.9g}" for v in r) + "\n" for r in rec).encode())
+
+
+def test_pcd_io_round_trips_main_clouds(tmp_path):
+    """pcl::io::loadPCDFile / savePCDFileASCII / savePCDFileBinary of the C++
+    header (RealTimeRobot.cpp:34-35, 108-109) on main's two clouds, in both
+    layouts the reference's files use: every coordinate read back exactly."""
+    import sys
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+    from make_golden import read_pcd
+    demo = Path(__file__).resolve().parents[1] / "realtime_robot_gb300" / "realtime_robot_demo"
+    if not demo.exists():
+        pytest.skip("demo not built")
+    d = np.load(Path(__file__).resolve().parent / "golden" / "main_clouds.npz")
+    for name, binary, rgb in (("chair1", True, True), ("T0_m8111", False, False)):
+        src = tmp_path / f"{name}.pcd"
+        _write_pcd(src, d[name], binary, rgb)
+        oa, ob = tmp_path / f"{name}_a.pcd", tmp_path / f"{name}_b.pcd"
+        r = subprocess.run([str(demo), "pcd", str(src), str(oa), str(ob)], capture_output=True, text=True, timeout=60)
+        assert r.returncode == 0, r.stderr
+        assert f"points {d[name].shape[0]}" in r.stdout
+        for out in (oa, ob):
+            back = read_pcd(out)
+            assert np.array_equal(back[:, :3], d[name][:, :3]), (name, out)
+    bad = tmp_path / "bad.pcd"
+    bad.write_text("VERSION 0.7\nFIELDS a b\nSIZE 4 4\nTYPE F F\nCOUNT 1 1\nPOINTS 1\nDATA ascii\n1 2\n")
+    r = subprocess.run([str(demo), "pcd", str(bad), str(tmp_path / "x.pcd"), str(tmp_path / "y.pcd")],
+                       capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2
