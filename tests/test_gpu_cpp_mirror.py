@@ -5,9 +5,10 @@ drives them (realtime_robot_demo) on a cropped, moved chair.
 
 The demo exits 0 when its refined pose is within 1 cm / 1 degree of the
 generator's.  Some crops leave only part of the chair, along which the view
-slides (seeds 2 and 3 keep a few centimetres of slide): the oracle pipeline
-on the same clouds lands there too.  So each seed's verdict must equal the
-oracle's verdict, and most seeds must register."""
+slides (seeds 2 and 3 keep 5 and 15 cm of slide): the oracle pipeline on the
+same clouds lands there too.  So wherever the oracle pipeline finds the
+chair (best instance within 2 cm / 3 degrees) the demo must register it
+within 1 cm / 1 degree, and most seeds must register."""
 import re
 import subprocess
 from pathlib import Path
@@ -21,9 +22,9 @@ DEMO = Path(__file__).resolve().parents[1] / "realtime_robot_gb300" / "realtime_
 SEEDS = range(8)
 
 
-def _oracle_within(R, O, OP, om, seed):
+def _oracle_found(R, O, OP, om, seed):
     """The oracle pipeline on the demo's clouds (same generator calls):
-    whether its best instance is within 1 cm / 1 degree of the truth."""
+    whether its best instance is within 2 cm / 3 degrees of the truth."""
     Tm = R.synth_rigid(100 + seed, 30.0, 0.3)
     seg = R.synth_transform_noise(R.synth_crop(R.synth_shape(R.CHAIR, 20000, 500 + seed), 0.4, seed), Tm, 0.002,
                                   9 + seed)
@@ -31,7 +32,7 @@ def _oracle_within(R, O, OP, om, seed):
     if not ref["instances"]:
         return False
     e = O.pose_error(ref["instances"][0]["pose"], Tm)
-    return e[0] < 0.01 and e[1] < np.radians(1.0)
+    return e[0] < 0.02 and e[1] < np.radians(3.0)
 
 
 def test_cpp_entry_points_register_a_chair(rtr):
@@ -49,7 +50,8 @@ def test_cpp_entry_points_register_a_chair(rtr):
         assert m, (seed, r.stdout)
         within = float(m.group(1)) < 0.01 and float(m.group(2)) < 1.0
         assert within == (r.returncode == 0), (seed, r.stdout)
-        assert within == _oracle_within(rtr, O, OP, om, seed), (seed, r.stdout)
+        if _oracle_found(rtr, O, OP, om, seed):
+            assert within, (seed, r.stdout)
         ok += within
     assert ok >= 6, ok
 
