@@ -714,6 +714,8 @@ __global__ void __launch_bounds__(32 * REFW_WARPS, 2)
     }
     OctBox b0;
     oct_define(b0, lo, hi, dres);
+    OctBoxF bf0;
+    oct_float(b0, bf0);
     double dt = 0.0, best = 100000000.0;
     int best_i = 0;
     bool bad = false;
@@ -724,8 +726,7 @@ __global__ void __launch_bounds__(32 * REFW_WARPS, 2)
           if (lane + 32 * q < n) xf3(M, px[q], py[q], pz[q]);
       }
       OctBox b = b0;
-      OctBoxF bf;
-      oct_float(b, bf);
+      OctBoxF bf = bf0;
       for (int round = 0; round < 4 * REF_MAX_DEPTH + 4; ++round) {
         int first = 0x7fffffff;
 #pragma unroll
