@@ -434,21 +434,6 @@ __device__ __forceinline__ float field_at(const float* __restrict__ grid, const 
   return (idx >= 0 && idx < REF_VOL) ? __ldg(grid + idx) : 900.f;
 }
 
-// field_at from the leaf centres (cx, cy, cz).
-__device__ __forceinline__ float field_at_c(const float* __restrict__ grid, float cx, float cy, float cz,
-                                            const float lo[3], float res) {
-  const float c[3] = {cx, cy, cz};
-  long long ix[3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    const float q = __fdiv_rn(__fsub_rn(c[a], lo[a]), res);
-    if (!(q > -2147483648.f && q < 2147483648.f)) return 900.f;
-    ix[a] = (long long)__float2int_rz(q);
-  }
-  const long long idx = ix[1] * REF_DIM + ix[2] * (REF_DIM * REF_DIM) + ix[0];
-  return (idx >= 0 && idx < REF_VOL) ? __ldg(grid + idx) : 900.f;
-}
-
 template <int NT>
 __global__ void __launch_bounds__(NT) k_ref_distance(const float4* __restrict__ mcloud,
                                                      const float4* __restrict__ mkeys,
