@@ -127,6 +127,23 @@ def _dist():
     return ws, rank, local
 
 
+def max_over_ranks(x: float, dist: bool, device="cpu") -> float:
+    """The slowest rank's value (all-reduce MAX), or x on one process."""
+    if not dist:
+        return x
+    import torch
+    import torch.distributed as tdist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank: float, seconds_local: float, ws: int, dist: bool, device="cpu") -> float:
+    """Whole-job throughput of ws independent replicas: every rank's units
+    over the slowest rank's time (weak scaling, no data-path collective)."""
+    return units_per_rank * ws / max_over_ranks(seconds_local, dist, device)
+
+
 def _room():
     import realtime_robot_gb300 as R
     scene, shapes, poses = R.synth_room(ROOM_SEED)
@@ -285,12 +302,8 @@ def run_ours(args):
     prof = ctx.profile(clear=True)
     ctx.set_profiling(False)
     ctx.check()
-    total_ms = sum(step_ms)
-    if dist:
-        t = torch.tensor([total_ms], device=dev)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = args.steps * ws / (total_ms / 1e3)
+    total_ms = max_over_ranks(sum(step_ms), dist, dev)
+    value = replica_throughput(args.steps, total_ms / 1e3, ws, False)
     r = R.parse_recog_result(res)
     stage_ms = {}
     for nm, ms in prof:
@@ -347,12 +360,8 @@ def run_ours(args):
     e0 = time.perf_counter()
     for _ in range(args.steps):
         host_step()
-    e_s = time.perf_counter() - e0
-    if dist:
-        t = torch.tensor([e_s], device=dev)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        e_s = float(t.item())
-    e2e = {"value": args.steps * ws / e_s, "unit": "recognitions/s",
+    e_s = max_over_ranks(time.perf_counter() - e0, dist, dev)
+    e2e = {"value": replica_throughput(args.steps, e_s, ws, False), "unit": "recognitions/s",
            "h2d_bytes_per_step": int(scene.nbytes), "d2h_bytes_per_step": int(R.C.sizeof(R.RecogResult)),
            "path": "rtr_recognize_host (C ABI): pinned host scene in, rtr_recog_result out, wall clock"}
 
