@@ -63,3 +63,25 @@ def test_recognize_host_entry_and_empty_scene(ctx, rtr):
     for inst in r["instances"]:
         assert np.all(np.isfinite(inst["pose"]))
     m.close()
+
+
+def test_recognize_main_clouds_matches_oracle(ctx, rtr):
+    """The recognition chain on main's own inputs (chair1.pcd as the model,
+    T0_m8111.pcd as the segment; tests/golden/main_clouds.npz): voxels and
+    keypoints exact, correspondences within 3 %, the same instance as the
+    oracle pipeline within 1 cm / 1 degree."""
+    from pathlib import Path
+    d = np.load(Path(__file__).resolve().parent / "golden" / "main_clouds.npz")
+    model, scan = d["chair1"], d["T0_m8111"]
+    prm = rtr.recog_default_params(scene_outward=1)
+    m = rtr.Model(ctx, _dev(model), prm)
+    om = OP.prepare_model(model, OP.params(scene_outward=1))
+    assert m.n_voxels == len(om["vox"]) and m.n_keypoints == len(om["keys"])
+    res = rtr.parse_recog_result(rtr.recognize(ctx, m, _dev(scan), prm))
+    ref = OP.recognize(om, scan, OP.params(scene_outward=1))
+    assert res["n_voxels"] == ref["n_voxels"] and res["n_keypoints"] == ref["n_keypoints"]
+    assert abs(res["n_correspondences"] - ref["n_correspondences"]) <= 0.03 * ref["n_correspondences"] + 3
+    assert len(res["instances"]) == len(ref["instances"]) == 1, (res["instances"], ref["instances"])
+    dt, dr = O.pose_error(res["instances"][0]["pose"], ref["instances"][0]["pose"])
+    assert dt < 0.01 and dr < np.radians(1.0), (dt, dr)
+    m.close()
