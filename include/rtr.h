@@ -389,9 +389,12 @@ rtr_status rtr_match_exact(rtr_context* ctx, const float* d_query, int n_query,
  * the first max_clusters clusters: members (original correspondence indices,
  * max_members per row, -1 padded), sizes, and the least-squares model->scene
  * pose (row-major 4x4, FP64).  The walk runs on the device in one cooperative
- * launch; the call synchronises once, to return the cluster count.  Consensus
- * sets longer than 128 members, or more than 1,441,792 correspondences,
- * return RTR_ERR_CAPACITY. */
+ * launch; the call synchronises once, to return the cluster count.  A set
+ * may hold every correspondence while n_corr^2 ints fit in 128 MiB (n_corr
+ * up to 5,792); above that, sets longer than 128 MiB / (4 n_corr) members
+ * (at least 128), or more than 1,441,792 correspondences, return
+ * RTR_ERR_CAPACITY.  A cluster longer than max_members keeps its first
+ * max_members members in d_members; d_sizes and the pose cover all of them. */
 rtr_status rtr_gc_group(rtr_context* ctx, const float* d_model_kp, const float* d_scene_kp,
                         const int32_t* d_corr_m, const int32_t* d_corr_s, const float* d_corr_d,
                         int n_corr, float gc_size, int gc_thresh, int max_clusters,

@@ -11,6 +11,8 @@ import ctypes as C
 import os
 from pathlib import Path
 
+import weakref
+
 import numpy as np
 
 __all__ = ["lib", "RtrError", "Context", "IcpParams", "IcpResult", "RoomParams", "LIB_PATH"]
@@ -245,9 +247,12 @@ class Context:
         check(lib().rtr_context_create(device, C.byref(h)))
         self.h = h
         self.device = device
+        self._graphs = weakref.WeakSet()  # batch graphs, destroyed before the context
 
     def close(self):
         if self.h:
+            for g in list(self._graphs):
+                g.close()
             lib().rtr_context_destroy(self.h)
             self.h = None
 
@@ -761,6 +766,8 @@ class BatchGraph:
         check(lib().rtr_batch_graph_create(ctx.h, _batch_args(models, scenes), n, C.byref(params),
                                            mlp.h if mlp else None, float(keep), _ptr(self.results), C.byref(h)))
         self.h = h
+        self._ctx = ctx  # the context outlives the graph
+        ctx._graphs.add(self)
 
     def launch(self, stream=None):
         check(lib().rtr_batch_graph_launch(self.h, _stream(stream)))

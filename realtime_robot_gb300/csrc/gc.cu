@@ -25,7 +25,17 @@
 namespace rtr {
 
 constexpr int GC_WARPS = 8;
-constexpr int GC_MAXS = 128;  // members per consensus set (larger sets: RTR_ERR_CAPACITY)
+constexpr int GC_MAXS = 128;  // members of a set staged in shared memory (the rest are read from set_mem)
+// Members stored per consensus set: every member while C rows of C fit in
+// GC_SET_BUDGET bytes, else as many as fit, never fewer than GC_MAXS (a set
+// beyond the stride: RTR_ERR_CAPACITY).
+constexpr size_t GC_SET_BUDGET = (size_t)128 << 20;
+inline int gc_set_stride(int C) {
+  const long long n = C > 0 ? C : 1;
+  const long long by_budget = (long long)(GC_SET_BUDGET / sizeof(int)) / n;
+  const long long m = n < by_budget ? n : by_budget;
+  return (int)(m > GC_MAXS ? m : GC_MAXS);
+}
 
 struct GcDev {
   const float4* pm;        // model keypoint of sorted correspondence a
@@ -35,7 +45,8 @@ struct GcDev {
   float gc;
   unsigned* taken;         // bitset over sorted positions
   int* set_size;           // [C]
-  int* set_mem;            // [C][GC_MAXS] sorted positions
+  int* set_mem;            // [C][maxs] sorted positions
+  int maxs;                // members stored per set (gc_set_stride)
 };
 
 __device__ __forceinline__ float sqrt_approx(float x) {
@@ -79,7 +90,7 @@ struct GcCoop {
                        // [12] the next round's window (0: the first window)
   unsigned* arrive;    // grid barrier counter (zero at launch)
   int* computed;       // [C] 1 once the seed's set has been computed
-  int* cl_members;     // [max_clusters][GC_MAXS] sorted positions
+  int* cl_members;     // [max_clusters][maxs] sorted positions
   int* cl_sizes;       // [max_clusters]
   int thresh, max_clusters;
   long long budget;    // clock64 cycles per barrier wait
@@ -139,6 +150,7 @@ constexpr int GC_PREF = 7;   // mask loads in flight per lane during admission
 // members so far in parallel; then, lowest lane first, the next passing
 // candidate is admitted and every later candidate is also tested against
 // it.  Same result as admitting one candidate at a time.
+template <bool LONG>
 __device__ __forceinline__ void gc_admit(const GcDev& g, int a, const int* slot, int n, float4* mem_m,
                                          float4* mem_s, int& cnt, float r2max, int* n_tested) {
   const int lane = threadIdx.x & 31;
@@ -150,21 +162,31 @@ __device__ __forceinline__ void gc_admit(const GcDev& g, int a, const int* slot,
   }
   *n_tested += n;
   bool pass = pj >= 0;
-  const int stored = min(cnt, GC_MAXS);
-  for (int m = 1; m < stored; ++m) {
+  const int maxs = LONG ? g.maxs : GC_MAXS;
+  const int stored = min(cnt, maxs);
+  const int staged = min(stored, GC_MAXS);
+  for (int m = 1; m < staged; ++m) {
     if (pass) pass = gc_consistent(mem_m[m], mem_s[m], cm, cs, g.gc, r2max);
     if ((m & 3) == 0 && !__any_sync(0xffffffffu, pass)) break;
   }
+  // members past the shared-memory stage, read through set_mem
+  if (LONG)
+    for (int m = GC_MAXS; m < stored && __any_sync(0xffffffffu, pass); ++m) {
+      const int pb = __ldcg(g.set_mem + (size_t)a * maxs + m);
+      if (pass) pass = gc_consistent(__ldg(g.pm + pb), __ldg(g.ps + pb), cm, cs, g.gc, r2max);
+    }
   unsigned bal = __ballot_sync(0xffffffffu, pass);
   while (bal) {
     const int f = __ffs(bal) - 1;
     const float4 fm = shfl4(cm, f), fs = shfl4(cs, f);
-    if (lane == f && cnt < GC_MAXS) {
-      mem_m[cnt] = cm;
-      mem_s[cnt] = cs;
-      g.set_mem[(size_t)a * GC_MAXS + cnt] = pj;
+    if (lane == f && cnt < maxs) {
+      if (cnt < GC_MAXS) {
+        mem_m[cnt] = cm;
+        mem_s[cnt] = cs;
+      }
+      g.set_mem[(size_t)a * maxs + cnt] = pj;
     }
-    ++cnt;  // counted beyond GC_MAXS too: reported by the walk
+    ++cnt;  // counted beyond the stride too: reported by the walk
     if (lane > f && pass) pass = gc_consistent(fm, fs, cm, cs, g.gc, r2max);
     if (lane <= f) pass = false;
     bal = __ballot_sync(0xffffffffu, pass);
@@ -189,7 +211,11 @@ __device__ __forceinline__ void gc_admit(const GcDev& g, int a, const int* slot,
 // A stored set stays exact while none of its members is taken (removing
 // rejected candidates never changes a greedy walk).  Every round advances the
 // walk by at least one seed (the seed at pos is exact when B starts).
+// LONG: sets may be stored past GC_MAXS members (g.maxs > GC_MAXS); false
+// compiles the fixed GC_MAXS stride.
+template <bool LONG>
 __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c) {
+  const int maxs = LONG ? g.maxs : GC_MAXS;
   extern __shared__ unsigned s_taken[];  // copy of the taken bitset
   __shared__ float4 mem_m[GC_WARPS][GC_MAXS], mem_s[GC_WARPS][GC_MAXS];
   __shared__ int s_slot[GC_WARPS][GC_PEND];
@@ -243,9 +269,9 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
         if (!__ldcg(c.computed + a)) {
           need = true;
         } else {
-          const int n = min(__ldcg(g.set_size + a), GC_MAXS);
+          const int n = min(__ldcg(g.set_size + a), maxs);
           bool st = false;
-          for (int k = lane; k < n; k += 32) st |= sbit(s_taken, __ldcg(g.set_mem + (size_t)a * GC_MAXS + k));
+          for (int k = lane; k < n; k += 32) st |= sbit(s_taken, __ldcg(g.set_mem + (size_t)a * maxs + k));
           need = __any_sync(0xffffffffu, st);
         }
       }
@@ -309,7 +335,7 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
       if (lane == 0) {
         mem_m[wid][0] = __ldg(g.pm + a);
         mem_s[wid][0] = __ldg(g.ps + a);
-        g.set_mem[(size_t)a * GC_MAXS] = a;
+        g.set_mem[(size_t)a * maxs] = a;
       }
       __syncwarp();
       int cnt = 1, npend = 0, ntest = 0;
@@ -352,7 +378,7 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
             npend += min(total, room);
             __syncwarp();
             while (npend >= 32) {
-              gc_admit(g, a, s_slot[wid], 32, mem_m[wid], mem_s[wid], cnt, r2max, &ntest);
+              gc_admit<LONG>(g, a, s_slot[wid], 32, mem_m[wid], mem_s[wid], cnt, r2max, &ntest);
               const int rest = npend - 32;
               const int mv = lane < rest ? s_slot[wid][32 + lane] : 0;
               __syncwarp();
@@ -363,7 +389,7 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
           }
         }
       }
-      if (npend > 0) gc_admit(g, a, s_slot[wid], npend, mem_m[wid], mem_s[wid], cnt, r2max, &ntest);
+      if (npend > 0) gc_admit<LONG>(g, a, s_slot[wid], npend, mem_m[wid], mem_s[wid], cnt, r2max, &ntest);
       if (lane == 0) {
         g.set_size[a] = cnt;
         c.computed[a] = 1;
@@ -391,7 +417,7 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
       int n_pre = (p < wend && lane < nbc) ? __ldcg(g.set_size + p + lane) : 0;
       int mv[32];
 #pragma unroll
-      for (int t = 0; t < 32; ++t) mv[t] = (p < wend && t < nbc) ? __ldcg(g.set_mem + (size_t)(p + t) * GC_MAXS + lane) : 0;
+      for (int t = 0; t < 32; ++t) mv[t] = (p < wend && t < nbc) ? __ldcg(g.set_mem + (size_t)(p + t) * maxs + lane) : 0;
       while (p < wend && !stop) {
         const int nb = nbc;
         const int my = p + lane;
@@ -405,9 +431,9 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
           n_pre = (pn < wend && lane < nbc) ? __ldcg(g.set_size + pn + lane) : 0;
 #pragma unroll
           for (int t = 0; t < 32; ++t)
-            mv[t] = (pn < wend && t < nbc) ? __ldcg(g.set_mem + (size_t)(pn + t) * GC_MAXS + lane) : 0;
+            mv[t] = (pn < wend && t < nbc) ? __ldcg(g.set_mem + (size_t)(pn + t) * maxs + lane) : 0;
         }
-        const int ns_l = min(n_l, GC_MAXS);
+        const int ns_l = min(n_l, maxs);
         int cursor = 0;
         for (;;) {
           bool taken_l = true, stale_l = false;
@@ -415,7 +441,7 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
             taken_l = sbit(s_taken, my);
             if (!taken_l)
               for (int k = 0; k < ns_l && !stale_l; ++k) {
-                const int mb = k < 32 ? s_bmem[lane][k] : __ldcg(g.set_mem + (size_t)my * GC_MAXS + k);
+                const int mb = k < 32 ? s_bmem[lane][k] : __ldcg(g.set_mem + (size_t)my * maxs + k);
                 stale_l = sbit(s_taken, mb);
               }
           }
@@ -432,16 +458,16 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
             stop = true;
             break;
           }
-          if (nf > GC_MAXS) {
+          if (nf > maxs) {
             err = (int)RTR_ERR_CAPACITY;
             done = stop = true;
             p += f;
             break;
           }
           for (int k = lane; k < nf; k += 32) {
-            const int mb = k < 32 ? s_bmem[f][k] : __ldcg(g.set_mem + (size_t)(p + f) * GC_MAXS + k);
+            const int mb = k < 32 ? s_bmem[f][k] : __ldcg(g.set_mem + (size_t)(p + f) * maxs + k);
             atomicOr(&s_taken[mb >> 5], 1u << (mb & 31));
-            c.cl_members[(size_t)ncl * GC_MAXS + k] = mb;
+            c.cl_members[(size_t)ncl * maxs + k] = mb;
           }
           if (lane == 0) c.cl_sizes[ncl] = nf;
           __syncwarp();
@@ -621,7 +647,7 @@ static void gc_plan(ScratchPlan& p, int C, int max_clusters, int max_members) {
   p.add<float4>(n);
   p.add<unsigned>((n + 31) / 32);
   p.add<int>(n);
-  p.add<int>((size_t)n * GC_MAXS);
+  p.add<int>((size_t)n * gc_set_stride(C));
   p.add<int>(n);
   p.add<int>(16);
   p.add<unsigned>(1);
@@ -644,7 +670,7 @@ static bool gc_take(Scratch& s, int C, int max_clusters, int max_members, GcBufs
   b->ps = s.take<float4>(n);
   b->taken = s.take<unsigned>((n + 31) / 32);
   b->set_size = s.take<int>(n);
-  b->set_mem = s.take<int>((size_t)n * GC_MAXS);
+  b->set_mem = s.take<int>((size_t)n * gc_set_stride(C));
   b->computed = s.take<int>(n);
   b->misc = s.take<int>(16);
   b->arrive = s.take<unsigned>(1);
@@ -671,7 +697,7 @@ namespace rtr {
 
 size_t gc_scratch_bytes(int C, int max_clusters) {
   ScratchPlan plan;
-  gc_plan(plan, C, max_clusters, GC_MAXS);
+  gc_plan(plan, C, max_clusters, gc_set_stride(C));
   return plan.bytes;
 }
 
@@ -683,7 +709,7 @@ static rtr_status gc_launch(rtr_context* ctx, Scratch& s, const float* d_model_k
                             GcBufs* bo, uint32_t** order) {
   const int C = C_cap;
   GcBufs& b = *bo;
-  if (!gc_take(s, C, max_clusters, GC_MAXS, &b)) return fail(RTR_ERR_CAPACITY, "rtr_gc_group: scratch");
+  if (!gc_take(s, C, max_clusters, gc_set_stride(C), &b)) return fail(RTR_ERR_CAPACITY, "rtr_gc_group: scratch");
   const size_t dyn = sizeof(unsigned) * (size_t)((C + 31) / 32);
   if (dyn > GC_MAX_DYN_SMEM)
     return fail(RTR_ERR_CAPACITY, "rtr_gc_group: %d correspondences exceed the supported %d", C,
@@ -699,14 +725,16 @@ static rtr_status gc_launch(rtr_context* ctx, Scratch& s, const float* d_model_k
   RTR_CUDA(cudaMemsetAsync(b.computed, 0, sizeof(int) * C, st));
   RTR_CUDA(cudaMemsetAsync(b.misc, 0, sizeof(int) * 16, st));
   RTR_CUDA(cudaMemsetAsync(b.arrive, 0, sizeof(unsigned), st));
-  GcDev g{b.pm, b.ps, C, d_C, gc_size, b.taken, b.set_size, b.set_mem};
+  GcDev g{b.pm, b.ps, C, d_C, gc_size, b.taken, b.set_size, b.set_mem, gc_set_stride(C)};
   bbox_build(b.mbox, b.pm, C, d_C, st);
   GcCoop c{b.misc, b.arrive, b.computed, b.members, b.sizes, gc_thresh, max_clusters,
            ctx->wait_budget_cycles, ctx->d_status, b.mbox, b.need, b.mask,
            gc_win(C, ctx->tune_gc_window > 0 ? ctx->tune_gc_window : 0), gc_win(C, GC_WIN_MAX), gc_nwp(C)};
-  RTR_CUDA(cudaFuncSetAttribute(k_gc_coop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GC_MAX_DYN_SMEM));
+  const bool long_sets = gc_set_stride(C) > GC_MAXS;
+  auto kern = long_sets ? k_gc_coop<true> : k_gc_coop<false>;
+  RTR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GC_MAX_DYN_SMEM));
   int per_sm = 0;
-  RTR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gc_coop, GC_WARPS * 32, dyn));
+  RTR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, GC_WARPS * 32, dyn));
   if (per_sm < 1) return fail(RTR_ERR_CAPACITY, "rtr_gc_group: grouping kernel does not fit an SM");
   // enough warps for the work (a few thousand correspondences need a few
   // blocks), and a share of the GPU when several contexts run at once
@@ -727,7 +755,7 @@ static rtr_status gc_launch(rtr_context* ctx, Scratch& s, const float* d_model_k
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    RTR_CUDA(cudaLaunchKernelEx(&cfg, k_gc_coop, g, c));
+    RTR_CUDA(cudaLaunchKernelEx(&cfg, kern, g, c));
   }
   RTR_LAUNCHED(3);
   *order = vs;
@@ -746,8 +774,8 @@ rtr_status gc_group_async(rtr_context* ctx, Scratch& s, const float* d_model_kp,
   RTR_TRY(gc_launch(ctx, s, d_model_kp, d_scene_kp, d_corr_m, d_corr_s, d_corr_d, C_cap > 0 ? C_cap : 1, d_C,
                     gc_size, gc_thresh, max_clusters, st, &b, &order));
   k_gc_post<<<1, 32, 0, st>>>(b.misc, max_clusters, d_ncl, ctx->d_status, ctx->d_status + 16);
-  k_gc_poses<<<(max_clusters + 3) / 4, 128, 0, st>>>(b.pm, b.ps, b.members, b.sizes, max_clusters, d_ncl, GC_MAXS,
-                                                      b.poses);
+  k_gc_poses<<<(max_clusters + 3) / 4, 128, 0, st>>>(b.pm, b.ps, b.members, b.sizes, max_clusters, d_ncl,
+                                                      gc_set_stride(C_cap > 0 ? C_cap : 1), b.poses);
   RTR_LAUNCHED(2);
   if (d_poses)
     RTR_CUDA(cudaMemcpyAsync(d_poses, b.poses, sizeof(double) * 16 * max_clusters, cudaMemcpyDeviceToDevice, st));
@@ -774,17 +802,19 @@ rtr_status gc_group_dev(rtr_context* ctx, Scratch& s, const float* d_model_kp, c
   RTR_CUDA(cudaStreamSynchronize(st));
   const int ncl = h[1];
   if (h[3] == (int)RTR_ERR_CAPACITY)
-    return fail(RTR_ERR_CAPACITY, "rtr_gc_group: a consensus set exceeds %d members", GC_MAXS);
+    return fail(RTR_ERR_CAPACITY, "rtr_gc_group: a consensus set exceeds %d members", gc_set_stride(n_corr));
   if (h[3] == (int)RTR_ERR_TIMEOUT)
     return fail(RTR_ERR_TIMEOUT, "rtr_gc_group: a grid barrier wait exceeded the budget");
   if (ncl > 0) {
-    k_gc_poses<<<(ncl + 3) / 4, 128, 0, st>>>(b.pm, b.ps, b.members, b.sizes, ncl, nullptr, GC_MAXS, b.poses);
+    k_gc_poses<<<(ncl + 3) / 4, 128, 0, st>>>(b.pm, b.ps, b.members, b.sizes, ncl, nullptr, gc_set_stride(n_corr),
+                                               b.poses);
     RTR_LAUNCHED(1);
     if (d_poses) RTR_CUDA(cudaMemcpyAsync(d_poses, b.poses, sizeof(double) * 16 * ncl, cudaMemcpyDeviceToDevice, st));
     if (d_sizes) RTR_CUDA(cudaMemcpyAsync(d_sizes, b.sizes, sizeof(int) * ncl, cudaMemcpyDeviceToDevice, st));
     if (d_members) {
-      k_gc_members_out<<<(ncl * max_members + 255) / 256, 256, 0, st>>>(b.members, b.sizes, vs, ncl, GC_MAXS,
-                                                                         max_members, d_members);
+      k_gc_members_out<<<(ncl * max_members + 255) / 256, 256, 0, st>>>(b.members, b.sizes, vs, ncl,
+                                                                         gc_set_stride(n_corr), max_members,
+                                                                         d_members);
       RTR_LAUNCHED(1);
     }
   }

@@ -94,9 +94,9 @@ def test_batch_graph_replays_the_batch(ctx, rtr, batch):
 
 
 def test_batch_graph_refuses_to_run_after_scratch_moved(rtr, batch):
-    # a fresh context: the plain graph is made on scratch sized for the plain
-    # batch; the learned batch then needs more and reallocates it, so the
-    # graph's launch must be refused on the host (no kernel runs)
+    # a fresh context: the plain graph is made on its scratch; growing the
+    # arena afterwards (as a larger call would) reallocates it, so the graph's
+    # launch must be refused on the host (no kernel runs)
     import torch
     prm, mods, scenes = batch
     c2 = rtr.Context(0)
@@ -104,8 +104,7 @@ def test_batch_graph_refuses_to_run_after_scratch_moved(rtr, batch):
     g = rtr.BatchGraph(c2, mods[:4], scenes[:4], prm)
     g.launch()
     torch.cuda.synchronize()
-    mlp = rtr.Mlp(c2, seed=11)
-    rtr.recognize_batch(c2, mods[:4], scenes[:4], prm, mlp=mlp, keep=0.5)
+    c2.reserve(2 * c2.scratch_bytes() + (1 << 20))
     with pytest.raises(rtr.RtrError) as e:
         g.launch()
     assert e.value.status == 1 and "recreate" in str(e.value)

@@ -85,3 +85,29 @@ def test_recognize_main_clouds_matches_oracle(ctx, rtr):
     dt, dr = O.pose_error(res["instances"][0]["pose"], ref["instances"][0]["pose"])
     assert dt < 0.01 and dr < np.radians(1.0), (dt, dr)
     m.close()
+
+
+@pytest.mark.parametrize("pair", [("p70761", "p70761_c", "t70761"), ("p5", "mcloud", "t5")])
+@pytest.mark.parametrize("outward", [0, 1])
+def test_recognize_recorded_known_answer_pairs(ctx, rtr, pair, outward):
+    """Pinned end to end: the reference's recorded pairs (70761.pcd ->
+    70761_c.pcd, a translation by (+1, +0.5, 0); 5.pcd -> mcloud.pcd, by
+    (+0.8, +0.8, 0); tests/golden/pcd_pairs.npz) recognised with the first
+    cloud as the model and the second as the scene: the best instance is the
+    recorded translation within 0.1 mm / 0.01 degree, as the oracle's is."""
+    from pathlib import Path
+    d = np.load(Path(__file__).resolve().parent / "golden" / "pcd_pairs.npz")
+    model, scene = d[pair[0]], d[pair[1]]
+    T = np.eye(4)
+    T[:3, 3] = d[pair[2]]
+    prm = rtr.recog_default_params(scene_outward=outward)
+    m = rtr.Model(ctx, _dev(model), prm)
+    res = rtr.parse_recog_result(rtr.recognize(ctx, m, _dev(scene), prm))
+    m.close()
+    assert res["instances"], res
+    dt, dr = O.pose_error(res["instances"][0]["pose"], T)
+    assert dt < 1e-4 and dr < np.radians(0.01), (dt, dr)
+    ref = OP.recognize(OP.prepare_model(model, OP.params(scene_outward=outward)), scene,
+                       OP.params(scene_outward=outward))
+    dt, dr = O.pose_error(ref["instances"][0]["pose"], T)
+    assert dt < 1e-4 and dr < np.radians(0.01), (dt, dr)
