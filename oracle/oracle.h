@@ -7,7 +7,9 @@
  * uniform sampling, SHOT, matching, GC) restate published methods because PCL
  * 1.8.0's source is not part of the reference; they are pinned only by the
  * reference's recorded PCD fixtures (translation pairs, see tests/golden).  The
- * TDF restates kernel.cu:8-31 exactly.
+ * TDF restates kernel.cu:8-31 exactly.  refmatch.c restates the reference's
+ * own descriptor route (getOccupiedGrid, get_TSDF, get_Distance, the gates,
+ * Ransac) over PCL's octree rules; against PCL itself it is unpinned.
  *
  * Arithmetic rules shared with the GPU (compile with -ffp-contract=off):
  *   d2(q, p)  = ((dx*dx + dy*dy) + dz*dz), dx = q.x - p.x, each op rounded;
