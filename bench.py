@@ -15,7 +15,8 @@ Metric: scene recognitions per second.  The same line carries config 0
 The path does not shard (one scene is one unit): with N GPUs every rank runs
 its own replica and `value` sums the units of all ranks over the slowest
 rank's time.  `--impl reference` times the CPU restatement of the path
-(oracle/, all host threads) on bounded samples of the same workloads.
+(oracle/, all host threads): whole recognitions of the same room, with its
+inputs made by oracle/libsynth.so (no library of the GPU path is loaded).
 """
 from __future__ import annotations
 
@@ -144,17 +145,22 @@ def replica_throughput(units_per_rank: float, seconds_local: float, ws: int, dis
     return units_per_rank * ws / max_over_ranks(seconds_local, dist, device)
 
 
-def _room():
-    import realtime_robot_gb300 as R
-    scene, shapes, poses = R.synth_room(ROOM_SEED)
-    model = R.synth_shape(R.CHAIR, N_PTS, SEED)
+def _room(gen=None):
+    """The config-1 room, the chair model and the three chairs' true poses,
+    from `gen` (the package's generator, or oracle.synth: the same source
+    built host-only, for the reference arm)."""
+    if gen is None:
+        import realtime_robot_gb300 as gen
+    scene, shapes, poses = gen.synth_room(ROOM_SEED)
+    model = gen.synth_shape(gen.CHAIR, N_PTS, SEED)
     chairs = [poses[i] for i in range(len(shapes)) if shapes[i] == 0]
     return scene, model, chairs
 
 
-def _icp_pair():
-    import realtime_robot_gb300 as R
-    return R.config0_pair(SEED, N_PTS)
+def _icp_pair(gen=None):
+    if gen is None:
+        import realtime_robot_gb300 as gen
+    return gen.config0_pair(SEED, N_PTS)
 
 
 def _grid_cells(tgt: np.ndarray, h: float) -> int:
@@ -171,43 +177,44 @@ def _nearest_errors(instances, chairs):
     return out
 
 
+def _chairs_found(instances, chairs) -> int:
+    """Chairs with an instance within 1 cm / 1 degree of the generator's pose."""
+    import oracle as O
+    found = 0
+    for g in chairs:
+        found += any(O.pose_error(inst["pose"], g)[0] <= 0.01 and O.pose_error(inst["pose"], g)[1] <= np.radians(1.0)
+                     for inst in instances)
+    return found
+
+
 # ---------------------------------------------------------------------------
-# CPU baseline: the oracle (C restatement, OpenMP) on bounded samples
+# CPU baseline: the oracle (C restatement, OpenMP, all host threads)
 # ---------------------------------------------------------------------------
-def cpu_recognition_sample(scene, model, budget_s: float = 25.0) -> dict:
-    """Times every oracle stage on the full scene except the two costly ones:
-    matching on 1/8 of the scene keypoints (cost linear in them, x8) and
-    grouping on the correspondences of that 1/8 (cost quadratic, x64).
-    About 3 s of CPU work per sample on 16 cores."""
+def cpu_recognition(scene, model, steps: int = 1, warmup: int = 0) -> dict:
+    """The whole oracle pipeline on the whole config-1 scene, per step: voxel
+    filter, normals, keypoints, SHOT, exact 1-NN of every scene keypoint,
+    grouping of every correspondence (256-cluster cap, as on the GPU),
+    hypothesis scores, 16 ICP refinements, final scores.  The model is
+    prepared once beforehand, as on the GPU."""
     import oracle as O
     from oracle import pipeline as OP
     p = OP.params(viewpoint=CAM)
     m = OP.prepare_model(model, p)
-    t = {}
-    a = time.perf_counter()
-    sv = O.voxel_downsample(scene, p["voxel_leaf"]); t["voxel"] = time.perf_counter() - a
-    a = time.perf_counter()
-    sn = O.normals(sv, p["normal_k"], CAM); t["normals"] = time.perf_counter() - a
-    a = time.perf_counter()
-    keys = O.uniform_sample(sv, p["scene_keypoint_r"]); t["keypoints"] = time.perf_counter() - a
-    a = time.perf_counter()
-    sd, _ = O.shot352(sv, sn, keys, p["descriptor_r"]); t["shot"] = time.perf_counter() - a
-    frac = 8
-    sub = max(1, len(keys) // frac)
-    a = time.perf_counter()
-    idx, d2 = O.match(sd[:sub], m["desc"])
-    t["match"] = (time.perf_counter() - a) * (len(keys) / sub)
-    mm = d2 < np.float32(p["match_max_d2"])
-    cs = np.nonzero(mm)[0].astype(np.int32)
-    a = time.perf_counter()
-    O.gc_group(m["kp"], sv[keys], idx[mm], cs, d2[mm], p["gc_size"], p["gc_thresh"], p["max_clusters"])
-    t["gc"] = (time.perf_counter() - a) * (len(keys) / sub) ** 2
-    total = sum(t.values())
-    return {"value": 1.0 / total, "unit": "recognitions/s", "cores": O.num_threads(), "kind": "port",
-            "sample": "C oracle (OpenMP) on the config-1 scene: voxel/normals/keypoints/SHOT full; "
-                      "matching timed on 1/8 of the scene keypoints (x8, linear), grouping on the "
-                      "correspondences of that 1/8 (x64, quadratic in their count)",
-            "stage_s": {k: round(v, 3) for k, v in t.items()}}
+    for _ in range(warmup):
+        OP.recognize(m, scene, p)
+    times, stage = [], {}
+    r = None
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        r = OP.recognize(m, scene, p, timing=stage)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    return {"value": len(times) / total, "unit": "recognitions/s", "cores": O.num_threads(), "kind": "port",
+            "sample": f"full: {len(times)} whole recognitions of the config-1 scene by the C oracle (every scene "
+                      "keypoint matched, every correspondence grouped), model prepared beforehand",
+            "stage_s": {k: round(v / len(times), 3) for k, v in stage.items()},
+            "counts": {k: r[k] for k in ("n_voxels", "n_keypoints", "n_correspondences", "n_clusters")},
+            "instances": len(r["instances"])}
 
 
 def cpu_icp_sample(src, tgt, budget_s: float = 10.0) -> dict:
@@ -225,24 +232,29 @@ def cpu_icp_sample(src, tgt, budget_s: float = 10.0) -> dict:
 
 
 def run_reference(args):
+    """The reference arm: the CPU restatement of the path (oracle/, all host
+    threads) timed on the same workload, W untimed and K timed steps, each a
+    whole recognition of the config-1 room.  Its inputs come from
+    oracle/libsynth.so, so no library of the GPU path is loaded."""
     ws, rank, _ = _dist()
     if rank != 0:
         return 0
-    scene, model, chairs = _room()
-    times = []
-    for _ in range(max(1, min(args.steps, 3))):
-        c = cpu_recognition_sample(scene, model)
-        times.append(1.0 / c["value"])
-    v = 1.0 / (sum(times) / len(times))
-    src, tgt, _ = _icp_pair()
+    from oracle import synth as S
+    scene, model, chairs = _room(S)
+    c = cpu_recognition(scene, model, steps=args.steps, warmup=args.warmup)
+    v = c["value"]
+    src, tgt, _ = _icp_pair(S)
     icp = cpu_icp_sample(src, tgt, 5.0)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "recognitions/s",
-            "n_gpus": args.gpus, "steps": len(times), "warmup": 0, "ms_per_step": 1e3 / v,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": {"workload": "config1_room300k_chair20k", "room_seed": ROOM_SEED},
-            "cpu_baseline": {**c, "value": v},
+            "data": "synthetic", "config": {"workload": "config1_room300k_chair20k", "room_seed": ROOM_SEED,
+                                            "model_points": N_PTS, "scene_points": int(scene.shape[0])},
+            "cpu_baseline": {k: c[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "stage_s": c["stage_s"], "counts": c["counts"],
             "e2e": {"value": v, "unit": "recognitions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "icp": {"metric": "ICP iters/s (config 0)", "value": icp["value"], "unit": "iters/s"}}
+            "icp": {"metric": "ICP iters/s (config 0)", "value": icp["value"], "unit": "iters/s",
+                    "sample": icp["sample"]}}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -424,6 +436,7 @@ def run_ours(args):
         "counts": {k: r[k] for k in ("n_voxels", "n_keypoints", "n_correspondences", "n_clusters")},
         "model_keypoints": Km,
         "instances_err_to_nearest_chair_m_deg_score": _nearest_errors(r["instances"], chairs),
+        "chairs_within_1cm_1deg": f"{_chairs_found(r['instances'], chairs)} of {len(chairs)}",
         "e2e": e2e,
         "gpu_launches": int(launches),
         "clocks": clocks,
@@ -434,7 +447,7 @@ def run_ours(args):
         "reference_route": ref_route,
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_recognition_sample(scene, model)
+        line["cpu_baseline"] = cpu_recognition(scene, model, steps=1, warmup=0)
         line["icp"]["cpu_baseline"] = cpu_icp_sample(src, tgt, 5.0)
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -423,7 +423,7 @@ typedef struct rtr_recog_params {
   float voxel_leaf;             /* 0.01 m                                        */
   int   normal_k;               /* 10                                            */
   float scene_keypoint_r;       /* uniform sampling of the scene, 0.02 m         */
-  float model_keypoint_r;       /* uniform sampling of the model, 0.01 m         */
+  float model_keypoint_r;       /* uniform sampling of the model, 0.02 m         */
   float descriptor_r;           /* SHOT support radius, 0.04 m                   */
   float match_max_d2;           /* keep a match when d^2 < this (0.25)           */
   float gc_size;                /* consistency bin, 0.01 m                       */

@@ -34,12 +34,19 @@ _SIG = {
     "orc_transform_f32": (None, [_P, _P, _I, _P]),
     "orc_rigid_fit": (_I, [_P, _P, _P, _I, _P]),
     "orc_icp": (None, [_P, _I, _P, _I, _I, _F, _D, _D, _P, C.POINTER(IcpOut), _P, _P]),
+    "orc_grid_create": (_P, [_P, _I, _F]),
+    "orc_grid_destroy": (None, [_P]),
+    "orc_grid_nn1": (None, [_P, _P, _I, _F, _P, _P]),
+    "orc_grid_inlier_fraction": (None, [_P, _P, _I, _I, _P, _I, _F, _P]),
+    "orc_grid_icp": (None, [_P, _P, _I, _I, _F, _D, _D, _P, C.POINTER(IcpOut)]),
+    "orc_grid_icp_multi": (None, [_P, _P, _I, _I, _F, _P, _I, _P]),
     "orc_icp_replay": (None, [_P, _I, _P, _I, _F, _P, _I, _P, _P, _P]),
     "orc_tdf": (None, [_P, _I, _I, _P]),
     "orc_voxel_downsample": (_I, [_P, _I, _F, _P]),
     "orc_normals": (None, [_P, _I, _I, _P, _P]),
     "orc_eig3": (None, [_P, _P, _P]),
     "orc_uniform_sample": (_I, [_P, _I, _F, _P]),
+    "orc_set_shot_flags": (None, [_I]),
     "orc_shot352": (None, [_P, _P, _I, _P, _I, _F, _P, _P]),
     "orc_match": (None, [_P, _I, _P, _I, _I, _P, _P]),
     "orc_gc_group": (_I, [_P, _P, _P, _P, _P, _I, _F, _I, _I, _P, _P, _P]),
@@ -160,6 +167,57 @@ def icp(src, tgt, max_iterations=10, max_corr_dist=0.0, init=None, eps_t=0.0, ep
     return res
 
 
+class Grid:
+    """A target cloud's search grid kept across calls (exact searches: the
+    results equal the one-shot nn1 / icp calls')."""
+
+    def __init__(self, pts, cell: float = 0.0):
+        self.pts = _f4(pts)
+        self.h = lib().orc_grid_create(self.pts.ctypes.data, self.pts.shape[0], float(cell))
+
+    def close(self):
+        if self.h:
+            lib().orc_grid_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def nn1(self, q, max_dist: float = 0.0):
+        q = _f4(q)
+        idx = np.empty(q.shape[0], np.int32)
+        d2 = np.empty(q.shape[0], np.float32)
+        lib().orc_grid_nn1(self.h, q.ctypes.data, q.shape[0], _r2(max_dist), idx.ctypes.data, d2.ctypes.data)
+        return idx, d2
+
+    def inlier_fraction(self, src, stride: int, poses, r: float) -> np.ndarray:
+        src = _f4(src)
+        P = np.ascontiguousarray(poses, np.float64).reshape(-1, 16)
+        out = np.zeros(P.shape[0], np.float64)
+        lib().orc_grid_inlier_fraction(self.h, src.ctypes.data, src.shape[0], int(stride), P.ctypes.data,
+                                       P.shape[0], float(r), out.ctypes.data)
+        return out
+
+    def icp(self, src, max_iterations=10, max_corr_dist=0.0, init=None) -> dict:
+        src = _f4(src)
+        out = IcpOut()
+        ini = None if init is None else np.ascontiguousarray(init, np.float64).reshape(16)
+        lib().orc_grid_icp(self.h, src.ctypes.data, src.shape[0], max_iterations, float(max_corr_dist), 0.0, 0.0,
+                           None if ini is None else ini.ctypes.data, C.byref(out))
+        return {"pose": np.array(out.pose[:]).reshape(4, 4), "fitness": out.fitness,
+                "iterations": out.iterations, "converged": out.converged, "n_corr": out.n_corr}
+
+    def icp_multi(self, src, max_iterations, max_corr_dist, inits) -> list[dict]:
+        """Independent ICP problems from several initial poses, one per thread."""
+        src = _f4(src)
+        P = np.ascontiguousarray(inits, np.float64).reshape(-1, 16)
+        outs = (IcpOut * max(1, P.shape[0]))()
+        lib().orc_grid_icp_multi(self.h, src.ctypes.data, src.shape[0], int(max_iterations), float(max_corr_dist),
+                                 P.ctypes.data, P.shape[0], outs)
+        return [{"pose": np.array(o.pose[:]).reshape(4, 4), "fitness": o.fitness, "iterations": o.iterations,
+                 "converged": o.converged, "n_corr": o.n_corr} for o in outs[: P.shape[0]]]
+
+
 def icp_replay(src, tgt, max_corr_dist, poses_in):
     """Replay GPU iterations: poses_in[k] -> (corr[k], poses_out[k+1])."""
     src, tgt = _f4(src), _f4(tgt)
@@ -213,6 +271,13 @@ def uniform_sample(pts, r: float) -> np.ndarray:
     if k < 0:
         raise ValueError("voxel key space exceeds 32 bits")
     return out[:k].copy()
+
+
+def set_shot_flags(flags: int) -> None:
+    """Probe switches of the SHOT conventions (0 = the GPU path's): bit 0
+    keeps support points whose normals face away, bit 1 signs the LRF z axis
+    by the majority rule over the support's offsets."""
+    lib().orc_set_shot_flags(int(flags))
 
 
 def shot352(pts, nrm, keys, radius: float):

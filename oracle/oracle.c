@@ -193,20 +193,69 @@ static void cg_search(const cgrid* g, const float* qf, topk* T) {
   }
 }
 
-void orc_nn1_grid(const float* q, int nq, const float* t, int nt, float r2max, float cell, int32_t* idx,
-                  float* d2) {
-  cgrid g;
-  cg_build(&g, t, nt, cell > 0 ? cell : (r2max < INFINITY ? 0.5 * sqrt(r2max) : -1));
+static void cg_nn1(const cgrid* g, int nt, const float* q, int nq, float r2max, int32_t* idx, float* d2) {
 #pragma omp parallel for schedule(dynamic, 256)
   for (int i = 0; i < nq; ++i) {
     float bd = r2max;
     int bi = INT_MAX;
     topk T = {1, &bd, &bi};
-    if (nt > 0) cg_search(&g, q + 4 * i, &T);
+    if (nt > 0) cg_search(g, q + 4 * i, &T);
     idx[i] = bi == INT_MAX ? -1 : bi;
     if (d2) d2[i] = bi == INT_MAX ? INFINITY : bd;
   }
+}
+
+void orc_nn1_grid(const float* q, int nq, const float* t, int nt, float r2max, float cell, int32_t* idx,
+                  float* d2) {
+  cgrid g;
+  cg_build(&g, t, nt, cell > 0 ? cell : (r2max < INFINITY ? 0.5 * sqrt(r2max) : -1));
+  cg_nn1(&g, nt, q, nq, r2max, idx, d2);
   cg_free(&g);
+}
+
+/* A target grid kept across calls (the searches are exact, so their
+ * results do not depend on the cell size or on reusing the grid). */
+struct orc_grid {
+  cgrid g;
+  int n;
+};
+
+orc_grid* orc_grid_create(const float* pts, int n, float cell) {
+  orc_grid* G = (orc_grid*)malloc(sizeof(orc_grid));
+  cg_build(&G->g, pts, n, cell > 0 ? cell : -1.0);
+  G->n = n;
+  return G;
+}
+
+void orc_grid_destroy(orc_grid* G) {
+  if (!G) return;
+  cg_free(&G->g);
+  free(G);
+}
+
+void orc_grid_nn1(const orc_grid* G, const float* q, int nq, float r2max, int32_t* idx, float* d2) {
+  cg_nn1(&G->g, G->n, q, nq, r2max, idx, d2);
+}
+
+/* Fraction of every stride-th source point that lands, under each pose,
+ * within r of the grid's points: scores[h] for poses16[16 h]. */
+void orc_grid_inlier_fraction(const orc_grid* G, const float* src, int ns, int stride, const double* poses16,
+                              int nh, float r, double* scores) {
+  const int m = stride > 0 ? (ns + stride - 1) / stride : 0;
+  float* sub = (float*)malloc(sizeof(float) * 4 * (m > 0 ? m : 1));
+  float* tmp = (float*)malloc(sizeof(float) * 4 * (m > 0 ? m : 1));
+  int32_t* idx = (int32_t*)malloc(sizeof(int32_t) * (m > 0 ? m : 1));
+  for (int i = 0; i < m; ++i) memcpy(sub + 4 * i, src + 4 * (size_t)i * stride, 16);
+  for (int h = 0; h < nh; ++h) {
+    orc_transform_f32(poses16 + 16 * (size_t)h, sub, m, tmp);
+    cg_nn1(&G->g, G->n, tmp, m, r * r, idx, NULL);
+    int c = 0;
+    for (int i = 0; i < m; ++i) c += idx[i] >= 0;
+    scores[h] = (double)c / (double)(m > 0 ? m : 1);
+  }
+  free(sub);
+  free(tmp);
+  free(idx);
 }
 
 void orc_knn_brute(const float* q, int nq, const float* t, int nt, int k, int32_t* idx, float* d2) {
@@ -369,11 +418,11 @@ static void mat4mul(const double* A, const double* B, double* C) {
 /* One ICP iteration at pose P (PCL IterativeClosestPoint::computeTransformation:
  * transform source, correspondences by exact 1-NN with d^2 <= max^2, SVD
  * estimate on the transformed source, transformation = delta * transformation). */
-static int icp_step(const float* src, int ns, const float* tgt, int nt, float r2max, float cell, const double* P,
-                    int32_t* corr, float* tmp, double* Pnext, double* dT, double* fitness) {
+static int icp_step(const float* src, int ns, const cgrid* g, const float* tgt, int nt, float r2max,
+                    const double* P, int32_t* corr, float* tmp, double* Pnext, double* dT, double* fitness) {
   orc_transform_f32(P, src, ns, tmp);
   float* d2 = (float*)malloc(sizeof(float) * (ns > 0 ? ns : 1));
-  orc_nn1_grid(tmp, ns, tgt, nt, r2max, cell, corr, d2);
+  cg_nn1(g, nt, tmp, ns, r2max, corr, d2);
   double fs = 0;
   int m = 0;
   for (int i = 0; i < ns; ++i)
@@ -392,10 +441,10 @@ static int icp_step(const float* src, int ns, const float* tgt, int nt, float r2
   return m;
 }
 
-void orc_icp(const float* src, int ns, const float* tgt, int nt, int max_it, float max_dist, double eps_t,
-             double eps_r, const double* init, orc_icp_out* out, double* trace_pose, int32_t* trace_corr) {
+static void icp_run(const float* src, int ns, const cgrid* g, const float* tgt, int nt, int max_it,
+                    float max_dist, double eps_t, double eps_r, const double* init, orc_icp_out* out,
+                    double* trace_pose, int32_t* trace_corr) {
   const float r2max = (max_dist > 0 && max_dist < 1e18f) ? max_dist * max_dist : INFINITY;
-  const float cell = (max_dist > 0 && max_dist < 1e18f) ? 0.5f * max_dist : -1.f;
   double P[16];
   for (int k = 0; k < 16; ++k) P[k] = init ? init[k] : (k % 5 == 0);
   if (trace_pose) memcpy(trace_pose, P, sizeof(P));
@@ -407,7 +456,7 @@ void orc_icp(const float* src, int ns, const float* tgt, int nt, int max_it, flo
   out->n_corr = 0;
   for (int it = 0; it < max_it; ++it) {
     double Pn[16], dT[16], fit = 0;
-    int m = icp_step(src, ns, tgt, nt, r2max, cell, P, corr, tmp, Pn, dT, &fit);
+    int m = icp_step(src, ns, g, tgt, nt, r2max, P, corr, tmp, Pn, dT, &fit);
     if (trace_corr) memcpy(trace_corr + (size_t)it * ns, corr, sizeof(int32_t) * ns);
     out->iterations = it + 1;
     out->n_corr = m;
@@ -427,18 +476,47 @@ void orc_icp(const float* src, int ns, const float* tgt, int nt, int max_it, flo
   free(corr);
 }
 
+void orc_icp(const float* src, int ns, const float* tgt, int nt, int max_it, float max_dist, double eps_t,
+             double eps_r, const double* init, orc_icp_out* out, double* trace_pose, int32_t* trace_corr) {
+  /* the target grid is built once for all iterations */
+  const float cell = (max_dist > 0 && max_dist < 1e18f) ? 0.5f * max_dist : -1.f;
+  cgrid g;
+  cg_build(&g, tgt, nt, cell);
+  icp_run(src, ns, &g, tgt, nt, max_it, max_dist, eps_t, eps_r, init, out, trace_pose, trace_corr);
+  cg_free(&g);
+}
+
+/* ICP against a kept grid (its points are the target). */
+void orc_grid_icp(const orc_grid* G, const float* src, int ns, int max_it, float max_dist, double eps_t,
+                  double eps_r, const double* init, orc_icp_out* out) {
+  icp_run(src, ns, &G->g, G->g.pts, G->n, max_it, max_dist, eps_t, eps_r, init, out, NULL, NULL);
+}
+
+/* Several ICP problems of one source against a kept grid, one problem per
+ * thread (each problem's searches then run on its own thread). */
+void orc_grid_icp_multi(const orc_grid* G, const float* src, int ns, int max_it, float max_dist,
+                        const double* inits16, int nh, orc_icp_out* outs) {
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int h = 0; h < nh; ++h)
+    icp_run(src, ns, &G->g, G->g.pts, G->n, max_it, max_dist, 0.0, 0.0, inits16 + 16 * (size_t)h, outs + h,
+            NULL, NULL);
+}
+
 void orc_icp_replay(const float* src, int ns, const float* tgt, int nt, float max_dist, const double* poses_in,
                     int iters, int32_t* corr_out, double* poses_out, int32_t* ncorr_out) {
   const float r2max = (max_dist > 0 && max_dist < 1e18f) ? max_dist * max_dist : INFINITY;
   const float cell = (max_dist > 0 && max_dist < 1e18f) ? 0.5f * max_dist : -1.f;
   float* tmp = (float*)malloc(sizeof(float) * 4 * (ns > 0 ? ns : 1));
+  cgrid g;
+  cg_build(&g, tgt, nt, cell);
   memcpy(poses_out, poses_in, 16 * sizeof(double));
   for (int it = 0; it < iters; ++it) {
     double dT[16], fit = 0;
-    int m = icp_step(src, ns, tgt, nt, r2max, cell, poses_in + 16 * (size_t)it, corr_out + (size_t)it * ns, tmp,
+    int m = icp_step(src, ns, &g, tgt, nt, r2max, poses_in + 16 * (size_t)it, corr_out + (size_t)it * ns, tmp,
                      poses_out + 16 * (size_t)(it + 1), dT, &fit);
     if (ncorr_out) ncorr_out[it] = m;
   }
+  cg_free(&g);
   free(tmp);
 }
 
@@ -721,6 +799,14 @@ int orc_uniform_sample(const float* pts, int n, float r, int32_t* out_idx) {
  *  values are L2-normalised. */
 #define SHOT_PI 3.14159265358979f
 #define SHOT_FACING (-0.2f)
+
+/* Convention switches for probes of descriptor repeatability (0 = the
+ * conventions the GPU path uses).  bit 0: keep support points facing away
+ * (no n_j . n_k >= -0.2 filter); bit 1: sign of z by the paper's majority
+ * rule over the support's offsets instead of agreement with the oriented
+ * normals. */
+static int g_shot_flags = 0;
+void orc_set_shot_flags(int flags) { g_shot_flags = flags; }
 static void shot_bins(float pos, int nb, int circular, int* b0, float* w0, int* b1, float* w1) {
   const float fl = floorf(pos);
   int lo = (int)fl;
@@ -769,7 +855,7 @@ void orc_shot352(const float* pts, const float* normals, int n, const int32_t* k
             const float* nkp = normals + 4 * keys[kk];
             const float f0 = nj[0] * nkp[0], f1 = nj[1] * nkp[1], f2 = nj[2] * nkp[2];
             const float facing = (f0 + f1) + f2;
-            if (d2f(kp, pts + 4 * j) <= R2 && facing >= SHOT_FACING) {
+            if (d2f(kp, pts + 4 * j) <= R2 && (facing >= SHOT_FACING || (g_shot_flags & 1))) {
               if (cnt == cap) {
                 cap *= 2;
                 sup = (int*)realloc(sup, sizeof(int) * cap);
@@ -806,18 +892,20 @@ void orc_shot352(const float* pts, const float* normals, int n, const int32_t* k
     float ev[3], V[9];
     orc_eig3(M, ev, V);
     float X[3] = {V[2], V[5], V[8]}, Z[3] = {V[0], V[3], V[6]};
-    int px = 0, nx = 0;
+    int px = 0, nx = 0, pz = 0, nz = 0;
     float zn = 0.f;
     for (int s = 0; s < cnt; ++s) {
       const float* p = pts + 4 * sup[s];
       const float* nv = normals + 4 * sup[s];
       const float dx = p[0] - kp[0], dy = p[1] - kp[1], dz = p[2] - kp[2];
       if (dx * X[0] + dy * X[1] + dz * X[2] >= 0.f) ++px; else ++nx;
+      if (dx * Z[0] + dy * Z[1] + dz * Z[2] >= 0.f) ++pz; else ++nz;
       const float w = R - sqrtf(d2f(p, kp));
       zn += w * (nv[0] * Z[0] + nv[1] * Z[1] + nv[2] * Z[2]);
     }
     if (px < nx) for (int a = 0; a < 3; ++a) X[a] = -X[a];
-    if (zn < 0.f) for (int a = 0; a < 3; ++a) Z[a] = -Z[a];
+    if ((g_shot_flags & 2) ? (pz < nz) : (zn < 0.f))
+      for (int a = 0; a < 3; ++a) Z[a] = -Z[a];
     const float Y[3] = {Z[1] * X[2] - Z[2] * X[1], Z[2] * X[0] - Z[0] * X[2], Z[0] * X[1] - Z[1] * X[0]};
     if (lrf_out) {
       float* L = lrf_out + (size_t)kk * 9;
@@ -865,28 +953,72 @@ void orc_shot352(const float* pts, const float* normals, int n, const int32_t* k
   cg_free(&g);
 }
 
+/* Exact FP32 1-NN of descriptors: d^2 = sum over k in order of (a_k - b_k)^2,
+ * each operation rounded separately, ties to the lowest row.  For speed the
+ * database is read from a transposed copy, 16 rows x 4 queries at a time,
+ * with GCC's generic vector types: every lane holds one (query, row) pair's
+ * own running sum, added in the same k order, so each sum is bit-identical
+ * to the scalar loop's (no reassociation; -ffp-contract=off keeps the
+ * multiply and the add separate). */
+typedef float orc_v4 __attribute__((vector_size(16)));
+#define MATCH_RB 16
+#define MATCH_QB 4
 void orc_match(const float* q, int nq, const float* db, int ndb, int dim, int32_t* idx, float* d2) {
-#pragma omp parallel for schedule(dynamic, 64)
-  for (int i = 0; i < nq; ++i) {
-    const float* a = q + (size_t)i * dim;
-    float bd = INFINITY;
-    int bi = -1;
-    for (int j = 0; j < ndb; ++j) {
-      const float* b = db + (size_t)j * dim;
-      float s = 0.f;
-      for (int k = 0; k < dim; ++k) {
-        const float t = a[k] - b[k];
-        const float tt = t * t;
-        s = s + tt;
+  const int nblk = (ndb + MATCH_RB - 1) / MATCH_RB;
+  float* dbT = (float*)aligned_alloc(64, sizeof(float) * (size_t)(nblk > 0 ? nblk : 1) * dim * MATCH_RB);
+  for (int b = 0; b < nblk; ++b)
+    for (int k = 0; k < dim; ++k)
+      for (int r = 0; r < MATCH_RB; ++r) {
+        const int j = b * MATCH_RB + r;
+        dbT[((size_t)b * dim + k) * MATCH_RB + r] = j < ndb ? db[(size_t)j * dim + k] : 0.f;
       }
-      if (s < bd) {
-        bd = s;
-        bi = j;
+  const int nqb = (nq + MATCH_QB - 1) / MATCH_QB;
+#pragma omp parallel for schedule(dynamic, 8)
+  for (int qb = 0; qb < nqb; ++qb) {
+    const int q0 = qb * MATCH_QB;
+    const float* a[MATCH_QB];
+    float bd[MATCH_QB];
+    int bi[MATCH_QB];
+    for (int u = 0; u < MATCH_QB; ++u) {
+      a[u] = q + (size_t)(q0 + u < nq ? q0 + u : q0) * dim;
+      bd[u] = INFINITY;
+      bi[u] = -1;
+    }
+    for (int b = 0; b < nblk; ++b) {
+      const orc_v4* B = (const orc_v4*)(dbT + (size_t)b * dim * MATCH_RB);
+      orc_v4 acc[MATCH_QB][MATCH_RB / 4];
+      for (int u = 0; u < MATCH_QB; ++u)
+        for (int v = 0; v < MATCH_RB / 4; ++v) acc[u][v] = (orc_v4){0.f, 0.f, 0.f, 0.f};
+      for (int k = 0; k < dim; ++k) {
+        const orc_v4* Bk = B + (size_t)k * (MATCH_RB / 4);
+        for (int u = 0; u < MATCH_QB; ++u) {
+          const float x = a[u][k];
+          const orc_v4 xa = {x, x, x, x};
+          for (int v = 0; v < MATCH_RB / 4; ++v) {
+            const orc_v4 t = xa - Bk[v];
+            const orc_v4 tt = t * t;
+            acc[u][v] = acc[u][v] + tt;
+          }
+        }
+      }
+      for (int u = 0; u < MATCH_QB; ++u) {
+        float sums[MATCH_RB];
+        memcpy(sums, acc[u], sizeof(sums));
+        for (int r = 0; r < MATCH_RB; ++r) {
+          const int j = b * MATCH_RB + r;
+          if (j < ndb && sums[r] < bd[u]) {
+            bd[u] = sums[r];
+            bi[u] = j;
+          }
+        }
       }
     }
-    idx[i] = bi;
-    if (d2) d2[i] = bd;
+    for (int u = 0; u < MATCH_QB && q0 + u < nq; ++u) {
+      idx[q0 + u] = bi[u];
+      if (d2) d2[q0 + u] = bd[u];
+    }
   }
+  free(dbT);
 }
 
 typedef struct {
@@ -919,20 +1051,36 @@ int orc_gc_group(const float* mk, const float* sk, const int32_t* cm, const int3
   }
   qsort(ord, (size_t)nc, sizeof(dk_t), dk_cmp);
   char* taken = (char*)calloc((size_t)nc + 1, 1);
+  /* pass[b]: candidate ord[b] is consistent with the current seed — the
+   * first member every candidate is tested against, computed for all
+   * candidates in parallel; the in-order admission then tests the other
+   * members only.  Same predicate, same order, same sets. */
+  char* pass = (char*)malloc((size_t)nc + 1);
   int* set = (int*)malloc(sizeof(int) * (nc > 0 ? nc : 1));
   float* P = (float*)malloc(sizeof(float) * 4 * (nc > 0 ? nc : 1));
   float* Q = (float*)malloc(sizeof(float) * 4 * (nc > 0 ? nc : 1));
   int ncl = 0;
-  for (int a = 0; a < nc; ++a) {
+  /* clusters past max_clusters are not reported, and the walk that finds
+   * the first max_clusters does not depend on later seeds: stop there */
+  for (int a = 0; a < nc && ncl < max_clusters; ++a) {
     const int i = ord[a].i;
     if (taken[i]) continue;
+    const float* mi = mk + 4 * cm[i];
+    const float* si = sk + 4 * cs[i];
+#pragma omp parallel for schedule(static, 4096)
+    for (int b = 0; b < nc; ++b) {
+      const int j = ord[b].i;
+      const float dm = sqrtf(d2f(mi, mk + 4 * cm[j]));
+      const float ds = sqrtf(d2f(si, sk + 4 * cs[j]));
+      pass[b] = !(fabsf(dm - ds) > gc_size);
+    }
     int ns = 0;
     set[ns++] = i;
     for (int b = 0; b < nc; ++b) {
       const int j = ord[b].i;
-      if (j == i || taken[j]) continue;
+      if (j == i || taken[j] || !pass[b]) continue;
       int ok = 1;
-      for (int s = 0; s < ns && ok; ++s) {
+      for (int s = 1; s < ns && ok; ++s) {
         const int m = set[s];
         const float dm = sqrtf(d2f(mk + 4 * cm[m], mk + 4 * cm[j]));
         const float ds = sqrtf(d2f(sk + 4 * cs[m], sk + 4 * cs[j]));
@@ -945,21 +1093,20 @@ int orc_gc_group(const float* mk, const float* sk, const int32_t* cm, const int3
         taken[set[s]] = 1;
         cluster_of[set[s]] = ncl;
       }
-      if (ncl < max_clusters) {
-        for (int s = 0; s < ns; ++s) {
-          memcpy(P + 4 * s, mk + 4 * cm[set[s]], 16);
-          memcpy(Q + 4 * s, sk + 4 * cs[set[s]], 16);
-        }
-        orc_rigid_fit(P, Q, NULL, ns, poses16 + 16 * ncl);
-        sizes[ncl] = ns;
+      for (int s = 0; s < ns; ++s) {
+        memcpy(P + 4 * s, mk + 4 * cm[set[s]], 16);
+        memcpy(Q + 4 * s, sk + 4 * cs[set[s]], 16);
       }
+      orc_rigid_fit(P, Q, NULL, ns, poses16 + 16 * ncl);
+      sizes[ncl] = ns;
       ++ncl;
     }
   }
   free(ord);
   free(taken);
+  free(pass);
   free(set);
   free(P);
   free(Q);
-  return ncl < max_clusters ? ncl : max_clusters;
+  return ncl;
 }

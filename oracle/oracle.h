@@ -48,6 +48,18 @@ typedef struct orc_icp_out {
   int converged;
   int n_corr;
 } orc_icp_out;
+/* A target grid kept across calls: exact 1-NN, inlier fractions of posed
+ * source subsets, and ICP against it (results equal the one-shot calls'). */
+typedef struct orc_grid orc_grid;
+orc_grid* orc_grid_create(const float* pts, int n, float cell);
+void orc_grid_destroy(orc_grid* g);
+void orc_grid_nn1(const orc_grid* g, const float* q, int nq, float r2max, int32_t* idx, float* d2);
+void orc_grid_inlier_fraction(const orc_grid* g, const float* src, int ns, int stride, const double* poses16,
+                              int nh, float r, double* scores);
+void orc_grid_icp(const orc_grid* g, const float* src, int ns, int max_it, float max_dist, double eps_t,
+                  double eps_r, const double* init16, orc_icp_out* out);
+void orc_grid_icp_multi(const orc_grid* g, const float* src, int ns, int max_it, float max_dist,
+                        const double* inits16, int nh, orc_icp_out* outs);
 /* Full oracle ICP: fixed max_iterations unless eps_t > 0 criteria stop it. */
 void orc_icp(const float* src, int ns, const float* tgt, int nt, int max_it, float max_dist,
              double eps_t, double eps_r, const double* init16, orc_icp_out* out,
@@ -87,6 +99,7 @@ int orc_uniform_sample(const float* pts, int n, float r, int32_t* out_idx);
 
 /* ---- SHOT-style 352-d descriptor (Tombari, Salti, Di Stefano 2010) with the
  * conventions in oracle.c.  keys: indices into pts. */
+void orc_set_shot_flags(int flags);
 void orc_shot352(const float* pts, const float* normals, int n, const int32_t* keys, int nk,
                  float radius, float* desc, float* lrf9);
 

@@ -12,10 +12,10 @@ from __future__ import annotations
 
 import numpy as np
 
-from . import (gc_group, icp, match, nn1, normals, orient_outward, shot352, transform_f32,
-               uniform_sample, voxel_downsample)
+from . import (Grid, gc_group, match, normals, orient_outward, shot352, uniform_sample,
+               voxel_downsample)
 
-DEFAULTS = dict(voxel_leaf=0.01, normal_k=10, scene_keypoint_r=0.02, model_keypoint_r=0.01,
+DEFAULTS = dict(voxel_leaf=0.01, normal_k=10, scene_keypoint_r=0.02, model_keypoint_r=0.02,
                 descriptor_r=0.04, match_max_d2=0.25, gc_size=0.01, gc_thresh=5, max_clusters=256,
                 hv_inlier_r=0.02, hv_subsample=4, refine_top=16, icp_iterations=30,
                 icp_max_dist=0.02, accept_inlier_r=0.01, accept_score=0.2, nms_dist=0.1,
@@ -37,22 +37,31 @@ def prepare_model(pts, p: dict) -> dict:
     return {"vox": v, "nrm": n, "keys": k, "kp": v[k], "desc": d}
 
 
-def _score(model_vox, scene_vox, pose, stride, r):
-    sub = model_vox[::stride]
-    _, d2 = nn1(transform_f32(pose, sub), scene_vox, r)
-    return float(np.isfinite(d2).sum()) / max(1, len(sub))
+def recognize(model: dict, scene, p: dict, stages: dict | None = None, timing: dict | None = None) -> dict:
+    """timing (optional): filled with seconds per stage."""
+    import time
+    clock = [time.perf_counter()]
 
+    def lap(name):
+        if timing is not None:
+            now = time.perf_counter()
+            timing[name] = timing.get(name, 0.0) + now - clock[0]
+            clock[0] = now
 
-def recognize(model: dict, scene, p: dict, stages: dict | None = None) -> dict:
     sv = voxel_downsample(scene, p["voxel_leaf"])
+    lap("voxel")
     sn = normals(sv, p["normal_k"], p["viewpoint"])
     if p["scene_outward"]:
         sn = orient_outward(sv, sn)
+    lap("normals")
     keys = uniform_sample(sv, p["scene_keypoint_r"])
     if p["keypoint_min_curvature"] > 0:
         keys = keys[sn[keys, 3] >= np.float32(p["keypoint_min_curvature"])]
+    lap("keypoints")
     sd, _ = shot352(sv, sn, keys, p["descriptor_r"])
+    lap("shot")
     idx, d2 = match(sd, model["desc"])
+    lap("match")
     m = (idx >= 0) & (d2 < np.float32(p["match_max_d2"]))
     cs = np.nonzero(m)[0].astype(np.int32)
     cm = idx[m]
@@ -64,19 +73,25 @@ def recognize(model: dict, scene, p: dict, stages: dict | None = None) -> dict:
     if len(cs) == 0:
         out["n_clusters"] = 0
         return out
-    _, poses, sizes = gc_group(model["kp"], sv[keys], cm, cs, cd, p["gc_size"], p["gc_thresh"],
-                               p["max_clusters"])
+    clus, poses, sizes = gc_group(model["kp"], sv[keys], cm, cs, cd, p["gc_size"], p["gc_thresh"],
+                                  p["max_clusters"])
+    lap("grouping")
+    if stages is not None:
+        stages.update(corr_s=cs, corr_m=cm, cluster_of=clus)
     out["n_clusters"] = len(sizes)
     if len(sizes) == 0:
         return out
-    hv = np.array([_score(model["vox"], sv, poses[h], p["hv_subsample"], p["hv_inlier_r"])
-                   for h in range(len(sizes))])
+    # one exact search grid over the scene voxels serves the hypothesis
+    # scores, the ICP refinements and the final scores
+    grid = Grid(sv, 0.5 * p["icp_max_dist"])
+    hv = grid.inlier_fraction(model["vox"], p["hv_subsample"], poses, p["hv_inlier_r"])
     order = sorted(range(len(sizes)), key=lambda h: (-hv[h], h))[: p["refine_top"]]
-    refined, fscore = [], []
-    for h in order:
-        r = icp(model["vox"], sv, p["icp_iterations"], p["icp_max_dist"], init=poses[h])
-        refined.append(r["pose"])
-        fscore.append(_score(model["vox"], sv, r["pose"], 1, p["accept_inlier_r"]))
+    refined = [r["pose"] for r in grid.icp_multi(model["vox"], p["icp_iterations"], p["icp_max_dist"],
+                                                 poses[order])] if order else []
+    fscore = list(grid.inlier_fraction(model["vox"], 1, np.array(refined).reshape(-1, 16),
+                                       p["accept_inlier_r"])) if refined else []
+    grid.close()
+    lap("verify_refine")
     picked = []
     for k in sorted(range(len(order)), key=lambda k: (-fscore[k], k)):
         if len(picked) >= p["max_instances"] or fscore[k] < p["accept_score"]:

@@ -322,7 +322,7 @@ void rtr_recog_default_params(rtr_recog_params* p) {
   p->voxel_leaf = 0.01f;
   p->normal_k = 10;
   p->scene_keypoint_r = 0.02f;
-  p->model_keypoint_r = 0.01f;
+  p->model_keypoint_r = 0.02f;
   p->descriptor_r = 0.04f;
   p->match_max_d2 = 0.25f;
   p->gc_size = 0.01f;

@@ -25,7 +25,7 @@ def _pair(R, seed):
     return model, seg, T
 
 
-@pytest.mark.parametrize("seed", [0, 1])
+@pytest.mark.parametrize("seed", [1, 3])
 def test_recognize_pair_matches_oracle(ctx, rtr, seed):
     model, seg, T = _pair(rtr, seed)
     prm = rtr.recog_default_params(scene_outward=1)
@@ -48,7 +48,7 @@ def test_recognize_pair_matches_oracle(ctx, rtr, seed):
 
 def test_recognize_host_entry_and_empty_scene(ctx, rtr):
     import torch
-    model, seg, T = _pair(rtr, 0)
+    model, seg, T = _pair(rtr, 1)
     prm = rtr.recog_default_params(scene_outward=1)
     m = rtr.Model(ctx, _dev(model), prm)
     r = rtr.recognize_host(ctx, m, seg, prm)

@@ -171,3 +171,17 @@ def test_pcd_io_round_trips_main_clouds(tmp_path):
     r = subprocess.run([str(demo), "pcd", str(bad), str(tmp_path / "x.pcd"), str(tmp_path / "y.pcd")],
                        capture_output=True, text=True, timeout=60)
     assert r.returncode == 2
+
+
+def test_host_only_generator_matches_the_library(rtr):
+    """oracle/libsynth.so (the CPU baseline's input generator, built without
+    CUDA from the same synth.cpp) gives the same clouds as librtr.so."""
+    from oracle import synth as S
+    a, sa, pa = rtr.synth_room(1)
+    b, sb, pb = S.synth_room(1)
+    assert np.array_equal(a, b) and np.array_equal(sa, sb) and np.array_equal(pa, pb)
+    assert np.array_equal(rtr.synth_shape(rtr.CHAIR, 20000, 2024), S.synth_shape(S.CHAIR, 20000, 2024))
+    for x, y in zip(rtr.config0_pair(2024, 5000), S.config0_pair(2024, 5000)):
+        assert np.array_equal(x, y)
+    crop = rtr.synth_crop(rtr.synth_shape(rtr.SOFA, 3000, 4), 0.4, 4)
+    assert np.array_equal(crop, S.synth_crop(S.synth_shape(S.SOFA, 3000, 4), 0.4, 4))
