@@ -168,17 +168,17 @@ rtr_status rtr_ref_tdf(rtr_context* ctx, const float* d_cloud, const float* d_ke
  * moved by (k - sk), turned 36 times by 10 degrees about the keypoint's
  * vertical axis (cumulatively, in float), and each time its occupied leaves
  * in the keypoint's field box (all but the first) read the field as
- * grid[y*30 + z*900 + x]; the running score is (score + sum of squared field
- * values) / (leaves - 1), the lowest wins.  d_score[p] = that score (float),
+ * grid[y*30 + z*900 + x]; as in the reference, the squared field values are
+ * added in float, leaf by leaf in the tree's depth-first order, into a
+ * running score that no rotation resets, which is then divided by
+ * (leaves - 1) in float; the lowest wins.  d_score[p] = that score,
  * d_T[16p] = the row-major 4x4 scale(kz/sz) * T(k) * Rz(best) * T(-k) *
  * T(k - sk).  Definitions where the reference is undefined: a field index
  * outside [0, 27000) reads 900; a cloud that would need more than 21 octree
- * levels, or a non-finite keypoint, gives score NaN and the identity.  One
- * change: each rotation's sum is exact (integers) and the running score is
- * kept in double (the reference adds in float, leaf by leaf; the two agree
- * to a few parts in 10^5).  The field must be 30^3 (half_tdf / resolution
- * = 15); occupancy clouds of up to 8192 points whose rotated extent stays
- * within 32 leaves (half_box <= 0.106 m at 1 cm). */
+ * levels, or a non-finite keypoint, gives score NaN and the identity.  The
+ * field must be 30^3 (half_tdf / resolution = 15); occupancy clouds of up to
+ * 8192 points whose rotated extent stays within 32 leaves (half_box <=
+ * 0.106 m at 1 cm). */
 rtr_status rtr_ref_distance(rtr_context* ctx, const float* d_mcloud, const float* d_mkeys,
                             int n_model, const int32_t* d_moffsets, const int32_t* d_mindices,
                             const float* d_mtdf, const float* d_skeys, int n_scan,
@@ -242,7 +242,11 @@ rtr_status rtr_knn1(rtr_context* ctx, const float* d_query, int n_query,
  *
  * The first call on a device looks up the array's address
  * (cudaGetSymbolAddress), which may load the module; make that first call
- * before capturing a stream.  The array is shared by every call on a device:
+ * before capturing a stream.  The address is kept for the life of the
+ * process, so calls after cudaDeviceReset on that device are not supported.
+ * Every buffer must be device (or managed) memory of the current device;
+ * others return RTR_ERR_INVALID_ARG before any launch.  The array is shared
+ * by every call on a device:
  * two calls whose work overlaps in time (different streams, or different
  * host threads, without ordering between them) race and both may return wrong
  * indices.  Order them on one stream or with events. */

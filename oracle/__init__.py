@@ -364,9 +364,12 @@ def ref_tdf(cloud, keys, offsets, indices, res: float = 0.01, half: float = 0.15
 
 
 def ref_distance(mcloud, mkeys, moff, midx, mtdf, skeys, pair_m=None, pair_s=None, res: float = 0.01,
-                 half: float = 0.15, float_order: bool = False):
+                 half: float = 0.15, float_order: bool = True):
     """get_Distance for pairs (all model x scan pairs, model-major, when
-    pair_m is None): (score [P] float32, T [P, 4, 4] float32)."""
+    pair_m is None): (score [P] float32, T [P, 4, 4] float32).  float_order
+    (default): the reference's float running sum, leaf by leaf in tree order;
+    False: exact integer sums per rotation with a double running score (a
+    variant kept to measure the difference)."""
     mcloud, mkeys, skeys = _f4(mcloud), _f4(mkeys), _f4(skeys)
     moff, midx = _i32(moff), _i32(midx)
     mtdf = np.ascontiguousarray(mtdf, np.float32)

@@ -40,10 +40,12 @@
  *     it is the identity;
  *   - a cloud that would grow the tree past 21 levels, or a non-finite
  *     keypoint: score NaN, identity.
- * And one deliberate change: get_Distance accumulates its running score in
- * float in leaf order; here each rotation's sum of squared field values is
- * exact (integers) and the running score is kept in double (float_order = 1
- * gives the reference's float accumulation, to measure the difference).
+ * get_Distance accumulates its running score in float, leaf by leaf in
+ * tree order, never reset between rotations (matching.h:141,179-189):
+ * float_order = 1 reproduces that and is what the GPU path matches bit for
+ * bit.  float_order = 0 is a variant kept to measure the rounding: each
+ * rotation's sum of squared field values exact (integers), the running
+ * score in double.
  *
  * Arithmetic (compile with -ffp-contract=off): transforms are
  * ((m0*x + m1*y) + m2*z) + m3 per row in float; 4x4 float products sum

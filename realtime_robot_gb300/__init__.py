@@ -308,12 +308,17 @@ class Context:
         preallocated by the caller; allocated here when omitted."""
         import torch
         nq, nt = query.shape[0], target.shape[0]
+        for t in (target,) + (tuple(out) if out is not None else ()):
+            if t.device != query.device:
+                raise ValueError("knn1_static: query, target and outputs must be on one device")
         if out is None:
             out = (torch.empty(nq, dtype=torch.int32, device=query.device),
                    torch.empty(nq, dtype=torch.float32, device=query.device))
         idx, d2 = out
-        check(lib().rtr_knn1_static(_ptr(query), nq, _ptr(target), nt, float(max_dist),
-                                    _ptr(idx), _ptr(d2), _stream(stream)))
+        # the entry point runs on the calling thread's current device
+        with torch.cuda.device(query.device):
+            check(lib().rtr_knn1_static(_ptr(query), nq, _ptr(target), nt, float(max_dist),
+                                        _ptr(idx), _ptr(d2), _stream(stream)))
         return idx, d2
 
     def synth_depth_frames(self, boxes: np.ndarray, poses: np.ndarray, width=640, height=480, fx=525.0, fy=525.0,

@@ -37,7 +37,9 @@
 //                    first leaf dropped, as integer voxels -> k_tdf (tdf.cu);
 //   k_ref_distance   36 yaw steps of the translated occupancy cloud, leaves
 //                    deduplicated in a 32^3 bitmap around the cloud, the
-//                    field read per leaf, score recurrence, pair transform;
+//                    field read per leaf, the leaves sorted into tree order
+//                    and their squared values added in float one by one
+//                    (the reference's running score), pair transform;
 //   k_ref_gates / k_ref_scatter   the kept pairs in loop order;
 //   k_ref_ransac / k_ref_argmax   inliers of every kept pair's transform.
 #include <math.h>
@@ -55,7 +57,6 @@ constexpr int REF_PPT = 8;        // cloud points per thread in k_ref_distance
 constexpr int REF_WIN = 32;       // leaves per axis of the distance kernel's bitmap window
 constexpr int REF_OCC_DEPTH = 5;  // cube depth the occupancy and field kernels hold in a bitmap
 constexpr double REF_FLT_EPS = 1.1920928955078125e-07;  // FLT_EPSILON
-constexpr double REF_SIZE_MAX = 18446744073709551615.0;  // (double)(size_t)-1
 
 // error bits of the status word
 constexpr int REF_ERR_WINDOW = 1;  // a rotated occupancy cloud spans more than REF_WIN leaves
@@ -414,9 +415,52 @@ struct RefShared {
   int first[NT / 32];
   unsigned long long mmin[NT / 32];
   unsigned kmin[NT / 32][3], kmax[NT / 32][3];
-  long long sum[NT / 32];
-  int cnt[NT / 32];
+  int u;  // distinct leaves of the current rotation
   float px, py, pz;
+};
+
+// get_Distance adds the squared field values of a rotation's leaves (all but
+// the first) in float, one by one in the octree's depth-first order, into a
+// running score that no rotation resets (matching.h:141,179-189).  Float
+// addition does not reassociate, so the leaves are first put in that order:
+// a bitonic sort of (Morton code, field value) pairs in shared memory (codes
+// are distinct; padding keys are ~0), then one thread adds them in sequence.
+// P is a power of two >= 2; `t` / `nt` this thread's index and the number of
+// threads sorting; `sync` orders the stages (__syncwarp or __syncthreads).
+template <class Sync>
+__device__ __forceinline__ void leaf_sort(unsigned long long* key, float* val, int P, int t, int nt, Sync sync) {
+  for (int k = 2; k <= P; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int q = t; q < (P >> 1); q += nt) {
+        const int i = ((q & ~(j - 1)) << 1) | (q & (j - 1));  // bit j of i clear
+        const int l = i | j;
+        const unsigned long long a = key[i], b = key[l];
+        if ((a > b) == ((i & k) == 0)) {
+          key[i] = b;
+          key[l] = a;
+          const float x = val[i];
+          val[i] = val[l];
+          val[l] = x;
+        }
+      }
+      sync();
+    }
+}
+
+// The running score's update for one rotation from its sorted leaves:
+// score = (score + v_1^2 + ... + v_{u-1}^2) / (u - 1), each operation a
+// float operation rounded to nearest; (size_t)(u - 1) is 2^64 for u = 0.
+__device__ __forceinline__ float leaf_running_score(float dtf, const float* val, int u) {
+  for (int i = 1; i < u; ++i) dtf = __fadd_rn(dtf, __fmul_rn(val[i], val[i]));
+  const float div = u == 0 ? 18446744073709551616.f : (float)(u - 1);
+  return __fdiv_rn(dtf, div);
+}
+
+struct WarpSync {
+  __device__ void operator()() const { __syncwarp(); }
+};
+struct BlockSync {
+  __device__ void operator()() const { __syncthreads(); }
 };
 
 __device__ __forceinline__ float field_at(const float* __restrict__ grid, const OctBox& b, unsigned kx, unsigned ky,
@@ -445,7 +489,10 @@ __global__ void __launch_bounds__(NT) k_ref_distance(const float4* __restrict__ 
                                                      RefRot rot, float* __restrict__ score, float* __restrict__ Tout,
                                                      int* __restrict__ err) {
   constexpr int NW = NT / 32;
+  constexpr int CAP = NT * REF_PPT;  // distinct leaves <= points
   __shared__ RefShared<NT> sh;
+  extern __shared__ unsigned long long s_leaf_key[];  // [CAP] keys, then [CAP] floats
+  float* s_leaf_val = reinterpret_cast<float*>(s_leaf_key + CAP);
   const long long p = blockIdx.x;
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const int m = pair_m ? pair_m[p] : (int)(p / ns);
@@ -493,7 +540,7 @@ __global__ void __launch_bounds__(NT) k_ref_distance(const float4* __restrict__ 
   }
   OctBox b0;
   oct_define(b0, lo, hi, dres);
-  double dt = 0.0, best = 100000000.0;
+  float dtf = 0.f, bestf = 100000000.f;
   int best_i = 0;
   bool bad = false;
   for (int it = 0; it < 36 && !bad; ++it) {
@@ -566,6 +613,7 @@ __global__ void __launch_bounds__(NT) k_ref_distance(const float4* __restrict__ 
       for (int a = 0; a < 3; ++a) sh.kmin[w][a] = kmin[a], sh.kmax[w][a] = kmax[a];
     }
     for (int i = tid; i < REF_WIN * REF_WIN * REF_WIN / 32; i += NT) sh.bm[i] = 0u;
+    if (tid == 0) sh.u = 0;
     __syncthreads();
     for (int i = 0; i < NW; ++i) {
       mmin = min(mmin, sh.mmin[i]);
@@ -575,9 +623,8 @@ __global__ void __launch_bounds__(NT) k_ref_distance(const float4* __restrict__ 
     const bool window_ok = n == 0 || (kmax[0] - kmin[0] < (unsigned)REF_WIN && kmax[1] - kmin[1] < (unsigned)REF_WIN &&
                                       kmax[2] - kmin[2] < (unsigned)REF_WIN);
     if (!window_ok && tid == 0) atomicOr(err, REF_ERR_WINDOW);
-    // distinct leaves: the thread that sets a leaf's bit reads its field
-    long long sum = 0;
-    int cnt = 0;
+    // distinct leaves: the thread that sets a leaf's bit reads its field and
+    // lists (Morton code, value); the first leaf's value is never added
     if (window_ok) {
 #pragma unroll
       for (int q = 0; q < REF_PPT; ++q) {
@@ -588,27 +635,23 @@ __global__ void __launch_bounds__(NT) k_ref_distance(const float4* __restrict__ 
         const unsigned bit = 1u << (l & 31u);
         const unsigned old = atomicOr(&sh.bm[l >> 5], bit);
         if (old & bit) continue;
-        ++cnt;
-        if (mc[q] == mmin) continue;
-        const float v = field_at(grid, b, kx, ky, kz, lo, res);
-        sum += (long long)v * (long long)v;
+        const float v = mc[q] == mmin ? 0.f : field_at(grid, b, kx, ky, kz, lo, res);
+        const int slot = atomicAdd(&sh.u, 1);
+        s_leaf_key[slot] = mc[q];
+        s_leaf_val[slot] = v;
       }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      sum += __shfl_xor_sync(0xffffffffu, sum, o);
-      cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-    }
-    if (lane == 0) sh.sum[w] = sum, sh.cnt[w] = cnt;
     __syncthreads();
+    const int u = sh.u;
+    int P = 2;
+    while (P < u) P <<= 1;
+    for (int i = u + tid; i < P; i += NT) s_leaf_key[i] = ~0ull;
+    __syncthreads();
+    leaf_sort(s_leaf_key, s_leaf_val, P, tid, NT, BlockSync());
     if (tid == 0) {
-      long long S = 0;
-      int u = 0;
-      for (int i = 0; i < NW; ++i) S += sh.sum[i], u += sh.cnt[i];
-      const double div = u == 0 ? REF_SIZE_MAX : (double)(u - 1);
-      dt = __ddiv_rn(__dadd_rn(dt, (double)S), div);
-      if (dt < best) {
-        best = dt;
+      dtf = leaf_running_score(dtf, s_leaf_val, u);
+      if (dtf < bestf) {
+        bestf = dtf;
         best_i = it;
       }
     }
@@ -620,7 +663,7 @@ __global__ void __launch_bounds__(NT) k_ref_distance(const float4* __restrict__ 
     eye4(To);
     return;
   }
-  score[p] = __double2float_rn(best);
+  score[p] = bestf;
   float S[16], R2[16], A[16];
   eye4(S);
   const float cs = __fdiv_rn(km.z, ks.z);
@@ -639,9 +682,9 @@ __global__ void __launch_bounds__(NT) k_ref_distance(const float4* __restrict__ 
 // shuffle, the growth's point broadcast by shuffle, and the warp's own 4 KB
 // bitmap cleared by the points that set it.
 constexpr int REFW_PPT = 8;
-constexpr int REFW_WARPS = 8;
+constexpr int REFW_WARPS = 4;
 
-__global__ void __launch_bounds__(32 * REFW_WARPS, 2)
+__global__ void __launch_bounds__(32 * REFW_WARPS, 4)
     k_ref_distance_warp(const float4* __restrict__ mcloud, const float4* __restrict__ mkeys,
                         const int* __restrict__ moff, const int* __restrict__ midx, const float* __restrict__ mtdf,
                         const float4* __restrict__ skeys, int ns, const int* __restrict__ pair_m,
@@ -649,6 +692,9 @@ __global__ void __launch_bounds__(32 * REFW_WARPS, 2)
                         float* __restrict__ score, float* __restrict__ Tout, int* __restrict__ err) {
   __shared__ unsigned s_bm[REFW_WARPS][REF_WIN * REF_WIN * REF_WIN / 32];
   __shared__ long long s_ix[REFW_WARPS][3][REF_WIN];
+  __shared__ unsigned long long s_key[REFW_WARPS][REFW_PPT * 32];
+  __shared__ float s_val[REFW_WARPS][REFW_PPT * 32];
+  __shared__ int s_u[REFW_WARPS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   unsigned* bm = s_bm[w];
   const float inv = __fdiv_rn(1.f, res);
@@ -701,7 +747,7 @@ __global__ void __launch_bounds__(32 * REFW_WARPS, 2)
     oct_define(b0, lo, hi, dres);
     OctBoxF bf0;
     oct_float(b0, bf0);
-    double dt = 0.0, best = 100000000.0;
+    float dtf = 0.f, bestf = 100000000.f;
     int best_i = 0;
     bool bad = false;
     for (int it = 0; it < 36 && !bad; ++it) {
@@ -781,38 +827,45 @@ __global__ void __launch_bounds__(32 * REFW_WARPS, 2)
         demorton3(mmin, b.depth, fx, fy, fz);
         pk_first = (unsigned long long)fx | ((unsigned long long)fy << 21) | ((unsigned long long)fz << 42);
       }
+      if (lane == 0) s_u[w] = 0;
       __syncwarp();
-      long long sum = 0;
-      int cnt = 0;
+      // distinct leaves: the lane that sets a leaf's bit reads its field and
+      // lists (Morton code, value); the first leaf's value is never added
       unsigned lw[REFW_PPT];
 #pragma unroll
       for (int q = 0; q < REFW_PPT; ++q) {
         lw[q] = 0xffffffffu;
         if (!window_ok || pk[q] == ~0ull) continue;
-        const unsigned lx = (unsigned)(pk[q] & 0x1fffffull) - kmin[0];
-        const unsigned ly = (unsigned)((pk[q] >> 21) & 0x1fffffull) - kmin[1];
-        const unsigned lz = (unsigned)(pk[q] >> 42) - kmin[2];
+        const unsigned kx = (unsigned)(pk[q] & 0x1fffffull), ky = (unsigned)((pk[q] >> 21) & 0x1fffffull),
+                       kz = (unsigned)(pk[q] >> 42);
+        const unsigned lx = kx - kmin[0], ly = ky - kmin[1], lz = kz - kmin[2];
         const unsigned l = lx + REF_WIN * (ly + REF_WIN * lz);
         lw[q] = l >> 5;
         const unsigned bit = 1u << (l & 31u);
         const unsigned old = atomicOr(&bm[l >> 5], bit);
         if (old & bit) continue;
-        ++cnt;
-        if (pk[q] == pk_first) continue;
-        const long long idx = s_ix[w][1][ly] * REF_DIM + s_ix[w][2][lz] * (REF_DIM * REF_DIM) + s_ix[w][0][lx];
-        const float v = (idx >= 0 && idx < REF_VOL) ? __ldg(grid + idx) : 900.f;
-        sum += (long long)v * (long long)v;
+        float v = 0.f;
+        if (pk[q] != pk_first) {
+          const long long idx = s_ix[w][1][ly] * REF_DIM + s_ix[w][2][lz] * (REF_DIM * REF_DIM) + s_ix[w][0][lx];
+          v = (idx >= 0 && idx < REF_VOL) ? __ldg(grid + idx) : 900.f;
+        }
+        const int slot = atomicAdd(&s_u[w], 1);
+        s_key[w][slot] = morton3(kx, ky, kz, b.depth);
+        s_val[w][slot] = v;
       }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        sum += __shfl_xor_sync(0xffffffffu, sum, o);
-        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-      }
-      const double div = cnt == 0 ? REF_SIZE_MAX : (double)(cnt - 1);
-      dt = __ddiv_rn(__dadd_rn(dt, (double)sum), div);
-      if (dt < best) {
-        best = dt;
-        best_i = it;
+      __syncwarp();
+      const int u = s_u[w];
+      int P = 2;
+      while (P < u) P <<= 1;
+      for (int i = u + lane; i < P; i += 32) s_key[w][i] = ~0ull;
+      __syncwarp();
+      leaf_sort(s_key[w], s_val[w], P, lane, 32, WarpSync());
+      if (lane == 0) {
+        dtf = leaf_running_score(dtf, s_val[w], u);
+        if (dtf < bestf) {
+          bestf = dtf;
+          best_i = it;
+        }
       }
       __syncwarp();
 #pragma unroll
@@ -826,7 +879,7 @@ __global__ void __launch_bounds__(32 * REFW_WARPS, 2)
       eye4(To);
       continue;
     }
-    score[p] = __double2float_rn(best);
+    score[p] = bestf;
     float S[16], R2[16], A[16];
     eye4(S);
     const float cs = __fdiv_rn(km.z, ks.z);
@@ -1108,6 +1161,22 @@ rtr_status rtr_ref_tdf(rtr_context* ctx, const float* d_cloud, const float* d_ke
   return RTR_OK;
 }
 
+}  // extern "C"
+
+// Dynamic shared memory of k_ref_distance<NT>: the sort list of a rotation's
+// distinct leaves, 8-byte codes and 4-byte values, one per cloud point.
+static size_t ref_leaf_smem(int nt) { return (size_t)nt * REF_PPT * (sizeof(unsigned long long) + sizeof(float)); }
+
+template <int NT>
+static rtr_status ref_distance_smem() {
+  // the attribute is per function and device; setting it again is harmless
+  RTR_CUDA(cudaFuncSetAttribute(k_ref_distance<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)ref_leaf_smem(NT)));
+  return RTR_OK;
+}
+
+extern "C" {
+
 rtr_status rtr_ref_distance(rtr_context* ctx, const float* d_mcloud, const float* d_mkeys, int n_model,
                             const int32_t* d_moffsets, const int32_t* d_mindices, const float* d_mtdf,
                             const float* d_skeys, int n_scan, const int32_t* d_pair_m, const int32_t* d_pair_s,
@@ -1165,15 +1234,22 @@ rtr_status rtr_ref_distance(rtr_context* ctx, const float* d_mcloud, const float
     k_ref_distance_warp<<<(unsigned)nbw, 32 * REFW_WARPS, 0, st>>>(mc, mk, d_moffsets, d_mindices, d_mtdf, sk, n_scan,
                                                                    d_pair_m, d_pair_s, n_pairs, resolution, half_tdf,
                                                                    rot, d_score, d_T, err);
-  } else if (nmax <= REF_PPT * 256)
-    k_ref_distance<256><<<nb, 256, 0, st>>>(mc, mk, d_moffsets, d_mindices, d_mtdf, sk, n_scan, d_pair_m, d_pair_s,
-                                            resolution, half_tdf, rot, d_score, d_T, err);
-  else if (nmax <= REF_PPT * 512)
-    k_ref_distance<512><<<nb, 512, 0, st>>>(mc, mk, d_moffsets, d_mindices, d_mtdf, sk, n_scan, d_pair_m, d_pair_s,
-                                            resolution, half_tdf, rot, d_score, d_T, err);
-  else
-    k_ref_distance<1024><<<nb, 1024, 0, st>>>(mc, mk, d_moffsets, d_mindices, d_mtdf, sk, n_scan, d_pair_m,
-                                              d_pair_s, resolution, half_tdf, rot, d_score, d_T, err);
+  } else if (nmax <= REF_PPT * 256) {
+    RTR_TRY(ref_distance_smem<256>());
+    k_ref_distance<256><<<nb, 256, ref_leaf_smem(256), st>>>(mc, mk, d_moffsets, d_mindices, d_mtdf, sk, n_scan,
+                                                             d_pair_m, d_pair_s, resolution, half_tdf, rot, d_score,
+                                                             d_T, err);
+  } else if (nmax <= REF_PPT * 512) {
+    RTR_TRY(ref_distance_smem<512>());
+    k_ref_distance<512><<<nb, 512, ref_leaf_smem(512), st>>>(mc, mk, d_moffsets, d_mindices, d_mtdf, sk, n_scan,
+                                                             d_pair_m, d_pair_s, resolution, half_tdf, rot, d_score,
+                                                             d_T, err);
+  } else {
+    RTR_TRY(ref_distance_smem<1024>());
+    k_ref_distance<1024><<<nb, 1024, ref_leaf_smem(1024), st>>>(mc, mk, d_moffsets, d_mindices, d_mtdf, sk, n_scan,
+                                                                d_pair_m, d_pair_s, resolution, half_tdf, rot, d_score,
+                                                                d_T, err);
+  }
   RTR_LAUNCHED(1);
   RTR_CUDA(cudaGetLastError());
   RTR_TRY(ref_read_ints(ctx, err, 4, st, h));

@@ -62,6 +62,19 @@ constexpr int KNN1_STATIC_DEVICES = 64;
 static std::mutex g_knn1_static_mu;
 static void* g_knn1_static_ptr[KNN1_STATIC_DEVICES];
 
+// A pointer rtr_knn1_static may hand to its kernel on device `dev`: device
+// memory of that device, or managed memory.  cudaPointerGetAttributes reads
+// the driver's records and allocates nothing.
+static bool on_device(const void* p, int dev) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  if (a.type == cudaMemoryTypeManaged) return true;
+  return a.type == cudaMemoryTypeDevice && a.device == dev;
+}
+
 }  // namespace rtr
 
 using namespace rtr;
@@ -121,6 +134,11 @@ rtr_status rtr_knn1_static(const float* d_query, int n_query, const float* d_tar
   if (dev < 0 || dev >= KNN1_STATIC_DEVICES)
     return fail(RTR_ERR_INVALID_ARG, "rtr_knn1_static: device %d beyond the supported %d", dev,
                 KNN1_STATIC_DEVICES);
+  // the kernel runs on the current device: every buffer must live there
+  if (!on_device(d_query, dev) || !on_device(d_target, dev) || !on_device(d_out_idx, dev) ||
+      (d_out_d2 && !on_device(d_out_d2, dev)))
+    return fail(RTR_ERR_INVALID_ARG,
+                "rtr_knn1_static: a buffer is not device memory of the current device %d", dev);
   void* base = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_knn1_static_mu);
@@ -136,7 +154,9 @@ rtr_status rtr_knn1_static(const float* d_query, int n_query, const float* d_tar
     }
     base = g_knn1_static_ptr[dev];
   }
-  const unsigned cap = default_cell_cap(RTR_KNN1_STATIC_MAX_TARGET);
+  // the same cell table as rtr_knn1 builds for this target count (at most
+  // the maximum target count's, which the array is sized for)
+  const unsigned cap = default_cell_cap(n_target);
   ScratchPlan plan;
   grid_plan(plan, n_target, cap);
   if (plan.bytes > KNN1_STATIC_BYTES)

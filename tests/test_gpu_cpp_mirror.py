@@ -4,12 +4,11 @@ realtime_robot_gb300/cpp/realtime_robot.hpp over the C ABI, driven as main
 drives them (realtime_robot_demo) on a cropped, moved chair.
 
 The demo exits 0 when its refined pose is within 1 cm / 1 degree of the
-generator's.  Some crops leave only part of the chair, along which the view
-slides, and with 2 cm model keypoints some seeds settle on the chair turned
-by 180 degrees: the oracle pipeline on the same clouds lands there too.  So
-wherever the oracle pipeline finds the chair (best instance within 2 cm /
-3 degrees) the demo must register it within 1 cm / 1 degree, and at least
-half the seeds must register."""
+generator's.  With the workload's 2 cm model keypoints the oracle pipeline
+itself registers only some crops within 1 cm / 1 degree (others keep a
+slide along the chair or settle on the chair turned by 180 degrees).  So
+wherever the oracle pipeline registers the chair the demo must register it
+too, and it must register at least as many seeds as the oracle does."""
 import re
 import subprocess
 from pathlib import Path
@@ -25,7 +24,7 @@ SEEDS = range(8)
 
 def _oracle_found(R, O, OP, om, seed):
     """The oracle pipeline on the demo's clouds (same generator calls):
-    whether its best instance is within 2 cm / 3 degrees of the truth."""
+    whether its best instance is within 1 cm / 1 degree of the truth."""
     Tm = R.synth_rigid(100 + seed, 30.0, 0.3)
     seg = R.synth_transform_noise(R.synth_crop(R.synth_shape(R.CHAIR, 20000, 500 + seed), 0.4, seed), Tm, 0.002,
                                   9 + seed)
@@ -33,7 +32,7 @@ def _oracle_found(R, O, OP, om, seed):
     if not ref["instances"]:
         return False
     e = O.pose_error(ref["instances"][0]["pose"], Tm)
-    return e[0] < 0.02 and e[1] < np.radians(3.0)
+    return e[0] < 0.01 and e[1] < np.radians(1.0)
 
 
 def test_cpp_entry_points_register_a_chair(rtr):
@@ -41,7 +40,7 @@ def test_cpp_entry_points_register_a_chair(rtr):
     from oracle import pipeline as OP
     assert DEMO.exists(), "build() makes the demo next to librtr.so"
     om = OP.prepare_model(rtr.synth_shape(rtr.CHAIR, 20000, 2024), OP.params(scene_outward=1))
-    ok = 0
+    ok = found = 0
     for seed in SEEDS:
         r = subprocess.run([str(DEMO), str(seed)], capture_output=True, text=True, timeout=120)
         assert r.returncode in (0, 1), (seed, r.returncode, r.stdout, r.stderr)
@@ -52,9 +51,10 @@ def test_cpp_entry_points_register_a_chair(rtr):
         within = float(m.group(1)) < 0.01 and float(m.group(2)) < 1.0
         assert within == (r.returncode == 0), (seed, r.stdout)
         if _oracle_found(rtr, O, OP, om, seed):
+            found += 1
             assert within, (seed, r.stdout)
         ok += within
-    assert ok >= 4, ok
+    assert found >= 2 and ok >= found, (ok, found)
 
 
 @pytest.mark.parametrize("seed", [1, 3])

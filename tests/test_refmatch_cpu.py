@@ -134,7 +134,7 @@ def np_distance(cloud, km, idx, grid, ks, res=0.01, half=0.15):
     T3[0, 3], T3[1, 3] = k3[0], k3[1]
     Rs[0, 0], Rs[1, 0], Rs[0, 1], Rs[1, 1] = c1, s1, -s1, c1
     M = np_mm(np_mm(T3, Rs), T1)
-    dt, best, best_i = 0.0, 1e8, 0
+    dt, best, best_i = F32(0), F32(1e8), 0
     for i in range(36):
         if i:
             P = np_xf(M, P)
@@ -146,17 +146,20 @@ def np_distance(cloud, km, idx, grid, ks, res=0.01, half=0.15):
             assert np_grow(b, P[out[0]], r)
         L = np_leaves(b, P, r)
         u = L.shape[0]
-        s = 0
         if u > 1:
             ctr = np_centre(b, L[1:], r)
             q = (ctr - lo) / r32
             ix = np.trunc(q).astype(np.int64)
             lin = ix[:, 1] * 30 + ix[:, 2] * 900 + ix[:, 0]
             ok = (lin >= 0) & (lin < 27000)
-            v = np.where(ok, grid[np.clip(lin, 0, 26999)], F32(900)).astype(np.int64)
-            s = int((v * v).sum())
-        div = 18446744073709551615.0 if u == 0 else float(u - 1)
-        dt = (dt + float(s)) / div
+            v = np.where(ok, grid[np.clip(lin, 0, 26999)], F32(900)).astype(F32)
+            # matching.h:179-189: float adds, leaf by leaf in tree order,
+            # into the running score that no rotation resets
+            for x in v:
+                dt = F32(dt + F32(x * x))
+        div = F32(18446744073709551615.0) if u == 0 else F32(u - 1)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            dt = F32(F32(dt) / div)
         if dt < best:
             best, best_i = dt, i
     th = F32(best_i) * theta
@@ -237,14 +240,14 @@ def test_distance_explicit_pairs_equal_all_pairs():
 
 
 def test_float_order_agrees_with_exact_sums():
-    """The reference adds the squared field values in float, leaf by leaf;
-    the route here sums each rotation exactly and keeps the running score in
-    double.  The two agree to a few parts in 10^5."""
+    """The reference adds the squared field values in float, leaf by leaf
+    (the route's definition); the variant with exact per-rotation sums and a
+    double running score agrees to a few parts in 10^5."""
     model, scan, km, ks = _chair_case(nk=10, ns=10)
     _, off, idx = O.ref_occupancy(model, km, 0.01, 0.1)
     tdf = O.ref_tdf(model, km, off, idx)
-    s1, _ = O.ref_distance(model, km, off, idx, tdf, ks)
-    s2, _ = O.ref_distance(model, km, off, idx, tdf, ks, float_order=True)
+    s1, _ = O.ref_distance(model, km, off, idx, tdf, ks, float_order=False)
+    s2, _ = O.ref_distance(model, km, off, idx, tdf, ks)
     ok = np.isfinite(s1)
     assert ok.all()
     rel = np.abs(s1.astype(np.float64) - s2) / np.maximum(np.abs(s1.astype(np.float64)), 1e-30)

@@ -42,6 +42,28 @@ def test_knn1_static_matches_knn1_twice(ctx, rtr):
         assert np.all(np.isinf(sd[~ok]))
 
 
+def test_knn1_static_flat_and_duplicate_targets(ctx, rtr):
+    """Where the cell table's size limit binds (a flat target, unbounded
+    search) and where targets repeat (ties go to the lowest index), the
+    static call still equals rtr_knn1, on two calls in a row."""
+    import torch
+    rng = np.random.default_rng(79)
+    flat = _rand(rng, 6000, 1.0)
+    flat[:, 2] = 0.0
+    dup = _rand(rng, 3000, 0.2)
+    dup = np.concatenate([dup, dup[::-1], dup[:500]])  # every point at least twice
+    q1, q2 = _rand(rng, 4000, 1.2), dup[:, :].copy()
+    q2[:, :3] += rng.normal(0, 1e-3, (q2.shape[0], 3)).astype(np.float32)
+    outs = []
+    for t, q in ((flat, q1), (dup, q2)):
+        dq, dt = _dev(q), _dev(t)
+        outs.append((dq, dt, ctx.knn1_static(dq, dt, 0.0)))
+    torch.cuda.synchronize()
+    for dq, dt, (si, sd) in outs:
+        ki, kd = ctx.knn1(dq, dt, 0.0)
+        assert torch.equal(si, ki) and torch.equal(sd, kd)
+
+
 def test_knn1_static_preallocated_outputs_and_limit(ctx, rtr):
     import torch
     rng = np.random.default_rng(78)
@@ -57,3 +79,9 @@ def test_knn1_static_preallocated_outputs_and_limit(ctx, rtr):
     with pytest.raises(rtr.RtrError, match="exceeds the fixed maximum"):
         ctx.knn1_static(dq, big, 0.0, out=out)
     assert torch.equal(out[0], ki)  # outputs untouched by the refused call
+    # a host buffer is refused on the host, before any launch
+    host_q = np.ascontiguousarray(q)
+    st = rtr.lib().rtr_knn1_static(host_q.ctypes.data, 3000, dt.data_ptr(), 5000, 0.0, out[0].data_ptr(),
+                                   out[1].data_ptr(), 0)
+    assert st == 1 and "not device memory" in rtr.lib().rtr_last_error().decode()
+    assert torch.equal(out[0], ki)
