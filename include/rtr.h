@@ -71,7 +71,11 @@ const char* rtr_version(void);
  *                    verification and ICP refinement (default: 1.5 x the ICP
  *                    distance; the table's size limit may widen it);
  *   "normals_grid_mm" cell edge (mm) of the scene normals' k-NN grid
- *                    (default: five voxel leaves).
+ *                    (default: five voxel leaves);
+ *   "scratch_limit_mb" the largest scratch arena the context may hold, in
+ *                    MiB (0: no limit): a call needing more returns
+ *                    RTR_ERR_OOM, as when cudaMalloc fails, and the arena
+ *                    held so far stays usable.
  * Unknown keys or values return RTR_ERR_INVALID_ARG.  Results do not depend
  * on the knobs beyond FP32 summation order. */
 rtr_status rtr_context_set_tuning(rtr_context* ctx, const char* key, int value);

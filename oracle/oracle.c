@@ -70,19 +70,25 @@ typedef struct {
 
 static int cg_cell(const cgrid* g, double v, int a) {
   double f = floor((v - g->o[a]) / g->h);
-  if (f < -1e8) f = -1e8;
+  if (!(f >= -1e8)) f = -1e8; /* also NaN, as the GPU's fmaxf does */
   if (f > 1e8) f = 1e8;
   return (int)f;
 }
 
 static void cg_build(cgrid* g, const float* pts, int n, double h) {
   double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, hi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
-  for (int i = 0; i < n; ++i)
+  int nf = 0;
+  for (int i = 0; i < n; ++i) {
+    /* points with a non-finite coordinate do not size the grid; they sit in
+     * a border cell and never match (their d^2 is NaN or inf) */
+    if (!(isfinite(pts[4 * i]) && isfinite(pts[4 * i + 1]) && isfinite(pts[4 * i + 2]))) continue;
+    ++nf;
     for (int a = 0; a < 3; ++a) {
       if (pts[4 * i + a] < lo[a]) lo[a] = pts[4 * i + a];
       if (pts[4 * i + a] > hi[a]) hi[a] = pts[4 * i + a];
     }
-  if (n == 0)
+  }
+  if (nf == 0)
     for (int a = 0; a < 3; ++a) lo[a] = hi[a] = 0;
   if (!(h > 0)) {
     double vol = 1;
@@ -172,7 +178,8 @@ static void cg_search(const cgrid* g, const float* qf, topk* T) {
             int j = g->order[s];
             float d = d2f(qf, g->pts + 4 * j);
             int last = T->k - 1;
-            if (d > T->bd[last] || (d == T->bd[last] && j >= T->bi[last])) continue;
+            /* a NaN distance is never taken */
+            if (!(d < T->bd[last]) && !(d == T->bd[last] && j < T->bi[last])) continue;
             int p = last;
             while (p > 0 && (d < T->bd[p - 1] || (d == T->bd[p - 1] && j < T->bi[p - 1]))) {
               T->bd[p] = T->bd[p - 1];
@@ -270,7 +277,7 @@ void orc_knn_brute(const float* q, int nq, const float* t, int nt, int k, int32_
     for (int j = 0; j < nt; ++j) {
       float d = d2f(q + 4 * i, t + 4 * j);
       int last = k - 1;
-      if (d > bd[last] || (d == bd[last] && j >= bi[last])) continue;
+      if (!(d < bd[last]) && !(d == bd[last] && j < bi[last])) continue; /* NaN never taken */
       int p = last;
       while (p > 0 && (d < bd[p - 1] || (d == bd[p - 1] && j < bi[p - 1]))) {
         bd[p] = bd[p - 1];
@@ -560,43 +567,56 @@ static int kv_cmp(const void* a, const void* b) {
 /* Voxel keys floor(p * inv) relative to the minimum voxel; returns the number
  * of keys or -1 when the key space does not fit 32 bits.  kv sorted by
  * (key, index), i.e. a stable sort by key. */
+/* Voxel keys floor(p * inv) relative to the minimum voxel, sorted by
+ * (key, index) (a stable sort by key).  Points with a non-finite coordinate
+ * get no voxel (PCL's VoxelGrid skips them in clouds that are not dense):
+ * they are left out and the number of keyed points is returned.  -1 when a
+ * finite point's voxel index reaches 10^9 or the key space does not fit in
+ * 32 bits with one key (0xffffffff) to spare. */
 static int voxel_keys(const float* pts, int n, float inv, kv_t* kv, int* ijk_out) {
   int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {INT_MIN, INT_MIN, INT_MIN};
-  for (int i = 0; i < n; ++i)
+  int m = 0;
+  for (int i = 0; i < n; ++i) {
+    const float* p = pts + 4 * i;
+    if (!(isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]))) continue;
     for (int a = 0; a < 3; ++a) {
-      float f = pts[4 * i + a] * inv;
-      int v = (int)floorf(f);
+      const float f = floorf(p[a] * inv);
+      if (!(fabsf(f) < 1.0e9f)) return -1;
+      const int v = (int)f;
       ijk_out[3 * i + a] = v;
       if (v < lo[a]) lo[a] = v;
       if (v > hi[a]) hi[a] = v;
     }
-  if (n == 0) return 0;
+    kv[m++].idx = i;
+  }
+  if (m == 0) return 0;
   uint64_t d0 = (uint64_t)(hi[0] - lo[0] + 1), d1 = (uint64_t)(hi[1] - lo[1] + 1), d2 = (uint64_t)(hi[2] - lo[2] + 1);
-  if (d0 * d1 * d2 > 0xffffffffull) return -1;
-  for (int i = 0; i < n; ++i) {
+  if (d0 * d1 > 0xffffffffull || d0 * d1 * d2 >= 0xffffffffull) return -1;
+  for (int k = 0; k < m; ++k) {
+    const int i = kv[k].idx;
     uint32_t x = (uint32_t)(ijk_out[3 * i] - lo[0]), y = (uint32_t)(ijk_out[3 * i + 1] - lo[1]),
              z = (uint32_t)(ijk_out[3 * i + 2] - lo[2]);
-    kv[i].key = (z * (uint32_t)d1 + y) * (uint32_t)d0 + x;
-    kv[i].idx = i;
+    kv[k].key = (z * (uint32_t)d1 + y) * (uint32_t)d0 + x;
   }
-  qsort(kv, (size_t)n, sizeof(kv_t), kv_cmp);
-  return n;
+  qsort(kv, (size_t)m, sizeof(kv_t), kv_cmp);
+  return m;
 }
 
 int orc_voxel_downsample(const float* pts, int n, float leaf, float* out) {
   const float inv = 1.0f / leaf;
   kv_t* kv = (kv_t*)malloc(sizeof(kv_t) * (n > 0 ? n : 1));
   int* ijk = (int*)malloc(sizeof(int) * 3 * (n > 0 ? n : 1));
-  if (voxel_keys(pts, n, inv, kv, ijk) < 0) {
+  const int m = voxel_keys(pts, n, inv, kv, ijk);
+  if (m < 0) {
     free(kv);
     free(ijk);
     return -1;
   }
   int v = 0;
-  for (int s = 0; s < n;) {
+  for (int s = 0; s < m;) {
     int e = s;
     float sx = 0.f, sy = 0.f, sz = 0.f;
-    while (e < n && kv[e].key == kv[s].key) {
+    while (e < m && kv[e].key == kv[s].key) {
       const float* p = pts + 4 * kv[e].idx;
       sx = sx + p[0];
       sy = sy + p[1];
@@ -753,16 +773,17 @@ int orc_uniform_sample(const float* pts, int n, float r, int32_t* out_idx) {
   const float inv = 1.0f / r;
   kv_t* kv = (kv_t*)malloc(sizeof(kv_t) * (n > 0 ? n : 1));
   int* ijk = (int*)malloc(sizeof(int) * 3 * (n > 0 ? n : 1));
-  if (voxel_keys(pts, n, inv, kv, ijk) < 0) {
+  const int m = voxel_keys(pts, n, inv, kv, ijk);
+  if (m < 0) {
     free(kv);
     free(ijk);
     return -1;
   }
   int K = 0;
-  for (int s = 0; s < n;) {
+  for (int s = 0; s < m;) {
     int e = s, best = -1;
     float bd = INFINITY;
-    while (e < n && kv[e].key == kv[s].key) {
+    while (e < m && kv[e].key == kv[s].key) {
       const int i = kv[e].idx;
       const float* p = pts + 4 * i;
       float c[3];

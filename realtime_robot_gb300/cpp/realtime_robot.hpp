@@ -203,9 +203,14 @@ inline int loadPCDFile(const std::string& path, PointCloud<PointXYZ>& cloud) {
       if (fields[i].name == std::string(1, "xyz"[a])) col[a] = (int)i;
   }
   if (col[0] < 0 || col[1] < 0 || col[2] < 0) return -1;
+  if (data != "binary" && data != "ascii") return -1;  // binary_compressed (LZF) is not read
+  // the data section must hold the declared points before anything is sized
+  // from the header (a corrupt POINTS must not allocate): a binary record is
+  // rec bytes, an ascii one at least a digit and a separator per value
+  const size_t avail = pos <= raw.size() ? raw.size() - pos : 0;
+  if (data == "binary" ? (size_t)points > avail / rec : (size_t)points > (avail + 1) / (2 * ncol)) return -1;
   cloud.points.assign((size_t)points, PointXYZ());
   if (data == "binary") {
-    if (raw.size() < pos + rec * (size_t)points) return -1;
     for (long long i = 0; i < points; ++i) {
       const unsigned char* r = raw.data() + pos + rec * (size_t)i;
       double v[3];
@@ -213,7 +218,7 @@ inline int loadPCDFile(const std::string& path, PointCloud<PointXYZ>& cloud) {
         if (!detail::pcd_value(r + off[(size_t)col[a]], fields[(size_t)col[a]], &v[a])) return -1;
       cloud.points[(size_t)i] = PointXYZ((float)v[0], (float)v[1], (float)v[2]);
     }
-  } else if (data == "ascii") {
+  } else {
     std::vector<double> row(ncol);
     const char* c = reinterpret_cast<const char*>(raw.data()) + pos;
     const char* e = reinterpret_cast<const char*>(raw.data()) + raw.size();
@@ -228,8 +233,6 @@ inline int loadPCDFile(const std::string& path, PointCloud<PointXYZ>& cloud) {
       cloud.points[(size_t)i] = PointXYZ((float)row[first_col[(size_t)col[0]]], (float)row[first_col[(size_t)col[1]]],
                                          (float)row[first_col[(size_t)col[2]]]);
     }
-  } else {
-    return -1;  // binary_compressed (LZF) is not read
   }
   cloud.width = (uint32_t)points;
   cloud.height = 1;

@@ -47,6 +47,7 @@ rtr_status batch_ensure_workers(rtr_context* ctx, int n) {
     w->wait_budget_ms = ctx->wait_budget_ms;
     w->wait_budget_cycles = ctx->wait_budget_cycles;
     w->tune_icp_group = ctx->tune_icp_group;
+    w->scratch_limit = ctx->scratch_limit;
   }
   return RTR_OK;
 }

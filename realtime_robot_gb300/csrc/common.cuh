@@ -73,6 +73,7 @@ struct rtr_context {
   cudaStream_t host_stream = nullptr;  // stream of the host-pointer entry points
   int* h_pin = nullptr;                // 64 pinned ints for small device->host reads
   int tune_icp_group = 0;              // lanes per ICP source point (0: automatic)
+  size_t scratch_limit = 0;            // largest scratch arena this context may hold (0: no limit)
   int tune_batch_workers = 0;          // workers of rtr_recognize_batch (0: automatic)
   int coop_div = 1;                    // cooperative grids use 1/coop_div of the GPU
   int tune_gc_window = 0;              // seeds per grouping window (0: automatic)

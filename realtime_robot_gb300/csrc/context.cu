@@ -68,6 +68,14 @@ rtr_status ensure_scratch(rtr_context* ctx, size_t bytes, cudaStream_t stream, S
                   "being captured; call rtr_context_reserve first",
                   ctx->arena_bytes, bytes);
     size_t grow = bytes + bytes / 4 + (1u << 20);
+    if (ctx->scratch_limit) {
+      // a memory budget set by the caller: refused exactly as a failed
+      // cudaMalloc would be, with the arena held so far kept
+      if (bytes > ctx->scratch_limit)
+        return fail(RTR_ERR_OOM, "scratch arena: %zu bytes needed, the context's limit is %zu", bytes,
+                    ctx->scratch_limit);
+      if (grow > ctx->scratch_limit) grow = ctx->scratch_limit;
+    }
     RTR_CUDA(cudaDeviceSynchronize());
     ++ctx->scratch_gen;  // from here on the old arena is gone, whatever the allocation below does
     if (ctx->arena) RTR_CUDA(cudaFree(ctx->arena));
@@ -253,6 +261,11 @@ rtr_status rtr_context_set_tuning(rtr_context* ctx, const char* key, int value) 
     if (value < 0 || value > 1000)
       return rtr::fail(RTR_ERR_INVALID_ARG, "%s must be 0..1000 (got %d)", key, value);
     (key[0] == 's' ? ctx->tune_scene_grid_mm : ctx->tune_normals_grid_mm) = value;
+    return RTR_OK;
+  }
+  if (strcmp(key, "scratch_limit_mb") == 0) {
+    if (value < 0) return rtr::fail(RTR_ERR_INVALID_ARG, "scratch_limit_mb must be >= 0 (got %d)", value);
+    ctx->scratch_limit = (size_t)value << 20;
     return RTR_OK;
   }
   if (strcmp(key, "icp_group") == 0) {

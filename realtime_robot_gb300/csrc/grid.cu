@@ -170,6 +170,9 @@ __global__ void __launch_bounds__(256) k_bbox(const float4* __restrict__ pts, in
   unsigned mn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, mx[3] = {0u, 0u, 0u};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     float4 p = pts[i];
+    // a point with a non-finite coordinate does not size the grid: it sits in
+    // a clamped border cell and never matches (its d^2 is NaN or inf)
+    if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) continue;
     unsigned u[3] = {float_to_ordered(p.x), float_to_ordered(p.y), float_to_ordered(p.z)};
 #pragma unroll
     for (int a = 0; a < 3; ++a) {

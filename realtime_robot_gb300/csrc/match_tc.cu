@@ -77,14 +77,22 @@ __device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// bounded wait; returns false (and raises the CTA abort flag) on timeout
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort) {
-  for (long long i = 0; i < TC_SPIN_LIMIT; ++i) {
+// bounded wait (`limit` tries, from the context's wait budget); returns false
+// (and raises the CTA abort flag) on timeout or when another role aborted
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort, long long limit) {
+  for (long long i = 0; i < limit; ++i) {
     if (mbar_try(b, parity)) return true;
     if (*abort) return false;
   }
   *abort = 1;
   return false;
+}
+// the drain after an abort: wait for work already issued, up to the fixed
+// TC_SPIN_LIMIT tries whatever the budget (a copy or MMA in flight ends by
+// itself; this only bounds the wait if the hardware stopped answering)
+__device__ __forceinline__ void mbar_drain(uint64_t* b, uint32_t parity) {
+  for (long long i = 0; i < TC_SPIN_LIMIT; ++i)
+    if (mbar_try(b, parity)) return;
 }
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1) {
   asm volatile(
@@ -192,6 +200,7 @@ struct TcArgs {
   int* status;
   const float* thr;  // band pass: [nq_cap] largest d~ a row may have and still tie the winner
   int* band_n;       // band pass: [nq_cap] rows listed (over TC_BAND: overflowed)
+  long long spin_limit;  // tries per mbarrier wait (the context's wait budget)
 };
 
 // BAND = false: per query the 8 smallest d~ (the first pass).  BAND = true:
@@ -207,7 +216,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constan
                                                             const __grid_constant__ CUtensorMap mb_lo, TcArgs a) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  __shared__ uint64_t full_bar[TC_STAGES], empty_bar[TC_STAGES], acc_full[2], acc_empty[2];
+  __shared__ uint64_t full_bar[TC_STAGES], empty_bar[TC_STAGES], acc_full[2], acc_empty[2], drain_bar;
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
 
@@ -231,6 +240,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constan
       mbar_init(&acc_full[b], 1);
       mbar_init(&acc_empty[b], 128);
     }
+    mbar_init(&drain_bar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 5) {  // allocate 512 TMEM columns (two 128 x 256 FP32 accumulators)
@@ -242,6 +252,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constan
   tc_fence_after();
   const uint32_t tmem = tmem_base;
   volatile int* abort = &abort_flag;
+  const long long lim = a.spin_limit;
+  int issued = 0;  // producer: stage loads issued
 
   if (warp == 4) {
     // ---------------- TMA producer ----------------
@@ -251,7 +263,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constan
         for (int kb = 0; kb < TC_NKB && !*abort; ++kb, ++it) {
           const int s = it % TC_STAGES;
           const uint32_t ph = (uint32_t)(it / TC_STAGES) & 1u;
-          if (it >= TC_STAGES && !mbar_wait(&empty_bar[s], ph ^ 1u, abort)) break;
+          if (it >= TC_STAGES && !mbar_wait(&empty_bar[s], ph ^ 1u, abort, lim)) break;
           uint8_t* st = smem + s * TC_STAGE_BYTES;
           mbar_expect_tx(&full_bar[s], TC_STAGE_BYTES);
           tma_load_2d(st, &mq_hi, &full_bar[s], kb * TC_KB, q0);
@@ -260,6 +272,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constan
           tma_load_2d(st + 2 * TC_A_BYTES + TC_B_BYTES, &mb_lo, &full_bar[s], kb * TC_KB, t * TC_BN);
         }
       }
+      issued = it;
     }
   } else if (warp == 5) {
     // ---------------- MMA issuer ----------------
@@ -269,13 +282,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constan
       for (int t = t_lo; t < t_hi && !*abort; ++t) {
         const int buf = (t - t_lo) & 1;
         const uint32_t use = (uint32_t)((t - t_lo) >> 1);
-        if (t - t_lo >= 2 && !mbar_wait(&acc_empty[buf], (use - 1) & 1u, abort)) break;
+        if (t - t_lo >= 2 && !mbar_wait(&acc_empty[buf], (use - 1) & 1u, abort, lim)) break;
         tc_fence_after();
         const uint32_t dcol = tmem + (uint32_t)buf * TC_BN;
         for (int kb = 0; kb < TC_NKB; ++kb, ++it) {
           const int s = it % TC_STAGES;
           const uint32_t ph = (uint32_t)(it / TC_STAGES) & 1u;
-          if (!mbar_wait(&full_bar[s], ph, abort)) break;
+          if (!mbar_wait(&full_bar[s], ph, abort, lim)) break;
           tc_fence_after();
           const uint32_t base = smem_u32(smem + s * TC_STAGE_BYTES);
           const uint32_t ah = base, al = base + TC_A_BYTES, bh = base + 2 * TC_A_BYTES,
@@ -309,7 +322,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constan
       for (int t = t_lo; t < t_hi; ++t) {
         const int buf = (t - t_lo) & 1;
         const uint32_t use = (uint32_t)((t - t_lo) >> 1);
-        if (!mbar_wait(&acc_full[buf], use & 1u, abort)) break;
+        if (!mbar_wait(&acc_full[buf], use & 1u, abort, lim)) break;
         tc_fence_after();
         const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)buf * TC_BN;
         const int valid = min(TC_BN, a.ndb - t * TC_BN);
@@ -346,7 +359,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constan
     for (int t = t_lo; t < t_hi; ++t) {
       const int buf = (t - t_lo) & 1;
       const uint32_t use = (uint32_t)((t - t_lo) >> 1);
-      if (!mbar_wait(&acc_full[buf], use & 1u, abort)) break;
+      if (!mbar_wait(&acc_full[buf], use & 1u, abort, lim)) break;
       tc_fence_after();
       const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)buf * TC_BN;
       const int valid = min(TC_BN, a.ndb - t * TC_BN);  // rows past the database read as zero
@@ -384,6 +397,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_match_tc(const __grid_constan
       }
     }
     }
+  }
+  // after an abort nothing of this CTA may still be in flight when it frees
+  // its TMEM and exits: the MMA issuer waits for every MMA it issued, the
+  // producer for the stage loads not yet seen complete (the last ones; each
+  // earlier load of a stage completed before the stage was reused)
+  __syncthreads();
+  if (abort_flag) {
+    if (warp == 5 && lane == 0) {
+      umma_commit(&drain_bar);
+      mbar_drain(&drain_bar, 0u);
+    }
+    if (warp == 4 && lane == 0)
+      for (int i = issued > TC_STAGES ? issued - TC_STAGES : 0; i < issued; ++i)
+        mbar_drain(&full_bar[i % TC_STAGES], (uint32_t)(i / TC_STAGES) & 1u);
   }
   tc_fence_before();
   __syncthreads();
@@ -451,7 +478,8 @@ __global__ void __launch_bounds__(256) k_rerank(const float* __restrict__ q, int
 #pragma unroll
     for (int o = 4; o > 0; o >>= 1) nz |= __shfl_xor_sync(0xffffffffu, (int)nz, o) != 0;
     const bool zq = valid && !nz;  // (no early exit: the shuffles below need every lane)
-    const int c = valid && !zq ? cand_idx[(size_t)i * TC_TOP + l8] : -1;
+    int c = valid && !zq ? cand_idx[(size_t)i * TC_TOP + l8] : -1;
+    if (c >= ndb) c = -1;  // never read past the database, whatever the first pass left
     float d = __int_as_float(0x7f800000);
     if (c >= 0) d = exact_d2<V4>(q + (size_t)i * TC_DIM, db + (size_t)c * TC_DIM);
     int bi = c >= 0 ? c : 0x7fffffff;
@@ -648,6 +676,13 @@ size_t match_tc_bf16_bytes(int rows) { return (size_t)rows * TC_KPAD * 2; }
 // rows of the band pass (a multiple of TC_BM)
 static int band_rows(int nqp) { return nqp < TC_BAND_Q ? nqp : TC_BAND_Q; }
 
+// mbarrier tries per wait for the context's wait budget (a try is a few
+// dozen cycles; the default 2 s budget gives about 2^26 tries)
+static long long tc_spin_limit(const rtr_context* ctx) {
+  const long long t = ctx->wait_budget_cycles / 64;
+  return t < 1 ? 1 : t;
+}
+
 void match_tc_plan(ScratchPlan& p, int nq_cap, bool with_db, int ndb) {
   const int nqp = ((nq_cap + TC_BM - 1) / TC_BM) * TC_BM;
   p.add<__nv_bfloat16>((size_t)nqp * TC_KPAD);
@@ -733,7 +768,7 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
   // per call: the attribute is per device, and calls may come from several threads
   RTR_CUDA(cudaFuncSetAttribute(k_match_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   RTR_CUDA(cudaFuncSetAttribute(k_match_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  TcArgs a{nq_cap, d_nq, nq_cap, ndb, qn, cidx, cd, ctx->d_status, nullptr, nullptr};
+  TcArgs a{nq_cap, d_nq, nq_cap, ndb, qn, cidx, cd, ctx->d_status, nullptr, nullptr, tc_spin_limit(ctx)};
   {
     ProfScope pg(ctx, st, "match_gemm");
     k_match_tc<false><<<nqp / TC_BM, TC_THREADS, smem, st>>>(m_qh, m_ql, m_bh, m_bl, a);
@@ -748,7 +783,7 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
   const bool v4 = ((reinterpret_cast<uintptr_t>(q) | reinterpret_cast<uintptr_t>(db)) & 15u) == 0;
   // band pass over the uncertified queries: the GEMM again, listing every
   // row within the tie margin, then exact distances to those rows only
-  TcArgs ab{bq, nredo, bq, ndb, qn2, band_idx, nullptr, ctx->d_status, redo_thr, band_n};
+  TcArgs ab{bq, nredo, bq, ndb, qn2, band_idx, nullptr, ctx->d_status, redo_thr, band_n, tc_spin_limit(ctx)};
   if (v4)
     k_rerank<true><<<rb, 256, 0, st>>>(q, nq_cap, d_nq, nq_cap, db, ndb, cidx, cd, out_idx, out_d2, redo, nredo,
                                        redo_best, redo_thr, qn, db_n2 + ndb, zero_best);

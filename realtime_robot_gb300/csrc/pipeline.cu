@@ -252,6 +252,15 @@ __global__ void k_copy_result_poses(const rtr_icp_result* __restrict__ r, int m,
   for (int i = threadIdx.x; i < m * 16; i += blockDim.x) out[i] = r[i / 16].pose[i % 16];
 }
 
+// The result records of an empty scene: nothing found.
+__global__ void k_result_empty(rtr_recog_result* __restrict__ out, int n) {
+  const int words = (int)(sizeof(rtr_recog_result) / sizeof(int));
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n * words; i += gridDim.x * blockDim.x)
+    reinterpret_cast<int*>(out)[i] = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) out[i].status = RTR_ERR_NOT_FOUND;
+}
+
 // Non-maximum suppression and the result record (one thread).
 __global__ void k_finalize(const float* __restrict__ fscore, const double* __restrict__ refined,
                            const int* __restrict__ order, const int* __restrict__ cl_sizes, int m_cap,
@@ -862,7 +871,9 @@ rtr_status rtr_recognize(rtr_context* ctx, const rtr_model* model, const float* 
   cudaStream_t st = (cudaStream_t)stream;
   RTR_CUDA(cudaSetDevice(ctx->device));
   if (n == 0) {
-    RTR_CUDA(cudaMemsetAsync(d_result, 0, sizeof(rtr_recog_result), st));
+    k_result_empty<<<1, 256, 0, st>>>(d_result, 1);
+    RTR_LAUNCHED(1);
+    RTR_CUDA(cudaGetLastError());
     return RTR_OK;
   }
   return recognize_impl(ctx, model, reinterpret_cast<const float4*>(d_scene), n, p, d_result, st);
@@ -882,7 +893,9 @@ rtr_status rtr_recognize_learned(rtr_context* ctx, const rtr_model* model, const
   cudaStream_t st = (cudaStream_t)stream;
   RTR_CUDA(cudaSetDevice(ctx->device));
   if (n == 0) {
-    RTR_CUDA(cudaMemsetAsync(d_result, 0, sizeof(rtr_recog_result), st));
+    k_result_empty<<<1, 256, 0, st>>>(d_result, 1);
+    RTR_LAUNCHED(1);
+    RTR_CUDA(cudaGetLastError());
     return RTR_OK;
   }
   return recognize_impl(ctx, model, reinterpret_cast<const float4*>(d_scene), n, p, d_result, st, mlp, keep);
@@ -905,7 +918,9 @@ rtr_status rtr_recognize_multi(rtr_context* ctx, const rtr_model* const* h_model
   cudaStream_t st = (cudaStream_t)stream;
   RTR_CUDA(cudaSetDevice(ctx->device));
   if (n == 0) {
-    RTR_CUDA(cudaMemsetAsync(d_results, 0, sizeof(rtr_recog_result) * (size_t)n_models, st));
+    k_result_empty<<<1, 256, 0, st>>>(d_results, n_models);
+    RTR_LAUNCHED(1);
+    RTR_CUDA(cudaGetLastError());
     RTR_CUDA(cudaStreamSynchronize(st));
     return RTR_OK;
   }

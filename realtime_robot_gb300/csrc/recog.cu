@@ -39,6 +39,12 @@ __device__ __forceinline__ int vox_coord(float v, float inv, int* err) {
   return (int)f;
 }
 
+// Points with a non-finite coordinate get no voxel (PCL's VoxelGrid skips
+// them in clouds that are not dense): they take the key VOX_SKIP, sort last
+// and belong to no segment.
+constexpr uint32_t VOX_SKIP = 0xffffffffu;
+__device__ __forceinline__ bool finite3(float4 p) { return isfinite(p.x) && isfinite(p.y) && isfinite(p.z); }
+
 __global__ void __launch_bounds__(256) k_vox_bounds(const float4* __restrict__ pts, int n_host,
                                                     const int* d_n, float inv, VoxMeta* m) {
   const int n = cnt_of(n_host, d_n);
@@ -46,6 +52,7 @@ __global__ void __launch_bounds__(256) k_vox_bounds(const float4* __restrict__ p
   int err = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float4 p = pts[i];
+    if (!finite3(p)) continue;
     const int c[3] = {vox_coord(p.x, inv, &err), vox_coord(p.y, inv, &err), vox_coord(p.z, inv, &err)};
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -78,9 +85,15 @@ __global__ void k_vox_setup(VoxMeta* m, int n_host, const int* d_n) {
     m->dx = m->dy = m->dz = 1;
     return;
   }
+  if (m->lo[0] > m->hi[0]) {  // no finite point: every key is VOX_SKIP
+    m->lo[0] = m->lo[1] = m->lo[2] = 0;
+    m->dx = m->dy = m->dz = 1;
+    return;
+  }
   const long long dx = (long long)m->hi[0] - m->lo[0] + 1, dy = (long long)m->hi[1] - m->lo[1] + 1,
                   dz = (long long)m->hi[2] - m->lo[2] + 1;
-  if (dx * dy > 0xffffffffLL || dx * dy * dz > 0xffffffffLL) m->error = 1;
+  // one key (VOX_SKIP) stays free for the points without a voxel
+  if (dx * dy > 0xffffffffLL || dx * dy * dz >= 0xffffffffLL) m->error = 1;
   m->dx = (unsigned)dx;
   m->dy = (unsigned)dy;
   m->dz = (unsigned)dz;
@@ -95,6 +108,10 @@ __global__ void __launch_bounds__(256) k_vox_keys(const float4* __restrict__ pts
   const unsigned dx = m->dx, dy = m->dy;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float4 p = pts[i];
+    if (!finite3(p)) {
+      keys[i] = VOX_SKIP;
+      continue;
+    }
     int e = 0;
     const unsigned x = (unsigned)(vox_coord(p.x, inv, &e) - l0), y = (unsigned)(vox_coord(p.y, inv, &e) - l1),
                    z = (unsigned)(vox_coord(p.z, inv, &e) - l2);
@@ -106,7 +123,7 @@ __global__ void __launch_bounds__(256) k_seg_heads(const uint32_t* __restrict__ 
                                                    const int* d_n, uint32_t* __restrict__ flags) {
   const int n = cnt_of(n_host, d_n);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    flags[i] = (i == 0 || k[i] != k[i - 1]) ? 1u : 0u;
+    flags[i] = (k[i] != VOX_SKIP && (i == 0 || k[i] != k[i - 1])) ? 1u : 0u;
 }
 
 __global__ void __launch_bounds__(256) k_seg_starts(const uint32_t* __restrict__ k,
@@ -115,8 +132,12 @@ __global__ void __launch_bounds__(256) k_seg_starts(const uint32_t* __restrict__
                                                     const int* __restrict__ d_nseg) {
   const int n = cnt_of(n_host, d_n);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    if (i == 0 || k[i] != k[i - 1]) start[pos[i]] = i;
-    if (i == 0) start[*d_nseg] = n;
+    const bool keyed = k[i] != VOX_SKIP;
+    if (keyed && (i == 0 || k[i] != k[i - 1])) start[pos[i]] = i;
+    // the end of the last segment: past the last keyed point (the skipped
+    // points sort after every key)
+    if (keyed && (i + 1 == n || k[i + 1] == VOX_SKIP)) start[*d_nseg] = i + 1;
+    if (i == 0 && !keyed) start[*d_nseg] = 0;
   }
 }
 

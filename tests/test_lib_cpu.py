@@ -173,6 +173,40 @@ def test_pcd_io_round_trips_main_clouds(tmp_path):
     assert r.returncode == 2
 
 
+def test_corrupt_pcd_files_are_refused(tmp_path):
+    """Corrupt PCD files make loadPCDFile return -1 (the demo exits 2 with a
+    message), never crash or allocate from a corrupt header: truncated
+    binary data, a POINTS count far beyond the file, truncated ascii rows,
+    binary_compressed data, a missing DATA line, an empty file."""
+    demo = Path(__file__).resolve().parents[1] / "realtime_robot_gb300" / "realtime_robot_demo"
+    if not demo.exists():
+        pytest.skip("demo not built")
+    pts = np.arange(30, dtype=np.float32).reshape(10, 3)
+    hdr = ("VERSION 0.7\nFIELDS x y z\nSIZE 4 4 4\nTYPE F F F\nCOUNT 1 1 1\nWIDTH {n}\nHEIGHT 1\n"
+           "POINTS {n}\nDATA {d}\n")
+    cases = {
+        "truncated_binary": hdr.format(n=10, d="binary").encode() + pts.tobytes()[:100],
+        "huge_points_binary": hdr.format(n=1 << 40, d="binary").encode() + pts.tobytes(),
+        "huge_points_ascii": hdr.format(n=1 << 40, d="ascii").encode() + b"1 2 3\n",
+        "truncated_ascii": hdr.format(n=10, d="ascii").encode() + b"1 2 3\n4 5\n",
+        "compressed": hdr.format(n=10, d="binary_compressed").encode() + b"\x00" * 64,
+        "no_data_line": b"VERSION 0.7\nFIELDS x y z\nSIZE 4 4 4\nTYPE F F F\nCOUNT 1 1 1\nPOINTS 1\n",
+        "empty": b"",
+    }
+    for name, blob in cases.items():
+        f = tmp_path / f"{name}.pcd"
+        f.write_bytes(blob)
+        r = subprocess.run([str(demo), "pcd", str(f), str(tmp_path / "a.pcd"), str(tmp_path / "b.pcd")],
+                           capture_output=True, text=True, timeout=60)
+        assert r.returncode == 2 and "cannot read" in r.stderr, (name, r.returncode, r.stderr)
+    # the same header with its data intact reads
+    ok = tmp_path / "ok.pcd"
+    ok.write_bytes(hdr.format(n=10, d="binary").encode() + pts.tobytes())
+    r = subprocess.run([str(demo), "pcd", str(ok), str(tmp_path / "a.pcd"), str(tmp_path / "b.pcd")],
+                       capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "points 10" in r.stdout
+
+
 def test_host_only_generator_matches_the_library(rtr):
     """oracle/libsynth.so (the CPU baseline's input generator, built without
     CUDA from the same synth.cpp) gives the same clouds as librtr.so."""
