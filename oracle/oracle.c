@@ -50,7 +50,8 @@ void orc_nn1_brute(const float* q, int nq, const float* t, int nt, float r2max, 
     int bi = INT_MAX;
     for (int j = 0; j < nt; ++j) {
       float d = d2f(q + 4 * i, t + 4 * j);
-      if (d < bd || (d == bd && j < bi)) {
+      /* an infinite or NaN d^2 is never a neighbour */
+      if (d < bd || (d == bd && j < bi && d < INFINITY)) {
         bd = d;
         bi = j;
       }
@@ -166,20 +167,24 @@ static void cg_search(const cgrid* g, const float* qf, topk* T) {
     if (c[a] - (g->n[a] - 1) > k0) k0 = c[a] - (g->n[a] - 1);
   }
   for (int k = k0;; ++k) {
-    for (int z = c[2] - k; z <= c[2] + k; ++z) {
-      if (z < 0 || z >= g->n[2]) continue;
-      for (int y = c[1] - k; y <= c[1] + k; ++y) {
-        if (y < 0 || y >= g->n[1]) continue;
+    /* the ring's cells inside the grid: loops clamped to the grid (a query
+     * far outside, or with a NaN coordinate, starts at a huge ring) */
+    const int z0 = c[2] - k > 0 ? c[2] - k : 0, z1 = c[2] + k < g->n[2] - 1 ? c[2] + k : g->n[2] - 1;
+    const int y0 = c[1] - k > 0 ? c[1] - k : 0, y1 = c[1] + k < g->n[1] - 1 ? c[1] + k : g->n[1] - 1;
+    for (int z = z0; z <= z1; ++z) {
+      for (int y = y0; y <= y1; ++y) {
         int edge = (z == c[2] - k || z == c[2] + k || y == c[1] - k || y == c[1] + k);
-        for (int x = c[0] - k; x <= c[0] + k; x += (edge || k == 0) ? 1 : 2 * k) {
+        const int xs = edge || k == 0 ? (c[0] - k > 0 ? c[0] - k : 0) : c[0] - k;
+        const int xe = edge || k == 0 ? (c[0] + k < g->n[0] - 1 ? c[0] + k : g->n[0] - 1) : c[0] + k;
+        for (int x = xs; x <= xe; x += (edge || k == 0) ? 1 : 2 * k) {
           if (x < 0 || x >= g->n[0]) continue;
           int cell = (z * g->n[1] + y) * g->n[0] + x;
           for (int s = g->start[cell]; s < g->start[cell + 1]; ++s) {
             int j = g->order[s];
             float d = d2f(qf, g->pts + 4 * j);
             int last = T->k - 1;
-            /* a NaN distance is never taken */
-            if (!(d < T->bd[last]) && !(d == T->bd[last] && j < T->bi[last])) continue;
+            /* an infinite or NaN distance is never taken */
+            if (!(d < T->bd[last]) && !(d == T->bd[last] && j < T->bi[last] && d < INFINITY)) continue;
             int p = last;
             while (p > 0 && (d < T->bd[p - 1] || (d == T->bd[p - 1] && j < T->bi[p - 1]))) {
               T->bd[p] = T->bd[p - 1];
@@ -277,7 +282,7 @@ void orc_knn_brute(const float* q, int nq, const float* t, int nt, int k, int32_
     for (int j = 0; j < nt; ++j) {
       float d = d2f(q + 4 * i, t + 4 * j);
       int last = k - 1;
-      if (!(d < bd[last]) && !(d == bd[last] && j < bi[last])) continue; /* NaN never taken */
+      if (!(d < bd[last]) && !(d == bd[last] && j < bi[last] && d < INFINITY)) continue; /* nor inf */
       int p = last;
       while (p > 0 && (d < bd[p - 1] || (d == bd[p - 1] && j < bi[p - 1]))) {
         bd[p] = bd[p - 1];

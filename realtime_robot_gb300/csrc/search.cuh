@@ -131,7 +131,9 @@ __device__ __forceinline__ int first_ring(const GridView& g, int cx, int cy, int
 __device__ __forceinline__ void nn_take(float4 p, unsigned j, float4 q, float& bd, int& bi, int& bpos) {
   const float d2 = dist2_exact(q, p);
   const int id = pt_index(p);
-  if (d2 < bd || (d2 == bd && id < bi)) {
+  // a candidate at infinite (or NaN) d^2 is never a neighbour: points with a
+  // non-finite coordinate never match
+  if (d2 < bd || (d2 == bd && id < bi && d2 < __int_as_float(0x7f800000))) {
     bd = d2;
     bi = id;
     bpos = (int)j;
@@ -291,7 +293,8 @@ __device__ __forceinline__ void grid_nn1_group(const GridView& g, float4 q, floa
 // order are unique, so any k <= K of them form the exact k-NN.
 template <int K>
 __device__ __forceinline__ void knn_insert(float (&bd)[K], int (&bi)[K], float d2, int id) {
-  if (d2 > bd[K - 1] || (d2 == bd[K - 1] && id >= bi[K - 1])) return;
+  // NaN and infinite d^2 never enter the list
+  if (!(d2 < bd[K - 1]) && !(d2 == bd[K - 1] && id < bi[K - 1] && d2 < __int_as_float(0x7f800000))) return;
   bd[K - 1] = d2;
   bi[K - 1] = id;
 #pragma unroll

@@ -55,7 +55,7 @@ def test_icp_wait_budget_runs_out_then_recovers(rtr):
     try:
         s, t = _dev(src), _dev(tgt)
         c.set_wait_budget_ms(1e-6)
-        res = c.icp(s, t, 30, 0.05)
+        res, _, _ = c.icp(s, t, 30, 0.05)
         with pytest.raises(rtr.RtrError, match="RTR_ERR_TIMEOUT"):
             c.check()
         r = c.parse_icp_result(res)
@@ -142,7 +142,7 @@ def test_recognize_ignores_nonfinite_points_and_finds_nothing_in_empty_scenes(ct
 def test_icp_never_matches_nonfinite_points(ctx, rtr):
     src, tgt, T = rtr.config0_pair(2024, 6000)
     bsrc, btgt = _poison(src, 0.01, 7), _poison(tgt, 0.01, 8)
-    res, tp, tc = ctx.icp(_dev(bsrc), _dev(btgt), 20, 0.05, trace=True)
+    res, tp, tc = ctx.icp(_dev(bsrc), _dev(btgt), 50, 0.05, trace=True)
     ctx.check()
     r = ctx.parse_icp_result(res)
     assert r["status"] == 0 and np.all(np.isfinite(r["pose"]))
@@ -154,6 +154,15 @@ def test_icp_never_matches_nonfinite_points(ctx, rtr):
     assert np.all(gc[:, nonfinite_src] == -1) and not np.isin(gc, nonfinite_tgt).any()
     dt, dr = O.pose_error(r["pose"], T)
     assert dt < 0.01 and dr < np.radians(1.0)
+    # unbounded: an infinite source point is at infinite d^2 from everything
+    # and still matches nothing
+    res, tp, tc = ctx.icp(_dev(bsrc), _dev(btgt), 50, 0.0, trace=True)
+    r = ctx.parse_icp_result(res)
+    assert np.all(np.isfinite(r["pose"]))
+    gc = tc.cpu().numpy()
+    assert np.all(gc[:, nonfinite_src] == -1) and not np.isin(gc, nonfinite_tgt).any()
+    corr, _, _ = O.icp_replay(bsrc, btgt, 0.0, tp.cpu().numpy())
+    assert np.array_equal(corr, gc)
 
 
 def test_scratch_limit_returns_oom_and_context_stays_usable(rtr):
