@@ -217,6 +217,68 @@ rtr_status rtr_ref_ransac(rtr_context* ctx, const float* d_mkeys, int n_model, c
                           float max_des, float* h_T, int* h_inliers, int* h_best,
                           rtr_stream_t stream);
 
+/* ---- plane segmentation and the plane-area vector --------------------------
+ * ModelPoint::getArea / ScanPoint::get_Area (model_point.h:170-245,
+ * scan_point.h:117-188) and KeyPoint::get_Vector3D (key_point.h:87-111).
+ * The reference uses PCL's SACSegmentation (RANSAC plane, 150 iterations,
+ * 5 mm), ExtractIndices and ConvexHull: planes are taken out of the cloud one
+ * after another while more than 15 % of the points remain.  Here:
+ *   - points with a non-finite coordinate take no part;
+ *   - RANSAC sample s of round r draws three positions in the remaining
+ *     points from a SplitMix64 hash of (seed, r, s); repeated positions or
+ *     collinear points skip the sample (at most 10 x max_iterations skips);
+ *     the plane's score is its number of points within `distance` (float
+ *     |n.p + d|); samples are taken in order until 99 % confidence (the
+ *     adaptive count log(0.01) / log(1 - w^3)) or max_iterations valid
+ *     ones; the first best wins;
+ *   - the plane is refitted by least squares to its inliers (FP64 sums in a
+ *     fixed order, smallest covariance eigenvector), and its inliers are
+ *     selected again with the refitted plane (no inlier ends the loop);
+ *   - area = the area of the 2-D convex hull of the inliers projected onto
+ *     the plane; perimeter = that hull's perimeter (for a hull Qhull takes
+ *     as two-dimensional, PCL's getTotalArea reports Qhull's "area", the
+ *     perimeter);
+ *   - is_vertical: 0 when the normal is within 10 degrees of z (is_h_plane),
+ *     1 when within 80-100 degrees (is_v_plane), -1 otherwise; kept = the
+ *     reference's surface list (horizontal or vertical, area >= min_area).
+ * Results are bit-identical to the CPU oracle's (oracle/planes.c). */
+typedef struct rtr_plane_params {
+  int      max_iterations; /* 150                                         */
+  float    distance;       /* inlier distance, 0.005 m                     */
+  double   remain_frac;    /* stop when at most this fraction remains (0.15) */
+  double   min_area;       /* surfaces kept from this area (0.16 m^2)      */
+  uint64_t seed;           /* RANSAC samples (0)                           */
+} rtr_plane_params;
+
+typedef struct rtr_surface {
+  double area;          /* hull area in the plane, m^2                    */
+  double perimeter;     /* hull perimeter, m                              */
+  float  coeffs[4];     /* a, b, c (unit normal), d: a x + b y + c z + d = 0 */
+  int    is_vertical;   /* 0 horizontal, 1 vertical, -1 neither            */
+  int    kept;          /* in the reference's surface list                 */
+  int    n_inliers;
+  int    hull_vertices;
+  int    flat;          /* smallest / largest inlier covariance eigenvalue < 1e-3 */
+  int    pad;
+} rtr_surface;
+
+void rtr_plane_default_params(rtr_plane_params* p);
+/* Every extracted plane in order, kept or not, into h_surfaces (room for
+ * max_surfaces; more planes return RTR_ERR_CAPACITY with the first
+ * max_surfaces written); *h_n_surfaces = the number written.  Synchronises. */
+rtr_status rtr_plane_segment(rtr_context* ctx, const float* d_pts, int n, const rtr_plane_params* p,
+                             rtr_surface* h_surfaces, int max_surfaces, int* h_n_surfaces,
+                             rtr_stream_t stream);
+/* get_Vector3D for n_keys keypoints over the kept surfaces of h_surfaces,
+ * in list order: the first horizontal surface within 5 cm gives v3[0], the
+ * first two vertical ones within 2 cm give v3[1] and v3[2] (then sorted
+ * descending); 0.16 where none.  The distance is getDistance's (key_point.h
+ * :38-43): float expressions, sqrt of a float sum, divided in double.
+ * d_v3: n_keys x 3 doubles, ready for rtr_ref_correspond's area gate.
+ * Synchronises. */
+rtr_status rtr_vector3d(rtr_context* ctx, const float* d_keys, int n_keys, const rtr_surface* h_surfaces,
+                        int n_surfaces, double* d_v3, rtr_stream_t stream);
+
 /* ---- nearest-neighbour search ---------------------------------------------
  * Exact searches over a radix-sorted uniform grid.  Squared distances are
  * computed in FP32 as ((dx*dx + dy*dy) + dz*dz) with dx = q.x - p.x, each

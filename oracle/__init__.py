@@ -51,6 +51,8 @@ _SIG = {
     "orc_match": (None, [_P, _I, _P, _I, _I, _P, _P]),
     "orc_gc_group": (_I, [_P, _P, _P, _P, _P, _I, _F, _I, _I, _P, _P, _P]),
     "orc_orient_outward": (None, [_P, _P, _I, _F, _F, _F]),
+    "orc_plane_segment": (_I, [_P, _I, _I, _F, _D, _D, C.c_uint64, _I, _P, _P]),
+    "orc_vector3d": (None, [_P, _I, _P, _I, _P]),
     "orc_ref_occupancy": (C.c_longlong, [_P, _I, _P, _I, _F, _F, _P, _P, _P, C.c_longlong]),
     "orc_ref_tdf": (_I, [_P, _P, _I, _P, _P, _F, _F, _P]),
     "orc_ref_distance": (None, [_P, _P, _P, _P, _P, _I, _P, _I, _P, _P, C.c_longlong, _F, _F, _I, _P, _P]),
@@ -314,6 +316,38 @@ def gc_group(model_kp, scene_kp, corr_m, corr_s, corr_d, gc_size=0.01, gc_thresh
                            cd.ctypes.data, nc, float(gc_size), int(gc_thresh), max_clusters,
                            clus.ctypes.data, poses.ctypes.data, sizes.ctypes.data)
     return clus, poses[:n].reshape(n, 4, 4), sizes[:n]
+
+
+class Surface(C.Structure):
+    _fields_ = [("area", C.c_double), ("perimeter", C.c_double), ("coeffs", C.c_float * 4),
+                ("is_vertical", C.c_int), ("kept", C.c_int), ("n_inliers", C.c_int), ("hull_vertices", C.c_int),
+                ("flat", C.c_int), ("pad", C.c_int)]
+
+
+def plane_segment(pts, max_iterations: int = 150, distance: float = 0.005, remain_frac: float = 0.15,
+                  min_area: float = 0.16, seed: int = 0, max_planes: int = 64):
+    """ModelPoint::getArea / ScanPoint::get_Area restated (planes.c): the
+    extracted planes in order (kept or not) as Surface records, and the
+    number extracted (more than max_planes means some were not stored)."""
+    pts = _f4(pts)
+    out = (Surface * max_planes)()
+    tot = C.c_int(0)
+    n = lib().orc_plane_segment(pts.ctypes.data, pts.shape[0], int(max_iterations), float(distance),
+                                float(remain_frac), float(min_area), int(seed), int(max_planes), out,
+                                C.byref(tot))
+    return list(out[:n]), tot.value
+
+
+def vector3d(keys, surfaces) -> np.ndarray:
+    """KeyPoint::get_Vector3D for every keypoint over the surfaces' kept
+    ones: [nk, 3] float64."""
+    keys = _f4(keys)
+    arr = (Surface * max(1, len(surfaces)))()
+    for i, x in enumerate(surfaces):  # any record with this layout (the GPU path's too)
+        C.memmove(C.byref(arr[i]), C.byref(x), C.sizeof(Surface))
+    v = np.zeros((keys.shape[0], 3), np.float64)
+    lib().orc_vector3d(keys.ctypes.data, keys.shape[0], arr, len(surfaces), v.ctypes.data)
+    return v
 
 
 def pose_error(Ta, Tb) -> tuple[float, float]:

@@ -132,6 +132,25 @@ int orc_ref_ransac(const float* mkeys, const float* skeys, int ns, const int32_t
                    const float* score_all, const float* T_all, float inlier, float max_des, float* T_out,
                    int32_t* best_inliers);
 
+/* ---- plane segmentation + plane-area vector (planes.c) ---- */
+typedef struct {
+  double area;      /* 2-D convex hull area of the inliers in the plane   */
+  double perimeter; /* that hull's perimeter                              */
+  float coeffs[4];  /* unit normal (a, b, c) and d                         */
+  int is_vertical;  /* 0 horizontal, 1 vertical, -1 neither               */
+  int kept;         /* horizontal or vertical with area >= min_area        */
+  int n_inliers;
+  int hull_vertices;
+  int flat;         /* smallest / largest inlier covariance eigenvalue < 1e-3 */
+  int pad;
+} orc_surface;
+void orc_plane_basis(const float* c, float* e1, float* e2);
+void orc_hull_measure(const void* hull_uv, int h, double* area, double* perim);
+int orc_plane_class(const float* c);
+int orc_plane_segment(const float* pts, int n, int max_iterations, float distance, double remain_frac,
+                      double min_area, uint64_t seed, int max_planes, orc_surface* out, int* n_total);
+void orc_vector3d(const float* keys, int nk, const orc_surface* s, int ns, double* v3);
+
 #ifdef __cplusplus
 }
 #endif

@@ -57,6 +57,27 @@ MAX_INSTANCES = 16
 KNN1_STATIC_MAX_TARGET = 65536  # RTR_KNN1_STATIC_MAX_TARGET
 
 
+class PlaneParams(C.Structure):
+    _fields_ = [("max_iterations", C.c_int), ("distance", C.c_float), ("remain_frac", C.c_double),
+                ("min_area", C.c_double), ("seed", C.c_uint64)]
+
+
+class Surface(C.Structure):
+    """rtr_surface: one extracted plane (area and perimeter of its hull in
+    the plane, unit-normal coefficients, class, kept flag)."""
+    _fields_ = [("area", C.c_double), ("perimeter", C.c_double), ("coeffs", C.c_float * 4),
+                ("is_vertical", C.c_int), ("kept", C.c_int), ("n_inliers", C.c_int), ("hull_vertices", C.c_int),
+                ("flat", C.c_int), ("pad", C.c_int)]
+
+
+def plane_default_params(**kw) -> PlaneParams:
+    p = PlaneParams()
+    lib().rtr_plane_default_params(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
 class RecogParams(C.Structure):
     _fields_ = [("voxel_leaf", C.c_float), ("normal_k", C.c_int), ("scene_keypoint_r", C.c_float),
                 ("model_keypoint_r", C.c_float), ("descriptor_r", C.c_float),
@@ -135,6 +156,9 @@ _SIG = {
                             C.POINTER(C.c_int), _P]),
     "rtr_knn1": (_I, [_P, _P, _I, _P, _I, _F, _P, _P, _P]),
     "rtr_knn1_static": (_I, [_P, _I, _P, _I, _F, _P, _P, _P]),
+    "rtr_plane_default_params": (None, [C.c_void_p]),
+    "rtr_plane_segment": (_I, [_P, _P, _I, C.c_void_p, C.c_void_p, _I, C.POINTER(C.c_int), _P]),
+    "rtr_vector3d": (_I, [_P, _P, _I, C.c_void_p, _I, _P, _P]),
     "rtr_knn": (_I, [_P, _P, _I, _P, _I, _I, _P, _P, _P]),
     "rtr_icp_default_params": (None, [C.POINTER(IcpParams)]),
     "rtr_icp": (_I, [_P, _P, _I, _P, _I, C.POINTER(IcpParams), _P, _P, _P, _P, _P]),
@@ -348,6 +372,28 @@ class Context:
                                         None if P is None else P.ctypes.data, min_z, max_z, _ptr(out),
                                         _ptr(count), _stream(stream)))
         return out, count
+
+    def plane_segment(self, pts, params: PlaneParams | None = None, max_surfaces: int = 64, stream=None):
+        """rtr_plane_segment (ModelPoint::getArea / ScanPoint::get_Area):
+        the extracted planes, kept or not, as a list of Surface records."""
+        p = params or plane_default_params()
+        out = (Surface * max_surfaces)()
+        n = C.c_int(0)
+        check(lib().rtr_plane_segment(self.h, _ptr(pts), pts.shape[0], C.byref(p), out, max_surfaces, C.byref(n),
+                                      _stream(stream)))
+        return list(out[: n.value])
+
+    def vector3d(self, keys, surfaces, stream=None):
+        """rtr_vector3d (KeyPoint::get_Vector3D) for device keypoints [k, 4]:
+        the plane-area vectors [k, 3] float64 on the device."""
+        import torch
+        nk = keys.shape[0]
+        out = torch.empty((max(nk, 1), 3), dtype=torch.float64, device=keys.device)
+        arr = (Surface * max(1, len(surfaces)))()
+        for i, x in enumerate(surfaces):  # any record with the rtr_surface layout
+            C.memmove(C.byref(arr[i]), C.byref(x), C.sizeof(Surface))
+        check(lib().rtr_vector3d(self.h, _ptr(keys), nk, arr, len(surfaces), _ptr(out), _stream(stream)))
+        return out[:nk]
 
     def knn(self, query, target, k: int, stream=None):
         import torch

@@ -69,6 +69,11 @@ struct PointXYZ {
 };
 static_assert(sizeof(PointXYZ) == 16, "the rtr entry points read 16-byte points");
 
+// pcl::ModelCoefficients: a plane's a, b, c, d in `values`.
+struct ModelCoefficients {
+  std::vector<float> values;
+};
+
 template <class T>
 struct PointCloud {
   using Ptr = std::shared_ptr<PointCloud<T>>;
@@ -329,6 +334,56 @@ inline rtr_context* thread_context() {
 
 constexpr int kDescDim = 352;
 
+// Surface (key_point.h:47-51): one plane of the reference's surface list.
+struct Surface {
+  double Area = 0.0;
+  pcl::ModelCoefficients Coefficients;
+  bool IsVertical = false;
+};
+
+// getArea / get_Area (model_point.h:170-245, scan_point.h:117-188) through
+// rtr_plane_segment: the kept planes (horizontal or vertical, area >= 0.16)
+// in extraction order.  The plane's area is its inliers' 2-D convex-hull
+// area in the plane.
+inline std::vector<Surface> segment_surfaces(const Cloud& cloud, std::vector<rtr_surface>* all = nullptr) {
+  rtr_context* ctx = thread_context();
+  const int n = (int)cloud.size();
+  std::vector<Surface> out;
+  if (n == 0) return out;
+  DeviceArray<float> d_pts(4 * (size_t)n);
+  d_pts.upload(reinterpret_cast<const float*>(cloud.points.data()), 4 * (size_t)n);
+  rtr_plane_params prm;
+  rtr_plane_default_params(&prm);
+  std::vector<rtr_surface> s(256);
+  int ns = 0;
+  check(rtr_plane_segment(ctx, d_pts.p, n, &prm, s.data(), (int)s.size(), &ns, nullptr), "rtr_plane_segment");
+  s.resize((size_t)ns);
+  for (const rtr_surface& r : s) {
+    if (!r.kept) continue;
+    Surface t;
+    t.Area = r.area;
+    t.Coefficients.values.assign(r.coeffs, r.coeffs + 4);
+    t.IsVertical = r.is_vertical == 1;
+    out.push_back(t);
+  }
+  if (all) *all = s;
+  return out;
+}
+
+// The kept surfaces back in the C ABI's record form (for rtr_vector3d).
+inline std::vector<rtr_surface> to_records(const std::vector<Surface>& surface) {
+  std::vector<rtr_surface> r(surface.size());
+  for (size_t i = 0; i < surface.size(); ++i) {
+    std::memset(&r[i], 0, sizeof(rtr_surface));
+    r[i].area = surface[i].Area;
+    for (int k = 0; k < 4; ++k)
+      r[i].coeffs[k] = k < (int)surface[i].Coefficients.values.size() ? surface[i].Coefficients.values[(size_t)k] : 0.f;
+    r[i].is_vertical = surface[i].IsVertical ? 1 : 0;
+    r[i].kept = 1;
+  }
+  return r;
+}
+
 // OccupiedGrid (key_point.h:52-57): the points of the keypoint's box and the
 // number of occupied 1 cm leaves among them.
 struct OccupiedGrid {
@@ -339,9 +394,9 @@ struct OccupiedGrid {
 
 // A keypoint (key_point.h:59-86).  The SHOT route fills `descriptor`; the
 // reference's own route fills Occupiedgrid (getOccupiedGrid), grid_value and
-// Border (get_TSDF); vector3D is the plane-area vector (0.16 each by
-// default, as the reference's constructor sets it; plane areas are not
-// computed here).
+// Border (get_TSDF); vector3D is the plane-area vector (0.16 each as the
+// reference's constructor sets it, until get_Vector3D over the cloud's
+// surfaces fills it).
 struct KeyPoint {
   pcl::PointXYZ Key_coordinate;
   std::vector<float> descriptor;  // kDescDim values, L2-normalised
@@ -356,7 +411,36 @@ struct KeyPoint {
   void getOccupiedGrid(Cloud::Ptr cloud, float resolution = 0.01f, float f_adjust = 0.1f);
   // key_point.h:251-334 through rtr_ref_tdf, from Occupiedgrid.cloud.
   void get_TSDF(Cloud::Ptr cloud, float resolution = 0.01f, float f_adjust = 0.15f);
+  // key_point.h:87-111 through rtr_vector3d (vector3d_all does many at once).
+  void get_Vector3D(std::vector<Surface>& surface);
 };
+
+// get_Vector3D for many keypoints in one rtr_vector3d call.
+inline void vector3d_all(std::vector<KeyPoint>& keys, const std::vector<Surface>& surface) {
+  if (keys.empty()) return;
+  rtr_context* ctx = thread_context();
+  std::vector<float> k(4 * keys.size());
+  for (size_t i = 0; i < keys.size(); ++i) {
+    k[4 * i] = keys[i].Key_coordinate.x;
+    k[4 * i + 1] = keys[i].Key_coordinate.y;
+    k[4 * i + 2] = keys[i].Key_coordinate.z;
+    k[4 * i + 3] = 0.f;
+  }
+  DeviceArray<float> d_k(k.size());
+  DeviceArray<double> d_v(3 * keys.size());
+  d_k.upload(k.data(), k.size());
+  const std::vector<rtr_surface> rec = to_records(surface);
+  check(rtr_vector3d(ctx, d_k.p, (int)keys.size(), rec.data(), (int)rec.size(), d_v.p, nullptr), "rtr_vector3d");
+  std::vector<double> v(3 * keys.size());
+  d_v.download(v.data(), v.size());
+  for (size_t i = 0; i < keys.size(); ++i) keys[i].vector3D.assign(v.begin() + 3 * i, v.begin() + 3 * i + 3);
+}
+
+inline void KeyPoint::get_Vector3D(std::vector<Surface>& surface) {
+  std::vector<KeyPoint> one(1, *this);
+  vector3d_all(one, surface);
+  vector3D = one[0].vector3D;
+}
 
 // A model keypoint paired with a scene keypoint (point_i model, point_j
 // scene, as main builds them), with the descriptor distance that ranks it.
@@ -429,11 +513,17 @@ struct KeypointSet {
 class ModelPoint : public KeypointSet {
  public:
   Cloud::Ptr Mpoint;
+  std::vector<Surface> surface;
   ModelPoint() = default;
   explicit ModelPoint(Cloud::Ptr m) : Mpoint(std::move(m)) {}
   void getKeypoint() {
     const float vp[3] = {0.f, 0.f, 0.f};
     compute(*Mpoint, vp, true, true);
+  }
+  // model_point.h:170-245
+  void getArea(Cloud::Ptr modelPoint) {
+    const std::vector<Surface> s = segment_surfaces(*modelPoint);
+    surface.insert(surface.end(), s.begin(), s.end());
   }
 };
 
@@ -443,6 +533,12 @@ class ModelPoint : public KeypointSet {
 class ScanPoint : public KeypointSet {
  public:
   Cloud::Ptr Spoint;
+  std::vector<Surface> surface;
+  // scan_point.h:117-188
+  void get_Area(Cloud::Ptr scanPoint) {
+    const std::vector<Surface> s = segment_surfaces(*scanPoint);
+    surface.insert(surface.end(), s.begin(), s.end());
+  }
   float viewpoint[3] = {0.f, 0.f, 0.f};
   bool orient_outward = false;
   ScanPoint() = default;

@@ -57,18 +57,27 @@ static int reference_route(unsigned long long seed) {
   rtr_robot::check(rtr_synth_shape(0, 41 + seed, n, scan.data()), "rtr_synth_shape");
   for (int i = 0; i < n; ++i) scan[4 * (size_t)i] += 0.01f * (float)(seed % 5);
   Cloud::Ptr mcloud = to_cloud(model, n), cloud = to_cloud(scan, n);
+  // main's plane areas (model_point.h:170-245, scan_point.h:117-188), which
+  // fill each keypoint's vector3D for the area gate
+  rtr_robot::ModelPoint modelpoint(mcloud);
+  modelpoint.getArea(mcloud);
+  rtr_robot::ScanPoint scanpoint(cloud);
+  scanpoint.get_Area(cloud);
   std::vector<rtr_robot::KeyPoint> mk, sk;
   for (int i = 0; i < n; i += 150) {
     rtr_robot::KeyPoint p(mcloud->points[(size_t)i]);
     p.getOccupiedGrid(mcloud);
     p.get_TSDF(mcloud);
+    p.get_Vector3D(modelpoint.surface);
     mk.push_back(std::move(p));
   }
   for (int i = 0; i < n; i += 200) {
     rtr_robot::KeyPoint p(cloud->points[(size_t)i]);
     p.getOccupiedGrid(cloud);
+    p.get_Vector3D(scanpoint.surface);
     sk.push_back(std::move(p));
   }
+  std::printf("surfaces %zu %zu\n", modelpoint.surface.size(), scanpoint.surface.size());
   int kept = 0;
   for (size_t m = 0; m < mk.size(); ++m)
     for (size_t s = 0; s < sk.size(); ++s) {

@@ -59,11 +59,12 @@ def test_cpp_entry_points_register_a_chair(rtr):
 
 @pytest.mark.parametrize("seed", [1, 3])
 def test_cpp_reference_route_members(rtr, seed):
-    """main's own route on the kept KeyPoint members (getOccupiedGrid,
-    get_TSDF, get_Distance, match_by_*; one keypoint / pair per call):
-    every pair's score bit for bit and every keep decision equal to the
+    """main's own route on the kept KeyPoint members (getArea / get_Area,
+    getOccupiedGrid, get_TSDF, get_Vector3D, get_Distance, match_by_*; one
+    keypoint / pair per call): every pair's score bit for bit and every keep
+    decision (the area gate live on the clouds' plane areas) equal to the
     oracle's batched route on the same clouds."""
-    from oracle import ref_correspond, ref_distance, ref_occupancy, ref_tdf
+    from oracle import plane_segment, ref_correspond, ref_distance, ref_occupancy, ref_tdf, vector3d
     r = subprocess.run([str(DEMO), "ref", str(seed)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, (r.returncode, r.stdout[-2000:], r.stderr)
     got = [ln.split() for ln in r.stdout.splitlines() if ln.startswith("pair ")]
@@ -74,7 +75,10 @@ def test_cpp_reference_route_members(rtr, seed):
     mn, mo, mi = ref_occupancy(model, km)
     sn, _, _ = ref_occupancy(scan, ks)
     sc, _ = ref_distance(model, km, mo, mi, ref_tdf(model, km, mo, mi), ks)
-    kept = set(ref_correspond(km, mn, ks, sn, sc).tolist())
+    ms, ss = plane_segment(model)[0], plane_segment(scan)[0]
+    m_surf = re.search(r"surfaces (\d+) (\d+)", r.stdout)
+    assert m_surf and (int(m_surf.group(1)), int(m_surf.group(2))) == (sum(x.kept for x in ms), sum(x.kept for x in ss))
+    kept = set(ref_correspond(km, mn, ks, sn, sc, mv3=vector3d(km, ms), sv3=vector3d(ks, ss)).tolist())
     assert len(got) == km.shape[0] * ks.shape[0]
     for g in got:
         m, s = int(g[1]), int(g[2])
