@@ -217,6 +217,34 @@ rtr_status rtr_ref_ransac(rtr_context* ctx, const float* d_mkeys, int n_model, c
                           float max_des, float* h_T, int* h_inliers, int* h_best,
                           rtr_stream_t stream);
 
+/* ---- Harris3D keypoints -----------------------------------------------------
+ * The detector of ModelPoint::getKeypoint / ScanPoint::getKeypoint
+ * (model_point.h:127-136, scan_point.h:85-94: pcl::HarrisKeypoint3D with
+ * radius 0.05, threshold 0.01, non-maximum suppression, refinement at its
+ * default, on).  PCL is absent, so the operator is stated here: neighbours
+ * are the points within `radius` (the point included), every sum in
+ * ascending index order; normal = smallest eigenvector of the neighbours'
+ * FP32 covariance; M = mean of n n^T over the neighbours' normals; response
+ * R = det(M) - 0.04 tr(M)^2 + 0.04, which for unit normals is det(M): 0 on
+ * faces and edges, up to 1/27 at a corner of three faces (the scale the
+ * reference's 0.01 threshold fits).  Keypoints: R > threshold and (non_max)
+ * no neighbour with a larger R.  Refinement moves each to the least-squares
+ * intersection of the tangent planes of the points within `radius` (FP64),
+ * at most 10 steps, while well conditioned and within `radius` of its
+ * point.  d_keys: up to n x {x, y, z, R} in ascending point index; d_src
+ * (optional): the keypoints' point indices; *d_count (device) = K.
+ * A point with more than 1024 neighbours returns RTR_ERR_CAPACITY.
+ * Synchronises.  Equal to the CPU oracle (oracle/harris.c) bit for bit. */
+typedef struct rtr_harris_params {
+  float radius;     /* 0.05 m */
+  float threshold;  /* 0.01   */
+  int   non_max;    /* 1      */
+  int   refine;     /* 1      */
+} rtr_harris_params;
+void rtr_harris_default_params(rtr_harris_params* p);
+rtr_status rtr_harris3d(rtr_context* ctx, const float* d_pts, int n, const rtr_harris_params* p, float* d_keys,
+                        int32_t* d_src, int* d_count, rtr_stream_t stream);
+
 /* ---- plane segmentation and the plane-area vector --------------------------
  * ModelPoint::getArea / ScanPoint::get_Area (model_point.h:170-245,
  * scan_point.h:117-188) and KeyPoint::get_Vector3D (key_point.h:87-111).

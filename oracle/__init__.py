@@ -53,6 +53,7 @@ _SIG = {
     "orc_orient_outward": (None, [_P, _P, _I, _F, _F, _F]),
     "orc_plane_segment": (_I, [_P, _I, _I, _F, _D, _D, C.c_uint64, _I, _P, _P]),
     "orc_vector3d": (None, [_P, _I, _P, _I, _P]),
+    "orc_harris3d": (_I, [_P, _I, _F, _F, _I, _I, _P, _P]),
     "orc_ref_occupancy": (C.c_longlong, [_P, _I, _P, _I, _F, _F, _P, _P, _P, C.c_longlong]),
     "orc_ref_tdf": (_I, [_P, _P, _I, _P, _P, _F, _F, _P]),
     "orc_ref_distance": (None, [_P, _P, _P, _P, _P, _I, _P, _I, _P, _P, C.c_longlong, _F, _F, _I, _P, _P]),
@@ -316,6 +317,18 @@ def gc_group(model_kp, scene_kp, corr_m, corr_s, corr_d, gc_size=0.01, gc_thresh
                            cd.ctypes.data, nc, float(gc_size), int(gc_thresh), max_clusters,
                            clus.ctypes.data, poses.ctypes.data, sizes.ctypes.data)
     return clus, poses[:n].reshape(n, 4, 4), sizes[:n]
+
+
+def harris3d(pts, radius: float = 0.05, threshold: float = 0.01, non_max: bool = True, refine: bool = True):
+    """Harris3D keypoints restated (harris.c): (keys [K, 4] = x, y, z,
+    response; point index [K])."""
+    pts = _f4(pts)
+    n = pts.shape[0]
+    keys = np.zeros((max(n, 1), 4), np.float32)
+    src = np.zeros(max(n, 1), np.int32)
+    k = lib().orc_harris3d(pts.ctypes.data, n, float(radius), float(threshold), int(bool(non_max)),
+                           int(bool(refine)), keys.ctypes.data, src.ctypes.data)
+    return keys[:k].copy(), src[:k].copy()
 
 
 class Surface(C.Structure):

@@ -151,6 +151,10 @@ int orc_plane_segment(const float* pts, int n, int max_iterations, float distanc
                       double min_area, uint64_t seed, int max_planes, orc_surface* out, int* n_total);
 void orc_vector3d(const float* keys, int nk, const orc_surface* s, int ns, double* v3);
 
+/* ---- Harris3D keypoints (harris.c): keys [K][4] = x, y, z, response;
+ * src[K] = the keypoint's point index (optional); returns K ---- */
+int orc_harris3d(const float* pts, int n, float r, float thr, int non_max, int refine, float* keys, int32_t* src);
+
 #ifdef __cplusplus
 }
 #endif

@@ -57,6 +57,18 @@ MAX_INSTANCES = 16
 KNN1_STATIC_MAX_TARGET = 65536  # RTR_KNN1_STATIC_MAX_TARGET
 
 
+class HarrisParams(C.Structure):
+    _fields_ = [("radius", C.c_float), ("threshold", C.c_float), ("non_max", C.c_int), ("refine", C.c_int)]
+
+
+def harris_default_params(**kw) -> HarrisParams:
+    p = HarrisParams()
+    lib().rtr_harris_default_params(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
 class PlaneParams(C.Structure):
     _fields_ = [("max_iterations", C.c_int), ("distance", C.c_float), ("remain_frac", C.c_double),
                 ("min_area", C.c_double), ("seed", C.c_uint64)]
@@ -156,6 +168,8 @@ _SIG = {
                             C.POINTER(C.c_int), _P]),
     "rtr_knn1": (_I, [_P, _P, _I, _P, _I, _F, _P, _P, _P]),
     "rtr_knn1_static": (_I, [_P, _I, _P, _I, _F, _P, _P, _P]),
+    "rtr_harris_default_params": (None, [C.c_void_p]),
+    "rtr_harris3d": (_I, [_P, _P, _I, C.c_void_p, _P, _P, _P, _P]),
     "rtr_plane_default_params": (None, [C.c_void_p]),
     "rtr_plane_segment": (_I, [_P, _P, _I, C.c_void_p, C.c_void_p, _I, C.POINTER(C.c_int), _P]),
     "rtr_vector3d": (_I, [_P, _P, _I, C.c_void_p, _I, _P, _P]),
@@ -372,6 +386,19 @@ class Context:
                                         None if P is None else P.ctypes.data, min_z, max_z, _ptr(out),
                                         _ptr(count), _stream(stream)))
         return out, count
+
+    def harris3d(self, pts, params: HarrisParams | None = None, stream=None):
+        """rtr_harris3d (the detector of ModelPoint / ScanPoint::getKeypoint):
+        (keys [K, 4] = x, y, z, response; point indices [K]) on the device."""
+        import torch
+        p = params or harris_default_params()
+        n = pts.shape[0]
+        keys = torch.empty((max(n, 1), 4), dtype=torch.float32, device=pts.device)
+        src = torch.empty(max(n, 1), dtype=torch.int32, device=pts.device)
+        cnt = torch.zeros(1, dtype=torch.int32, device=pts.device)
+        check(lib().rtr_harris3d(self.h, _ptr(pts), n, C.byref(p), _ptr(keys), _ptr(src), _ptr(cnt), _stream(stream)))
+        k = int(cnt.item())
+        return keys[:k], src[:k]
 
     def plane_segment(self, pts, params: PlaneParams | None = None, max_surfaces: int = 64, stream=None):
         """rtr_plane_segment (ModelPoint::getArea / ScanPoint::get_Area):

@@ -508,6 +508,31 @@ struct KeypointSet {
   }
 };
 
+// The reference's own detector (model_point.h:127-136, scan_point.h:85-94:
+// HarrisKeypoint3D, radius 0.05, threshold 0.01, non-maximum suppression)
+// through rtr_harris3d: the keypoint positions of `cloud`.
+inline Cloud harris_keypoints(const Cloud& cloud, float radius = 0.05f, float threshold = 0.01f) {
+  rtr_context* ctx = thread_context();
+  const int n = (int)cloud.size();
+  Cloud out;
+  if (n == 0) return out;
+  DeviceArray<float> d_pts(4 * (size_t)n), d_keys(4 * (size_t)n);
+  DeviceArray<int32_t> d_src((size_t)n);
+  DeviceArray<int> d_cnt(1);
+  d_pts.upload(reinterpret_cast<const float*>(cloud.points.data()), 4 * (size_t)n);
+  rtr_harris_params prm;
+  rtr_harris_default_params(&prm);
+  prm.radius = radius;
+  prm.threshold = threshold;
+  check(rtr_harris3d(ctx, d_pts.p, n, &prm, d_keys.p, d_src.p, d_cnt.p, nullptr), "rtr_harris3d");
+  int K = 0;
+  d_cnt.download(&K, 1);
+  std::vector<float> k(4 * (size_t)K);
+  d_keys.download(k.data(), k.size());
+  for (int i = 0; i < K; ++i) out.push_back(pcl::PointXYZ(k[4 * (size_t)i], k[4 * (size_t)i + 1], k[4 * (size_t)i + 2]));
+  return out;
+}
+
 // model_point.h:82-94: the model cloud (a full 360-degree cloud: normals are
 // oriented outward; keypoints at the model radius).
 class ModelPoint : public KeypointSet {

@@ -78,6 +78,9 @@ static int reference_route(unsigned long long seed) {
     sk.push_back(std::move(p));
   }
   std::printf("surfaces %zu %zu\n", modelpoint.surface.size(), scanpoint.surface.size());
+  // the reference's detector on the same clouds (its keypoints are where
+  // main runs this route; the fixed strides above keep the pair count even)
+  std::printf("harris %zu %zu\n", rtr_robot::harris_keypoints(*mcloud).size(), rtr_robot::harris_keypoints(*cloud).size());
   int kept = 0;
   for (size_t m = 0; m < mk.size(); ++m)
     for (size_t s = 0; s < sk.size(); ++s) {

@@ -78,6 +78,9 @@ def test_cpp_reference_route_members(rtr, seed):
     ms, ss = plane_segment(model)[0], plane_segment(scan)[0]
     m_surf = re.search(r"surfaces (\d+) (\d+)", r.stdout)
     assert m_surf and (int(m_surf.group(1)), int(m_surf.group(2))) == (sum(x.kept for x in ms), sum(x.kept for x in ss))
+    from oracle import harris3d
+    m_h = re.search(r"harris (\d+) (\d+)", r.stdout)
+    assert m_h and (int(m_h.group(1)), int(m_h.group(2))) == (len(harris3d(model)[0]), len(harris3d(scan)[0]))
     kept = set(ref_correspond(km, mn, ks, sn, sc, mv3=vector3d(km, ms), sv3=vector3d(ks, ss)).tolist())
     assert len(got) == km.shape[0] * ks.shape[0]
     for g in got:
