@@ -467,17 +467,21 @@ def batch_block(ctx, R, steps: int):
     import torch
     from realtime_robot_gb300 import learned as L
     prm = R.recog_default_params(viewpoint=(0.0, 0.0, 0.0))
-    models, mods, scenes, npts = {}, [], [], 0
+    mods, scenes, npts, nmodel = [], [], 0, 0
     for seed in range(3000, 3064):
-        shape, model, seg, _ = L.make_pair(seed)
-        if shape not in models:
-            models[shape] = R.Model(ctx, torch.from_numpy(model).cuda(), prm)
-        mods.append(models[shape])
+        # source and target sizes both log-uniform in [2k, 60k]
+        shape, model, seg, _ = L.make_pair(seed, n_model=None)
+        mods.append(R.Model(ctx, torch.from_numpy(model).cuda(), prm))
         scenes.append(torch.from_numpy(seg).cuda())
         npts += seg.shape[0]
+        nmodel += model.shape[0]
+    models = {i: m for i, m in enumerate(mods)}
     t0 = time.perf_counter()
-    X, y = L.build_dataset(ctx, range(4000, 4040), prm, label_pose="truth")
-    mlp, losses = L.train(ctx, X, y, epochs=20, batch=4096, lr=1e-3)
+    # labels at the plain pipeline's final pose; credible keypoints repeated
+    # to a tenth of the rows
+    X, y = L.build_dataset(ctx, range(4000, 4160), prm, label_pose="plain")
+    Xb, yb = L.balance(X, y, 0.1)
+    mlp, losses = L.train(ctx, Xb, yb, epochs=20, batch=4096, lr=1e-3)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
 
@@ -510,15 +514,27 @@ def batch_block(ctx, R, steps: int):
     ctx.set_tuning("batch_workers", 0)
     ctx.set_tuning("icp_group", 0)
     res_p = [R.parse_recog_result(bytes(r)) for r in R.recognize_batch(ctx, mods, scenes, prm).cpu().numpy()]
-    res_l = [R.parse_recog_result(bytes(r)) for r in
-             R.recognize_batch(ctx, mods, scenes, prm, mlp=mlp, keep=0.25).cpu().numpy()]
-    agree = 0
-    for a, b in zip(res_p, res_l):
-        if a["instances"] and b["instances"]:
-            dt, dr = L.pose_diff(a["instances"][0]["pose"], b["instances"][0]["pose"])
-            agree += int(dt <= 0.01 and dr <= 1.0)
-        else:
-            agree += int(not a["instances"] and not b["instances"])
+
+    def agreement(net, keep):
+        """(pairs agreeing with plain, of them pairs where plain found one)"""
+        res = [R.parse_recog_result(bytes(r)) for r in
+               R.recognize_batch(ctx, mods, scenes, prm, mlp=net, keep=keep).cpu().numpy()]
+        agree = found = 0
+        for a, b in zip(res_p, res):
+            if a["instances"] and b["instances"]:
+                dt, dr = L.pose_diff(a["instances"][0]["pose"], b["instances"][0]["pose"])
+                found += int(dt <= 0.01 and dr <= 1.0)
+                agree += int(dt <= 0.01 and dr <= 1.0)
+            else:
+                agree += int(not a["instances"] and not b["instances"])
+        return agree, found
+
+    agree, found_agree = agreement(mlp, 0.25)
+    untrained = R.Mlp(ctx, seed=99)
+    gain = {"plain_found": sum(1 for a in res_p if a["instances"]),
+            "trained_keep0.25": found_agree, "random_keep0.25": agreement(untrained, 0.25)[1],
+            "trained_keep0.5": agreement(mlp, 0.5)[1], "random_keep0.5": agreement(untrained, 0.5)[1]}
+    untrained.close()
     for m in models.values():
         m.close()
     n = len(scenes)
@@ -530,9 +546,16 @@ def batch_block(ctx, R, steps: int):
             "graph_learned_with_fallback": n / (t_glearned + (n - agree) / n * t_gplain),
             "learned_graph_over_plain_sequential": t_seq / t_glearned,
             "autotuned": {"workers": workers, "icp_group": group},
-            "learned": {"keep": 0.25, "train_rows": int(X.shape[0]), "positive_rate": float(y.mean()),
+            "graph_learned_with_fallback_over_sequential_plain": (n / (t_glearned + (n - agree) / n * t_gplain)) /
+                                                                  (n / t_seq),
+            "target_learned_over_plain": 5.0,
+            "sizes": "source and target log-uniform in [2k, 60k]", "model_points": nmodel,
+            "learned": {"keep": 0.25, "labels": "plain pipeline's final pose, 1 cm inliers",
+                        "train_rows": int(X.shape[0]), "positives": int(y.sum().item()),
+                        "positive_rate": float(y.mean()), "train_rows_balanced": int(Xb.shape[0]),
                         "train_s_incl_harvest": train_s, "final_loss": float(losses[-1]),
-                        "pairs_agreeing_with_plain_1cm_1deg": agree, "fallbacks": n - agree}}
+                        "pairs_agreeing_with_plain_1cm_1deg": agree, "fallbacks": n - agree,
+                        "found_pairs_agreeing_trained_vs_random": gain}}
 
 
 def learned_room_block(ctx, R, m, s_d, prm, mlp, steps, stream, flush, plain) -> dict:

@@ -7,12 +7,13 @@ transform (rotation <= 30 deg, translation +-0.3 m per axis), with
 N(0, 2 mm) noise and 0-40 % of it cropped away by a random plane.
 
 Labels: a scene keypoint is credible (label 1) when its descriptor match is
-an inlier, within 1 cm, at a reference pose.  With label_pose="plain" the
-reference is the plain pipeline's final pose (keypoints of pairs where it
-finds no instance are all 0); with "truth" it is the generator's pose of the
-pair, which these box-built shapes need: the plain pipeline recovers few of
-their poses, so plain-pose labels are almost all 0.  Training runs on the GPU (rtr_mlp_train: the
-library's own forward/backward/Adam kernels).  Evaluation compares the
+an inlier, within 1 cm, at the plain pipeline's final pose (its first
+instance; keypoints of pairs where it finds none are all 0).  This is the
+default (label_pose="plain"); label_pose="truth" labels at the generator's
+pose instead, a side experiment.  Credible keypoints are a few in 10^4, so
+training repeats them (balance) until they make a tenth of the rows.
+Training runs on the GPU (rtr_mlp_train: the library's own
+forward/backward/Adam kernels).  Evaluation compares the
 learned form with the plain one pair by pair; a pair whose learned pose
 differs from the plain pose by more than 1 cm or 1 deg counts as a fallback
 (the plain result stands).
@@ -32,12 +33,16 @@ from . import (CHAIR, DESK, SOFA, Mlp, Model, parse_recog_result, recog_default_
 SHAPES = (CHAIR, DESK, SOFA)
 
 
-def make_pair(seed: int, shape: int | None = None, n_model: int = 20000, n_seg: int | None = None):
-    """(shape, model points, segment points, true model->segment pose)."""
+def make_pair(seed: int, shape: int | None = None, n_model: int | None = 20000, n_seg: int | None = None):
+    """(shape, model points, segment points, true model->segment pose).
+    n_seg / n_model None: drawn log-uniform in [2,000, 60,000] (the batched
+    workload draws both the source and the target size)."""
     rng = np.random.default_rng(seed)
     shape = SHAPES[seed % 3] if shape is None else shape
     if n_seg is None:
         n_seg = int(round(math.exp(rng.uniform(math.log(2000), math.log(60000)))))
+    if n_model is None:
+        n_model = int(round(math.exp(rng.uniform(math.log(2000), math.log(60000)))))
     model = synth_shape(shape, n_model, 1000 + shape)
     T = synth_rigid(seed, 30.0, 0.3)
     seg = synth_transform_noise(synth_shape(shape, n_seg, 7 * seed + 1), T, 0.002, seed + 11)
@@ -106,7 +111,7 @@ def harvest(ctx, model_dev, scene_dev, p=None, model: Model | None = None, truth
     return sdesc, y, plain
 
 
-def build_dataset(ctx, seeds, p=None, label_pose: str = "truth"):
+def build_dataset(ctx, seeds, p=None, label_pose: str = "plain"):
     """Descriptors and labels harvested from the pairs of the given seeds."""
     import torch
     xs, ys = [], []
@@ -117,6 +122,24 @@ def build_dataset(ctx, seeds, p=None, label_pose: str = "truth"):
         xs.append(x)
         ys.append(y)
     return torch.cat(xs).contiguous(), torch.cat(ys).contiguous()
+
+
+def balance(X, y, pos_frac: float = 0.1, seed: int = 0):
+    """(X, y) with the positive rows repeated until they make about pos_frac
+    of the rows (credible keypoints are a few in 10^4; without this the
+    network scores every keypoint near 0 and ranks them poorly)."""
+    import torch
+    pos = torch.nonzero(y > 0.5).flatten()
+    n_pos, n = int(pos.numel()), int(y.numel())
+    if n_pos == 0 or n_pos >= pos_frac * n:
+        return X, y
+    reps = int(math.ceil(pos_frac * (n - n_pos) / ((1.0 - pos_frac) * n_pos)))
+    extra = pos.repeat(reps - 1)
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    order = torch.randperm(n + extra.numel(), generator=g).to(y.device)
+    Xb = torch.cat([X, X[extra]])[order].contiguous()
+    yb = torch.cat([y, y[extra]])[order].contiguous()
+    return Xb, yb
 
 
 def train(ctx, X, y, epochs: int = 20, batch: int = 4096, lr: float = 1e-3, seed: int = 0):

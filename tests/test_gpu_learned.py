@@ -47,3 +47,29 @@ def test_learned_rejects_bad_keep(ctx, rtr, pair):
     for bad in (0.0, 1.5):
         with pytest.raises(rtr.RtrError):
             rtr.recognize_learned(ctx, m, mlp, seg, keep=bad, params=prm)
+
+
+def test_trained_net_beats_a_random_ranking(ctx, rtr):
+    """The credibility MLP trained on plain-pose labels (the library's own
+    kernels) against an untrained one (an arbitrary ranking) at the same keep
+    fraction, on held-out pairs where the plain pipeline finds the object:
+    the trained net's pruning reproduces the plain pose (<= 1 cm / 1 deg) on
+    more of them.  Keep 0.5: at 0.25 neither reproduces any (the credible
+    keypoints are a few in 10^4 of the training rows)."""
+    from realtime_robot_gb300 import learned as L
+    prm = rtr.recog_default_params(viewpoint=(0.0, 0.0, 0.0))
+    X, y = L.build_dataset(ctx, range(4000, 4160), prm, label_pose="plain")
+    assert y.sum().item() > 20
+    Xb, yb = L.balance(X, y, 0.1)
+    assert abs(yb.mean().item() - 0.1) < 0.02
+    mlp, losses = L.train(ctx, Xb, yb, epochs=20)
+    assert losses[-1] < losses[0]
+    rand = rtr.Mlp(ctx, seed=99)
+
+    def found_agree(net):
+        rows = L.evaluate(ctx, net, range(6000, 6060), keep=0.5, p=prm, repeats=1)
+        return sum(r["agree"] for r in rows if r["plain_found"]), sum(r["plain_found"] for r in rows)
+
+    t, n_found = found_agree(mlp)
+    r, _ = found_agree(rand)
+    assert n_found >= 20 and t >= 5 and t > r + 2, (t, r, n_found)
