@@ -502,6 +502,7 @@ def batch_block(ctx, R, steps: int):
     reps = max(1, min(steps, 5))
     t_seq = timed(seq, reps)
     workers, group = R.batch_autotune(ctx, mods[:16], scenes[:16], prm)
+    tuned = R.batch_tuning(ctx)
     t_plain = timed(lambda: R.recognize_batch(ctx, mods, scenes, prm), reps)
     t_learned = timed(lambda: R.recognize_batch(ctx, mods, scenes, prm, mlp=mlp, keep=0.25), reps)
     # the same batches captured once into CUDA graphs and replayed
@@ -511,8 +512,8 @@ def batch_block(ctx, R, steps: int):
     t_glearned = timed(lambda: gl.launch(), reps)
     gp.close()
     gl.close()
-    ctx.set_tuning("batch_workers", 0)
-    ctx.set_tuning("icp_group", 0)
+    for k in ("batch_workers", "icp_group", "scene_grid_mm", "normals_grid_mm"):
+        ctx.set_tuning(k, 0)
     res_p = [R.parse_recog_result(bytes(r)) for r in R.recognize_batch(ctx, mods, scenes, prm).cpu().numpy()]
 
     def agreement(net, keep):
@@ -545,7 +546,7 @@ def batch_block(ctx, R, steps: int):
             # a pair whose learned pose disagrees with the plain one is re-run plain
             "graph_learned_with_fallback": n / (t_glearned + (n - agree) / n * t_gplain),
             "learned_graph_over_plain_sequential": t_seq / t_glearned,
-            "autotuned": {"workers": workers, "icp_group": group},
+            "autotuned": tuned,
             "graph_learned_with_fallback_over_sequential_plain": (n / (t_glearned + (n - agree) / n * t_gplain)) /
                                                                   (n / t_seq),
             "target_learned_over_plain": 5.0,

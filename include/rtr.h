@@ -79,6 +79,8 @@ const char* rtr_version(void);
  * Unknown keys or values return RTR_ERR_INVALID_ARG.  Results do not depend
  * on the knobs beyond FP32 summation order. */
 rtr_status rtr_context_set_tuning(rtr_context* ctx, const char* key, int value);
+/* The current value of a tuning knob (0 = the automatic choice). */
+rtr_status rtr_context_get_tuning(const rtr_context* ctx, const char* key, int* value);
 
 /* Create a context on `device`: owns a scratch arena, a device status word
  * and the tensor-map cache.  Fails with RTR_ERR_NO_DEVICE when the device is
@@ -633,9 +635,15 @@ rtr_status rtr_batch_graph_create(rtr_context* ctx, const rtr_batch_pair* h_pair
                                   rtr_recog_result* d_results, rtr_batch_graph** out);
 rtr_status rtr_batch_graph_launch(rtr_batch_graph* g, rtr_stream_t stream);
 rtr_status rtr_batch_graph_destroy(rtr_batch_graph* g);
-/* Times the batch under each (workers 1/2/4/8) x (ICP lanes per point 2/4/8)
- * setting and keeps the fastest in the context's tuning knobs; reports it in
- * h_workers / h_icp_group (either may be NULL).  Runs the batch 24 times;
+/* Autotuner of the batch: times it under each (workers 1/2/4/8: pairs per
+ * stream, the share of the GPU each pair's kernels get) x (ICP lanes per
+ * source point 2/4/8) setting, then, with the fastest fixed, each scene-grid
+ * cell of the verification and refinement searches (automatic, 20, 40,
+ * 60 mm) and each normals k-NN grid cell (automatic, 20, 30, 80 mm); keeps
+ * the fastest in the context's tuning knobs (rtr_context_get_tuning reads
+ * them) and reports workers / ICP lanes in h_workers / h_icp_group (either
+ * may be NULL).  The searches are exact, so the knobs change speed, not
+ * results (beyond FP32 block-sum order in ICP).  Runs the batch 40 times;
  * d_results holds the last run's results. */
 rtr_status rtr_batch_autotune(rtr_context* ctx, const rtr_batch_pair* h_pairs, int n_pairs,
                               const rtr_recog_params* p, const rtr_mlp* mlp, float keep,

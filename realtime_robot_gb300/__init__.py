@@ -153,6 +153,7 @@ _SIG = {
     "rtr_context_set_wait_budget_ms": (_I, [_P, _D]),
     "rtr_context_check": (_I, [_P, _P]),
     "rtr_context_set_tuning": (_I, [_P, C.c_char_p, _I]),
+    "rtr_context_get_tuning": (_I, [_P, C.c_char_p, C.POINTER(C.c_int)]),
     "rtr_context_set_profiling": (_I, [_P, _I]),
     "rtr_context_profile_count": (_I, [_P]),
     "rtr_context_profile_get": (_I, [_P, _I, C.POINTER(C.c_char_p), C.POINTER(C.c_float)]),
@@ -308,6 +309,11 @@ class Context:
 
     def set_wait_budget_ms(self, ms: float):
         check(lib().rtr_context_set_wait_budget_ms(self.h, ms))
+
+    def get_tuning(self, key: str) -> int:
+        v = C.c_int(0)
+        check(lib().rtr_context_get_tuning(self.h, key.encode(), C.byref(v)))
+        return v.value
 
     def set_tuning(self, key: str, value: int):
         check(lib().rtr_context_set_tuning(self.h, key.encode(), int(value)))
@@ -872,6 +878,11 @@ def batch_autotune(ctx: "Context", models, scenes, params: RecogParams, mlp: "Ml
     check(lib().rtr_batch_autotune(ctx.h, _batch_args(models, scenes), n, C.byref(params),
                                    mlp.h if mlp else None, float(keep), _ptr(results), C.byref(w), C.byref(g)))
     return w.value, g.value
+
+
+def batch_tuning(ctx: "Context") -> dict:
+    """The tuple the autotuner settled on (0 = the automatic choice)."""
+    return {k: ctx.get_tuning(k) for k in ("batch_workers", "icp_group", "scene_grid_mm", "normals_grid_mm")}
 
 
 def recognize_host(ctx: "Context", model: Model, scene: np.ndarray, params: RecogParams | None = None):

@@ -47,6 +47,8 @@ rtr_status batch_ensure_workers(rtr_context* ctx, int n) {
     w->wait_budget_ms = ctx->wait_budget_ms;
     w->wait_budget_cycles = ctx->wait_budget_cycles;
     w->tune_icp_group = ctx->tune_icp_group;
+    w->tune_scene_grid_mm = ctx->tune_scene_grid_mm;
+    w->tune_normals_grid_mm = ctx->tune_normals_grid_mm;
     w->scratch_limit = ctx->scratch_limit;
   }
   return RTR_OK;
@@ -188,24 +190,40 @@ rtr_status rtr_batch_autotune(rtr_context* ctx, const rtr_batch_pair* h_pairs, i
                               rtr_recog_result* d_results, int* h_workers, int* h_icp_group) {
   RTR_CHECK_ARG(ctx && p && h_pairs && d_results && n_pairs > 0, "rtr_batch_autotune: bad arguments");
   RTR_CUDA(cudaSetDevice(ctx->device));
+  const int saved[4] = {ctx->tune_batch_workers, ctx->tune_icp_group, ctx->tune_scene_grid_mm,
+                        ctx->tune_normals_grid_mm};
+  int* knob[4] = {&ctx->tune_batch_workers, &ctx->tune_icp_group, &ctx->tune_scene_grid_mm,
+                  &ctx->tune_normals_grid_mm};
+  // one untimed pass (scratch growth), then one timed pass
+  auto run = [&](double* dt) -> rtr_status {
+    rtr_status r = rtr_recognize_batch(ctx, h_pairs, n_pairs, p, mlp, keep, d_results);
+    const auto t0 = std::chrono::steady_clock::now();
+    if (r == RTR_OK) r = rtr_recognize_batch(ctx, h_pairs, n_pairs, p, mlp, keep, d_results);
+    *dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return r;
+  };
+  auto restore = [&]() {
+    for (int k = 0; k < 4; ++k) *knob[k] = saved[k];
+  };
+  // stage 1: workers (pairs per stream, "warps per pair" of the shared GPU)
+  // x lanes per ICP source point; stages 2 and 3, with those fixed: the
+  // scene grid's cell (verification and refinement searches) and the
+  // normals' k-NN grid cell, in mm (0 = the automatic choice)
   static const int kWorkers[] = {1, 2, 4, 8};
   static const int kGroups[] = {2, 4, 8};
+  static const int kSceneMm[] = {0, 20, 40, 60};
+  static const int kNormalsMm[] = {0, 20, 30, 80};
   double best = 1e300;
   int bw = 4, bg = 0;
-  const int saved_w = ctx->tune_batch_workers, saved_g = ctx->tune_icp_group;
-  for (int g : kGroups) {
+  for (int g : kGroups)
     for (int w : kWorkers) {
       if (w > n_pairs && w != 1) continue;
       ctx->tune_batch_workers = w;
       ctx->tune_icp_group = g;
-      // one untimed pass (scratch growth), then one timed pass
-      rtr_status r = rtr_recognize_batch(ctx, h_pairs, n_pairs, p, mlp, keep, d_results);
-      const auto t0 = std::chrono::steady_clock::now();
-      if (r == RTR_OK) r = rtr_recognize_batch(ctx, h_pairs, n_pairs, p, mlp, keep, d_results);
-      const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      double dt = 0;
+      const rtr_status r = run(&dt);
       if (r != RTR_OK) {
-        ctx->tune_batch_workers = saved_w;
-        ctx->tune_icp_group = saved_g;
+        restore();
         return r;
       }
       if (dt < best) {
@@ -214,9 +232,27 @@ rtr_status rtr_batch_autotune(rtr_context* ctx, const rtr_batch_pair* h_pairs, i
         bg = g;
       }
     }
-  }
   ctx->tune_batch_workers = bw;
   ctx->tune_icp_group = bg;
+  for (int stage = 2; stage <= 3; ++stage) {
+    const int* cand = stage == 2 ? kSceneMm : kNormalsMm;
+    int* k = stage == 2 ? &ctx->tune_scene_grid_mm : &ctx->tune_normals_grid_mm;
+    int bestv = *k;
+    for (int i = 0; i < 4; ++i) {
+      *k = cand[i];
+      double dt = 0;
+      const rtr_status r = run(&dt);
+      if (r != RTR_OK) {
+        restore();
+        return r;
+      }
+      if (dt < best) {
+        best = dt;
+        bestv = cand[i];
+      }
+    }
+    *k = bestv;
+  }
   if (h_workers) *h_workers = bw;
   if (h_icp_group) *h_icp_group = bg;
   return RTR_OK;

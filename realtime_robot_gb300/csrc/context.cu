@@ -277,6 +277,18 @@ rtr_status rtr_context_set_tuning(rtr_context* ctx, const char* key, int value) 
   return rtr::fail(RTR_ERR_INVALID_ARG, "rtr_context_set_tuning: unknown key '%s'", key);
 }
 
+rtr_status rtr_context_get_tuning(const rtr_context* ctx, const char* key, int* value) {
+  if (!ctx || !key || !value) return rtr::fail(RTR_ERR_INVALID_ARG, "rtr_context_get_tuning: NULL argument");
+  if (strcmp(key, "batch_workers") == 0) *value = ctx->tune_batch_workers;
+  else if (strcmp(key, "gc_window") == 0) *value = ctx->tune_gc_window;
+  else if (strcmp(key, "scene_grid_mm") == 0) *value = ctx->tune_scene_grid_mm;
+  else if (strcmp(key, "normals_grid_mm") == 0) *value = ctx->tune_normals_grid_mm;
+  else if (strcmp(key, "icp_group") == 0) *value = ctx->tune_icp_group;
+  else if (strcmp(key, "scratch_limit_mb") == 0) *value = (int)(ctx->scratch_limit >> 20);
+  else return rtr::fail(RTR_ERR_INVALID_ARG, "rtr_context_get_tuning: unknown key '%s'", key);
+  return RTR_OK;
+}
+
 rtr_status rtr_context_check(rtr_context* ctx, rtr_stream_t stream) {
   if (!ctx) return rtr::fail(RTR_ERR_INVALID_ARG, "rtr_context_check: ctx is NULL");
   int st = 0;

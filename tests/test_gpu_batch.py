@@ -65,10 +65,18 @@ def test_batch_learned_equals_single_calls(ctx, rtr, batch):
 
 def test_batch_autotune(ctx, rtr, batch):
     prm, mods, scenes = batch
+    ref = [bytes(r) for r in rtr.recognize_batch(ctx, mods[:4], scenes[:4], prm).cpu().numpy()]
     w, g = rtr.batch_autotune(ctx, mods[:4], scenes[:4], prm)
+    t = rtr.batch_tuning(ctx)
     assert w in (1, 2, 4, 8) and g in (2, 4, 8)
-    ctx.set_tuning("batch_workers", 0)
-    ctx.set_tuning("icp_group", 0)
+    assert t["batch_workers"] == w and t["icp_group"] == g
+    assert t["scene_grid_mm"] in (0, 20, 40, 60) and t["normals_grid_mm"] in (0, 20, 30, 80)
+    # the tuned grids change speed, not results (ICP block sums aside)
+    got = [bytes(r) for r in rtr.recognize_batch(ctx, mods[:4], scenes[:4], prm).cpu().numpy()]
+    for a, b in zip(got, ref):
+        _same(rtr, a, b)
+    for k in ("batch_workers", "icp_group", "scene_grid_mm", "normals_grid_mm"):
+        ctx.set_tuning(k, 0)
 
 
 def test_batch_empty(ctx, rtr, batch):
