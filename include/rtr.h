@@ -67,6 +67,13 @@ const char* rtr_version(void);
  *                    (2, 4 or 8);
  *   "batch_workers"  workers (streams) of rtr_recognize_batch (1..16);
  *   "gc_window"      seeds per window of the grouping walk (32..1024);
+ *   "gc_pass_lists"  1: the grouping keeps no pass lists, so a consensus
+ *                    set that lost a member is recomputed by a new round
+ *                    instead of in place by the walk (same clusters;
+ *                    slower; 0 restores the default);
+ *   "gc_inline"      sets the grouping walk recomputes in place per round
+ *                    before it hands the rest of the window back to the
+ *                    parallel phase (1..4096; default 16);
  *   "scene_grid_mm"  cell edge (mm) of the recognition's scene grid, used by
  *                    verification and ICP refinement (default: 1.5 x the ICP
  *                    distance; the table's size limit may widen it);

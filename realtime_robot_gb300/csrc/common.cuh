@@ -77,6 +77,8 @@ struct rtr_context {
   int tune_batch_workers = 0;          // workers of rtr_recognize_batch (0: automatic)
   int coop_div = 1;                    // cooperative grids use 1/coop_div of the GPU
   int tune_gc_window = 0;              // seeds per grouping window (0: automatic)
+  int tune_gc_no_lists = 0;            // 1: the grouping keeps no pass lists (every stale set ends a round)
+  int tune_gc_inline = 0;              // sets the grouping walk recomputes in place per round (0: automatic)
   int tune_scene_grid_mm = 0;          // cell edge of the recognition's scene grid (0: 1.5 ICP distances)
   int tune_normals_grid_mm = 0;        // cell edge of the scene normals' k-NN grid (0: 5 voxel leaves)
   std::vector<rtr_context*> workers;   // child contexts of the batch driver

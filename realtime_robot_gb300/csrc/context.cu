@@ -257,6 +257,18 @@ rtr_status rtr_context_set_tuning(rtr_context* ctx, const char* key, int value) 
     ctx->tune_gc_window = value;
     return RTR_OK;
   }
+  if (strcmp(key, "gc_pass_lists") == 0) {
+    if (value < 0 || value > 1)
+      return rtr::fail(RTR_ERR_INVALID_ARG, "gc_pass_lists must be 0 or 1 (got %d)", value);
+    ctx->tune_gc_no_lists = value;
+    return RTR_OK;
+  }
+  if (strcmp(key, "gc_inline") == 0) {
+    if (value < 0 || value > 4096)
+      return rtr::fail(RTR_ERR_INVALID_ARG, "gc_inline must be 0..4096 (got %d)", value);
+    ctx->tune_gc_inline = value;
+    return RTR_OK;
+  }
   if (strcmp(key, "scene_grid_mm") == 0 || strcmp(key, "normals_grid_mm") == 0) {
     if (value < 0 || value > 1000)
       return rtr::fail(RTR_ERR_INVALID_ARG, "%s must be 0..1000 (got %d)", key, value);
@@ -281,6 +293,8 @@ rtr_status rtr_context_get_tuning(const rtr_context* ctx, const char* key, int* 
   if (!ctx || !key || !value) return rtr::fail(RTR_ERR_INVALID_ARG, "rtr_context_get_tuning: NULL argument");
   if (strcmp(key, "batch_workers") == 0) *value = ctx->tune_batch_workers;
   else if (strcmp(key, "gc_window") == 0) *value = ctx->tune_gc_window;
+  else if (strcmp(key, "gc_pass_lists") == 0) *value = ctx->tune_gc_no_lists;
+  else if (strcmp(key, "gc_inline") == 0) *value = ctx->tune_gc_inline;
   else if (strcmp(key, "scene_grid_mm") == 0) *value = ctx->tune_scene_grid_mm;
   else if (strcmp(key, "normals_grid_mm") == 0) *value = ctx->tune_normals_grid_mm;
   else if (strcmp(key, "icp_group") == 0) *value = ctx->tune_icp_group;

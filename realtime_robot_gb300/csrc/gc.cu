@@ -81,13 +81,157 @@ __device__ __forceinline__ bool gc_consistent(float4 am, float4 as, float4 bm, f
   return !(fabsf(__fsub_rn(__fsqrt_rn(u), __fsqrt_rn(v))) > gc);
 }
 
+// Spatial pruning of the seed tests.  A candidate b passes seed a only if
+// |d_model(a, b) - d_scene(a, b)| <= gc, and d_model(a, b) is at most F_a,
+// the distance from a's model endpoint to the farthest corner of the model
+// endpoints' box; so every passing b has its scene endpoint within
+// R_a = F_a + gc of a's.  The candidates are sorted by a coarse cell of
+// their scene endpoint, cut into chunks of 32 and each chunk given the exact
+// box of its endpoints; a seed skips every chunk whose box lies farther than
+// R_a (plus a slack far above the rounding of every quantity involved) and
+// tests the others' candidates as before, so the pass bits are the same as
+// testing every candidate.  A chunk holding a point with a non-finite
+// coordinate is never skipped.
+struct GcGrid {
+  GridMeta m;     // box of the scene endpoints, origin, cell edge, dims, ncells
+  float mlo[3], mhi[3];  // box of the model endpoints
+  float slack;    // metres added to every reach
+};
+constexpr unsigned GC_GRID_CELLS = 1u << 15;
+
+__device__ __forceinline__ int gcg_cell(float v, float o, float inv_h, int n) {
+  float f = __fmul_rn(__fsub_rn(v, o), inv_h);
+  f = fminf(fmaxf(f, -1.0e8f), 1.0e8f);
+  const int c = (int)floorf(f);
+  return c < 0 ? 0 : (c > n - 1 ? n - 1 : c);
+}
+
+// Cell edge an eighth of the largest reach (model box diagonal + gc), grown
+// until the scene endpoints' box needs at most GC_GRID_CELLS cells.
+__global__ void k_gcg_setup(GcGrid* gg, const GridMeta* __restrict__ mbox, float gc, int C_host, const int* d_C) {
+  if (threadIdx.x != 0) return;
+  const int n = d_C ? min(*d_C, C_host) : C_host;
+  GridMeta& m = gg->m;
+  float lo[3], hi[3];
+  double diag2 = 0.0, mag = 0.0;
+  for (int a = 0; a < 3; ++a) {
+    lo[a] = n > 0 ? ordered_to_float(m.bmin[a]) : 0.f;
+    hi[a] = n > 0 ? ordered_to_float(m.bmax[a]) : 0.f;
+    if (!isfinite(lo[a]) || !isfinite(hi[a]) || !(hi[a] >= lo[a])) {
+      lo[a] = isfinite(lo[a]) ? lo[a] : (isfinite(hi[a]) ? hi[a] : 0.f);
+      hi[a] = isfinite(hi[a]) && hi[a] >= lo[a] ? hi[a] : lo[a];
+    }
+    const float ml = n > 0 ? ordered_to_float(mbox->bmin[a]) : 0.f;
+    const float mh = n > 0 ? ordered_to_float(mbox->bmax[a]) : 0.f;
+    gg->mlo[a] = ml;
+    gg->mhi[a] = mh;
+    const double e = (double)mh - (double)ml;
+    diag2 += e * e;
+    mag = fmax(mag, fmax(fmax(fabs((double)lo[a]), fabs((double)hi[a])), fmax(fabs((double)ml), fabs((double)mh))));
+  }
+  const double R = sqrt(diag2) + (double)gc;
+  double h = R / 8.0;
+  if (!(h > 1.0e-4) || !(h < 1.0e15)) h = !(h < 1.0e15) ? 1.0e15 : 1.0e-4;
+  int dims[3] = {1, 1, 1};
+  bool fits = false;
+  for (int tries = 0; tries < 64 && !fits; ++tries) {
+    double cells = 1.0;
+    for (int a = 0; a < 3; ++a) {
+      double e = floor(((double)hi[a] - (double)lo[a]) / h) + 1.0;
+      if (e > 2.0e9) e = 2.0e9;
+      dims[a] = (int)e;
+      cells *= e;
+    }
+    if (cells <= (double)GC_GRID_CELLS) fits = true;
+    else h = h * cbrt(cells / (double)GC_GRID_CELLS) * 1.001;
+  }
+  if (!fits) {  // one cell: the order is the sorted order, boxes stay exact
+    dims[0] = dims[1] = dims[2] = 1;
+    h = 1.0e15;
+  }
+  const float hf = (float)h;
+  m.ox = lo[0];
+  m.oy = lo[1];
+  m.oz = lo[2];
+  m.h = hf;
+  m.inv_h = 1.0f / hf;
+  m.nx = dims[0];
+  m.ny = dims[1];
+  m.nz = dims[2];
+  m.n = n;
+  m.ncells = (unsigned)dims[0] * (unsigned)dims[1] * (unsigned)dims[2];
+  const double slack = 1.0e-4 + 1.0e-5 * (R + mag);
+  gg->slack = (float)(slack < 1.0e30 ? slack : 1.0e30);
+}
+
+__global__ void __launch_bounds__(256) k_gcg_keys(const float4* __restrict__ ps, int C_host, const int* d_C,
+                                                  const GcGrid* __restrict__ gg, uint32_t* __restrict__ keys) {
+  const int n = d_C ? min(*d_C, C_host) : C_host;
+  const GridMeta& m = gg->m;
+  const float ox = m.ox, oy = m.oy, oz = m.oz, ih = m.inv_h;
+  const int nx = m.nx, ny = m.ny, nz = m.nz;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4 p = ps[i];
+    if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) {
+      keys[i] = m.ncells;
+      continue;
+    }
+    const int cx = gcg_cell(p.x, ox, ih, nx), cy = gcg_cell(p.y, oy, ih, ny), cz = gcg_cell(p.z, oz, ih, nz);
+    keys[i] = ((uint32_t)cz * (uint32_t)ny + (uint32_t)cy) * (uint32_t)nx + (uint32_t)cx;
+  }
+}
+
+// Candidates in cell order (w = sorted position) and, per chunk of 32, the
+// box of their scene endpoints (lo.w = 1 when the chunk holds a non-finite
+// point).  Block size a multiple of 32: each warp covers whole chunks.
+__global__ void __launch_bounds__(256) k_gcg_gather(const float4* __restrict__ ps, const float4* __restrict__ pm,
+                                                    const uint32_t* __restrict__ order, int C_host, const int* d_C,
+                                                    float4* __restrict__ cpts, float4* __restrict__ cpm,
+                                                    float4* __restrict__ cbox) {
+  const int n = d_C ? min(*d_C, C_host) : C_host;
+  const int lane = threadIdx.x & 31;
+  const int stride = gridDim.x * blockDim.x;
+  for (int i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); i0 < n; i0 += stride) {
+    const int i = i0 + lane;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    int nf = 0;
+    if (i < n) {
+      const uint32_t o = order[i];
+      float4 p = ps[o];
+      if (isfinite(p.x) && isfinite(p.y) && isfinite(p.z)) {
+        lo[0] = hi[0] = p.x;
+        lo[1] = hi[1] = p.y;
+        lo[2] = hi[2] = p.z;
+      } else {
+        nf = 1;
+      }
+      p.w = __int_as_float((int)o);
+      cpts[i] = p;
+      cpm[i] = pm[o];
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], off));
+        hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], off));
+      }
+    nf = __any_sync(0xffffffffu, nf);
+    if (lane == 0) {
+      cbox[2 * (i0 >> 5)] = make_float4(lo[0], lo[1], lo[2], nf ? 1.f : 0.f);
+      cbox[2 * (i0 >> 5) + 1] = make_float4(hi[0], hi[1], hi[2], 0.f);
+    }
+  }
+}
+
 // Device-side control block of the grouping walk.
 struct GcCoop {
   int* ctl;            // [0] walk position, [1] clusters, [2] done, [3] error status, [4] rounds,
                        // [5] sets computed, [6] seeds needing a set this round,
                        // [7] candidates that passed a seed test (summed over sets),
                        // [8..11] microseconds in phases P, A1, A2, B (block 0's view),
-                       // [12] the next round's window (0: the first window)
+                       // [12] the next round's window (0: the first window),
+                       // [13] pass-list pool entries handed out
   unsigned* arrive;    // grid barrier counter (zero at launch)
   int* computed;       // [C] 1 once the seed's set has been computed
   int* cl_members;     // [max_clusters][maxs] sorted positions
@@ -101,6 +245,19 @@ struct GcCoop {
   int win;             // seeds in the first window
   int win_max;         // seeds a window may grow to (the need/mask capacity)
   int nwp;             // words per mask row (C/32 rounded up to a multiple of 4)
+  const GcGrid* sg;    // pruning constants (model box, slack)
+  const float4* cpts;  // scene endpoints sorted by coarse cell; w = sorted position (int bits)
+  const float4* cpm;   // model endpoints in the same order
+  const float4* cbox;  // [chunks][2] box of each chunk of 32 cpts (lo.w = 1: holds a non-finite point)
+  float4* seed_s;      // [win_max] listed seed's scene endpoint, w = its reach (+inf: unbounded)
+  float4* seed_m;      // [win_max] listed seed's model endpoint
+  int* pcnt;           // [win_max] seed-test passes of each listed seed
+  int* plist_off;      // [C] start of the seed's pass list in pool (-1: none kept)
+  int* plist_cnt;      // [C] length of the seed's pass list
+  float4* pool_m;      // pass lists in ascending sorted position: model endpoint (w = position bits)
+  float4* pool_s;      // ... and scene endpoint
+  int pool_cap;        // entries (0: no lists kept)
+  int inline_max;      // sets the walk recomputes in place per round before it ends the round
 };
 
 __device__ __forceinline__ bool sbit(const unsigned* s, int i) { return (s[i >> 5] >> (i & 31)) & 1u; }
@@ -152,13 +309,18 @@ constexpr int GC_PREF = 7;   // mask loads in flight per lane during admission
 // it.  Same result as admitting one candidate at a time.
 template <bool LONG>
 __device__ __forceinline__ void gc_admit(const GcDev& g, int a, const int* slot, int n, float4* mem_m,
-                                         float4* mem_s, int& cnt, float r2max, int* n_tested) {
+                                         float4* mem_s, int& cnt, float r2max, int* n_tested, float4* list_m,
+                                         float4* list_s, int list_len) {
   const int lane = threadIdx.x & 31;
   const int pj = lane < n ? slot[lane] : -1;
   float4 cm = make_float4(0, 0, 0, 0), cs = cm;
   if (pj >= 0) {
     cm = __ldg(g.pm + pj);
     cs = __ldg(g.ps + pj);
+    if (list_m && *n_tested + lane < list_len) {  // the pass list entry: endpoints, position in w
+      list_m[*n_tested + lane] = make_float4(cm.x, cm.y, cm.z, __int_as_float(pj));
+      list_s[*n_tested + lane] = cs;
+    }
   }
   *n_tested += n;
   bool pass = pj >= 0;
@@ -194,6 +356,60 @@ __device__ __forceinline__ void gc_admit(const GcDev& g, int a, const int* slot,
   __syncwarp();
 }
 
+// The consensus set of seed a under the current taken bits, from a's pass
+// list (entries in ascending sorted position that passed a's seed test when
+// it was computed; a superset of the ones not taken now): greedy admission in
+// list order, candidates taken since skipped, each candidate tested against
+// every member so far (member 0 is the seed).  Members go to rec[]
+// (positions) and mem_m/mem_s.  Returns the member count, or -1 when the set
+// would exceed cap (the caller falls back to a recompute in the next round).
+__device__ __forceinline__ int gc_inline_set(const GcDev& g, int a, const float4* lm, const float4* ls, int nl,
+                                             const unsigned* taken, float4* mem_m, float4* mem_s, int* rec, int cap,
+                                             float r2max) {
+  const int lane = threadIdx.x & 31;
+  if (lane == 0) {
+    mem_m[0] = __ldg(g.pm + a);
+    mem_s[0] = __ldg(g.ps + a);
+    rec[0] = a;
+  }
+  __syncwarp();
+  int cnt = 1;
+  float4 nm = make_float4(0.f, 0.f, 0.f, 0.f), ns = nm;
+  if (lane < nl) {
+    nm = __ldcg(lm + lane);
+    ns = __ldcg(ls + lane);
+  }
+  for (int i0 = 0; i0 < nl; i0 += 32) {
+    const bool have = i0 + lane < nl;
+    const float4 cm = nm, cs = ns;
+    if (i0 + 32 + lane < nl) {  // the next chunk's entries in flight during this one
+      nm = __ldcg(lm + i0 + 32 + lane);
+      ns = __ldcg(ls + i0 + 32 + lane);
+    }
+    const int b = have ? __float_as_int(cm.w) : -1;
+    bool pass = have && !sbit(taken, b);
+    for (int m = 1; m < cnt; ++m)
+      if (pass) pass = gc_consistent(mem_m[m], mem_s[m], cm, cs, g.gc, r2max);
+    unsigned bal = __ballot_sync(0xffffffffu, pass);
+    while (bal) {
+      const int f = __ffs(bal) - 1;
+      if (cnt >= cap) return -1;
+      const float4 fm = shfl4(cm, f), fs = shfl4(cs, f);
+      if (lane == f) {
+        mem_m[cnt] = cm;
+        mem_s[cnt] = cs;
+        rec[cnt] = b;
+      }
+      ++cnt;
+      if (lane > f && pass) pass = gc_consistent(fm, fs, cm, cs, g.gc, r2max);
+      if (lane <= f) pass = false;
+      bal = __ballot_sync(0xffffffffu, pass);
+    }
+    __syncwarp();
+  }
+  return cnt;
+}
+
 // The whole grouping in one cooperative launch.  Each round:
 //  P. warps check the seeds of the window [pos, pos + win): a seed that is
 //     not taken and has no set yet, or whose set lost a member to a commit,
@@ -219,9 +435,8 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
   extern __shared__ unsigned s_taken[];  // copy of the taken bitset
   __shared__ float4 mem_m[GC_WARPS][GC_MAXS], mem_s[GC_WARPS][GC_MAXS];
   __shared__ int s_slot[GC_WARPS][GC_PEND];
-  __shared__ float4 s_gm[GC_WARPS][32], s_gs[GC_WARPS][32];  // seed tests: the chunk's candidates
-  __shared__ int s_ga[GC_WARPS][32];                          // (sorted position, -1: skipped)
   __shared__ int s_bmem[32][33];  // walk: first 32 members of the next 32 seeds (padded rows)
+  __shared__ int s_rec[GC_MAXS];  // walk: members of a set recomputed in place
   __shared__ int s_pos, s_done, s_ok, s_win;
   __shared__ float s_r2max;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -275,54 +490,81 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
           need = __any_sync(0xffffffffu, st);
         }
       }
-      if (need && lane == 0) c.need[atomicAdd(c.ctl + 6, 1)] = a;
+      int slot = 0;
+      if (need && lane == 0) {
+        slot = atomicAdd(c.ctl + 6, 1);
+        c.need[slot] = a;
+        c.pcnt[slot] = 0;
+        // reach: farthest corner of the model box from a's model endpoint, plus gc
+        const float4 am = __ldg(g.pm + a), as = __ldg(g.ps + a);
+        const float fx = fmaxf(fabsf(am.x - c.sg->mlo[0]), fabsf(c.sg->mhi[0] - am.x));
+        const float fy = fmaxf(fabsf(am.y - c.sg->mlo[1]), fabsf(c.sg->mhi[1] - am.y));
+        const float fz = fmaxf(fabsf(am.z - c.sg->mlo[2]), fabsf(c.sg->mhi[2] - am.z));
+        float R = sqrtf(fx * fx + fy * fy + fz * fz) * 1.00001f + g.gc + c.sg->slack;
+        R = R < 1.0e18f ? R * R : __int_as_float(0x7f800000);  // NaN reach: unbounded
+        c.seed_s[slot] = make_float4(as.x, as.y, as.z, R);
+        c.seed_m[slot] = am;
+      }
+      // the seed tests only set bits: its mask row starts clear
+      slot = __shfl_sync(0xffffffffu, slot, 0);
+      if (need) {
+        uint4* row = reinterpret_cast<uint4*>(c.mask + (size_t)slot * c.nwp);
+        for (int v = lane; v < (nwp >> 2); v += 32) row[v] = make_uint4(0u, 0u, 0u, 0u);
+      }
     }
     target += gridDim.x;
     if (!gc_barrier(c, target, &s_ok)) return;
     GC_PHASE(0)
     const int nneed = __ldcg(c.ctl + 6);
-    // ---- A1: seed tests -> pass bitmasks.  Items are (group of 32 listed
-    // seeds, chunk of 32 candidates); every warp takes a contiguous run of
-    // items.  Lane k holds seed k of its group in registers; the chunk's
-    // candidates are staged in shared memory once, and each lane tests its
-    // seed against all 32 of them, building its mask word bit by bit.
+    // ---- A1: seed tests -> pass bitmasks.  Items are (chunk of 32
+    // candidates in cell order, group of 32 listed seeds), spread over all
+    // warps (a chunk near many seeds is shared by as many warps as it has
+    // seed groups).  Lane k holds candidate k of the chunk and seed k of the
+    // group; the group's seeds whose reach meets the chunk's box are taken in
+    // turn, and every lane tests its candidate against each, setting its pass
+    // bit in the seed's row.
     if (nneed > 0) {
-      const int ngrp = (nneed + 31) >> 5;
-      const long long items = (long long)nwp * ngrp;
-      const long long per = (items + nwarps - 1) / nwarps;
-      const long long it0 = (long long)gw * per, it1 = min(items, it0 + per);
-      int cur = -1, kend = 0, sa = -1;
-      float4 sm = make_float4(0, 0, 0, 0), ss = sm;
-      for (long long it = it0; it < it1; ++it) {
-        const int grp = (int)(it / nwp), ch = (int)(it - (long long)grp * nwp);
-        if (grp != cur) {
-          kend = min(32, nneed - grp * 32);
-          sa = -1;
-          if (lane < kend) {
-            sa = __ldcg(c.need + grp * 32 + lane);
-            sm = __ldg(g.pm + sa);
-            ss = __ldg(g.ps + sa);
-          }
-          cur = grp;
+      const int nchunks = (g.C + 31) >> 5;
+      const int ngroups = (nneed + 31) >> 5;
+      const long long items = (long long)nchunks * ngroups;
+      for (long long it = gw; it < items; it += nwarps) {
+        const int ch = (int)(it / ngroups);
+        const int s0 = (int)(it - (long long)ch * ngroups) * 32;
+        const int i = ch * 32 + lane, k = s0 + lane;
+        float4 q = make_float4(0.f, 0.f, 0.f, 0.f), bm = q, sa = q, sm = q;
+        int sa_i = -1;
+        if (i < g.C) {
+          q = __ldg(c.cpts + i);
+          bm = __ldg(c.cpm + i);
         }
-        const int b = ch * 32 + lane;
-        const bool okb = b < g.C && !sbit(s_taken, b);
-        __syncwarp();
-        s_ga[wid][lane] = okb ? b : -1;
-        if (okb) {
-          s_gm[wid][lane] = __ldg(g.pm + b);
-          s_gs[wid][lane] = __ldg(g.ps + b);
+        if (k < nneed) {
+          sa = __ldcg(c.seed_s + k);
+          sm = __ldcg(c.seed_m + k);
+          sa_i = __ldcg(c.need + k);
         }
-        __syncwarp();
-        unsigned mine = 0u;
-        if (lane < kend) {
-#pragma unroll 4
-          for (int j = 0; j < 32; ++j) {
-            const int cb = s_ga[wid][j];
-            if (cb >= 0 && cb != sa && gc_consistent(sm, ss, s_gm[wid][j], s_gs[wid][j], g.gc, r2max))
-              mine |= 1u << j;
-          }
-          c.mask[(size_t)(grp * 32 + lane) * c.nwp + ch] = mine;
+        const float4 blo = __ldg(c.cbox + 2 * ch), bhi = __ldg(c.cbox + 2 * ch + 1);
+        const int b = i < g.C ? __float_as_int(q.w) : -1;
+        const bool ok = b >= 0 && !sbit(s_taken, b);
+        if (!__any_sync(0xffffffffu, ok)) continue;
+        bool hit = false;
+        if (k < nneed) {
+          const float dx = fmaxf(fmaxf(blo.x - sa.x, sa.x - bhi.x), 0.f);
+          const float dy = fmaxf(fmaxf(blo.y - sa.y, sa.y - bhi.y), 0.f);
+          const float dz = fmaxf(fmaxf(blo.z - sa.z, sa.z - bhi.z), 0.f);
+          hit = blo.w != 0.f || !(dx * dx + dy * dy + dz * dz > sa.w);  // NaN distance: not skipped
+        }
+        const unsigned bit = 1u << (b & 31);
+        const int word = b >> 5;
+        unsigned hits = __ballot_sync(0xffffffffu, hit);
+        while (hits) {
+          const int f = __ffs(hits) - 1;
+          hits &= hits - 1;
+          const float4 fa = shfl4(sa, f), fm = shfl4(sm, f);
+          const int a = __shfl_sync(0xffffffffu, sa_i, f);
+          const bool pass = ok && b != a && gc_consistent(fm, fa, bm, q, g.gc, r2max);
+          const unsigned pb = __ballot_sync(0xffffffffu, pass);
+          if (pass) atomicOr(c.mask + (size_t)(s0 + f) * c.nwp + word, bit);
+          if (lane == 0 && pb) atomicAdd(c.pcnt + s0 + f, __popc(pb));
         }
       }
     }
@@ -339,6 +581,19 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
       }
       __syncwarp();
       int cnt = 1, npend = 0, ntest = 0;
+      // the seed's pass list (ascending) is kept for the walk, which
+      // recomputes a set that lost a member from it
+      int n_list = 0, off = -1;
+      if (lane == 0) {
+        n_list = __ldcg(c.pcnt + slot);
+        off = atomicAdd(c.ctl + 13, n_list);
+        if (off < 0 || (long long)off + n_list > (long long)c.pool_cap) off = -1;
+      }
+      n_list = __shfl_sync(0xffffffffu, n_list, 0);
+      off = __shfl_sync(0xffffffffu, off, 0);
+      int nemit = 0;
+      float4* lmp = off >= 0 ? c.pool_m + off : nullptr;
+      float4* lsp = off >= 0 ? c.pool_s + off : nullptr;
       const uint4* row = reinterpret_cast<const uint4*>(c.mask + (size_t)slot * c.nwp);
       const int nv = nwp >> 2;
       for (int v0 = 0; v0 < nv; v0 += 32 * GC_PREF) {
@@ -375,10 +630,11 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
                 --rc;
               }
             }
+            nemit += min(total, room);
             npend += min(total, room);
             __syncwarp();
             while (npend >= 32) {
-              gc_admit<LONG>(g, a, s_slot[wid], 32, mem_m[wid], mem_s[wid], cnt, r2max, &ntest);
+              gc_admit<LONG>(g, a, s_slot[wid], 32, mem_m[wid], mem_s[wid], cnt, r2max, &ntest, lmp, lsp, n_list);
               const int rest = npend - 32;
               const int mv = lane < rest ? s_slot[wid][32 + lane] : 0;
               __syncwarp();
@@ -389,8 +645,10 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
           }
         }
       }
-      if (npend > 0) gc_admit<LONG>(g, a, s_slot[wid], npend, mem_m[wid], mem_s[wid], cnt, r2max, &ntest);
+      if (npend > 0) gc_admit<LONG>(g, a, s_slot[wid], npend, mem_m[wid], mem_s[wid], cnt, r2max, &ntest, lmp, lsp, n_list);
       if (lane == 0) {
+        c.plist_off[a] = (nemit == n_list && ntest == n_list) ? off : -1;
+        c.plist_cnt[a] = n_list;
         g.set_size[a] = cnt;
         c.computed[a] = 1;
         atomicAdd(c.ctl + 5, 1);
@@ -406,7 +664,7 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
     // stale set) are handled in order, and after a commit the later lanes
     // evaluate again.
     if (blockIdx.x == 0 && wid == 0) {
-      int ncl = __ldcg(c.ctl + 1), err = 0;
+      int ncl = __ldcg(c.ctl + 1), err = 0, n_inline = 0;
       bool done = false, stop = false;
       int p = pos;
       const int wend = min(pos + win, g.C);
@@ -453,10 +711,38 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
           const int f = __ffs(ev) - 1;
           const bool f_stale = __shfl_sync(0xffffffffu, stale_l, f);
           const int nf = __shfl_sync(0xffffffffu, n_l, f);
-          if (f_stale) {  // lost a member: recompute from p + f
-            p += f;
-            stop = true;
-            break;
+          if (f_stale) {
+            // lost a member: recompute in place from the pass list, or
+            // (no list kept, or too many members) end the round here
+            const int sa = p + f;
+            const int off = n_inline < c.inline_max ? __ldcg(c.plist_off + sa) : -1;
+            const int ns = off < 0 ? -1
+                                   : gc_inline_set(g, sa, c.pool_m + off, c.pool_s + off, __ldcg(c.plist_cnt + sa),
+                                                   s_taken, mem_m[0], mem_s[0], s_rec, min(GC_MAXS, maxs), r2max);
+            ++n_inline;
+            if (ns < 0) {
+              p += f;
+              stop = true;
+              break;
+            }
+            if (lane == 0) atomicAdd(c.ctl + 5, 1);
+            if (ns >= c.thresh) {
+              for (int k = lane; k < ns; k += 32) {
+                const int mb = s_rec[k];
+                atomicOr(&s_taken[mb >> 5], 1u << (mb & 31));
+                c.cl_members[(size_t)ncl * maxs + k] = mb;
+              }
+              if (lane == 0) c.cl_sizes[ncl] = ns;
+              __syncwarp();
+              ++ncl;
+              if (ncl >= c.max_clusters) {
+                done = stop = true;
+                p += f + 1;
+                break;
+              }
+            }
+            cursor = f + 1;
+            continue;
           }
           if (nf > maxs) {
             err = (int)RTR_ERR_CAPACITY;
@@ -624,6 +910,13 @@ struct GcBufs {
   GridMeta* mbox;
   int* need;
   unsigned* mask;
+  GcGrid* sg;
+  uint32_t *gk0, *gv0, *gk1, *gv1;
+  float4 *cpts, *cpm;
+  float4* cbox;
+  float4 *seed_s, *seed_m;
+  int *pcnt, *plist_off, *plist_cnt;
+  float4 *pool_m, *pool_s;
 };
 
 // Window of the walk and the width of a pass-mask row.
@@ -638,6 +931,16 @@ static int gc_win(int C, int want = 0) {
   if (w < 32) w = 32;
   return (int)w;
 }
+
+// Pass-list pool: 64 entries (32 bytes each) per correspondence, between
+// 256K and 4M (a seed whose list does not fit keeps none: its set is
+// recomputed by a round).
+static int gc_pool_cap(int C) {
+  const long long want = (long long)(C > 0 ? C : 1) * 64;
+  return (int)(want < (1 << 18) ? (1 << 18) : (want > (4 << 20) ? (4 << 20) : want));
+}
+// Sets the walk recomputes in place per round (measured on the room scene).
+constexpr int GC_INLINE_MAX = 16;
 
 static void gc_plan(ScratchPlan& p, int C, int max_clusters, int max_members) {
   const int n = C > 0 ? C : 1;
@@ -657,6 +960,18 @@ static void gc_plan(ScratchPlan& p, int C, int max_clusters, int max_members) {
   p.add<GridMeta>(1);
   p.add<int>(gc_win(C, GC_WIN_MAX));
   p.add<unsigned>((size_t)gc_win(C, GC_WIN_MAX) * gc_nwp(C));
+  p.add<GcGrid>(1);
+  for (int i = 0; i < 4; ++i) p.add<uint32_t>(n);
+  p.add<float4>(n);
+  p.add<float4>(n);
+  p.add<float4>((size_t)2 * ((n + 31) / 32));
+  p.add<float4>(gc_win(C, GC_WIN_MAX));
+  p.add<float4>(gc_win(C, GC_WIN_MAX));
+  p.add<int>(gc_win(C, GC_WIN_MAX));
+  p.add<int>(n);
+  p.add<int>(n);
+  p.add<float4>(gc_pool_cap(C));
+  p.add<float4>(gc_pool_cap(C));
 }
 
 static bool gc_take(Scratch& s, int C, int max_clusters, int max_members, GcBufs* b) {
@@ -680,7 +995,22 @@ static bool gc_take(Scratch& s, int C, int max_clusters, int max_members, GcBufs
   b->mbox = s.take<GridMeta>(1);
   b->need = s.take<int>(gc_win(C, GC_WIN_MAX));
   b->mask = s.take<unsigned>((size_t)gc_win(C, GC_WIN_MAX) * gc_nwp(C));
-  return b->mask != nullptr;
+  b->sg = s.take<GcGrid>(1);
+  b->gk0 = s.take<uint32_t>(n);
+  b->gv0 = s.take<uint32_t>(n);
+  b->gk1 = s.take<uint32_t>(n);
+  b->gv1 = s.take<uint32_t>(n);
+  b->cpts = s.take<float4>(n);
+  b->cpm = s.take<float4>(n);
+  b->cbox = s.take<float4>((size_t)2 * ((n + 31) / 32));
+  b->seed_s = s.take<float4>(gc_win(C, GC_WIN_MAX));
+  b->seed_m = s.take<float4>(gc_win(C, GC_WIN_MAX));
+  b->pcnt = s.take<int>(gc_win(C, GC_WIN_MAX));
+  b->plist_off = s.take<int>(n);
+  b->plist_cnt = s.take<int>(n);
+  b->pool_m = s.take<float4>(gc_pool_cap(C));
+  b->pool_s = s.take<float4>(gc_pool_cap(C));
+  return b->pool_s != nullptr;
 }
 
 // Shared memory of k_gc_coop beyond its static part (the taken bitset).  The
@@ -727,9 +1057,20 @@ static rtr_status gc_launch(rtr_context* ctx, Scratch& s, const float* d_model_k
   RTR_CUDA(cudaMemsetAsync(b.arrive, 0, sizeof(unsigned), st));
   GcDev g{b.pm, b.ps, C, d_C, gc_size, b.taken, b.set_size, b.set_mem, gc_set_stride(C)};
   bbox_build(b.mbox, b.pm, C, d_C, st);
+  // the coarse grid over the scene endpoints (seed-test pruning)
+  bbox_build(&b.sg->m, b.ps, C, d_C, st);
+  k_gcg_setup<<<1, 32, 0, st>>>(b.sg, b.mbox, gc_size, C, d_C);
+  k_gcg_keys<<<nb, 256, 0, st>>>(b.ps, C, d_C, b.sg, b.gk0);
+  uint32_t *gks, *gvs;  // gks unused: the cell order is all the seed tests need
+  radix_sort_pairs(b.gk0, b.gv0, b.gk1, b.gv1, b.hist, C, C, d_C, 16, true, st, &gks, &gvs);
+  k_gcg_gather<<<nb, 256, 0, st>>>(b.ps, b.pm, gvs, C, d_C, b.cpts, b.cpm, b.cbox);
+  RTR_LAUNCHED(3);
   GcCoop c{b.misc, b.arrive, b.computed, b.members, b.sizes, gc_thresh, max_clusters,
            ctx->wait_budget_cycles, ctx->d_status, b.mbox, b.need, b.mask,
-           gc_win(C, ctx->tune_gc_window > 0 ? ctx->tune_gc_window : 0), gc_win(C, GC_WIN_MAX), gc_nwp(C)};
+           gc_win(C, ctx->tune_gc_window > 0 ? ctx->tune_gc_window : 0), gc_win(C, GC_WIN_MAX), gc_nwp(C),
+           b.sg, b.cpts, b.cpm, b.cbox, b.seed_s, b.seed_m, b.pcnt, b.plist_off, b.plist_cnt, b.pool_m, b.pool_s,
+           ctx->tune_gc_no_lists ? 0 : gc_pool_cap(C),
+           ctx->tune_gc_inline > 0 ? ctx->tune_gc_inline : GC_INLINE_MAX};
   const bool long_sets = gc_set_stride(C) > GC_MAXS;
   auto kern = long_sets ? k_gc_coop<true> : k_gc_coop<false>;
   RTR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GC_MAX_DYN_SMEM));

@@ -130,3 +130,49 @@ def test_gc_wait_budget_runs_out_then_recovers(rtr):
         _check(c, mk, sk, cm, cs, cd, 0.01, 3, 64)
     finally:
         c.close()
+
+
+@pytest.mark.parametrize("case", ["dense", "far"])
+def test_gc_without_pass_lists_same_clusters_more_rounds(rtr, case):
+    """The walk recomputes a set that lost a member in place, from the pass
+    list its admission kept; with no lists kept (the gc_pass_lists knob) every
+    such set ends the round and the next round recomputes it.  Both give the
+    oracle's clusters; the in-place form needs fewer rounds."""
+    if case == "dense":
+        mk, sk, cm, cs, cd = _random_scene(3, 600, 4000, 20000, 0.5)
+        gc, th, maxc = 0.01, 3, 256
+    else:
+        mk, sk, cm, cs, cd = _random_scene(4, 300, 3000, 9000, 3.0)
+        gc, th, maxc = 0.005, 4, 256
+    c = rtr.Context(0)
+    try:
+        rounds = {}
+        for off in (0, 1):
+            c.set_tuning("gc_pass_lists", off)
+            assert c.get_tuning("gc_pass_lists") == off
+            _check(c, mk, sk, cm, cs, cd, gc, th, maxc)
+            rounds[off] = c.gc_stats()["rounds"]
+        assert rounds[0] <= rounds[1]
+        if case == "dense":
+            assert rounds[0] < rounds[1]
+    finally:
+        c.close()
+
+
+def test_gc_nonfinite_scene_endpoints(ctx):
+    """Scene keypoints with a NaN or infinite coordinate: the seed tests never
+    skip the chunks that hold them (the consistency test of a NaN distance
+    passes, as in the oracle), so the clusters stay the oracle's."""
+    mk, sk, cm, cs, cd = _random_scene(6, 400, 3000, 12000, 0.6)
+    used = np.unique(cs)
+    rng = np.random.default_rng(6)
+    bad = rng.choice(used, 6, replace=False)
+    sk[bad[:3], 0] = np.nan
+    sk[bad[3:], 1] = np.inf
+    mem, sizes, _ = ctx.gc_group(_dev(mk), _dev(sk), _dev(cm, np.int32), _dev(cs, np.int32), _dev(cd),
+                                 0.01, 3, 64, 128)
+    mem, sizes = mem.cpu().numpy(), sizes.cpu().numpy()
+    clus, _, rsizes = O.gc_group(mk, sk, cm, cs, cd, 0.01, 3, 64)
+    assert np.array_equal(sizes, rsizes) and len(sizes) > 0
+    for k in range(len(sizes)):
+        assert set(mem[k][: sizes[k]].tolist()) == set(np.nonzero(clus == k)[0].tolist()), k
