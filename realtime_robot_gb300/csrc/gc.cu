@@ -388,8 +388,9 @@ __device__ __forceinline__ int gc_inline_set(const GcDev& g, int a, const float4
     }
     const int b = have ? __float_as_int(cm.w) : -1;
     bool pass = have && !sbit(taken, b);
-    for (int m = 1; m < cnt; ++m)
-      if (pass) pass = gc_consistent(mem_m[m], mem_s[m], cm, cs, g.gc, r2max);
+    // the member tests are independent: no early exit, so they overlap
+#pragma unroll 4
+    for (int m = 1; m < cnt; ++m) pass &= gc_consistent(mem_m[m], mem_s[m], cm, cs, g.gc, r2max);
     unsigned bal = __ballot_sync(0xffffffffu, pass);
     while (bal) {
       const int f = __ffs(bal) - 1;
@@ -697,11 +698,21 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
           bool taken_l = true, stale_l = false;
           if (lane >= cursor && lane < nb) {
             taken_l = sbit(s_taken, my);
-            if (!taken_l)
-              for (int k = 0; k < ns_l && !stale_l; ++k) {
+            if (!taken_l) {
+              // the first 8 members' taken bits in two rounds of independent
+              // loads (a slot past the set reads the seed's own bit: clear)
+              int mb8[8];
+#pragma unroll
+              for (int k = 0; k < 8; ++k) mb8[k] = k < ns_l ? s_bmem[lane][k] : my;
+              unsigned acc = 0u;
+#pragma unroll
+              for (int k = 0; k < 8; ++k) acc |= s_taken[mb8[k] >> 5] >> (mb8[k] & 31);
+              stale_l = (acc & 1u) != 0u;
+              for (int k = 8; k < ns_l && !stale_l; ++k) {
                 const int mb = k < 32 ? s_bmem[lane][k] : __ldcg(g.set_mem + (size_t)my * maxs + k);
                 stale_l = sbit(s_taken, mb);
               }
+            }
           }
           const unsigned ev = __ballot_sync(0xffffffffu, !taken_l && (stale_l || n_l >= c.thresh));
           if (!ev) {
@@ -920,7 +931,7 @@ struct GcBufs {
 };
 
 // Window of the walk and the width of a pass-mask row.
-constexpr int GC_WIN = 256;      // first window: room 2.69 ms (256) vs 3.06 ms (1024 throughout); results identical
+constexpr int GC_WIN = 512;      // first window (room scene: 1.21 ms at 512, 1.27 at 256, 1.25 at 128); results identical
 constexpr int GC_WIN_MAX = 2048;  // a window grows to this while the walk keeps using whole windows
 static int gc_nwp(int C) { return (((C > 0 ? C : 1) + 31) / 32 + 3) & ~3; }
 static int gc_win(int C, int want = 0) {
