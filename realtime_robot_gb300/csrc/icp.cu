@@ -64,6 +64,7 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(const IcpDev* __restrict__ 
   }
   const int B = a.nblk;
   const GridView g = load_view(a.grid);
+  const bool near27 = grid_near27_ok(g, a.r2max);  // every match within the 27 cells around a query
   // Centring: target terms about the target box centre c, source terms about
   // the source box centre moved by the current pose (cp), so the FP32 products
   // stay small even while the clouds are far apart.
@@ -99,7 +100,10 @@ __global__ void __launch_bounds__(ICP_THREADS) k_icp(const IcpDev* __restrict__ 
       const float4 p = xform_exact(T, a.src[i]);
       float d2;
       int j, pos;
-      grid_nn1_group<G, true>(g, p, a.r2max, lg, gmask, d2, j, pos);  // the group agrees on (d2, j, pos)
+      if (near27)  // the group agrees on (d2, j, pos)
+        grid_nn1_near<G>(g, p, a.r2max, lg, gmask, d2, j, pos);
+      else
+        grid_nn1_group<G, true>(g, p, a.r2max, lg, gmask, d2, j, pos);
       if (j >= 0) {
         const float4 q = g.pts[pos];
         const float dp[3] = {__fsub_rn(p.x, cp.x), __fsub_rn(p.y, cp.y), __fsub_rn(p.z, cp.z)};
@@ -368,15 +372,20 @@ int icp_max_blocks(rtr_context* ctx) {
 }
 
 // Lanes per source point: the tuning override when set, else the most lanes
-// (8, 4, 2) with which the launch needs at most four passes over its points
-// (measured on GB300: a 20k-point ICP is fastest at 8, two passes; sixteen
-// 9.2k-point refinements at 2, 3.8 passes: 2.35 ms against 2.48 at 4).
-int icp_pick_group(const rtr_context* ctx, long long total_pts, int blocks) {
+// (8, 4, 2) with which the launch needs at most max_passes passes over its
+// points: four for the ring search, eight for the 27-cell search (near:
+// every problem's grid cell is wider than its correspondence distance).
+// Measured on GB300: a 20k-point ICP (ring search) is fastest at 8, two
+// passes; sixteen 9.2k-point refinements on the ring search at 2, 3.8 passes
+// (2.35 ms against 2.48 at 4); the same on the 27-cell search at 4, 7.6
+// passes (1.63 ms against 1.90 at 2 and 1.78 at 8).
+int icp_pick_group(const rtr_context* ctx, long long total_pts, int blocks, bool near) {
   const int t = ctx->tune_icp_group;
   if (t == 2 || t == 4 || t == 8) return t;
   const long long lanes = (long long)blocks * ICP_THREADS;
-  if (total_pts * 8 <= 4 * lanes) return 8;
-  return total_pts * 4 <= 4 * lanes ? 4 : 2;
+  const long long max_passes = near ? 8 : 4;
+  if (total_pts * 8 <= max_passes * lanes) return 8;
+  return total_pts * 4 <= max_passes * lanes ? 4 : 2;
 }
 
 static rtr_status launch_icp(int G, const IcpDev* d_probs, const int* d_blk2prob, int blocks, cudaStream_t st) {
@@ -436,7 +445,7 @@ void icp_multi_plan(ScratchPlan& p, int n_probs, int max_blocks) {
   p.add<unsigned>((size_t)n_probs * 2);
 }
 
-rtr_status icp_multi(rtr_context* ctx, Scratch& s, std::vector<IcpSpec>& specs, cudaStream_t st) {
+rtr_status icp_multi(rtr_context* ctx, Scratch& s, std::vector<IcpSpec>& specs, cudaStream_t st, bool near) {
   const int M = (int)specs.size();
   if (M == 0) return RTR_OK;
   const int maxb = icp_max_blocks(ctx);
@@ -499,7 +508,7 @@ rtr_status icp_multi(rtr_context* ctx, Scratch& s, std::vector<IcpSpec>& specs, 
   RTR_CUDA(cudaGetLastError());
   long long total = 0;
   for (int i = 0; i < M; ++i) total += specs[i].dev.n_src;
-  return launch_icp(icp_pick_group(ctx, total, used), d_probs, d_b2p, used, st);
+  return launch_icp(icp_pick_group(ctx, total, used, near), d_probs, d_b2p, used, st);
 }
 
 }  // namespace rtr

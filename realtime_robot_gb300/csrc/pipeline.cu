@@ -155,6 +155,7 @@ __global__ void __launch_bounds__(256) k_hv_count(GridDev gd, const float4* __re
   if (d_nhyp) n_hyp = min(*d_nhyp, n_hyp);
   if (h >= n_hyp) return;
   const GridView g = load_view(gd);
+  const bool near27 = grid_near27_ok(g, r2);  // every inlier within the 27 cells around a point
   float T[12];
 #pragma unroll
   for (int k = 0; k < 12; ++k) T[k] = __double2float_rn(poses[(size_t)h * 16 + k]);
@@ -167,10 +168,16 @@ __global__ void __launch_bounds__(256) k_hv_count(GridDev gd, const float4* __re
   const int i1 = min(total, (part + 1) * HV_PPB);
   for (int i = part * HV_PPB + threadIdx.x / HV_G; i < i1; i += blockDim.x / HV_G) {
     const float4 p = xform_exact(T, model[(size_t)i * stride]);
-    float d2;
-    int bi, bp;
-    grid_nn1_group<HV_G, true>(g, p, r2, lg, gmask, d2, bi, bp);
-    if (lg == 0 && bi >= 0) ++cnt;
+    bool in;
+    if (near27) {
+      in = grid_any_near<HV_G>(g, p, r2, lg, gmask);
+    } else {
+      float d2;
+      int bi, bp;
+      grid_nn1_group<HV_G, true>(g, p, r2, lg, gmask, d2, bi, bp);
+      in = bi >= 0;
+    }
+    if (lg == 0 && in) ++cnt;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
@@ -772,7 +779,10 @@ static rtr_status model_stages(rtr_context* ctx, const Scratch& stage, const Sce
       d.slot = k;
       specs[k].init_dev = b.init + 16 * k;
     }
-    RTR_TRY(icp_multi(ctx, t, specs, st));
+    // the scene grid's cell (1.5 x the ICP distance unless tuned) against the
+    // correspondence distance: the 27-cell search applies
+    const float cell = ctx->tune_scene_grid_mm > 0 ? 1e-3f * (float)ctx->tune_scene_grid_mm : 1.5f * q->icp_max_dist;
+    RTR_TRY(icp_multi(ctx, t, specs, st, cell >= 1.01f * q->icp_max_dist));
   }
   {
     ProfScope ps(ctx, st, "final_score");

@@ -289,6 +289,121 @@ __device__ __forceinline__ void grid_nn1_group(const GridView& g, float4 q, floa
   }
 }
 
+// True when every point within sqrt(r2max) of any query lies in the 3x3x3
+// cells around the query's cell: the cell edge exceeds the radius by 1 % and
+// the grid is small enough (<= 4096 cells per axis) that the rounding of a
+// cell index stays far below that slack.
+__device__ __forceinline__ bool grid_near27_ok(const GridView& g, float r2max) {
+  const float r = sqrtf(r2max);
+  return r2max >= 0.f && isfinite(r) && g.h >= 1.01f * r && g.nx <= 4096 && g.ny <= 4096 && g.nz <= 4096;
+}
+
+// Exact 1-NN with d^2 <= r2max over the 27 cells around the query's cell
+// (precondition: grid_near27_ok), G lanes per query as grid_nn1_group; same
+// result.  The query's own cell is scanned first; a neighbour is fetched only
+// when its box, measured through the query's distances to its own cell's
+// faces (an underestimate), is within the lane's current best plus the
+// rounding margin.  No ring bookkeeping, no division, no square root per
+// cell.
+template <int G>
+__device__ __forceinline__ void grid_nn1_near(const GridView& g, float4 q, float r2max, int lg, unsigned gmask,
+                                              float& bd, int& bi, int& bpos) {
+  bd = r2max;
+  bi = INT_MAX;
+  bpos = -1;
+  const int cx = q_cell(q.x, g.ox, g.inv_h), cy = q_cell(q.y, g.oy, g.inv_h),
+            cz = q_cell(q.z, g.oz, g.inv_h);
+  const float margin = search_margin(g, q, 1);
+  // distances to the own cell's lower and upper faces (clamped at 0)
+  const float xl = g.ox + (float)cx * g.h, yl = g.oy + (float)cy * g.h, zl = g.oz + (float)cz * g.h;
+  const float fxm = fmaxf(q.x - xl, 0.f), fxp = fmaxf(xl + g.h - q.x, 0.f);
+  const float fym = fmaxf(q.y - yl, 0.f), fyp = fmaxf(yl + g.h - q.y, 0.f);
+  const float fzm = fmaxf(q.z - zl, 0.f), fzp = fmaxf(zl + g.h - q.z, 0.f);
+  const float fxm2 = fxm * fxm, fxp2 = fxp * fxp, fym2 = fym * fym, fyp2 = fyp * fyp, fzm2 = fzm * fzm,
+              fzp2 = fzp * fzp;
+  // own cell, its points split over the group
+  if (cx >= 0 && cx < g.nx && cy >= 0 && cy < g.ny && cz >= 0 && cz < g.nz) {
+    const uint2 c = g.cells[((unsigned)cz * (unsigned)g.ny + (unsigned)cy) * (unsigned)g.nx + (unsigned)cx];
+    for (unsigned j = c.x + (unsigned)lg; j < c.y; j += G) nn_take(g.pts[j], j, q, bd, bi, bpos);
+  }
+  // neighbours: lane lg takes neighbours lg, lg + G, ... of the 26 (the
+  // centre skipped); a cell is skipped when its box lies beyond
+  // (margin + sqrt(best)).  The table entries are fetched first, then scanned.
+  const float t = margin + sqrtf(bd * 1.000001f + 1e-30f);
+  const float thr2 = t * t * 1.00001f;
+  constexpr int NK = (26 + G - 1) / G;
+  uint2 cc[NK];
+#pragma unroll
+  for (int k = 0; k < NK; ++k) {
+    const int idx = k * G + lg;
+    uint2 c = make_uint2(0u, 0u);
+    if (idx < 26) {
+      const int n = idx < 13 ? idx : idx + 1;
+      const int dx = n % 3 - 1, dy = (n / 3) % 3 - 1, dz = n / 9 - 1;
+      const int x = cx + dx, y = cy + dy, z = cz + dz;
+      const float b2 = (dx < 0 ? fxm2 : (dx > 0 ? fxp2 : 0.f)) + (dy < 0 ? fym2 : (dy > 0 ? fyp2 : 0.f)) +
+                       (dz < 0 ? fzm2 : (dz > 0 ? fzp2 : 0.f));
+      if (x >= 0 && x < g.nx && y >= 0 && y < g.ny && z >= 0 && z < g.nz && !(b2 > thr2))
+        c = g.cells[((unsigned)z * (unsigned)g.ny + (unsigned)y) * (unsigned)g.nx + (unsigned)x];
+    }
+    cc[k] = c;
+  }
+#pragma unroll
+  for (int k = 0; k < NK; ++k)
+    for (unsigned j = cc[k].x; j < cc[k].y; ++j) nn_take(g.pts[j], j, q, bd, bi, bpos);
+  group_best<G>(gmask, bd, bi, bpos);
+  if (bi == INT_MAX) {
+    bi = -1;
+    bpos = -1;
+    bd = __int_as_float(0x7f800000);
+  }
+}
+
+// Whether any point lies within sqrt(r2) of q (d^2 <= r2, finite), over the
+// 27 cells around q's cell (precondition: grid_near27_ok(g, r2)), G lanes
+// per query; the same answer as grid_nn1_group finding a neighbour.  The own
+// cell first, then the neighbours whose box is within reach; every lane stops
+// once the group has found one.
+template <int G>
+__device__ __forceinline__ bool grid_any_near(const GridView& g, float4 q, float r2, int lg, unsigned gmask) {
+  const int cx = q_cell(q.x, g.ox, g.inv_h), cy = q_cell(q.y, g.oy, g.inv_h),
+            cz = q_cell(q.z, g.oz, g.inv_h);
+  bool found = false;
+  if (cx >= 0 && cx < g.nx && cy >= 0 && cy < g.ny && cz >= 0 && cz < g.nz) {
+    const uint2 c = g.cells[((unsigned)cz * (unsigned)g.ny + (unsigned)cy) * (unsigned)g.nx + (unsigned)cx];
+    for (unsigned j = c.x + (unsigned)lg; j < c.y && !found; j += G) found = dist2_exact(q, g.pts[j]) <= r2;
+  }
+  if (__any_sync(gmask, found)) return true;
+  const float margin = search_margin(g, q, 1);
+  const float xl = g.ox + (float)cx * g.h, yl = g.oy + (float)cy * g.h, zl = g.oz + (float)cz * g.h;
+  const float fxm = fmaxf(q.x - xl, 0.f), fxp = fmaxf(xl + g.h - q.x, 0.f);
+  const float fym = fmaxf(q.y - yl, 0.f), fyp = fmaxf(yl + g.h - q.y, 0.f);
+  const float fzm = fmaxf(q.z - zl, 0.f), fzp = fmaxf(zl + g.h - q.z, 0.f);
+  const float t = margin + sqrtf(r2 * 1.000001f + 1e-30f);
+  const float thr2 = t * t * 1.00001f;
+  constexpr int NK = (26 + G - 1) / G;
+  uint2 cc[NK];
+#pragma unroll
+  for (int k = 0; k < NK; ++k) {
+    const int idx = k * G + lg;
+    uint2 c = make_uint2(0u, 0u);
+    if (idx < 26) {
+      const int n = idx < 13 ? idx : idx + 1;
+      const int dx = n % 3 - 1, dy = (n / 3) % 3 - 1, dz = n / 9 - 1;
+      const int x = cx + dx, y = cy + dy, z = cz + dz;
+      const float ex = dx < 0 ? fxm : (dx > 0 ? fxp : 0.f), ey = dy < 0 ? fym : (dy > 0 ? fyp : 0.f),
+                  ez = dz < 0 ? fzm : (dz > 0 ? fzp : 0.f);
+      if (x >= 0 && x < g.nx && y >= 0 && y < g.ny && z >= 0 && z < g.nz && !(ex * ex + ey * ey + ez * ez > thr2))
+        c = g.cells[((unsigned)z * (unsigned)g.ny + (unsigned)y) * (unsigned)g.nx + (unsigned)x];
+    }
+    cc[k] = c;
+  }
+#pragma unroll
+  for (int k = 0; k < NK; ++k)
+    for (unsigned j = cc[k].x; j < cc[k].y && !found; ++j) found = dist2_exact(q, g.pts[j]) <= r2;
+  return __any_sync(gmask, found);
+}
+
 // Exact K-NN (K compile-time), sorted by (d^2, index).  The K nearest by that
 // order are unique, so any k <= K of them form the exact k-NN.
 template <int K>

@@ -100,3 +100,25 @@ def test_icp_early_stop_criteria(ctx, rtr):
     assert abs(o["iterations"] - r["iterations"]) <= 2
     dt, dr = O.pose_error(r["pose"], o["pose"])
     assert dt < 1e-4 and dr < 1e-4
+
+
+@pytest.mark.parametrize("seed", [0, 3])
+def test_icp_near_cell_search_same_correspondences(ctx, rtr, seed):
+    """With a grid cell wider than the correspondence distance, every match
+    lies in the 27 cells around a query and the kernel takes the shorter
+    search (no rings).  Its correspondences are those of the ring search and
+    of the oracle, iteration by iteration."""
+    src, tgt, _ = rtr.config0_pair(seed)
+    for d in (0.02, 0.05):
+        ring, tp_r, tc_r = ctx.icp(_dev(src), _dev(tgt), 20, d, trace=True)
+        near, tp_n, tc_n = ctx.icp(_dev(src), _dev(tgt), 20, d, cell_size=1.5 * d, trace=True)
+        assert np.array_equal(tc_r.cpu().numpy(), tc_n.cpu().numpy())
+        # the source is sorted by target cell, so another cell size changes the
+        # order of the compensated sums: poses agree to rounding
+        np.testing.assert_allclose(tp_r.cpu().numpy(), tp_n.cpu().numpy(), rtol=0, atol=1e-9)
+        r = ctx.parse_icp_result(near)
+        poses = tp_n.cpu().numpy()[: r["iterations"] + 1]
+        ocorr, _, _ = O.icp_replay(src, tgt, d, poses)
+        corr = tc_n.cpu().numpy()[: r["iterations"]]
+        for k in range(r["iterations"]):
+            assert np.array_equal(corr[k], ocorr[k]), k
