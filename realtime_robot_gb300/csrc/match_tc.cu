@@ -159,29 +159,60 @@ __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::
 // rows, -|b|^2 / 2 (itself split) in database rows.
 __global__ void k_split_bf16(const float* __restrict__ x, int n_host, const int* d_n, int n_cap,
                              __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
-                             float* __restrict__ norm2, unsigned* __restrict__ max_bits, bool is_db) {
+                             float* __restrict__ norm2, unsigned* __restrict__ max_bits, bool is_db,
+                             unsigned char* __restrict__ zero_row) {
+  static_assert(TC_DIM % 4 == 0 && TC_KPAD == 96 * 4, "a row is 96 groups of four columns");
   const int n = d_n ? min(*d_n, n_cap) : n_host;
   const int lane = threadIdx.x & 31;
+  const bool v4 = (reinterpret_cast<uintptr_t>(x) & 15u) == 0;
   for (int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < n_cap; r += gridDim.x * (blockDim.x >> 5)) {
+    // lane takes column groups lane, lane + 32, lane + 64: four columns each,
+    // one 16-byte load and two 8-byte stores
     float ss = 0.f;
-    for (int k = lane; k < TC_KPAD; k += 32) {
-      if (k == TC_DIM) continue;  // written below
-      const float v = (r < n && k < TC_DIM) ? x[(size_t)r * TC_DIM + k] : 0.f;
-      const __nv_bfloat16 h = __float2bfloat16_rn(v);
-      const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
-      hi[(size_t)r * TC_KPAD + k] = h;
-      lo[(size_t)r * TC_KPAD + k] = l;
-      ss += v * v;
+    bool nz = false;
+    float4 vv[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int c4 = lane + 32 * k;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (r < n && c4 < TC_DIM / 4) {
+        const float* src = x + (size_t)r * TC_DIM + 4 * c4;
+        v = v4 ? __ldg(reinterpret_cast<const float4*>(src)) : make_float4(src[0], src[1], src[2], src[3]);
+      }
+      vv[k] = v;
+      nz |= v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f;
+      ss += v.x * v.x + v.y * v.y + v.z * v.z + v.w * v.w;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+    nz = __any_sync(0xffffffffu, nz);
+    // column TC_DIM carries the norm term: 1 in query rows, -|b|^2 / 2 in
+    // database rows (zero in padding rows)
+    const float tv = r < n ? (is_db ? -0.5f * ss : 1.f) : 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int c4 = lane + 32 * k;
+      float4 v = vv[k];
+      if (c4 == TC_DIM / 4) v.x = tv;
+      const float e[4] = {v.x, v.y, v.z, v.w};
+      __nv_bfloat16 h[4], l[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        h[j] = __float2bfloat16_rn(e[j]);
+        l[j] = __float2bfloat16_rn(e[j] - __bfloat162float(h[j]));
+      }
+      uint2 hp, lp;
+      hp.x = (unsigned)__bfloat16_as_ushort(h[0]) | ((unsigned)__bfloat16_as_ushort(h[1]) << 16);
+      hp.y = (unsigned)__bfloat16_as_ushort(h[2]) | ((unsigned)__bfloat16_as_ushort(h[3]) << 16);
+      lp.x = (unsigned)__bfloat16_as_ushort(l[0]) | ((unsigned)__bfloat16_as_ushort(l[1]) << 16);
+      lp.y = (unsigned)__bfloat16_as_ushort(l[2]) | ((unsigned)__bfloat16_as_ushort(l[3]) << 16);
+      reinterpret_cast<uint2*>(hi + (size_t)r * TC_KPAD)[c4] = hp;
+      reinterpret_cast<uint2*>(lo + (size_t)r * TC_KPAD)[c4] = lp;
+    }
     if (lane == 0) {
       norm2[r] = ss;
       if (max_bits && r < n) atomicMax(max_bits, __float_as_uint(ss));  // ss >= 0 (or NaN: stays largest)
-      const float v = r < n ? (is_db ? -0.5f * ss : 1.f) : 0.f;
-      const __nv_bfloat16 h = __float2bfloat16_rn(v);
-      hi[(size_t)r * TC_KPAD + TC_DIM] = h;
-      lo[(size_t)r * TC_KPAD + TC_DIM] = __float2bfloat16_rn(v - __bfloat162float(h));
+      if (zero_row) zero_row[r] = (r < n && !nz) ? 1 : 0;
     }
   }
 }
@@ -462,7 +493,8 @@ __global__ void __launch_bounds__(256) k_rerank(const float* __restrict__ q, int
                                                 unsigned long long* __restrict__ redo_best,
                                                 float* __restrict__ redo_thr,
                                                 const float* __restrict__ qn, const float* __restrict__ db_max,
-                                                const unsigned long long* __restrict__ zero_best) {
+                                                const unsigned long long* __restrict__ zero_best,
+                                                const unsigned char* __restrict__ qzero) {
   const int nq = d_nq ? min(*d_nq, nq_cap) : nq_host;
   const int lane = threadIdx.x & 31, sub = lane >> 3, l8 = lane & 7;
   const int warps = gridDim.x * (blockDim.x >> 5);
@@ -472,17 +504,18 @@ __global__ void __launch_bounds__(256) k_rerank(const float* __restrict__ q, int
     // an all-zero query ties (up to rounding) with every unit-norm row: its
     // answer is the same for every such query, the row of least exact
     // sequential |b|^2 (lowest index on ties), found once per call
-    bool nz = false;
-    if (valid)
-      for (int k = l8; k < TC_DIM; k += 8) nz |= q[(size_t)i * TC_DIM + k] != 0.f;
-#pragma unroll
-    for (int o = 4; o > 0; o >>= 1) nz |= __shfl_xor_sync(0xffffffffu, (int)nz, o) != 0;
-    const bool zq = valid && !nz;  // (no early exit: the shuffles below need every lane)
+    const bool zq = valid && qzero[i] != 0;  // (no early exit: the shuffles below need every lane)
     int c = valid && !zq ? cand_idx[(size_t)i * TC_TOP + l8] : -1;
     if (c >= ndb) c = -1;  // never read past the database, whatever the first pass left
+    // |d~ - d| <= err: a candidate whose d~ exceeds the smallest d~ (the
+    // first, the list is ascending) by more than 2 err has an exact distance
+    // above that candidate's, so it can neither win nor tie: its exact
+    // distance is not computed
+    const float err_q = valid ? TC_ERR * fmaxf(qn[i], *db_max) : 0.f;
+    const bool need = c >= 0 && cand_d[(size_t)i * TC_TOP + l8] <= cand_d[(size_t)i * TC_TOP] + 2.f * err_q;
     float d = __int_as_float(0x7f800000);
-    if (c >= 0) d = exact_d2<V4>(q + (size_t)i * TC_DIM, db + (size_t)c * TC_DIM);
-    int bi = c >= 0 ? c : 0x7fffffff;
+    if (need) d = exact_d2<V4>(q + (size_t)i * TC_DIM, db + (size_t)c * TC_DIM);
+    int bi = need ? c : 0x7fffffff;
     float bd = d;
 #pragma unroll
     for (int o = 4; o > 0; o >>= 1) {  // within the aligned group of 8 lanes
@@ -708,6 +741,7 @@ void match_tc_plan(ScratchPlan& p, int nq_cap, bool with_db, int ndb) {
   p.add<float>(bq);
   p.add<int>((size_t)bq * TC_BAND);
   p.add<int>(bq);
+  p.add<unsigned char>(nqp);
 }
 
 // Splits a descriptor database once (the model side keeps the result).
@@ -719,7 +753,7 @@ rtr_status match_tc_prepare_db(const float* db, int ndb, __nv_bfloat16* hi, __nv
   // norm2[ndb] receives the largest squared norm (scales the error bound)
   RTR_CUDA(cudaMemsetAsync(norm2 + ndb, 0, sizeof(float), st));
   k_split_bf16<<<blocks, 256, 0, st>>>(db, ndb, nullptr, ndb, hi, lo, norm2, reinterpret_cast<unsigned*>(norm2 + ndb),
-                                       true);
+                                       true, nullptr);
   RTR_LAUNCHED(1);
   RTR_CUDA(cudaGetLastError());
   return RTR_OK;
@@ -756,10 +790,14 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
   float* qn2 = s.take<float>(bq);
   int* band_idx = s.take<int>((size_t)bq * TC_BAND);
   int* band_n = s.take<int>(bq);
-  if (!band_n) return fail(RTR_ERR_CAPACITY, "match_tc: scratch");
+  unsigned char* qzero = s.take<unsigned char>(nqp);
+  if (!qzero) return fail(RTR_ERR_CAPACITY, "match_tc: scratch");
   int sb = (nqp + 7) / 8;
   if (sb > 152 * 16) sb = 152 * 16;
-  k_split_bf16<<<sb, 256, 0, st>>>(q, nq_cap, d_nq, nqp, qhi, qlo, qn, nullptr, false);
+  {
+    ProfScope pp(ctx, st, "match_split");
+    k_split_bf16<<<sb, 256, 0, st>>>(q, nq_cap, d_nq, nqp, qhi, qlo, qn, nullptr, false, qzero);
+  }
   CUtensorMap m_qh, m_ql, m_bh, m_bl, m_qh2, m_ql2;
   if (!make_map(&m_qh, qhi, nqp, TC_BM) || !make_map(&m_ql, qlo, nqp, TC_BM) || !make_map(&m_bh, db_hi, ndb, TC_BN) ||
       !make_map(&m_bl, db_lo, ndb, TC_BN) || !make_map(&m_qh2, hi2, bq, TC_BM) || !make_map(&m_ql2, lo2, bq, TC_BM))
@@ -784,12 +822,15 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
   // band pass over the uncertified queries: the GEMM again, listing every
   // row within the tie margin, then exact distances to those rows only
   TcArgs ab{bq, nredo, bq, ndb, qn2, band_idx, nullptr, ctx->d_status, redo_thr, band_n, tc_spin_limit(ctx)};
+  ProfScope pr(ctx, st, "match_rerank");
   if (v4)
     k_rerank<true><<<rb, 256, 0, st>>>(q, nq_cap, d_nq, nq_cap, db, ndb, cidx, cd, out_idx, out_d2, redo, nredo,
-                                       redo_best, redo_thr, qn, db_n2 + ndb, zero_best);
+                                       redo_best, redo_thr, qn, db_n2 + ndb, zero_best, qzero);
   else
     k_rerank<false><<<rb, 256, 0, st>>>(q, nq_cap, d_nq, nq_cap, db, ndb, cidx, cd, out_idx, out_d2, redo, nredo,
-                                        redo_best, redo_thr, qn, db_n2 + ndb, zero_best);
+                                        redo_best, redo_thr, qn, db_n2 + ndb, zero_best, qzero);
+  pr.end();
+  ProfScope pu(ctx, st, "match_uncertified");
   k_band_gather<<<(bq + 7) / 8, 256, 0, st>>>(reinterpret_cast<const uint4*>(qhi), reinterpret_cast<const uint4*>(qlo),
                                               qn, redo, nredo, bq, reinterpret_cast<uint4*>(hi2),
                                               reinterpret_cast<uint4*>(lo2), qn2);
