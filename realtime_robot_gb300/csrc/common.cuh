@@ -141,6 +141,16 @@ struct ProfScope {
   ~ProfScope() { end(); }
 };
 
+// A prepared descriptor database's FP32 side: the squared norms [ndb], their
+// maximum, then (8-byte aligned) the packed answer for an all-zero query.
+inline int db_norm_floats(int ndb) { return ((ndb + 2) & ~1) + 2; }
+__host__ __device__ inline unsigned long long* db_zero_key(float* n2, int ndb) {
+  return reinterpret_cast<unsigned long long*>(n2 + ((ndb + 2) & ~1));
+}
+__host__ __device__ inline const unsigned long long* db_zero_key(const float* n2, int ndb) {
+  return reinterpret_cast<const unsigned long long*>(n2 + ((ndb + 2) & ~1));
+}
+
 }  // namespace rtr
 
 // ---------------------------------------------------------------------------

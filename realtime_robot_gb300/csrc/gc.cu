@@ -1056,6 +1056,7 @@ static rtr_status gc_launch(rtr_context* ctx, Scratch& s, const float* d_model_k
     return fail(RTR_ERR_CAPACITY, "rtr_gc_group: %d correspondences exceed the supported %d", C,
                 (int)(GC_MAX_DYN_SMEM * 8));
   const int nb = (C + 255) / 256 > 152 * 8 ? 152 * 8 : (C + 255) / 256;
+  ProfScope pso(ctx, st, "gc_sort");
   k_gc_keys<<<nb, 256, 0, st>>>(d_corr_d, C, d_C, b.k0);
   uint32_t *ks, *vs;
   radix_sort_pairs(b.k0, b.v0, b.k1, b.v1, b.hist, C, C, d_C, 32, true, st, &ks, &vs);
@@ -1068,7 +1069,9 @@ static rtr_status gc_launch(rtr_context* ctx, Scratch& s, const float* d_model_k
   RTR_CUDA(cudaMemsetAsync(b.arrive, 0, sizeof(unsigned), st));
   GcDev g{b.pm, b.ps, C, d_C, gc_size, b.taken, b.set_size, b.set_mem, gc_set_stride(C)};
   bbox_build(b.mbox, b.pm, C, d_C, st);
+  pso.end();
   // the coarse grid over the scene endpoints (seed-test pruning)
+  ProfScope pgr(ctx, st, "gc_grid");
   bbox_build(&b.sg->m, b.ps, C, d_C, st);
   k_gcg_setup<<<1, 32, 0, st>>>(b.sg, b.mbox, gc_size, C, d_C);
   k_gcg_keys<<<nb, 256, 0, st>>>(b.ps, C, d_C, b.sg, b.gk0);
@@ -1076,6 +1079,7 @@ static rtr_status gc_launch(rtr_context* ctx, Scratch& s, const float* d_model_k
   radix_sort_pairs(b.gk0, b.gv0, b.gk1, b.gv1, b.hist, C, C, d_C, 16, true, st, &gks, &gvs);
   k_gcg_gather<<<nb, 256, 0, st>>>(b.ps, b.pm, gvs, C, d_C, b.cpts, b.cpm, b.cbox);
   RTR_LAUNCHED(3);
+  pgr.end();
   GcCoop c{b.misc, b.arrive, b.computed, b.members, b.sizes, gc_thresh, max_clusters,
            ctx->wait_budget_cycles, ctx->d_status, b.mbox, b.need, b.mask,
            gc_win(C, ctx->tune_gc_window > 0 ? ctx->tune_gc_window : 0), gc_win(C, GC_WIN_MAX), gc_nwp(C),
@@ -1125,6 +1129,7 @@ rtr_status gc_group_async(rtr_context* ctx, Scratch& s, const float* d_model_kp,
   uint32_t* order = nullptr;
   RTR_TRY(gc_launch(ctx, s, d_model_kp, d_scene_kp, d_corr_m, d_corr_s, d_corr_d, C_cap > 0 ? C_cap : 1, d_C,
                     gc_size, gc_thresh, max_clusters, st, &b, &order));
+  ProfScope pp(ctx, st, "gc_poses");
   k_gc_post<<<1, 32, 0, st>>>(b.misc, max_clusters, d_ncl, ctx->d_status, ctx->d_status + 16);
   k_gc_poses<<<(max_clusters + 3) / 4, 128, 0, st>>>(b.pm, b.ps, b.members, b.sizes, max_clusters, d_ncl,
                                                       gc_set_stride(C_cap > 0 ? C_cap : 1), b.poses);

@@ -31,37 +31,64 @@ __global__ void __launch_bounds__(RS_BLOCK) k_rs_hist(const uint32_t* __restrict
   for (int d = threadIdx.x; d < RS_RADIX; d += RS_BLOCK) hist[d * nb + blockIdx.x] = cnt[d];
 }
 
-// In-place exclusive scan of `total` entries by one block of 1024 threads.
+// In-place exclusive scan of `total` entries by one block of 1024 threads,
+// in chunks of 8192 entries staged through shared memory with coalesced
+// loads and stores (eight per thread), a carry between chunks.
 __global__ void __launch_bounds__(1024) k_rs_scan(uint32_t* __restrict__ h, int total) {
+  constexpr int PER = 8, CH = 1024 * PER;
+  __shared__ uint32_t sh[CH];
   __shared__ uint32_t wsum[32];
-  const int per = (total + 1023) / 1024;
-  const int beg = min(total, (int)threadIdx.x * per), end = min(total, beg + per);
-  uint32_t s = 0;
-  for (int i = beg; i < end; ++i) s += h[i];
+  __shared__ uint32_t s_carry;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t incl = s;
+  if (threadIdx.x == 0) s_carry = 0;
+  for (int c0 = 0; c0 < total; c0 += CH) {
+    const int cn = min(CH, total - c0);
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += t;
-  }
-  if (lane == 31) wsum[warp] = incl;
-  __syncthreads();
-  if (warp == 0) {
-    uint32_t w = wsum[lane], wi = w;
+    for (int k = 0; k < PER; ++k) {
+      const int i = k * 1024 + threadIdx.x;
+      sh[i] = i < cn ? h[c0 + i] : 0u;
+    }
+    __syncthreads();
+    // thread t owns sh[t*PER .. t*PER+PER)
+    uint32_t v[PER], s = 0;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      v[k] = sh[threadIdx.x * PER + k];
+      s += v[k];
+    }
+    uint32_t incl = s;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      uint32_t t = __shfl_up_sync(0xffffffffu, wi, o);
-      if (lane >= o) wi += t;
+      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
     }
-    wsum[lane] = wi - w;
-  }
-  __syncthreads();
-  uint32_t run = wsum[warp] + incl - s;
-  for (int i = beg; i < end; ++i) {
-    uint32_t v = h[i];
-    h[i] = run;
-    run += v;
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+      const uint32_t w = wsum[lane];
+      uint32_t wi = w;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, wi, o);
+        if (lane >= o) wi += t;
+      }
+      wsum[lane] = wi - w;
+    }
+    __syncthreads();
+    uint32_t run = s_carry + wsum[warp] + incl - s;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      sh[threadIdx.x * PER + k] = run;
+      run += v[k];
+    }
+    __syncthreads();
+    if (threadIdx.x == 1023) s_carry = run;  // the last thread ends with the chunk's total
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const int i = k * 1024 + threadIdx.x;
+      if (i < cn) h[c0 + i] = sh[i];
+    }
+    __syncthreads();
   }
 }
 
@@ -164,10 +191,12 @@ __global__ void k_bbox_init(GridMeta* m) {
   }
 }
 
+// Launched with 256 threads and at most bbox_blocks(n) blocks.
 __global__ void __launch_bounds__(256) k_bbox(const float4* __restrict__ pts, int n_host,
                                               const int* d_n, GridMeta* m) {
   const int n = count_of(n_host, d_n);
   unsigned mn[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, mx[3] = {0u, 0u, 0u};
+#pragma unroll 4
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     float4 p = pts[i];
     // a point with a non-finite coordinate does not size the grid: it sits in
@@ -188,12 +217,27 @@ __global__ void __launch_bounds__(256) k_bbox(const float4* __restrict__ pts, in
       mx[a] = max(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
     }
   }
+  // the block's extremes, then six atomics per block (atomics from every
+  // warp on the same six words serialise: 39 us for 1216 blocks)
+  __shared__ unsigned s_mn[3][8], s_mx[3][8];
+  const int warp = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0) {
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-      atomicMin(&m->bmin[a], mn[a]);
-      atomicMax(&m->bmax[a], mx[a]);
+      s_mn[a][warp] = mn[a];
+      s_mx[a][warp] = mx[a];
     }
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    const int a = threadIdx.x;
+    unsigned lo = s_mn[a][0], hi = s_mx[a][0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+      lo = min(lo, s_mn[a][w]);
+      hi = max(hi, s_mx[a][w]);
+    }
+    atomicMin(&m->bmin[a], lo);
+    atomicMax(&m->bmax[a], hi);
   }
 }
 
@@ -332,12 +376,19 @@ static int grid_blocks(int n) {
   if (b > 152 * 8) b = 152 * 8;
   return b;
 }
+// Blocks of a reduction to a few words: two per SM at most.
+static int bbox_blocks(int n) {
+  int b = (n + 255) / 256;
+  if (b < 1) b = 1;
+  if (b > 152 * 2) b = 152 * 2;
+  return b;
+}
 
 void bbox_build(GridMeta* m, const float4* pts, int n, cudaStream_t st) { bbox_build(m, pts, n, nullptr, st); }
 
 void bbox_build(GridMeta* m, const float4* pts, int n_cap, const int* d_n, cudaStream_t st) {
   k_bbox_init<<<1, 32, 0, st>>>(m);
-  k_bbox<<<grid_blocks(n_cap), 256, 0, st>>>(pts, n_cap, d_n, m);
+  k_bbox<<<bbox_blocks(n_cap), 256, 0, st>>>(pts, n_cap, d_n, m);
   RTR_LAUNCHED(2);
 }
 
@@ -345,7 +396,7 @@ void grid_build(const GridBufs& b, const float4* pts, int n_host, const int* d_n
                 cudaStream_t st) {
   const int nb = grid_blocks(b.n_cap);
   k_bbox_init<<<1, 32, 0, st>>>(b.meta);
-  k_bbox<<<nb, 256, 0, st>>>(pts, n_host, d_n, b.meta);
+  k_bbox<<<bbox_blocks(b.n_cap), 256, 0, st>>>(pts, n_host, d_n, b.meta);
   k_grid_setup<<<1, 1, 0, st>>>(b.meta, h_req, b.cell_cap, n_host, d_n);
   k_grid_keys<<<nb, 256, 0, st>>>(pts, n_host, d_n, b.meta, b.k0);
   int bits = 1;

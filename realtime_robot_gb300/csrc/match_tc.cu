@@ -481,9 +481,9 @@ __device__ __forceinline__ float exact_d2(const float* __restrict__ x, const flo
   return acc;
 }
 
-// Exact FP32 re-rank of the 8 candidates and certification; four queries per
-// warp, one lane per candidate.  Uncertified queries go to the redo list with
-// their running minimum reset.
+// Exact FP32 re-rank of the candidates that can still win and
+// certification; four queries per warp, one lane per candidate.  Uncertified
+// queries go to the redo list with their running minimum reset.
 template <bool V4>
 __global__ void __launch_bounds__(256) k_rerank(const float* __restrict__ q, int nq_host, const int* d_nq, int nq_cap,
                                                 const float* __restrict__ db, int ndb,
@@ -501,9 +501,6 @@ __global__ void __launch_bounds__(256) k_rerank(const float* __restrict__ q, int
   for (int base = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 4; base < nq; base += warps * 4) {
     const int i = base + sub;
     const bool valid = i < nq;
-    // an all-zero query ties (up to rounding) with every unit-norm row: its
-    // answer is the same for every such query, the row of least exact
-    // sequential |b|^2 (lowest index on ties), found once per call
     const bool zq = valid && qzero[i] != 0;  // (no early exit: the shuffles below need every lane)
     int c = valid && !zq ? cand_idx[(size_t)i * TC_TOP + l8] : -1;
     if (c >= ndb) c = -1;  // never read past the database, whatever the first pass left
@@ -527,6 +524,9 @@ __global__ void __launch_bounds__(256) k_rerank(const float* __restrict__ q, int
       }
     }
     if (zq && l8 == 0) {
+      // an all-zero query ties (up to rounding) with every unit-norm row: its
+      // answer is the database's, the row of least exact sequential |b|^2
+      // (lowest index on ties), found when the database was split
       const unsigned long long key = *zero_best;
       out_idx[i] = key == ~0ull ? -1 : (int)(unsigned)(key & 0xffffffffull);
       if (out_d2) out_d2[i] = key == ~0ull ? __int_as_float(0x7f800000) : __uint_as_float((unsigned)(key >> 32));
@@ -555,7 +555,8 @@ __global__ void __launch_bounds__(256) k_rerank(const float* __restrict__ q, int
 // The answer for an all-zero query: min over rows of the exact sequential
 // sum of (0 - b_k)^2 = b_k^2 (each operation rounded, as exact_d2 with a
 // zero row), packed (d^2 bits, index) so that atomicMin keeps the lowest
-// index on ties.  Rows with an infinite or NaN sum never win.
+// index on ties.  Rows with an infinite or NaN sum never win.  It depends on
+// the database only: computed when the database is split.
 __global__ void k_zero_best(const float* __restrict__ db, int ndb, unsigned long long* __restrict__ best) {
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < ndb; j += gridDim.x * blockDim.x) {
     const float* y = db + (size_t)j * TC_DIM;
@@ -569,8 +570,6 @@ __global__ void k_zero_best(const float* __restrict__ db, int ndb, unsigned long
   }
 }
 
-// Band pass, step 1: the first TC_BAND_Q uncertified queries' split rows and
-// norms, gathered into compact arrays (warp per row, 16-byte copies).
 __global__ void k_band_gather(const uint4* __restrict__ qhi, const uint4* __restrict__ qlo,
                               const float* __restrict__ qn, const int* __restrict__ redo,
                               const int* __restrict__ n_redo, int cap, uint4* __restrict__ hi2, uint4* __restrict__ lo2,
@@ -724,14 +723,13 @@ void match_tc_plan(ScratchPlan& p, int nq_cap, bool with_db, int ndb) {
   if (with_db) {
     p.add<__nv_bfloat16>((size_t)ndb * TC_KPAD);
     p.add<__nv_bfloat16>((size_t)ndb * TC_KPAD);
-    p.add<float>(ndb + 1);
+    p.add<float>(db_norm_floats(ndb));
   }
   p.add<int>((size_t)nqp * TC_TOP);
   p.add<float>((size_t)nqp * TC_TOP);
   p.add<int>(nqp);
   p.add<unsigned long long>(nqp);
   p.add<int>(4);
-  p.add<unsigned long long>(1);
   // band pass
   const int bq = band_rows(nqp);
   p.add<float>(nqp);
@@ -750,11 +748,15 @@ rtr_status match_tc_prepare_db(const float* db, int ndb, __nv_bfloat16* hi, __nv
   int blocks = (ndb + 7) / 8;
   if (blocks > 152 * 16) blocks = 152 * 16;
   if (blocks < 1) blocks = 1;
-  // norm2[ndb] receives the largest squared norm (scales the error bound)
+  // norm2[ndb] receives the largest squared norm (scales the error bound),
+  // db_zero_key the answer for an all-zero query
   RTR_CUDA(cudaMemsetAsync(norm2 + ndb, 0, sizeof(float), st));
+  RTR_CUDA(cudaMemsetAsync(db_zero_key(norm2, ndb), 0xff, sizeof(unsigned long long), st));
   k_split_bf16<<<blocks, 256, 0, st>>>(db, ndb, nullptr, ndb, hi, lo, norm2, reinterpret_cast<unsigned*>(norm2 + ndb),
                                        true, nullptr);
-  RTR_LAUNCHED(1);
+  const int zb = (ndb + 255) / 256 < 152 * 4 ? (ndb + 255) / 256 : 152 * 4;
+  k_zero_best<<<zb > 0 ? zb : 1, 256, 0, st>>>(db, ndb, db_zero_key(norm2, ndb));
+  RTR_LAUNCHED(2);
   RTR_CUDA(cudaGetLastError());
   return RTR_OK;
 }
@@ -769,7 +771,7 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
   if (!db_hi) {
     __nv_bfloat16* h = s.take<__nv_bfloat16>((size_t)ndb * TC_KPAD);
     __nv_bfloat16* l = s.take<__nv_bfloat16>((size_t)ndb * TC_KPAD);
-    float* n2 = s.take<float>(ndb + 1);
+    float* n2 = s.take<float>(db_norm_floats(ndb));
     if (!n2) return fail(RTR_ERR_CAPACITY, "match_tc: scratch");
     RTR_TRY(match_tc_prepare_db(db, ndb, h, l, n2, st));
     db_hi = h;
@@ -781,7 +783,6 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
   int* redo = s.take<int>(nqp);
   unsigned long long* redo_best = s.take<unsigned long long>(nqp);
   int* nredo = s.take<int>(4);  // [0] uncertified, [1] left to the full scan
-  unsigned long long* zero_best = s.take<unsigned long long>(1);
   const int bq = band_rows(nqp);
   float* redo_thr = s.take<float>(nqp);
   int* full = s.take<int>(nqp);
@@ -812,8 +813,6 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
     k_match_tc<false><<<nqp / TC_BM, TC_THREADS, smem, st>>>(m_qh, m_ql, m_bh, m_bl, a);
   }
   RTR_CUDA(cudaMemsetAsync(nredo, 0, 2 * sizeof(int), st));
-  RTR_CUDA(cudaMemsetAsync(zero_best, 0xff, sizeof(unsigned long long), st));
-  k_zero_best<<<(ndb + 255) / 256 < 152 * 4 ? (ndb + 255) / 256 : 152 * 4, 256, 0, st>>>(db, ndb, zero_best);
   int rb = (nq_cap + 31) / 32;
   if (rb > 152 * 16) rb = 152 * 16;
   int wb = (nqp + 7) / 8;  // warp per uncertified query
@@ -825,10 +824,10 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
   ProfScope pr(ctx, st, "match_rerank");
   if (v4)
     k_rerank<true><<<rb, 256, 0, st>>>(q, nq_cap, d_nq, nq_cap, db, ndb, cidx, cd, out_idx, out_d2, redo, nredo,
-                                       redo_best, redo_thr, qn, db_n2 + ndb, zero_best, qzero);
+                                       redo_best, redo_thr, qn, db_n2 + ndb, db_zero_key(db_n2, ndb), qzero);
   else
     k_rerank<false><<<rb, 256, 0, st>>>(q, nq_cap, d_nq, nq_cap, db, ndb, cidx, cd, out_idx, out_d2, redo, nredo,
-                                        redo_best, redo_thr, qn, db_n2 + ndb, zero_best, qzero);
+                                        redo_best, redo_thr, qn, db_n2 + ndb, db_zero_key(db_n2, ndb), qzero);
   pr.end();
   ProfScope pu(ctx, st, "match_uncertified");
   k_band_gather<<<(bq + 7) / 8, 256, 0, st>>>(reinterpret_cast<const uint4*>(qhi), reinterpret_cast<const uint4*>(qlo),

@@ -327,7 +327,7 @@ struct rtr_model {
   GridMeta* vox_meta = nullptr;  // bbox of the voxel cloud (ICP centring)
   __nv_bfloat16* db_hi = nullptr;  // [n_kp][384] descriptor split for the tensor cores
   __nv_bfloat16* db_lo = nullptr;
-  float* db_n2 = nullptr;          // [n_kp + 1] squared norms, then their maximum
+  float* db_n2 = nullptr;          // [db_norm_floats(n_kp)] squared norms, their maximum, the all-zero answer
 };
 
 extern "C" {
@@ -423,7 +423,7 @@ rtr_status rtr_model_create(rtr_context* ctx, const float* d_pts, int n, const r
   RTR_LAUNCHED(1);
   if (cudaMalloc(&m->db_hi, match_tc_bf16_bytes(K)) != cudaSuccess ||
       cudaMalloc(&m->db_lo, match_tc_bf16_bytes(K)) != cudaSuccess ||
-      cudaMalloc(&m->db_n2, (size_t)(K + 1) * sizeof(float)) != cudaSuccess) {
+      cudaMalloc(&m->db_n2, (size_t)db_norm_floats(K) * sizeof(float)) != cudaSuccess) {
     cudaGetLastError();
     return cleanup(fail(RTR_ERR_OOM, "rtr_model_create: tensor-core database"));
   }

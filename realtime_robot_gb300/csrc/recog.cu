@@ -50,6 +50,7 @@ __global__ void __launch_bounds__(256) k_vox_bounds(const float4* __restrict__ p
   const int n = cnt_of(n_host, d_n);
   int lo[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, hi[3] = {(int)0x80000000, (int)0x80000000, (int)0x80000000};
   int err = 0;
+#pragma unroll 4
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float4 p = pts[i];
     if (!finite3(p)) continue;
@@ -68,13 +69,29 @@ __global__ void __launch_bounds__(256) k_vox_bounds(const float4* __restrict__ p
       hi[a] = max(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
     }
   err = __any_sync(0xffffffffu, err);
+  // the block's extremes, then a few atomics per block (not per warp)
+  __shared__ int s_lo[3][8], s_hi[3][8], s_err[8];
+  const int warp = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0) {
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-      atomicMin(&m->lo[a], lo[a]);
-      atomicMax(&m->hi[a], hi[a]);
+      s_lo[a][warp] = lo[a];
+      s_hi[a][warp] = hi[a];
     }
-    if (err) atomicExch(&m->error, 1);
+    s_err[warp] = err;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    const int a = threadIdx.x;
+    int l = s_lo[a][0], h = s_hi[a][0], e = s_err[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+      l = min(l, s_lo[a][w]);
+      h = max(h, s_hi[a][w]);
+      e |= s_err[w];
+    }
+    atomicMin(&m->lo[a], l);
+    atomicMax(&m->hi[a], h);
+    if (a == 0 && e) atomicExch(&m->error, 1);
   }
 }
 
@@ -171,7 +188,7 @@ bool voxseg_take(Scratch& s, int n_cap, VoxSeg* v) {
 void voxseg_build(VoxSeg& v, const float4* pts, int n_host, const int* d_n, float inv, cudaStream_t st) {
   const int nb = blocks_for(v.n_cap);
   k_vox_init<<<1, 32, 0, st>>>(v.meta);
-  k_vox_bounds<<<nb, 256, 0, st>>>(pts, n_host, d_n, inv, v.meta);
+  k_vox_bounds<<<nb < 152 * 2 ? nb : 152 * 2, 256, 0, st>>>(pts, n_host, d_n, inv, v.meta);  // block-reduced
   k_vox_setup<<<1, 1, 0, st>>>(v.meta, n_host, d_n);
   k_vox_keys<<<nb, 256, 0, st>>>(pts, n_host, d_n, inv, v.meta, v.k0);
   uint32_t *ks, *vs;
