@@ -372,20 +372,16 @@ int icp_max_blocks(rtr_context* ctx) {
 }
 
 // Lanes per source point: the tuning override when set, else the most lanes
-// (8, 4, 2) with which the launch needs at most max_passes passes over its
-// points: four for the ring search, eight for the 27-cell search (near:
-// every problem's grid cell is wider than its correspondence distance).
-// Measured on GB300: a 20k-point ICP (ring search) is fastest at 8, two
-// passes; sixteen 9.2k-point refinements on the ring search at 2, 3.8 passes
-// (2.35 ms against 2.48 at 4); the same on the 27-cell search at 4, 7.6
-// passes (1.63 ms against 1.90 at 2 and 1.78 at 8).
-int icp_pick_group(const rtr_context* ctx, long long total_pts, int blocks, bool near) {
+// (8, 4, 2) with which the launch needs at most four passes over its points
+// (measured on GB300: a 20k-point ICP on the ring search is fastest at 8, two
+// passes; sixteen 9.2k-point refinements on the 27-cell search at 2, 3.8
+// passes: 1.40 ms against 1.48 at 4 and 1.75 at 8).
+int icp_pick_group(const rtr_context* ctx, long long total_pts, int blocks) {
   const int t = ctx->tune_icp_group;
   if (t == 2 || t == 4 || t == 8) return t;
   const long long lanes = (long long)blocks * ICP_THREADS;
-  const long long max_passes = near ? 8 : 4;
-  if (total_pts * 8 <= max_passes * lanes) return 8;
-  return total_pts * 4 <= max_passes * lanes ? 4 : 2;
+  if (total_pts * 8 <= 4 * lanes) return 8;
+  return total_pts * 4 <= 4 * lanes ? 4 : 2;
 }
 
 static rtr_status launch_icp(int G, const IcpDev* d_probs, const int* d_blk2prob, int blocks, cudaStream_t st) {
@@ -445,7 +441,7 @@ void icp_multi_plan(ScratchPlan& p, int n_probs, int max_blocks) {
   p.add<unsigned>((size_t)n_probs * 2);
 }
 
-rtr_status icp_multi(rtr_context* ctx, Scratch& s, std::vector<IcpSpec>& specs, cudaStream_t st, bool near) {
+rtr_status icp_multi(rtr_context* ctx, Scratch& s, std::vector<IcpSpec>& specs, cudaStream_t st) {
   const int M = (int)specs.size();
   if (M == 0) return RTR_OK;
   const int maxb = icp_max_blocks(ctx);
@@ -508,7 +504,7 @@ rtr_status icp_multi(rtr_context* ctx, Scratch& s, std::vector<IcpSpec>& specs, 
   RTR_CUDA(cudaGetLastError());
   long long total = 0;
   for (int i = 0; i < M; ++i) total += specs[i].dev.n_src;
-  return launch_icp(icp_pick_group(ctx, total, used, near), d_probs, d_b2p, used, st);
+  return launch_icp(icp_pick_group(ctx, total, used), d_probs, d_b2p, used, st);
 }
 
 }  // namespace rtr

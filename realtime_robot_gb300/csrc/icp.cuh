@@ -43,13 +43,9 @@ struct IcpSpec {
 };
 
 int icp_max_blocks(rtr_context* ctx);
-int icp_pick_group(const rtr_context* ctx, long long total_pts, int blocks, bool near = false);
+int icp_pick_group(const rtr_context* ctx, long long total_pts, int blocks);
 void icp_multi_plan(ScratchPlan& p, int n_probs, int max_blocks);
 // Runs every problem; specs are completed (blocks, state buffers) in place.
-// near: every problem's target grid has a cell edge of at least 1.01 x its
-// correspondence distance (the kernel then takes the 27-cell search; the
-// flag only steers the lanes-per-point choice).
-rtr_status icp_multi(rtr_context* ctx, Scratch& s, std::vector<IcpSpec>& specs, cudaStream_t st,
-                     bool near = false);
+rtr_status icp_multi(rtr_context* ctx, Scratch& s, std::vector<IcpSpec>& specs, cudaStream_t st);
 
 }  // namespace rtr

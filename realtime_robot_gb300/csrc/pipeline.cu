@@ -779,10 +779,7 @@ static rtr_status model_stages(rtr_context* ctx, const Scratch& stage, const Sce
       d.slot = k;
       specs[k].init_dev = b.init + 16 * k;
     }
-    // the scene grid's cell (1.5 x the ICP distance unless tuned) against the
-    // correspondence distance: the 27-cell search applies
-    const float cell = ctx->tune_scene_grid_mm > 0 ? 1e-3f * (float)ctx->tune_scene_grid_mm : 1.5f * q->icp_max_dist;
-    RTR_TRY(icp_multi(ctx, t, specs, st, cell >= 1.01f * q->icp_max_dist));
+    RTR_TRY(icp_multi(ctx, t, specs, st));
   }
   {
     ProfScope ps(ctx, st, "final_score");

@@ -298,59 +298,93 @@ __device__ __forceinline__ bool grid_near27_ok(const GridView& g, float r2max) {
   return r2max >= 0.f && isfinite(r) && g.h >= 1.01f * r && g.nx <= 4096 && g.ny <= 4096 && g.nz <= 4096;
 }
 
+// Offsets (-1, 0, +1 as bits 0, 1, 2) along one axis that stay in the grid
+// (0 <= c + d < n) and, for d != 0, whose face lies within reach (squared
+// face distance <= thr2).
+__device__ __forceinline__ unsigned near_axis_mask(int c, int n, float fm2, float fp2, float thr2) {
+  unsigned m = 0u;
+  if (c - 1 >= 0 && c - 1 < n && !(fm2 > thr2)) m |= 1u;
+  if (c >= 0 && c < n) m |= 2u;
+  if (c + 1 >= 0 && c + 1 < n && !(fp2 > thr2)) m |= 4u;
+  return m;
+}
+// Offset of the k-th set bit (k < popc(m)) of a 3-bit axis mask.
+__device__ __forceinline__ int near_axis_pick(unsigned m, int k) {
+  const int b0 = (int)(m & 1u), b1 = (int)((m >> 1) & 1u);
+  return k < b0 ? -1 : (k < b0 + b1 ? 0 : 1);
+}
+
+// The query's position relative to its cell: squared distances to the six
+// faces (clamped at 0; underestimates under rounding).
+struct NearCell {
+  int cx, cy, cz;
+  float xm2, xp2, ym2, yp2, zm2, zp2;
+};
+__device__ __forceinline__ NearCell near_cell(const GridView& g, float4 q) {
+  NearCell c;
+  c.cx = q_cell(q.x, g.ox, g.inv_h);
+  c.cy = q_cell(q.y, g.oy, g.inv_h);
+  c.cz = q_cell(q.z, g.oz, g.inv_h);
+  const float xl = g.ox + (float)c.cx * g.h, yl = g.oy + (float)c.cy * g.h, zl = g.oz + (float)c.cz * g.h;
+  const float fxm = fmaxf(q.x - xl, 0.f), fxp = fmaxf(xl + g.h - q.x, 0.f);
+  const float fym = fmaxf(q.y - yl, 0.f), fyp = fmaxf(yl + g.h - q.y, 0.f);
+  const float fzm = fmaxf(q.z - zl, 0.f), fzp = fmaxf(zl + g.h - q.z, 0.f);
+  c.xm2 = fxm * fxm;
+  c.xp2 = fxp * fxp;
+  c.ym2 = fym * fym;
+  c.yp2 = fyp * fyp;
+  c.zm2 = fzm * fzm;
+  c.zp2 = fzp * fzp;
+  return c;
+}
+
+// The neighbour cells a query must visit: every (dx, dy, dz) != 0 from the
+// per-axis masks whose box is within reach; entry k (k = lg, lg + G, ...) of
+// that list for lane lg.  thr2 must be the same in every lane of the group
+// (the lists then agree).  Calls body(x, y, z) for each of the lane's cells.
+template <int G, typename F>
+__device__ __forceinline__ void near_neighbours(const GridView& g, const NearCell& c, float thr2, int lg, F body) {
+  const unsigned mx = near_axis_mask(c.cx, g.nx, c.xm2, c.xp2, thr2);
+  const unsigned my = near_axis_mask(c.cy, g.ny, c.ym2, c.yp2, thr2);
+  const unsigned mz = near_axis_mask(c.cz, g.nz, c.zm2, c.zp2, thr2);
+  const int nxo = __popc(mx), nyo = __popc(my), nzo = __popc(mz);
+  const int total = nxo * nyo * nzo;
+  for (int k = lg; k < total; k += G) {
+    const int ix = k % nxo, iy = (k / nxo) % nyo, iz = k / (nxo * nyo);
+    const int dx = near_axis_pick(mx, ix), dy = near_axis_pick(my, iy), dz = near_axis_pick(mz, iz);
+    if ((dx | dy | dz) == 0) continue;  // the own cell
+    const float b2 = (dx < 0 ? c.xm2 : (dx > 0 ? c.xp2 : 0.f)) + (dy < 0 ? c.ym2 : (dy > 0 ? c.yp2 : 0.f)) +
+                     (dz < 0 ? c.zm2 : (dz > 0 ? c.zp2 : 0.f));
+    if (b2 > thr2) continue;  // an edge or corner cell beyond reach
+    body(c.cx + dx, c.cy + dy, c.cz + dz);
+  }
+}
+
 // Exact 1-NN with d^2 <= r2max over the 27 cells around the query's cell
 // (precondition: grid_near27_ok), G lanes per query as grid_nn1_group; same
-// result.  The query's own cell is scanned first; a neighbour is fetched only
-// when its box, measured through the query's distances to its own cell's
-// faces (an underestimate), is within the lane's current best plus the
-// rounding margin.  No ring bookkeeping, no division, no square root per
-// cell.
+// result.  The query's own cell is scanned first and the group agrees on its
+// best; then only the neighbours whose box, measured through the query's
+// distances to its own cell's faces (an underestimate), is within that best
+// plus the rounding margin are fetched, spread over the group.  No ring
+// bookkeeping and no square root per cell.
 template <int G>
 __device__ __forceinline__ void grid_nn1_near(const GridView& g, float4 q, float r2max, int lg, unsigned gmask,
                                               float& bd, int& bi, int& bpos) {
   bd = r2max;
   bi = INT_MAX;
   bpos = -1;
-  const int cx = q_cell(q.x, g.ox, g.inv_h), cy = q_cell(q.y, g.oy, g.inv_h),
-            cz = q_cell(q.z, g.oz, g.inv_h);
-  const float margin = search_margin(g, q, 1);
-  // distances to the own cell's lower and upper faces (clamped at 0)
-  const float xl = g.ox + (float)cx * g.h, yl = g.oy + (float)cy * g.h, zl = g.oz + (float)cz * g.h;
-  const float fxm = fmaxf(q.x - xl, 0.f), fxp = fmaxf(xl + g.h - q.x, 0.f);
-  const float fym = fmaxf(q.y - yl, 0.f), fyp = fmaxf(yl + g.h - q.y, 0.f);
-  const float fzm = fmaxf(q.z - zl, 0.f), fzp = fmaxf(zl + g.h - q.z, 0.f);
-  const float fxm2 = fxm * fxm, fxp2 = fxp * fxp, fym2 = fym * fym, fyp2 = fyp * fyp, fzm2 = fzm * fzm,
-              fzp2 = fzp * fzp;
-  // own cell, its points split over the group
-  if (cx >= 0 && cx < g.nx && cy >= 0 && cy < g.ny && cz >= 0 && cz < g.nz) {
-    const uint2 c = g.cells[((unsigned)cz * (unsigned)g.ny + (unsigned)cy) * (unsigned)g.nx + (unsigned)cx];
-    for (unsigned j = c.x + (unsigned)lg; j < c.y; j += G) nn_take(g.pts[j], j, q, bd, bi, bpos);
+  const NearCell c = near_cell(g, q);
+  if (c.cx >= 0 && c.cx < g.nx && c.cy >= 0 && c.cy < g.ny && c.cz >= 0 && c.cz < g.nz) {
+    const uint2 e = g.cells[((unsigned)c.cz * (unsigned)g.ny + (unsigned)c.cy) * (unsigned)g.nx + (unsigned)c.cx];
+    for (unsigned j = e.x + (unsigned)lg; j < e.y; j += G) nn_take(g.pts[j], j, q, bd, bi, bpos);
   }
-  // neighbours: lane lg takes neighbours lg, lg + G, ... of the 26 (the
-  // centre skipped); a cell is skipped when its box lies beyond
-  // (margin + sqrt(best)).  The table entries are fetched first, then scanned.
-  const float t = margin + sqrtf(bd * 1.000001f + 1e-30f);
+  group_best<G>(gmask, bd, bi, bpos);
+  const float t = search_margin(g, q, 1) + sqrtf(bd * 1.000001f + 1e-30f);
   const float thr2 = t * t * 1.00001f;
-  constexpr int NK = (26 + G - 1) / G;
-  uint2 cc[NK];
-#pragma unroll
-  for (int k = 0; k < NK; ++k) {
-    const int idx = k * G + lg;
-    uint2 c = make_uint2(0u, 0u);
-    if (idx < 26) {
-      const int n = idx < 13 ? idx : idx + 1;
-      const int dx = n % 3 - 1, dy = (n / 3) % 3 - 1, dz = n / 9 - 1;
-      const int x = cx + dx, y = cy + dy, z = cz + dz;
-      const float b2 = (dx < 0 ? fxm2 : (dx > 0 ? fxp2 : 0.f)) + (dy < 0 ? fym2 : (dy > 0 ? fyp2 : 0.f)) +
-                       (dz < 0 ? fzm2 : (dz > 0 ? fzp2 : 0.f));
-      if (x >= 0 && x < g.nx && y >= 0 && y < g.ny && z >= 0 && z < g.nz && !(b2 > thr2))
-        c = g.cells[((unsigned)z * (unsigned)g.ny + (unsigned)y) * (unsigned)g.nx + (unsigned)x];
-    }
-    cc[k] = c;
-  }
-#pragma unroll
-  for (int k = 0; k < NK; ++k)
-    for (unsigned j = cc[k].x; j < cc[k].y; ++j) nn_take(g.pts[j], j, q, bd, bi, bpos);
+  near_neighbours<G>(g, c, thr2, lg, [&](int x, int y, int z) {
+    const uint2 e = g.cells[((unsigned)z * (unsigned)g.ny + (unsigned)y) * (unsigned)g.nx + (unsigned)x];
+    for (unsigned j = e.x; j < e.y; ++j) nn_take(g.pts[j], j, q, bd, bi, bpos);
+  });
   group_best<G>(gmask, bd, bi, bpos);
   if (bi == INT_MAX) {
     bi = -1;
@@ -362,45 +396,24 @@ __device__ __forceinline__ void grid_nn1_near(const GridView& g, float4 q, float
 // Whether any point lies within sqrt(r2) of q (d^2 <= r2, finite), over the
 // 27 cells around q's cell (precondition: grid_near27_ok(g, r2)), G lanes
 // per query; the same answer as grid_nn1_group finding a neighbour.  The own
-// cell first, then the neighbours whose box is within reach; every lane stops
-// once the group has found one.
+// cell first, then the neighbours within reach; every lane stops once the
+// group has found one.
 template <int G>
 __device__ __forceinline__ bool grid_any_near(const GridView& g, float4 q, float r2, int lg, unsigned gmask) {
-  const int cx = q_cell(q.x, g.ox, g.inv_h), cy = q_cell(q.y, g.oy, g.inv_h),
-            cz = q_cell(q.z, g.oz, g.inv_h);
+  const NearCell c = near_cell(g, q);
   bool found = false;
-  if (cx >= 0 && cx < g.nx && cy >= 0 && cy < g.ny && cz >= 0 && cz < g.nz) {
-    const uint2 c = g.cells[((unsigned)cz * (unsigned)g.ny + (unsigned)cy) * (unsigned)g.nx + (unsigned)cx];
-    for (unsigned j = c.x + (unsigned)lg; j < c.y && !found; j += G) found = dist2_exact(q, g.pts[j]) <= r2;
+  if (c.cx >= 0 && c.cx < g.nx && c.cy >= 0 && c.cy < g.ny && c.cz >= 0 && c.cz < g.nz) {
+    const uint2 e = g.cells[((unsigned)c.cz * (unsigned)g.ny + (unsigned)c.cy) * (unsigned)g.nx + (unsigned)c.cx];
+    for (unsigned j = e.x + (unsigned)lg; j < e.y && !found; j += G) found = dist2_exact(q, g.pts[j]) <= r2;
   }
   if (__any_sync(gmask, found)) return true;
-  const float margin = search_margin(g, q, 1);
-  const float xl = g.ox + (float)cx * g.h, yl = g.oy + (float)cy * g.h, zl = g.oz + (float)cz * g.h;
-  const float fxm = fmaxf(q.x - xl, 0.f), fxp = fmaxf(xl + g.h - q.x, 0.f);
-  const float fym = fmaxf(q.y - yl, 0.f), fyp = fmaxf(yl + g.h - q.y, 0.f);
-  const float fzm = fmaxf(q.z - zl, 0.f), fzp = fmaxf(zl + g.h - q.z, 0.f);
-  const float t = margin + sqrtf(r2 * 1.000001f + 1e-30f);
+  const float t = search_margin(g, q, 1) + sqrtf(r2 * 1.000001f + 1e-30f);
   const float thr2 = t * t * 1.00001f;
-  constexpr int NK = (26 + G - 1) / G;
-  uint2 cc[NK];
-#pragma unroll
-  for (int k = 0; k < NK; ++k) {
-    const int idx = k * G + lg;
-    uint2 c = make_uint2(0u, 0u);
-    if (idx < 26) {
-      const int n = idx < 13 ? idx : idx + 1;
-      const int dx = n % 3 - 1, dy = (n / 3) % 3 - 1, dz = n / 9 - 1;
-      const int x = cx + dx, y = cy + dy, z = cz + dz;
-      const float ex = dx < 0 ? fxm : (dx > 0 ? fxp : 0.f), ey = dy < 0 ? fym : (dy > 0 ? fyp : 0.f),
-                  ez = dz < 0 ? fzm : (dz > 0 ? fzp : 0.f);
-      if (x >= 0 && x < g.nx && y >= 0 && y < g.ny && z >= 0 && z < g.nz && !(ex * ex + ey * ey + ez * ez > thr2))
-        c = g.cells[((unsigned)z * (unsigned)g.ny + (unsigned)y) * (unsigned)g.nx + (unsigned)x];
-    }
-    cc[k] = c;
-  }
-#pragma unroll
-  for (int k = 0; k < NK; ++k)
-    for (unsigned j = cc[k].x; j < cc[k].y && !found; ++j) found = dist2_exact(q, g.pts[j]) <= r2;
+  near_neighbours<G>(g, c, thr2, lg, [&](int x, int y, int z) {
+    if (found) return;
+    const uint2 e = g.cells[((unsigned)z * (unsigned)g.ny + (unsigned)y) * (unsigned)g.nx + (unsigned)x];
+    for (unsigned j = e.x; j < e.y && !found; ++j) found = dist2_exact(q, g.pts[j]) <= r2;
+  });
   return __any_sync(gmask, found);
 }
 
