@@ -334,12 +334,14 @@ def run_ours(args):
         # correspondence; everything else (C x sets consistency checks over
         # those endpoints, the pass masks, the sets) lives in L2
         "gc_walk": ("hbm", 32.0 * C, "k_gc_coop (cooperative grouping walk)",
-                    f"compute- and barrier-bound: {C} x {gcs['sets']} = {C * gcs['sets']:.3g} consistency checks "
-                    f"in {gcs['rounds']} rounds of four grid-wide phases; the 32 B x C endpoints stay in L2"),
+                    f"barrier- and latency-bound: {gcs['sets']} consensus sets over {C} correspondences in "
+                    f"{gcs['rounds']} rounds of four grid-wide phases (seed tests pruned to the chunks within "
+                    f"each seed's reach; stale sets recomputed in place); the 32 B x C endpoints stay in L2"),
         # per hypothesis and iteration: each model voxel (16 B) and its matched scene point (16 B)
         "icp_refine": ("hbm", 32.0 * M_ref * prm.icp_iterations * m.n_voxels, "k_icp (multi-problem refinement)",
-                       "latency-bound: ~8 dependent grid lookups per source point, ~4 points per 2-lane group "
-                       "per iteration, then a grid barrier and the FP64 pose solve"),
+                       "latency- and barrier-bound: per iteration a 27-cell 1-NN per source point (own cell, "
+                       "then only the neighbours within reach; grid and voxels stay in L2), a per-hypothesis "
+                       "barrier and the FP64 pose solve"),
     }
     kern = {k: v for k, v in kern.items() if k in stage_ms}
     top = max(kern, key=lambda k: stage_ms[k])
