@@ -363,6 +363,25 @@ rtr_status rtr_knn(rtr_context* ctx, const float* d_query, int n_query,
                    const float* d_target, int n_target, int k,
                    int32_t* d_out_idx, float* d_out_d2, rtr_stream_t stream);
 
+/* Fixed-radius and box searches: for each query, every target with
+ * d^2 <= radius^2 (rtr_radius_search; d^2 as above), or every target inside
+ * the axis-aligned box [q - h, q + h] with the bounds formed in FP32 and
+ * included (rtr_box_search; the box of OctreePointCloudSearch::boxSearch in
+ * KeyPoint::getOccupiedGrid, key_point.h:118-140), in ascending target index.
+ * d_out_count[q] (optional) receives the true count; d_out_idx[q *
+ * max_per_query ...] the first max_per_query indices (the lowest ones when
+ * the count is larger), the slots past the count -1.  max_per_query = 0
+ * counts only (d_out_idx may then be NULL).  Queries or targets with a
+ * non-finite coordinate never match.  radius / half extent: finite, >= 0. */
+rtr_status rtr_radius_search(rtr_context* ctx, const float* d_query, int n_query,
+                             const float* d_target, int n_target, float radius,
+                             int max_per_query, int32_t* d_out_idx, int32_t* d_out_count,
+                             rtr_stream_t stream);
+rtr_status rtr_box_search(rtr_context* ctx, const float* d_query, int n_query,
+                          const float* d_target, int n_target, float half_extent,
+                          int max_per_query, int32_t* d_out_idx, int32_t* d_out_count,
+                          rtr_stream_t stream);
+
 /* ---- ICP (point-to-point) -------------------------------------------------
  * Replaces the PCL IterativeClosestPoint of keyPointICP (function.h:111-148).
  * One persistent cooperative kernel runs all iterations: per iteration it

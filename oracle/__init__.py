@@ -31,6 +31,7 @@ _SIG = {
     "orc_nn1_brute": (None, [_P, _I, _P, _I, _F, _P, _P]),
     "orc_nn1_grid": (None, [_P, _I, _P, _I, _F, _F, _P, _P]),
     "orc_knn_brute": (None, [_P, _I, _P, _I, _I, _P, _P]),
+    "orc_range_search": (None, [_P, _I, _P, _I, C.c_float, _I, _I, _P, _P]),
     "orc_transform_f32": (None, [_P, _P, _I, _P]),
     "orc_rigid_fit": (_I, [_P, _P, _P, _I, _P]),
     "orc_icp": (None, [_P, _I, _P, _I, _I, _F, _D, _D, _P, C.POINTER(IcpOut), _P, _P]),
@@ -132,6 +133,19 @@ def knn(q, t, k: int):
     lib().orc_knn_brute(q.ctypes.data, q.shape[0], t.ctypes.data, t.shape[0], int(k),
                         idx.ctypes.data, d2.ctypes.data)
     return idx, d2
+
+
+def range_search(q, t, r: float, box: bool = False, max_per_query: int = 64):
+    """Every target within r of each query (box: inside [q - r, q + r]), in
+    ascending index: (idx [nq, max_per_query] with -1 past the count,
+    count [nq]).  orc_range_search."""
+    q, t = _f4(q), _f4(t)
+    m = max(int(max_per_query), 0)
+    idx = np.empty((q.shape[0], max(m, 1)), np.int32)
+    cnt = np.empty(q.shape[0], np.int32)
+    lib().orc_range_search(q.ctypes.data, q.shape[0], t.ctypes.data, t.shape[0], float(r), 1 if box else 0, m,
+                           idx.ctypes.data, cnt.ctypes.data)
+    return idx[:, :m], cnt
 
 
 def transform_f32(T, pts) -> np.ndarray:

@@ -270,6 +270,39 @@ void orc_grid_inlier_fraction(const orc_grid* G, const float* src, int ns, int s
   free(idx);
 }
 
+/* Fixed-radius (box = 0: d^2 <= r^2, d^2 as d2f) and box (box = 1: the
+ * inclusive box [q - r, q + r] with the bounds formed in float, as
+ * KeyPoint::getOccupiedGrid forms v_min / v_max, key_point.h:118-140) searches
+ * by brute force: every target in ascending index; cnt[i] the true count, the
+ * first maxk indices in idx[i * maxk ...], -1 past the count.  A query or
+ * target with a non-finite coordinate never matches. */
+void orc_range_search(const float* q, int nq, const float* t, int nt, float r, int box, int maxk, int32_t* idx,
+                      int32_t* cnt) {
+  const float r2 = r * r;
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int i = 0; i < nq; ++i) {
+    const float* qi = q + 4 * i;
+    const int fin = isfinite(qi[0]) && isfinite(qi[1]) && isfinite(qi[2]);
+    float lo[3], hi[3];
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = qi[a] - r;
+      hi[a] = qi[a] + r;
+    }
+    int c = 0;
+    for (int j = 0; j < nt && fin; ++j) {
+      const float* p = t + 4 * j;
+      const int hit = box ? (p[0] >= lo[0] && p[1] >= lo[1] && p[2] >= lo[2] && p[0] <= hi[0] && p[1] <= hi[1] &&
+                             p[2] <= hi[2])
+                          : (d2f(qi, p) <= r2);
+      if (!hit) continue;
+      if (c < maxk) idx[(size_t)i * maxk + c] = j;
+      ++c;
+    }
+    for (int s = c; s < maxk; ++s) idx[(size_t)i * maxk + s] = -1;
+    cnt[i] = c;
+  }
+}
+
 void orc_knn_brute(const float* q, int nq, const float* t, int nt, int k, int32_t* idx, float* d2) {
 #pragma omp parallel for schedule(dynamic, 64)
   for (int i = 0; i < nq; ++i) {

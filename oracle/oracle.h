@@ -33,6 +33,8 @@ void orc_nn1_brute(const float* q, int nq, const float* t, int nt, float r2max, 
 void orc_nn1_grid(const float* q, int nq, const float* t, int nt, float r2max, float cell,
                   int32_t* idx, float* d2);
 void orc_knn_brute(const float* q, int nq, const float* t, int nt, int k, int32_t* idx, float* d2);
+void orc_range_search(const float* q, int nq, const float* t, int nt, float r, int box, int maxk, int32_t* idx,
+                      int32_t* cnt);
 
 /* ---- pose */
 void orc_transform_f32(const double* T16, const float* in, int n, float* out);

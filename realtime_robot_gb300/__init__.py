@@ -175,6 +175,8 @@ _SIG = {
     "rtr_plane_segment": (_I, [_P, _P, _I, C.c_void_p, C.c_void_p, _I, C.POINTER(C.c_int), _P]),
     "rtr_vector3d": (_I, [_P, _P, _I, C.c_void_p, _I, _P, _P]),
     "rtr_knn": (_I, [_P, _P, _I, _P, _I, _I, _P, _P, _P]),
+    "rtr_radius_search": (_I, [_P, _P, _I, _P, _I, C.c_float, _I, _P, _P, _P]),
+    "rtr_box_search": (_I, [_P, _P, _I, _P, _I, C.c_float, _I, _P, _P, _P]),
     "rtr_icp_default_params": (None, [C.POINTER(IcpParams)]),
     "rtr_icp": (_I, [_P, _P, _I, _P, _I, C.POINTER(IcpParams), _P, _P, _P, _P, _P]),
     "rtr_icp_host": (_I, [_P, _P, _I, _P, _I, C.POINTER(IcpParams), _P, C.POINTER(IcpResult)]),
@@ -344,6 +346,21 @@ class Context:
         check(lib().rtr_knn1(self.h, _ptr(query), nq, _ptr(target), nt, float(max_dist),
                              _ptr(idx), _ptr(d2), _stream(stream)))
         return idx, d2
+
+    def radius_search(self, query, target, radius: float, max_per_query: int = 64, box: bool = False,
+                      stream=None):
+        """rtr_radius_search (box=True: rtr_box_search with half extent
+        `radius`): (idx int32 [nq, max_per_query], ascending, -1 past the
+        count; count int32 [nq], the true count)."""
+        import torch
+        nq, nt = query.shape[0], target.shape[0]
+        m = int(max_per_query)
+        idx = torch.empty((nq, max(m, 1)), dtype=torch.int32, device=query.device)
+        cnt = torch.empty(nq, dtype=torch.int32, device=query.device)
+        fn = lib().rtr_box_search if box else lib().rtr_radius_search
+        check(fn(self.h, _ptr(query), nq, _ptr(target), nt, float(radius), m, _ptr(idx) if m > 0 else None,
+                 _ptr(cnt), _stream(stream)))
+        return idx[:, :m], cnt
 
     def knn1_static(self, query, target, max_dist: float = 0.0, out=None, stream=None):
         """rtr_knn1_static: rtr_knn1 with its grid in the library's fixed

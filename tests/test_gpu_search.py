@@ -5,6 +5,10 @@ import pytest
 
 import oracle as O
 
+from pathlib import Path
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
 pytestmark = pytest.mark.gpu
 
 
@@ -84,3 +88,38 @@ def test_knn_bit_exact(ctx, k):
     ri, rd = O.knn(q, t, k)
     assert np.array_equal(idx.cpu().numpy(), ri)
     assert np.array_equal(d2.cpu().numpy(), rd)
+
+
+@pytest.mark.parametrize("box", [False, True])
+def test_range_search_equals_oracle(ctx, box):
+    """rtr_radius_search / rtr_box_search against the oracle's brute force:
+    the same indices in the same (ascending) order and the same counts, with
+    cuts at max_per_query, non-finite points and an empty target set."""
+    import torch
+    rng = np.random.default_rng(5 + box)
+    q = rng.uniform(-1, 1, (3000, 4)).astype(np.float32)
+    t = rng.uniform(-1, 1, (50000, 4)).astype(np.float32)
+    q[[5, 77], 0] = np.nan
+    t[[3, 999], 1] = np.inf
+    dq, dt = torch.from_numpy(q).cuda(), torch.from_numpy(t).cuda()
+    for r, m in ((0.05, 64), (0.12, 16), (0.3, 0), (3.0, 8)):
+        idx, cnt = ctx.radius_search(dq, dt, r, m, box=box)
+        oidx, ocnt = O.range_search(q, t, r, box, m)
+        assert np.array_equal(cnt.cpu().numpy(), ocnt)
+        assert np.array_equal(idx.cpu().numpy(), oidx)
+    e = torch.zeros((0, 4), dtype=torch.float32, device="cuda")
+    idx, cnt = ctx.radius_search(dq, e, 0.1, 4, box=box)
+    assert int(cnt.sum()) == 0 and bool((idx == -1).all())
+
+
+def test_box_search_at_keypoints_of_main_scan(ctx):
+    """The reference's use: the +-10 cm box around each keypoint of the scan
+    main registers (KeyPoint::getOccupiedGrid, key_point.h:118-140)."""
+    import torch
+    d = np.load(GOLDEN / "main_clouds.npz")
+    scan = np.ascontiguousarray(d["T0_m8111"], np.float32)
+    keys = scan[O.uniform_sample(scan, 0.05)]
+    idx, cnt = ctx.radius_search(torch.from_numpy(keys).cuda(), torch.from_numpy(scan).cuda(), 0.1, 4096, box=True)
+    oidx, ocnt = O.range_search(keys, scan, 0.1, True, 4096)
+    assert np.array_equal(cnt.cpu().numpy(), ocnt) and ocnt.max() < 4096
+    assert np.array_equal(idx.cpu().numpy(), oidx)

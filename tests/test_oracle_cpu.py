@@ -146,3 +146,31 @@ def test_mlp_oracle_gradient_finite_differences():
             lm, _ = OM.loss_and_grad((theta - e).astype(np.float32), X, y)
             fd = (lp - lm) / (2e-5)
             assert abs(fd - g[int(idx)]) < 2e-4 + 1e-2 * abs(fd), (name, int(idx), fd, g[int(idx)])
+
+
+def test_range_search_oracle_against_numpy():
+    """orc_range_search: every target within r (d^2 in float32 as
+    ((dx*dx + dy*dy) + dz*dz)) or inside the float32 box [q - r, q + r],
+    ascending, the count true and the list cut at max_per_query."""
+    rng = np.random.default_rng(11)
+    q = rng.uniform(-1, 1, (64, 4)).astype(np.float32)
+    t = rng.uniform(-1, 1, (4000, 4)).astype(np.float32)
+    q[3, 1] = np.nan
+    t[7, 2] = np.inf
+    dx = (q[:, None, 0] - t[None, :, 0]).astype(np.float32)
+    dy = (q[:, None, 1] - t[None, :, 1]).astype(np.float32)
+    dz = (q[:, None, 2] - t[None, :, 2]).astype(np.float32)
+    d2 = ((dx * dx + dy * dy).astype(np.float32) + dz * dz).astype(np.float32)
+    r = np.float32(0.25)
+    lo, hi = (q[:, :3] - r).astype(np.float32), (q[:, :3] + r).astype(np.float32)
+    inbox = np.all((t[None, :, :3] >= lo[:, None, :]) & (t[None, :, :3] <= hi[:, None, :]), axis=2)
+    for box, want in ((False, d2 <= r * r), (True, inbox)):
+        for m in (0, 5, 400):
+            idx, cnt = O.range_search(q, t, float(r), box, m)
+            assert np.array_equal(cnt, want.sum(1))
+            for i in range(len(q)):
+                hits = np.nonzero(want[i])[0]
+                row = np.full(m, -1, np.int64)
+                row[: min(m, len(hits))] = hits[:m]
+                assert np.array_equal(idx[i], row)
+    assert O.range_search(q, t, 0.25, False, 4)[1][3] == 0
