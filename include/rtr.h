@@ -382,6 +382,15 @@ rtr_status rtr_box_search(rtr_context* ctx, const float* d_query, int n_query,
                           int max_per_query, int32_t* d_out_idx, int32_t* d_out_count,
                           rtr_stream_t stream);
 
+/* Inlier counts of candidate poses (the recognition's hypothesis score,
+ * exported): for each of the n_poses model -> scene poses (row-major 4x4
+ * doubles on the device, applied in FP32 as ((r0 x + r1 y) + r2 z) + t), the
+ * number of model points with a scene point within radius (d^2 <= radius^2
+ * as above).  d_counts[n_poses] on the device.  radius: finite, > 0. */
+rtr_status rtr_pose_inliers(rtr_context* ctx, const float* d_model, int n_model,
+                            const float* d_scene, int n_scene, const double* d_poses,
+                            int n_poses, float radius, int32_t* d_counts, rtr_stream_t stream);
+
 /* ---- ICP (point-to-point) -------------------------------------------------
  * Replaces the PCL IterativeClosestPoint of keyPointICP (function.h:111-148).
  * One persistent cooperative kernel runs all iterations: per iteration it
@@ -424,6 +433,17 @@ rtr_status rtr_icp(rtr_context* ctx, const float* d_src, int n_src,
 rtr_status rtr_icp_host(rtr_context* ctx, const float* h_src, int n_src,
                         const float* h_tgt, int n_tgt, const rtr_icp_params* params,
                         const double* h_init_pose, rtr_icp_result* h_result);
+
+/* Independent ICP problems of one source against one target, each from its
+ * own initial pose (d_init_poses: n_problems row-major 4x4 doubles on the
+ * device; NULL: identity), in one persistent launch over one target grid:
+ * the multi-hypothesis refinement of the recognition, exported.  params as
+ * rtr_icp (record_trace ignored); d_results[k] receives problem k's result.
+ * n_problems: 1 .. the co-resident block count (a few hundred); the source
+ * is used in its given order. */
+rtr_status rtr_icp_multi(rtr_context* ctx, const float* d_src, int n_src, const float* d_tgt,
+                         int n_tgt, const rtr_icp_params* params, const double* d_init_poses,
+                         int n_problems, rtr_icp_result* d_results, rtr_stream_t stream);
 
 /* Where the last ICP launch of the context spent its time (first problem of
  * the launch, summed over iterations, nanoseconds): [0] block 0's search and

@@ -180,6 +180,8 @@ _SIG = {
     "rtr_icp_default_params": (None, [C.POINTER(IcpParams)]),
     "rtr_icp": (_I, [_P, _P, _I, _P, _I, C.POINTER(IcpParams), _P, _P, _P, _P, _P]),
     "rtr_icp_host": (_I, [_P, _P, _I, _P, _I, C.POINTER(IcpParams), _P, C.POINTER(IcpResult)]),
+    "rtr_icp_multi": (_I, [_P, _P, _I, _P, _I, C.POINTER(IcpParams), _P, _I, _P, _P]),
+    "rtr_pose_inliers": (_I, [_P, _P, _I, _P, _I, _P, _I, C.c_float, _P, _P]),
     "rtr_voxel_downsample": (_I, [_P, _P, _I, _F, _P, _P, _P]),
     "rtr_uniform_sample": (_I, [_P, _P, _I, _F, _P, _P, _P]),
     "rtr_normals": (_I, [_P, _P, _I, _I, _P, _F, _P, _P]),
@@ -478,6 +480,31 @@ class Context:
                             None if ini is None else ini.ctypes.data, _ptr(result), _ptr(tp),
                             _ptr(tc), _stream(stream)))
         return result, tp, tc
+
+    def icp_multi(self, src, tgt, inits, max_iterations=10, max_corr_dist=0.0, cell_size=0.0,
+                  transformation_epsilon=0.0, rotation_epsilon=0.0, stream=None) -> list:
+        """rtr_icp_multi: one ICP per initial pose (inits: [n, 16] or [n, 4, 4]
+        float64, host or device) of src onto tgt; the parsed results."""
+        import torch
+        ini = torch.as_tensor(inits, dtype=torch.float64).reshape(-1, 16).contiguous().to(src.device)
+        n = ini.shape[0]
+        p = IcpParams(max_iterations, max_corr_dist, transformation_epsilon, rotation_epsilon, cell_size, 0)
+        res = torch.zeros(n * C.sizeof(IcpResult), dtype=torch.uint8, device=src.device)
+        check(lib().rtr_icp_multi(self.h, _ptr(src), src.shape[0], _ptr(tgt), tgt.shape[0], C.byref(p), _ptr(ini), n,
+                                  _ptr(res), _stream(stream)))
+        raw = bytes(res.cpu().numpy().tobytes())
+        k = C.sizeof(IcpResult)
+        return [self.parse_icp_result(raw[i * k:(i + 1) * k]) for i in range(n)]
+
+    def pose_inliers(self, model, scene, poses, radius: float, stream=None):
+        """rtr_pose_inliers: per model -> scene pose ([n, 16] or [n, 4, 4]
+        float64), the model points with a scene point within radius."""
+        import torch
+        P = torch.as_tensor(poses, dtype=torch.float64).reshape(-1, 16).contiguous().to(model.device)
+        cnt = torch.zeros(P.shape[0], dtype=torch.int32, device=model.device)
+        check(lib().rtr_pose_inliers(self.h, _ptr(model), model.shape[0], _ptr(scene), scene.shape[0], _ptr(P),
+                                     P.shape[0], float(radius), _ptr(cnt), _stream(stream)))
+        return cnt
 
     @staticmethod
     def parse_icp_result(buf) -> dict:

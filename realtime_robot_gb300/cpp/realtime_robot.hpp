@@ -30,6 +30,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <iostream>
 #include <memory>
 #include <ostream>
@@ -332,6 +333,55 @@ inline rtr_context* thread_context() {
   return h.ctx;
 }
 
+// Device scratch of the calling thread for the temporaries of one call: a
+// single buffer that only grows (a cudaMalloc only when a call needs more
+// than any before it), carved per call.  A call lists its arrays, commits,
+// then uses them; calls do not nest (each finishes with a synchronous copy
+// back, so the next call may reuse the bytes).
+struct ThreadArena {
+  char* base = nullptr;
+  size_t cap = 0;
+  ~ThreadArena() { cudaFree(base); }
+};
+inline ThreadArena& thread_arena() {
+  thread_local ThreadArena a;
+  return a;
+}
+class Carve {
+ public:
+  template <class T>
+  Carve& add(T*& out, size_t count) {
+    const size_t o = off_;
+    set_.push_back([&out, o](char* b) { out = reinterpret_cast<T*>(b + o); });
+    off_ += (count * sizeof(T) + 255) & ~size_t(255);
+    return *this;
+  }
+  void commit() {
+    ThreadArena& a = thread_arena();
+    if (off_ > a.cap) {
+      const size_t want = off_ > 2 * a.cap ? off_ : 2 * a.cap;
+      cudaFree(a.base);
+      a.base = nullptr;
+      a.cap = 0;
+      check_cuda(cudaMalloc(reinterpret_cast<void**>(&a.base), want), "cudaMalloc");
+      a.cap = want;
+    }
+    for (auto& f : set_) f(a.base);
+  }
+
+ private:
+  std::vector<std::function<void(char*)>> set_;
+  size_t off_ = 0;
+};
+template <class T>
+inline void to_device(T* d, const T* h, size_t count) {
+  if (count) check_cuda(cudaMemcpy(d, h, count * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+}
+template <class T>
+inline void to_host(T* h, const T* d, size_t count) {
+  if (count) check_cuda(cudaMemcpy(h, d, count * sizeof(T), cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+}
+
 constexpr int kDescDim = 352;
 
 // Surface (key_point.h:47-51): one plane of the reference's surface list.
@@ -350,13 +400,14 @@ inline std::vector<Surface> segment_surfaces(const Cloud& cloud, std::vector<rtr
   const int n = (int)cloud.size();
   std::vector<Surface> out;
   if (n == 0) return out;
-  DeviceArray<float> d_pts(4 * (size_t)n);
-  d_pts.upload(reinterpret_cast<const float*>(cloud.points.data()), 4 * (size_t)n);
+  float* d_pts;
+  Carve().add(d_pts, 4 * (size_t)n).commit();
+  to_device(d_pts, reinterpret_cast<const float*>(cloud.points.data()), 4 * (size_t)n);
   rtr_plane_params prm;
   rtr_plane_default_params(&prm);
   std::vector<rtr_surface> s(256);
   int ns = 0;
-  check(rtr_plane_segment(ctx, d_pts.p, n, &prm, s.data(), (int)s.size(), &ns, nullptr), "rtr_plane_segment");
+  check(rtr_plane_segment(ctx, d_pts, n, &prm, s.data(), (int)s.size(), &ns, nullptr), "rtr_plane_segment");
   s.resize((size_t)ns);
   for (const rtr_surface& r : s) {
     if (!r.kept) continue;
@@ -426,13 +477,14 @@ inline void vector3d_all(std::vector<KeyPoint>& keys, const std::vector<Surface>
     k[4 * i + 2] = keys[i].Key_coordinate.z;
     k[4 * i + 3] = 0.f;
   }
-  DeviceArray<float> d_k(k.size());
-  DeviceArray<double> d_v(3 * keys.size());
-  d_k.upload(k.data(), k.size());
+  float* d_k;
+  double* d_v;
+  Carve().add(d_k, k.size()).add(d_v, 3 * keys.size()).commit();
+  to_device(d_k, k.data(), k.size());
   const std::vector<rtr_surface> rec = to_records(surface);
-  check(rtr_vector3d(ctx, d_k.p, (int)keys.size(), rec.data(), (int)rec.size(), d_v.p, nullptr), "rtr_vector3d");
+  check(rtr_vector3d(ctx, d_k, (int)keys.size(), rec.data(), (int)rec.size(), d_v, nullptr), "rtr_vector3d");
   std::vector<double> v(3 * keys.size());
-  d_v.download(v.data(), v.size());
+  to_host(v.data(), d_v, v.size());
   for (size_t i = 0; i < keys.size(); ++i) keys[i].vector3D.assign(v.begin() + 3 * i, v.begin() + 3 * i + 3);
 }
 
@@ -466,31 +518,37 @@ struct KeypointSet {
     rtr_recog_default_params(&prm);
     const int n = (int)cloud.size();
     if (n <= 0) throw std::invalid_argument("getKeypoint: empty cloud");
-    DeviceArray<float> d_pts(4 * (size_t)n), d_vox(4 * (size_t)n), d_nrm(4 * (size_t)n);
-    DeviceArray<int> d_cnt(2);
-    DeviceArray<int32_t> d_keys((size_t)n);
-    d_pts.upload(reinterpret_cast<const float*>(cloud.points.data()), 4 * (size_t)n);
-    check(rtr_voxel_downsample(ctx, d_pts.p, n, prm.voxel_leaf, d_vox.p, d_cnt.p, nullptr), "rtr_voxel_downsample");
+    float *d_pts, *d_vox, *d_nrm;
+    int* d_cnt;
+    int32_t* d_keys;
+    Carve()
+        .add(d_pts, 4 * (size_t)n)
+        .add(d_vox, 4 * (size_t)n)
+        .add(d_nrm, 4 * (size_t)n)
+        .add(d_cnt, 2)
+        .add(d_keys, (size_t)n)
+        .commit();
+    to_device(d_pts, reinterpret_cast<const float*>(cloud.points.data()), 4 * (size_t)n);
+    check(rtr_voxel_downsample(ctx, d_pts, n, prm.voxel_leaf, d_vox, d_cnt, nullptr), "rtr_voxel_downsample");
     int V = 0;
-    d_cnt.download(&V, 1);
+    to_host(&V, d_cnt, 1);
     if (V <= 0) throw std::runtime_error("getKeypoint: the voxel filter kept no point");
-    check(rtr_normals(ctx, d_vox.p, V, prm.normal_k, viewpoint, 2.f * prm.voxel_leaf, d_nrm.p, nullptr),
-          "rtr_normals");
-    if (outward) check(rtr_orient_normals_outward(ctx, d_vox.p, d_nrm.p, V, 0.01f, 0.005f, 1.0f, nullptr),
+    check(rtr_normals(ctx, d_vox, V, prm.normal_k, viewpoint, 2.f * prm.voxel_leaf, d_nrm, nullptr), "rtr_normals");
+    if (outward) check(rtr_orient_normals_outward(ctx, d_vox, d_nrm, V, 0.01f, 0.005f, 1.0f, nullptr),
                        "rtr_orient_normals_outward");
     const float r_kp = model_side ? prm.model_keypoint_r : prm.scene_keypoint_r;
-    check(rtr_uniform_sample(ctx, d_vox.p, V, r_kp, d_keys.p, d_cnt.p + 1, nullptr), "rtr_uniform_sample");
+    check(rtr_uniform_sample(ctx, d_vox, V, r_kp, d_keys, d_cnt + 1, nullptr), "rtr_uniform_sample");
     int K = 0;
-    check_cuda(cudaMemcpy(&K, d_cnt.p + 1, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    to_host(&K, d_cnt + 1, 1);
     n_kp = K;
     d_desc.resize((size_t)K * kDescDim);
     if (K > 0)
-      check(rtr_shot352(ctx, d_vox.p, d_nrm.p, V, d_keys.p, K, prm.descriptor_r, d_desc.p, nullptr, nullptr),
+      check(rtr_shot352(ctx, d_vox, d_nrm, V, d_keys, K, prm.descriptor_r, d_desc.p, nullptr, nullptr),
             "rtr_shot352");
     std::vector<float> vox(4 * (size_t)V), desc((size_t)K * kDescDim);
     std::vector<int32_t> keys((size_t)K);
-    d_vox.download(vox.data(), vox.size());
-    d_keys.download(keys.data(), keys.size());
+    to_host(vox.data(), d_vox, vox.size());
+    to_host(keys.data(), d_keys, keys.size());
     d_desc.download(desc.data(), desc.size());
     std::vector<float> kp(4 * (size_t)K);
     key_coordinates = Cloud();
@@ -516,19 +574,20 @@ inline Cloud harris_keypoints(const Cloud& cloud, float radius = 0.05f, float th
   const int n = (int)cloud.size();
   Cloud out;
   if (n == 0) return out;
-  DeviceArray<float> d_pts(4 * (size_t)n), d_keys(4 * (size_t)n);
-  DeviceArray<int32_t> d_src((size_t)n);
-  DeviceArray<int> d_cnt(1);
-  d_pts.upload(reinterpret_cast<const float*>(cloud.points.data()), 4 * (size_t)n);
+  float *d_pts, *d_keys;
+  int32_t* d_src;
+  int* d_cnt;
+  Carve().add(d_pts, 4 * (size_t)n).add(d_keys, 4 * (size_t)n).add(d_src, (size_t)n).add(d_cnt, 1).commit();
+  to_device(d_pts, reinterpret_cast<const float*>(cloud.points.data()), 4 * (size_t)n);
   rtr_harris_params prm;
   rtr_harris_default_params(&prm);
   prm.radius = radius;
   prm.threshold = threshold;
-  check(rtr_harris3d(ctx, d_pts.p, n, &prm, d_keys.p, d_src.p, d_cnt.p, nullptr), "rtr_harris3d");
+  check(rtr_harris3d(ctx, d_pts, n, &prm, d_keys, d_src, d_cnt, nullptr), "rtr_harris3d");
   int K = 0;
-  d_cnt.download(&K, 1);
+  to_host(&K, d_cnt, 1);
   std::vector<float> k(4 * (size_t)K);
-  d_keys.download(k.data(), k.size());
+  to_host(k.data(), d_keys, k.size());
   for (int i = 0; i < K; ++i) out.push_back(pcl::PointXYZ(k[4 * (size_t)i], k[4 * (size_t)i + 1], k[4 * (size_t)i + 2]));
   return out;
 }
@@ -583,13 +642,14 @@ inline std::vector<PairPoint> match_keypoints(const ModelPoint& model, const Sca
   }
   std::vector<PairPoint> out;
   if (model.n_kp == 0 || scan.n_kp == 0) return out;
-  DeviceArray<int32_t> d_idx((size_t)scan.n_kp);
-  DeviceArray<float> d_d2((size_t)scan.n_kp);
-  check(rtr_match(ctx, scan.d_desc.p, scan.n_kp, model.d_desc.p, model.n_kp, d_idx.p, d_d2.p, nullptr), "rtr_match");
+  int32_t* d_idx;
+  float* d_d2;
+  Carve().add(d_idx, (size_t)scan.n_kp).add(d_d2, (size_t)scan.n_kp).commit();
+  check(rtr_match(ctx, scan.d_desc.p, scan.n_kp, model.d_desc.p, model.n_kp, d_idx, d_d2, nullptr), "rtr_match");
   std::vector<int32_t> idx((size_t)scan.n_kp);
   std::vector<float> d2((size_t)scan.n_kp);
-  d_idx.download(idx.data(), idx.size());
-  d_d2.download(d2.data(), d2.size());
+  to_host(idx.data(), d_idx, idx.size());
+  to_host(d2.data(), d_d2, d2.size());
   for (int s = 0; s < scan.n_kp; ++s) {
     if (idx[s] < 0 || !(d2[s] < max_d2)) continue;
     PairPoint p;
@@ -608,17 +668,19 @@ inline void KeyPoint::getOccupiedGrid(Cloud::Ptr cloud, float resolution, float 
   rtr_context* ctx = thread_context();
   const int n = (int)cloud->size();
   const float key[4] = {Key_coordinate.x, Key_coordinate.y, Key_coordinate.z, 0.f};
-  DeviceArray<float> d_cloud(4 * (size_t)(n > 0 ? n : 1)), d_key(4);
-  DeviceArray<int32_t> d_num(1), d_off(2), d_idx((size_t)(n > 0 ? n : 1));
-  d_cloud.upload(reinterpret_cast<const float*>(cloud->points.data()), 4 * (size_t)n);
-  d_key.upload(key, 4);
+  const size_t cap = (size_t)(n > 0 ? n : 1);
+  float *d_cloud, *d_key;
+  int32_t *d_num, *d_off, *d_idx;
+  Carve().add(d_cloud, 4 * cap).add(d_key, 4).add(d_num, 1).add(d_off, 2).add(d_idx, cap).commit();
+  to_device(d_cloud, reinterpret_cast<const float*>(cloud->points.data()), 4 * (size_t)n);
+  to_device(d_key, key, 4);
   long long total = 0;
-  check(rtr_ref_occupancy(ctx, d_cloud.p, n, d_key.p, 1, resolution, f_adjust, d_num.p, d_off.p, d_idx.p,
-                          (long long)d_idx.n, &total, nullptr),
+  check(rtr_ref_occupancy(ctx, d_cloud, n, d_key, 1, resolution, f_adjust, d_num, d_off, d_idx, (long long)cap, &total,
+                          nullptr),
         "rtr_ref_occupancy");
   std::vector<int32_t> idx((size_t)total);
-  d_idx.download(idx.data(), idx.size());
-  d_num.download(&Occupiedgrid.Number, 1);
+  to_host(idx.data(), d_idx, idx.size());
+  to_host(&Occupiedgrid.Number, d_num, 1);
   Occupiedgrid.cloud.reset(new Cloud);
   Occupiedgrid.cloud->points.reserve(idx.size());
   for (int32_t i : idx) Occupiedgrid.cloud->points.push_back(cloud->points[(size_t)i]);
@@ -634,17 +696,23 @@ inline void KeyPoint::get_TSDF(Cloud::Ptr cloud, float resolution, float f_adjus
   std::vector<int32_t> idx((size_t)(n > 0 ? n : 1));
   for (int i = 0; i < n; ++i) idx[(size_t)i] = i;
   const int32_t off[2] = {0, n};
-  DeviceArray<float> d_cloud(4 * (size_t)(n > 0 ? n : 1)), d_key(4), d_tdf(27000);
-  DeviceArray<int32_t> d_off(2), d_idx(idx.size());
-  d_cloud.upload(reinterpret_cast<const float*>(occ.points.data()), 4 * (size_t)n);
-  d_key.upload(key, 4);
-  d_off.upload(off, 2);
-  d_idx.upload(idx.data(), idx.size());
+  float *d_cloud, *d_key, *d_tdf;
+  int32_t *d_off, *d_idx;
+  Carve()
+      .add(d_cloud, 4 * (size_t)(n > 0 ? n : 1))
+      .add(d_key, 4)
+      .add(d_tdf, 27000)
+      .add(d_off, 2)
+      .add(d_idx, idx.size())
+      .commit();
+  to_device(d_cloud, reinterpret_cast<const float*>(occ.points.data()), 4 * (size_t)n);
+  to_device(d_key, key, 4);
+  to_device(d_off, off, 2);
+  to_device(d_idx, idx.data(), idx.size());
   int dim = 0;
-  check(rtr_ref_tdf(ctx, d_cloud.p, d_key.p, 1, d_off.p, d_idx.p, resolution, f_adjust, d_tdf.p, &dim, nullptr),
-        "rtr_ref_tdf");
+  check(rtr_ref_tdf(ctx, d_cloud, d_key, 1, d_off, d_idx, resolution, f_adjust, d_tdf, &dim, nullptr), "rtr_ref_tdf");
   grid_value.assign(27000, 0.f);
-  d_tdf.download(grid_value.data(), (size_t)dim * dim * dim);
+  to_host(grid_value.data(), d_tdf, (size_t)dim * dim * dim);
   const float k3[3] = {Key_coordinate.x, Key_coordinate.y, Key_coordinate.z};
   for (int a = 0; a < 3; ++a) {
     Border[a] = k3[a] - f_adjust;
@@ -666,22 +734,29 @@ inline float get_Distance(Eigen::Matrix4f& key_transform, KeyPoint& p1_key, KeyP
   std::vector<int32_t> idx((size_t)(n > 0 ? n : 1));
   for (int i = 0; i < n; ++i) idx[(size_t)i] = i;
   const int32_t off[2] = {0, n}, pm = 0, ps = 0;
-  DeviceArray<float> d_cloud(4 * (size_t)(n > 0 ? n : 1)), d_km(4), d_ks(4), d_tdf(27000), d_score(1), d_T(16);
-  DeviceArray<int32_t> d_off(2), d_idx(idx.size()), d_pm(1), d_ps(1);
-  d_cloud.upload(reinterpret_cast<const float*>(occ.points.data()), 4 * (size_t)n);
-  d_km.upload(km, 4);
-  d_ks.upload(ks, 4);
-  d_tdf.upload(p1_key.grid_value.data(), 27000);
-  d_off.upload(off, 2);
-  d_idx.upload(idx.data(), idx.size());
-  d_pm.upload(&pm, 1);
-  d_ps.upload(&ps, 1);
-  check(rtr_ref_distance(ctx, d_cloud.p, d_km.p, 1, d_off.p, d_idx.p, d_tdf.p, d_ks.p, 1, d_pm.p, d_ps.p, 1,
-                         resolution, 0.15f, d_score.p, d_T.p, nullptr),
+  // one upload of the packed inputs: keypoints (2 x 4 floats), the field,
+  // the cloud; and of the integer inputs: offsets, pair, indices
+  const size_t nf = 8 + 27000 + 4 * (size_t)n, ni = 4 + idx.size();
+  std::vector<float> hf(nf);
+  std::memcpy(hf.data(), km, sizeof(km));
+  std::memcpy(hf.data() + 4, ks, sizeof(ks));
+  std::memcpy(hf.data() + 8, p1_key.grid_value.data(), 27000 * sizeof(float));
+  if (n) std::memcpy(hf.data() + 8 + 27000, occ.points.data(), 4 * (size_t)n * sizeof(float));
+  std::vector<int32_t> hi(ni);
+  hi[0] = off[0], hi[1] = off[1], hi[2] = pm, hi[3] = ps;
+  std::memcpy(hi.data() + 4, idx.data(), idx.size() * sizeof(int32_t));
+  float *d_f, *d_out;
+  int32_t* d_i;
+  Carve().add(d_f, nf).add(d_i, ni).add(d_out, 20).commit();
+  to_device(d_f, hf.data(), nf);
+  to_device(d_i, hi.data(), ni);
+  check(rtr_ref_distance(ctx, d_f + 8 + 27000, d_f, 1, d_i, d_i + 4, d_f + 8, d_f + 4, 1, d_i + 2, d_i + 3, 1,
+                         resolution, 0.15f, d_out, d_out + 4, nullptr),
         "rtr_ref_distance");
-  float score = 0.f, T[16];
-  d_score.download(&score, 1);
-  d_T.download(T, 16);
+  float o[20];
+  to_host(o, d_out, 20);
+  const float score = o[0];
+  const float* T = o + 4;
   for (int i = 0; i < 16; ++i) key_transform(i / 4, i % 4) = T[i];
   return score;
 }
@@ -705,44 +780,14 @@ inline bool match_by_occupied(OccupiedGrid& o1, OccupiedGrid& o2) {
   return !(q > 2 || q < 0.5);
 }
 
-// Inlier counts of candidate model -> scene poses (row-major 4x4 doubles):
-// for each pose, how many points of mcloud it brings within r of a point of
-// the scene cloud (already on the device), from one exact grid 1-NN call
-// over all poses' transformed points.
-inline std::vector<long long> pose_inliers(rtr_context* ctx, const std::vector<double>& poses, const Cloud& mcloud,
-                                           const float* d_scene, int ns, float r) {
-  const int np = (int)(poses.size() / 16), nm = (int)mcloud.size();
-  std::vector<long long> out((size_t)np, 0);
-  if (np == 0 || nm == 0 || ns == 0) return out;
-  if ((size_t)np * (size_t)nm > (size_t)INT32_MAX) throw rtr_error(RTR_ERR_INVALID_ARG, "pose_inliers: too many points");
-  std::vector<float> q((size_t)np * nm * 4);
-  for (int c = 0; c < np; ++c) {
-    const double* T = &poses[(size_t)c * 16];
-    for (int i = 0; i < nm; ++i) {
-      const pcl::PointXYZ& m = mcloud.points[(size_t)i];
-      float* o = &q[((size_t)c * nm + i) * 4];
-      for (int k = 0; k < 3; ++k) o[k] = (float)(T[k * 4] * m.x + T[k * 4 + 1] * m.y + T[k * 4 + 2] * m.z + T[k * 4 + 3]);
-      o[3] = 0.f;
-    }
-  }
-  DeviceArray<float> d_q(q.size()), d_d2((size_t)np * nm);
-  DeviceArray<int32_t> d_idx((size_t)np * nm);
-  d_q.upload(q.data(), q.size());
-  check(rtr_knn1(ctx, d_q.p, np * nm, d_scene, ns, r, d_idx.p, d_d2.p, nullptr), "rtr_knn1");
-  std::vector<int32_t> idx((size_t)np * nm);
-  d_idx.download(idx.data(), idx.size());
-  for (int c = 0; c < np; ++c)
-    for (int i = 0; i < nm; ++i) out[(size_t)c] += idx[(size_t)c * nm + i] >= 0;
-  return out;
-}
-
 // function.h:35-109.  The reference scores candidate transforms and keeps
 // the best.  Here the candidates are the groups of geometric-consistency
 // grouping (bin 1 cm, at least 5 members, the configs' parameters), each
 // with its least-squares pose, verified as the library's recognition does:
-// each pose scored by the model points (mcloud) it brings within
-// 2 * inlier_r of a scene point (cloud), the 16 best refined by ICP
-// (30 iterations, 2 cm), and the refined pose with the most model points
+// each pose scored on the device by the model points (mcloud) it brings
+// within 2 * inlier_r of a scene point (cloud, rtr_pose_inliers), the 16 best
+// refined together by one multi-problem ICP (rtr_icp_multi: 30 iterations,
+// 2 cm, a 3 cm target grid), and the refined pose with the most model points
 // within inlier_r kept (ties: the better first score).  As in main, the
 // result maps the scene onto the model (main applies it to `cloud`).
 // ransac_times is kept for the signature (the grouping is deterministic).
@@ -765,44 +810,67 @@ inline Eigen::Matrix4f Ransac(std::vector<PairPoint> pairpoint, int ransac_times
     cs[(size_t)i] = i;
     cd[(size_t)i] = p.distance2;
   }
-  constexpr int kMaxClusters = 256, kMaxMembers = 128;
-  DeviceArray<float> d_mk(mk.size()), d_sk(sk.size()), d_cd(cd.size());
-  DeviceArray<int32_t> d_cm(cm.size()), d_cs(cs.size()), d_mem((size_t)kMaxClusters * kMaxMembers), d_sizes(kMaxClusters);
-  DeviceArray<double> d_poses((size_t)kMaxClusters * 16);
-  d_mk.upload(mk.data(), mk.size());
-  d_sk.upload(sk.data(), sk.size());
-  d_cd.upload(cd.data(), cd.size());
-  d_cm.upload(cm.data(), cm.size());
-  d_cs.upload(cs.data(), cs.size());
+  constexpr int kMaxClusters = 256, kMaxMembers = 128, kTop = 16;
+  const int ns = (int)cloud->size(), nm = (int)mcloud->size();
+  float *d_mk, *d_sk, *d_cd, *d_s, *d_m;
+  int32_t *d_cm, *d_cs, *d_mem, *d_sizes, *d_cnt;
+  double *d_poses, *d_init;
+  rtr_icp_result* d_res;
+  Carve()
+      .add(d_mk, mk.size())
+      .add(d_sk, sk.size())
+      .add(d_cd, cd.size())
+      .add(d_cm, cm.size())
+      .add(d_cs, cs.size())
+      .add(d_mem, (size_t)kMaxClusters * kMaxMembers)
+      .add(d_sizes, kMaxClusters)
+      .add(d_poses, (size_t)kMaxClusters * 16)
+      .add(d_s, 4 * (size_t)(ns > 0 ? ns : 1))
+      .add(d_m, 4 * (size_t)(nm > 0 ? nm : 1))
+      .add(d_cnt, kMaxClusters)
+      .add(d_init, (size_t)kTop * 16)
+      .add(d_res, kTop)
+      .commit();
+  to_device(d_mk, mk.data(), mk.size());
+  to_device(d_sk, sk.data(), sk.size());
+  to_device(d_cd, cd.data(), cd.size());
+  to_device(d_cm, cm.data(), cm.size());
+  to_device(d_cs, cs.data(), cs.size());
   int ncl = 0;
-  check(rtr_gc_group(ctx, d_mk.p, d_sk.p, d_cm.p, d_cs.p, d_cd.p, C, 0.01f, 5, kMaxClusters, kMaxMembers, d_mem.p,
-                     d_sizes.p, d_poses.p, &ncl, nullptr),
+  check(rtr_gc_group(ctx, d_mk, d_sk, d_cm, d_cs, d_cd, C, 0.01f, 5, kMaxClusters, kMaxMembers, d_mem, d_sizes, d_poses,
+                     &ncl, nullptr),
         "rtr_gc_group");
-  if (ncl <= 0) return best;
+  if (ncl <= 0 || ns == 0 || nm == 0) return best;
+  to_device(d_s, reinterpret_cast<const float*>(cloud->points.data()), 4 * (size_t)ns);
+  to_device(d_m, reinterpret_cast<const float*>(mcloud->points.data()), 4 * (size_t)nm);
+  // first scores of every group's pose, on the device
+  check(rtr_pose_inliers(ctx, d_m, nm, d_s, ns, d_poses, ncl, 2.f * inlier_r, d_cnt, nullptr), "rtr_pose_inliers");
+  std::vector<int32_t> first((size_t)ncl);
+  to_host(first.data(), d_cnt, first.size());
   std::vector<double> poses((size_t)ncl * 16);
-  d_poses.download(poses.data(), poses.size());
-  const int ns = (int)cloud->size();
-  DeviceArray<float> d_s(4 * (size_t)ns);
-  d_s.upload(reinterpret_cast<const float*>(cloud->points.data()), 4 * (size_t)ns);
-  const std::vector<long long> first = pose_inliers(ctx, poses, *mcloud, d_s.p, ns, 2.f * inlier_r);
+  to_host(poses.data(), d_poses, poses.size());
   std::vector<int> order((size_t)ncl);
   for (int c = 0; c < ncl; ++c) order[(size_t)c] = c;
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return first[(size_t)x] > first[(size_t)y]; });
-  const int top = ncl < 16 ? ncl : 16;
+  const int top = ncl < kTop ? ncl : kTop;
+  std::vector<double> init((size_t)top * 16);
+  for (int k = 0; k < top; ++k) std::memcpy(&init[(size_t)k * 16], &poses[(size_t)order[(size_t)k] * 16], 16 * sizeof(double));
+  to_device(d_init, init.data(), init.size());
+  // the top candidates refined together
   rtr_icp_params ip;
   rtr_icp_default_params(&ip);
   ip.max_iterations = 30;
   ip.max_corr_dist = 0.02f;
+  ip.cell_size = 0.03f;
+  check(rtr_icp_multi(ctx, d_m, nm, d_s, ns, &ip, d_init, top, d_res, nullptr), "rtr_icp_multi");
+  std::vector<rtr_icp_result> res((size_t)top);
+  to_host(res.data(), d_res, res.size());
   std::vector<double> refined((size_t)top * 16);
-  for (int k = 0; k < top; ++k) {
-    rtr_icp_result r;
-    check(rtr_icp_host(ctx, reinterpret_cast<const float*>(mcloud->points.data()), (int)mcloud->size(),
-                       reinterpret_cast<const float*>(cloud->points.data()), ns, &ip,
-                       &poses[(size_t)order[(size_t)k] * 16], &r),
-          "rtr_icp_host");
-    std::memcpy(&refined[(size_t)k * 16], r.pose, sizeof(r.pose));
-  }
-  const std::vector<long long> fin = pose_inliers(ctx, refined, *mcloud, d_s.p, ns, inlier_r);
+  for (int k = 0; k < top; ++k) std::memcpy(&refined[(size_t)k * 16], res[(size_t)k].pose, 16 * sizeof(double));
+  to_device(d_init, refined.data(), refined.size());
+  check(rtr_pose_inliers(ctx, d_m, nm, d_s, ns, d_init, top, inlier_r, d_cnt, nullptr), "rtr_pose_inliers");
+  std::vector<int32_t> fin((size_t)top);
+  to_host(fin.data(), d_cnt, fin.size());
   int w = 0;
   for (int k = 1; k < top; ++k)
     if (fin[(size_t)k] > fin[(size_t)w]) w = k;

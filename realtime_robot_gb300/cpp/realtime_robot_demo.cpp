@@ -13,6 +13,7 @@
 // (occupancy grids, TDF, get_Distance, the gates) on the kept KeyPoint calls;
 // `realtime_robot_demo pcd <in> <ascii out> <binary out>` round-trips a PCD
 // file through pcl::io (no GPU).
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -57,6 +58,8 @@ static int reference_route(unsigned long long seed) {
   rtr_robot::check(rtr_synth_shape(0, 41 + seed, n, scan.data()), "rtr_synth_shape");
   for (int i = 0; i < n; ++i) scan[4 * (size_t)i] += 0.01f * (float)(seed % 5);
   Cloud::Ptr mcloud = to_cloud(model, n), cloud = to_cloud(scan, n);
+  using clk = std::chrono::steady_clock;
+  const auto t0 = clk::now();
   // main's plane areas (model_point.h:170-245, scan_point.h:117-188), which
   // fill each keypoint's vector3D for the area gate
   rtr_robot::ModelPoint modelpoint(mcloud);
@@ -77,11 +80,13 @@ static int reference_route(unsigned long long seed) {
     p.get_Vector3D(scanpoint.surface);
     sk.push_back(std::move(p));
   }
+  const auto t1 = clk::now();
   std::printf("surfaces %zu %zu\n", modelpoint.surface.size(), scanpoint.surface.size());
   // the reference's detector on the same clouds (its keypoints are where
   // main runs this route; the fixed strides above keep the pair count even)
   std::printf("harris %zu %zu\n", rtr_robot::harris_keypoints(*mcloud).size(), rtr_robot::harris_keypoints(*cloud).size());
   int kept = 0;
+  const auto t2 = clk::now();
   for (size_t m = 0; m < mk.size(); ++m)
     for (size_t s = 0; s < sk.size(); ++s) {
       Eigen::Matrix4f T;
@@ -95,7 +100,15 @@ static int reference_route(unsigned long long seed) {
       std::printf("pair %zu %zu %08x %d\n", m, s, bits, keep ? 1 : 0);
       kept += keep;
     }
+  const auto t3 = clk::now();
   std::printf("reference route: %zu x %zu keypoints, %d pairs\n", mk.size(), sk.size(), kept);
+  // wall clock of main's route through the kept API: surfaces and keypoint
+  // members (getArea / get_Area, getOccupiedGrid, get_TSDF, get_Vector3D),
+  // then the pair loop (get_Distance and the gates, printing included)
+  const double s_keys = std::chrono::duration<double>(t1 - t0).count();
+  const double s_pairs = std::chrono::duration<double>(t3 - t2).count();
+  std::printf("timing keypoints %zu keypoint_s %.6f pairs %zu pair_s %.6f\n", mk.size() + sk.size(), s_keys,
+              mk.size() * sk.size(), s_pairs);
   return 0;
 }
 

@@ -608,6 +608,55 @@ rtr_status rtr_icp(rtr_context* ctx, const float* d_src, int n_src, const float*
   return icp_multi(ctx, s, specs, st);
 }
 
+rtr_status rtr_icp_multi(rtr_context* ctx, const float* d_src, int n_src, const float* d_tgt, int n_tgt,
+                         const rtr_icp_params* params, const double* d_init_poses, int n_problems,
+                         rtr_icp_result* d_results, rtr_stream_t stream) {
+  RTR_CHECK_ARG(ctx && params && d_results, "rtr_icp_multi: ctx, params and d_results are required");
+  RTR_CHECK_ARG(n_src > 0 && n_tgt > 0 && d_src && d_tgt, "rtr_icp_multi: empty source or target");
+  RTR_CHECK_ARG(params->max_iterations > 0, "rtr_icp_multi: max_iterations must be > 0");
+  RTR_CHECK_ARG(((uintptr_t)d_src & 15) == 0 && ((uintptr_t)d_tgt & 15) == 0,
+                "rtr_icp_multi: point arrays must be 16-byte aligned");
+  cudaStream_t st = (cudaStream_t)stream;
+  RTR_CUDA(cudaSetDevice(ctx->device));
+  const int maxb = icp_max_blocks(ctx);
+  RTR_CHECK_ARG(n_problems >= 1 && n_problems <= maxb, "rtr_icp_multi: n_problems must be in [1, %d]", maxb);
+  const unsigned cell_cap = default_cell_cap(n_tgt);
+  ScratchPlan plan;
+  grid_plan(plan, n_tgt, cell_cap);
+  plan.add<GridMeta>(1);
+  icp_multi_plan(plan, n_problems, maxb);
+  Scratch s;
+  RTR_TRY(ensure_scratch(ctx, plan.bytes, st, &s));
+  GridBufs gb;
+  if (!grid_take(s, n_tgt, cell_cap, &gb)) return fail(RTR_ERR_CAPACITY, "rtr_icp_multi: scratch carve");
+  GridMeta* src_meta = s.take<GridMeta>(1);
+  if (!src_meta) return fail(RTR_ERR_CAPACITY, "rtr_icp_multi: scratch carve");
+  float h = params->cell_size;
+  if (!(h > 0.f)) h = params->max_corr_dist > 0.f ? 0.5f * params->max_corr_dist : -1.f;
+  ProfScope ps(ctx, st, "icp_multi");
+  grid_build(gb, reinterpret_cast<const float4*>(d_tgt), n_tgt, nullptr, h, st);
+  bbox_build(src_meta, reinterpret_cast<const float4*>(d_src), n_src, st);
+  std::vector<IcpSpec> specs((size_t)n_problems);
+  const float r = params->max_corr_dist;
+  for (int k = 0; k < n_problems; ++k) {
+    IcpDev& a = specs[(size_t)k].dev;
+    memset(&a, 0, sizeof(a));
+    a.grid = grid_dev(gb);
+    a.src_meta = src_meta;
+    a.src = reinterpret_cast<const float4*>(d_src);
+    a.src_idx = nullptr;
+    a.n_src = n_src;
+    a.max_it = params->max_iterations;
+    a.r2max = (r > 0.f && r < 1e18f) ? r * r : __builtin_inff();
+    a.eps_t = params->transformation_epsilon;
+    a.eps_r = params->rotation_epsilon;
+    for (int e = 0; e < 16; ++e) a.init[e] = (e % 5) == 0 ? 1.0 : 0.0;
+    a.result = d_results + k;
+    specs[(size_t)k].init_dev = d_init_poses ? d_init_poses + 16 * (size_t)k : nullptr;
+  }
+  return icp_multi(ctx, s, specs, st);
+}
+
 rtr_status rtr_icp_host(rtr_context* ctx, const float* h_src, int n_src, const float* h_tgt,
                         int n_tgt, const rtr_icp_params* params, const double* h_init_pose,
                         rtr_icp_result* h_result) {

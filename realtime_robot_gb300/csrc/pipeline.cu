@@ -955,4 +955,37 @@ rtr_status rtr_recognize_host(rtr_context* ctx, const rtr_model* model, const fl
   return rtr_context_check(ctx, st);
 }
 
+rtr_status rtr_pose_inliers(rtr_context* ctx, const float* d_model, int n_model, const float* d_scene, int n_scene,
+                            const double* d_poses, int n_poses, float radius, int32_t* d_counts,
+                            rtr_stream_t stream) {
+  RTR_CHECK_ARG(ctx && n_model >= 0 && n_scene >= 0 && n_poses >= 0, "rtr_pose_inliers: bad arguments");
+  RTR_CHECK_ARG(radius > 0.f && radius < 1.0e18f, "rtr_pose_inliers: radius must be finite and > 0");
+  if (n_poses == 0) return RTR_OK;
+  RTR_CHECK_ARG(d_poses && d_counts, "rtr_pose_inliers: NULL poses or counts");
+  cudaStream_t st = (cudaStream_t)stream;
+  RTR_CUDA(cudaSetDevice(ctx->device));
+  if (n_model == 0 || n_scene == 0) {
+    RTR_CUDA(cudaMemsetAsync(d_counts, 0, sizeof(int32_t) * (size_t)n_poses, st));
+    return RTR_OK;
+  }
+  RTR_CHECK_ARG(d_model && d_scene, "rtr_pose_inliers: NULL model or scene");
+  const unsigned cap = default_cell_cap(n_scene);
+  ScratchPlan plan;
+  grid_plan(plan, n_scene, cap);
+  plan.add<float>(n_poses);
+  Scratch s;
+  RTR_TRY(ensure_scratch(ctx, plan.bytes, st, &s));
+  GridBufs gb;
+  if (!grid_take(s, n_scene, cap, &gb)) return fail(RTR_ERR_CAPACITY, "rtr_pose_inliers: scratch");
+  float* score = s.take<float>(n_poses);
+  if (!score) return fail(RTR_ERR_CAPACITY, "rtr_pose_inliers: scratch");
+  ProfScope ps(ctx, st, "pose_inliers");
+  // a cell 1.5 x the radius: the counts take the 27-cell existence search
+  grid_build(gb, reinterpret_cast<const float4*>(d_scene), n_scene, nullptr, 1.5f * radius, st);
+  RTR_TRY(hv_score(grid_dev(gb), reinterpret_cast<const float4*>(d_model), n_model, 1, d_poses, n_poses, nullptr,
+                   radius * radius, d_counts, score, st));
+  RTR_CUDA(cudaGetLastError());
+  return RTR_OK;
+}
+
 }  // extern "C"

@@ -122,3 +122,41 @@ def test_icp_near_cell_search_same_correspondences(ctx, rtr, seed):
         corr = tc_n.cpu().numpy()[: r["iterations"]]
         for k in range(r["iterations"]):
             assert np.array_equal(corr[k], ocorr[k]), k
+
+
+def test_icp_multi_equals_oracle_refinement(ctx, rtr):
+    """rtr_icp_multi: independent problems from several initial poses over one
+    target grid, against the oracle's multi-problem ICP (the recognition's
+    refinement) and against one-problem runs of the same kernel."""
+    src, tgt, T = rtr.config0_pair(5, 6000)
+    inits = []
+    for k in range(6):
+        E = np.eye(4)
+        E[:3, 3] = T[:3, 3] + np.float64(0.01) * np.array([k % 3 - 1, (k // 3) - 0.5, 0.2 * k])
+        E[:3, :3] = T[:3, :3]
+        inits.append(E)
+    inits = np.array(inits)
+    got = ctx.icp_multi(_dev(src), _dev(tgt), inits, 30, 0.02, cell_size=0.03)
+    g = O.Grid(tgt, 0.03)
+    ref = g.icp_multi(src, 30, 0.02, inits)
+    g.close()
+    for a, b in zip(got, ref):
+        assert a["status"] == 0 and a["iterations"] == 30
+        dt, dr = O.pose_error(a["pose"], b["pose"])
+        assert dt < 1e-5 and dr < 1e-5, (dt, dr)
+        assert abs(a["n_corr"] - b["n_corr"]) <= 2
+
+
+def test_pose_inliers_equals_oracle(ctx, rtr):
+    """rtr_pose_inliers: per pose, the model points within r of a scene point,
+    as the oracle's grid counts them."""
+    src, tgt, T = rtr.config0_pair(6, 5000)
+    poses = np.array([T, np.eye(4), T @ np.diag([1.0, 1.0, 1.0, 1.0])])
+    poses[2][:3, 3] += 0.015
+    import torch
+    for r in (0.005, 0.02):
+        cnt = ctx.pose_inliers(_dev(src), _dev(tgt), torch.from_numpy(poses), r).cpu().numpy()
+        g = O.Grid(tgt, 1.5 * r)
+        frac = g.inlier_fraction(src, 1, poses.reshape(-1, 16), r)
+        g.close()
+        assert np.array_equal(cnt, np.rint(frac * src.shape[0]).astype(np.int32)), (cnt, frac)
