@@ -400,18 +400,67 @@ __device__ __forceinline__ void shot_bins(float pos, int nb, bool circular, int&
         }                                                                                        \
       }
 
+// The support is gathered once, in pass 1, into a per-warp list in shared
+// memory (SHOT_CAP entries: offset from the keypoint and distance, normal);
+// passes 2 and 3 read the list.  Cells whose box lies beyond R are not
+// walked.  A keypoint with more support points than the list holds walks
+// the cells again in passes 2 and 3 (same sums, another order).
+constexpr int SHOT_CAP = 192;
+
+__device__ __forceinline__ float shot_cell_d2(const GridView& g, float4 q, int x, int y, int z) {
+  const float lx = g.ox + (float)x * g.h, ly = g.oy + (float)y * g.h, lz = g.oz + (float)z * g.h;
+  const float dx = fmaxf(fmaxf(lx - q.x, q.x - (lx + g.h)), 0.f);
+  const float dy = fmaxf(fmaxf(ly - q.y, q.y - (ly + g.h)), 0.f);
+  const float dz = fmaxf(fmaxf(lz - q.z, q.z - (lz + g.h)), 0.f);
+  return dx * dx + dy * dy + dz * dz;
+}
+
+// One support point's contribution to the histogram (16 interpolated bins).
+__device__ __forceinline__ void shot_add(float* H, float dx, float dy, float dz, float d, float cs, float R,
+                                         float X0, float X1, float X2, float Y0, float Y1, float Y2, float Z0,
+                                         float Z1, float Z2) {
+  const float PI = 3.14159265358979f;
+  const float lx = dx * X0 + dy * X1 + dz * X2;
+  const float ly = dx * Y0 + dy * Y1 + dz * Y2;
+  const float lz = dx * Z0 + dy * Z1 + dz * Z2;
+  cs = fminf(fmaxf(cs, -1.f), 1.f);
+  const float az = atan2f(ly, lx);
+  const float el = atan2f(lz, sqrtf(lx * lx + ly * ly));
+  int cb[2], ab[2], eb[2], rb[2];
+  float cw[2], aw[2], ew[2], rw[2];
+  shot_bins((cs + 1.f) * 5.5f - 0.5f, 11, false, cb[0], cw[0], cb[1], cw[1]);
+  shot_bins((az + PI) * (8.f / (2.f * PI)) - 0.5f, 8, true, ab[0], aw[0], ab[1], aw[1]);
+  shot_bins((el + 0.5f * PI) * (2.f / PI) - 0.5f, 2, false, eb[0], ew[0], eb[1], ew[1]);
+  shot_bins(d / R * 2.f - 0.5f, 2, false, rb[0], rw[0], rb[1], rw[1]);
+#pragma unroll
+  for (int i0 = 0; i0 < 2; ++i0)
+#pragma unroll
+    for (int i1 = 0; i1 < 2; ++i1)
+#pragma unroll
+      for (int i2 = 0; i2 < 2; ++i2)
+#pragma unroll
+        for (int i3 = 0; i3 < 2; ++i3) {
+          const float w = rw[i0] * ew[i1] * aw[i2] * cw[i3];
+          if (w != 0.f) atomicAdd(&H[((rb[i0] * 2 + eb[i1]) * 8 + ab[i2]) * 11 + cb[i3]], w);
+        }
+}
+
 __global__ void __launch_bounds__(SHOT_WARPS * 32) k_shot(GridDev gd, const float4* __restrict__ pts,
                                                           const float4* __restrict__ nrm,
                                                           const int* __restrict__ keys, int nk_host,
                                                           const int* d_nk, float R,
                                                           float* __restrict__ desc, float* __restrict__ lrf) {
   __shared__ float hist[SHOT_WARPS][352];
+  __shared__ float4 s_off[SHOT_WARPS][SHOT_CAP];  // (dx, dy, dz, d)
+  __shared__ float4 s_nrm[SHOT_WARPS][SHOT_CAP];  // normal
   const GridView g = load_view(gd);
   const int nk_total = cnt_of(nk_host, d_nk);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const float R2 = __fmul_rn(R, R);
-  const float PI = 3.14159265358979f;
+  const float cell_r2 = R2 * 1.0001f + 1e-12f;  // a cell is walked when its box is within R (with a margin)
   float* H = hist[wid];
+  float4* SO = s_off[wid];
+  float4* SN = s_nrm[wid];
   for (int kk = blockIdx.x * SHOT_WARPS + wid; kk < nk_total; kk += gridDim.x * SHOT_WARPS) {
     const int key = keys[kk];
     const float4 kp = pts[key];
@@ -419,14 +468,44 @@ __global__ void __launch_bounds__(SHOT_WARPS * 32) k_shot(GridDev gd, const floa
     const int cx = min(max(q_cell(kp.x, g.ox, g.inv_h), 0), g.nx - 1);
     const int cy = min(max(q_cell(kp.y, g.oy, g.inv_h), 0), g.ny - 1);
     const int cz = min(max(q_cell(kp.z, g.oz, g.inv_h), 0), g.nz - 1);
-    // pass 1: weighted covariance
+    // pass 1: weighted covariance, and the support gathered in walk order
     float m0 = 0.f, m1 = 0.f, m2 = 0.f, m3 = 0.f, m4 = 0.f, m5 = 0.f;
-    SHOT_FOR_SUPPORT({
-      const float w = R - sqrtf(d2);
-      const float dx = q.x - kp.x, dy = q.y - kp.y, dz = q.z - kp.z;
-      m0 += w * dx * dx; m1 += w * dx * dy; m2 += w * dx * dz;
-      m3 += w * dy * dy; m4 += w * dy * dz; m5 += w * dz * dz;
-    })
+    int ns = 0;
+    for (int z = max(cz - 1, 0); z <= min(cz + 1, g.nz - 1); ++z)
+      for (int y = max(cy - 1, 0); y <= min(cy + 1, g.ny - 1); ++y)
+        for (int x = max(cx - 1, 0); x <= min(cx + 1, g.nx - 1); ++x) {
+          if (shot_cell_d2(g, kp, x, y, z) > cell_r2) continue;
+          const uint2 c = g.cells[((unsigned)z * (unsigned)g.ny + (unsigned)y) * (unsigned)g.nx + (unsigned)x];
+          for (unsigned j0 = c.x; j0 < c.y; j0 += 32) {
+            const unsigned j = j0 + (unsigned)lane;
+            bool in = false;
+            float4 q = kp, qn = nk;
+            float d2 = 0.f;
+            if (j < c.y) {
+              q = g.pts[j];
+              d2 = dist2_exact(kp, q);
+              if (d2 <= R2) {
+                qn = nrm[pt_index(q)];
+                const float facing =
+                    __fadd_rn(__fadd_rn(__fmul_rn(qn.x, nk.x), __fmul_rn(qn.y, nk.y)), __fmul_rn(qn.z, nk.z));
+                in = facing >= SHOT_FACING;
+              }
+            }
+            const float dx = q.x - kp.x, dy = q.y - kp.y, dz = q.z - kp.z;
+            if (in) {
+              const float w = R - sqrtf(d2);
+              m0 += w * dx * dx; m1 += w * dx * dy; m2 += w * dx * dz;
+              m3 += w * dy * dy; m4 += w * dy * dz; m5 += w * dz * dz;
+            }
+            const unsigned bal = __ballot_sync(0xffffffffu, in);
+            const int slot = ns + __popc(bal & lanemask_lt());
+            if (in && slot < SHOT_CAP) {
+              SO[slot] = make_float4(dx, dy, dz, sqrtf(d2));
+              SN[slot] = qn;
+            }
+            ns += __popc(bal);
+          }
+        }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       m0 += __shfl_xor_sync(0xffffffffu, m0, o);
@@ -436,6 +515,8 @@ __global__ void __launch_bounds__(SHOT_WARPS * 32) k_shot(GridDev gd, const floa
       m4 += __shfl_xor_sync(0xffffffffu, m4, o);
       m5 += __shfl_xor_sync(0xffffffffu, m5, o);
     }
+    __syncwarp();
+    const bool listed = ns <= SHOT_CAP;
     const float M[9] = {m0, m1, m2, m1, m3, m4, m2, m4, m5};
     float ev[3], V[9];
     eig3_exact(M, ev, V);
@@ -443,11 +524,19 @@ __global__ void __launch_bounds__(SHOT_WARPS * 32) k_shot(GridDev gd, const floa
     // pass 2: signs
     int px = 0, nx = 0;
     float zn = 0.f;
-    SHOT_FOR_SUPPORT({
-      const float dx = q.x - kp.x, dy = q.y - kp.y, dz = q.z - kp.z;
-      if (dx * X0 + dy * X1 + dz * X2 >= 0.f) ++px; else ++nx;
-      zn += (R - sqrtf(d2)) * (qn.x * Z0 + qn.y * Z1 + qn.z * Z2);
-    })
+    if (listed) {
+      for (int i = lane; i < ns; i += 32) {
+        const float4 o = SO[i], qn = SN[i];
+        if (o.x * X0 + o.y * X1 + o.z * X2 >= 0.f) ++px; else ++nx;
+        zn += (R - o.w) * (qn.x * Z0 + qn.y * Z1 + qn.z * Z2);
+      }
+    } else {
+      SHOT_FOR_SUPPORT({
+        const float dx = q.x - kp.x, dy = q.y - kp.y, dz = q.z - kp.z;
+        if (dx * X0 + dy * X1 + dz * X2 >= 0.f) ++px; else ++nx;
+        zn += (R - sqrtf(d2)) * (qn.x * Z0 + qn.y * Z1 + qn.z * Z2);
+      })
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       px += __shfl_xor_sync(0xffffffffu, px, o);
@@ -463,37 +552,20 @@ __global__ void __launch_bounds__(SHOT_WARPS * 32) k_shot(GridDev gd, const floa
     }
     for (int b = lane; b < 352; b += 32) H[b] = 0.f;
     __syncwarp();
-    // pass 3: histogram
-    SHOT_FOR_SUPPORT({
-      if (d2 > 0.f) {
-        const float dx = q.x - kp.x, dy = q.y - kp.y, dz = q.z - kp.z;
-        const float lx = dx * X0 + dy * X1 + dz * X2;
-        const float ly = dx * Y0 + dy * Y1 + dz * Y2;
-        const float lz = dx * Z0 + dy * Z1 + dz * Z2;
-        float cs = qn.x * Z0 + qn.y * Z1 + qn.z * Z2;
-        cs = fminf(fmaxf(cs, -1.f), 1.f);
-        const float d = sqrtf(d2);
-        const float az = atan2f(ly, lx);
-        const float el = atan2f(lz, sqrtf(lx * lx + ly * ly));
-        int cb[2], ab[2], eb[2], rb[2];
-        float cw[2], aw[2], ew[2], rw[2];
-        shot_bins((cs + 1.f) * 5.5f - 0.5f, 11, false, cb[0], cw[0], cb[1], cw[1]);
-        shot_bins((az + PI) * (8.f / (2.f * PI)) - 0.5f, 8, true, ab[0], aw[0], ab[1], aw[1]);
-        shot_bins((el + 0.5f * PI) * (2.f / PI) - 0.5f, 2, false, eb[0], ew[0], eb[1], ew[1]);
-        shot_bins(d / R * 2.f - 0.5f, 2, false, rb[0], rw[0], rb[1], rw[1]);
-#pragma unroll
-        for (int i0 = 0; i0 < 2; ++i0)
-#pragma unroll
-          for (int i1 = 0; i1 < 2; ++i1)
-#pragma unroll
-            for (int i2 = 0; i2 < 2; ++i2)
-#pragma unroll
-              for (int i3 = 0; i3 < 2; ++i3) {
-                const float w = rw[i0] * ew[i1] * aw[i2] * cw[i3];
-                if (w != 0.f) atomicAdd(&H[((rb[i0] * 2 + eb[i1]) * 8 + ab[i2]) * 11 + cb[i3]], w);
-              }
+    // pass 3: histogram (the keypoint itself, d = 0, does not vote)
+    if (listed) {
+      for (int i = lane; i < ns; i += 32) {
+        const float4 o = SO[i], qn = SN[i];
+        if (o.w > 0.f)
+          shot_add(H, o.x, o.y, o.z, o.w, qn.x * Z0 + qn.y * Z1 + qn.z * Z2, R, X0, X1, X2, Y0, Y1, Y2, Z0, Z1, Z2);
       }
-    })
+    } else {
+      SHOT_FOR_SUPPORT({
+        if (d2 > 0.f)
+          shot_add(H, q.x - kp.x, q.y - kp.y, q.z - kp.z, sqrtf(d2), qn.x * Z0 + qn.y * Z1 + qn.z * Z2, R, X0, X1, X2,
+                   Y0, Y1, Y2, Z0, Z1, Z2);
+      })
+    }
     __syncwarp();
     float ss = 0.f;
     for (int b = lane; b < 352; b += 32) ss += H[b] * H[b];
