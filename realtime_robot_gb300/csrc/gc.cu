@@ -261,6 +261,9 @@ struct GcCoop {
 };
 
 __device__ __forceinline__ bool sbit(const unsigned* s, int i) { return (s[i >> 5] >> (i & 31)) & 1u; }
+__device__ __forceinline__ uint32_t smem_u32_gc(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
 
 // Grid barrier (all blocks co-resident: cooperative launch).  Bounded: a
 // block that waits longer than the budget records RTR_ERR_TIMEOUT and
@@ -436,8 +439,8 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
   extern __shared__ unsigned s_taken[];  // copy of the taken bitset
   __shared__ float4 mem_m[GC_WARPS][GC_MAXS], mem_s[GC_WARPS][GC_MAXS];
   __shared__ int s_slot[GC_WARPS][GC_PEND];
-  __shared__ int s_bmem[32][33];  // walk: first 32 members of the next 32 seeds (padded rows)
   __shared__ int s_rec[GC_MAXS];  // walk: members of a set recomputed in place
+  __shared__ int s_pf[3][32][9];  // walk: sizes and first 8 members of the next batches (cp.async ring)
   __shared__ int s_pos, s_done, s_ok, s_win;
   __shared__ float s_r2max;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -669,29 +672,40 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
       bool done = false, stop = false;
       int p = pos;
       const int wend = min(pos + win, g.C);
-      // the batch's sizes and first 32 members are loaded one batch ahead:
-      // they do not change during the walk (only the taken bits do), and the
-      // walk goes on to the next batch only as a whole
-      int nbc = min(32, wend - p);
-      int n_pre = (p < wend && lane < nbc) ? __ldcg(g.set_size + p + lane) : 0;
-      int mv[32];
+      // each lane's seed size and first 8 members are copied two batches
+      // ahead into a 3-slot shared-memory ring with cp.async (a slot past the
+      // set holds a stale member, which the size masks): they do not change
+      // during the walk (only the taken bits do), and the walk goes on to
+      // the next batch of 32 only as a whole
+      auto prefetch = [&](int pb, int slot) {
+        if (pb + lane < wend) {
+          const int* src = g.set_mem + (size_t)(pb + lane) * maxs;
 #pragma unroll
-      for (int t = 0; t < 32; ++t) mv[t] = (p < wend && t < nbc) ? __ldcg(g.set_mem + (size_t)(p + t) * maxs + lane) : 0;
-      while (p < wend && !stop) {
-        const int nb = nbc;
-        const int my = p + lane;
-        const int n_l = n_pre;
-#pragma unroll
-        for (int t = 0; t < 32; ++t) s_bmem[t][lane] = mv[t];  // member `lane` of seed p + t
-        __syncwarp();
-        {
-          const int pn = p + nb;
-          nbc = min(32, wend - pn);
-          n_pre = (pn < wend && lane < nbc) ? __ldcg(g.set_size + pn + lane) : 0;
-#pragma unroll
-          for (int t = 0; t < 32; ++t)
-            mv[t] = (pn < wend && t < nbc) ? __ldcg(g.set_mem + (size_t)(pn + t) * maxs + lane) : 0;
+          for (int k = 0; k < 8; ++k)
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32_gc(&s_pf[slot][lane][k])),
+                         "l"(src + k)
+                         : "memory");
+          asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32_gc(&s_pf[slot][lane][8])),
+                       "l"(g.set_size + pb + lane)
+                       : "memory");
         }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+      };
+      int ring = 0;
+      prefetch(p, 0);
+      prefetch(p + 32, 1);
+      while (p < wend && !stop) {
+        const int nb = min(32, wend - p);
+        const int my = p + lane;
+        prefetch(p + 64, (ring + 2) % 3);
+        asm volatile("cp.async.wait_group 2;" ::: "memory");  // this batch's copies are in
+        __syncwarp();
+        const bool have = lane < nb;
+        const int n_l = have ? s_pf[ring][lane][8] : 0;
+        int m_cur[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) m_cur[k] = s_pf[ring][lane][k];
+        ring = ring == 2 ? 0 : ring + 1;
         const int ns_l = min(n_l, maxs);
         int cursor = 0;
         for (;;) {
@@ -699,18 +713,26 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
           if (lane >= cursor && lane < nb) {
             taken_l = sbit(s_taken, my);
             if (!taken_l) {
-              // the first 8 members' taken bits in two rounds of independent
-              // loads (a slot past the set reads the seed's own bit: clear)
-              int mb8[8];
-#pragma unroll
-              for (int k = 0; k < 8; ++k) mb8[k] = k < ns_l ? s_bmem[lane][k] : my;
+              // the first 8 members' taken bits in one round of independent
+              // shared-memory loads (a slot past the set reads the seed's own
+              // bit: clear)
               unsigned acc = 0u;
 #pragma unroll
-              for (int k = 0; k < 8; ++k) acc |= s_taken[mb8[k] >> 5] >> (mb8[k] & 31);
+              for (int k = 0; k < 8; ++k) {
+                const int mb = k < ns_l ? m_cur[k] : my;
+                acc |= s_taken[mb >> 5] >> (mb & 31);
+              }
               stale_l = (acc & 1u) != 0u;
-              for (int k = 8; k < ns_l && !stale_l; ++k) {
-                const int mb = k < 32 ? s_bmem[lane][k] : __ldcg(g.set_mem + (size_t)my * maxs + k);
-                stale_l = sbit(s_taken, mb);
+              // a longer set: its other members eight independent loads at a time
+              for (int k0 = 8; k0 < ns_l && !stale_l; k0 += 8) {
+                int mbk[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j)
+                  mbk[j] = k0 + j < ns_l ? __ldcg(g.set_mem + (size_t)my * maxs + k0 + j) : my;
+                unsigned a2 = 0u;
+#pragma unroll
+                for (int j = 0; j < 8; ++j) a2 |= s_taken[mbk[j] >> 5] >> (mbk[j] & 31);
+                stale_l = (a2 & 1u) != 0u;
               }
             }
           }
@@ -761,8 +783,15 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
             p += f;
             break;
           }
+          // the committing seed's first 8 members from lane f's registers
+          int mine = 0;
+#pragma unroll
+          for (int k = 0; k < 8; ++k) {
+            const int v = __shfl_sync(0xffffffffu, m_cur[k], f);
+            if (lane == k) mine = v;
+          }
           for (int k = lane; k < nf; k += 32) {
-            const int mb = k < 32 ? s_bmem[f][k] : __ldcg(g.set_mem + (size_t)(p + f) * maxs + k);
+            const int mb = k < 8 ? mine : __ldcg(g.set_mem + (size_t)(p + f) * maxs + k);
             atomicOr(&s_taken[mb >> 5], 1u << (mb & 31));
             c.cl_members[(size_t)ncl * maxs + k] = mb;
           }
@@ -778,6 +807,7 @@ __global__ void __launch_bounds__(GC_WARPS * 32, 2) k_gc_coop(GcDev g, GcCoop c)
         }
         __syncwarp();
       }
+      asm volatile("cp.async.wait_all;" ::: "memory");  // no copy left in flight into the ring
       if (p >= g.C) done = true;
       __syncwarp();
       for (int i = lane; i < nwords; i += 32) g.taken[i] = s_taken[i];

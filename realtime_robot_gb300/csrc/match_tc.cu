@@ -857,6 +857,251 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
   return RTR_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Keypoint-credibility MLP inference on the tensor cores: 352 -> 128 -> 64
+// -> 1 (ReLU, ReLU, sigmoid) with BF16 weights.  Layer 1 is a tcgen05 GEMM:
+// each FP32 descriptor is split into three BF16 parts (hi + mid + lo = x up
+// to the last part's rounding, 2^-24 of |x|), and the three products with
+// the BF16 weights accumulate in FP32 in tensor memory: FP32-level accuracy.
+// The epilogue (thread = row) adds the bias, applies the ReLU, runs layer 2
+// (64 outputs, FP32 FMAs over the 128 inputs in order), the head and the
+// sigmoid, so only the score leaves the CTA.
+// ---------------------------------------------------------------------------
+constexpr int MLP_TC_IN = 352, MLP_TC_H1 = 128, MLP_TC_H2 = 64;
+constexpr int MLP_TC_A_BYTES = TC_BM * TC_KB * 2;     // 8 KB: one part's K-block
+constexpr int MLP_TC_B_BYTES = MLP_TC_H1 * TC_KB * 2;  // 8 KB: W1's K-block
+constexpr int MLP_TC_STAGE_BYTES = 3 * MLP_TC_A_BYTES + MLP_TC_B_BYTES;  // 32 KB
+constexpr int MLP_TC_STAGES = 4;
+constexpr int MLP_TC_SMEM = MLP_TC_STAGES * MLP_TC_STAGE_BYTES + 1024;
+
+// hi / mid / lo BF16 parts of each row, padded to TC_KPAD (zero past 352 and
+// in padding rows); a warp per row, four columns per lane and 16-byte loads.
+__global__ void k_split3_bf16(const float* __restrict__ x, int n_cap_rows, const int* d_n, int n_pad,
+                              __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ mid,
+                              __nv_bfloat16* __restrict__ lo) {
+  const int n = d_n ? min(*d_n, n_cap_rows) : n_cap_rows;
+  const int lane = threadIdx.x & 31;
+  for (int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < n_pad; r += gridDim.x * (blockDim.x >> 5)) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int c4 = lane + 32 * k;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (r < n && c4 < MLP_TC_IN / 4) v = __ldg(reinterpret_cast<const float4*>(x + (size_t)r * MLP_TC_IN) + c4);
+      const float e[4] = {v.x, v.y, v.z, v.w};
+      unsigned short h[4], m[4], l[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const __nv_bfloat16 bh = __float2bfloat16_rn(e[j]);
+        const float r1 = e[j] - __bfloat162float(bh);
+        const __nv_bfloat16 bm = __float2bfloat16_rn(r1);
+        const __nv_bfloat16 bl = __float2bfloat16_rn(r1 - __bfloat162float(bm));
+        h[j] = __bfloat16_as_ushort(bh);
+        m[j] = __bfloat16_as_ushort(bm);
+        l[j] = __bfloat16_as_ushort(bl);
+      }
+      const size_t o = (size_t)r * (TC_KPAD / 4) + c4;
+      reinterpret_cast<uint2*>(hi)[o] = make_uint2(h[0] | ((unsigned)h[1] << 16), h[2] | ((unsigned)h[3] << 16));
+      reinterpret_cast<uint2*>(mid)[o] = make_uint2(m[0] | ((unsigned)m[1] << 16), m[2] | ((unsigned)m[3] << 16));
+      reinterpret_cast<uint2*>(lo)[o] = make_uint2(l[0] | ((unsigned)l[1] << 16), l[2] | ((unsigned)l[3] << 16));
+    }
+  }
+}
+
+__device__ __forceinline__ uint32_t umma_idesc_n(int n) {
+  uint32_t d = 0;
+  d |= 1u << 4;                        // D format F32
+  d |= 1u << 7;                        // A BF16
+  d |= 1u << 10;                       // B BF16
+  d |= (uint32_t)(n >> 3) << 17;       // N
+  d |= (uint32_t)(TC_BM >> 4) << 24;   // M
+  return d;
+}
+
+struct MlpTcArgs {
+  int n_cap;
+  const int* d_n;
+  const float* b1;         // [128]
+  const __nv_bfloat16* w2;  // [64][128]
+  const float* b2;         // [64]
+  const __nv_bfloat16* w3;  // [64]
+  const float* b3;         // [1]
+  float* score;            // [n]
+  int* status;
+  long long spin_limit;
+};
+
+__global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(const __grid_constant__ CUtensorMap m_hi,
+                                                          const __grid_constant__ CUtensorMap m_mid,
+                                                          const __grid_constant__ CUtensorMap m_lo,
+                                                          const __grid_constant__ CUtensorMap m_w1, MlpTcArgs a) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  __shared__ uint64_t full_bar[MLP_TC_STAGES], empty_bar[MLP_TC_STAGES], acc_full, drain_bar;
+  __shared__ uint32_t tmem_base;
+  __shared__ int abort_flag;
+  __shared__ float s_w2[MLP_TC_H1][MLP_TC_H2];  // [input c][output j]
+  __shared__ float s_b1[MLP_TC_H1], s_b2[MLP_TC_H2], s_w3[MLP_TC_H2];
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n = a.d_n ? min(*a.d_n, a.n_cap) : a.n_cap;
+  const int q0 = blockIdx.x * TC_BM;
+  if (q0 >= n) return;  // uniform per CTA, before any barrier or TMEM use
+
+  for (int i = threadIdx.x; i < MLP_TC_H1 * MLP_TC_H2; i += blockDim.x) {
+    const int j = i / MLP_TC_H1, c = i - j * MLP_TC_H1;  // w2 row-major [j][c]
+    s_w2[c][j] = __bfloat162float(a.w2[i]);
+  }
+  for (int i = threadIdx.x; i < MLP_TC_H1; i += blockDim.x) s_b1[i] = a.b1[i];
+  for (int i = threadIdx.x; i < MLP_TC_H2; i += blockDim.x) {
+    s_b2[i] = a.b2[i];
+    s_w3[i] = __bfloat162float(a.w3[i]);
+  }
+  if (threadIdx.x == 0) {
+    abort_flag = 0;
+    for (int s = 0; s < MLP_TC_STAGES; ++s) {
+      mbar_init(&full_bar[s], 1);
+      mbar_init(&empty_bar[s], 1);
+    }
+    mbar_init(&acc_full, 1);
+    mbar_init(&drain_bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 5) {  // 128 TMEM columns: one 128 x 128 FP32 accumulator
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(smem_u32(&tmem_base)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base;
+  volatile int* abort = &abort_flag;
+  const long long lim = a.spin_limit;
+  int issued = 0;
+
+  if (warp == 4) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      int kb = 0;
+      for (; kb < TC_NKB && !*abort; ++kb) {
+        const int s = kb % MLP_TC_STAGES;
+        const uint32_t ph = (uint32_t)(kb / MLP_TC_STAGES) & 1u;
+        if (kb >= MLP_TC_STAGES && !mbar_wait(&empty_bar[s], ph ^ 1u, abort, lim)) break;
+        uint8_t* st = smem + s * MLP_TC_STAGE_BYTES;
+        mbar_expect_tx(&full_bar[s], MLP_TC_STAGE_BYTES);
+        tma_load_2d(st, &m_hi, &full_bar[s], kb * TC_KB, q0);
+        tma_load_2d(st + MLP_TC_A_BYTES, &m_mid, &full_bar[s], kb * TC_KB, q0);
+        tma_load_2d(st + 2 * MLP_TC_A_BYTES, &m_lo, &full_bar[s], kb * TC_KB, q0);
+        tma_load_2d(st + 3 * MLP_TC_A_BYTES, &m_w1, &full_bar[s], kb * TC_KB, 0);
+      }
+      issued = kb;
+    }
+  } else if (warp == 5) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      const uint32_t idesc = umma_idesc_n(MLP_TC_H1);
+      bool ok = true;
+      for (int kb = 0; kb < TC_NKB; ++kb) {
+        const int s = kb % MLP_TC_STAGES;
+        const uint32_t ph = (uint32_t)(kb / MLP_TC_STAGES) & 1u;
+        if (!mbar_wait(&full_bar[s], ph, abort, lim)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t base = smem_u32(smem + s * MLP_TC_STAGE_BYTES);
+        const uint32_t ah = base, am = base + MLP_TC_A_BYTES, al = base + 2 * MLP_TC_A_BYTES,
+                       bw = base + 3 * MLP_TC_A_BYTES;
+#pragma unroll
+        for (int k = 0; k < TC_KB / 16; ++k) {
+          const uint32_t off = (uint32_t)k * 32;  // 16 bf16 along K inside the swizzle row
+          const uint32_t acc0 = (kb > 0 || k > 0) ? 1u : 0u;
+          umma_f16(tmem, umma_desc(ah + off), umma_desc(bw + off), idesc, acc0);
+          umma_f16(tmem, umma_desc(am + off), umma_desc(bw + off), idesc, 1u);
+          umma_f16(tmem, umma_desc(al + off), umma_desc(bw + off), idesc, 1u);
+        }
+        umma_commit(&empty_bar[s]);
+      }
+      if (ok) umma_commit(&acc_full);
+    }
+  } else {
+    // ---------------- epilogue: warps 0-3, thread = row ----------------
+    const int row = warp * 32 + lane;
+    const int q = q0 + row;
+    if (mbar_wait(&acc_full, 0u, abort, lim)) {
+      tc_fence_after();
+      float h2[MLP_TC_H2];
+#pragma unroll
+      for (int j = 0; j < MLP_TC_H2; ++j) h2[j] = 0.f;
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+      for (int c0 = 0; c0 < MLP_TC_H1; c0 += 32) {
+        float v[32];
+        tmem_ld32(taddr + (uint32_t)c0, v);
+#pragma unroll 4
+        for (int i = 0; i < 32; ++i) {
+          const float h = fmaxf(v[i] + s_b1[c0 + i], 0.f);
+#pragma unroll
+          for (int j = 0; j < MLP_TC_H2; ++j) h2[j] = fmaf(h, s_w2[c0 + i][j], h2[j]);
+        }
+      }
+      float z = 0.f;
+#pragma unroll
+      for (int j = 0; j < MLP_TC_H2; ++j) z = fmaf(fmaxf(h2[j] + s_b2[j], 0.f), s_w3[j], z);
+      z += *a.b3;
+      if (q < n) a.score[q] = 1.f / (1.f + __expf(-z));
+    }
+  }
+  __syncthreads();
+  if (abort_flag) {
+    if (warp == 5 && lane == 0) {
+      umma_commit(&drain_bar);
+      mbar_drain(&drain_bar, 0u);
+    }
+    if (warp == 4 && lane == 0)
+      for (int i = issued > MLP_TC_STAGES ? issued - MLP_TC_STAGES : 0; i < issued; ++i)
+        mbar_drain(&full_bar[i % MLP_TC_STAGES], (uint32_t)(i / MLP_TC_STAGES) & 1u);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (abort_flag && threadIdx.x == 0) atomicExch(a.status, (int)RTR_ERR_TIMEOUT);
+  if (warp == 5) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem));
+  }
+}
+
+size_t mlp_tc_bytes(int n_cap) {
+  const size_t nqp = (size_t)(((n_cap > 0 ? n_cap : 1) + TC_BM - 1) / TC_BM) * TC_BM;
+  ScratchPlan p;
+  for (int i = 0; i < 3; ++i) p.add<__nv_bfloat16>(nqp * TC_KPAD);
+  return p.bytes;
+}
+
+// Scores of rows X[0 .. *d_n) (n_cap rows of capacity).  w1pad: W1 as BF16
+// [128][TC_KPAD] with zero columns past 352; theta_b1/b2/b3: the FP32 biases.
+rtr_status mlp_tc_score(rtr_context* ctx, Scratch& s, const float* X, int n_cap, const int* d_n,
+                        const __nv_bfloat16* w1pad, const float* b1, const __nv_bfloat16* w2, const float* b2,
+                        const __nv_bfloat16* w3, const float* b3, float* score, cudaStream_t st) {
+  if (n_cap <= 0) return RTR_OK;
+  const int nqp = ((n_cap + TC_BM - 1) / TC_BM) * TC_BM;
+  __nv_bfloat16* hi = s.take<__nv_bfloat16>((size_t)nqp * TC_KPAD);
+  __nv_bfloat16* mid = s.take<__nv_bfloat16>((size_t)nqp * TC_KPAD);
+  __nv_bfloat16* lo = s.take<__nv_bfloat16>((size_t)nqp * TC_KPAD);
+  if (!lo) return fail(RTR_ERR_CAPACITY, "mlp_tc: scratch");
+  int sb = (nqp + 7) / 8;
+  if (sb > 152 * 16) sb = 152 * 16;
+  k_split3_bf16<<<sb, 256, 0, st>>>(X, n_cap, d_n, nqp, hi, mid, lo);
+  CUtensorMap mh, mm, ml, mw;
+  if (!make_map(&mh, hi, nqp, TC_BM) || !make_map(&mm, mid, nqp, TC_BM) || !make_map(&ml, lo, nqp, TC_BM) ||
+      !make_map(&mw, w1pad, MLP_TC_H1, MLP_TC_H1))
+    return fail(RTR_ERR_CUDA, "mlp_tc: cuTensorMapEncodeTiled failed");
+  RTR_CUDA(cudaFuncSetAttribute(k_mlp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, MLP_TC_SMEM));
+  MlpTcArgs a{n_cap, d_n, b1, w2, b2, w3, b3, score, ctx->d_status, tc_spin_limit(ctx)};
+  k_mlp_tc<<<nqp / TC_BM, TC_THREADS, MLP_TC_SMEM, st>>>(mh, mm, ml, mw, a);
+  RTR_LAUNCHED(2);
+  RTR_CUDA(cudaGetLastError());
+  return RTR_OK;
+}
+
 }  // namespace rtr
 
 using namespace rtr;

@@ -24,6 +24,7 @@ struct rtr_mlp {
   int device = 0;
   float* theta = nullptr;          // [RTR_MLP_PARAMS] FP32 master weights
   __nv_bfloat16* wbf = nullptr;    // BF16 W1 | W2 | w3
+  __nv_bfloat16* w1pad = nullptr;  // BF16 W1 as [128][384], zero past column 352 (tensor-core inference)
   float* m = nullptr;              // Adam first moment
   float* v = nullptr;              // Adam second moment
   int step = 0;                    // Adam steps taken
@@ -180,10 +181,16 @@ __global__ void k_colsum(const float* __restrict__ X, int n, int cols, float* __
   if (threadIdx.x == 0) out[c] = s[0];
 }
 
-__global__ void k_to_bf16(const float* __restrict__ theta, __nv_bfloat16* __restrict__ wbf) {
+constexpr int W1PAD_K = 384;
+__global__ void k_to_bf16(const float* __restrict__ theta, __nv_bfloat16* __restrict__ wbf,
+                          __nv_bfloat16* __restrict__ w1pad) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < BF_N; i += gridDim.x * blockDim.x) {
     const int src = i < BF_W2 ? OFF_W1 + i : (i < BF_W3 ? OFF_W2 + (i - BF_W2) : OFF_W3 + (i - BF_W3));
     wbf[i] = __float2bfloat16_rn(theta[src]);
+  }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < MLP_H1 * W1PAD_K; i += gridDim.x * blockDim.x) {
+    const int r = i / W1PAD_K, k = i - r * W1PAD_K;
+    w1pad[i] = __float2bfloat16_rn(k < MLP_IN ? theta[OFF_W1 + r * MLP_IN + k] : 0.f);
   }
 }
 
@@ -284,7 +291,7 @@ static void mlp_pass(const rtr_mlp* m, const float* X, const float* y, int n, fl
 }
 
 static void mlp_refresh_bf16(rtr_mlp* m, cudaStream_t st) {
-  k_to_bf16<<<(BF_N + 255) / 256, 256, 0, st>>>(m->theta, m->wbf);
+  k_to_bf16<<<(BF_N + 255) / 256, 256, 0, st>>>(m->theta, m->wbf, m->w1pad);
   RTR_LAUNCHED(1);
 }
 
@@ -315,9 +322,26 @@ static void mlp_host_init(uint64_t seed, float* out) {
   for (int i = 0; i < MLP_H2; ++i) out[OFF_W3 + i] = uni(bw3);
 }
 
+size_t mlp_tc_bytes(int n_cap);
+rtr_status mlp_tc_score(rtr_context* ctx, Scratch& s, const float* X, int n_cap, const int* d_n,
+                        const __nv_bfloat16* w1pad, const float* b1, const __nv_bfloat16* w2, const float* b2,
+                        const __nv_bfloat16* w3, const float* b3, float* score, cudaStream_t st);
+
+// Inference on the tensor cores (match_tc.cu: layer 1 as a tcgen05 GEMM of
+// three BF16 parts of X, layers 2 and 3 in its epilogue) when X is 16-byte
+// aligned; the SIMT passes otherwise.
+static bool mlp_tc_ok(const float* X) { return (reinterpret_cast<uintptr_t>(X) & 15u) == 0; }
+static rtr_status mlp_tc(rtr_context* ctx, Scratch& s, const rtr_mlp* m, const float* X, int n_cap, const int* d_n,
+                         float* score, cudaStream_t st) {
+  const float* th = m->theta;
+  return mlp_tc_score(ctx, s, X, n_cap, d_n, m->w1pad, th + OFF_B1, m->wbf + BF_W2, th + OFF_B2, m->wbf + BF_W3,
+                      th + OFF_B3, score, st);
+}
+
 rtr_status mlp_score_dev(rtr_context* ctx, Scratch& s, const rtr_mlp* m, const float* X, int n, float* score,
                          cudaStream_t st) {
   if (n <= 0) return RTR_OK;
+  if (mlp_tc_ok(X)) return mlp_tc(ctx, s, m, X, n, nullptr, score, st);
   MlpWork w;
   if (!mlp_take(s, n, &w)) return fail(RTR_ERR_CAPACITY, "mlp: scratch");
   (void)ctx;
@@ -332,12 +356,14 @@ size_t mlp_infer_bytes(int n_cap) {
   ScratchPlan p;
   p.add<float>((size_t)(n_cap > 0 ? n_cap : 1) * MLP_H1);
   p.add<float>((size_t)(n_cap > 0 ? n_cap : 1) * MLP_H2);
-  return p.bytes;
+  const size_t tc = mlp_tc_bytes(n_cap);
+  return p.bytes > tc ? p.bytes : tc;
 }
 
-rtr_status mlp_score_rows(Scratch& s, const rtr_mlp* m, const float* X, int n_cap, const int* d_n, float* score,
-                          cudaStream_t st) {
+rtr_status mlp_score_rows(rtr_context* ctx, Scratch& s, const rtr_mlp* m, const float* X, int n_cap, const int* d_n,
+                          float* score, cudaStream_t st) {
   if (n_cap <= 0) return RTR_OK;
+  if (mlp_tc_ok(X)) return mlp_tc(ctx, s, m, X, n_cap, d_n, score, st);
   float* h1 = s.take<float>((size_t)n_cap * MLP_H1);
   float* h2 = s.take<float>((size_t)n_cap * MLP_H2);
   if (!h2) return fail(RTR_ERR_CAPACITY, "mlp: scratch");
@@ -380,10 +406,12 @@ rtr_status rtr_mlp_create(rtr_context* ctx, const float* h_params, uint64_t seed
   m->device = ctx->device;
   if (cudaMalloc(&m->theta, sizeof(float) * N_PARAMS) != cudaSuccess ||
       cudaMalloc(&m->wbf, sizeof(__nv_bfloat16) * BF_N) != cudaSuccess ||
+      cudaMalloc(&m->w1pad, sizeof(__nv_bfloat16) * MLP_H1 * W1PAD_K) != cudaSuccess ||
       cudaMalloc(&m->m, sizeof(float) * N_PARAMS) != cudaSuccess ||
       cudaMalloc(&m->v, sizeof(float) * N_PARAMS) != cudaSuccess) {
     cudaFree(m->theta);
     cudaFree(m->wbf);
+    cudaFree(m->w1pad);
     cudaFree(m->m);
     cudaFree(m->v);
     delete m;
@@ -404,6 +432,7 @@ rtr_status rtr_mlp_destroy(rtr_mlp* m) {
   cudaSetDevice(m->device);
   cudaFree(m->theta);
   cudaFree(m->wbf);
+  cudaFree(m->w1pad);
   cudaFree(m->m);
   cudaFree(m->v);
   delete m;
@@ -439,7 +468,8 @@ rtr_status rtr_mlp_score(rtr_context* ctx, const rtr_mlp* m, const float* d_x, i
   cudaStream_t st = (cudaStream_t)stream;
   RTR_CUDA(cudaSetDevice(ctx->device));
   Scratch s;
-  RTR_TRY(ensure_scratch(ctx, mlp_scratch_bytes(n), st, &s));
+  const size_t need = mlp_scratch_bytes(n) > mlp_tc_bytes(n) ? mlp_scratch_bytes(n) : mlp_tc_bytes(n);
+  RTR_TRY(ensure_scratch(ctx, need, st, &s));
   ProfScope ps(ctx, st, "mlp_score");
   return mlp_score_dev(ctx, s, m, d_x, n, d_score, st);
 }

@@ -41,8 +41,8 @@ rtr_status gc_group_async(rtr_context* ctx, Scratch& s, const float* d_model_kp,
                           const int* d_C, float gc_size, int gc_thresh, int max_clusters, int32_t* d_sizes,
                           double* d_poses, int* d_ncl, cudaStream_t st);
 size_t mlp_infer_bytes(int n_cap);
-rtr_status mlp_score_rows(Scratch& s, const rtr_mlp* m, const float* X, int n_cap, const int* d_n, float* score,
-                          cudaStream_t st);
+rtr_status mlp_score_rows(rtr_context* ctx, Scratch& s, const rtr_mlp* m, const float* X, int n_cap, const int* d_n,
+                          float* score, cudaStream_t st);
 __global__ void k_orient_outward(const float4* __restrict__ pts, float4* __restrict__ nrm, int n_host, const int* d_n,
                                  float rc2, float gap, float len);
 rtr_status gc_group_dev(rtr_context* ctx, Scratch& s, const float* d_model_kp, const float* d_scene_kp,
@@ -689,7 +689,7 @@ static rtr_status scene_stages(rtr_context* ctx, const Scratch& stage, SceneBufs
     uint32_t* v1 = t.take<uint32_t>(n);
     uint32_t* hist = t.take<uint32_t>(radix_hist_entries(n));
     if (!hist) return fail(RTR_ERR_CAPACITY, "rtr_recognize_learned: scratch carve");
-    RTR_TRY(mlp_score_rows(t, mlp, b.desc, n, dKeys, score, st));
+    RTR_TRY(mlp_score_rows(ctx, t, mlp, b.desc, n, dKeys, score, st));
     k_score_keys<<<nb, 256, 0, st>>>(score, dKeys, n, k0);
     uint32_t *ks, *vs;
     radix_sort_pairs(k0, v0, k1, v1, hist, n, n, dKeys, 32, true, st, &ks, &vs);
