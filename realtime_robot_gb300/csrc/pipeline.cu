@@ -689,11 +689,18 @@ static rtr_status scene_stages(rtr_context* ctx, const Scratch& stage, SceneBufs
     uint32_t* v1 = t.take<uint32_t>(n);
     uint32_t* hist = t.take<uint32_t>(radix_hist_entries(n));
     if (!hist) return fail(RTR_ERR_CAPACITY, "rtr_recognize_learned: scratch carve");
-    RTR_TRY(mlp_score_rows(ctx, t, mlp, b.desc, n, dKeys, score, st));
-    k_score_keys<<<nb, 256, 0, st>>>(score, dKeys, n, k0);
-    uint32_t *ks, *vs;
-    radix_sort_pairs(k0, v0, k1, v1, hist, n, n, dKeys, 32, true, st, &ks, &vs);
-    k_mark_top<<<nb, 256, 0, st>>>(vs, dKeys, n, keep, b.flags);
+    {
+      ProfScope ps2(ctx, st, "prune_score");
+      RTR_TRY(mlp_score_rows(ctx, t, mlp, b.desc, n, dKeys, score, st));
+    }
+    {
+      ProfScope ps2(ctx, st, "prune_select");
+      k_score_keys<<<nb, 256, 0, st>>>(score, dKeys, n, k0);
+      uint32_t *ks, *vs;
+      radix_sort_pairs(k0, v0, k1, v1, hist, n, n, dKeys, 32, true, st, &ks, &vs);
+      k_mark_top<<<nb, 256, 0, st>>>(vs, dKeys, n, keep, b.flags);
+    }
+    ProfScope ps2(ctx, st, "prune_compact");
     scan_exclusive(b.flags, b.pos, b.tiles, n, n, nullptr, reinterpret_cast<uint32_t*>(b.cnt + 3), st);
     k_compact_int<<<nb, 256, 0, st>>>(keys, b.flags, b.pos, n, b.keys_p);
     k_compact_rows<<<nblocks(n, 8, 152 * 16), 256, 0, st>>>(b.desc, b.flags, b.pos, dKeys, n, b.desc_p);
