@@ -63,6 +63,10 @@ const char* rtr_last_error(void);
 const char* rtr_version(void);
 
 /* Tuning knobs of this context (value 0 restores the automatic choice):
+ *   "auto_graph"     1 (the default): rtr_recognize / rtr_recognize_learned /
+ *                    rtr_recognize_host replay a repeated call from a CUDA
+ *                    graph (see rtr_recognize); 0: every call enqueues its
+ *                    kernels one by one;
  *   "icp_group"      lanes cooperating on one ICP source point's 1-NN search
  *                    (2, 4 or 8);
  *   "batch_workers"  workers (streams) of rtr_recognize_batch (1..16);
@@ -629,7 +633,14 @@ rtr_status rtr_model_buffers(const rtr_model* m, const float** d_vox, const floa
  * after it, calls of at most that size can be captured into a CUDA graph.
  * Such a graph holds the scratch's address: a later call that grows the
  * scratch (a larger scene, the learned form) moves it, and the graph must not
- * be launched again (rtr_context_reserve the largest size first). */
+ * be launched again (rtr_context_reserve the largest size first).
+ * The context does this itself for a repeated call ("auto_graph", on by
+ * default): when a call repeats the previous one's model, scene and result
+ * addresses, n and parameters (the scene's contents may change), the second
+ * such call captures its launches into a CUDA graph and later ones replay
+ * it, with the same results; any other call, a tuning change or a grown
+ * scratch arena ends the replay.  Not while profiling or while the caller's
+ * stream is itself being captured. */
 rtr_status rtr_recognize(rtr_context* ctx, const rtr_model* model, const float* d_scene, int n,
                          const rtr_recog_params* p, rtr_recog_result* d_result,
                          rtr_stream_t stream);

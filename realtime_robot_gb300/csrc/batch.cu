@@ -44,6 +44,7 @@ rtr_status batch_ensure_workers(rtr_context* ctx, int n) {
   for (rtr_context* w : ctx->workers) {
     if (!w->ev_fork) RTR_CUDA(cudaEventCreateWithFlags(&w->ev_fork, cudaEventDisableTiming));
     w->coop_div = n;  // cooperative kernels of the n workers fit the GPU side by side
+    w->auto_graph = 0;  // a worker's consecutive pairs differ; whole batches are graphed instead
     w->wait_budget_ms = ctx->wait_budget_ms;
     w->wait_budget_cycles = ctx->wait_budget_cycles;
     w->tune_icp_group = ctx->tune_icp_group;

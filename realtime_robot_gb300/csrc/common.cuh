@@ -47,6 +47,8 @@ rtr_status cuda_fail(cudaError_t e, const char* what, const char* file, int line
 
 namespace rtr {
 extern std::atomic<uint64_t> g_launches;
+// A number no other model or network of this process has had (never 0).
+uint64_t next_uid();
 }
 // Count kernel launches issued by the library (rtr_launch_count).
 #define RTR_LAUNCHED(n) (rtr::g_launches.fetch_add((n), std::memory_order_relaxed))
@@ -54,6 +56,28 @@ extern std::atomic<uint64_t> g_launches;
 struct rtr_prof_rec {
   const char* name;
   cudaEvent_t a, b;
+};
+
+// The last recognition enqueued on a context and, once the same call has been
+// made twice in a row, its launches captured as a CUDA graph (pipeline.cu).
+// The key holds everything the enqueued work depends on: the inputs' device
+// addresses, the parameters, the model's and network's identities, the
+// arena's generation and the context's configuration generation.
+struct RecogGraphSlot {
+  const void* model = nullptr;
+  uint64_t model_uid = 0;
+  const void* mlp = nullptr;
+  uint64_t mlp_uid = 0;
+  float keep = 0.f;
+  const float* scene = nullptr;
+  int n = 0;
+  void* result = nullptr;
+  rtr_recog_params params{};
+  unsigned scratch_gen = 0, cfg_gen = 0;
+  bool armed = false;   // this key ran once directly (the arena is sized for it)
+  bool failed = false;  // its capture failed: it stays direct
+  cudaGraphExec_t exec = nullptr;
+  uint64_t launches = 0;  // kernels in the graph
 };
 
 struct rtr_context {
@@ -87,6 +111,10 @@ struct rtr_context {
   bool profiling = false;
   std::vector<rtr_prof_rec> prof;      // recorded stages (in order)
   std::vector<cudaEvent_t> event_pool; // reusable events
+  int auto_graph = 1;                  // replay repeated recognitions from a CUDA graph
+  unsigned cfg_gen = 0;                // bumped by every tuning or wait-budget change
+  cudaStream_t cap_stream = nullptr;   // private stream that graphs are captured on
+  RecogGraphSlot rgraph;
 };
 
 namespace rtr {

@@ -7,6 +7,8 @@
 namespace rtr {
 
 std::atomic<uint64_t> g_launches{0};
+static std::atomic<uint64_t> g_uid{0};
+uint64_t next_uid() { return g_uid.fetch_add(1, std::memory_order_relaxed) + 1; }
 static thread_local char g_last_error[512] = "";
 
 static cudaEvent_t pool_event(rtr_context* ctx) {
@@ -217,6 +219,8 @@ rtr_status rtr_context_destroy(rtr_context* ctx) {
   rtr_context_profile_clear(ctx);
   for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->rgraph.exec) cudaGraphExecDestroy(ctx->rgraph.exec);
+  if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
   if (ctx->arena) cudaFree(ctx->arena);
   if (ctx->io) cudaFree(ctx->io);
   if (ctx->host_stream) cudaStreamDestroy(ctx->host_stream);
@@ -240,11 +244,25 @@ rtr_status rtr_context_set_wait_budget_ms(rtr_context* ctx, double ms) {
   if (!ctx || !(ms > 0)) return rtr::fail(RTR_ERR_INVALID_ARG, "wait budget must be > 0 ms");
   ctx->wait_budget_ms = ms;
   ctx->wait_budget_cycles = (long long)(ms * 1e-3 * ctx->clock_khz * 1e3);
+  ++ctx->cfg_gen;
   return RTR_OK;
 }
 
+static rtr_status set_tuning(rtr_context* ctx, const char* key, int value);
+
 rtr_status rtr_context_set_tuning(rtr_context* ctx, const char* key, int value) {
   if (!ctx || !key) return rtr::fail(RTR_ERR_INVALID_ARG, "rtr_context_set_tuning: NULL argument");
+  const rtr_status r = set_tuning(ctx, key, value);
+  if (r == RTR_OK) ++ctx->cfg_gen;  // a captured recognition no longer matches
+  return r;
+}
+
+static rtr_status set_tuning(rtr_context* ctx, const char* key, int value) {
+  if (strcmp(key, "auto_graph") == 0) {
+    if (value < 0 || value > 1) return rtr::fail(RTR_ERR_INVALID_ARG, "auto_graph must be 0 or 1 (got %d)", value);
+    ctx->auto_graph = value;
+    return RTR_OK;
+  }
   if (strcmp(key, "batch_workers") == 0) {
     if (value < 0 || value > 16)
       return rtr::fail(RTR_ERR_INVALID_ARG, "batch_workers must be 0..16 (got %d)", value);
@@ -291,7 +309,8 @@ rtr_status rtr_context_set_tuning(rtr_context* ctx, const char* key, int value) 
 
 rtr_status rtr_context_get_tuning(const rtr_context* ctx, const char* key, int* value) {
   if (!ctx || !key || !value) return rtr::fail(RTR_ERR_INVALID_ARG, "rtr_context_get_tuning: NULL argument");
-  if (strcmp(key, "batch_workers") == 0) *value = ctx->tune_batch_workers;
+  if (strcmp(key, "auto_graph") == 0) *value = ctx->auto_graph;
+  else if (strcmp(key, "batch_workers") == 0) *value = ctx->tune_batch_workers;
   else if (strcmp(key, "gc_window") == 0) *value = ctx->tune_gc_window;
   else if (strcmp(key, "gc_pass_lists") == 0) *value = ctx->tune_gc_no_lists;
   else if (strcmp(key, "gc_inline") == 0) *value = ctx->tune_gc_inline;

@@ -28,7 +28,10 @@ struct rtr_mlp {
   float* m = nullptr;              // Adam first moment
   float* v = nullptr;              // Adam second moment
   int step = 0;                    // Adam steps taken
+  uint64_t uid = 0;                // identity for captured recognitions (rtr::next_uid)
 };
+
+uint64_t rtr_mlp_uid(const rtr_mlp* m) { return m ? m->uid : 0; }
 
 namespace rtr {
 
@@ -404,6 +407,7 @@ rtr_status rtr_mlp_create(rtr_context* ctx, const float* h_params, uint64_t seed
   }
   rtr_mlp* m = new rtr_mlp();
   m->device = ctx->device;
+  m->uid = next_uid();
   if (cudaMalloc(&m->theta, sizeof(float) * N_PARAMS) != cudaSuccess ||
       cudaMalloc(&m->wbf, sizeof(__nv_bfloat16) * BF_N) != cudaSuccess ||
       cudaMalloc(&m->w1pad, sizeof(__nv_bfloat16) * MLP_H1 * W1PAD_K) != cudaSuccess ||

@@ -328,7 +328,11 @@ struct rtr_model {
   __nv_bfloat16* db_hi = nullptr;  // [n_kp][384] descriptor split for the tensor cores
   __nv_bfloat16* db_lo = nullptr;
   float* db_n2 = nullptr;          // [db_norm_floats(n_kp)] squared norms, their maximum, the all-zero answer
+  uint64_t uid = 0;                // identity for captured recognitions (rtr::next_uid)
 };
+
+// rtr_mlp's identity, for the recognition graph's key (mlp.cu).
+uint64_t rtr_mlp_uid(const rtr_mlp* m);
 
 extern "C" {
 
@@ -366,6 +370,7 @@ rtr_status rtr_model_create(rtr_context* ctx, const float* d_pts, int n, const r
   RTR_CUDA(cudaSetDevice(ctx->device));
   cudaStream_t st = ctx->host_stream;
   rtr_model* m = new rtr_model();
+  m->uid = next_uid();
   m->device = ctx->device;
   auto cleanup = [&](rtr_status s) {
     rtr_model_destroy(m);
@@ -869,6 +874,75 @@ static rtr_status recognize_multi_impl(rtr_context* ctx, const rtr_model* const*
   return RTR_OK;
 }
 
+// A recognition enqueued through the context's graph slot.  The first call
+// with a key runs directly (sizing the arena); the second identical call
+// captures the same enqueue sequence on a private stream into a CUDA graph
+// and launches it on the caller's stream; later identical calls only launch
+// the graph: the same kernels with the same arguments, without the host's
+// per-launch cost (~150 launches a recognition).  Any change of key (inputs'
+// addresses, parameters, model or network, arena, tuning) runs directly
+// again.  Off while profiling, inside a caller's own capture, and on batch
+// workers.
+static rtr_status recognize_cached(rtr_context* ctx, const rtr_model* m, const float4* scene, int n,
+                                   const rtr_recog_params* q, rtr_recog_result* out, cudaStream_t st,
+                                   const rtr_mlp* mlp, float keep) {
+  if (!ctx->auto_graph || ctx->profiling || stream_is_capturing(st))
+    return recognize_impl(ctx, m, scene, n, q, out, st, mlp, keep);
+  RecogGraphSlot& g = ctx->rgraph;
+  const float* sc = reinterpret_cast<const float*>(scene);
+  const bool same = g.model == m && g.model_uid == m->uid && g.mlp == mlp && g.mlp_uid == rtr_mlp_uid(mlp) &&
+                    g.keep == keep && g.scene == sc && g.n == n && g.result == out &&
+                    memcmp(&g.params, q, sizeof(*q)) == 0 && g.scratch_gen == ctx->scratch_gen &&
+                    g.cfg_gen == ctx->cfg_gen;
+  if (same && g.exec) {
+    RTR_CUDA(cudaGraphLaunch(g.exec, st));
+    RTR_LAUNCHED(g.launches);
+    return RTR_OK;
+  }
+  if (!same) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = RecogGraphSlot();
+    g.model = m;
+    g.model_uid = m->uid;
+    g.mlp = mlp;
+    g.mlp_uid = rtr_mlp_uid(mlp);
+    g.keep = keep;
+    g.scene = sc;
+    g.n = n;
+    g.result = out;
+    g.params = *q;
+    g.cfg_gen = ctx->cfg_gen;
+  }
+  if (!g.armed || g.failed) {
+    const rtr_status r = recognize_impl(ctx, m, scene, n, q, out, st, mlp, keep);
+    g.armed = r == RTR_OK;
+    g.scratch_gen = ctx->scratch_gen;  // after any growth of this call
+    return r;
+  }
+  if (!ctx->cap_stream) RTR_CUDA(cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking));
+  const uint64_t l0 = g_launches.load();
+  RTR_CUDA(cudaStreamBeginCapture(ctx->cap_stream, cudaStreamCaptureModeThreadLocal));
+  const rtr_status r = recognize_impl(ctx, m, scene, n, q, out, ctx->cap_stream, mlp, keep);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(ctx->cap_stream, &graph);
+  const uint64_t nl = g_launches.load() - l0;
+  g_launches.fetch_sub(nl);  // captured, not launched
+  cudaGraphExec_t x = nullptr;
+  if (r == RTR_OK && e == cudaSuccess && graph && ctx->scratch_gen == g.scratch_gen &&
+      cudaGraphInstantiate(&x, graph, 0) == cudaSuccess) {
+    cudaGraphDestroy(graph);
+    g.exec = x;
+    g.launches = nl;
+    RTR_CUDA(cudaGraphLaunch(g.exec, st));
+    RTR_LAUNCHED(nl);
+    return RTR_OK;
+  }
+  if (graph) cudaGraphDestroy(graph);
+  cudaGetLastError();
+  g.failed = true;
+  return recognize_impl(ctx, m, scene, n, q, out, st, mlp, keep);
+}
+
 }  // namespace rtr
 
 extern "C" {
@@ -890,7 +964,7 @@ rtr_status rtr_recognize(rtr_context* ctx, const rtr_model* model, const float* 
     RTR_CUDA(cudaGetLastError());
     return RTR_OK;
   }
-  return recognize_impl(ctx, model, reinterpret_cast<const float4*>(d_scene), n, p, d_result, st);
+  return recognize_cached(ctx, model, reinterpret_cast<const float4*>(d_scene), n, p, d_result, st, nullptr, 1.f);
 }
 
 rtr_status rtr_recognize_learned(rtr_context* ctx, const rtr_model* model, const rtr_mlp* mlp, float keep,
@@ -912,7 +986,7 @@ rtr_status rtr_recognize_learned(rtr_context* ctx, const rtr_model* model, const
     RTR_CUDA(cudaGetLastError());
     return RTR_OK;
   }
-  return recognize_impl(ctx, model, reinterpret_cast<const float4*>(d_scene), n, p, d_result, st, mlp, keep);
+  return recognize_cached(ctx, model, reinterpret_cast<const float4*>(d_scene), n, p, d_result, st, mlp, keep);
 }
 
 rtr_status rtr_recognize_multi(rtr_context* ctx, const rtr_model* const* h_models, int n_models, const rtr_mlp* mlp,
