@@ -115,6 +115,8 @@ struct rtr_context {
   unsigned cfg_gen = 0;                // bumped by every tuning or wait-budget change
   cudaStream_t cap_stream = nullptr;   // private stream that graphs are captured on
   RecogGraphSlot rgraph;
+  cudaStream_t side_stream = nullptr;  // second stream of a recognition's independent stages
+  cudaEvent_t ev_side[3] = {};         // its fork and join events
 };
 
 namespace rtr {
@@ -148,6 +150,9 @@ struct Scratch {
 rtr_status ensure_scratch(rtr_context* ctx, size_t bytes, cudaStream_t stream, Scratch* out);
 
 bool stream_is_capturing(cudaStream_t s);
+
+// Create the context's side stream and its events on first use.
+rtr_status side_stream_ready(rtr_context* ctx);
 
 // Worker contexts of a batch (batch.cu): make sure `n` exist and share the
 // GPU's co-resident blocks; how many a call of `n_items` uses; and their

@@ -62,6 +62,13 @@ bool stream_is_capturing(cudaStream_t s) {
   return st != cudaStreamCaptureStatusNone;
 }
 
+rtr_status side_stream_ready(rtr_context* ctx) {
+  if (!ctx->side_stream) RTR_CUDA(cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking));
+  for (cudaEvent_t& e : ctx->ev_side)
+    if (!e) RTR_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  return RTR_OK;
+}
+
 rtr_status ensure_scratch(rtr_context* ctx, size_t bytes, cudaStream_t stream, Scratch* out) {
   if (bytes > ctx->arena_bytes) {
     if (stream_is_capturing(stream))
@@ -220,6 +227,9 @@ rtr_status rtr_context_destroy(rtr_context* ctx) {
   for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
   if (ctx->rgraph.exec) cudaGraphExecDestroy(ctx->rgraph.exec);
+  for (cudaEvent_t e : ctx->ev_side)
+    if (e) cudaEventDestroy(e);
+  if (ctx->side_stream) cudaStreamDestroy(ctx->side_stream);
   if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
   if (ctx->arena) cudaFree(ctx->arena);
   if (ctx->io) cudaFree(ctx->io);

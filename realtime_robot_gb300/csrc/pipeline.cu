@@ -486,6 +486,7 @@ struct SceneBufs {
   float* desc;
   uint32_t *flags, *pos, *tiles;
   GridBufs grid;            // scene voxels at the ICP distance (verification, refinement)
+  Scratch aux;              // temporaries of the keypoint stage on the side stream
   int* keys_p;              // learned pruning: kept keypoints
   float* desc_p;            // and their descriptors
   // what goes on to matching (set by scene_stages)
@@ -508,6 +509,14 @@ struct ModelBufs {
   rtr_icp_result* res;
 };
 
+// The keypoint stage's temporaries, which run beside the normals on the
+// context's side stream and so need a region of their own.
+static size_t aux_bytes(int n) {
+  ScratchPlan t;
+  voxseg_plan(t, n);
+  return t.bytes + 256;
+}
+
 static void scene_plan(ScratchPlan& p, int n, bool learned) {
   p.add<int>(8);
   p.add<float4>(n);
@@ -519,6 +528,7 @@ static void scene_plan(ScratchPlan& p, int n, bool learned) {
   p.add<uint32_t>(n);
   p.add<uint32_t>(scan_tiles(n));
   grid_plan(p, n, default_cell_cap(n));
+  p.add<char>(aux_bytes(n));
   if (learned) {
     p.add<int>(n);
     p.add<float>((size_t)n * 352);
@@ -536,6 +546,10 @@ static bool scene_take(Scratch& s, int n, bool learned, SceneBufs* b) {
   b->pos = s.take<uint32_t>(n);
   b->tiles = s.take<uint32_t>(scan_tiles(n));
   if (!b->tiles || !grid_take(s, n, default_cell_cap(n), &b->grid)) return false;
+  b->aux.base = s.take<char>(aux_bytes(n));
+  b->aux.off = 0;
+  b->aux.cap = aux_bytes(n);
+  if (!b->aux.base) return false;
   b->keys_p = nullptr;
   b->desc_p = nullptr;
   if (learned) {
@@ -646,6 +660,27 @@ static rtr_status scene_stages(rtr_context* ctx, const Scratch& stage, SceneBufs
     Scratch t = stage;
     RTR_TRY(voxel_downsample_dev(ctx, t, scene, n, nullptr, q->voxel_leaf, b.sv, dV, st));
   }
+  // The keypoints and the scene grid need only the voxels: they run on the
+  // context's side stream beside the normals, the descriptors and pruning
+  // (small sort-bound kernels that leave most of the GPU idle), joined
+  // before the descriptors and at the end.
+  RTR_TRY(side_stream_ready(ctx));
+  cudaStream_t ax = ctx->side_stream;
+  RTR_CUDA(cudaEventRecord(ctx->ev_side[0], st));
+  RTR_CUDA(cudaStreamWaitEvent(ax, ctx->ev_side[0], 0));
+  {
+    ProfScope ps(ctx, ax, "keypoints");
+    Scratch t = b.aux;
+    RTR_TRY(uniform_sample_dev(ctx, t, b.sv, n, dV, q->scene_keypoint_r, b.keys, dK, ax));
+  }
+  RTR_CUDA(cudaEventRecord(ctx->ev_side[1], ax));
+  {
+    ProfScope ps(ctx, ax, "scene_grid");
+    // 1.5 x the ICP distance measured fastest for refinement and verification
+    const float cell = ctx->tune_scene_grid_mm > 0 ? 1e-3f * (float)ctx->tune_scene_grid_mm : 1.5f * q->icp_max_dist;
+    grid_build(b.grid, b.sv, n, dV, cell, ax);
+  }
+  RTR_CUDA(cudaEventRecord(ctx->ev_side[2], ax));
   {
     ProfScope ps(ctx, st, "normals");
     Scratch t = stage;
@@ -660,11 +695,7 @@ static rtr_status scene_stages(rtr_context* ctx, const Scratch& stage, SceneBufs
       RTR_LAUNCHED(1);
     }
   }
-  {
-    ProfScope ps(ctx, st, "keypoints");
-    Scratch t = stage;
-    RTR_TRY(uniform_sample_dev(ctx, t, b.sv, n, dV, q->scene_keypoint_r, b.keys, dK, st));
-  }
+  RTR_CUDA(cudaStreamWaitEvent(st, ctx->ev_side[1], 0));  // the keypoints
   const int* keys = b.keys;
   const int* dKeys = dK;
   if (q->keypoint_min_curvature > 0.f) {
@@ -714,12 +745,7 @@ static rtr_status scene_stages(rtr_context* ctx, const Scratch& stage, SceneBufs
     dKeys = b.cnt + 3;
     desc = b.desc_p;
   }
-  {
-    ProfScope ps(ctx, st, "scene_grid");
-    // 1.5 x the ICP distance measured fastest for refinement and verification
-    const float cell = ctx->tune_scene_grid_mm > 0 ? 1e-3f * (float)ctx->tune_scene_grid_mm : 1.5f * q->icp_max_dist;
-    grid_build(b.grid, b.sv, n, dV, cell, st);
-  }
+  RTR_CUDA(cudaStreamWaitEvent(st, ctx->ev_side[2], 0));  // the scene grid
   b.keys_m = keys;
   b.d_nk = dKeys;
   b.desc_m = desc;
