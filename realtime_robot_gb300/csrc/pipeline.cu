@@ -27,6 +27,8 @@ rtr_status uniform_sample_dev(rtr_context*, Scratch&, const float4*, int, const 
 rtr_status normals_dev(rtr_context*, Scratch&, const float4*, int, const int*, int, const float*, float, float4*, cudaStream_t);
 rtr_status shot_dev(rtr_context*, Scratch&, const float4*, const float4*, int, const int*, const int*, int, const int*,
                     float, float*, float*, cudaStream_t);
+rtr_status shot_on_grid(const GridBufs&, const float4*, const float4*, const int*, int, const int*, float, float*,
+                        float*, cudaStream_t);
 rtr_status match_exact_dev(const float*, int, const int*, const float*, int, int*, float*, cudaStream_t);
 size_t match_tc_bf16_bytes(int rows);
 void match_tc_plan(ScratchPlan& p, int nq_cap, bool with_db, int ndb);
@@ -486,6 +488,7 @@ struct SceneBufs {
   float* desc;
   uint32_t *flags, *pos, *tiles;
   GridBufs grid;            // scene voxels at the ICP distance (verification, refinement)
+  GridBufs shot_grid;       // scene voxels at the descriptor radius (SHOT's support)
   Scratch aux;              // temporaries of the keypoint stage on the side stream
   int* keys_p;              // learned pruning: kept keypoints
   float* desc_p;            // and their descriptors
@@ -528,6 +531,7 @@ static void scene_plan(ScratchPlan& p, int n, bool learned) {
   p.add<uint32_t>(n);
   p.add<uint32_t>(scan_tiles(n));
   grid_plan(p, n, default_cell_cap(n));
+  grid_plan(p, n, default_cell_cap(n));
   p.add<char>(aux_bytes(n));
   if (learned) {
     p.add<int>(n);
@@ -545,7 +549,9 @@ static bool scene_take(Scratch& s, int n, bool learned, SceneBufs* b) {
   b->flags = s.take<uint32_t>(n);
   b->pos = s.take<uint32_t>(n);
   b->tiles = s.take<uint32_t>(scan_tiles(n));
-  if (!b->tiles || !grid_take(s, n, default_cell_cap(n), &b->grid)) return false;
+  if (!b->tiles || !grid_take(s, n, default_cell_cap(n), &b->grid) ||
+      !grid_take(s, n, default_cell_cap(n), &b->shot_grid))
+    return false;
   b->aux.base = s.take<char>(aux_bytes(n));
   b->aux.off = 0;
   b->aux.cap = aux_bytes(n);
@@ -660,10 +666,10 @@ static rtr_status scene_stages(rtr_context* ctx, const Scratch& stage, SceneBufs
     Scratch t = stage;
     RTR_TRY(voxel_downsample_dev(ctx, t, scene, n, nullptr, q->voxel_leaf, b.sv, dV, st));
   }
-  // The keypoints and the scene grid need only the voxels: they run on the
-  // context's side stream beside the normals, the descriptors and pruning
-  // (small sort-bound kernels that leave most of the GPU idle), joined
-  // before the descriptors and at the end.
+  // The keypoints, the descriptors' grid and the scene grid need only the
+  // voxels: they run on the context's side stream beside the normals, the
+  // descriptors and pruning (small sort-bound kernels that leave most of the
+  // GPU idle), joined before the descriptors and at the end.
   RTR_TRY(side_stream_ready(ctx));
   cudaStream_t ax = ctx->side_stream;
   RTR_CUDA(cudaEventRecord(ctx->ev_side[0], st));
@@ -672,6 +678,10 @@ static rtr_status scene_stages(rtr_context* ctx, const Scratch& stage, SceneBufs
     ProfScope ps(ctx, ax, "keypoints");
     Scratch t = b.aux;
     RTR_TRY(uniform_sample_dev(ctx, t, b.sv, n, dV, q->scene_keypoint_r, b.keys, dK, ax));
+  }
+  {
+    ProfScope ps(ctx, ax, "shot_grid");
+    grid_build(b.shot_grid, b.sv, n, dV, q->descriptor_r, ax);
   }
   RTR_CUDA(cudaEventRecord(ctx->ev_side[1], ax));
   {
@@ -695,7 +705,7 @@ static rtr_status scene_stages(rtr_context* ctx, const Scratch& stage, SceneBufs
       RTR_LAUNCHED(1);
     }
   }
-  RTR_CUDA(cudaStreamWaitEvent(st, ctx->ev_side[1], 0));  // the keypoints
+  RTR_CUDA(cudaStreamWaitEvent(st, ctx->ev_side[1], 0));  // the keypoints and the descriptors' grid
   const int* keys = b.keys;
   const int* dKeys = dK;
   if (q->keypoint_min_curvature > 0.f) {
@@ -709,8 +719,7 @@ static rtr_status scene_stages(rtr_context* ctx, const Scratch& stage, SceneBufs
   }
   {
     ProfScope ps(ctx, st, "shot352");
-    Scratch t = stage;
-    RTR_TRY(shot_dev(ctx, t, b.sv, b.sn, n, dV, keys, n, dKeys, q->descriptor_r, b.desc, nullptr, st));
+    RTR_TRY(shot_on_grid(b.shot_grid, b.sv, b.sn, keys, n, dKeys, q->descriptor_r, b.desc, nullptr, st));
   }
   const float* desc = b.desc;
   if (mlp) {

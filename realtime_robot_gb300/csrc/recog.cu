@@ -622,6 +622,15 @@ rtr_status normals_dev(rtr_context* ctx, Scratch& s, const float4* pts, int n_ca
   return RTR_OK;
 }
 
+// SHOT over a grid of the points already built with cell R (grid_build).
+rtr_status shot_on_grid(const GridBufs& gb, const float4* pts, const float4* nrm, const int* keys, int nk_cap,
+                        const int* d_nk, float R, float* desc, float* lrf, cudaStream_t st) {
+  k_shot<<<blocks_for(nk_cap, SHOT_WARPS, 152 * 32), SHOT_WARPS * 32, 0, st>>>(grid_dev(gb), pts, nrm, keys, nk_cap,
+                                                                                d_nk, R, desc, lrf);
+  RTR_LAUNCHED(1);
+  return RTR_OK;
+}
+
 rtr_status shot_dev(rtr_context* ctx, Scratch& s, const float4* pts, const float4* nrm, int n_cap, const int* d_n,
                     const int* keys, int nk_cap, const int* d_nk, float R, float* desc, float* lrf,
                     cudaStream_t st) {
@@ -629,10 +638,7 @@ rtr_status shot_dev(rtr_context* ctx, Scratch& s, const float4* pts, const float
   const unsigned cap = default_cell_cap(n_cap);
   if (!grid_take(s, n_cap, cap, &gb)) return fail(RTR_ERR_CAPACITY, "shot: scratch");
   grid_build(gb, pts, n_cap, d_n, R, st);
-  k_shot<<<blocks_for(nk_cap, SHOT_WARPS, 152 * 32), SHOT_WARPS * 32, 0, st>>>(grid_dev(gb), pts, nrm, keys, nk_cap,
-                                                                                d_nk, R, desc, lrf);
-  RTR_LAUNCHED(1);
-  return RTR_OK;
+  return shot_on_grid(gb, pts, nrm, keys, nk_cap, d_nk, R, desc, lrf, st);
 }
 
 }  // namespace rtr
