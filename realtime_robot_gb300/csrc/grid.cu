@@ -13,7 +13,13 @@ constexpr int RS_RADIX = 256;
 
 __device__ __forceinline__ int count_of(int n_host, const int* d_n) { return d_n ? *d_n : n_host; }
 
-// Per-tile digit histogram, written digit-major: hist[d * nb + tile].
+// Sorts of at most this many tiles skip the scan kernel: each scatter block
+// sums the tile-major histogram itself (nb rows of 1 KB from L2).
+constexpr int RS_FUSE_TILES = 128;
+
+// Per-tile digit histogram, written digit-major, hist[d * nb + tile], or
+// tile-major, hist[tile * 256 + d] (TILE_MAJOR, read by k_rs_scatter_own).
+template <bool TILE_MAJOR>
 __global__ void __launch_bounds__(RS_BLOCK) k_rs_hist(const uint32_t* __restrict__ keys, int n_host,
                                                       const int* d_n, int shift,
                                                       uint32_t* __restrict__ hist, int nb) {
@@ -28,7 +34,8 @@ __global__ void __launch_bounds__(RS_BLOCK) k_rs_hist(const uint32_t* __restrict
     if (i < n) atomicAdd(&cnt[(keys[i] >> shift) & (RS_RADIX - 1)], 1u);
   }
   __syncthreads();
-  for (int d = threadIdx.x; d < RS_RADIX; d += RS_BLOCK) hist[d * nb + blockIdx.x] = cnt[d];
+  for (int d = threadIdx.x; d < RS_RADIX; d += RS_BLOCK)
+    hist[TILE_MAJOR ? blockIdx.x * RS_RADIX + d : d * nb + blockIdx.x] = cnt[d];
 }
 
 // In-place exclusive scan of `total` entries by one block of 1024 threads,
@@ -92,9 +99,48 @@ __global__ void __launch_bounds__(1024) k_rs_scan(uint32_t* __restrict__ h, int 
   }
 }
 
+// This block's output offset of each digit from the tile-major histogram:
+// the keys of smaller digits in every tile plus those of the same digit in
+// earlier tiles (thread d owns digit d; a block-wide exclusive scan of the
+// digit totals).
+__device__ __forceinline__ void rs_own_offsets(const uint32_t* __restrict__ hist, int nb, uint32_t* boff,
+                                               uint32_t* wsum) {
+  static_assert(RS_BLOCK == RS_RADIX, "one thread per digit");
+  const int d = threadIdx.x, lane = d & 31, warp = d >> 5;
+  const int b = blockIdx.x;
+  uint32_t tot = 0, pre = 0;
+  int t = 0;
+  for (; t + 4 <= nb; t += 4) {
+    const uint32_t a0 = hist[(t + 0) * RS_RADIX + d], a1 = hist[(t + 1) * RS_RADIX + d];
+    const uint32_t a2 = hist[(t + 2) * RS_RADIX + d], a3 = hist[(t + 3) * RS_RADIX + d];
+    tot += a0 + a1 + a2 + a3;
+    pre += (t + 0 < b ? a0 : 0u) + (t + 1 < b ? a1 : 0u) + (t + 2 < b ? a2 : 0u) + (t + 3 < b ? a3 : 0u);
+  }
+  for (; t < nb; ++t) {
+    const uint32_t a0 = hist[t * RS_RADIX + d];
+    tot += a0;
+    pre += t < b ? a0 : 0u;
+  }
+  uint32_t inc = tot;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += v;
+  }
+  if (lane == 31) wsum[warp] = inc;
+  __syncthreads();
+  uint32_t wpre = 0;
+#pragma unroll
+  for (int w = 0; w < RS_WARPS; ++w) wpre += w < warp ? wsum[w] : 0u;
+  boff[d] = wpre + inc - tot + pre;
+}
+
 // Stable scatter.  Warp w of a block owns a contiguous run of RS_ITEMS*32 keys
 // and walks it 32 at a time, so (warp, step, lane) is the input order; ranks
 // inside a step come from __match_any_sync, so equal digits keep their order.
+// OWN: the block computes its offsets from the tile-major histogram
+// (rs_own_offsets); otherwise it reads them from the scanned digit-major one.
+template <bool OWN>
 __global__ void __launch_bounds__(RS_BLOCK) k_rs_scatter(const uint32_t* __restrict__ kin,
                                                          const uint32_t* __restrict__ vin,
                                                          uint32_t* __restrict__ kout,
@@ -103,10 +149,16 @@ __global__ void __launch_bounds__(RS_BLOCK) k_rs_scatter(const uint32_t* __restr
                                                          const uint32_t* __restrict__ hist, int nb) {
   __shared__ uint32_t wcnt[RS_WARPS][RS_RADIX];
   __shared__ uint32_t boff[RS_RADIX];
+  __shared__ uint32_t wsum[RS_WARPS];
   const int n = count_of(n_host, d_n);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int i = threadIdx.x; i < RS_WARPS * RS_RADIX; i += RS_BLOCK) (&wcnt[0][0])[i] = 0;
-  for (int d = threadIdx.x; d < RS_RADIX; d += RS_BLOCK) boff[d] = hist[d * nb + blockIdx.x];
+  if (OWN) {
+    if (blockIdx.x * RS_TILE >= n) return;  // whole tile empty (uniform per block)
+    rs_own_offsets(hist, nb, boff, wsum);
+  } else {
+    for (int d = threadIdx.x; d < RS_RADIX; d += RS_BLOCK) boff[d] = hist[d * nb + blockIdx.x];
+  }
   __syncthreads();
   const int base = blockIdx.x * RS_TILE + warp * (RS_ITEMS * 32);
   if (blockIdx.x * RS_TILE >= n) return;  // whole tile empty (uniform per block)
@@ -170,11 +222,16 @@ void radix_sort_pairs(uint32_t* k0, uint32_t* v0, uint32_t* k1, uint32_t* v1, ui
     uint32_t* vi = even ? ((p == 0 && vals_iota) ? nullptr : v0) : v1;
     uint32_t* ko = even ? k1 : k0;
     uint32_t* vo = even ? v1 : v0;
-    k_rs_hist<<<nb, RS_BLOCK, 0, st>>>(ki, n_host, d_n, shift, hist, nb);
-    k_rs_scan<<<1, 1024, 0, st>>>(hist, nb * RS_RADIX);
-    k_rs_scatter<<<nb, RS_BLOCK, 0, st>>>(ki, vi, ko, vo, n_host, d_n, shift, hist, nb);
+    if (nb <= RS_FUSE_TILES) {
+      k_rs_hist<true><<<nb, RS_BLOCK, 0, st>>>(ki, n_host, d_n, shift, hist, nb);
+      k_rs_scatter<true><<<nb, RS_BLOCK, 0, st>>>(ki, vi, ko, vo, n_host, d_n, shift, hist, nb);
+    } else {
+      k_rs_hist<false><<<nb, RS_BLOCK, 0, st>>>(ki, n_host, d_n, shift, hist, nb);
+      k_rs_scan<<<1, 1024, 0, st>>>(hist, nb * RS_RADIX);
+      k_rs_scatter<false><<<nb, RS_BLOCK, 0, st>>>(ki, vi, ko, vo, n_host, d_n, shift, hist, nb);
+    }
   }
-  RTR_LAUNCHED(3 * passes);
+  RTR_LAUNCHED((nb <= RS_FUSE_TILES ? 2 : 3) * passes);
   const bool odd = (passes & 1) != 0;
   *k_out = odd ? k1 : k0;
   *v_out = odd ? v1 : v0;
