@@ -405,7 +405,7 @@ __device__ __forceinline__ void shot_bins(float pos, int nb, bool circular, int&
 // passes 2 and 3 read the list.  Cells whose box lies beyond R are not
 // walked.  A keypoint with more support points than the list holds walks
 // the cells again in passes 2 and 3 (same sums, another order).
-constexpr int SHOT_CAP = 192;
+constexpr int SHOT_CAP = 176;  // with the histograms: 56 KB a block, four blocks an SM
 
 __device__ __forceinline__ float shot_cell_d2(const GridView& g, float4 q, int x, int y, int z) {
   const float lx = g.ox + (float)x * g.h, ly = g.oy + (float)y * g.h, lz = g.oz + (float)z * g.h;
@@ -445,7 +445,7 @@ __device__ __forceinline__ void shot_add(float* H, float dx, float dy, float dz,
         }
 }
 
-__global__ void __launch_bounds__(SHOT_WARPS * 32) k_shot(GridDev gd, const float4* __restrict__ pts,
+__global__ void __launch_bounds__(SHOT_WARPS * 32, 4) k_shot(GridDev gd, const float4* __restrict__ pts,
                                                           const float4* __restrict__ nrm,
                                                           const int* __restrict__ keys, int nk_host,
                                                           const int* d_nk, float R,
