@@ -147,9 +147,10 @@ constexpr int HV_G = 4;
 // Inlier count of every hypothesis: model points (every stride-th) moved by
 // the hypothesis pose with a scene point within sqrt(r2).  Blocks cover
 // (hypothesis, run of HV_PPB points); counts are integers, so the order of
-// the atomic adds does not matter.
+// the atomic adds does not matter.  Four blocks an SM (64 registers):
+// more searches in flight beat the spills that costs.
 constexpr int HV_PPB = 256;
-__global__ void __launch_bounds__(256) k_hv_count(GridDev gd, const float4* __restrict__ model, int n_model, int stride,
+__global__ void __launch_bounds__(256, 4) k_hv_count(GridDev gd, const float4* __restrict__ model, int n_model, int stride,
                                                   const double* __restrict__ poses, int n_hyp, const int* d_nhyp,
                                                   float r2, int bph, int* __restrict__ counts) {
   __shared__ int s_cnt;
