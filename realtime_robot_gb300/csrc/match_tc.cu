@@ -587,11 +587,12 @@ __global__ void k_band_gather(const uint4* __restrict__ qhi, const uint4* __rest
   }
 }
 
-// Band pass, step 3: exact FP32 distances to the listed rows, warp per
-// query.  The band holds every row that can tie or beat the exact winner, so
-// its exact minimum (lowest index on ties) is the scan's.  Queries past
-// TC_BAND_Q, with a band over TC_BAND rows, or with a non-finite threshold
-// (Inf or NaN values) go to the full scan list.
+// Band pass, step 3: exact FP32 distances to the listed rows, a block per
+// query and a thread per row (a band holds at most TC_BAND = 256 rows).  The
+// band holds every row that can tie or beat the exact winner, so its exact
+// minimum (lowest index on ties) is the scan's.  Queries past TC_BAND_Q,
+// with a band over TC_BAND rows, or with a non-finite threshold (Inf or NaN
+// values) go to the full scan list.
 template <bool V4>
 __global__ void __launch_bounds__(256) k_band_rerank(const float* __restrict__ q, const float* __restrict__ db,
                                                      const int* __restrict__ redo, const int* __restrict__ n_redo,
@@ -599,23 +600,24 @@ __global__ void __launch_bounds__(256) k_band_rerank(const float* __restrict__ q
                                                      const int* __restrict__ band_n, int cap, int ndb,
                                                      unsigned long long* __restrict__ redo_best,
                                                      int* __restrict__ full, int* __restrict__ n_full) {
+  static_assert(TC_BAND <= 256, "a thread per band row");
+  __shared__ unsigned long long s_min[8];
   const int n = *n_redo;
-  const int lane = threadIdx.x & 31;
-  for (int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < n; w += gridDim.x * (blockDim.x >> 5)) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int w = blockIdx.x; w < n; w += gridDim.x) {  // uniform per block
     const int cnt = w < cap ? band_n[w] : TC_BAND + 1;
     if (cnt > TC_BAND || !isfinite(w < cap ? thr[w] : 0.f)) {
-      if (lane == 0) full[atomicAdd(n_full, 1)] = w;
+      if (threadIdx.x == 0) full[atomicAdd(n_full, 1)] = w;
       continue;
     }
     const int i = redo[w];
     unsigned long long key = ~0ull;
-    for (int m = lane; m < cnt; m += 32) {
+    const int m = threadIdx.x;
+    if (m < cnt) {
       const int j = band_idx[(size_t)w * TC_BAND + m];
-      if ((unsigned)j >= (unsigned)ndb) continue;  // only after a timed-out band pass (status set)
-      const float d = exact_d2<V4>(q + (size_t)i * TC_DIM, db + (size_t)j * TC_DIM);
-      if (d < __int_as_float(0x7f800000)) {
-        const unsigned long long k2 = ((unsigned long long)__float_as_uint(d) << 32) | (unsigned)j;
-        key = k2 < key ? k2 : key;
+      if ((unsigned)j < (unsigned)ndb) {  // (out of range only after a timed-out band pass, status set)
+        const float d = exact_d2<V4>(q + (size_t)i * TC_DIM, db + (size_t)j * TC_DIM);
+        if (d < __int_as_float(0x7f800000)) key = ((unsigned long long)__float_as_uint(d) << 32) | (unsigned)j;
       }
     }
 #pragma unroll
@@ -623,7 +625,15 @@ __global__ void __launch_bounds__(256) k_band_rerank(const float* __restrict__ q
       const unsigned long long ok = __shfl_xor_sync(0xffffffffu, key, o);
       key = ok < key ? ok : key;
     }
-    if (lane == 0) redo_best[w] = key;
+    if (lane == 0) s_min[warp] = key;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned long long b = s_min[0];
+#pragma unroll
+      for (int k = 1; k < 8; ++k) b = s_min[k] < b ? s_min[k] : b;
+      redo_best[w] = b;
+    }
+    __syncthreads();  // s_min is reused by the next query
   }
 }
 
@@ -815,8 +825,8 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
   RTR_CUDA(cudaMemsetAsync(nredo, 0, 2 * sizeof(int), st));
   int rb = (nq_cap + 31) / 32;
   if (rb > 152 * 16) rb = 152 * 16;
-  int wb = (nqp + 7) / 8;  // warp per uncertified query
-  if (wb > 152 * 16) wb = 152 * 16;
+  // block per uncertified query (grid-stride over the device-side count)
+  const int wb = band_rows(nqp) < 152 * 8 ? band_rows(nqp) : 152 * 8;
   const bool v4 = ((reinterpret_cast<uintptr_t>(q) | reinterpret_cast<uintptr_t>(db)) & 15u) == 0;
   // band pass over the uncertified queries: the GEMM again, listing every
   // row within the tie margin, then exact distances to those rows only
@@ -830,7 +840,7 @@ rtr_status match_tc_dev(rtr_context* ctx, Scratch& s, const float* q, int nq_cap
                                         redo_best, redo_thr, qn, db_n2 + ndb, db_zero_key(db_n2, ndb), qzero);
   pr.end();
   ProfScope pu(ctx, st, "match_uncertified");
-  k_band_gather<<<(bq + 7) / 8, 256, 0, st>>>(reinterpret_cast<const uint4*>(qhi), reinterpret_cast<const uint4*>(qlo),
+  k_band_gather<<<(bq + 7) / 8 < 152 * 2 ? (bq + 7) / 8 : 152 * 2, 256, 0, st>>>(reinterpret_cast<const uint4*>(qhi), reinterpret_cast<const uint4*>(qlo),
                                               qn, redo, nredo, bq, reinterpret_cast<uint4*>(hi2),
                                               reinterpret_cast<uint4*>(lo2), qn2);
   RTR_CUDA(cudaMemsetAsync(band_n, 0, sizeof(int) * bq, st));
