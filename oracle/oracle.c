@@ -848,15 +848,28 @@ int orc_uniform_sample(const float* pts, int n, float r, int32_t* out_idx) {
 }
 
 /* SHOT conventions (restated from the paper):
- *  support: points within radius R of the keypoint (d^2 <= R*R);
+ *  support: points within radius R of the keypoint (d^2 <= R*R) whose
+ *  oriented normal faces the keypoint's (n_j . n_k >= -0.2);
  *  LRF: M = sum (R - d) (p - k)(p - k)^T, x = eigenvector of the largest
- *  eigenvalue, z of the smallest, each flipped so that at least half of the
- *  support has (p - k).axis >= 0, y = z cross x;
+ *  eigenvalue, z of the smallest; x flipped so that at least half of the
+ *  support has (p - k).x >= 0, z flipped so that sum (R - d)(n_p . z) >= 0;
+ *  y = z cross x;
  *  histogram: 2 radial shells (split at R/2) x 2 elevations x 8 azimuths x
  *  11 cosine bins of n_p . z, quadrilinear interpolation (azimuth circular,
  *  the others clamped at their ends), the keypoint itself excluded; the 352
- *  values are L2-normalised. */
-#define SHOT_PI 3.14159265358979f
+ *  values are L2-normalised.
+ * Arithmetic (the GPU kernel k_shot runs the same, so descriptors and LRFs
+ * agree bit for bit): every per-point term is a fixed sequence of IEEE
+ * single operations (no contraction: -ffp-contract=off); every sum over the
+ * support is an integer sum of fixed-point terms, each rounded to an int32
+ * (covariance terms in units of 2^-(30 - e3) with R^3 < 2^e3, z-sign terms
+ * in units of 2^-(30 - e1) with R < 2^e1, summed in int64; histogram votes
+ * in units of 2^-(31 - b), b the bit length of the support count, summed
+ * in uint32), so the order of the support does not matter; sums convert
+ * back by one int-to-float rounding and an exact power-of-two scale; angles
+ * come from shot_atan2 below; the norm is summed as 32 lanes of 11 bins
+ * each (lane l: bins l, l + 32, ...) closed by a xor butterfly. */
+#define SHOT_PI 0x1.921fb6p+1f
 #define SHOT_FACING (-0.2f)
 
 /* Convention switches for probes of descriptor repeatability (0 = the
@@ -866,6 +879,48 @@ int orc_uniform_sample(const float* pts, int n, float r, int32_t* out_idx) {
  * normals. */
 static int g_shot_flags = 0;
 void orc_set_shot_flags(int flags) { g_shot_flags = flags; }
+
+/* atan2 by the reduction atan(a) = pi/6 + atan((sqrt(3) a - 1) / (a +
+ * sqrt(3))) for a = min(|x|,|y|) / max(|x|,|y|) above tan(pi/12) (Cody and
+ * Waite, Software Manual for the Elementary Functions, 1980, ch. 11), the
+ * series u - u^3/3 + ... - u^11/11 on |u| <= tan(pi/12), then the octant and
+ * the signs; atan2(0, 0) = 0 and -0 counts as positive. */
+static float shot_atan2(float y, float x) {
+  const float ax = fabsf(x), ay = fabsf(y);
+  const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
+  if (!(mx > 0.f)) return 0.f;
+  const float a = mn / mx;
+  float u = a, base = 0.f;
+  if (a > 0x1.126146p-2f) {
+    u = (a * 0x1.bb67aep+0f - 1.f) / (a + 0x1.bb67aep+0f);
+    base = 0x1.0c1524p-1f;
+  }
+  const float z = u * u;
+  float p = -0x1.745d18p-4f;
+  p = p * z + 0x1.c71c72p-4f;
+  p = p * z + -0x1.24924ap-3f;
+  p = p * z + 0x1.99999ap-3f;
+  p = p * z + -0x1.555556p-2f;
+  p = p * z;
+  float r = base + (u + u * p);
+  if (ay > ax) r = 0x1.921fb6p+0f - r;
+  if (x < 0.f) r = SHOT_PI - r;
+  return y < 0.f ? -r : r;
+}
+
+static float dot3f(float a0, float a1, float a2, float b0, float b1, float b2) {
+  const float p0 = a0 * b0, p1 = a1 * b1, p2 = a2 * b2;
+  return (p0 + p1) + p2;
+}
+
+/* e with v < 2^e for a positive normal float v (frexp's exponent) */
+static int shot_exp2_above(float v) {
+  uint32_t u;
+  memcpy(&u, &v, 4);
+  return (int)((u >> 23) & 0xffu) - 126;
+}
+
+
 static void shot_bins(float pos, int nb, int circular, int* b0, float* w0, int* b1, float* w1) {
   const float fl = floorf(pos);
   int lo = (int)fl;
@@ -891,11 +946,13 @@ void orc_shot352(const float* pts, const float* normals, int n, const int32_t* k
   cgrid g;
   cg_build(&g, pts, n, R);
   const float R2 = R * R;
+  const int e_cov = 30 - shot_exp2_above(R2 * R), e_z = 30 - shot_exp2_above(R);
+  const float cov_scale = ldexpf(1.f, e_cov), cov_unscale = ldexpf(1.f, -e_cov), z_scale = ldexpf(1.f, e_z);
 #pragma omp parallel for schedule(dynamic, 16)
   for (int kk = 0; kk < nk; ++kk) {
     const float* kp = pts + 4 * keys[kk];
+    const float* nkp = normals + 4 * keys[kk];
     float* D = desc + (size_t)kk * 352;
-    for (int b = 0; b < 352; ++b) D[b] = 0.f;
     /* gather support by walking the 27 cells around the keypoint */
     int cap = 256, cnt = 0;
     int* sup = (int*)malloc(sizeof(int) * cap);
@@ -908,12 +965,8 @@ void orc_shot352(const float* pts, const float* normals, int n, const int32_t* k
           const int cell = (z * g.n[1] + y) * g.n[0] + x;
           for (int s = g.start[cell]; s < g.start[cell + 1]; ++s) {
             const int j = g.order[s];
-            /* support: within R, and facing the keypoint's hemisphere
-             * (n_j . n_k >= SHOT_FACING), i.e. surfaces one view sees together */
             const float* nj = normals + 4 * j;
-            const float* nkp = normals + 4 * keys[kk];
-            const float f0 = nj[0] * nkp[0], f1 = nj[1] * nkp[1], f2 = nj[2] * nkp[2];
-            const float facing = (f0 + f1) + f2;
+            const float facing = dot3f(nj[0], nj[1], nj[2], nkp[0], nkp[1], nkp[2]);
             if (d2f(kp, pts + 4 * j) <= R2 && (facing >= SHOT_FACING || (g_shot_flags & 1))) {
               if (cnt == cap) {
                 cap *= 2;
@@ -923,72 +976,66 @@ void orc_shot352(const float* pts, const float* normals, int n, const int32_t* k
             }
           }
         }
-    /* ascending index order so sums are order-independent of the walk */
-    for (int i = 1; i < cnt; ++i) {
-      int x = sup[i], j = i;
-      while (j > 0 && sup[j - 1] > x) {
-        sup[j] = sup[j - 1];
-        --j;
-      }
-      sup[j] = x;
-    }
-    float m[6] = {0, 0, 0, 0, 0, 0};
+    long long m[6] = {0, 0, 0, 0, 0, 0};
     for (int s = 0; s < cnt; ++s) {
       const float* p = pts + 4 * sup[s];
       const float dx = p[0] - kp[0], dy = p[1] - kp[1], dz = p[2] - kp[2];
-      const float d = sqrtf(d2f(p, kp));
-      const float w = R - d;
-      m[0] += w * dx * dx; m[1] += w * dx * dy; m[2] += w * dx * dz;
-      m[3] += w * dy * dy; m[4] += w * dy * dz; m[5] += w * dz * dz;
+      const float w = R - sqrtf(d2f(p, kp));
+      const float wx = w * dx, wy = w * dy, wz = w * dz;
+      m[0] += lrintf(wx * dx * cov_scale); m[1] += lrintf(wx * dy * cov_scale);
+      m[2] += lrintf(wx * dz * cov_scale); m[3] += lrintf(wy * dy * cov_scale);
+      m[4] += lrintf(wy * dz * cov_scale); m[5] += lrintf(wz * dz * cov_scale);
     }
-    /* SHOT LRF (weighted covariance eigenvectors: x largest, z smallest).
-     * Sign of x: the majority rule of the paper.  Sign of z: agreement with
-     * the support's oriented normals, sum_j w_j (n_j . z) >= 0 — the
-     * majority rule is a coin toss on flat patches, where every point lies in
-     * the tangent plane, while oriented normals are consistent between a
-     * model and a scene. */
-    const float M[9] = {m[0], m[1], m[2], m[1], m[3], m[4], m[2], m[4], m[5]};
+    const float m0 = (float)m[0] * cov_unscale, m1 = (float)m[1] * cov_unscale, m2 = (float)m[2] * cov_unscale,
+                m3 = (float)m[3] * cov_unscale, m4 = (float)m[4] * cov_unscale, m5 = (float)m[5] * cov_unscale;
+    const float M[9] = {m0, m1, m2, m1, m3, m4, m2, m4, m5};
     float ev[3], V[9];
     orc_eig3(M, ev, V);
     float X[3] = {V[2], V[5], V[8]}, Z[3] = {V[0], V[3], V[6]};
     int px = 0, nx = 0, pz = 0, nz = 0;
-    float zn = 0.f;
+    long long zn = 0;
     for (int s = 0; s < cnt; ++s) {
       const float* p = pts + 4 * sup[s];
       const float* nv = normals + 4 * sup[s];
       const float dx = p[0] - kp[0], dy = p[1] - kp[1], dz = p[2] - kp[2];
-      if (dx * X[0] + dy * X[1] + dz * X[2] >= 0.f) ++px; else ++nx;
-      if (dx * Z[0] + dy * Z[1] + dz * Z[2] >= 0.f) ++pz; else ++nz;
+      if (dot3f(dx, dy, dz, X[0], X[1], X[2]) >= 0.f) ++px; else ++nx;
+      if (dot3f(dx, dy, dz, Z[0], Z[1], Z[2]) >= 0.f) ++pz; else ++nz;
       const float w = R - sqrtf(d2f(p, kp));
-      zn += w * (nv[0] * Z[0] + nv[1] * Z[1] + nv[2] * Z[2]);
+      zn += lrintf(w * dot3f(nv[0], nv[1], nv[2], Z[0], Z[1], Z[2]) * z_scale);
     }
     if (px < nx) for (int a = 0; a < 3; ++a) X[a] = -X[a];
-    if ((g_shot_flags & 2) ? (pz < nz) : (zn < 0.f))
+    if ((g_shot_flags & 2) ? (pz < nz) : (zn < 0))
       for (int a = 0; a < 3; ++a) Z[a] = -Z[a];
     const float Y[3] = {Z[1] * X[2] - Z[2] * X[1], Z[2] * X[0] - Z[0] * X[2], Z[0] * X[1] - Z[1] * X[0]};
     if (lrf_out) {
       float* L = lrf_out + (size_t)kk * 9;
       for (int a = 0; a < 3; ++a) { L[a] = X[a]; L[3 + a] = Y[a]; L[6 + a] = Z[a]; }
     }
+    uint32_t H[352];
+    memset(H, 0, sizeof(H));
+    int bits = 0;
+    while (bits < 32 && (cnt >> bits) != 0) ++bits;
+    const float hs = ldexpf(1.f, 31 - bits), hu = ldexpf(1.f, bits - 31);
     for (int s = 0; s < cnt; ++s) {
       const float* p = pts + 4 * sup[s];
       const float d2 = d2f(p, kp);
       if (!(d2 > 0.f)) continue;
       const float dx = p[0] - kp[0], dy = p[1] - kp[1], dz = p[2] - kp[2];
-      const float lx = dx * X[0] + dy * X[1] + dz * X[2];
-      const float ly = dx * Y[0] + dy * Y[1] + dz * Y[2];
-      const float lz = dx * Z[0] + dy * Z[1] + dz * Z[2];
+      const float lx = dot3f(dx, dy, dz, X[0], X[1], X[2]);
+      const float ly = dot3f(dx, dy, dz, Y[0], Y[1], Y[2]);
+      const float lz = dot3f(dx, dy, dz, Z[0], Z[1], Z[2]);
       const float* nv = normals + 4 * sup[s];
-      float cs = nv[0] * Z[0] + nv[1] * Z[1] + nv[2] * Z[2];
-      cs = cs > 1.f ? 1.f : (cs < -1.f ? -1.f : cs);
+      float cs = dot3f(nv[0], nv[1], nv[2], Z[0], Z[1], Z[2]);
+      cs = fminf(fmaxf(cs, -1.f), 1.f);
       const float d = sqrtf(d2);
-      const float az = atan2f(ly, lx);
-      const float el = atan2f(lz, sqrtf(lx * lx + ly * ly));
+      const float az = shot_atan2(ly, lx);
+      const float lxx = lx * lx, lyy = ly * ly;
+      const float el = shot_atan2(lz, sqrtf(lxx + lyy));
       int cb0, cb1, ab0, ab1, eb0, eb1, rb0, rb1;
       float cw0, cw1, aw0, aw1, ew0, ew1, rw0, rw1;
       shot_bins((cs + 1.f) * 5.5f - 0.5f, 11, 0, &cb0, &cw0, &cb1, &cw1);
-      shot_bins((az + SHOT_PI) * (8.f / (2.f * SHOT_PI)) - 0.5f, 8, 1, &ab0, &aw0, &ab1, &aw1);
-      shot_bins((el + 0.5f * SHOT_PI) * (2.f / SHOT_PI) - 0.5f, 2, 0, &eb0, &ew0, &eb1, &ew1);
+      shot_bins((az + SHOT_PI) * 0x1.45f306p+0f - 0.5f, 8, 1, &ab0, &aw0, &ab1, &aw1);
+      shot_bins((el + 0x1.921fb6p+0f) * 0x1.45f306p-1f - 0.5f, 2, 0, &eb0, &ew0, &eb1, &ew1);
       shot_bins(d / R * 2.f - 0.5f, 2, 0, &rb0, &rw0, &rb1, &rw1);
       const int cb[2] = {cb0, cb1}, ab[2] = {ab0, ab1}, eb[2] = {eb0, eb1}, rb[2] = {rb0, rb1};
       const float cw[2] = {cw0, cw1}, aw[2] = {aw0, aw1}, ew[2] = {ew0, ew1}, rw[2] = {rw0, rw1};
@@ -998,15 +1045,24 @@ void orc_shot352(const float* pts, const float* normals, int n, const int32_t* k
             for (int i3 = 0; i3 < 2; ++i3) {
               const float w = rw[i0] * ew[i1] * aw[i2] * cw[i3];
               if (w == 0.f) continue;
-              D[((rb[i0] * 2 + eb[i1]) * 8 + ab[i2]) * 11 + cb[i3]] += w;
+              H[((rb[i0] * 2 + eb[i1]) * 8 + ab[i2]) * 11 + cb[i3]] += (uint32_t)lrintf(w * hs);
             }
     }
-    float ss = 0.f;
-    for (int b = 0; b < 352; ++b) ss += D[b] * D[b];
-    if (ss > 0.f) {
-      const float inv = 1.f / sqrtf(ss);
-      for (int b = 0; b < 352; ++b) D[b] *= inv;
+    float hb[352], lanes[32];
+    for (int b = 0; b < 352; ++b) hb[b] = (float)H[b] * hu;
+    for (int l = 0; l < 32; ++l) {
+      float s = 0.f;
+      for (int k = 0; k < 11; ++k) s = s + hb[l + 32 * k] * hb[l + 32 * k];
+      lanes[l] = s;
     }
+    for (int o = 16; o > 0; o >>= 1) {
+      float nxt[32];
+      for (int l = 0; l < 32; ++l) nxt[l] = lanes[l] + lanes[l ^ o];
+      memcpy(lanes, nxt, sizeof(lanes));
+    }
+    const float ss = lanes[0];
+    const float inv = ss > 0.f ? 1.f / sqrtf(ss) : 0.f;
+    for (int b = 0; b < 352; ++b) D[b] = hb[b] * inv;
     free(sup);
   }
   cg_free(&g);

@@ -359,18 +359,75 @@ __global__ void __launch_bounds__(256) k_orient_outward(const float4* __restrict
 // covariance (x largest, z smallest), x signed by the majority rule, z signed
 // by sum w (n_j . z) >= 0; 2 radial x 2 elevation x 8 azimuth volumes x 11
 // bins of cos(n_j, z), quadrilinear interpolation; L2 normalised.
+//
+// Bit-exact with the oracle's orc_shot352: every per-point term is a fixed
+// sequence of separately rounded IEEE operations, every sum over the support
+// is an integer sum of fixed-point terms (so the order in which lanes and
+// atomics add them cannot change the result), the angles come from
+// shot_atan2 below, and the final norm is summed in one stated order.  No
+// FP64: every conversion is a single-precision one.
 // ---------------------------------------------------------------------------
 constexpr int SHOT_WARPS = 8;
 constexpr float SHOT_FACING = -0.2f;
+constexpr float SHOT_PI = 0x1.921fb6p+1f;
+
+// Fixed-point scales.  Covariance terms are at most R^3 in magnitude and
+// z-sign terms at most R: each is scaled by 2^(30 - e), e the exponent with
+// bound < 2^e, so every term converts to an int32 and their sums are int64.
+// Histogram votes are at most 1 and a point casts at most one vote per bin,
+// so with ns support points and votes scaled by 2^(31 - bitlen(ns)) every
+// bin's sum fits a uint32.
+__device__ __forceinline__ int shot_exp2_above(float v) {  // e with v < 2^e (v > 0, normal)
+  return (int)((__float_as_uint(v) >> 23) & 0xffu) - 126;
+}
+
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }  // -126 <= e <= 127
+
+// atan2 for the angle bins, the same operations as the oracle's shot_atan2
+// (library atan2f differs between the GPU and host C libraries in the last
+// bits).  The ratio a = min(|x|,|y|) / max(|x|,|y|) lies in [0, 1]; above
+// tan(pi/12) the reduction atan(a) = pi/6 + atan((sqrt(3) a - 1) / (a +
+// sqrt(3))) (Cody and Waite, Software Manual for the Elementary Functions,
+// 1980, ch. 11) leaves |u| <= tan(pi/12), where the series u - u^3/3 + u^5/5
+// - u^7/7 + u^9/9 - u^11/11 is within 3e-9; then the octant and the signs.
+// atan2(0, 0) = 0, and -0 counts as positive.
+__device__ __forceinline__ float shot_atan2(float y, float x) {
+  const float ax = fabsf(x), ay = fabsf(y);
+  const float mx = fmaxf(ax, ay), mn = fminf(ax, ay);
+  if (!(mx > 0.f)) return 0.f;
+  const float a = __fdiv_rn(mn, mx);
+  float u = a, base = 0.f;
+  if (a > 0x1.126146p-2f) {  // tan(pi/12)
+    u = __fdiv_rn(__fsub_rn(__fmul_rn(a, 0x1.bb67aep+0f), 1.f), __fadd_rn(a, 0x1.bb67aep+0f));
+    base = 0x1.0c1524p-1f;  // pi/6
+  }
+  const float z = __fmul_rn(u, u);
+  float p = -0x1.745d18p-4f;                          // -1/11
+  p = __fadd_rn(__fmul_rn(p, z), 0x1.c71c72p-4f);     // 1/9
+  p = __fadd_rn(__fmul_rn(p, z), -0x1.24924ap-3f);    // -1/7
+  p = __fadd_rn(__fmul_rn(p, z), 0x1.99999ap-3f);     // 1/5
+  p = __fadd_rn(__fmul_rn(p, z), -0x1.555556p-2f);    // -1/3
+  p = __fmul_rn(p, z);
+  float r = __fadd_rn(base, __fadd_rn(u, __fmul_rn(u, p)));
+  if (ay > ax) r = __fsub_rn(0x1.921fb6p+0f, r);  // pi/2 - r
+  if (x < 0.f) r = __fsub_rn(SHOT_PI, r);
+  return y < 0.f ? -r : r;
+}
+
+__device__ __forceinline__ float dot3_exact(float a0, float a1, float a2, float b0, float b1, float b2) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(a0, b0), __fmul_rn(a1, b1)), __fmul_rn(a2, b2));
+}
+
+__device__ __forceinline__ int to_fixed(float t, float scale) { return __float2int_rn(__fmul_rn(t, scale)); }
 
 __device__ __forceinline__ void shot_bins(float pos, int nb, bool circular, int& b0, float& w0, int& b1, float& w1) {
   const float fl = floorf(pos);
   const int lo = (int)fl;
-  const float f = pos - fl;
+  const float f = __fsub_rn(pos, fl);
   if (circular) {
     b0 = ((lo % nb) + nb) % nb;
     b1 = (b0 + 1) % nb;
-    w0 = 1.f - f;
+    w0 = __fsub_rn(1.f, f);
     w1 = f;
     return;
   }
@@ -379,7 +436,7 @@ __device__ __forceinline__ void shot_bins(float pos, int nb, bool circular, int&
   } else if (lo >= nb - 1) {
     b0 = nb - 1; w0 = 1.f; b1 = nb - 1; w1 = 0.f;
   } else {
-    b0 = lo; w0 = 1.f - f; b1 = lo + 1; w1 = f;
+    b0 = lo; w0 = __fsub_rn(1.f, f); b1 = lo + 1; w1 = f;
   }
 }
 
@@ -394,17 +451,19 @@ __device__ __forceinline__ void shot_bins(float pos, int nb, bool circular, int&
           const float d2 = dist2_exact(kp, q);                                                   \
           if (!(d2 <= R2)) continue;                                                             \
           const float4 qn = nrm[qi];                                                             \
-          const float facing = __fadd_rn(__fadd_rn(__fmul_rn(qn.x, nk.x), __fmul_rn(qn.y, nk.y)), __fmul_rn(qn.z, nk.z)); \
+          const float facing = dot3_exact(qn.x, qn.y, qn.z, nk.x, nk.y, nk.z);                   \
           if (!(facing >= SHOT_FACING)) continue;                                                \
+          const float dx = __fsub_rn(q.x, kp.x), dy = __fsub_rn(q.y, kp.y), dz = __fsub_rn(q.z, kp.z); \
           __VA_ARGS__                                                                             \
         }                                                                                        \
       }
 
 // The support is gathered once, in pass 1, into a per-warp list in shared
-// memory (SHOT_CAP entries: offset from the keypoint and distance, normal);
-// passes 2 and 3 read the list.  Cells whose box lies beyond R are not
-// walked.  A keypoint with more support points than the list holds walks
-// the cells again in passes 2 and 3 (same sums, another order).
+// memory (SHOT_CAP entries: the offset from the keypoint with its squared
+// length, and the normal); passes 2 and 3 read the list.  Cells whose box
+// lies beyond R are not walked.  A keypoint with more support points than
+// the list holds walks the cells again in passes 2 and 3 (the fixed-point
+// sums make the order irrelevant).
 constexpr int SHOT_CAP = 176;  // with the histograms: 56 KB a block, four blocks an SM
 
 __device__ __forceinline__ float shot_cell_d2(const GridView& g, float4 q, int x, int y, int z) {
@@ -415,23 +474,27 @@ __device__ __forceinline__ float shot_cell_d2(const GridView& g, float4 q, int x
   return dx * dx + dy * dy + dz * dz;
 }
 
-// One support point's contribution to the histogram (16 interpolated bins).
-__device__ __forceinline__ void shot_add(float* H, float dx, float dy, float dz, float d, float cs, float R,
-                                         float X0, float X1, float X2, float Y0, float Y1, float Y2, float Z0,
-                                         float Z1, float Z2) {
-  const float PI = 3.14159265358979f;
-  const float lx = dx * X0 + dy * X1 + dz * X2;
-  const float ly = dx * Y0 + dy * Y1 + dz * Y2;
-  const float lz = dx * Z0 + dy * Z1 + dz * Z2;
-  cs = fminf(fmaxf(cs, -1.f), 1.f);
-  const float az = atan2f(ly, lx);
-  const float el = atan2f(lz, sqrtf(lx * lx + ly * ly));
+// One support point's contribution to the histogram (16 interpolated bins,
+// fixed-point votes, scale hs, added by shared-memory atomics).  (dx, dy,
+// dz): offset from the keypoint, d2 its exact squared length (> 0), n the
+// point's normal.
+__device__ __forceinline__ void shot_add(unsigned* H, float hs, float dx, float dy, float dz, float d2, float4 n,
+                                         float R, float X0, float X1, float X2, float Y0, float Y1, float Y2,
+                                         float Z0, float Z1, float Z2) {
+  const float lx = dot3_exact(dx, dy, dz, X0, X1, X2);
+  const float ly = dot3_exact(dx, dy, dz, Y0, Y1, Y2);
+  const float lz = dot3_exact(dx, dy, dz, Z0, Z1, Z2);
+  const float cs = fminf(fmaxf(dot3_exact(n.x, n.y, n.z, Z0, Z1, Z2), -1.f), 1.f);
+  const float d = __fsqrt_rn(d2);
+  const float az = shot_atan2(ly, lx);
+  const float el = shot_atan2(lz, __fsqrt_rn(__fadd_rn(__fmul_rn(lx, lx), __fmul_rn(ly, ly))));
   int cb[2], ab[2], eb[2], rb[2];
   float cw[2], aw[2], ew[2], rw[2];
-  shot_bins((cs + 1.f) * 5.5f - 0.5f, 11, false, cb[0], cw[0], cb[1], cw[1]);
-  shot_bins((az + PI) * (8.f / (2.f * PI)) - 0.5f, 8, true, ab[0], aw[0], ab[1], aw[1]);
-  shot_bins((el + 0.5f * PI) * (2.f / PI) - 0.5f, 2, false, eb[0], ew[0], eb[1], ew[1]);
-  shot_bins(d / R * 2.f - 0.5f, 2, false, rb[0], rw[0], rb[1], rw[1]);
+  shot_bins(__fsub_rn(__fmul_rn(__fadd_rn(cs, 1.f), 5.5f), 0.5f), 11, false, cb[0], cw[0], cb[1], cw[1]);
+  shot_bins(__fsub_rn(__fmul_rn(__fadd_rn(az, SHOT_PI), 0x1.45f306p+0f), 0.5f), 8, true, ab[0], aw[0], ab[1], aw[1]);
+  shot_bins(__fsub_rn(__fmul_rn(__fadd_rn(el, 0x1.921fb6p+0f), 0x1.45f306p-1f), 0.5f), 2, false, eb[0], ew[0], eb[1],
+            ew[1]);
+  shot_bins(__fsub_rn(__fmul_rn(__fdiv_rn(d, R), 2.f), 0.5f), 2, false, rb[0], rw[0], rb[1], rw[1]);
 #pragma unroll
   for (int i0 = 0; i0 < 2; ++i0)
 #pragma unroll
@@ -440,9 +503,15 @@ __device__ __forceinline__ void shot_add(float* H, float dx, float dy, float dz,
       for (int i2 = 0; i2 < 2; ++i2)
 #pragma unroll
         for (int i3 = 0; i3 < 2; ++i3) {
-          const float w = rw[i0] * ew[i1] * aw[i2] * cw[i3];
-          if (w != 0.f) atomicAdd(&H[((rb[i0] * 2 + eb[i1]) * 8 + ab[i2]) * 11 + cb[i3]], w);
+          const float w = __fmul_rn(__fmul_rn(__fmul_rn(rw[i0], ew[i1]), aw[i2]), cw[i3]);
+          if (w != 0.f) atomicAdd(&H[((rb[i0] * 2 + eb[i1]) * 8 + ab[i2]) * 11 + cb[i3]], __float2uint_rn(__fmul_rn(w, hs)));
         }
+}
+
+__device__ __forceinline__ long long warp_sum_ll(long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
 }
 
 __global__ void __launch_bounds__(SHOT_WARPS * 32, 4) k_shot(GridDev gd, const float4* __restrict__ pts,
@@ -450,15 +519,17 @@ __global__ void __launch_bounds__(SHOT_WARPS * 32, 4) k_shot(GridDev gd, const f
                                                           const int* __restrict__ keys, int nk_host,
                                                           const int* d_nk, float R,
                                                           float* __restrict__ desc, float* __restrict__ lrf) {
-  __shared__ float hist[SHOT_WARPS][352];
-  __shared__ float4 s_off[SHOT_WARPS][SHOT_CAP];  // (dx, dy, dz, d)
+  __shared__ unsigned hist[SHOT_WARPS][352];
+  __shared__ float4 s_off[SHOT_WARPS][SHOT_CAP];  // (dx, dy, dz, d^2)
   __shared__ float4 s_nrm[SHOT_WARPS][SHOT_CAP];  // normal
   const GridView g = load_view(gd);
   const int nk_total = cnt_of(nk_host, d_nk);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const float R2 = __fmul_rn(R, R);
   const float cell_r2 = R2 * 1.0001f + 1e-12f;  // a cell is walked when its box is within R (with a margin)
-  float* H = hist[wid];
+  const int e_cov = 30 - shot_exp2_above(__fmul_rn(R2, R)), e_z = 30 - shot_exp2_above(R);
+  const float cov_scale = pow2f(e_cov), cov_unscale = pow2f(-e_cov), z_scale = pow2f(e_z);
+  unsigned* H = hist[wid];
   float4* SO = s_off[wid];
   float4* SN = s_nrm[wid];
   for (int kk = blockIdx.x * SHOT_WARPS + wid; kk < nk_total; kk += gridDim.x * SHOT_WARPS) {
@@ -468,8 +539,8 @@ __global__ void __launch_bounds__(SHOT_WARPS * 32, 4) k_shot(GridDev gd, const f
     const int cx = min(max(q_cell(kp.x, g.ox, g.inv_h), 0), g.nx - 1);
     const int cy = min(max(q_cell(kp.y, g.oy, g.inv_h), 0), g.ny - 1);
     const int cz = min(max(q_cell(kp.z, g.oz, g.inv_h), 0), g.nz - 1);
-    // pass 1: weighted covariance, and the support gathered in walk order
-    float m0 = 0.f, m1 = 0.f, m2 = 0.f, m3 = 0.f, m4 = 0.f, m5 = 0.f;
+    // pass 1: weighted covariance (fixed point), and the support gathered in walk order
+    long long m0 = 0, m1 = 0, m2 = 0, m3 = 0, m4 = 0, m5 = 0;
     int ns = 0;
     for (int z = max(cz - 1, 0); z <= min(cz + 1, g.nz - 1); ++z)
       for (int y = max(cy - 1, 0); y <= min(cy + 1, g.ny - 1); ++y)
@@ -486,98 +557,108 @@ __global__ void __launch_bounds__(SHOT_WARPS * 32, 4) k_shot(GridDev gd, const f
               d2 = dist2_exact(kp, q);
               if (d2 <= R2) {
                 qn = nrm[pt_index(q)];
-                const float facing =
-                    __fadd_rn(__fadd_rn(__fmul_rn(qn.x, nk.x), __fmul_rn(qn.y, nk.y)), __fmul_rn(qn.z, nk.z));
-                in = facing >= SHOT_FACING;
+                in = dot3_exact(qn.x, qn.y, qn.z, nk.x, nk.y, nk.z) >= SHOT_FACING;
               }
             }
-            const float dx = q.x - kp.x, dy = q.y - kp.y, dz = q.z - kp.z;
+            const float dx = __fsub_rn(q.x, kp.x), dy = __fsub_rn(q.y, kp.y), dz = __fsub_rn(q.z, kp.z);
             if (in) {
-              const float w = R - sqrtf(d2);
-              m0 += w * dx * dx; m1 += w * dx * dy; m2 += w * dx * dz;
-              m3 += w * dy * dy; m4 += w * dy * dz; m5 += w * dz * dz;
+              const float w = __fsub_rn(R, __fsqrt_rn(d2));
+              const float wx = __fmul_rn(w, dx), wy = __fmul_rn(w, dy);
+              m0 += to_fixed(__fmul_rn(wx, dx), cov_scale);
+              m1 += to_fixed(__fmul_rn(wx, dy), cov_scale);
+              m2 += to_fixed(__fmul_rn(wx, dz), cov_scale);
+              m3 += to_fixed(__fmul_rn(wy, dy), cov_scale);
+              m4 += to_fixed(__fmul_rn(wy, dz), cov_scale);
+              m5 += to_fixed(__fmul_rn(__fmul_rn(w, dz), dz), cov_scale);
             }
             const unsigned bal = __ballot_sync(0xffffffffu, in);
             const int slot = ns + __popc(bal & lanemask_lt());
             if (in && slot < SHOT_CAP) {
-              SO[slot] = make_float4(dx, dy, dz, sqrtf(d2));
+              SO[slot] = make_float4(dx, dy, dz, d2);
               SN[slot] = qn;
             }
             ns += __popc(bal);
           }
         }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      m0 += __shfl_xor_sync(0xffffffffu, m0, o);
-      m1 += __shfl_xor_sync(0xffffffffu, m1, o);
-      m2 += __shfl_xor_sync(0xffffffffu, m2, o);
-      m3 += __shfl_xor_sync(0xffffffffu, m3, o);
-      m4 += __shfl_xor_sync(0xffffffffu, m4, o);
-      m5 += __shfl_xor_sync(0xffffffffu, m5, o);
-    }
     __syncwarp();
     const bool listed = ns <= SHOT_CAP;
-    const float M[9] = {m0, m1, m2, m1, m3, m4, m2, m4, m5};
+    float M[9];
+    M[0] = __fmul_rn(__ll2float_rn(warp_sum_ll(m0)), cov_unscale);
+    M[1] = M[3] = __fmul_rn(__ll2float_rn(warp_sum_ll(m1)), cov_unscale);
+    M[2] = M[6] = __fmul_rn(__ll2float_rn(warp_sum_ll(m2)), cov_unscale);
+    M[4] = __fmul_rn(__ll2float_rn(warp_sum_ll(m3)), cov_unscale);
+    M[5] = M[7] = __fmul_rn(__ll2float_rn(warp_sum_ll(m4)), cov_unscale);
+    M[8] = __fmul_rn(__ll2float_rn(warp_sum_ll(m5)), cov_unscale);
     float ev[3], V[9];
     eig3_exact(M, ev, V);
     float X0 = V[2], X1 = V[5], X2 = V[8], Z0 = V[0], Z1 = V[3], Z2 = V[6];
-    // pass 2: signs
+    // pass 2: signs (x: majority of offsets; z: sum of w (n . z), fixed point)
     int px = 0, nx = 0;
-    float zn = 0.f;
+    long long zn = 0;
     if (listed) {
       for (int i = lane; i < ns; i += 32) {
         const float4 o = SO[i], qn = SN[i];
-        if (o.x * X0 + o.y * X1 + o.z * X2 >= 0.f) ++px; else ++nx;
-        zn += (R - o.w) * (qn.x * Z0 + qn.y * Z1 + qn.z * Z2);
+        if (dot3_exact(o.x, o.y, o.z, X0, X1, X2) >= 0.f) ++px; else ++nx;
+        const float w = __fsub_rn(R, __fsqrt_rn(o.w));
+        zn += to_fixed(__fmul_rn(w, dot3_exact(qn.x, qn.y, qn.z, Z0, Z1, Z2)), z_scale);
       }
     } else {
       SHOT_FOR_SUPPORT({
-        const float dx = q.x - kp.x, dy = q.y - kp.y, dz = q.z - kp.z;
-        if (dx * X0 + dy * X1 + dz * X2 >= 0.f) ++px; else ++nx;
-        zn += (R - sqrtf(d2)) * (qn.x * Z0 + qn.y * Z1 + qn.z * Z2);
+        if (dot3_exact(dx, dy, dz, X0, X1, X2) >= 0.f) ++px; else ++nx;
+        const float w = __fsub_rn(R, __fsqrt_rn(d2));
+        zn += to_fixed(__fmul_rn(w, dot3_exact(qn.x, qn.y, qn.z, Z0, Z1, Z2)), z_scale);
       })
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       px += __shfl_xor_sync(0xffffffffu, px, o);
       nx += __shfl_xor_sync(0xffffffffu, nx, o);
-      zn += __shfl_xor_sync(0xffffffffu, zn, o);
     }
+    zn = warp_sum_ll(zn);
     if (px < nx) { X0 = -X0; X1 = -X1; X2 = -X2; }
-    if (zn < 0.f) { Z0 = -Z0; Z1 = -Z1; Z2 = -Z2; }
-    const float Y0 = Z1 * X2 - Z2 * X1, Y1 = Z2 * X0 - Z0 * X2, Y2 = Z0 * X1 - Z1 * X0;
+    if (zn < 0) { Z0 = -Z0; Z1 = -Z1; Z2 = -Z2; }
+    const float Y0 = __fsub_rn(__fmul_rn(Z1, X2), __fmul_rn(Z2, X1));
+    const float Y1 = __fsub_rn(__fmul_rn(Z2, X0), __fmul_rn(Z0, X2));
+    const float Y2 = __fsub_rn(__fmul_rn(Z0, X1), __fmul_rn(Z1, X0));
     if (lrf && lane == 0) {
       float* L = lrf + (size_t)kk * 9;
       L[0] = X0; L[1] = X1; L[2] = X2; L[3] = Y0; L[4] = Y1; L[5] = Y2; L[6] = Z0; L[7] = Z1; L[8] = Z2;
     }
-    for (int b = lane; b < 352; b += 32) H[b] = 0.f;
+    for (int b = lane; b < 352; b += 32) H[b] = 0u;
     __syncwarp();
     // pass 3: histogram (the keypoint itself, d = 0, does not vote)
+    const int e_h = 31 - (32 - __clz(ns));
+    const float hs = pow2f(e_h);
     if (listed) {
       for (int i = lane; i < ns; i += 32) {
-        const float4 o = SO[i], qn = SN[i];
-        if (o.w > 0.f)
-          shot_add(H, o.x, o.y, o.z, o.w, qn.x * Z0 + qn.y * Z1 + qn.z * Z2, R, X0, X1, X2, Y0, Y1, Y2, Z0, Z1, Z2);
+        const float4 o = SO[i];
+        if (o.w > 0.f) shot_add(H, hs, o.x, o.y, o.z, o.w, SN[i], R, X0, X1, X2, Y0, Y1, Y2, Z0, Z1, Z2);
       }
     } else {
       SHOT_FOR_SUPPORT({
-        if (d2 > 0.f)
-          shot_add(H, q.x - kp.x, q.y - kp.y, q.z - kp.z, sqrtf(d2), qn.x * Z0 + qn.y * Z1 + qn.z * Z2, R, X0, X1, X2,
-                   Y0, Y1, Y2, Z0, Z1, Z2);
+        if (d2 > 0.f) shot_add(H, hs, dx, dy, dz, d2, qn, R, X0, X1, X2, Y0, Y1, Y2, Z0, Z1, Z2);
       })
     }
     __syncwarp();
+    // L2 norm: lane l sums bins l, l + 32, ..., l + 320 in order, then the
+    // xor butterfly (each step adds the same two values in both lanes)
+    float hb[11];
     float ss = 0.f;
-    for (int b = lane; b < 352; b += 32) ss += H[b] * H[b];
+    const float hu = pow2f(-e_h);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
-    const float inv = ss > 0.f ? 1.f / sqrtf(ss) : 0.f;
+    for (int k = 0; k < 11; ++k) {
+      hb[k] = __fmul_rn(__uint2float_rn(H[lane + 32 * k]), hu);
+      ss = __fadd_rn(ss, __fmul_rn(hb[k], hb[k]));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ss = __fadd_rn(ss, __shfl_xor_sync(0xffffffffu, ss, o));
+    const float inv = ss > 0.f ? __fdiv_rn(1.f, __fsqrt_rn(ss)) : 0.f;
     float* D = desc + (size_t)kk * 352;
-    for (int b = lane; b < 352; b += 32) D[b] = H[b] * inv;
+#pragma unroll
+    for (int k = 0; k < 11; ++k) D[lane + 32 * k] = __fmul_rn(hb[k], inv);
     __syncwarp();
   }
 }
-
 // ---------------------------------------------------------------------------
 // host entry points
 // ---------------------------------------------------------------------------
@@ -625,6 +706,8 @@ rtr_status normals_dev(rtr_context* ctx, Scratch& s, const float4* pts, int n_ca
 // SHOT over a grid of the points already built with cell R (grid_build).
 rtr_status shot_on_grid(const GridBufs& gb, const float4* pts, const float4* nrm, const int* keys, int nk_cap,
                         const int* d_nk, float R, float* desc, float* lrf, cudaStream_t st) {
+  // the fixed-point scales of k_shot are powers of two derived from R
+  if (!(R >= 1e-6f && R <= 1e6f)) return fail(RTR_ERR_INVALID_ARG, "shot: radius outside [1e-6, 1e6]");
   k_shot<<<blocks_for(nk_cap, SHOT_WARPS, 152 * 32), SHOT_WARPS * 32, 0, st>>>(grid_dev(gb), pts, nrm, keys, nk_cap,
                                                                                 d_nk, R, desc, lrf);
   RTR_LAUNCHED(1);

@@ -1,8 +1,8 @@
 """End-to-end: rtr_recognize on the GPU vs the oracle pipeline.
 
-Voxel and keypoint counts must match exactly; correspondence and cluster
-counts within a few percent (SHOT is compared with a tolerance); the best
-instance within 1 cm / 1 degree of the oracle's and of the ground truth."""
+Voxel, keypoint and correspondence counts must match exactly (every stage
+up to the matcher is bit-exact); the best instance within 1 cm / 1 degree of
+the oracle's and of the ground truth."""
 import numpy as np
 import pytest
 
@@ -36,7 +36,8 @@ def test_recognize_pair_matches_oracle(ctx, rtr, seed):
     ref = OP.recognize(om, seg, OP.params(scene_outward=1))
     assert res["n_voxels"] == ref["n_voxels"]
     assert res["n_keypoints"] == ref["n_keypoints"]
-    assert abs(res["n_correspondences"] - ref["n_correspondences"]) <= 0.03 * ref["n_correspondences"] + 3
+    assert res["n_correspondences"] == ref["n_correspondences"]
+    assert res["n_clusters"] == ref["n_clusters"]
     assert res["instances"], res
     g = res["instances"][0]["pose"]
     dt, dr = O.pose_error(g, ref["instances"][0]["pose"])
@@ -67,9 +68,9 @@ def test_recognize_host_entry_and_empty_scene(ctx, rtr):
 
 def test_recognize_main_clouds_matches_oracle(ctx, rtr):
     """The recognition chain on main's own inputs (chair1.pcd as the model,
-    T0_m8111.pcd as the segment; tests/golden/main_clouds.npz): voxels and
-    keypoints exact, correspondences within 3 %, the same instance as the
-    oracle pipeline within 1 cm / 1 degree."""
+    T0_m8111.pcd as the segment; tests/golden/main_clouds.npz): voxels,
+    keypoints and correspondences exact, the same instance as the oracle
+    pipeline within 1 cm / 1 degree."""
     from pathlib import Path
     d = np.load(Path(__file__).resolve().parent / "golden" / "main_clouds.npz")
     model, scan = d["chair1"], d["T0_m8111"]
@@ -80,7 +81,7 @@ def test_recognize_main_clouds_matches_oracle(ctx, rtr):
     res = rtr.parse_recog_result(rtr.recognize(ctx, m, _dev(scan), prm))
     ref = OP.recognize(om, scan, OP.params(scene_outward=1))
     assert res["n_voxels"] == ref["n_voxels"] and res["n_keypoints"] == ref["n_keypoints"]
-    assert abs(res["n_correspondences"] - ref["n_correspondences"]) <= 0.03 * ref["n_correspondences"] + 3
+    assert res["n_correspondences"] == ref["n_correspondences"]
     assert len(res["instances"]) == len(ref["instances"]) == 1, (res["instances"], ref["instances"])
     dt, dr = O.pose_error(res["instances"][0]["pose"], ref["instances"][0]["pose"])
     assert dt < 0.01 and dr < np.radians(1.0), (dt, dr)

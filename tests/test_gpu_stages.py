@@ -2,8 +2,9 @@
 
 Voxel filter, uniform sampling, normals and the outward orientation are
 integer/rounding-exact restatements: bit-exact.  SHOT sums its support in
-warp order with FP32 atomics, so it is compared with a tolerance.  The
-descriptor matcher is bit-exact (sequential FP32 sums, lowest-index ties)."""
+64-bit fixed point (order-free) with the same IEEE operations per term as
+the oracle: descriptors and LRFs bit-exact.  The descriptor matcher is
+bit-exact (sequential FP32 sums, lowest-index ties)."""
 import numpy as np
 import pytest
 
@@ -89,9 +90,8 @@ def test_shot352_matches_oracle(ctx, clouds):
         got, glrf = ctx.shot352(_dev(v), _dev(n), torch.from_numpy(keys).cuda(), 0.04, lrf=True)
         got = _host(got)
         ref, rlrf = O.shot352(v, n, keys, 0.04)
-        err = np.abs(got - ref).max(axis=1)
-        # the LRF sign rules can flip on exact ties; everything else agrees
-        assert (err < 1e-3).mean() > 0.995, (err < 1e-3).mean()
+        assert np.array_equal(got, ref), (np.abs(got - ref).max(axis=1) > 0).sum()
+        assert np.array_equal(_host(glrf), rlrf)
         # unit-norm histograms, or all-zero for a keypoint with an empty support
         nrm = np.linalg.norm(got, axis=1)
         assert np.all((np.abs(nrm - 1.0) < 1e-5) | (nrm == 0.0))
