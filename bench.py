@@ -604,13 +604,27 @@ def learned_room_block(ctx, R, m, s_d, prm, mlp, steps, stream, flush, plain) ->
         ev[i][1].record(stream)
     torch.cuda.synchronize()
     ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+    # stage times of the same recognition, profiled (each stage bracketed by
+    # events, kernels launched by the host)
+    ctx.set_profiling(True)
+    ctx.profile(clear=True)
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize()
+    stage_ms = {}
+    for nm, t in ctx.profile(clear=True):
+        stage_ms[nm] = stage_ms.get(nm, 0.0) + t / 3
+    ctx.set_profiling(False)
+    gcs = ctx.gc_stats()
     rl = R.parse_recog_result(res)
     same = len(rl["instances"]) == len(plain["instances"]) and all(
         np.abs(a["pose"][:3, 3] - b["pose"][:3, 3]).max() <= 0.01 for a, b in zip(rl["instances"], plain["instances"]))
     return {"metric": "scene recognitions/s, learned form (keep 0.25), config 1", "value": 1e3 / ms,
             "unit": "recognitions/s", "ms_per_step": ms, "n_keypoints_matched": rl["n_keypoints"],
-            "n_correspondences": rl["n_correspondences"], "instances": len(rl["instances"]),
-            "agrees_with_plain_1cm": bool(same)}
+            "n_correspondences": rl["n_correspondences"], "n_clusters": rl["n_clusters"],
+            "instances": len(rl["instances"]), "agrees_with_plain_1cm": bool(same),
+            "stage_ms": {k: round(v, 3) for k, v in stage_ms.items()},
+            "grouping_walk": {"seeds_walked": gcs["walk_end"], "rounds": gcs["rounds"]}}
 
 
 def ref_route_block(ctx, R, steps: int, cpu: bool) -> dict:

@@ -7,7 +7,8 @@ seconds, and through size-independent properties where it does not:
 - matching: all 115k scene descriptors against the 9.2k-row model
   database, indices and distances bit-exact against the oracle;
 - grouping: every cluster is pairwise consistent, clusters are disjoint and
-  none is below the threshold;
+  none is below the threshold; and the whole chain against the oracle
+  pipeline: the same correspondences, clusters member for member, counts;
 - recognition: deterministic (two runs give the same bytes) and the host
   entry point gives what the device one does."""
 import numpy as np
@@ -110,6 +111,52 @@ def test_room_grouping_properties(ctx, rtr, room):
         ds = np.sqrt(((ps[:, None, :] - ps[None, :, :]) ** 2).sum(-1, dtype=np.float32)).astype(np.float32)
         # float32 arithmetic in numpy's order: a 1e-5 slack covers the rounding difference
         assert np.all(np.abs(dm - ds) <= 0.01 + 1e-5)
+
+
+def test_room_chain_matches_oracle_pipeline(ctx, rtr, room):
+    """The whole room against the oracle pipeline (every stage bit-exact up
+    to the matcher, SHOT included): the same scene keypoints, the same
+    correspondences (model and scene index per pair, strict d^2 < 0.25), the
+    same clusters member for member with poses within 1e-7 of the oracle's,
+    and the same counts out of rtr_recognize."""
+    import torch
+    from oracle import pipeline as OP
+    from realtime_robot_gb300.learned import _model_features, _scene_features
+    scene, model = room
+    prm = rtr.recog_default_params(viewpoint=CAM)
+    p = OP.params(viewpoint=CAM)
+    om = OP.prepare_model(model, p)
+    st = {}
+    ref = OP.recognize(om, scene, p, stages=st)
+    mk, mdesc = _model_features(ctx, _dev(model), prm)
+    sk, sdesc = _scene_features(ctx, _dev(scene), prm)
+    skr = st["sv"][st["keys"]]
+    assert np.array_equal(sk.cpu().numpy()[:, :3], skr[:, :3])
+    idx, d2 = ctx.match(sdesc, mdesc)
+    keep = (idx >= 0) & (d2 < prm.match_max_d2)
+    cs = torch.nonzero(keep).flatten().int()
+    cm = idx[keep].int()
+    cd = d2[keep].float()
+    assert np.array_equal(cs.cpu().numpy(), st["corr_s"]) and np.array_equal(cm.cpu().numpy(), st["corr_m"])
+    mem, sizes, poses = ctx.gc_group(mk, sk, cm, cs, cd, prm.gc_size, prm.gc_thresh, prm.max_clusters, 512)
+    mem, sizes, poses = mem.cpu().numpy(), sizes.cpu().numpy(), poses.cpu().numpy()
+    assert np.array_equal(cd.cpu().numpy(), st["d2"][st["corr_s"]])
+    _, rposes, rsizes = O.gc_group(om["kp"], skr, st["corr_m"], st["corr_s"], st["d2"][st["corr_s"]], p["gc_size"],
+                                   p["gc_thresh"], p["max_clusters"])
+    assert np.array_equal(sizes, rsizes) and len(sizes) == ref["n_clusters"]
+    for c in range(len(sizes)):
+        assert set(mem[c][: sizes[c]].tolist()) == set(np.nonzero(st["cluster_of"] == c)[0].tolist()), c
+        dt, dr = O.pose_error(poses[c], rposes[c])
+        assert dt < 1e-7 and dr < 1e-7, (c, dt, dr)
+    m = rtr.Model(ctx, _dev(model), prm)
+    r = rtr.parse_recog_result(rtr.recognize(ctx, m, _dev(scene), prm))
+    for k in ("n_voxels", "n_keypoints", "n_correspondences", "n_clusters"):
+        assert r[k] == ref[k], (k, r[k], ref[k])
+    assert len(r["instances"]) == len(ref["instances"])
+    for a, b in zip(r["instances"], ref["instances"]):
+        dt, dr = O.pose_error(a["pose"], b["pose"])
+        assert dt < 1e-5 and dr < 1e-5, (dt, dr)
+    m.close()
 
 
 def test_room_recognition_deterministic_and_host_entry(ctx, rtr, room):
