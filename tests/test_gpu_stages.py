@@ -97,6 +97,21 @@ def test_shot352_matches_oracle(ctx, clouds):
         assert np.all((np.abs(nrm - 1.0) < 1e-5) | (nrm == 0.0))
 
 
+def test_shot352_independent_of_point_order(ctx, clouds):
+    """The same voxels in a shuffled order (so the grid cells hold them in
+    another order and the lanes meet them in another order) give the same
+    descriptor and LRF bits per keypoint."""
+    import torch
+    v = O.voxel_downsample(clouds[1], 0.01)
+    n = O.normals(v, 10, (0.0, -2.5, 1.5))
+    keys = O.uniform_sample(v, 0.02)
+    perm = np.random.default_rng(9).permutation(len(v))
+    inv = np.argsort(perm).astype(np.int32)
+    a, la = ctx.shot352(_dev(v), _dev(n), torch.from_numpy(keys).cuda(), 0.04, lrf=True)
+    b, lb = ctx.shot352(_dev(v[perm]), _dev(n[perm]), torch.from_numpy(inv[keys]).cuda(), 0.04, lrf=True)
+    assert torch.equal(a, b) and torch.equal(la, lb)
+
+
 def test_match_exact_bit_exact(ctx, clouds):
     v = O.voxel_downsample(clouds[0], 0.01)
     n = O.normals(v, 10, (0, 0, 0))

@@ -174,3 +174,28 @@ def test_range_search_oracle_against_numpy():
                 row[: min(m, len(hits))] = hits[:m]
                 assert np.array_equal(idx[i], row)
     assert O.range_search(q, t, 0.25, False, 4)[1][3] == 0
+
+
+def test_shot_descriptors_do_not_depend_on_point_order():
+    """The SHOT restatement sums each keypoint's support in fixed point, so
+    the descriptor of a keypoint and its LRF are the same bits whatever the
+    order of the cloud (the GPU adds the support in lane and atomic order;
+    this property is what lets the two agree bit for bit)."""
+    rng = np.random.default_rng(5)
+    pts = np.zeros((6000, 4), np.float32)
+    # a box corner and a curved patch: support with every LRF case
+    pts[:2000, :3] = rng.uniform(0, 0.1, (2000, 3)) * [1, 1, 0]
+    pts[2000:4000, :3] = rng.uniform(0, 0.1, (2000, 3)) * [1, 0, 1]
+    t = rng.uniform(0, np.pi, 2000)
+    z = rng.uniform(0, 0.1, 2000)
+    pts[4000:, 0], pts[4000:, 1], pts[4000:, 2] = 0.2 + 0.05 * np.cos(t), 0.05 * np.sin(t), z
+    v = O.voxel_downsample(pts, 0.005)
+    n = O.normals(v, 10, (0.5, 0.5, 0.5))
+    k = O.uniform_sample(v, 0.02)
+    d, lrf = O.shot352(v, n, k, 0.04)
+    perm = rng.permutation(len(v))
+    inv = np.argsort(perm)
+    d2, lrf2 = O.shot352(v[perm], n[perm], inv[k].astype(np.int32), 0.04)
+    assert np.array_equal(d, d2) and np.array_equal(lrf, lrf2)
+    nrm = np.linalg.norm(d, axis=1)
+    assert np.all(np.abs(nrm - 1.0) < 1e-5)
