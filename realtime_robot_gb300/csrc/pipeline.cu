@@ -497,6 +497,9 @@ struct SceneBufs {
   const int* keys_m;
   const int* d_nk;
   const float* desc_m;
+  // recorded on the side stream once the scene grid is built: a stream waits
+  // on it before the first stage that reads the grid (verification)
+  cudaEvent_t grid_ready = nullptr;
 };
 
 // Model-side buffers: correspondences, hypotheses, refinement.
@@ -670,7 +673,8 @@ static rtr_status scene_stages(rtr_context* ctx, const Scratch& stage, SceneBufs
   // The keypoints, the descriptors' grid and the scene grid need only the
   // voxels: they run on the context's side stream beside the normals, the
   // descriptors and pruning (small sort-bound kernels that leave most of the
-  // GPU idle), joined before the descriptors and at the end.
+  // GPU idle), joined before the descriptors and, for the scene grid (its
+  // own buffers), before verification.
   RTR_TRY(side_stream_ready(ctx));
   cudaStream_t ax = ctx->side_stream;
   RTR_CUDA(cudaEventRecord(ctx->ev_side[0], st));
@@ -755,7 +759,7 @@ static rtr_status scene_stages(rtr_context* ctx, const Scratch& stage, SceneBufs
     dKeys = b.cnt + 3;
     desc = b.desc_p;
   }
-  RTR_CUDA(cudaStreamWaitEvent(st, ctx->ev_side[2], 0));  // the scene grid
+  b.grid_ready = ctx->ev_side[2];  // the scene grid: joined by model_stages
   b.keys_m = keys;
   b.d_nk = dKeys;
   b.desc_m = desc;
@@ -797,6 +801,7 @@ static rtr_status model_stages(rtr_context* ctx, const Scratch& stage, const Sce
                            st));
   }
   const int H = q->max_clusters, M = q->refine_top;
+  if (sb.grid_ready) RTR_CUDA(cudaStreamWaitEvent(st, sb.grid_ready, 0));  // the scene grid (side stream)
   {
     ProfScope ps(ctx, st, "verify");
     RTR_TRY(hv_score(grid_dev(sb.grid), m->vox, m->n_vox, q->hv_subsample > 0 ? q->hv_subsample : 1, b.poses, H,
@@ -882,6 +887,7 @@ static rtr_status recognize_multi_impl(rtr_context* ctx, const rtr_model* const*
     return RTR_OK;
   }
   RTR_TRY(scene_stages(ctx, s, sb, scene, n, q, mlp, keep, st));
+  RTR_CUDA(cudaStreamWaitEvent(st, sb.grid_ready, 0));  // joined before the workers fork
   RTR_TRY(batch_ensure_workers(ctx, nw));
   ScratchPlan mp;
   model_plan(mp, n, q);
