@@ -1,8 +1,8 @@
 """Repeatability of the SHOT-352 descriptor under the workload's parameters
 (1 cm voxels, k=10 normals, 2 cm keypoints, 4 cm support), measured on the
-oracle, whose stages the GPU path reproduces bit for bit (SHOT within 1e-3
-per bin).  These figures bound what the recognition chain can find on the
-config-1 room:
+oracle, whose stages the GPU path reproduces bit for bit (SHOT included).
+These figures bound what the recognition chain can find on the config-1
+room:
 
 - the descriptor is exactly rotation invariant on identical points;
 - a second random sample of the same full chair, in the same pose, matches
