@@ -499,7 +499,10 @@ rtr_status rtr_orient_normals_outward(rtr_context* ctx, const float* d_pts, floa
  * Support: points within `radius` facing the keypoint's side
  * (n_j . n_k >= -0.2).  LRF: weighted-covariance eigenvectors (x largest, z
  * smallest), x signed by the majority rule, z by agreement with the support's
- * oriented normals.  d_desc: nk x 352; d_lrf (optional): nk x 9 (rows x,y,z). */
+ * oriented normals.  d_desc: nk x 352; d_lrf (optional): nk x 9 (rows x,y,z).
+ * Deterministic: the support's sums are fixed-point, so the result does not
+ * depend on the order of the points.  radius: 1e-6 to 1e6 (RTR_ERR_INVALID_ARG
+ * outside). */
 rtr_status rtr_shot352(rtr_context* ctx, const float* d_pts, const float* d_normals, int n,
                        const int32_t* d_keys, int nk, float radius, float* d_desc,
                        float* d_lrf, rtr_stream_t stream);
