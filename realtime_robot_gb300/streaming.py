@@ -17,6 +17,39 @@ from . import FusionMap, parse_recog_result, recog_default_params, recognize_mul
 FX, FY, CX, CY = 525.0, 525.0, 319.5, 239.5
 
 
+def _angle_deg(R: np.ndarray) -> float:
+    c = max(-1.0, min(1.0, (float(np.trace(R)) - 1.0) / 2.0))
+    return float(np.degrees(np.arccos(c)))
+
+
+def trajectory_errors(est, true) -> dict:
+    """Accuracy of an estimated camera trajectory against the true one (both
+    lists of 4x4 camera-to-world poses, frame 0 shared): the absolute
+    trajectory error (RMS of the position errors over every frame), the
+    final position and rotation drift, and the relative pose error of each
+    frame-to-frame motion (translation in mm, rotation in degrees; median and
+    95th percentile)."""
+    est = [np.asarray(e, np.float64) for e in est]
+    true = [np.asarray(t, np.float64) for t in true]
+    if not est:
+        return {}
+    pos = np.array([np.linalg.norm(e[:3, 3] - t[:3, 3]) for e, t in zip(est, true)])
+    out = {"ate_rms_m": float(np.sqrt(np.mean(pos ** 2))),
+           "drift_final_m": float(pos[-1]),
+           "rot_drift_final_deg": _angle_deg(est[-1][:3, :3].T @ true[-1][:3, :3])}
+    if len(est) > 1:
+        rt, rr = [], []
+        for f in range(1, len(est)):
+            re = np.linalg.inv(est[f - 1]) @ est[f]
+            rg = np.linalg.inv(true[f - 1]) @ true[f]
+            d = np.linalg.inv(rg) @ re
+            rt.append(1e3 * float(np.linalg.norm(d[:3, 3])))
+            rr.append(_angle_deg(d[:3, :3]))
+        out.update({"rpe_trans_mm_median": float(np.median(rt)), "rpe_trans_mm_p95": float(np.percentile(rt, 95)),
+                    "rpe_rot_deg_median": float(np.median(rr)), "rpe_rot_deg_p95": float(np.percentile(rr, 95))})
+    return out
+
+
 class StreamPipeline:
     """State of one stream: the models, the previous frame's odometry cloud,
     the current pose estimate and the fusion map."""
@@ -76,12 +109,13 @@ class StreamPipeline:
     def run(self, frames, pose0, true_poses=None):
         """All frames; returns timing and accuracy figures."""
         self.start(pose0)
-        lat, drift = [], []
+        lat, drift, est = [], [], []
         t_all = time.perf_counter()
         for f in range(frames.shape[0]):
             t0 = time.perf_counter()
             pose, _ = self.frame(frames[f])
             lat.append((time.perf_counter() - t0) * 1e3)
+            est.append(pose)
             if true_poses is not None:
                 drift.append(float(np.linalg.norm(pose[:3, 3] - true_poses[f][:3, 3])))
         total = time.perf_counter() - t_all
@@ -93,7 +127,8 @@ class StreamPipeline:
                 "odometry_drift_m_final": drift[-1] if drift else None,
                 "odometry_drift_m_max": max(drift) if drift else None,
                 "map_voxels": nvox, "map_load": nvox / self.map_capacity,
-                "last_frame_instances": [len(r["instances"]) for r in res]}
+                "last_frame_instances": [len(r["instances"]) for r in res],
+                "trajectory": trajectory_errors(est, true_poses[: len(est)]) if true_poses is not None else None}
 
     def close(self):
         self.map.close()

@@ -110,5 +110,8 @@ def test_stream_pipeline_tracks_the_camera(ctx, rtr, room):
     assert out["frames"] == 30 and out["fps"] > 0
     # frame-to-frame ICP over 1 s (0.5 m) of motion with depth noise 1.5 mm * z^2
     assert out["odometry_drift_m_max"] < 0.08, out
+    tr = out["trajectory"]
+    assert tr["ate_rms_m"] <= out["odometry_drift_m_max"] + 1e-12 and tr["drift_final_m"] == out["odometry_drift_m_final"]
+    assert 0.0 <= tr["rpe_trans_mm_median"] <= tr["rpe_trans_mm_p95"] < 20.0 and tr["rpe_rot_deg_p95"] < 2.0, tr
     assert out["map_voxels"] > 100000 and out["map_load"] < 0.5
     pipe.close()
