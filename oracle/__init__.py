@@ -48,6 +48,7 @@ _SIG = {
     "orc_eig3": (None, [_P, _P, _P]),
     "orc_uniform_sample": (_I, [_P, _I, _F, _P]),
     "orc_set_shot_flags": (None, [_I]),
+    "orc_shot_atan2": (_F, [_F, _F]),
     "orc_shot352": (None, [_P, _P, _I, _P, _I, _F, _P, _P]),
     "orc_match": (None, [_P, _I, _P, _I, _I, _P, _P]),
     "orc_gc_group": (_I, [_P, _P, _P, _P, _P, _I, _F, _I, _I, _P, _P, _P]),
@@ -295,6 +296,11 @@ def set_shot_flags(flags: int) -> None:
     keeps support points whose normals face away, bit 1 signs the LRF z axis
     by the majority rule over the support's offsets."""
     lib().orc_set_shot_flags(int(flags))
+
+
+def shot_atan2(y: float, x: float) -> float:
+    """The atan2 that SHOT's angle bins use (own restatement, see oracle.c)."""
+    return float(lib().orc_shot_atan2(float(y), float(x)))
 
 
 def shot352(pts, nrm, keys, radius: float):

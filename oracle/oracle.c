@@ -908,6 +908,8 @@ static float shot_atan2(float y, float x) {
   return y < 0.f ? -r : r;
 }
 
+float orc_shot_atan2(float y, float x) { return shot_atan2(y, x); }
+
 static float dot3f(float a0, float a1, float a2, float b0, float b1, float b2) {
   const float p0 = a0 * b0, p1 = a1 * b1, p2 = a2 * b2;
   return (p0 + p1) + p2;

@@ -102,6 +102,8 @@ int orc_uniform_sample(const float* pts, int n, float r, int32_t* out_idx);
 /* ---- SHOT-style 352-d descriptor (Tombari, Salti, Di Stefano 2010) with the
  * conventions in oracle.c.  keys: indices into pts. */
 void orc_set_shot_flags(int flags);
+/* the atan2 of the SHOT angle bins (the GPU kernel runs the same operations) */
+float orc_shot_atan2(float y, float x);
 void orc_shot352(const float* pts, const float* normals, int n, const int32_t* keys, int nk,
                  float radius, float* desc, float* lrf9);
 

@@ -199,3 +199,18 @@ def test_shot_descriptors_do_not_depend_on_point_order():
     assert np.array_equal(d, d2) and np.array_equal(lrf, lrf2)
     nrm = np.linalg.norm(d, axis=1)
     assert np.all(np.abs(nrm - 1.0) < 1e-5)
+
+
+def test_shot_atan2_accuracy_and_conventions():
+    """SHOT's own atan2 (the GPU kernel runs the same operations): within
+    3e-7 rad of the true angle over every octant, 0 at the origin, and -0
+    treated as +0."""
+    rng = np.random.default_rng(3)
+    ys = np.concatenate([rng.uniform(-1, 1, 4000), rng.uniform(-1e-6, 1e-6, 500), [0.0, 1.0, -1.0]])
+    xs = np.concatenate([rng.uniform(-1, 1, 4000), rng.uniform(-1, 1, 500), [1.0, 0.0, 0.0]])
+    worst = 0.0
+    for y, x in zip(ys.astype(np.float32), xs.astype(np.float32)):
+        worst = max(worst, abs(O.shot_atan2(float(y), float(x)) - np.arctan2(np.float64(y), np.float64(x))))
+    assert worst < 3e-7, worst
+    assert O.shot_atan2(0.0, 0.0) == 0.0
+    assert O.shot_atan2(-0.0, -1.0) == np.float32(np.pi)
