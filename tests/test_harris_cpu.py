@@ -52,3 +52,36 @@ def test_unrefined_keypoints_are_cloud_points_and_local_maxima():
     plane = np.zeros((5000, 4), np.float32)
     plane[:, :2] = rng.uniform(-0.5, 0.5, (5000, 2))
     assert len(O.harris3d(plane)[0]) == 0
+
+
+def test_responses_against_numpy():
+    """Every point's Harris response against a float64 numpy restatement of
+    the operator: radius neighbours (the point included), normals as the
+    smallest covariance eigenvectors, M = mean of n n^T over the neighbours,
+    R = det(M) - 0.04 tr(M)^2 + 0.04 (unit normals: R = det(M)).  Points whose
+    own or whose neighbours' smallest eigenvalues are not separated (their
+    normal is not defined to float precision) are left out."""
+    spatial = __import__("pytest").importorskip("scipy.spatial")
+    pts = _cube(3000, 0.3, 4)
+    keys, src = O.harris3d(pts, 0.05, -1.0, non_max=False, refine=False)
+    assert len(src) == len(pts)
+    P = pts[:, :3].astype(np.float64)
+    nb = spatial.cKDTree(P).query_ball_point(P, 0.05 * (1 + 1e-6))
+    nrm = np.zeros((len(P), 3))
+    ok = np.zeros(len(P), bool)
+    for i, js in enumerate(nb):
+        Q = P[js] - P[js].mean(0)
+        w, V = np.linalg.eigh(Q.T @ Q / len(js))
+        nrm[i] = V[:, 0]
+        ok[i] = w[1] - w[0] > 1e-3 * w[2]
+    resp = np.full(len(P), np.nan)
+    for i, js in enumerate(nb):
+        if not ok[js].all():
+            continue
+        M = nrm[js].T @ nrm[js] / len(js)
+        resp[i] = np.linalg.det(M) - 0.04 * np.trace(M) ** 2 + 0.04
+    got = np.full(len(P), np.nan)
+    got[src] = keys[:, 3]
+    sel = ~np.isnan(resp)
+    assert sel.mean() > 0.5
+    np.testing.assert_allclose(got[sel], resp[sel], atol=2e-5)
