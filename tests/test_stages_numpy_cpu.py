@@ -77,3 +77,29 @@ def test_uniform_sampling_against_numpy():
     want = order[first]
     assert np.array_equal(np.sort(got), np.sort(want))
     assert np.all(np.diff(key[got]) > 0)
+
+
+def test_outward_orientation_against_numpy():
+    """Full-model normals turn to the side with fewer cloud points inside a
+    cylinder of radius rc along the normal (axial distance in (gap, len]);
+    ties keep the sign.  FP32 elementwise in numpy, as the rule states."""
+    f32 = np.float32
+    pts = O.voxel_downsample(_cloud(5, 8000), 0.01)
+    nrm = O.normals(pts, 10, (0.0, 0.0, 0.0))
+    got = O.orient_outward(pts, nrm, 0.01, 0.005, 1.0)
+    P = pts[:, :3]
+    flips = 0
+    for i in range(len(P)):
+        d = P - P[i]
+        n = nrm[i, :3]
+        ax = f32(f32(d[:, 0] * n[0] + d[:, 1] * n[1]) + d[:, 2] * n[2])
+        aa = np.abs(ax)
+        r2 = f32(f32(f32(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]) - ax * ax)
+        inside = (aa > f32(0.005)) & (aa <= f32(1.0)) & (r2 <= f32(0.01) * f32(0.01))
+        cp, cm = int((inside & (ax > 0)).sum()), int((inside & (ax <= 0)).sum())
+        want = -nrm[i] if cp > cm else nrm[i]
+        want = want.copy()
+        want[3] = nrm[i, 3]
+        flips += cp > cm
+        assert np.array_equal(got[i], want), i
+    assert 0 < flips < len(P)
