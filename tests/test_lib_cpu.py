@@ -219,3 +219,19 @@ def test_host_only_generator_matches_the_library(rtr):
         assert np.array_equal(x, y)
     crop = rtr.synth_crop(rtr.synth_shape(rtr.SOFA, 3000, 4), 0.4, 4)
     assert np.array_equal(crop, S.synth_crop(S.synth_shape(S.SOFA, 3000, 4), 0.4, 4))
+
+
+def test_oracle_pipeline_defaults_equal_the_library_defaults(rtr):
+    """The oracle pipeline and rtr_recog_default_params describe the same
+    recognition (the GPU-vs-oracle pipeline tests rest on it)."""
+    from oracle import pipeline as OP
+    p = rtr.recog_default_params()
+    for k, v in OP.DEFAULTS.items():
+        got = getattr(p, k)
+        if k == "viewpoint":
+            assert list(got) == [float(np.float32(x)) for x in v], k
+        elif isinstance(v, float):
+            assert got == float(np.float32(v)), (k, got, v)
+        else:
+            assert got == v, (k, got, v)
+    assert p.model_keypoint_r == np.float32(0.02) and p.scene_keypoint_r == np.float32(0.02)
