@@ -1,0 +1,59 @@
+"""Every function the ctypes binding declares has the header's parameter
+count and, parameter by parameter, a ctypes type of the same kind (pointer,
+float, double, int, 64-bit int, size_t): a float passed where the library
+reads an int, or a missing argument, would go through ctypes silently."""
+import ctypes as C
+import re
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def _prototypes():
+    txt = (ROOT / "include" / "rtr.h").read_text()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    txt = re.sub(r"//[^\n]*", "", txt)
+    out = {}
+    for m in re.finditer(r"\b([A-Za-z_]\w*)\s*\(([^;{}()]*(?:\([^()]*\)[^;{}()]*)*)\)\s*;", txt):
+        params = [p.strip() for p in m.group(2).split(",")]
+        if params == ["void"] or params == [""]:
+            params = []
+        out[m.group(1)] = params
+    return out
+
+
+def _kind_c(p):
+    if "*" in p or "rtr_stream_t" in p:
+        return "ptr"
+    base = re.sub(r"\b(const|unsigned)\b", "", p).split()
+    t = " ".join(base[:-1]) if len(base) > 1 else base[0]
+    return {"float": "f32", "double": "f64", "int": "i32", "int32_t": "i32", "size_t": "size",
+            "long long": "i64", "int64_t": "i64", "uint64_t": "u64", "uint32_t": "u32"}.get(t, t)
+
+
+def _kind_py(t):
+    if t in (C.c_void_p, C.c_char_p) or (isinstance(t, type) and issubclass(t, C._Pointer)):
+        return "ptr"
+    for kind, cands in (("f32", (C.c_float,)), ("f64", (C.c_double,)), ("size", (C.c_size_t,)),
+                        ("i64", (C.c_longlong, C.c_int64)), ("u64", (C.c_uint64, C.c_ulonglong)),
+                        ("u32", (C.c_uint32, C.c_uint)), ("i32", (C.c_int, C.c_int32))):
+        if t in cands:
+            return kind
+    return repr(t)
+
+
+def test_binding_signatures_match_the_header(rtr):
+    protos = _prototypes()
+    checked = 0
+    for name, (_, args) in rtr._SIG.items():
+        if name not in protos:
+            continue
+        params = protos[name]
+        assert len(params) == len(args), (name, params, args)
+        for p, a in zip(params, args):
+            kc, kp = _kind_c(p), _kind_py(a)
+            if {kc, kp} <= {"size", "u64"}:  # one unsigned 64-bit type on LP64 (ctypes aliases them)
+                continue
+            assert kc == kp, (name, p, a)
+        checked += 1
+    assert checked == len(rtr._SIG), (checked, len(rtr._SIG))  # every bound function is declared
