@@ -1,7 +1,8 @@
-"""Every function the ctypes binding declares has the header's parameter
-count and, parameter by parameter, a ctypes type of the same kind (pointer,
-float, double, int, 64-bit int, size_t): a float passed where the library
-reads an int, or a missing argument, would go through ctypes silently."""
+"""Every function the ctypes binding declares has the header's return kind,
+parameter count and, parameter by parameter, a ctypes type of the same kind
+(pointer, float, double, int, 64-bit int, size_t): a float passed where the
+library reads an int, or a missing argument, would go through ctypes
+silently."""
 import ctypes as C
 import re
 from pathlib import Path
@@ -14,12 +15,22 @@ def _prototypes():
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
     txt = re.sub(r"//[^\n]*", "", txt)
     out = {}
-    for m in re.finditer(r"\b([A-Za-z_]\w*)\s*\(([^;{}()]*(?:\([^()]*\)[^;{}()]*)*)\)\s*;", txt):
-        params = [p.strip() for p in m.group(2).split(",")]
+    for m in re.finditer(r"([A-Za-z_][\w \t]*?[\s\*]+)\b([A-Za-z_]\w*)\s*\(([^;{}()]*(?:\([^()]*\)[^;{}()]*)*)\)\s*;",
+                         txt):
+        params = [p.strip() for p in m.group(3).split(",")]
         if params == ["void"] or params == [""]:
             params = []
-        out[m.group(1)] = params
+        out[m.group(2)] = (m.group(1).split("\n")[-1].strip(), params)
     return out
+
+
+def _kind_ret(r):
+    r = r.replace("extern", "").strip()
+    if r == "void":
+        return None
+    if r in ("rtr_status", "cudaError_t", "int"):
+        return "i32"
+    return _kind_c(r + " x")
 
 
 def _kind_c(p):
@@ -45,10 +56,12 @@ def _kind_py(t):
 def test_binding_signatures_match_the_header(rtr):
     protos = _prototypes()
     checked = 0
-    for name, (_, args) in rtr._SIG.items():
+    for name, (res, args) in rtr._SIG.items():
         if name not in protos:
             continue
-        params = protos[name]
+        ret, params = protos[name]
+        kr, kres = _kind_ret(ret), (None if res is None else _kind_py(res))
+        assert kr == kres or {kr, kres} <= {"size", "u64"}, (name, ret, res)
         assert len(params) == len(args), (name, params, args)
         for p, a in zip(params, args):
             kc, kp = _kind_c(p), _kind_py(a)
