@@ -10,8 +10,8 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent.parent
 
 
-def _prototypes():
-    txt = (ROOT / "include" / "rtr.h").read_text()
+def _prototypes(header=ROOT / "include" / "rtr.h"):
+    txt = Path(header).read_text()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
     txt = re.sub(r"//[^\n]*", "", txt)
     out = {}
@@ -53,10 +53,9 @@ def _kind_py(t):
     return repr(t)
 
 
-def test_binding_signatures_match_the_header(rtr):
-    protos = _prototypes()
+def _check(table, protos):
     checked = 0
-    for name, (res, args) in rtr._SIG.items():
+    for name, (res, args) in table.items():
         if name not in protos:
             continue
         ret, params = protos[name]
@@ -69,4 +68,13 @@ def test_binding_signatures_match_the_header(rtr):
                 continue
             assert kc == kp, (name, p, a)
         checked += 1
-    assert checked == len(rtr._SIG), (checked, len(rtr._SIG))  # every bound function is declared
+    return checked
+
+
+def test_binding_signatures_match_the_header(rtr):
+    assert _check(rtr._SIG, _prototypes()) == len(rtr._SIG)  # every bound function is declared
+
+
+def test_oracle_binding_signatures_match_its_header():
+    import oracle as O
+    assert _check(O._SIG, _prototypes(ROOT / "oracle" / "oracle.h")) == len(O._SIG)
