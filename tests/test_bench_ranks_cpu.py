@@ -59,3 +59,33 @@ def test_reference_arm_other_ranks_exit_without_work(monkeypatch, capsys):
 
     assert bench.run_reference(A()) == 0
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_line_keeps_the_contract_and_loads_no_gpu_library():
+    """Rank 0 of the reference arm prints one JSON line with the contract's
+    keys, times whole oracle recognitions of the room, and maps only the
+    oracle's libraries (none of the GPU path's)."""
+    import json
+    import subprocess
+    code = (
+        "import sys, json; sys.path.insert(0, %r); import bench\n"
+        "class A: steps, warmup, gpus = 1, 0, 1\n"
+        "bench.run_reference(A())\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "print(json.dumps({'so': sorted({l.split()[-1] for l in maps.splitlines() if l.endswith('.so')})}))\n"
+    ) % str(ROOT)
+    env = dict(os.environ, RANK="0", WORLD_SIZE="1")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, env=env,
+                       cwd=str(ROOT))
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
+    line, so = lines[0], lines[1]["so"]
+    for k in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+              "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert k in line, k
+    assert line["impl"] == "reference" and line["value"] > 0 and line["unit"] == "recognitions/s"
+    assert line["cpu_baseline"]["kind"] == "port" and "full" in line["cpu_baseline"]["sample"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
+    assert line["counts"]["n_voxels"] > 200000 and line["counts"]["n_keypoints"] > 100000
+    mine = [s for s in so if str(ROOT) in s]
+    assert mine and all("/oracle/" in s for s in mine), mine
